@@ -1,0 +1,174 @@
+/*
+ * ec2d_gpu.h -- C-ABI of libec2d_gpu.so, the GB300-native (sm_103a)
+ * pseudo-time-marching core of OpenCFD-EC2D.
+ *
+ * The reference is one Fortran program whose main loop
+ * (opencfd_ec2d_v1.5.4.f90:172-186) calls NS_Time_advance(1),
+ * NS_2stge_multigrid or NS_3stge_multigrid.  This library replaces the bodies
+ * of those calls: the Fortran host (or any C/C++/Python host) keeps reading
+ * control.in, bc2d_1.in and Mesh2d.dat and writing Residual.dat/flow2d.dat,
+ * hands the grid and parameters over once, and then calls ec2d_step() per
+ * iteration.  The solution, metrics, residuals, turbulence variables and the
+ * multigrid levels stay on the GPU for the whole run; only the 12 residual
+ * norms (and snapshots on request) come back.
+ *
+ * Conventions
+ *  - Every function returns 0 on success or an EC2D_ERR_* code.
+ *  - Arrays crossing the boundary use the reference's Fortran layout
+ *    (column-major, variable index fastest), e.g. U(NVAR,-1:nx+1,-1:ny+1).
+ *  - Block, mesh and case numbers are 1-based like the Fortran; case ids
+ *    returned by ec2d_add_case start at 1.
+ *  - One context = one CUDA stream on one device.  A context is not
+ *    re-entrant; separate contexts are independent.  Calls are asynchronous
+ *    on the context's stream except where they return host data.
+ *  - A context may hold several cases (a batch, e.g. a polar sweep).  All
+ *    cases of a context share the method flags (scheme, flux,
+ *    reconstruction, viscous/turbulence model, time method, multigrid depth)
+ *    and advance together in one launch per stage.
+ */
+#ifndef EC2D_GPU_H
+#define EC2D_GPU_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EC2D_OK 0
+#define EC2D_ERR_ARG 1        /* invalid argument / call order              */
+#define EC2D_ERR_CUDA 2       /* CUDA runtime error                         */
+#define EC2D_ERR_STATE 3      /* non-physical state (T < 1e-5), see ec2d_status */
+#define EC2D_ERR_TIMEOUT 4    /* a device-side wait hit its iteration limit */
+#define EC2D_ERR_UNSUPPORTED 5 /* option combination the reference refuses  */
+#define EC2D_ERR_NOMEM 6
+
+/* The scalars of control.in (Global_Var, opencfd_ec2d_v1.5.4.f90:103-110),
+ * read from lines 2,4,6,8,10 (opencfd_ec2d_v1.5.4.f90:201-211); AoA in
+ * degrees and Twall in kelvin as written in control.in.  xaxis/yaxis come
+ * from control.in line 12 (moment reference point).  mg_lusgs=1 lifts the
+ * reference's refusal of LU-SGS with multigrid (opencfd_ec2d_v1.5.4.f90:216-221)
+ * and smooths every multigrid level with LU-SGS. */
+typedef struct ec2d_params {
+  double Ma, Re, gamma, AoA, Pr, t_end;
+  int Kstep_save, If_viscous, Iflag_turbulence_model, Iflag_init;
+  int Iflag_local_dt;
+  double dt_global, CFL, dtmax, dtmin;
+  int Time_Method;
+  double P_outlet, T_inf, Twall, vt_inf, Kt_inf, Wt_inf;
+  int Iflag_Scheme, Iflag_flux, IFlag_Reconstruction, Kstep_show;
+  int Num_Mesh, Num_Threads, Nstep_Inner_Limit;
+  double Res_Inner_Limit;
+  int Pre_Step_Mesh[3];
+  double xaxis, yaxis;
+  int mg_lusgs;
+} ec2d_params;
+
+typedef struct ec2d_ctx ec2d_ctx;
+
+/* Field ids for ec2d_get_field / ec2d_set_field (Fortran extents):
+ *  RES (NVAR,1:nx-1,1:ny-1)  DT (1:nx-1,1:ny-1)  LCI..LVJ (1:nx,1:ny)
+ *  DU (NVAR,1:nx,1:ny)  AMU, AMUT, X1, Y1 (-1:nx+1,-1:ny+1)
+ *  VOL,SI,SJ,NI1,NI2,NJ1,NJ2 (1:nx,1:ny)  DW (0:nx,0:ny)
+ *  QF (4,1:nx-1,1:ny-1)  DELTU (4,-1:nx+1,-1:ny+1)  UN (NVAR,0:nx,0:ny)
+ *  X, Y (-1:nx+2,-1:ny+2) */
+enum {
+  EC2D_F_RES = 0, EC2D_F_DT = 1, EC2D_F_LCI = 2, EC2D_F_LCJ = 3, EC2D_F_LVI = 4,
+  EC2D_F_LVJ = 5, EC2D_F_DU = 6, EC2D_F_AMU = 7, EC2D_F_AMUT = 8, EC2D_F_X1 = 9,
+  EC2D_F_Y1 = 10, EC2D_F_VOL = 11, EC2D_F_SI = 12, EC2D_F_SJ = 13, EC2D_F_NI1 = 14,
+  EC2D_F_NI2 = 15, EC2D_F_NJ1 = 16, EC2D_F_NJ2 = 17, EC2D_F_DW = 18, EC2D_F_QF = 19,
+  EC2D_F_DELTU = 20, EC2D_F_UN = 21, EC2D_F_X = 22, EC2D_F_Y = 23
+};
+
+/* Library version (major*10000+minor*100+patch) and error text. */
+int ec2d_version(void);
+const char *ec2d_error_string(int code);
+
+/* Create an empty context on CUDA device `device` (its own stream). */
+int ec2d_create(int device, ec2d_ctx **out);
+void ec2d_destroy(ec2d_ctx *ctx);
+
+/* Add one case with its control.in parameters (replaces read_parameter,
+ * opencfd_ec2d_v1.5.4.f90:197-235).  *case_id receives the 1-based id. */
+int ec2d_add_case(ec2d_ctx *ctx, const ec2d_params *p, int *case_id);
+
+/* Add block `nblocks+1` of a case: node coordinates x(1:nx,1:ny), y(1:nx,1:ny)
+ * (column-major, as read from Mesh2d.dat at sub_init.f90:176) and its nsub
+ * subfaces, 9 ints each: f_no, face, ist, iend, jst, jend, neighb, subface,
+ * orient (bc2d_1.in, sub_init.f90:246).  Replaces Creat_Mesh1 + read_bcin. */
+int ec2d_add_block(ec2d_ctx *ctx, int case_id, int nx, int ny, const double *x,
+                   const double *y, int nsub, const int *bc9);
+
+/* Mark a block as a finite-difference (WENO5/Steger-Warming) block, as a
+ * line of FDM.in does (sub_Finite_Difference.f90:287-308). */
+int ec2d_set_fdm_block(ec2d_ctx *ctx, int case_id, int block);
+
+/* Supply the cell wall distance dw(1:nx-1,1:ny-1) of a block, as
+ * dist_wall.dat does (sub_turbulence_SST.f90:295-306).  Without it the
+ * distance is computed on the GPU (comput_dw, sub_turbulence_SST.f90:310-340). */
+int ec2d_set_wall_distance(ec2d_ctx *ctx, int case_id, int block, const double *dw);
+
+/* Build everything on the device: multigrid depth (check_mesh_multigrid,
+ * sub_init.f90:39-107), coarse meshes (Creat_Mesh, sub_init.f90:256-380),
+ * ghost coordinates (Update_coordinate_buffer, sub_boundary.f90:159-301),
+ * metrics, FDM Jacobians and wall distance. */
+int ec2d_setup(ec2d_ctx *ctx);
+
+/* Number of multigrid levels in use and the variable count of a level. */
+int ec2d_num_mesh(ec2d_ctx *ctx, int *num_mesh);
+int ec2d_block_dims(ec2d_ctx *ctx, int case_id, int mesh, int block, int *nx, int *ny, int *nvar);
+
+/* Freestream start including the coarse-to-fine pre-iterations
+ * (init_flow_zero, sub_init.f90:423-495) for every case. */
+int ec2d_init_flow(ec2d_ctx *ctx);
+
+/* Copy the conservative field of one block in or out, Fortran layout
+ * U(NVAR,-1:nx+1,-1:ny+1) (the reference's B%U).  Host pointers may be
+ * pageable or pinned. */
+int ec2d_upload_U(ec2d_ctx *ctx, int case_id, int mesh, int block, const double *U);
+int ec2d_download_U(ec2d_ctx *ctx, int case_id, int mesh, int block, double *U);
+
+/* Advance `nsteps` iterations of the main loop (opencfd_ec2d_v1.5.4.f90:174-180):
+ * NS_Time_advance(1) when Num_Mesh==1, else one 2- or 3-level V-cycle. */
+int ec2d_step(ec2d_ctx *ctx, int nsteps);
+
+/* Residual norms of the last residual evaluation on `mesh` (MP%Res_max(1:6),
+ * MP%Res_rms(1:6), written to Residual.dat at opencfd_ec2d_v1.5.4.f90:276),
+ * the step counter and pseudo time.  Synchronises the stream; returns
+ * EC2D_ERR_STATE if the case hit the T<1e-5 stop (sub_Residual.f90:143-146). */
+int ec2d_residual(ec2d_ctx *ctx, int case_id, int mesh, double res_max[6], double res_rms[6],
+                  int *kstep, double *tt);
+
+/* Status word of a case: code (0 ok, 3 = T<1e-5) and the block/cell. */
+int ec2d_status(ec2d_ctx *ctx, int case_id, int *code, int *block, int *i, int *j);
+
+/* Lift, drag and moment coefficients (about xaxis, yaxis) from the wall
+ * pressure and viscous stress of mesh 1; no counterpart in the reference,
+ * whose read_flow-1.2.f90:36-51 writes wall Cp only. */
+int ec2d_forces(ec2d_ctx *ctx, int case_id, double *cl, double *cd, double *cm);
+
+/* Skin friction per wall face of subface `sub` of `block` (mesh 1) and the
+ * face-centre x; returns the face count in *n (at most maxn written). */
+int ec2d_wall_cf(ec2d_ctx *ctx, int case_id, int block, int sub, double *cf, double *xc,
+                 int maxn, int *n);
+
+/* Read or overwrite one field of one block (ids above, Fortran layout). */
+int ec2d_get_field(ec2d_ctx *ctx, int case_id, int mesh, int block, int field, double *out);
+int ec2d_field_size(ec2d_ctx *ctx, int case_id, int mesh, int block, int field, int *n);
+int ec2d_set_field(ec2d_ctx *ctx, int case_id, int mesh, int block, int field, const double *in);
+
+/* Finer-grained hooks with the reference's routine names (all blocks of all
+ * cases on one mesh level): */
+int ec2d_comput_residual(ec2d_ctx *ctx, int mesh);        /* Comput_Residual_one_mesh, sub_Residual.f90:13 */
+int ec2d_boundary_condition(ec2d_ctx *ctx, int mesh);     /* Boundary_condition_onemesh, sub_boundary.f90:10 */
+int ec2d_update_buffer(ec2d_ctx *ctx, int mesh);          /* update_buffer_onemesh, sub_boundary.f90:45 */
+int ec2d_du_lusgs(ec2d_ctx *ctx, int mesh, double alfa1); /* du_LU_SGS_2D, sub_LU_SGS.f90:4 */
+int ec2d_time_advance(ec2d_ctx *ctx, int mesh);           /* NS_Time_advance, sub_NS_singlegrid.f90:8 */
+int ec2d_interpolation2h(ec2d_ctx *ctx, int m1, int m2, int flag); /* sub_NS_multigrid.f90:349 */
+int ec2d_prolong(ec2d_ctx *ctx, int m1, int m2, int flag);         /* prolong_U, sub_NS_multigrid.f90:271 */
+int ec2d_force_function(ec2d_ctx *ctx, int mesh);         /* comput_force_function, sub_NS_multigrid.f90:156 */
+
+/* Wait for all queued work of the context. */
+int ec2d_sync(ec2d_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1154 @@
+// ec2d_api.cu -- the C-ABI (include/ec2d_gpu.h): context, one-time setup on
+// the host (geometry, ghost coordinates, coarse meshes, FDM metrics, device
+// layout) and the orchestration of the pseudo-time-marching sequences of
+// sub_NS_singlegrid.f90 and sub_NS_multigrid.f90 as kernel launches on the
+// context's stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/ec2d_gpu.h"
+#include "ec2d_dev.cuh"
+#include "ec2d_internal.h"
+
+using namespace ec2d;
+
+namespace {
+
+const double PI = 3.1415926535897932;
+constexpr int TILE = 256;
+
+struct HBlock {
+  int nx = 0, ny = 0;
+  std::vector<double> x, y;  // (1:nx,1:ny), i fastest
+  std::vector<int> bc;       // 9 per subface
+  int nsub = 0;
+  bool fdm = false;
+  std::vector<double> dw;    // supplied wall distance (1:nx-1,1:ny-1) or empty
+};
+
+struct HCase {
+  ec2d_params p{};
+  std::vector<HBlock> blocks;
+  int nvar = 4;
+  int kstep[4] = {0, 0, 0, 0};
+  double tt[4] = {0, 0, 0, 0};
+};
+
+// host-side frame-indexed 2-D array of one block
+struct Frame {
+  int nx = 0, ny = 0, P = 0;
+  std::vector<double> v;
+  void init(int nx_, int ny_, double val = 0.0) {
+    nx = nx_; ny = ny_; P = nx + 5;
+    v.assign((size_t)P * (ny + 5), val);
+  }
+  double &operator()(int i, int j) { return v[(size_t)(j + 2) * P + (i + 2)]; }
+};
+
+struct HLevelBlock {
+  int nx, ny, cas, blk;  // blk: 0-based block number within its case
+  std::vector<int> bc;   // 9 per subface (level indices)
+  int nsub;
+  bool fdm;
+  Frame x, y, x1, y1, vol, si, sj, ni1, ni2, nj1, nj2;
+  Frame akx, aky, aix, aiy, ajac;
+};
+
+struct DevBuf {
+  void *p = nullptr;
+  ~DevBuf() { if (p) cudaFree(p); }
+};
+
+struct Level {
+  std::vector<HLevelBlock> hb;
+  std::vector<BlkDev> blk;
+  std::vector<SubDev> sub;
+  std::vector<int2> tiles;
+  std::vector<int> case_tile0, case_ntile, case_ncell;
+  std::vector<int4> wall_faces;          // (block, face, k, 0) for forces
+  std::vector<int> case_face0, case_nface;
+  long long F = 0;
+  Lvl L{};
+  int *d_case_tile0 = nullptr, *d_case_ntile = nullptr, *d_case_ncell = nullptr;
+  int4 *d_faces = nullptr;
+  double *d_face_out = nullptr;
+  std::vector<std::unique_ptr<DevBuf>> bufs;
+};
+
+}  // namespace
+
+struct ec2d_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<HCase> cases;
+  bool setup_done = false;
+  int num_mesh = 1;
+  int nvar = 4;
+  ec2d_params P{};  // method flags (shared by all cases)
+  Level lv[4];
+  CaseDev *d_cases = nullptr;
+  double *d_stage = nullptr;  // staging for U upload/download
+  size_t stage_n = 0;
+  int dual_iflag1 = 0, dual_iflag = 0;
+  int last_err = 0;
+};
+
+namespace {
+
+#define CK(x)                                            \
+  do {                                                   \
+    cudaError_t e_ = (x);                                \
+    if (e_ != cudaSuccess) {                             \
+      fprintf(stderr, "ec2d: CUDA error %s at %s:%d\n", cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return EC2D_ERR_CUDA;                              \
+    }                                                    \
+  } while (0)
+
+template <class T>
+T *dalloc(Level &lv, size_t n) {
+  auto b = std::make_unique<DevBuf>();
+  if (n == 0) n = 1;
+  if (cudaMalloc(&b->p, n * sizeof(T)) != cudaSuccess) return nullptr;
+  cudaMemset(b->p, 0, n * sizeof(T));
+  T *r = (T *)b->p;
+  lv.bufs.push_back(std::move(b));
+  return r;
+}
+
+bool same_method(const ec2d_params &a, const ec2d_params &b) {
+  return a.If_viscous == b.If_viscous && a.Iflag_turbulence_model == b.Iflag_turbulence_model &&
+         a.Time_Method == b.Time_Method && a.Iflag_Scheme == b.Iflag_Scheme && a.Iflag_flux == b.Iflag_flux &&
+         a.IFlag_Reconstruction == b.IFlag_Reconstruction && a.Num_Mesh == b.Num_Mesh && a.mg_lusgs == b.mg_lusgs;
+}
+
+// check_mesh_multigrid (sub_init.f90:39-107)
+int mg_depth(const HCase &c) {
+  int Km_grid = c.blocks[0].nx;
+  for (auto &B : c.blocks) {
+    int Km = 1, NN = 2;
+    while ((B.nx - 1) % NN == 0 && (B.nx - 1) / NN >= 2 && (B.ny - 1) % NN == 0 && (B.ny - 1) / NN >= 2) { Km++; NN *= 2; }
+    Km_grid = std::min(Km_grid, Km);
+  }
+  for (auto &B : c.blocks)
+    for (int k = 0; k < B.nsub; k++) {
+      const int *s = &B.bc[9 * k];
+      int NN = 1, Km = 1;
+      while ((s[2] - 1) % NN == 0 && (s[3] - 1) % NN == 0 && (s[4] - 1) % NN == 0 && (s[5] - 1) % NN == 0) {
+        NN *= 2; Km++;
+        if (NN > (1 << 20)) break;
+      }
+      Km_grid = std::min(Km_grid, Km);
+    }
+  return std::min(3, std::min(Km_grid, c.p.Num_Mesh));
+}
+
+void geometry(HLevelBlock &B) {
+  int nx = B.nx, ny = B.ny;
+  // cell areas and face lengths/normals (sub_init.f90:180-204)
+  for (int j = 1; j <= ny - 1; j++)
+    for (int i = 1; i <= nx - 1; i++)
+      B.vol(i, j) = std::fabs((B.x(i, j) - B.x(i + 1, j + 1)) * (B.y(i + 1, j) - B.y(i, j + 1)) -
+                              (B.x(i + 1, j) - B.x(i, j + 1)) * (B.y(i, j) - B.y(i + 1, j + 1))) * 0.5;
+  for (int j = 1; j <= ny - 1; j++)
+    for (int i = 1; i <= nx; i++) {
+      double dx = B.x(i, j + 1) - B.x(i, j), dy = B.y(i, j + 1) - B.y(i, j);
+      double s = std::sqrt(dx * dx + dy * dy);
+      B.si(i, j) = s; B.ni1(i, j) = dy / s; B.ni2(i, j) = -dx / s;
+    }
+  for (int j = 1; j <= ny; j++)
+    for (int i = 1; i <= nx - 1; i++) {
+      double dx = B.x(i + 1, j) - B.x(i, j), dy = B.y(i + 1, j) - B.y(i, j);
+      double s = std::sqrt(dx * dx + dy * dy);
+      B.sj(i, j) = s; B.nj1(i, j) = -dy / s; B.nj2(i, j) = dx / s;
+    }
+}
+
+// ghost node coordinates and cell centres of one level of one case
+// (Update_coordinate_buffer_onemesh, sub_boundary.f90:174-282)
+void ghost_coordinates(std::vector<HLevelBlock *> &blocks) {
+  for (HLevelBlock *Bp : blocks) {
+    HLevelBlock &B = *Bp;
+    for (int ks = 0; ks < B.nsub; ks++) {
+      const int *c = &B.bc[9 * ks];
+      int face = c[1], ib2 = c[2], ie2 = c[3], jb2 = c[4], je2 = c[5], neighb = c[6], msub = c[7], orient = c[8];
+      if (neighb > 0) {
+        int n1 = ie2 - ib2 + je2 - jb2 + 1;
+        HLevelBlock &B1 = *blocks[neighb - 1];
+        const int *c1 = &B1.bc[9 * (msub - 1)];
+        int f1 = c1[1], ib1 = c1[2], ie1 = c1[3], jb1 = c1[4], je1 = c1[5];
+        std::vector<double> ux(2 * n1 * LAP);
+        auto UX = [&](int cc, int k, int l) -> double & { return ux[(cc - 1) + 2 * ((k - 1) + n1 * (l - 1))]; };
+        for (int l = 1; l <= LAP; l++) {
+          if (f1 == 1) for (int k = 1; k <= je1 - jb1 + 1; k++) { UX(1, k, l) = B1.x(ib1 + l, jb1 + k - 1); UX(2, k, l) = B1.y(ib1 + l, jb1 + k - 1); }
+          else if (f1 == 2) for (int k = 1; k <= ie1 - ib1 + 1; k++) { UX(1, k, l) = B1.x(ib1 + k - 1, jb1 + l); UX(2, k, l) = B1.y(ib1 + k - 1, jb1 + l); }
+          else if (f1 == 3) for (int k = 1; k <= je1 - jb1 + 1; k++) { UX(1, k, l) = B1.x(ie1 - LAP - 1 + l, jb1 + k - 1); UX(2, k, l) = B1.y(ie1 - LAP - 1 + l, jb1 + k - 1); }
+          else for (int k = 1; k <= ie1 - ib1 + 1; k++) { UX(1, k, l) = B1.x(ib1 + k - 1, je1 - LAP - 1 + l); UX(2, k, l) = B1.y(ib1 + k - 1, je1 - LAP - 1 + l); }
+        }
+        for (int k = 1; k <= n1; k++) {
+          int k1 = (orient == 2) ? k : n1 + 1 - k;
+          for (int l = 1; l <= LAP; l++) {
+            int di, dj;
+            if (face == 1) { di = ib2 - LAP - 1 + l; dj = jb2 + k - 1; }
+            else if (face == 2) { di = ib2 + k - 1; dj = jb2 - LAP - 1 + l; }
+            else if (face == 3) { di = ie2 + l; dj = jb2 + k - 1; }
+            else { di = ib2 + k - 1; dj = je2 + l; }
+            B.x(di, dj) = UX(1, k1, l);
+            B.y(di, dj) = UX(2, k1, l);
+          }
+        }
+      } else {
+        for (int l = 1; l <= LAP; l++) {
+          if (face == 1) for (int j = jb2; j <= je2; j++) { B.x(ib2 - l, j) = 2.0 * B.x(ib2, j) - B.x(ib2 + l, j); B.y(ib2 - l, j) = 2.0 * B.y(ib2, j) - B.y(ib2 + l, j); }
+          else if (face == 2) for (int i = ib2; i <= ie2; i++) { B.x(i, jb2 - l) = 2.0 * B.x(i, jb2) - B.x(i, jb2 + l); B.y(i, jb2 - l) = 2.0 * B.y(i, jb2) - B.y(i, jb2 + l); }
+          else if (face == 3) for (int j = jb2; j <= je2; j++) { B.x(ie2 + l, j) = 2.0 * B.x(ie2, j) - B.x(ie2 - l, j); B.y(ie2 + l, j) = 2.0 * B.y(ie2, j) - B.y(ie2 - l, j); }
+          else for (int i = ib2; i <= ie2; i++) { B.x(i, je2 + l) = 2.0 * B.x(i, je2) - B.x(i, je2 - l); B.y(i, je2 + l) = 2.0 * B.y(i, je2) - B.y(i, je2 - l); }
+        }
+      }
+    }
+    int nx = B.nx, ny = B.ny;
+    for (int j = 1; j <= LAP; j++)
+      for (int i = 1; i <= LAP; i++) {
+        int i1 = 1 - i, j1 = 1 - j, i2 = nx + i, j2 = ny + j;
+        B.x(i1, j1) = B.x(i1, 1) + B.x(1, j1) - B.x(1, 1); B.y(i1, j1) = B.y(i1, 1) + B.y(1, j1) - B.y(1, 1);
+        B.x(i2, j2) = B.x(i2, ny) + B.x(nx, j2) - B.x(nx, ny); B.y(i2, j2) = B.y(i2, ny) + B.y(nx, j2) - B.y(nx, ny);
+        B.x(i1, j2) = B.x(i1, ny) + B.x(1, j2) - B.x(1, ny); B.y(i1, j2) = B.y(i1, ny) + B.y(1, j2) - B.y(1, ny);
+        B.x(i2, j1) = B.x(i2, 1) + B.x(nx, j1) - B.x(nx, 1); B.y(i2, j1) = B.y(i2, 1) + B.y(nx, j1) - B.y(nx, 1);
+      }
+    for (int j = 1 - LAP; j <= ny + LAP - 1; j++)
+      for (int i = 1 - LAP; i <= nx + LAP - 1; i++) {
+        B.x1(i, j) = (B.x(i, j) + B.x(i + 1, j) + B.x(i, j + 1) + B.x(i + 1, j + 1)) * 0.25;
+        B.y1(i, j) = (B.y(i, j) + B.y(i + 1, j) + B.y(i, j + 1) + B.y(i + 1, j + 1)) * 0.25;
+      }
+  }
+}
+
+// 6th/4th-order metric derivatives (dx0/dy0, sub_Finite_Difference.f90:387-439)
+void fdm_metrics(HLevelBlock &B) {
+  int nx = B.nx - 1, ny = B.ny - 1;
+  auto d_i = [&](Frame &f, int i, int j) -> double {
+    const double b1 = 8.0 / 12.0, b2 = 1.0 / 12.0, a1 = 1.0 / 60.0, a2 = -3.0 / 20.0, a3 = 3.0 / 4.0;
+    if (i >= 4 && i <= nx - 3) return a1 * (f(i + 3, j) - f(i - 3, j)) + a2 * (f(i + 2, j) - f(i - 2, j)) + a3 * (f(i + 1, j) - f(i - 1, j));
+    if (i == 1) return (-3.0 * f(1, j) + 4.0 * f(2, j) - f(3, j)) / 2.0;
+    if (i == 2) return (-2.0 * f(1, j) - 3.0 * f(2, j) + 6.0 * f(3, j) - f(4, j)) / 6.0;
+    if (i == 3) return b1 * (f(4, j) - f(2, j)) - b2 * (f(5, j) - f(1, j));
+    if (i == nx - 2) return b1 * (f(nx - 1, j) - f(nx - 3, j)) - b2 * (f(nx, j) - f(nx - 4, j));
+    if (i == nx - 1) return (f(nx - 3, j) - 6.0 * f(nx - 2, j) + 3.0 * f(nx - 1, j) + 2.0 * f(nx, j)) / 6.0;
+    return (f(nx - 2, j) - 4.0 * f(nx - 1, j) + 3.0 * f(nx, j)) / 2.0;
+  };
+  auto d_j = [&](Frame &f, int i, int j) -> double {
+    const double b1 = 8.0 / 12.0, b2 = 1.0 / 12.0, a1 = 1.0 / 60.0, a2 = -3.0 / 20.0, a3 = 3.0 / 4.0;
+    if (j >= 4 && j <= ny - 3) return a1 * (f(i, j + 3) - f(i, j - 3)) + a2 * (f(i, j + 2) - f(i, j - 2)) + a3 * (f(i, j + 1) - f(i, j - 1));
+    if (j == 1) return (-3.0 * f(i, 1) + 4.0 * f(i, 2) - f(i, 3)) / 2.0;
+    if (j == 2) return (-2.0 * f(i, 1) - 3.0 * f(i, 2) + 6.0 * f(i, 3) - f(i, 4)) / 6.0;
+    if (j == 3) return b1 * (f(i, 4) - f(i, 2)) - b2 * (f(i, 5) - f(i, 1));
+    if (j == ny - 2) return b1 * (f(i, ny - 1) - f(i, ny - 3)) - b2 * (f(i, ny) - f(i, ny - 4));
+    if (j == ny - 1) return (f(i, ny - 3) - 6.0 * f(i, ny - 2) + 3.0 * f(i, ny - 1) + 2.0 * f(i, ny)) / 6.0;
+    return (f(i, ny - 2) - 4.0 * f(i, ny - 1) + 3.0 * f(i, ny)) / 2.0;
+  };
+  B.akx.init(B.nx, B.ny); B.aky.init(B.nx, B.ny); B.aix.init(B.nx, B.ny); B.aiy.init(B.nx, B.ny);
+  B.ajac.init(B.nx, B.ny, 1.0);
+  for (int j = 1; j <= ny; j++)
+    for (int i = 1; i <= nx; i++) {
+      double xk = d_i(B.x1, i, j), yk = d_i(B.y1, i, j), xi = d_j(B.x1, i, j), yi = d_j(B.y1, i, j);
+      double J = 1.0 / (xk * yi - xi * yk);
+      B.ajac(i, j) = J;
+      B.akx(i, j) = J * yi; B.aky(i, j) = -J * xi; B.aix(i, j) = -J * yk; B.aiy(i, j) = J * xk;
+    }
+}
+
+CaseDev make_casedev(const ec2d_params &p) {
+  CaseDev c{};
+  c.gamma = p.gamma; c.Ma = p.Ma; c.Re = p.Re; c.Pr = p.Pr;
+  c.Cv = 1.0 / (p.gamma * (p.gamma - 1.0) * p.Ma * p.Ma);
+  c.Cp = c.Cv * p.gamma;
+  double aoa = p.AoA * PI / 180.0;
+  c.cosA = 1.0 * std::cos(aoa); c.sinA = 1.0 * std::sin(aoa);
+  c.p00 = 1.0 / (p.gamma * p.Ma * p.Ma);
+  c.Tsb = 110.4 / p.T_inf;
+  c.Twall = p.Twall / p.T_inf;
+  c.p_outlet = p.P_outlet; c.vt_inf = p.vt_inf; c.Kt_inf = p.Kt_inf; c.Wt_inf = p.Wt_inf;
+  c.CFL = p.CFL; c.dtmax = p.dtmax; c.dtmin = p.dtmin; c.dt_global = p.dt_global; c.T_inf = p.T_inf;
+  c.xaxis = p.xaxis; c.yaxis = p.yaxis;
+  c.local_dt = p.Iflag_local_dt;
+  return c;
+}
+
+int build_level(ec2d_ctx *ctx, int l) {
+  Level &lv = ctx->lv[l];
+  const ec2d_params &P = ctx->P;
+  int ncase = (int)ctx->cases.size();
+  // host geometry
+  if (l == 1) {
+    for (int c = 0; c < ncase; c++)
+      for (int m = 0; m < (int)ctx->cases[c].blocks.size(); m++) {
+        const HBlock &hb = ctx->cases[c].blocks[m];
+        HLevelBlock B;
+        B.nx = hb.nx; B.ny = hb.ny; B.cas = c; B.blk = m; B.bc = hb.bc; B.nsub = hb.nsub; B.fdm = hb.fdm;
+        Frame *fr[] = {&B.x, &B.y, &B.x1, &B.y1, &B.vol, &B.si, &B.sj, &B.ni1, &B.ni2, &B.nj1, &B.nj2};
+        for (Frame *f : fr) f->init(B.nx, B.ny);
+        for (int j = 1; j <= B.ny; j++)
+          for (int i = 1; i <= B.nx; i++) {
+            B.x(i, j) = hb.x[(i - 1) + (size_t)B.nx * (j - 1)];
+            B.y(i, j) = hb.y[(i - 1) + (size_t)B.nx * (j - 1)];
+          }
+        lv.hb.push_back(std::move(B));
+      }
+  } else {
+    // coarse mesh by node skipping (Creat_Mesh, sub_init.f90:276-373)
+    for (auto &B1 : ctx->lv[l - 1].hb) {
+      HLevelBlock B;
+      B.nx = (B1.nx - 1) / 2 + 1; B.ny = (B1.ny - 1) / 2 + 1; B.cas = B1.cas; B.blk = B1.blk;
+      B.nsub = B1.nsub; B.fdm = false; B.bc = B1.bc;
+      for (int k = 0; k < B.nsub; k++)
+        for (int q = 2; q <= 5; q++) B.bc[9 * k + q] = (B1.bc[9 * k + q] - 1) / 2 + 1;
+      Frame *fr[] = {&B.x, &B.y, &B.x1, &B.y1, &B.vol, &B.si, &B.sj, &B.ni1, &B.ni2, &B.nj1, &B.nj2};
+      for (Frame *f : fr) f->init(B.nx, B.ny);
+      for (int j = 1; j <= B.ny; j++)
+        for (int i = 1; i <= B.nx; i++) { B.x(i, j) = B1.x(2 * i - 1, 2 * j - 1); B.y(i, j) = B1.y(2 * i - 1, 2 * j - 1); }
+      lv.hb.push_back(std::move(B));
+    }
+  }
+  for (auto &B : lv.hb) geometry(B);
+  // ghost coordinates per case (neighbour numbers are case-local)
+  for (int c = 0; c < ncase; c++) {
+    std::vector<HLevelBlock *> bl;
+    for (auto &B : lv.hb) if (B.cas == c) bl.push_back(&B);
+    ghost_coordinates(bl);
+  }
+  for (auto &B : lv.hb) if (B.fdm) fdm_metrics(B);
+  // device layout
+  std::vector<int> case_first_block(ncase, -1);
+  long long off = 0;
+  int tile = 0, sub0 = 0;
+  lv.case_tile0.assign(ncase, 0); lv.case_ntile.assign(ncase, 0); lv.case_ncell.assign(ncase, 0);
+  for (int k = 0; k < (int)lv.hb.size(); k++) {
+    auto &B = lv.hb[k];
+    if (case_first_block[B.cas] < 0) { case_first_block[B.cas] = k; lv.case_tile0[B.cas] = tile; }
+    BlkDev d{};
+    d.nx = B.nx; d.ny = B.ny; d.P = B.nx + 5; d.cas = B.cas; d.off = off; d.fdm = B.fdm ? 1 : 0;
+    d.nsub = B.nsub; d.sub0 = sub0; d.tile0 = tile;
+    off += ((long long)d.P * (B.ny + 5) + 31) / 32 * 32;
+    int items = (B.nx + 3) * (B.ny + 3);
+    int nt = (items + TILE - 1) / TILE;
+    for (int t = 0; t < nt; t++) lv.tiles.push_back(make_int2(k, t * TILE));
+    tile += nt;
+    lv.case_ntile[B.cas] += nt;
+    lv.case_ncell[B.cas] += (B.nx - 1) * (B.ny - 1);
+    for (int s = 0; s < B.nsub; s++) {
+      const int *c = &B.bc[9 * s];
+      SubDev sd{};
+      sd.face = c[1]; sd.ist = c[2]; sd.iend = c[3]; sd.jst = c[4]; sd.jend = c[5]; sd.neighb = c[6]; sd.orient = c[8];
+      sd.nbk = -1;
+      lv.sub.push_back(sd);
+    }
+    sub0 += B.nsub;
+    lv.blk.push_back(d);
+  }
+  // resolve neighbours to level-global block ids
+  for (int k = 0; k < (int)lv.hb.size(); k++) {
+    auto &B = lv.hb[k];
+    for (int s = 0; s < B.nsub; s++) {
+      SubDev &sd = lv.sub[lv.blk[k].sub0 + s];
+      if (sd.neighb < 0) continue;
+      int nb = case_first_block[B.cas] + sd.neighb - 1;
+      if (sd.neighb < 1 || nb >= (int)lv.hb.size() || lv.hb[nb].cas != B.cas) return EC2D_ERR_ARG;
+      int msub = B.bc[9 * s + 7];
+      if (msub < 1 || msub > lv.hb[nb].nsub) return EC2D_ERR_ARG;
+      const int *c1 = &lv.hb[nb].bc[9 * (msub - 1)];
+      // the copied strip must have the same cell count on both sides
+      if ((sd.iend - sd.ist + sd.jend - sd.jst) != (c1[3] - c1[2] + c1[5] - c1[4])) return EC2D_ERR_ARG;
+      sd.nbk = nb; sd.nface = c1[1]; sd.nist = c1[2]; sd.niend = c1[3]; sd.njst = c1[4]; sd.njend = c1[5];
+    }
+  }
+  // wall faces for forces (fine level only)
+  if (l == 1) {
+    lv.case_face0.assign(ncase, 0); lv.case_nface.assign(ncase, 0);
+    for (int c = 0; c < ncase; c++) {
+      lv.case_face0[c] = (int)lv.wall_faces.size();
+      for (int k = 0; k < (int)lv.hb.size(); k++) {
+        auto &B = lv.hb[k];
+        if (B.cas != c) continue;
+        lv.blk[k].lsub0 = (int)lv.wall_faces.size();
+        for (int s = 0; s < B.nsub; s++) {
+          const int *cc = &B.bc[9 * s];
+          if (cc[6] != BC_Wall) continue;
+          bool ifc = (cc[1] == 1 || cc[1] == 3);
+          int kb = ifc ? cc[4] : cc[2], ke = ifc ? cc[5] - 1 : cc[3] - 1;
+          for (int q = kb; q <= ke; q++) lv.wall_faces.push_back(make_int4(k, cc[1], q, s));
+        }
+      }
+      lv.case_nface[c] = (int)lv.wall_faces.size() - lv.case_face0[c];
+    }
+  }
+  lv.F = off;
+  const long long F = off;
+  // allocate device fields
+  Lvl &L = lv.L;
+  L.nblk = (int)lv.blk.size();
+  L.ncase = ncase;
+  L.ntiles = (int)lv.tiles.size();
+  L.F = F;
+  L.level = l;
+  L.nvar = (l == 1) ? ctx->nvar : 4;
+  L.scheme = (l == 1) ? P.Iflag_Scheme : Scheme_UD1;
+  L.gscheme = P.Iflag_Scheme;
+  L.flux = P.Iflag_flux;
+  L.recon = P.IFlag_Reconstruction;
+  L.visc = P.If_viscous;
+  L.turb = (l == 1) ? P.Iflag_turbulence_model : Turb_NONE;
+  L.time_method = P.Time_Method;
+  int nv = L.nvar;
+  BlkDev *dblk = dalloc<BlkDev>(lv, lv.blk.size());
+  SubDev *dsub = dalloc<SubDev>(lv, lv.sub.size());
+  int2 *dtiles = dalloc<int2>(lv, lv.tiles.size());
+  if (!dblk || !dsub || !dtiles) return EC2D_ERR_NOMEM;
+  CK(cudaMemcpy(dblk, lv.blk.data(), lv.blk.size() * sizeof(BlkDev), cudaMemcpyHostToDevice));
+  if (!lv.sub.empty()) CK(cudaMemcpy(dsub, lv.sub.data(), lv.sub.size() * sizeof(SubDev), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(dtiles, lv.tiles.data(), lv.tiles.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  L.blk = dblk; L.sub = dsub; L.tiles = dtiles; L.cs = ctx->d_cases;
+  L.U = dalloc<double>(lv, nv * F);
+  L.q = dalloc<double>(lv, NQ * F);
+  L.amu = dalloc<double>(lv, F);
+  L.amut = dalloc<double>(lv, F);
+  L.res = dalloc<double>(lv, nv * F);
+  L.lc = dalloc<double>(lv, NL * F);
+  L.du = dalloc<double>(lv, nv * F);
+  L.geo = dalloc<double>(lv, NG * F);
+  L.un = dalloc<double>(lv, nv * F);
+  L.deltu = dalloc<double>(lv, 4 * F);
+  L.qf = dalloc<double>(lv, 4 * F);
+  L.un1 = (P.Time_Method == Time_Dual && l == 1) ? dalloc<double>(lv, nv * F) : nullptr;
+  L.fi = dalloc<double>(lv, 6 * F);
+  L.fj = dalloc<double>(lv, 6 * F);
+  L.tb = (L.turb == Turb_SST) ? dalloc<double>(lv, 5 * F) : nullptr;
+  bool anyfdm = false;
+  for (auto &B : lv.hb) anyfdm |= B.fdm;
+  L.met = anyfdm ? dalloc<double>(lv, 5 * F) : nullptr;
+  L.fdm = anyfdm ? dalloc<double>(lv, 30 * F) : nullptr;
+  L.npart = dalloc<double>(lv, lv.tiles.size() * 12);
+  L.norms = dalloc<double>(lv, ncase * 12);
+  L.status = dalloc<int>(lv, ncase * 4);
+  if (!L.U || !L.q || !L.amu || !L.amut || !L.res || !L.lc || !L.du || !L.geo || !L.un || !L.deltu || !L.qf ||
+      !L.fi || !L.fj || !L.npart || !L.norms || !L.status)
+    return EC2D_ERR_NOMEM;
+  lv.d_case_tile0 = dalloc<int>(lv, ncase);
+  lv.d_case_ntile = dalloc<int>(lv, ncase);
+  lv.d_case_ncell = dalloc<int>(lv, ncase);
+  CK(cudaMemcpy(lv.d_case_tile0, lv.case_tile0.data(), ncase * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(lv.d_case_ntile, lv.case_ntile.data(), ncase * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(lv.d_case_ncell, lv.case_ncell.data(), ncase * sizeof(int), cudaMemcpyHostToDevice));
+  if (!lv.wall_faces.empty()) {
+    lv.d_faces = dalloc<int4>(lv, lv.wall_faces.size());
+    lv.d_face_out = dalloc<double>(lv, lv.wall_faces.size() * 5);
+    CK(cudaMemcpy(lv.d_faces, lv.wall_faces.data(), lv.wall_faces.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  }
+  // geometry planes and initial values
+  {
+    std::vector<double> g((size_t)NG * F, 0.0);
+    std::vector<double> u((size_t)nv * F, 0.0), un((size_t)nv * F, 0.0);
+    std::vector<double> met(anyfdm ? (size_t)5 * F : 0, 0.0);
+    for (int k = 0; k < (int)lv.hb.size(); k++) {
+      auto &B = lv.hb[k];
+      long long o = lv.blk[k].off;
+      size_t n = B.x.v.size();
+      Frame *src[] = {&B.vol, &B.si, &B.sj, &B.ni1, &B.ni2, &B.nj1, &B.nj2, &B.x, &B.y, &B.x1, &B.y1};
+      for (int q = 0; q < 11; q++) std::copy(src[q]->v.begin(), src[q]->v.end(), g.begin() + (size_t)q * F + o);
+      for (size_t t = 0; t < n; t++) g[(size_t)G_DW * F + o + t] = 1.0;
+      // B%U(1)=1, U(2)=U(3)=0, U(4)=1 (+ turbulence) ; Un(4)=0 fine, 1 coarse (sub_init.f90:161-174, 311-312)
+      for (size_t t = 0; t < n; t++) {
+        u[0 * F + o + t] = 1.0; u[3 * F + o + t] = 1.0;
+        un[0 * F + o + t] = 1.0; un[3 * F + o + t] = (l == 1) ? 0.0 : 1.0;
+        if (l == 1 && nv == 5) u[4 * F + o + t] = 1.0 / ctx->cases[B.cas].p.Re;
+        if (l == 1 && nv == 6) { u[4 * F + o + t] = 0.0; u[5 * F + o + t] = 1.0; }
+      }
+      if (B.fdm) {
+        Frame *ms[] = {&B.akx, &B.aky, &B.aix, &B.aiy, &B.ajac};
+        for (int q = 0; q < 5; q++) std::copy(ms[q]->v.begin(), ms[q]->v.end(), met.begin() + (size_t)q * F + o);
+      }
+    }
+    CK(cudaMemcpy(L.geo, g.data(), g.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(L.U, u.data(), u.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(L.un, un.data(), un.size() * sizeof(double), cudaMemcpyHostToDevice));
+    if (anyfdm) CK(cudaMemcpy(L.met, met.data(), met.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  return EC2D_OK;
+}
+
+int wall_distance(ec2d_ctx *ctx) {
+  Level &lv = ctx->lv[1];
+  for (int c = 0; c < (int)ctx->cases.size(); c++) {
+    std::vector<double> wxy;
+    for (auto &B : lv.hb) {
+      if (B.cas != c) continue;
+      for (int s = 0; s < B.nsub; s++) {
+        const int *cc = &B.bc[9 * s];
+        if (cc[6] != BC_Wall) continue;
+        for (int j = cc[4]; j <= cc[5]; j++)
+          for (int i = cc[2]; i <= cc[3]; i++) { wxy.push_back(B.x(i, j)); wxy.push_back(B.y(i, j)); }
+      }
+    }
+    double *dw = nullptr;
+    if (!wxy.empty()) {
+      CK(cudaMalloc(&dw, wxy.size() * sizeof(double)));
+      CK(cudaMemcpy(dw, wxy.data(), wxy.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    for (int k = 0; k < (int)lv.hb.size(); k++) {
+      auto &B = lv.hb[k];
+      if (B.cas != c) continue;
+      const HBlock &hb = ctx->cases[c].blocks[B.blk];
+      if (!hb.dw.empty()) {
+        Frame f; f.init(B.nx, B.ny, 1.0);
+        for (int j = 1; j <= B.ny - 1; j++)
+          for (int i = 1; i <= B.nx - 1; i++) f(i, j) = hb.dw[(i - 1) + (size_t)(B.nx - 1) * (j - 1)];
+        CK(cudaMemcpy(lv.L.geo + (size_t)G_DW * lv.F + lv.blk[k].off, f.v.data(), f.v.size() * sizeof(double),
+                      cudaMemcpyHostToDevice));
+      } else if (dw) {
+        launch_wall_distance(lv.L, k, dw, (int)wxy.size() / 2, B.nx, B.ny, ctx->stream);
+      }
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (dw) cudaFree(dw);
+  }
+  return EC2D_OK;
+}
+
+// ---------------- orchestration -------------------------------------------
+
+// Comput_Residual_one_mesh (sub_Residual.f90:13-107) for all blocks of a level
+void residual(ec2d_ctx *ctx, int l) {
+  Level &lv = ctx->lv[l];
+  const Lvl &L = lv.L;
+  cudaStream_t s = ctx->stream;
+  launch_prim(L, s);
+  if (L.visc) {
+    if (L.turb == Turb_SA) launch_sa(L, s);
+    else if (L.turb == Turb_SST) launch_sst(L, s);
+  }
+  launch_flux(L, s);
+  launch_res(L, s);
+  if (L.fdm) launch_fdm(L, s);
+  if (ctx->P.Time_Method == Time_Dual && l == 1) {
+    double sfac;
+    if (ctx->dual_iflag1 == 0) { ctx->dual_iflag1 = 1; sfac = 1.0 / (3.0 * ctx->P.dt_global); }
+    else sfac = 1.0 / (2.0 * ctx->P.dt_global);
+    launch_dual_term(L, sfac, s);
+  }
+  launch_norms(L, lv.d_case_tile0, lv.d_case_ntile, lv.d_case_ncell, s);
+}
+
+void bc_all(ec2d_ctx *ctx, int l) { launch_bc(ctx->lv[l].L, 1 | 2 | 4, ctx->stream); }
+
+void advance_counters(ec2d_ctx *ctx, int l) {
+  for (auto &c : ctx->cases) { c.tt[l] += c.p.dt_global; c.kstep[l] += 1; }
+}
+
+// NS_Time_advance_1Euler (sub_NS_singlegrid.f90:67-106)
+void step_euler(ec2d_ctx *ctx, int l) {
+  residual(ctx, l);
+  launch_euler(ctx->lv[l].L, l != 1, ctx->stream);
+  bc_all(ctx, l);
+  advance_counters(ctx, l);
+}
+// NS_Time_advance_RK3 (sub_NS_singlegrid.f90:115-176)
+void step_rk3(ec2d_ctx *ctx, int l) {
+  const Lvl &L = ctx->lv[l].L;
+  launch_set_un(L, L.nvar, ctx->stream);
+  for (int k = 0; k < 3; k++) {
+    residual(ctx, l);
+    launch_rk3(L, k, l != 1, ctx->stream);
+    bc_all(ctx, l);
+  }
+  advance_counters(ctx, l);
+}
+// NS_Time_advance_LU_SGS (sub_NS_singlegrid.f90:185-224); on a coarse level of
+// an LU-SGS-smoothed multigrid cycle the forcing is added after the residual
+void step_lusgs(ec2d_ctx *ctx, int l, double alfa1 = 0.0) {
+  const Lvl &L = ctx->lv[l].L;
+  residual(ctx, l);
+  if (l != 1) launch_add_force(L, ctx->stream);
+  launch_lusgs(L, alfa1, ctx->stream);
+  launch_add_du(L, ctx->stream);
+  bc_all(ctx, l);
+  advance_counters(ctx, l);
+}
+void clip(ec2d_ctx *ctx, int l) {
+  if (ctx->lv[l].L.nvar >= 5) launch_bc(ctx->lv[l].L, 8, ctx->stream);
+}
+// Dual_time_LU_SGS (sub_NS_singlegrid.f90:231-310).  The inner-loop exit test
+// on the RMS residual needs the norms on the host after every inner step.
+int step_dual(ec2d_ctx *ctx) {
+  double alfa1;
+  if (ctx->dual_iflag == 0) { ctx->dual_iflag = 1; alfa1 = 1.0 / ctx->P.dt_global; }
+  else alfa1 = 3.0 / (2.0 * ctx->P.dt_global);
+  Level &lv = ctx->lv[1];
+  const Lvl &L = lv.L;
+  for (int kt = 1; kt <= ctx->P.Nstep_Inner_Limit; kt++) {
+    residual(ctx, 1);
+    launch_lusgs(L, alfa1, ctx->stream);
+    launch_add_du(L, ctx->stream);
+    bc_all(ctx, 1);
+    std::vector<double> nm(12 * L.ncase);
+    CK(cudaMemcpyAsync(nm.data(), L.norms, nm.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    bool all_done = true;
+    for (int c = 0; c < L.ncase; c++) {
+      double mx = nm[12 * c + 6];
+      for (int m = 0; m < ctx->nvar; m++) mx = std::max(mx, nm[12 * c + 6 + m]);
+      if (!(mx <= ctx->P.Res_Inner_Limit)) all_done = false;
+    }
+    if (all_done) break;
+  }
+  // U(n-1) <= U(n), U(n) <= U on interior cells
+  cudaStream_t s = ctx->stream;
+  size_t bytes = (size_t)L.nvar * lv.F * sizeof(double);
+  CK(cudaMemcpyAsync(L.un1, L.un, bytes, cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(L.un, L.U, bytes, cudaMemcpyDeviceToDevice, s));
+  advance_counters(ctx, 1);
+  return EC2D_OK;
+}
+int time_advance(ec2d_ctx *ctx, int l) {
+  int tm = ctx->P.Time_Method;
+  if (tm == Time_Euler1) step_euler(ctx, l);
+  else if (tm == Time_RK3) step_rk3(ctx, l);
+  else if (tm == Time_LU_SGS) step_lusgs(ctx, l);
+  else if (tm == Time_Dual) { int r = step_dual(ctx); if (r) return r; }
+  clip(ctx, l);
+  return EC2D_OK;
+}
+void mg_smooth_fine(ec2d_ctx *ctx) {
+  int tm = ctx->P.Time_Method;
+  if (tm == Time_Euler1) step_euler(ctx, 1);
+  else if (tm == Time_LU_SGS) { step_lusgs(ctx, 1); clip(ctx, 1); }
+  else step_rk3(ctx, 1);
+}
+void mg_smooth_coarse(ec2d_ctx *ctx, int l) {
+  const int Time_step_coarse_mesh = 3;
+  int tm = ctx->P.Time_Method;
+  if (tm == Time_Euler1) {
+    launch_set_un(ctx->lv[l].L, 4, ctx->stream);
+    for (int m = 0; m < Time_step_coarse_mesh; m++) step_euler(ctx, l);
+  } else if (tm == Time_LU_SGS) {
+    launch_set_un(ctx->lv[l].L, 4, ctx->stream);
+    step_lusgs(ctx, l);
+  } else step_rk3(ctx, l);
+}
+// NS_2stge_multigrid (sub_NS_multigrid.f90:14-58)
+void mg2(ec2d_ctx *ctx) {
+  cudaStream_t s = ctx->stream;
+  Level &l1 = ctx->lv[1], &l2 = ctx->lv[2];
+  mg_smooth_fine(ctx);
+  residual(ctx, 1);
+  launch_restrict(l1.L, l2.L, 2, s);
+  launch_restrict(l1.L, l2.L, 1, s);
+  bc_all(ctx, 2);
+  residual(ctx, 2);
+  launch_force_fn(l2.L, s);
+  mg_smooth_coarse(ctx, 2);
+  launch_delt_u(l2.L, s);
+  launch_prolong(l2.L, l1.L, 2, s);
+  launch_new_u(l1.L, s);
+  bc_all(ctx, 1);
+}
+// NS_3stge_multigrid (sub_NS_multigrid.f90:66-142)
+void mg3(ec2d_ctx *ctx) {
+  cudaStream_t s = ctx->stream;
+  Level &l1 = ctx->lv[1], &l2 = ctx->lv[2], &l3 = ctx->lv[3];
+  mg_smooth_fine(ctx);
+  residual(ctx, 1);
+  launch_restrict(l1.L, l2.L, 2, s);
+  launch_restrict(l1.L, l2.L, 1, s);
+  bc_all(ctx, 2);
+  residual(ctx, 2);
+  launch_force_fn(l2.L, s);
+  mg_smooth_coarse(ctx, 2);
+  residual(ctx, 2);
+  launch_add_force(l2.L, s);
+  launch_restrict(l2.L, l3.L, 2, s);
+  launch_restrict(l2.L, l3.L, 1, s);
+  bc_all(ctx, 3);
+  residual(ctx, 3);
+  launch_force_fn(l3.L, s);
+  mg_smooth_coarse(ctx, 3);
+  launch_delt_u(l3.L, s);
+  launch_prolong(l3.L, l2.L, 2, s);
+  launch_new_u(l2.L, s);
+  launch_delt_u(l2.L, s);
+  launch_prolong(l2.L, l1.L, 2, s);
+  launch_new_u(l1.L, s);
+  bc_all(ctx, 1);
+}
+
+bool valid_case(ec2d_ctx *ctx, int c) { return ctx && c >= 1 && c <= (int)ctx->cases.size(); }
+
+// Fortran extents of the fields of ec2d_get_field
+struct FieldShape { int nv, i0, i1, j0, j1, plane_base; double *base; };
+bool field_shape(ec2d_ctx *ctx, int l, int field, const BlkDev &b, FieldShape &fs) {
+  const Lvl &L = ctx->lv[l].L;
+  int nx = b.nx, ny = b.ny;
+  fs.plane_base = 0;
+  switch (field) {
+    case EC2D_F_RES: fs = {L.nvar, 1, nx - 1, 1, ny - 1, 0, L.res}; return true;
+    case EC2D_F_DT: fs = {1, 1, nx - 1, 1, ny - 1, 0, L.lc + (size_t)L_DT * L.F}; return true;
+    case EC2D_F_LCI: fs = {1, 1, nx, 1, ny, 0, L.lc + (size_t)L_CI * L.F}; return true;
+    case EC2D_F_LCJ: fs = {1, 1, nx, 1, ny, 0, L.lc + (size_t)L_CJ * L.F}; return true;
+    case EC2D_F_LVI: fs = {1, 1, nx, 1, ny, 0, L.lc + (size_t)L_VI * L.F}; return true;
+    case EC2D_F_LVJ: fs = {1, 1, nx, 1, ny, 0, L.lc + (size_t)L_VJ * L.F}; return true;
+    case EC2D_F_DU: fs = {L.nvar, 1, nx, 1, ny, 0, L.du}; return true;
+    case EC2D_F_AMU: fs = {1, -1, nx + 1, -1, ny + 1, 0, L.amu}; return true;
+    case EC2D_F_AMUT: fs = {1, -1, nx + 1, -1, ny + 1, 0, L.amut}; return true;
+    case EC2D_F_X1: fs = {1, -1, nx + 1, -1, ny + 1, 0, L.geo + (size_t)G_X1 * L.F}; return true;
+    case EC2D_F_Y1: fs = {1, -1, nx + 1, -1, ny + 1, 0, L.geo + (size_t)G_Y1 * L.F}; return true;
+    case EC2D_F_VOL: fs = {1, 1, nx, 1, ny, 0, L.geo + (size_t)G_VOL * L.F}; return true;
+    case EC2D_F_SI: fs = {1, 1, nx, 1, ny, 0, L.geo + (size_t)G_SI * L.F}; return true;
+    case EC2D_F_SJ: fs = {1, 1, nx, 1, ny, 0, L.geo + (size_t)G_SJ * L.F}; return true;
+    case EC2D_F_NI1: fs = {1, 1, nx, 1, ny, 0, L.geo + (size_t)G_NI1 * L.F}; return true;
+    case EC2D_F_NI2: fs = {1, 1, nx, 1, ny, 0, L.geo + (size_t)G_NI2 * L.F}; return true;
+    case EC2D_F_NJ1: fs = {1, 1, nx, 1, ny, 0, L.geo + (size_t)G_NJ1 * L.F}; return true;
+    case EC2D_F_NJ2: fs = {1, 1, nx, 1, ny, 0, L.geo + (size_t)G_NJ2 * L.F}; return true;
+    case EC2D_F_DW: fs = {1, 0, nx, 0, ny, 0, L.geo + (size_t)G_DW * L.F}; return true;
+    case EC2D_F_QF: fs = {4, 1, nx - 1, 1, ny - 1, 0, L.qf}; return true;
+    case EC2D_F_DELTU: fs = {4, -1, nx + 1, -1, ny + 1, 0, L.deltu}; return true;
+    case EC2D_F_UN: fs = {L.nvar, 0, nx, 0, ny, 0, L.un}; return true;
+    case EC2D_F_X: fs = {1, -1, nx + 2, -1, ny + 2, 0, L.geo + (size_t)G_X * L.F}; return true;
+    case EC2D_F_Y: fs = {1, -1, nx + 2, -1, ny + 2, 0, L.geo + (size_t)G_Y * L.F}; return true;
+  }
+  return false;
+}
+
+int find_block(ec2d_ctx *ctx, int case_id, int mesh, int block) {
+  if (!ctx->setup_done || !valid_case(ctx, case_id) || mesh < 1 || mesh > ctx->num_mesh) return -1;
+  Level &lv = ctx->lv[mesh];
+  for (int k = 0; k < (int)lv.hb.size(); k++)
+    if (lv.hb[k].cas == case_id - 1 && lv.hb[k].blk == block - 1) return k;
+  return -1;
+}
+
+int check_launch(ec2d_ctx *ctx) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    fprintf(stderr, "ec2d: launch error %s\n", cudaGetErrorString(e));
+    return EC2D_ERR_CUDA;
+  }
+  return EC2D_OK;
+}
+
+}  // namespace
+
+// =============================== C-ABI =====================================
+extern "C" {
+
+int ec2d_version(void) { return 10000; }
+
+const char *ec2d_error_string(int code) {
+  switch (code) {
+    case EC2D_OK: return "ok";
+    case EC2D_ERR_ARG: return "invalid argument or call order";
+    case EC2D_ERR_CUDA: return "CUDA error";
+    case EC2D_ERR_STATE: return "non-physical state (T < 1e-5)";
+    case EC2D_ERR_TIMEOUT: return "device wait timed out";
+    case EC2D_ERR_UNSUPPORTED: return "option combination not supported";
+    case EC2D_ERR_NOMEM: return "out of device memory";
+  }
+  return "unknown error";
+}
+
+int ec2d_create(int device, ec2d_ctx **out) {
+  if (!out) return EC2D_ERR_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return EC2D_ERR_CUDA;
+  CK(cudaSetDevice(device));
+  ec2d_ctx *c = new ec2d_ctx();
+  c->device = device;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { delete c; return EC2D_ERR_CUDA; }
+  *out = c;
+  return EC2D_OK;
+}
+
+void ec2d_destroy(ec2d_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto &lv : ctx->lv) lv.bufs.clear();
+  if (ctx->d_cases) cudaFree(ctx->d_cases);
+  if (ctx->d_stage) cudaFree(ctx->d_stage);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+int ec2d_add_case(ec2d_ctx *ctx, const ec2d_params *p, int *case_id) {
+  if (!ctx || !p || ctx->setup_done) return EC2D_ERR_ARG;
+  if (!ctx->cases.empty() && !same_method(ctx->cases[0].p, *p)) return EC2D_ERR_ARG;
+  HCase c;
+  c.p = *p;
+  c.nvar = (p->Iflag_turbulence_model == Turb_SST) ? 6 : (p->Iflag_turbulence_model == Turb_SA) ? 5 : 4;
+  ctx->cases.push_back(c);
+  if (case_id) *case_id = (int)ctx->cases.size();
+  return EC2D_OK;
+}
+
+int ec2d_add_block(ec2d_ctx *ctx, int case_id, int nx, int ny, const double *x, const double *y, int nsub,
+                   const int *bc9) {
+  if (!valid_case(ctx, case_id) || ctx->setup_done || nx < 3 || ny < 3 || !x || !y || nsub < 0 || (nsub && !bc9))
+    return EC2D_ERR_ARG;
+  HBlock b;
+  b.nx = nx; b.ny = ny; b.nsub = nsub;
+  b.x.assign(x, x + (size_t)nx * ny);
+  b.y.assign(y, y + (size_t)nx * ny);
+  b.bc.assign(bc9, bc9 + 9 * nsub);
+  // every ghost-cell kernel indexes through these ranges: reject anything
+  // that is not a proper block face (face 1: i=1, 3: i=nx, 2: j=1, 4: j=ny)
+  for (int k = 0; k < nsub; k++) {
+    const int *s = &b.bc[9 * k];
+    if (s[1] < 1 || s[1] > 4 || s[2] < 1 || s[3] > nx || s[4] < 1 || s[5] > ny || s[2] > s[3] || s[4] > s[5])
+      return EC2D_ERR_ARG;
+    if ((s[1] == 1 && (s[2] != 1 || s[3] != 1)) || (s[1] == 3 && (s[2] != nx || s[3] != nx)) ||
+        (s[1] == 2 && (s[4] != 1 || s[5] != 1)) || (s[1] == 4 && (s[4] != ny || s[5] != ny)))
+      return EC2D_ERR_ARG;
+    if ((s[1] == 1 || s[1] == 3) ? (s[4] == s[5]) : (s[2] == s[3])) return EC2D_ERR_ARG;
+    if (s[6] >= 0 && s[6] < 1) return EC2D_ERR_ARG;
+  }
+  ctx->cases[case_id - 1].blocks.push_back(std::move(b));
+  return EC2D_OK;
+}
+
+int ec2d_set_fdm_block(ec2d_ctx *ctx, int case_id, int block) {
+  if (!valid_case(ctx, case_id) || ctx->setup_done) return EC2D_ERR_ARG;
+  auto &bl = ctx->cases[case_id - 1].blocks;
+  if (block < 1 || block > (int)bl.size()) return EC2D_ERR_ARG;  // "error in 'FDM.in'"
+  bl[block - 1].fdm = true;
+  return EC2D_OK;
+}
+
+int ec2d_set_wall_distance(ec2d_ctx *ctx, int case_id, int block, const double *dw) {
+  if (!valid_case(ctx, case_id) || ctx->setup_done || !dw) return EC2D_ERR_ARG;
+  auto &bl = ctx->cases[case_id - 1].blocks;
+  if (block < 1 || block > (int)bl.size()) return EC2D_ERR_ARG;
+  HBlock &b = bl[block - 1];
+  b.dw.assign(dw, dw + (size_t)(b.nx - 1) * (b.ny - 1));
+  return EC2D_OK;
+}
+
+int ec2d_setup(ec2d_ctx *ctx) {
+  if (!ctx || ctx->setup_done || ctx->cases.empty()) return EC2D_ERR_ARG;
+  CK(cudaSetDevice(ctx->device));
+  ctx->P = ctx->cases[0].p;
+  const ec2d_params &P = ctx->P;
+  for (auto &c : ctx->cases) if (c.blocks.empty()) return EC2D_ERR_ARG;
+  // opencfd_ec2d_v1.5.4.f90:216-221 (lifted for LU-SGS when mg_lusgs is set)
+  if ((P.Time_Method == Time_LU_SGS && P.Num_Mesh != 1 && !P.mg_lusgs) ||
+      (P.Time_Method == Time_Dual && P.Num_Mesh != 1))
+    return EC2D_ERR_UNSUPPORTED;
+  if (P.If_viscous && P.Iflag_turbulence_model == Turb_BL) return EC2D_ERR_UNSUPPORTED;
+  if (P.Iflag_turbulence_model != Turb_NONE && !P.If_viscous) return EC2D_ERR_UNSUPPORTED;
+  int nm = 3;
+  for (auto &c : ctx->cases) nm = std::min(nm, mg_depth(c));
+  ctx->num_mesh = nm;
+  ctx->nvar = ctx->cases[0].nvar;
+  std::vector<CaseDev> cd;
+  for (auto &c : ctx->cases) cd.push_back(make_casedev(c.p));
+  CK(cudaMalloc(&ctx->d_cases, cd.size() * sizeof(CaseDev)));
+  CK(cudaMemcpy(ctx->d_cases, cd.data(), cd.size() * sizeof(CaseDev), cudaMemcpyHostToDevice));
+  for (int l = 1; l <= nm; l++) {
+    int r = build_level(ctx, l);
+    if (r) return r;
+  }
+  if (P.Iflag_turbulence_model == Turb_SA || P.Iflag_turbulence_model == Turb_SST) {
+    int r = wall_distance(ctx);
+    if (r) return r;
+  }
+  size_t mx = 0;
+  for (int l = 1; l <= nm; l++)
+    for (auto &b : ctx->lv[l].blk) mx = std::max(mx, (size_t)(b.nx + 3) * (b.ny + 3) * 6);
+  CK(cudaMalloc(&ctx->d_stage, mx * sizeof(double)));
+  ctx->stage_n = mx;
+  CK(cudaDeviceSynchronize());
+  ctx->setup_done = true;
+  return EC2D_OK;
+}
+
+int ec2d_num_mesh(ec2d_ctx *ctx, int *num_mesh) {
+  if (!ctx || !ctx->setup_done || !num_mesh) return EC2D_ERR_ARG;
+  *num_mesh = ctx->num_mesh;
+  return EC2D_OK;
+}
+
+int ec2d_block_dims(ec2d_ctx *ctx, int case_id, int mesh, int block, int *nx, int *ny, int *nvar) {
+  int k = find_block(ctx, case_id, mesh, block);
+  if (k < 0) return EC2D_ERR_ARG;
+  const BlkDev &b = ctx->lv[mesh].blk[k];
+  if (nx) *nx = b.nx;
+  if (ny) *ny = b.ny;
+  if (nvar) *nvar = ctx->lv[mesh].L.nvar;
+  return EC2D_OK;
+}
+
+// init_flow_zero (sub_init.f90:423-495)
+int ec2d_init_flow(ec2d_ctx *ctx) {
+  if (!ctx || !ctx->setup_done) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  int nm = ctx->num_mesh;
+  if (ctx->nvar >= 5) launch_freestream(ctx->lv[1].L, 0, 1, ctx->stream);
+  launch_freestream(ctx->lv[nm].L, 1, 0, ctx->stream);
+  bc_all(ctx, nm);
+  for (int l = nm; l >= 1; l--) {
+    int pre = ctx->P.Pre_Step_Mesh[l - 1];
+    for (int st = 0; st < pre; st++) {
+      int r = time_advance(ctx, l);
+      if (r) return r;
+    }
+    if (l > 1) {
+      launch_prolong(ctx->lv[l].L, ctx->lv[l - 1].L, 1, ctx->stream);
+      bc_all(ctx, l - 1);
+    }
+  }
+  if (ctx->P.Time_Method == Time_Dual) {
+    const Lvl &L = ctx->lv[1].L;
+    size_t bytes = (size_t)L.nvar * ctx->lv[1].F * sizeof(double);
+    CK(cudaMemcpyAsync(L.un, L.U, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(L.un1, L.U, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  return check_launch(ctx);
+}
+
+int ec2d_upload_U(ec2d_ctx *ctx, int case_id, int mesh, int block, const double *U) {
+  int k = find_block(ctx, case_id, mesh, block);
+  if (k < 0 || !U) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  const Lvl &L = ctx->lv[mesh].L;
+  const BlkDev &b = ctx->lv[mesh].blk[k];
+  int items = (b.nx + 3) * (b.ny + 3);
+  CK(cudaMemcpyAsync(ctx->d_stage, U, (size_t)items * L.nvar * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  launch_pack_u(L, k, L.nvar, ctx->d_stage, items, ctx->stream);
+  return check_launch(ctx);
+}
+
+int ec2d_download_U(ec2d_ctx *ctx, int case_id, int mesh, int block, double *U) {
+  int k = find_block(ctx, case_id, mesh, block);
+  if (k < 0 || !U) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  const Lvl &L = ctx->lv[mesh].L;
+  const BlkDev &b = ctx->lv[mesh].blk[k];
+  int items = (b.nx + 3) * (b.ny + 3);
+  launch_unpack_u(L, k, L.nvar, ctx->d_stage, items, ctx->stream);
+  CK(cudaMemcpyAsync(U, ctx->d_stage, (size_t)items * L.nvar * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return EC2D_OK;
+}
+
+int ec2d_step(ec2d_ctx *ctx, int nsteps) {
+  if (!ctx || !ctx->setup_done || nsteps < 0) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  for (int n = 0; n < nsteps; n++) {
+    if (ctx->num_mesh == 1) { int r = time_advance(ctx, 1); if (r) return r; }
+    else if (ctx->num_mesh == 2) mg2(ctx);
+    else mg3(ctx);
+  }
+  return check_launch(ctx);
+}
+
+int ec2d_residual(ec2d_ctx *ctx, int case_id, int mesh, double res_max[6], double res_rms[6], int *kstep,
+                  double *tt) {
+  if (!ctx || !ctx->setup_done || !valid_case(ctx, case_id) || mesh < 1 || mesh > ctx->num_mesh) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  const Lvl &L = ctx->lv[mesh].L;
+  double nm[12];
+  int st[4];
+  CK(cudaMemcpyAsync(nm, L.norms + 12 * (case_id - 1), sizeof(nm), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(st, L.status + 4 * (case_id - 1), sizeof(st), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (res_max) for (int m = 0; m < 6; m++) res_max[m] = nm[m];
+  if (res_rms) for (int m = 0; m < 6; m++) res_rms[m] = nm[6 + m];
+  if (kstep) *kstep = ctx->cases[case_id - 1].kstep[mesh];
+  if (tt) *tt = ctx->cases[case_id - 1].tt[mesh];
+  return st[0] ? EC2D_ERR_STATE : EC2D_OK;
+}
+
+int ec2d_status(ec2d_ctx *ctx, int case_id, int *code, int *block, int *i, int *j) {
+  if (!ctx || !ctx->setup_done || !valid_case(ctx, case_id)) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  int st[4] = {0, 0, 0, 0};
+  for (int l = 1; l <= ctx->num_mesh; l++) {
+    CK(cudaMemcpyAsync(st, ctx->lv[l].L.status + 4 * (case_id - 1), sizeof(st), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (st[0]) {
+      if (st[1] >= 0 && st[1] < (int)ctx->lv[l].hb.size()) st[1] = ctx->lv[l].hb[st[1]].blk + 1;
+      break;
+    }
+  }
+  if (code) *code = st[0];
+  if (block) *block = st[1];
+  if (i) *i = st[2];
+  if (j) *j = st[3];
+  return EC2D_OK;
+}
+
+static int run_forces(ec2d_ctx *ctx, int case_id, std::vector<double> &out) {
+  Level &lv = ctx->lv[1];
+  int c = case_id - 1;
+  if (lv.wall_faces.empty()) { out.clear(); return EC2D_OK; }
+  launch_prim(lv.L, ctx->stream);
+  launch_forces(lv.L, lv.d_faces, (int)lv.wall_faces.size(), lv.d_face_out, ctx->stream);
+  int n = lv.case_nface[c];
+  out.assign((size_t)n * 5, 0.0);
+  if (n)
+    CK(cudaMemcpyAsync(out.data(), lv.d_face_out + (size_t)5 * lv.case_face0[c], out.size() * sizeof(double),
+                       cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return check_launch(ctx);
+}
+
+int ec2d_forces(ec2d_ctx *ctx, int case_id, double *cl, double *cd, double *cm) {
+  if (!ctx || !ctx->setup_done || !valid_case(ctx, case_id)) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  std::vector<double> out;
+  int r = run_forces(ctx, case_id, out);
+  if (r) return r;
+  const ec2d_params &p = ctx->cases[case_id - 1].p;
+  double Fx = 0, Fy = 0, Mz = 0;
+  for (size_t f = 0; f < out.size() / 5; f++) {
+    Fx += out[5 * f]; Fy += out[5 * f + 1];
+    Mz += (out[5 * f + 2] - p.xaxis) * out[5 * f + 1] - (out[5 * f + 3] - p.yaxis) * out[5 * f];
+  }
+  double aoa = p.AoA * PI / 180.0, q = 0.5, ca = std::cos(aoa), sa = std::sin(aoa);
+  if (cl) *cl = (-Fx * sa + Fy * ca) / q;
+  if (cd) *cd = (Fx * ca + Fy * sa) / q;
+  if (cm) *cm = -Mz / q;
+  return EC2D_OK;
+}
+
+int ec2d_wall_cf(ec2d_ctx *ctx, int case_id, int block, int sub, double *cf, double *xc, int maxn, int *n) {
+  if (!ctx || !ctx->setup_done || !valid_case(ctx, case_id)) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  std::vector<double> out;
+  int r = run_forces(ctx, case_id, out);
+  if (r) return r;
+  Level &lv = ctx->lv[1];
+  int cnt = 0;
+  int f0 = lv.case_face0[case_id - 1];
+  for (int f = 0; f < lv.case_nface[case_id - 1]; f++) {
+    int4 w = lv.wall_faces[f0 + f];
+    if (lv.hb[w.x].blk != block - 1 || w.w != sub - 1) continue;
+    if (cnt < maxn) { if (cf) cf[cnt] = out[5 * f + 4]; if (xc) xc[cnt] = out[5 * f + 2]; }
+    cnt++;
+  }
+  if (n) *n = cnt;
+  return EC2D_OK;
+}
+
+int ec2d_field_size(ec2d_ctx *ctx, int case_id, int mesh, int block, int field, int *n) {
+  int k = find_block(ctx, case_id, mesh, block);
+  FieldShape fs;
+  if (k < 0 || !n || !field_shape(ctx, mesh, field, ctx->lv[mesh].blk[k], fs)) return EC2D_ERR_ARG;
+  *n = fs.nv * (fs.i1 - fs.i0 + 1) * (fs.j1 - fs.j0 + 1);
+  return EC2D_OK;
+}
+
+int ec2d_get_field(ec2d_ctx *ctx, int case_id, int mesh, int block, int field, double *out) {
+  int k = find_block(ctx, case_id, mesh, block);
+  FieldShape fs;
+  if (k < 0 || !out || !field_shape(ctx, mesh, field, ctx->lv[mesh].blk[k], fs)) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  CK(cudaStreamSynchronize(ctx->stream));
+  const BlkDev &b = ctx->lv[mesh].blk[k];
+  long long F = ctx->lv[mesh].F;
+  size_t fsz = (size_t)b.P * (b.ny + 5);
+  std::vector<double> fr(fsz);
+  int ni = fs.i1 - fs.i0 + 1, nj = fs.j1 - fs.j0 + 1;
+  for (int m = 0; m < fs.nv; m++) {
+    CK(cudaMemcpy(fr.data(), fs.base + (size_t)m * F + b.off, fsz * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int j = 0; j < nj; j++)
+      for (int i = 0; i < ni; i++)
+        out[(size_t)m + (size_t)fs.nv * (i + (size_t)ni * j)] = fr[(size_t)(fs.j0 + j + 2) * b.P + (fs.i0 + i + 2)];
+  }
+  return EC2D_OK;
+}
+
+int ec2d_set_field(ec2d_ctx *ctx, int case_id, int mesh, int block, int field, const double *in) {
+  int k = find_block(ctx, case_id, mesh, block);
+  FieldShape fs;
+  if (k < 0 || !in || !field_shape(ctx, mesh, field, ctx->lv[mesh].blk[k], fs)) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  CK(cudaStreamSynchronize(ctx->stream));
+  const BlkDev &b = ctx->lv[mesh].blk[k];
+  long long F = ctx->lv[mesh].F;
+  size_t fsz = (size_t)b.P * (b.ny + 5);
+  std::vector<double> fr(fsz);
+  int ni = fs.i1 - fs.i0 + 1, nj = fs.j1 - fs.j0 + 1;
+  for (int m = 0; m < fs.nv; m++) {
+    double *dst = fs.base + (size_t)m * F + b.off;
+    CK(cudaMemcpy(fr.data(), dst, fsz * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int j = 0; j < nj; j++)
+      for (int i = 0; i < ni; i++)
+        fr[(size_t)(fs.j0 + j + 2) * b.P + (fs.i0 + i + 2)] = in[(size_t)m + (size_t)fs.nv * (i + (size_t)ni * j)];
+    CK(cudaMemcpy(dst, fr.data(), fsz * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  return EC2D_OK;
+}
+
+int ec2d_comput_residual(ec2d_ctx *ctx, int mesh) {
+  if (!ctx || !ctx->setup_done || mesh < 1 || mesh > ctx->num_mesh) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  residual(ctx, mesh);
+  return check_launch(ctx);
+}
+int ec2d_boundary_condition(ec2d_ctx *ctx, int mesh) {
+  if (!ctx || !ctx->setup_done || mesh < 1 || mesh > ctx->num_mesh) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  launch_bc(ctx->lv[mesh].L, 1, ctx->stream);
+  return check_launch(ctx);
+}
+int ec2d_update_buffer(ec2d_ctx *ctx, int mesh) {
+  if (!ctx || !ctx->setup_done || mesh < 1 || mesh > ctx->num_mesh) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  launch_bc(ctx->lv[mesh].L, 2 | 4, ctx->stream);
+  return check_launch(ctx);
+}
+int ec2d_du_lusgs(ec2d_ctx *ctx, int mesh, double alfa1) {
+  if (!ctx || !ctx->setup_done || mesh < 1 || mesh > ctx->num_mesh) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  launch_lusgs(ctx->lv[mesh].L, alfa1, ctx->stream);
+  return check_launch(ctx);
+}
+int ec2d_time_advance(ec2d_ctx *ctx, int mesh) {
+  if (!ctx || !ctx->setup_done || mesh < 1 || mesh > ctx->num_mesh) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  int r = time_advance(ctx, mesh);
+  if (r) return r;
+  return check_launch(ctx);
+}
+int ec2d_interpolation2h(ec2d_ctx *ctx, int m1, int m2, int flag) {
+  if (!ctx || !ctx->setup_done || m2 != m1 + 1 || m1 < 1 || m2 > ctx->num_mesh || (flag != 1 && flag != 2))
+    return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  launch_restrict(ctx->lv[m1].L, ctx->lv[m2].L, flag, ctx->stream);
+  return check_launch(ctx);
+}
+int ec2d_prolong(ec2d_ctx *ctx, int m1, int m2, int flag) {
+  if (!ctx || !ctx->setup_done || m2 != m1 - 1 || m2 < 1 || m1 > ctx->num_mesh || (flag != 1 && flag != 2))
+    return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  launch_prolong(ctx->lv[m1].L, ctx->lv[m2].L, flag, ctx->stream);
+  return check_launch(ctx);
+}
+int ec2d_force_function(ec2d_ctx *ctx, int mesh) {
+  if (!ctx || !ctx->setup_done || mesh < 2 || mesh > ctx->num_mesh) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  launch_force_fn(ctx->lv[mesh].L, ctx->stream);
+  return check_launch(ctx);
+}
+int ec2d_sync(ec2d_ctx *ctx) {
+  if (!ctx) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  CK(cudaStreamSynchronize(ctx->stream));
+  return EC2D_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,43 @@
+// ec2d_internal.h -- launch wrappers shared between the kernel files and the
+// C-ABI layer (not part of the public interface).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "ec2d_dev.cuh"
+
+namespace ec2d {
+
+// k_residual.cu
+void launch_prim(const Lvl &L, cudaStream_t s);
+void launch_flux(const Lvl &L, cudaStream_t s);
+void launch_res(const Lvl &L, cudaStream_t s);
+void launch_norms(const Lvl &L, const int *case_tile0, const int *case_ntile, const int *case_ncell,
+                  cudaStream_t s);
+// k_turb.cu
+void launch_sa(const Lvl &L, cudaStream_t s);
+void launch_sst(const Lvl &L, cudaStream_t s);
+void launch_amut_boundary(const Lvl &L, cudaStream_t s);
+void launch_fdm(const Lvl &L, cudaStream_t s);
+void launch_dual_term(const Lvl &L, double sfac, cudaStream_t s);
+// k_bc.cu
+void launch_bc(const Lvl &L, int phases, cudaStream_t s);
+// k_lusgs.cu
+void launch_lusgs(const Lvl &L, double alfa1, cudaStream_t s);
+void launch_add_du(const Lvl &L, cudaStream_t s);
+void launch_euler(const Lvl &L, int force, cudaStream_t s);
+void launch_rk3(const Lvl &L, int stage, int force, cudaStream_t s);
+void launch_add_force(const Lvl &L, cudaStream_t s);
+void launch_force_fn(const Lvl &L, cudaStream_t s);
+void launch_set_un(const Lvl &L, int nv, cudaStream_t s);
+void launch_delt_u(const Lvl &L, cudaStream_t s);
+void launch_new_u(const Lvl &L, cudaStream_t s);
+void launch_restrict(const Lvl &Lf, const Lvl &Lc, int flag, cudaStream_t s);
+void launch_prolong(const Lvl &Lc, const Lvl &Lf, int flag, cudaStream_t s);
+void launch_freestream(const Lvl &L, int flow, int turb, cudaStream_t s);
+// k_misc.cu
+void launch_pack_u(const Lvl &L, int bk, int nv, const double *aos, int nitems, cudaStream_t s);
+void launch_unpack_u(const Lvl &L, int bk, int nv, double *aos, int nitems, cudaStream_t s);
+void launch_wall_distance(const Lvl &L, int bk, const double *wall_xy, int nwall, int nx, int ny, cudaStream_t s);
+void launch_forces(const Lvl &L, const int4 *faces, int nfaces, double *out, cudaStream_t s);
+
+}  // namespace ec2d

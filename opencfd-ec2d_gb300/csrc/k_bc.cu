@@ -1,0 +1,252 @@
+// k_bc.cu -- ghost cells: physical boundary conditions (sub_boundary.f90:10-34,
+// 306-581), block-interface halo copy and ghost-corner extrapolation
+// (update_buffer_onemesh, sub_boundary.f90:45-153), and the nu~/k/omega
+// clip (force_vt_kw, sub_NS_singlegrid.f90:30-60).
+//
+// Write order.  The reference runs every physical subface of every block in
+// (block, subface) order, then per block its halo copies followed by its four
+// ghost corners.  A physical subface loops over node indices ist..iend,
+// jst..jend, so its end points write ghost rows that later subfaces read.
+// The write sets of one subface never overlap its read set, halo copies read
+// only interior cells, and corners read only the block's own ghosts.  Hence
+// one CTA per block reproduces the reference exactly: subfaces of phase 1 in
+// order with a barrier between them, all halo items of phase 2 in parallel,
+// then the corners.
+#include "ec2d_dev.cuh"
+#include "ec2d_internal.h"
+
+namespace ec2d {
+
+__device__ __forceinline__ void ghost_pair(int face, int i, int j, int k, int &i1, int &j1, int &i2, int &j2) {
+  if (face == 1) { i1 = i + k - 1; j1 = j; i2 = i - k; j2 = j; }
+  else if (face == 2) { i1 = i; j1 = j + k - 1; i2 = i; j2 = j - k; }
+  else if (face == 3) { i1 = i - k; j1 = j; i2 = i + k - 1; j2 = j; }
+  else { i1 = i; j1 = j - k; i2 = i; j2 = j + k - 1; }
+}
+
+// boundary_wall, sub_boundary.f90:306-386
+__device__ void bc_wall(const Lvl &L, const BlkDev &b, const CaseDev &c, const SubDev &s, int i, int j, int k) {
+  const long long F = L.F;
+  int i1, j1, i2, j2;
+  ghost_pair(s.face, i, j, k, i1, j1, i2, j2);
+  long long a = fidx(b, i1, j1), g = fidx(b, i2, j2);
+  double *U = L.U;
+  double d1 = U[a];
+  if (c.Twall <= 0) {
+    U[g] = U[a];
+    U[F + g] = -U[F + a];
+    U[2 * F + g] = -U[2 * F + a];
+    U[3 * F + g] = U[3 * F + a];
+  } else {
+    double u1 = U[F + a] / d1, v1 = U[2 * F + a] / d1;
+    double p1 = (U[3 * F + a] - 0.5 * d1 * (u1 * u1 + v1 * v1)) * (c.gamma - 1.0);
+    double T1 = c.gamma * c.Ma * c.Ma * p1 / d1;
+    double p2 = p1, T2 = 2.0 * c.Twall - T1, u2 = -u1, v2 = -v1;
+    double d2 = c.gamma * c.Ma * c.Ma * p2 / T2;
+    U[g] = d2;
+    U[F + g] = d2 * u2;
+    U[2 * F + g] = d2 * v2;
+    U[3 * F + g] = p2 / (c.gamma - 1.0) + 0.5 * d2 * (u2 * u2 + v2 * v2);
+  }
+  if (L.nvar == 5) U[4 * F + g] = 0.0;
+  if (L.nvar == 6) {
+    const double beta1 = 0.075;
+    double d2 = U[g];
+    double r2 = U[F + g], r3 = U[2 * F + g];
+    double T2 = (U[3 * F + g] - 0.5 * (r2 * r2 + r3 * r3) / d2) / (c.Cv * d2);
+    double Amu2 = (1.0 + c.Tsb) * sqrt(T2 * T2 * T2) / (c.Tsb + T2);
+    double dw = L.geo[G_DW * F + a];
+    double wt = 60.0 * Amu2 / (d2 * beta1 * (dw * dw) * c.Re * c.Re);
+    U[4 * F + g] = -U[4 * F + a];
+    U[5 * F + g] = (d1 + d2) * wt - U[5 * F + a];
+  }
+}
+
+// Symmetry_or_slidewall, sub_boundary.f90:391-451
+__device__ void bc_symmetry(const Lvl &L, const BlkDev &b, const SubDev &s, int i, int j, int k) {
+  const long long F = L.F;
+  const double *x = L.geo + G_X * F, *y = L.geo + G_Y * F;
+  double n1, n2;
+  if (s.face == 1 || s.face == 3) {
+    long long p0 = fidx(b, i, j), p1 = fidx(b, i, j + 1);
+    double dx = x[p1] - x[p0], dy = y[p1] - y[p0];
+    double si = sqrt(dx * dx + dy * dy);
+    n1 = dy / si; n2 = -dx / si;
+  } else {
+    long long p0 = fidx(b, i, j), p1 = fidx(b, i + 1, j);
+    double dx = x[p1] - x[p0], dy = y[p1] - y[p0];
+    double si = sqrt(dx * dx + dy * dy);
+    n1 = -dy / si; n2 = dx / si;
+  }
+  int i1, j1, i2, j2;
+  ghost_pair(s.face, i, j, k, i1, j1, i2, j2);
+  long long a = fidx(b, i1, j1), g = fidx(b, i2, j2);
+  double *U = L.U;
+  double Vn = U[F + a] * n1 + U[2 * F + a] * n2;
+  U[g] = U[a];
+  U[F + g] = U[F + a] - 2.0 * Vn * n1;
+  U[2 * F + g] = U[2 * F + a] - 2.0 * Vn * n2;
+  U[3 * F + g] = U[3 * F + a];
+  for (int m = 4; m < L.nvar; m++) U[m * F + g] = U[m * F + a];
+}
+
+// boundary_Farfield_inlet_outlet, sub_boundary.f90:457-581.  The inflow /
+// outflow switch is a sign test on a computed normal Mach number, so this
+// routine is evaluated with separately rounded operations (no contraction)
+// to take the same branch as the reference on every cell.
+__device__ void bc_farfield(const Lvl &L, const BlkDev &b, const CaseDev &c, const SubDev &s, int i, int j, int k) {
+  const long long F = L.F;
+  double *U = L.U;
+  const double *x = L.geo + G_X * F, *y = L.geo + G_Y * F;
+  const double gamma = c.gamma, gm1 = gamma - 1.0;
+  int i1, j1;
+  if (s.face == 1 || s.face == 2) { i1 = i; j1 = j; }
+  else if (s.face == 3) { i1 = i - 1; j1 = j; }
+  else { i1 = i; j1 = j - 1; }
+  long long a = fidx(b, i1, j1);
+  double d1 = U[a];
+  double u1 = __ddiv_rn(U[F + a], d1), v1 = __ddiv_rn(U[2 * F + a], d1);
+  double ke = __dmul_rn(__dmul_rn(0.5, d1), __dadd_rn(__dmul_rn(u1, u1), __dmul_rn(v1, v1)));
+  double p1 = __dmul_rn(__dsub_rn(U[3 * F + a], ke), gm1);
+  double c1 = __dsqrt_rn(__ddiv_rn(__dmul_rn(gamma, p1), d1));
+  double dx, dy, n1, n2;
+  if (s.face == 1 || s.face == 3) {
+    long long p0 = fidx(b, i, j), p1i = fidx(b, i, j + 1);
+    dx = __dsub_rn(x[p1i], x[p0]); dy = __dsub_rn(y[p1i], y[p0]);
+  } else {
+    long long p0 = fidx(b, i, j), p1i = fidx(b, i + 1, j);
+    dx = __dsub_rn(x[p1i], x[p0]); dy = __dsub_rn(y[p1i], y[p0]);
+  }
+  double sl = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+  if (s.face == 1 || s.face == 4) { n1 = __ddiv_rn(-dy, sl); n2 = __ddiv_rn(dx, sl); }
+  else { n1 = __ddiv_rn(dy, sl); n2 = __ddiv_rn(-dx, sl); }
+  double Ma_n = __ddiv_rn(__dadd_rn(__dmul_rn(u1, n1), __dmul_rn(v1, n2)), c1);
+  int i2, j2;
+  if (s.face == 1) { i2 = i - k; j2 = j; }
+  else if (s.face == 2) { i2 = i; j2 = j - k; }
+  else if (s.face == 3) { i2 = i + k - 1; j2 = j; }
+  else { i2 = i; j2 = j + k - 1; }
+  long long g = fidx(b, i2, j2);
+  int type = s.neighb;
+  if (type == BC_Outlet || (type == BC_Farfield && Ma_n >= 0.0)) {
+    if (Ma_n > 1.0 || c.p_outlet < 0 || type == BC_Farfield) {
+      for (int m = 0; m < L.nvar; m++) U[m * F + g] = U[m * F + a];
+    } else {
+      double pb = c.p_outlet;
+      double db = d1 + (c.p_outlet - p1) / (c1 * c1);
+      double ub = u1 + (p1 - c.p_outlet) / (d1 * c1) * n1;
+      double vb = v1 + (p1 - c.p_outlet) / (d1 * c1) * n2;
+      double p2 = 2.0 * pb - p1, d2 = 2.0 * db - d1, u2 = 2.0 * ub - u1, v2 = 2.0 * vb - v1;
+      U[g] = d2; U[F + g] = d2 * u2; U[2 * F + g] = d2 * v2;
+      U[3 * F + g] = p2 / gm1 + 0.5 * d2 * (u2 * u2 + v2 * v2);
+      for (int m = 4; m < L.nvar; m++) U[m * F + g] = U[m * F + a];
+    }
+  } else {
+    const double d_inf = 1.0, u_inf = c.cosA, v_inf = c.sinA, p_inf = c.p00;
+    if (c.p_outlet < 0 || Ma_n <= -1.0) {
+      U[g] = d_inf; U[F + g] = d_inf * u_inf; U[2 * F + g] = d_inf * v_inf;
+      U[3 * F + g] = p_inf / gm1 + 0.5 * d_inf * (u_inf * u_inf + v_inf * v_inf);
+    } else {
+      double pb = 0.5 * (p1 + p_inf - d1 * c1 * ((u_inf - u1) * n1 + (v_inf - v1) * n2));
+      double db = d_inf + (pb - p_inf) / (c1 * c1);
+      double ub = u_inf - (p_inf - pb) / (d1 * c1) * n1;
+      double vb = v_inf - (p_inf - pb) / (d1 * c1) * n2;
+      double p2 = 2.0 * pb - p1, d2 = 2.0 * db - d1, u2 = 2.0 * ub - u1, v2 = 2.0 * vb - v1;
+      U[g] = d2; U[F + g] = d2 * u2; U[2 * F + g] = d2 * v2;
+      U[3 * F + g] = p2 / gm1 + 0.5 * d2 * (u2 * u2 + v2 * v2);
+    }
+    if (L.nvar == 5) U[4 * F + g] = c.vt_inf / c.Re;
+    else if (L.nvar == 6) { U[4 * F + g] = d_inf * c.Kt_inf; U[5 * F + g] = d_inf * c.Wt_inf; }
+  }
+}
+
+// U_average_conner, sub_boundary.f90:595-612
+__device__ void corner(const Lvl &L, const CaseDev &c, long long i1, long long i2, long long i3, long long i4) {
+  const long long F = L.F;
+  double *U = L.U;
+  double Cv = c.Cv;
+  double d1 = U[i1], uu1 = U[F + i1] / d1, v1 = U[2 * F + i1] / d1;
+  double T1 = (U[3 * F + i1] - (uu1 * U[F + i1] + v1 * U[2 * F + i1]) * 0.5) / (d1 * Cv);
+  double d2 = U[i2], uu2 = U[F + i2] / d2, v2 = U[2 * F + i2] / d2;
+  double T2 = (U[3 * F + i2] - (uu2 * U[F + i2] + v2 * U[2 * F + i2]) * 0.5) / (d2 * Cv);
+  double d3 = U[i3], uu3 = U[F + i3] / d3, v3 = U[2 * F + i3] / d3;
+  double T3 = (U[3 * F + i3] - (uu3 * U[F + i3] + v3 * U[2 * F + i3]) * 0.5) / (d3 * Cv);
+  double d4 = d1 + d3 - d2, uu4 = uu1 + uu3 - uu2, v4 = v1 + v3 - v2, T4 = T1 + T3 - T2;
+  U[i4] = d4;
+  U[F + i4] = d4 * uu4;
+  U[2 * F + i4] = d4 * v4;
+  U[3 * F + i4] = d4 * (Cv * T4 + (uu4 * uu4 + v4 * v4) * 0.5);
+  for (int m = 4; m < L.nvar; m++) U[m * F + i4] = U[m * F + i1] + U[m * F + i3] - U[m * F + i2];
+}
+
+// phases: 1 physical BCs, 2 halo copy, 4 corners, 8 nu~/k/omega clip
+__global__ void __launch_bounds__(256) k_bc(Lvl L, int phases) {
+  const int bk = blockIdx.x;
+  const BlkDev &b = L.blk[bk];
+  const CaseDev &c = L.cs[b.cas];
+  const long long F = L.F;
+  if (phases & 1) {
+    for (int ks = 0; ks < b.nsub; ks++) {
+      const SubDev s = L.sub[b.sub0 + ks];
+      if (s.neighb < 0) {
+        int ni = s.iend - s.ist + 1, nj = s.jend - s.jst + 1;
+        int nitem = ni * nj * LAP;
+        for (int t = threadIdx.x; t < nitem; t += blockDim.x) {
+          int k = t % LAP + 1, r = t / LAP;
+          int i = s.ist + r % ni, j = s.jst + r / ni;
+          if (s.neighb == BC_Wall) bc_wall(L, b, c, s, i, j, k);
+          else if (s.neighb == BC_Farfield || s.neighb == BC_Inlet || s.neighb == BC_Outlet)
+            bc_farfield(L, b, c, s, i, j, k);
+          else if (s.neighb == BC_Symmetry) bc_symmetry(L, b, s, i, j, k);
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if (phases & 2) {
+    for (int ks = 0; ks < b.nsub; ks++) {
+      const SubDev s = L.sub[b.sub0 + ks];
+      if (s.neighb < 0) continue;
+      const BlkDev &nb = L.blk[s.nbk];
+      int n1 = s.iend - s.ist + s.jend - s.jst;
+      for (int t = threadIdx.x; t < n1 * LAP; t += blockDim.x) {
+        int l = t % LAP + 1, k = t / LAP + 1;
+        int k1 = (s.orient == 2) ? k : n1 + 1 - k;
+        int si, sj;
+        if (s.nface == 1) { si = s.nist + l - 1; sj = s.njst + k1 - 1; }
+        else if (s.nface == 2) { si = s.nist + k1 - 1; sj = s.njst + l - 1; }
+        else if (s.nface == 3) { si = s.niend - LAP - 1 + l; sj = s.njst + k1 - 1; }
+        else { si = s.nist + k1 - 1; sj = s.njend - LAP - 1 + l; }
+        int di, dj;
+        if (s.face == 1) { di = s.ist - LAP - 1 + l; dj = s.jst + k - 1; }
+        else if (s.face == 2) { di = s.ist + k - 1; dj = s.jst - LAP - 1 + l; }
+        else if (s.face == 3) { di = s.iend + l - 1; dj = s.jst + k - 1; }
+        else { di = s.ist + k - 1; dj = s.jend + l - 1; }
+        long long src = fidx(nb, si, sj), dst = fidx(b, di, dj);
+        for (int m = 0; m < L.nvar; m++) L.U[m * F + dst] = L.U[m * F + src];
+      }
+    }
+    __syncthreads();
+  }
+  if (phases & 4) {
+    int nx = b.nx, ny = b.ny;
+    if (threadIdx.x == 0) corner(L, c, fidx(b, 1, 0), fidx(b, 1, 1), fidx(b, 0, 1), fidx(b, 0, 0));
+    if (threadIdx.x == 32) corner(L, c, fidx(b, 1, ny), fidx(b, 1, ny - 1), fidx(b, 0, ny - 1), fidx(b, 0, ny));
+    if (threadIdx.x == 64) corner(L, c, fidx(b, nx - 1, 0), fidx(b, nx - 1, 1), fidx(b, nx, 1), fidx(b, nx, 0));
+    if (threadIdx.x == 96) corner(L, c, fidx(b, nx - 1, ny), fidx(b, nx - 1, ny - 1), fidx(b, nx, ny - 1), fidx(b, nx, ny));
+    __syncthreads();
+  }
+  if ((phases & 8) && L.nvar >= 5) {
+    int nc = (b.nx - 1) * (b.ny - 1);
+    for (int t = threadIdx.x; t < nc; t += blockDim.x) {
+      int i = t % (b.nx - 1) + 1, j = t / (b.nx - 1) + 1;
+      long long id = fidx(b, i, j);
+      for (int m = 4; m < L.nvar; m++)
+        if (L.U[m * F + id] < 0) L.U[m * F + id] = 1.0e-10;
+    }
+  }
+}
+
+void launch_bc(const Lvl &L, int phases, cudaStream_t s) { k_bc<<<L.nblk, 256, 0, s>>>(L, phases); }
+
+}  // namespace ec2d

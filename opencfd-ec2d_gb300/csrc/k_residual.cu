@@ -1,0 +1,301 @@
+// k_residual.cu -- the residual of sub_Residual.f90 on the GPU.
+//
+// One residual evaluation of a mesh level (Comput_Residual_one_mesh,
+// sub_Residual.f90:13-107) is a chain of launches over all blocks of all cases:
+//   k_prim      primitives d,u,v,T,p (+c, Sutherland mu)       comput_duvtpckw + get_viscous
+//   k_flux_i/j  reconstruction + Riemann flux + viscous stress  Residual_FVM face loops
+//   k_res       flux differences, spectral radii, time step    Residual_FVM:460-468, comput_Lvc, comput_dt
+//   k_norm_*    max / RMS residual norms, deterministic order  sub_Residual.f90:72-106
+// Work is distributed by 256-item tiles of each block's extended index range
+// [-1,nx+1] x [-1,ny+1]; a kernel maps the tile item to (i,j) and keeps the
+// items that lie in its own index range.
+#include "ec2d_dev.cuh"
+#include "ec2d_internal.h"
+
+namespace ec2d {
+
+constexpr int TILE = 256;
+
+__device__ __forceinline__ bool tile_ij(const Lvl &L, int &bk, int &i, int &j) {
+  int2 t = L.tiles[blockIdx.x];
+  bk = t.x;
+  const BlkDev &b = L.blk[bk];
+  int W = b.nx + 3, H = b.ny + 3;
+  int lin = t.y + threadIdx.x;
+  if (lin >= W * H) return false;
+  i = lin % W - 1;
+  j = lin / W - 1;
+  return true;
+}
+
+// comput_duvtpckw (sub_Residual.f90:114-152) + get_viscous (:670-689) + Amu_t=0 (:172)
+__global__ void __launch_bounds__(TILE) k_prim(Lvl L) {
+  int bk, i, j;
+  if (!tile_ij(L, bk, i, j)) return;
+  const BlkDev &b = L.blk[bk];
+  const CaseDev &c = L.cs[b.cas];
+  long long id = fidx(b, i, j);
+  const long long F = L.F;
+  double d = L.U[id], ru = L.U[F + id], rv = L.U[2 * F + id], E = L.U[3 * F + id];
+  double uu = ru / d, v = rv / d;
+  double T = (E - 0.5 * d * (uu * uu + v * v)) / (c.Cv * d);
+  double p = c.p00 * d * T;
+  L.q[Q_D * F + id] = d;
+  L.q[Q_U * F + id] = uu;
+  L.q[Q_V * F + id] = v;
+  L.q[Q_T * F + id] = T;
+  L.q[Q_P * F + id] = p;
+  bool interior = (i >= 1 && i <= b.nx - 1 && j >= 1 && j <= b.ny - 1);
+  if (interior) {
+    if (!(T >= 1.0e-5)) set_status(L.status + 4 * b.cas, 3, bk, i, j);
+    L.q[Q_C * F + id] = sqrt(T) / c.Ma;
+  }
+  if (L.visc) {
+    if (i >= 0 && i <= b.nx && j >= 0 && j <= b.ny)
+      L.amu[id] = 1.0 / c.Re * (1.0 + c.Tsb) * sqrt(T * T * T) / (c.Tsb + T);
+    L.amut[id] = 0.0;
+  }
+}
+
+__device__ __forceinline__ bool in_fdm_core(const BlkDev &b, int i, int j) {
+  return b.fdm && (i >= LFDM + 2 && i <= b.nx - LFDM - 1) && (j >= LFDM + 2 && j <= b.ny - LFDM - 1);
+}
+
+// i-direction face loop of Residual_FVM (sub_Residual.f90:238-346): face (i,j),
+// i=1..nx, j=1..ny-1, between cells (i-1,j) and (i,j).
+__global__ void __launch_bounds__(TILE) k_flux_i(Lvl L) {
+  int bk, i, j;
+  if (!tile_ij(L, bk, i, j)) return;
+  const BlkDev &b = L.blk[bk];
+  if (i < 1 || i > b.nx || j < 1 || j > b.ny - 1) return;
+  if (in_fdm_core(b, i, j)) return;
+  const CaseDev &c = L.cs[b.cas];
+  const long long F = L.F;
+  long long id = fidx(b, i, j);
+  double si = L.geo[G_SI * F + id], n1 = L.geo[G_NI1 * F + id], n2 = L.geo[G_NI2 * F + id];
+  double S0[4][4], UL[4], UR[4];
+  if (L.recon == Recon_Original) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      long long s = id + (k - 2);
+      S0[k][0] = L.q[Q_D * F + s]; S0[k][1] = L.q[Q_U * F + s];
+      S0[k][2] = L.q[Q_V * F + s]; S0[k][3] = L.q[Q_P * F + s];
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+#pragma unroll
+      for (int m = 0; m < 4; m++) S0[k][m] = L.U[m * F + id + (k - 2)];
+  }
+  reconstruct(L.recon, L.scheme, S0, c.gamma, UL, UR);
+  double QL[4] = {UL[0], UL[1] * n1 + UL[2] * n2, -UL[1] * n2 + UL[2] * n1, UL[3]};
+  double QR[4] = {UR[0], UR[1] * n1 + UR[2] * n2, -UR[1] * n2 + UR[2] * n1, UR[3]};
+  double Fl[4];
+  face_flux(L.flux, QL, QR, Fl, c.gamma);
+  double F0 = -Fl[0] * si, F1 = -(Fl[1] * n1 - Fl[2] * n2) * si, F2 = -(Fl[1] * n2 + Fl[2] * n1) * si, F3 = -Fl[3] * si;
+  if (L.visc) {
+    long long w = id - 1, nN = id + b.P, nS = id - b.P;
+    double Amu1, Amk1;
+    if (i == 1) {
+      Amu1 = L.amu[id] + L.amut[id];
+      Amk1 = c.Cp * (L.amu[id] / c.Pr + L.amut[id] / PrT);
+    } else if (i == b.nx) {
+      Amu1 = L.amu[w] + L.amut[w];
+      Amk1 = c.Cp * (L.amu[w] / c.Pr + L.amut[w] / PrT);
+    } else {
+      Amu1 = (L.amu[w] + L.amu[id] + L.amut[w] + L.amut[id]) * 0.5;
+      Amk1 = c.Cp * ((L.amu[w] + L.amu[id]) / c.Pr + (L.amut[w] + L.amut[id]) / PrT) * 0.5;
+    }
+    const double *x1 = L.geo + G_X1 * F, *y1 = L.geo + G_Y1 * F;
+    const double *uu = L.q + Q_U * F, *vv = L.q + Q_V * F, *TT = L.q + Q_T * F;
+    double Dix = x1[id] - x1[w], Diy = y1[id] - y1[w];
+    double Djx = (x1[nN - 1] + x1[nN] - x1[nS - 1] - x1[nS]) * 0.25;
+    double Djy = (y1[nN - 1] + y1[nN] - y1[nS - 1] - y1[nS]) * 0.25;
+    double Diu = uu[id] - uu[w], Div = vv[id] - vv[w], DiT = TT[id] - TT[w];
+    double Dju = (uu[nN - 1] + uu[nN] - uu[nS - 1] - uu[nS]) * 0.25;
+    double Djv = (vv[nN - 1] + vv[nN] - vv[nS - 1] - vv[nS]) * 0.25;
+    double DjT = (TT[nN - 1] + TT[nN] - TT[nS - 1] - TT[nS]) * 0.25;
+    double u1 = (uu[id] + uu[w]) * 0.5, v1 = (vv[id] + vv[w]) * 0.5;
+    viscous_face(Dix, Diy, Djx, Djy, Diu, Div, DiT, Dju, Djv, DjT, Amu1, Amk1, u1, v1, n1, n2, si, F1, F2, F3);
+  }
+  L.fi[id] = F0; L.fi[F + id] = F1; L.fi[2 * F + id] = F2; L.fi[3 * F + id] = F3;
+}
+
+// j-direction face loop of Residual_FVM (sub_Residual.f90:352-455): face (i,j),
+// i=1..nx-1, j=1..ny, between cells (i,j-1) and (i,j).
+__global__ void __launch_bounds__(TILE) k_flux_j(Lvl L) {
+  int bk, i, j;
+  if (!tile_ij(L, bk, i, j)) return;
+  const BlkDev &b = L.blk[bk];
+  if (i < 1 || i > b.nx - 1 || j < 1 || j > b.ny) return;
+  if (in_fdm_core(b, i, j)) return;
+  const CaseDev &c = L.cs[b.cas];
+  const long long F = L.F;
+  const long long P = b.P;
+  long long id = fidx(b, i, j);
+  double sj = L.geo[G_SJ * F + id], n1 = L.geo[G_NJ1 * F + id], n2 = L.geo[G_NJ2 * F + id];
+  double S0[4][4], UL[4], UR[4];
+  int scheme = L.scheme;
+  if (L.recon == Recon_Original) {
+    scheme = L.gscheme;  // the reference passes the global Iflag_Scheme here (sub_Residual.f90:367)
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      long long s = id + (k - 2) * P;
+      S0[k][0] = L.q[Q_D * F + s]; S0[k][1] = L.q[Q_U * F + s];
+      S0[k][2] = L.q[Q_V * F + s]; S0[k][3] = L.q[Q_P * F + s];
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+#pragma unroll
+      for (int m = 0; m < 4; m++) S0[k][m] = L.U[m * F + id + (k - 2) * P];
+  }
+  reconstruct(L.recon, scheme, S0, c.gamma, UL, UR);
+  double QL[4] = {UL[0], UL[1] * n1 + UL[2] * n2, -UL[1] * n2 + UL[2] * n1, UL[3]};
+  double QR[4] = {UR[0], UR[1] * n1 + UR[2] * n2, -UR[1] * n2 + UR[2] * n1, UR[3]};
+  double Fl[4];
+  face_flux(L.flux, QL, QR, Fl, c.gamma);
+  double F0 = -Fl[0] * sj, F1 = -(Fl[1] * n1 - Fl[2] * n2) * sj, F2 = -(Fl[1] * n2 + Fl[2] * n1) * sj, F3 = -Fl[3] * sj;
+  if (L.visc) {
+    long long s = id - P;
+    double Amu1, Amk1;
+    if (j == 1) {
+      Amu1 = L.amu[id] + L.amut[id];
+      Amk1 = c.Cp * (L.amu[id] / c.Pr + L.amut[id] / PrT);
+    } else if (j == b.ny) {
+      Amu1 = L.amu[s] + L.amut[s];
+      Amk1 = c.Cp * (L.amu[s] / c.Pr + L.amut[s] / PrT);
+    } else {
+      Amu1 = (L.amu[id] + L.amu[s] + L.amut[id] + L.amut[s]) * 0.5;
+      Amk1 = c.Cp * ((L.amu[s] + L.amu[id]) / c.Pr + (L.amut[s] + L.amut[id]) / PrT) * 0.5;
+    }
+    const double *x1 = L.geo + G_X1 * F, *y1 = L.geo + G_Y1 * F;
+    const double *uu = L.q + Q_U * F, *vv = L.q + Q_V * F, *TT = L.q + Q_T * F;
+    double Dix = (x1[s + 1] + x1[id + 1] - x1[s - 1] - x1[id - 1]) * 0.25;
+    double Diy = (y1[s + 1] + y1[id + 1] - y1[s - 1] - y1[id - 1]) * 0.25;
+    double Djx = x1[id] - x1[s], Djy = y1[id] - y1[s];
+    double Diu = (uu[s + 1] + uu[id + 1] - uu[s - 1] - uu[id - 1]) * 0.25;
+    double Div = (vv[s + 1] + vv[id + 1] - vv[s - 1] - vv[id - 1]) * 0.25;
+    double DiT = (TT[s + 1] + TT[id + 1] - TT[s - 1] - TT[id - 1]) * 0.25;
+    double Dju = uu[id] - uu[s], Djv = vv[id] - vv[s], DjT = TT[id] - TT[s];
+    double u1 = (uu[id] + uu[s]) * 0.5, v1 = (vv[id] + vv[s]) * 0.5;
+    viscous_face(Dix, Diy, Djx, Djy, Diu, Div, DiT, Dju, Djv, DjT, Amu1, Amk1, u1, v1, n1, n2, sj, F1, F2, F3);
+  }
+  L.fj[id] = F0; L.fj[F + id] = F1; L.fj[2 * F + id] = F2; L.fj[3 * F + id] = F3;
+}
+
+// flux differences (sub_Residual.f90:460-468), comput_Lvc (sub_NS_singlegrid.f90:352-388)
+// and comput_dt (sub_NS_singlegrid.f90:324-348) for interior cells
+__global__ void __launch_bounds__(TILE) k_res(Lvl L) {
+  int bk, i, j;
+  if (!tile_ij(L, bk, i, j)) return;
+  const BlkDev &b = L.blk[bk];
+  if (i < 1 || i > b.nx - 1 || j < 1 || j > b.ny - 1) return;
+  const CaseDev &c = L.cs[b.cas];
+  const long long F = L.F, P = b.P;
+  long long id = fidx(b, i, j);
+  bool fdm = b.fdm && (i >= LFDM + 1 && i <= b.nx - LFDM - 1) && (j >= LFDM + 1 && j <= b.ny - LFDM - 1);
+  if (!fdm) {
+#pragma unroll
+    for (int m = 0; m < 4; m++)
+      L.res[m * F + id] = L.fi[m * F + id + 1] - L.fi[m * F + id] + L.fj[m * F + id + P] - L.fj[m * F + id];
+  }
+  const double *g = L.geo;
+  double s0 = g[G_VOL * F + id];
+  double si = 0.5 * (g[G_SI * F + id] + g[G_SI * F + id + 1]);
+  double ni1 = 0.5 * (g[G_NI1 * F + id] + g[G_NI1 * F + id + 1]);
+  double ni2 = 0.5 * (g[G_NI2 * F + id] + g[G_NI2 * F + id + 1]);
+  double sj = 0.5 * (g[G_SJ * F + id] + g[G_SJ * F + id + P]);
+  double nj1 = 0.5 * (g[G_NJ1 * F + id] + g[G_NJ1 * F + id + P]);
+  double nj2 = 0.5 * (g[G_NJ2 * F + id] + g[G_NJ2 * F + id + P]);
+  double uu = L.q[Q_U * F + id], vv = L.q[Q_V * F + id], cc = L.q[Q_C * F + id], d = L.q[Q_D * F + id];
+  double uni = uu * ni1 + vv * ni2, unj = uu * nj1 + vv * nj2;
+  double Lci = (fabs(uni) + cc) * si, Lcj = (fabs(unj) + cc) * sj;
+  double amu = L.visc ? L.amu[id] : 0.0, amut = L.visc ? L.amut[id] : 0.0;
+  double tmp1 = c.gamma / d * (amu / c.Pr + amut / PrT);
+  double Lvi = tmp1 * si * si / s0, Lvj = tmp1 * sj * sj / s0;
+  L.lc[L_CI * F + id] = Lci;
+  L.lc[L_CJ * F + id] = Lcj;
+  L.lc[L_VI * F + id] = Lvi;
+  L.lc[L_VJ * F + id] = Lvj;
+  double dt;
+  if (c.local_dt == 0) dt = c.dt_global;
+  else {
+    dt = c.CFL * s0 / (Lci + Lcj + 1.0 * (Lvi + Lvj));
+    if (dt > c.dtmax) dt = c.dtmax;
+    if (dt < c.dtmin) dt = c.dtmin;
+  }
+  L.lc[L_DT * F + id] = dt;
+}
+
+// per-tile partial norms of Res (max |Res| and sum Res^2 per variable)
+__global__ void __launch_bounds__(TILE) k_norm_partial(Lvl L) {
+  __shared__ double smax[6][TILE / 32], ssum[6][TILE / 32];
+  int bk, i, j;
+  double vmax[6] = {0, 0, 0, 0, 0, 0}, vsum[6] = {0, 0, 0, 0, 0, 0};
+  if (tile_ij(L, bk, i, j)) {
+    const BlkDev &b = L.blk[bk];
+    if (i >= 1 && i <= b.nx - 1 && j >= 1 && j <= b.ny - 1) {
+      long long id = fidx(b, i, j);
+      for (int m = 0; m < L.nvar; m++) {
+        double r = L.res[m * L.F + id];
+        vmax[m] = fabs(r);
+        vsum[m] = r * r;
+      }
+    }
+  }
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int m = 0; m < 6; m++) {
+    double a = vmax[m], s = vsum[m];
+    for (int o = 16; o > 0; o >>= 1) {
+      a = fmax(a, __shfl_down_sync(0xffffffffu, a, o));
+      s += __shfl_down_sync(0xffffffffu, s, o);
+    }
+    if (lane == 0) { smax[m][w] = a; ssum[m][w] = s; }
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    int m = threadIdx.x;
+    double a = 0.0, s = 0.0;
+    for (int k = 0; k < TILE / 32; k++) { a = fmax(a, smax[m][k]); s += ssum[m][k]; }
+    L.npart[(size_t)blockIdx.x * 12 + m] = a;
+    L.npart[(size_t)blockIdx.x * 12 + 6 + m] = s;
+  }
+}
+
+// per-case reduction of the tile partials in a fixed order
+__global__ void k_norm_final(Lvl L, const int *case_tile0, const int *case_ntile, const int *case_ncell) {
+  int cs = blockIdx.x;
+  int t0 = case_tile0[cs], nt = case_ntile[cs];
+  __shared__ double sm[12][32];
+  int m = threadIdx.y;  // 0..11
+  int lane = threadIdx.x;  // 0..31
+  double acc = 0.0;
+  for (int t = lane; t < nt; t += 32) {
+    double v = L.npart[(size_t)(t0 + t) * 12 + m];
+    acc = (m < 6) ? fmax(acc, v) : acc + v;
+  }
+  sm[m][lane] = acc;
+  __syncthreads();
+  if (lane == 0) {
+    double a = 0.0;
+    for (int k = 0; k < 32; k++) a = (m < 6) ? fmax(a, sm[m][k]) : a + sm[m][k];
+    if (m >= 6) a = (m - 6 < L.nvar) ? sqrt(a / (1.0 * case_ncell[cs])) : 0.0;
+    L.norms[cs * 12 + m] = a;
+  }
+}
+
+void launch_prim(const Lvl &L, cudaStream_t s) { k_prim<<<L.ntiles, TILE, 0, s>>>(L); }
+void launch_flux(const Lvl &L, cudaStream_t s) {
+  k_flux_i<<<L.ntiles, TILE, 0, s>>>(L);
+  k_flux_j<<<L.ntiles, TILE, 0, s>>>(L);
+}
+void launch_res(const Lvl &L, cudaStream_t s) { k_res<<<L.ntiles, TILE, 0, s>>>(L); }
+void launch_norms(const Lvl &L, const int *case_tile0, const int *case_ntile, const int *case_ncell,
+                  cudaStream_t s) {
+  k_norm_partial<<<L.ntiles, TILE, 0, s>>>(L);
+  k_norm_final<<<L.ncase, dim3(32, 12), 0, s>>>(L, case_tile0, case_ntile, case_ncell);
+}
+
+}  // namespace ec2d

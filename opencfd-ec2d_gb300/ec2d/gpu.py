@@ -1,0 +1,260 @@
+"""ctypes binding of libec2d_gpu.so (the C-ABI declared in include/ec2d_gpu.h).
+
+This is the same binding a Python host of the Fortran code's logic would use;
+it adds nothing to the computation.  There is no CPU fallback: if the library
+cannot be loaded, or no CUDA device is present, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+LIB = os.path.join(PKG, "lib", "libec2d_gpu.so")
+
+F_RES, F_DT, F_LCI, F_LCJ, F_LVI, F_LVJ, F_DU, F_AMU, F_AMUT, F_X1, F_Y1, F_VOL = range(12)
+F_SI, F_SJ, F_NI1, F_NI2, F_NJ1, F_NJ2, F_DW, F_QF, F_DELTU, F_UN, F_X, F_Y = range(12, 24)
+
+ERRORS = {1: "invalid argument or call order", 2: "CUDA error", 3: "non-physical state (T < 1e-5)",
+          4: "device wait timed out", 5: "option combination not supported", 6: "out of device memory"}
+
+
+class EC2DError(RuntimeError):
+    def __init__(self, code, what):
+        super().__init__(f"{what}: {ERRORS.get(code, code)} (code {code})")
+        self.code = code
+
+
+class Params(ctypes.Structure):
+    """ec2d_params of include/ec2d_gpu.h (field order matters)."""
+    _fields_ = [
+        ("Ma", ctypes.c_double), ("Re", ctypes.c_double), ("gamma", ctypes.c_double),
+        ("AoA", ctypes.c_double), ("Pr", ctypes.c_double), ("t_end", ctypes.c_double),
+        ("Kstep_save", ctypes.c_int), ("If_viscous", ctypes.c_int),
+        ("Iflag_turbulence_model", ctypes.c_int), ("Iflag_init", ctypes.c_int),
+        ("Iflag_local_dt", ctypes.c_int),
+        ("dt_global", ctypes.c_double), ("CFL", ctypes.c_double), ("dtmax", ctypes.c_double),
+        ("dtmin", ctypes.c_double),
+        ("Time_Method", ctypes.c_int),
+        ("P_outlet", ctypes.c_double), ("T_inf", ctypes.c_double), ("Twall", ctypes.c_double),
+        ("vt_inf", ctypes.c_double), ("Kt_inf", ctypes.c_double), ("Wt_inf", ctypes.c_double),
+        ("Iflag_Scheme", ctypes.c_int), ("Iflag_flux", ctypes.c_int),
+        ("IFlag_Reconstruction", ctypes.c_int), ("Kstep_show", ctypes.c_int),
+        ("Num_Mesh", ctypes.c_int), ("Num_Threads", ctypes.c_int), ("Nstep_Inner_Limit", ctypes.c_int),
+        ("Res_Inner_Limit", ctypes.c_double),
+        ("Pre_Step_Mesh", ctypes.c_int * 3),
+        ("xaxis", ctypes.c_double), ("yaxis", ctypes.c_double),
+        ("mg_lusgs", ctypes.c_int),
+    ]
+
+    @classmethod
+    def from_params(cls, p):
+        s = cls()
+        for name, _ in cls._fields_:
+            v = getattr(p, name)
+            if name == "Pre_Step_Mesh":
+                s.Pre_Step_Mesh = (ctypes.c_int * 3)(*[int(t) for t in (list(v) + [0, 0, 0])[:3]])
+            else:
+                setattr(s, name, v)
+        return s
+
+
+_lib = None
+
+
+def lib():
+    """Load libec2d_gpu.so (built by build.py); raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB):
+        raise OSError(f"{LIB} not built; run ec2d_build.py")
+    L = ctypes.CDLL(LIB)
+    vp, ip, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
+    cpp = ctypes.POINTER(ctypes.c_void_p)
+    sig = {
+        "ec2d_version": ([], ctypes.c_int),
+        "ec2d_error_string": ([ctypes.c_int], ctypes.c_char_p),
+        "ec2d_create": ([ctypes.c_int, cpp], ctypes.c_int),
+        "ec2d_destroy": ([vp], None),
+        "ec2d_add_case": ([vp, ctypes.POINTER(Params), ip], ctypes.c_int),
+        "ec2d_add_block": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, ctypes.c_int, ip], ctypes.c_int),
+        "ec2d_set_fdm_block": ([vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "ec2d_set_wall_distance": ([vp, ctypes.c_int, ctypes.c_int, dp], ctypes.c_int),
+        "ec2d_setup": ([vp], ctypes.c_int),
+        "ec2d_num_mesh": ([vp, ip], ctypes.c_int),
+        "ec2d_block_dims": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ip, ip, ip], ctypes.c_int),
+        "ec2d_init_flow": ([vp], ctypes.c_int),
+        "ec2d_upload_U": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp], ctypes.c_int),
+        "ec2d_download_U": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp], ctypes.c_int),
+        "ec2d_step": ([vp, ctypes.c_int], ctypes.c_int),
+        "ec2d_residual": ([vp, ctypes.c_int, ctypes.c_int, dp, dp, ip, dp], ctypes.c_int),
+        "ec2d_status": ([vp, ctypes.c_int, ip, ip, ip, ip], ctypes.c_int),
+        "ec2d_forces": ([vp, ctypes.c_int, dp, dp, dp], ctypes.c_int),
+        "ec2d_wall_cf": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, ctypes.c_int, ip], ctypes.c_int),
+        "ec2d_get_field": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp], ctypes.c_int),
+        "ec2d_field_size": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ip], ctypes.c_int),
+        "ec2d_set_field": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp], ctypes.c_int),
+        "ec2d_comput_residual": ([vp, ctypes.c_int], ctypes.c_int),
+        "ec2d_boundary_condition": ([vp, ctypes.c_int], ctypes.c_int),
+        "ec2d_update_buffer": ([vp, ctypes.c_int], ctypes.c_int),
+        "ec2d_du_lusgs": ([vp, ctypes.c_int, ctypes.c_double], ctypes.c_int),
+        "ec2d_time_advance": ([vp, ctypes.c_int], ctypes.c_int),
+        "ec2d_interpolation2h": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "ec2d_prolong": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "ec2d_force_function": ([vp, ctypes.c_int], ctypes.c_int),
+        "ec2d_sync": ([vp], ctypes.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ck(r, what):
+    if r:
+        raise EC2DError(r, what)
+
+
+class Solver:
+    """A context of one or more cases sharing the method flags (a batch)."""
+
+    def __init__(self, cases, device=0, fdm_blocks=None, dw=None):
+        """cases: list of (Params, [Block, ...]); fdm_blocks: per case list of
+        1-based block ids; dw: per case list of per-block wall distances."""
+        self.L = lib()
+        h = ctypes.c_void_p()
+        _ck(self.L.ec2d_create(device, ctypes.byref(h)), "ec2d_create")
+        self.h = h
+        self.ncase = len(cases)
+        self.params = [c[0] for c in cases]
+        self.nblocks = [len(c[1]) for c in cases]
+        for ci, (p, blocks) in enumerate(cases):
+            sp = Params.from_params(p)
+            cid = ctypes.c_int()
+            _ck(self.L.ec2d_add_case(self.h, ctypes.byref(sp), ctypes.byref(cid)), "ec2d_add_case")
+            for b in blocks:
+                x = np.asfortranarray(b.x, dtype=np.float64)
+                y = np.asfortranarray(b.y, dtype=np.float64)
+                bc = np.ascontiguousarray(np.array(b.bc, dtype=np.int32).reshape(-1))
+                _ck(self.L.ec2d_add_block(self.h, cid.value, b.nx, b.ny, _dp(x), _dp(y), len(b.bc),
+                                          bc.ctypes.data_as(ctypes.POINTER(ctypes.c_int))), "ec2d_add_block")
+            if fdm_blocks is not None:
+                for k in fdm_blocks[ci]:
+                    _ck(self.L.ec2d_set_fdm_block(self.h, cid.value, int(k)), "ec2d_set_fdm_block")
+            if dw is not None and dw[ci] is not None:
+                for k, d in enumerate(dw[ci]):
+                    d = np.asfortranarray(d, dtype=np.float64)
+                    _ck(self.L.ec2d_set_wall_distance(self.h, cid.value, k + 1, _dp(d)), "ec2d_set_wall_distance")
+        _ck(self.L.ec2d_setup(self.h), "ec2d_setup")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ec2d_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def num_mesh(self):
+        n = ctypes.c_int()
+        _ck(self.L.ec2d_num_mesh(self.h, ctypes.byref(n)), "ec2d_num_mesh")
+        return n.value
+
+    def dims(self, case, mesh, block):
+        nx, ny, nv = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _ck(self.L.ec2d_block_dims(self.h, case, mesh, block, ctypes.byref(nx), ctypes.byref(ny), ctypes.byref(nv)),
+            "ec2d_block_dims")
+        return nx.value, ny.value, nv.value
+
+    def init_flow(self):
+        _ck(self.L.ec2d_init_flow(self.h), "ec2d_init_flow")
+
+    def upload_U(self, case, mesh, block, U):
+        U = np.asfortranarray(U, dtype=np.float64)
+        _ck(self.L.ec2d_upload_U(self.h, case, mesh, block, _dp(U)), "ec2d_upload_U")
+
+    def download_U(self, case, mesh, block, out=None):
+        nx, ny, nv = self.dims(case, mesh, block)
+        U = out if out is not None else np.zeros((nv, nx + 3, ny + 3), order="F")
+        _ck(self.L.ec2d_download_U(self.h, case, mesh, block, _dp(U)), "ec2d_download_U")
+        return U
+
+    def step(self, n=1):
+        _ck(self.L.ec2d_step(self.h, n), "ec2d_step")
+
+    def norms(self, case=1, mesh=1):
+        a = np.zeros(6); b = np.zeros(6)
+        k = ctypes.c_int(); t = ctypes.c_double()
+        _ck(self.L.ec2d_residual(self.h, case, mesh, _dp(a), _dp(b), ctypes.byref(k), ctypes.byref(t)),
+            "ec2d_residual")
+        return a, b, k.value, t.value
+
+    def status(self, case=1):
+        c, b, i, j = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _ck(self.L.ec2d_status(self.h, case, ctypes.byref(c), ctypes.byref(b), ctypes.byref(i), ctypes.byref(j)),
+            "ec2d_status")
+        return c.value, b.value, i.value, j.value
+
+    def forces(self, case=1):
+        cl, cd, cm = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _ck(self.L.ec2d_forces(self.h, case, ctypes.byref(cl), ctypes.byref(cd), ctypes.byref(cm)), "ec2d_forces")
+        return cl.value, cd.value, cm.value
+
+    def wall_cf(self, case, block, sub, maxn=8192):
+        cf = np.zeros(maxn); xc = np.zeros(maxn); n = ctypes.c_int()
+        _ck(self.L.ec2d_wall_cf(self.h, case, block, sub, _dp(cf), _dp(xc), maxn, ctypes.byref(n)), "ec2d_wall_cf")
+        return cf[:n.value], xc[:n.value]
+
+    def field(self, case, mesh, block, fid, shape=None):
+        n = ctypes.c_int()
+        _ck(self.L.ec2d_field_size(self.h, case, mesh, block, fid, ctypes.byref(n)), "ec2d_field_size")
+        out = np.zeros(n.value)
+        _ck(self.L.ec2d_get_field(self.h, case, mesh, block, fid, _dp(out)), "ec2d_get_field")
+        if shape is not None:
+            out = out.reshape(shape, order="F")
+        return out
+
+    def set_field(self, case, mesh, block, fid, arr):
+        a = np.asfortranarray(arr, dtype=np.float64).reshape(-1, order="F").copy()
+        _ck(self.L.ec2d_set_field(self.h, case, mesh, block, fid, _dp(a)), "ec2d_set_field")
+
+    def residual(self, mesh=1):
+        _ck(self.L.ec2d_comput_residual(self.h, mesh), "ec2d_comput_residual")
+
+    def bc(self, mesh=1):
+        _ck(self.L.ec2d_boundary_condition(self.h, mesh), "ec2d_boundary_condition")
+
+    def halo(self, mesh=1):
+        _ck(self.L.ec2d_update_buffer(self.h, mesh), "ec2d_update_buffer")
+
+    def lusgs(self, mesh=1, alfa1=0.0):
+        _ck(self.L.ec2d_du_lusgs(self.h, mesh, alfa1), "ec2d_du_lusgs")
+
+    def time_advance(self, mesh=1):
+        _ck(self.L.ec2d_time_advance(self.h, mesh), "ec2d_time_advance")
+
+    def interpolation2h(self, m1, m2, flag):
+        _ck(self.L.ec2d_interpolation2h(self.h, m1, m2, flag), "ec2d_interpolation2h")
+
+    def prolong(self, m1, m2, flag):
+        _ck(self.L.ec2d_prolong(self.h, m1, m2, flag), "ec2d_prolong")
+
+    def force_function(self, mesh):
+        _ck(self.L.ec2d_force_function(self.h, mesh), "ec2d_force_function")
+
+    def sync(self):
+        _ck(self.L.ec2d_sync(self.h), "ec2d_sync")

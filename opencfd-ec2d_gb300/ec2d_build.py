@@ -1,0 +1,65 @@
+"""Build libec2d_gpu.so (sm_103a) in-tree: one nvcc process per translation
+unit, in parallel, then a shared-library link.  Usage: python ec2d_build.py [-v]"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "lib", "libec2d_gpu.so")
+SOURCES = ["ec2d_api.cu", "k_residual.cu", "k_turb.cu", "k_bc.cu", "k_lusgs.cu", "k_misc.cu"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+
+
+def nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _stale(obj: str, deps) -> bool:
+    if not os.path.exists(obj):
+        return True
+    t = os.path.getmtime(obj)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(verbose: bool = False, extra=()) -> str:
+    os.makedirs(OUT, exist_ok=True)
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    headers = [os.path.join(SRC, h) for h in os.listdir(SRC) if h.endswith((".h", ".cuh"))]
+    headers.append(os.path.join(HERE, "..", "include", "ec2d_gpu.h"))
+    srcs = [s for s in SOURCES if os.path.exists(os.path.join(SRC, s))]
+    objs, jobs = [], []
+    for s in srcs:
+        src = os.path.join(SRC, s)
+        obj = os.path.join(OUT, s.replace(".cu", ".o"))
+        objs.append(obj)
+        if _stale(obj, [src] + headers):
+            jobs.append([nvcc(), *ARCH, *FLAGS, *extra, "-c", src, "-o", obj])
+
+    def run(cmd):
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        if verbose and (r.stdout or r.stderr):
+            print(r.stdout, r.stderr, flush=True)
+
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
+        list(ex.map(run, jobs))
+    if jobs or not os.path.exists(LIB):
+        run([nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

@@ -1,0 +1,198 @@
+"""GPU parity: the CUDA path (through the C-ABI) against the CPU oracle on
+the same seeded inputs.
+
+Tolerances (FP64): one residual evaluation matches per cell within 1e-12
+relative to the larger of |Res| and the cell's face-flux scale; pointwise
+fields (primitives, spectral radii, dt, ghost cells, dU) within 1e-12
+relative; multi-step states within the bounds stated per test."""
+import numpy as np
+import pytest
+
+from helpers import (compare_U, compare_fields, compare_residual, copy_state, make_gpu, make_oracle,
+                     perturb_state, small_case)
+
+pytestmark = pytest.mark.gpu
+
+GEOM = [9, 10, 11, 12, 13, 14, 15, 16, 17, 22, 23]  # x1 y1 vol si sj ni1 ni2 nj1 nj2 x y
+
+
+def _pair(p, blocks, fdm=(), steps=0, perturb=True, seed=1):
+    orc = make_oracle(p, blocks, fdm=fdm)
+    orc.init_flow()
+    if steps:
+        orc.step(steps)
+    if perturb:
+        perturb_state(orc, seed=seed)
+    g = make_gpu(p, blocks, fdm=fdm)
+    g.init_flow()
+    copy_state(orc, g)
+    return orc, g
+
+
+def test_geometry_all_levels(gpu_lib):
+    p, bl = small_case(nx=65, ny=17, nblocks=2, Num_Mesh=3, Time_Method=1)
+    orc = make_oracle(p, bl)
+    g = make_gpu(p, bl)
+    assert g.num_mesh == orc.num_mesh == 3
+    for mesh in (1, 2, 3):
+        compare_fields(orc, g, GEOM, mesh=mesh, tol=1e-13)
+
+
+@pytest.mark.parametrize("flux", [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("recon", [0, 1, 2])
+def test_residual_inviscid(gpu_lib, flux, recon):
+    p, bl = small_case(Ma=0.7, AoA=2.0, Iflag_flux=flux, IFlag_Reconstruction=recon, Iflag_Scheme=5)
+    orc, g = _pair(p, bl, steps=5)
+    orc.residual(); g.residual()
+    compare_residual(orc, g)
+    compare_fields(orc, g, [1, 2, 3, 4, 5])
+
+
+@pytest.mark.parametrize("scheme", [0, 1, 2, 3, 4, 5, 6])
+def test_residual_schemes(gpu_lib, scheme):
+    p, bl = small_case(Ma=0.6, AoA=1.0, Iflag_flux=4, IFlag_Reconstruction=0, Iflag_Scheme=scheme)
+    orc, g = _pair(p, bl, steps=3)
+    orc.residual(); g.residual()
+    compare_residual(orc, g)
+
+
+@pytest.mark.parametrize("recon", [0, 2])
+def test_residual_viscous(gpu_lib, recon):
+    p, bl = small_case(Ma=0.5, AoA=3.0, Re=5.0e3, If_viscous=1, Iflag_flux=6, IFlag_Reconstruction=recon,
+                       Iflag_Scheme=5, nblocks=2)
+    orc, g = _pair(p, bl, steps=5)
+    orc.residual(); g.residual()
+    compare_residual(orc, g)
+    compare_fields(orc, g, [1, 2, 3, 4, 5, 7])
+
+
+def test_residual_sa(gpu_lib):
+    p, bl = small_case(Ma=0.6, AoA=2.0, Re=1.0e6, If_viscous=1, Iflag_turbulence_model=2, Iflag_flux=4,
+                       Iflag_Scheme=5, first=2e-4)
+    orc, g = _pair(p, bl, steps=5)
+    compare_fields(orc, g, [18], tol=1e-13)  # wall distance
+    orc.residual(); g.residual()
+    compare_residual(orc, g)
+    compare_fields(orc, g, [1, 2, 3, 4, 5, 7, 8])
+
+
+def test_residual_sst(gpu_lib):
+    p, bl = small_case(Ma=0.6, AoA=2.0, Re=1.0e6, If_viscous=1, Iflag_turbulence_model=3, Iflag_flux=4,
+                       Iflag_Scheme=5, first=2e-4, Kt_inf=1e-6, Wt_inf=1e-2)
+    orc, g = _pair(p, bl, steps=5)
+    orc.residual(); g.residual()
+    compare_residual(orc, g)
+    compare_fields(orc, g, [1, 2, 3, 4, 5, 7, 8])
+
+
+@pytest.mark.parametrize("visc", [0, 1])
+def test_residual_fdm_weno5(gpu_lib, visc):
+    p, bl = small_case(nx=97, ny=33, Ma=0.6, AoA=1.5, Re=1.0e4, If_viscous=visc, Iflag_flux=4, Iflag_Scheme=5,
+                       nblocks=2)
+    orc, g = _pair(p, bl, fdm=(1, 2), steps=3)
+    orc.residual(); g.residual()
+    compare_residual(orc, g)
+
+
+def test_boundary_and_halo(gpu_lib):
+    p, bl = small_case(Ma=0.7, AoA=4.0, nblocks=2, If_viscous=0)
+    orc, g = _pair(p, bl, steps=2)
+    orc.bc(); g.bc()
+    compare_U(orc, g, tol=1e-15)
+    orc.halo(); g.halo()
+    compare_U(orc, g, tol=1e-15)
+
+
+def test_boundary_wall_isothermal_symmetry_sa(gpu_lib):
+    from ec2d import grids
+    from ec2d.inputs import Params
+    bl = grids.flat_plate(33, 17, first=1e-3, ratio=1.2)
+    p = Params(Ma=0.3, Re=1e4, If_viscous=1, Iflag_turbulence_model=2, Twall=300.0, Iflag_flux=6, Iflag_Scheme=5)
+    orc, g = _pair(p, bl, steps=2)
+    orc.bc(); g.bc(); orc.halo(); g.halo()
+    compare_U(orc, g, tol=1e-14)
+
+
+def test_lusgs_sweep(gpu_lib):
+    p, bl = small_case(Ma=0.7, AoA=2.0, nblocks=2, If_viscous=1, Re=1e4, Iflag_flux=4)
+    orc, g = _pair(p, bl, steps=3)
+    orc.residual()
+    # identical inputs on both sides: Res, dt and spectral radii from the oracle
+    for b in (1, 2):
+        for f in (0, 1, 2, 3, 4, 5):
+            g.set_field(1, 1, b, f, orc.field(1, b, f))
+    for b in (1, 2):
+        orc.lusgs(1, b, 0.0)
+    g.lusgs(1, 0.0)
+    compare_fields(orc, g, [6], tol=1e-12)
+
+
+@pytest.mark.parametrize("tm", [0, 1, 3])
+def test_steps_single_grid(gpu_lib, tm):
+    p, bl = small_case(Ma=0.75, AoA=1.25, Iflag_flux=4, Iflag_Scheme=5, Time_Method=tm, CFL=2.0 if tm else 5.0)
+    orc = make_oracle(p, bl)
+    orc.init_flow()
+    g = make_gpu(p, bl)
+    g.init_flow()
+    compare_U(orc, g, tol=1e-15)
+    orc.step(20); g.step(20)
+    compare_U(orc, g, tol=1e-10)
+    a_o, r_o, k_o, t_o = orc.norms()
+    a_g, r_g, k_g, t_g = g.norms()
+    assert k_o == k_g == 20
+    np.testing.assert_allclose(r_g, r_o, rtol=1e-8, atol=1e-300)
+
+
+@pytest.mark.parametrize("tm", [1, 3, 0])
+def test_multigrid_cycles(gpu_lib, tm):
+    p, bl = small_case(nx=65, ny=17, Ma=0.6, AoA=2.0, Iflag_flux=6, Iflag_Scheme=5, Time_Method=tm, Num_Mesh=3,
+                       CFL=1.5 if tm else 4.0, Pre_Step_Mesh=(0, 5, 5), mg_lusgs=1, nblocks=2)
+    orc = make_oracle(p, bl)
+    orc.init_flow()
+    g = make_gpu(p, bl)
+    g.init_flow()
+    assert g.num_mesh == 3
+    compare_U(orc, g, tol=1e-11)
+    orc.step(5); g.step(5)
+    compare_U(orc, g, tol=1e-9)
+
+
+def test_multigrid_viscous_lusgs_flat_plate(gpu_lib):
+    from ec2d import cases
+    p, bl = cases.laminar_flat_plate(33, 33, num_mesh=3)
+    orc = make_oracle(p, bl)
+    orc.init_flow()
+    g = make_gpu(p, bl)
+    g.init_flow()
+    orc.step(4); g.step(4)
+    compare_U(orc, g, tol=1e-9)
+
+
+def test_norms_and_forces(gpu_lib):
+    p, bl = small_case(Ma=0.5, AoA=3.0, Re=2e3, If_viscous=1, Iflag_flux=4, Iflag_Scheme=5)
+    orc, g = _pair(p, bl, steps=10, perturb=False)
+    orc.residual(); g.residual()
+    a_o, r_o, _, _ = orc.norms()
+    a_g, r_g, _, _ = g.norms()
+    np.testing.assert_allclose(a_g, a_o, rtol=1e-12)
+    np.testing.assert_allclose(r_g, r_o, rtol=1e-12)
+    fo = np.array(orc.forces())
+    fg = np.array(g.forces())
+    np.testing.assert_allclose(fg, fo, rtol=1e-11, atol=1e-13)
+    cfo, xo = orc.wall_cf(1, 3)
+    cfg, xg = g.wall_cf(1, 1, 3)
+    np.testing.assert_allclose(cfg, cfo, rtol=1e-10, atol=1e-13)
+
+
+def test_batch_equals_single(gpu_lib):
+    from ec2d import gpu
+    p1, bl1 = small_case(Ma=0.6, AoA=1.0, Iflag_flux=4, Iflag_Scheme=5)
+    p2, bl2 = small_case(nx=97, ny=17, Ma=0.7, AoA=3.0, Iflag_flux=4, Iflag_Scheme=5, nblocks=2)
+    batch = gpu.Solver([(p1, bl1), (p2, bl2)])
+    batch.init_flow(); batch.step(8)
+    for ci, (p, bl) in enumerate([(p1, bl1), (p2, bl2)], start=1):
+        one = gpu.Solver([(p, bl)])
+        one.init_flow(); one.step(8)
+        for b in range(1, len(bl) + 1):
+            np.testing.assert_array_equal(batch.download_U(ci, 1, b), one.download_U(1, 1, b))
+        np.testing.assert_array_equal(batch.norms(ci)[1], one.norms(1)[1])
