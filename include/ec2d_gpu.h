@@ -165,6 +165,16 @@ int ec2d_interpolation2h(ec2d_ctx *ctx, int m1, int m2, int flag); /* sub_NS_mul
 int ec2d_prolong(ec2d_ctx *ctx, int m1, int m2, int flag);         /* prolong_U, sub_NS_multigrid.f90:271 */
 int ec2d_force_function(ec2d_ctx *ctx, int mesh);         /* comput_force_function, sub_NS_multigrid.f90:156 */
 
+/* Instrumentation for benchmarks: the context's cudaStream_t (so callers
+ * can record CUDA events on it), the number of kernel launches issued so
+ * far, and optional per-kernel event timing.  ec2d_kernel_times writes one
+ * line "name level calls kernels total_ms" per kernel and level recorded
+ * since timing was enabled (or since the last call) and clears the record. */
+int ec2d_stream(ec2d_ctx *ctx, void **stream);
+int ec2d_launch_count(ec2d_ctx *ctx, long long *n);
+int ec2d_kernel_timing(ec2d_ctx *ctx, int enable);
+int ec2d_kernel_times(ec2d_ctx *ctx, char *buf, int buflen);
+
 /* Wait for all queued work of the context. */
 int ec2d_sync(ec2d_ctx *ctx);
 

@@ -98,6 +98,12 @@ struct ec2d_ctx {
   size_t stage_n = 0;
   int dual_iflag1 = 0, dual_iflag = 0;
   int last_err = 0;
+  // launch accounting and optional per-kernel event timing
+  long long launches = 0;
+  bool timing = false;
+  struct KRec { const char *name; int level, nk; cudaEvent_t a, b; };
+  std::vector<KRec> krec;
+  std::vector<cudaEvent_t> evpool;
 };
 
 namespace {
@@ -520,30 +526,52 @@ int wall_distance(ec2d_ctx *ctx) {
 }
 
 // ---------------- orchestration -------------------------------------------
+cudaEvent_t pool_event(ec2d_ctx *ctx) {
+  if (!ctx->evpool.empty()) { cudaEvent_t e = ctx->evpool.back(); ctx->evpool.pop_back(); return e; }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+// every kernel launch of the time-marching path goes through K(): it counts
+// the launches (nk kernels per call) and, when timing is on, brackets them
+// with events on the context's stream
+template <class Fn>
+void K(ec2d_ctx *ctx, const char *name, int level, int nk, Fn fn) {
+  ctx->launches += nk;
+  if (!ctx->timing) { fn(); return; }
+  cudaEvent_t a = pool_event(ctx), b = pool_event(ctx);
+  cudaEventRecord(a, ctx->stream);
+  fn();
+  cudaEventRecord(b, ctx->stream);
+  ctx->krec.push_back({name, level, nk, a, b});
+}
 
 // Comput_Residual_one_mesh (sub_Residual.f90:13-107) for all blocks of a level
 void residual(ec2d_ctx *ctx, int l) {
   Level &lv = ctx->lv[l];
   const Lvl &L = lv.L;
   cudaStream_t s = ctx->stream;
-  launch_prim(L, s);
+  K(ctx, "k_prim", l, 1, [&] { launch_prim(L, s); });
   if (L.visc) {
-    if (L.turb == Turb_SA) launch_sa(L, s);
-    else if (L.turb == Turb_SST) launch_sst(L, s);
+    if (L.turb == Turb_SA) K(ctx, "sa", l, 4, [&] { launch_sa(L, s); });
+    else if (L.turb == Turb_SST) K(ctx, "sst", l, 4, [&] { launch_sst(L, s); });
   }
-  launch_flux(L, s);
-  launch_res(L, s);
-  if (L.fdm) launch_fdm(L, s);
+  K(ctx, "k_flux_i", l, 1, [&] { launch_flux_i(L, s); });
+  K(ctx, "k_flux_j", l, 1, [&] { launch_flux_j(L, s); });
+  K(ctx, "k_res", l, 1, [&] { launch_res(L, s); });
+  if (L.fdm) K(ctx, "fdm", l, 3, [&] { launch_fdm(L, s); });
   if (ctx->P.Time_Method == Time_Dual && l == 1) {
     double sfac;
     if (ctx->dual_iflag1 == 0) { ctx->dual_iflag1 = 1; sfac = 1.0 / (3.0 * ctx->P.dt_global); }
     else sfac = 1.0 / (2.0 * ctx->P.dt_global);
-    launch_dual_term(L, sfac, s);
+    K(ctx, "k_dual", l, 1, [&] { launch_dual_term(L, sfac, s); });
   }
-  launch_norms(L, lv.d_case_tile0, lv.d_case_ntile, lv.d_case_ncell, s);
+  K(ctx, "norms", l, 2, [&] { launch_norms(L, lv.d_case_tile0, lv.d_case_ntile, lv.d_case_ncell, s); });
 }
 
-void bc_all(ec2d_ctx *ctx, int l) { launch_bc(ctx->lv[l].L, 1 | 2 | 4, ctx->stream); }
+void bc_all(ec2d_ctx *ctx, int l) {
+  K(ctx, "k_bc", l, 1, [&] { launch_bc(ctx->lv[l].L, 1 | 2 | 4, ctx->stream); });
+}
 
 void advance_counters(ec2d_ctx *ctx, int l) {
   for (auto &c : ctx->cases) { c.tt[l] += c.p.dt_global; c.kstep[l] += 1; }
@@ -552,17 +580,17 @@ void advance_counters(ec2d_ctx *ctx, int l) {
 // NS_Time_advance_1Euler (sub_NS_singlegrid.f90:67-106)
 void step_euler(ec2d_ctx *ctx, int l) {
   residual(ctx, l);
-  launch_euler(ctx->lv[l].L, l != 1, ctx->stream);
+  K(ctx, "k_euler", l, 1, [&] { launch_euler(ctx->lv[l].L, l != 1, ctx->stream); });
   bc_all(ctx, l);
   advance_counters(ctx, l);
 }
 // NS_Time_advance_RK3 (sub_NS_singlegrid.f90:115-176)
 void step_rk3(ec2d_ctx *ctx, int l) {
   const Lvl &L = ctx->lv[l].L;
-  launch_set_un(L, L.nvar, ctx->stream);
+  K(ctx, "k_set_un", l, 1, [&] { launch_set_un(L, L.nvar, ctx->stream); });
   for (int k = 0; k < 3; k++) {
     residual(ctx, l);
-    launch_rk3(L, k, l != 1, ctx->stream);
+    K(ctx, "k_rk3", l, 1, [&] { launch_rk3(L, k, l != 1, ctx->stream); });
     bc_all(ctx, l);
   }
   advance_counters(ctx, l);
@@ -572,14 +600,14 @@ void step_rk3(ec2d_ctx *ctx, int l) {
 void step_lusgs(ec2d_ctx *ctx, int l, double alfa1 = 0.0) {
   const Lvl &L = ctx->lv[l].L;
   residual(ctx, l);
-  if (l != 1) launch_add_force(L, ctx->stream);
-  launch_lusgs(L, alfa1, ctx->stream);
-  launch_add_du(L, ctx->stream);
+  if (l != 1) K(ctx, "k_add_force", l, 1, [&] { launch_add_force(L, ctx->stream); });
+  K(ctx, "k_lusgs", l, 1, [&] { launch_lusgs(L, alfa1, ctx->stream); });
+  K(ctx, "k_add_du", l, 1, [&] { launch_add_du(L, ctx->stream); });
   bc_all(ctx, l);
   advance_counters(ctx, l);
 }
 void clip(ec2d_ctx *ctx, int l) {
-  if (ctx->lv[l].L.nvar >= 5) launch_bc(ctx->lv[l].L, 8, ctx->stream);
+  if (ctx->lv[l].L.nvar >= 5) K(ctx, "k_clip", l, 1, [&] { launch_bc(ctx->lv[l].L, 8, ctx->stream); });
 }
 // Dual_time_LU_SGS (sub_NS_singlegrid.f90:231-310).  The inner-loop exit test
 // on the RMS residual needs the norms on the host after every inner step.
@@ -591,8 +619,8 @@ int step_dual(ec2d_ctx *ctx) {
   const Lvl &L = lv.L;
   for (int kt = 1; kt <= ctx->P.Nstep_Inner_Limit; kt++) {
     residual(ctx, 1);
-    launch_lusgs(L, alfa1, ctx->stream);
-    launch_add_du(L, ctx->stream);
+    K(ctx, "k_lusgs", 1, 1, [&] { launch_lusgs(L, alfa1, ctx->stream); });
+    K(ctx, "k_add_du", 1, 1, [&] { launch_add_du(L, ctx->stream); });
     bc_all(ctx, 1);
     std::vector<double> nm(12 * L.ncase);
     CK(cudaMemcpyAsync(nm.data(), L.norms, nm.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -605,7 +633,7 @@ int step_dual(ec2d_ctx *ctx) {
     }
     if (all_done) break;
   }
-  // U(n-1) <= U(n), U(n) <= U on interior cells
+  // U(n-1) <= U(n), U(n) <= U
   cudaStream_t s = ctx->stream;
   size_t bytes = (size_t)L.nvar * lv.F * sizeof(double);
   CK(cudaMemcpyAsync(L.un1, L.un, bytes, cudaMemcpyDeviceToDevice, s));
@@ -632,56 +660,56 @@ void mg_smooth_coarse(ec2d_ctx *ctx, int l) {
   const int Time_step_coarse_mesh = 3;
   int tm = ctx->P.Time_Method;
   if (tm == Time_Euler1) {
-    launch_set_un(ctx->lv[l].L, 4, ctx->stream);
+    K(ctx, "k_set_un", l, 1, [&] { launch_set_un(ctx->lv[l].L, 4, ctx->stream); });
     for (int m = 0; m < Time_step_coarse_mesh; m++) step_euler(ctx, l);
   } else if (tm == Time_LU_SGS) {
-    launch_set_un(ctx->lv[l].L, 4, ctx->stream);
+    K(ctx, "k_set_un", l, 1, [&] { launch_set_un(ctx->lv[l].L, 4, ctx->stream); });
     step_lusgs(ctx, l);
   } else step_rk3(ctx, l);
 }
+// restriction of the residual (flag 2) and of U (flag 1) from level f to f+1
+void restrict_both(ec2d_ctx *ctx, int f) {
+  const Lvl &Lf = ctx->lv[f].L, &Lc = ctx->lv[f + 1].L;
+  K(ctx, "k_restrict", f + 1, 1, [&] { launch_restrict(Lf, Lc, 2, ctx->stream); });
+  K(ctx, "k_restrict", f + 1, 1, [&] { launch_restrict(Lf, Lc, 1, ctx->stream); });
+}
+// deltU = U - Un on level c, prolonged to level c-1 and added there
+void correct_from(ec2d_ctx *ctx, int c) {
+  const Lvl &Lc = ctx->lv[c].L, &Lf = ctx->lv[c - 1].L;
+  K(ctx, "k_delt_u", c, 1, [&] { launch_delt_u(Lc, ctx->stream); });
+  K(ctx, "k_prolong", c - 1, 1, [&] { launch_prolong(Lc, Lf, 2, ctx->stream); });
+  K(ctx, "k_new_u", c - 1, 1, [&] { launch_new_u(Lf, ctx->stream); });
+}
 // NS_2stge_multigrid (sub_NS_multigrid.f90:14-58)
 void mg2(ec2d_ctx *ctx) {
-  cudaStream_t s = ctx->stream;
-  Level &l1 = ctx->lv[1], &l2 = ctx->lv[2];
   mg_smooth_fine(ctx);
   residual(ctx, 1);
-  launch_restrict(l1.L, l2.L, 2, s);
-  launch_restrict(l1.L, l2.L, 1, s);
+  restrict_both(ctx, 1);
   bc_all(ctx, 2);
   residual(ctx, 2);
-  launch_force_fn(l2.L, s);
+  K(ctx, "k_force_fn", 2, 1, [&] { launch_force_fn(ctx->lv[2].L, ctx->stream); });
   mg_smooth_coarse(ctx, 2);
-  launch_delt_u(l2.L, s);
-  launch_prolong(l2.L, l1.L, 2, s);
-  launch_new_u(l1.L, s);
+  correct_from(ctx, 2);
   bc_all(ctx, 1);
 }
 // NS_3stge_multigrid (sub_NS_multigrid.f90:66-142)
 void mg3(ec2d_ctx *ctx) {
-  cudaStream_t s = ctx->stream;
-  Level &l1 = ctx->lv[1], &l2 = ctx->lv[2], &l3 = ctx->lv[3];
   mg_smooth_fine(ctx);
   residual(ctx, 1);
-  launch_restrict(l1.L, l2.L, 2, s);
-  launch_restrict(l1.L, l2.L, 1, s);
+  restrict_both(ctx, 1);
   bc_all(ctx, 2);
   residual(ctx, 2);
-  launch_force_fn(l2.L, s);
+  K(ctx, "k_force_fn", 2, 1, [&] { launch_force_fn(ctx->lv[2].L, ctx->stream); });
   mg_smooth_coarse(ctx, 2);
   residual(ctx, 2);
-  launch_add_force(l2.L, s);
-  launch_restrict(l2.L, l3.L, 2, s);
-  launch_restrict(l2.L, l3.L, 1, s);
+  K(ctx, "k_add_force", 2, 1, [&] { launch_add_force(ctx->lv[2].L, ctx->stream); });
+  restrict_both(ctx, 2);
   bc_all(ctx, 3);
   residual(ctx, 3);
-  launch_force_fn(l3.L, s);
+  K(ctx, "k_force_fn", 3, 1, [&] { launch_force_fn(ctx->lv[3].L, ctx->stream); });
   mg_smooth_coarse(ctx, 3);
-  launch_delt_u(l3.L, s);
-  launch_prolong(l3.L, l2.L, 2, s);
-  launch_new_u(l2.L, s);
-  launch_delt_u(l2.L, s);
-  launch_prolong(l2.L, l1.L, 2, s);
-  launch_new_u(l1.L, s);
+  correct_from(ctx, 3);
+  correct_from(ctx, 2);
   bc_all(ctx, 1);
 }
 
@@ -777,6 +805,8 @@ void ec2d_destroy(ec2d_ctx *ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   for (auto &lv : ctx->lv) lv.bufs.clear();
+  for (auto &r : ctx->krec) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+  for (auto e : ctx->evpool) cudaEventDestroy(e);
   if (ctx->d_cases) cudaFree(ctx->d_cases);
   if (ctx->d_stage) cudaFree(ctx->d_stage);
   cudaStreamDestroy(ctx->stream);
@@ -1144,6 +1174,51 @@ int ec2d_force_function(ec2d_ctx *ctx, int mesh) {
   launch_force_fn(ctx->lv[mesh].L, ctx->stream);
   return check_launch(ctx);
 }
+int ec2d_stream(ec2d_ctx *ctx, void **stream) {
+  if (!ctx || !stream) return EC2D_ERR_ARG;
+  *stream = (void *)ctx->stream;
+  return EC2D_OK;
+}
+
+int ec2d_launch_count(ec2d_ctx *ctx, long long *n) {
+  if (!ctx || !n) return EC2D_ERR_ARG;
+  *n = ctx->launches;
+  return EC2D_OK;
+}
+
+int ec2d_kernel_timing(ec2d_ctx *ctx, int enable) {
+  if (!ctx) return EC2D_ERR_ARG;
+  ctx->timing = enable != 0;
+  return EC2D_OK;
+}
+
+int ec2d_kernel_times(ec2d_ctx *ctx, char *buf, int buflen) {
+  if (!ctx || !buf || buflen <= 0) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  CK(cudaStreamSynchronize(ctx->stream));
+  struct Acc { std::string name; int level; long long calls, nk; double ms; };
+  std::vector<Acc> acc;
+  for (auto &r : ctx->krec) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    ctx->evpool.push_back(r.a);
+    ctx->evpool.push_back(r.b);
+    bool found = false;
+    for (auto &x : acc)
+      if (x.name == r.name && x.level == r.level) { x.calls++; x.nk += r.nk; x.ms += ms; found = true; break; }
+    if (!found) acc.push_back({r.name, r.level, 1, r.nk, (double)ms});
+  }
+  ctx->krec.clear();
+  std::string out;
+  char line[160];
+  for (auto &x : acc) {
+    snprintf(line, sizeof(line), "%s %d %lld %lld %.6f\n", x.name.c_str(), x.level, x.calls, x.nk, x.ms);
+    out += line;
+  }
+  snprintf(buf, buflen, "%s", out.c_str());
+  return (int)out.size() < buflen ? EC2D_OK : EC2D_ERR_ARG;
+}
+
 int ec2d_sync(ec2d_ctx *ctx) {
   if (!ctx) return EC2D_ERR_ARG;
   cudaSetDevice(ctx->device);

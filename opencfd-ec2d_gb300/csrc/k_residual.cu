@@ -287,10 +287,8 @@ __global__ void k_norm_final(Lvl L, const int *case_tile0, const int *case_ntile
 }
 
 void launch_prim(const Lvl &L, cudaStream_t s) { k_prim<<<L.ntiles, TILE, 0, s>>>(L); }
-void launch_flux(const Lvl &L, cudaStream_t s) {
-  k_flux_i<<<L.ntiles, TILE, 0, s>>>(L);
-  k_flux_j<<<L.ntiles, TILE, 0, s>>>(L);
-}
+void launch_flux_i(const Lvl &L, cudaStream_t s) { k_flux_i<<<L.ntiles, TILE, 0, s>>>(L); }
+void launch_flux_j(const Lvl &L, cudaStream_t s) { k_flux_j<<<L.ntiles, TILE, 0, s>>>(L); }
 void launch_res(const Lvl &L, cudaStream_t s) { k_res<<<L.ntiles, TILE, 0, s>>>(L); }
 void launch_norms(const Lvl &L, const int *case_tile0, const int *case_ntile, const int *case_ncell,
                   cudaStream_t s) {

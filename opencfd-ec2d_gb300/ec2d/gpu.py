@@ -107,6 +107,10 @@ def lib():
         "ec2d_prolong": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "ec2d_force_function": ([vp, ctypes.c_int], ctypes.c_int),
         "ec2d_sync": ([vp], ctypes.c_int),
+        "ec2d_stream": ([vp, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+        "ec2d_launch_count": ([vp, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
+        "ec2d_kernel_timing": ([vp, ctypes.c_int], ctypes.c_int),
+        "ec2d_kernel_times": ([vp, ctypes.c_char_p, ctypes.c_int], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -258,3 +262,27 @@ class Solver:
 
     def sync(self):
         _ck(self.L.ec2d_sync(self.h), "ec2d_sync")
+
+    def stream_handle(self):
+        """The context's cudaStream_t as an integer (for CUDA events)."""
+        s = ctypes.c_void_p()
+        _ck(self.L.ec2d_stream(self.h, ctypes.byref(s)), "ec2d_stream")
+        return s.value or 0
+
+    def launch_count(self):
+        n = ctypes.c_longlong()
+        _ck(self.L.ec2d_launch_count(self.h, ctypes.byref(n)), "ec2d_launch_count")
+        return n.value
+
+    def kernel_timing(self, enable=True):
+        _ck(self.L.ec2d_kernel_timing(self.h, 1 if enable else 0), "ec2d_kernel_timing")
+
+    def kernel_times(self):
+        """{(name, level): (calls, kernels, total_ms)} since timing was enabled."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        _ck(self.L.ec2d_kernel_times(self.h, buf, len(buf)), "ec2d_kernel_times")
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, lvl, calls, nk, ms = line.split()
+            out[(name, int(lvl))] = (int(calls), int(nk), float(ms))
+        return out

@@ -124,12 +124,24 @@ def test_lusgs_sweep(gpu_lib):
     for b in (1, 2):
         orc.lusgs(1, b, 0.0)
     g.lusgs(1, 0.0)
-    compare_fields(orc, g, [6], tol=1e-12)
+    # dU = (Res + dui + duj)/alfa with dui built from F(U+dU) - F(U): the
+    # round-off of that difference scales with F(U) s / alfa, i.e. with the
+    # cell's |U|, not with |dU|, and it accumulates along the sweep's
+    # dependency chain.  Per cell: |ddU| <= 1e-12 |dU| + 1e-14 |U| (~100 ulp of U).
+    worst = 0.0
+    for b in (1, 2):
+        nx, ny = orc.dims(1, b)
+        a = orc.field(1, b, 6, (4, nx, ny))[:, :nx - 1, :ny - 1]
+        c = g.field(1, 1, b, 6, (4, nx, ny))[:, :nx - 1, :ny - 1]
+        U = orc.get_U(1, b)[:4, 2:nx + 1, 2:ny + 1]
+        bound = 1e-12 * np.maximum(np.abs(a), np.abs(c)) + 1e-14 * np.abs(U)
+        worst = max(worst, np.max(np.abs(a - c) / bound))
+    assert worst <= 1.0, worst
 
 
 @pytest.mark.parametrize("tm", [0, 1, 3])
 def test_steps_single_grid(gpu_lib, tm):
-    p, bl = small_case(Ma=0.75, AoA=1.25, Iflag_flux=4, Iflag_Scheme=5, Time_Method=tm, CFL=2.0 if tm else 5.0)
+    p, bl = small_case(Ma=0.75, AoA=1.25, Iflag_flux=4, Iflag_Scheme=5, Time_Method=tm, CFL={0: 5.0, 1: 0.8, 3: 1.5}[tm])
     orc = make_oracle(p, bl)
     orc.init_flow()
     g = make_gpu(p, bl)
@@ -146,7 +158,7 @@ def test_steps_single_grid(gpu_lib, tm):
 @pytest.mark.parametrize("tm", [1, 3, 0])
 def test_multigrid_cycles(gpu_lib, tm):
     p, bl = small_case(nx=65, ny=17, Ma=0.6, AoA=2.0, Iflag_flux=6, Iflag_Scheme=5, Time_Method=tm, Num_Mesh=3,
-                       CFL=1.5 if tm else 4.0, Pre_Step_Mesh=(0, 5, 5), mg_lusgs=1, nblocks=2)
+                       CFL={0: 4.0, 1: 0.8, 3: 1.5}[tm], Pre_Step_Mesh=(0, 5, 5), mg_lusgs=1, nblocks=2)
     orc = make_oracle(p, bl)
     orc.init_flow()
     g = make_gpu(p, bl)
