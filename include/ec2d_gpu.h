@@ -175,6 +175,22 @@ int ec2d_launch_count(ec2d_ctx *ctx, long long *n);
 int ec2d_kernel_timing(ec2d_ctx *ctx, int enable);
 int ec2d_kernel_times(ec2d_ctx *ctx, char *buf, int buflen);
 
+/* Residual norms without any device allocation.  No counterpart in the
+ * reference: it serves hosts that cannot call cudaMalloc (a Fortran/OpenACC
+ * host whose device memory belongs to another allocator or memory pool, or a
+ * host that must not allocate after start-up) and already hold a residual
+ * array on the device.  res: device pointer to Res(nvar, ncell) (variable
+ * fastest, e.g. the reference's Res(NVAR,1:nx-1,1:ny-1) of one block);
+ * out: device pointer to 12 doubles, max|Res_m| for m=1..6 then sum Res_m^2
+ * for m=1..6 (entries past nvar are 0); stream: a cudaStream_t or NULL.
+ * The tile partials live in one file-scope __device__ array of 768 KiB per
+ * GPU, so ncell is limited to EC2D_NOALLOC_MAX_CELLS (larger sizes return
+ * EC2D_ERR_ARG).  All calls share that array: calls that overlap on the GPU
+ * race.  The first call on a device looks up the array's address; make it
+ * before any stream capture. */
+#define EC2D_NOALLOC_MAX_CELLS 2097152
+int ec2d_residual_norms_noalloc(const double *res, int nvar, int ncell, double *out, void *stream);
+
 /* Wait for all queued work of the context. */
 int ec2d_sync(ec2d_ctx *ctx);
 
