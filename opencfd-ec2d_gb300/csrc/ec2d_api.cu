@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -75,6 +76,7 @@ struct Level {
   std::vector<int4> wall_faces;          // (block, face, k, 0) for forces
   std::vector<int> case_face0, case_nface;
   long long F = 0;
+  int max_rows = 0;   // widest block (ny-1) of the level: LU-SGS threads per CTA
   Lvl L{};
   int *d_case_tile0 = nullptr, *d_case_ntile = nullptr, *d_case_ncell = nullptr;
   int4 *d_faces = nullptr;
@@ -100,6 +102,7 @@ struct ec2d_ctx {
   int last_err = 0;
   // launch accounting and optional per-kernel event timing
   long long launches = 0;
+  int lusgs_cs = 1;  // CTAs per block in the LU-SGS wavefront (1: one CTA, >1: a cluster)
   bool timing = false;
   struct KRec { const char *name; int level, nk; cudaEvent_t a, b; };
   std::vector<KRec> krec;
@@ -340,6 +343,8 @@ int build_level(ec2d_ctx *ctx, int l) {
     BlkDev d{};
     d.nx = B.nx; d.ny = B.ny; d.P = B.nx + 5; d.cas = B.cas; d.off = off; d.fdm = B.fdm ? 1 : 0;
     d.nsub = B.nsub; d.sub0 = sub0; d.tile0 = tile;
+    d.cell0 = lv.L.ncell;
+    lv.L.ncell += (B.nx - 1) * (B.ny - 1);
     off += ((long long)d.P * (B.ny + 5) + 31) / 32 * 32;
     int items = (B.nx + 3) * (B.ny + 3);
     int nt = (items + TILE - 1) / TILE;
@@ -438,6 +443,8 @@ int build_level(ec2d_ctx *ctx, int l) {
   for (auto &B : lv.hb) anyfdm |= B.fdm;
   L.met = anyfdm ? dalloc<double>(lv, 5 * F) : nullptr;
   L.fdm = anyfdm ? dalloc<double>(lv, 30 * F) : nullptr;
+  for (auto &B : lv.hb) lv.max_rows = std::max(lv.max_rows, B.ny - 1);
+  L.rec = (lv.max_rows <= 1024) ? dalloc<double>(lv, (size_t)2 * L.ncell * lusgs_planes(nv)) : nullptr;
   L.npart = dalloc<double>(lv, lv.tiles.size() * 12);
   L.norms = dalloc<double>(lv, ncase * 12);
   L.status = dalloc<int>(lv, ncase * 4);
@@ -595,14 +602,25 @@ void step_rk3(ec2d_ctx *ctx, int l) {
   }
   advance_counters(ctx, l);
 }
+// du_LU_SGS_2D for every block of the level followed by U += dU
+// (sub_NS_singlegrid.f90:196-213): the wavefront kernels fuse the update into
+// the backward sweep; blocks wider than 1024 rows take the generic kernel
+void lusgs_update(ec2d_ctx *ctx, int l, double alfa1) {
+  const Lvl &L = ctx->lv[l].L;
+  if (L.rec) {
+    K(ctx, "k_lusgs", l, 2, [&] { launch_lusgs_fast(L, alfa1, 1, ctx->lv[l].max_rows, ctx->lusgs_cs, ctx->stream); });
+  } else {
+    K(ctx, "k_lusgs_generic", l, 1, [&] { launch_lusgs(L, alfa1, ctx->stream); });
+    K(ctx, "k_add_du", l, 1, [&] { launch_add_du(L, ctx->stream); });
+  }
+}
 // NS_Time_advance_LU_SGS (sub_NS_singlegrid.f90:185-224); on a coarse level of
 // an LU-SGS-smoothed multigrid cycle the forcing is added after the residual
 void step_lusgs(ec2d_ctx *ctx, int l, double alfa1 = 0.0) {
   const Lvl &L = ctx->lv[l].L;
   residual(ctx, l);
   if (l != 1) K(ctx, "k_add_force", l, 1, [&] { launch_add_force(L, ctx->stream); });
-  K(ctx, "k_lusgs", l, 1, [&] { launch_lusgs(L, alfa1, ctx->stream); });
-  K(ctx, "k_add_du", l, 1, [&] { launch_add_du(L, ctx->stream); });
+  lusgs_update(ctx, l, alfa1);
   bc_all(ctx, l);
   advance_counters(ctx, l);
 }
@@ -619,8 +637,7 @@ int step_dual(ec2d_ctx *ctx) {
   const Lvl &L = lv.L;
   for (int kt = 1; kt <= ctx->P.Nstep_Inner_Limit; kt++) {
     residual(ctx, 1);
-    K(ctx, "k_lusgs", 1, 1, [&] { launch_lusgs(L, alfa1, ctx->stream); });
-    K(ctx, "k_add_du", 1, 1, [&] { launch_add_du(L, ctx->stream); });
+    lusgs_update(ctx, 1, alfa1);
     bc_all(ctx, 1);
     std::vector<double> nm(12 * L.ncase);
     CK(cudaMemcpyAsync(nm.data(), L.norms, nm.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -795,6 +812,7 @@ int ec2d_create(int device, ec2d_ctx **out) {
   CK(cudaSetDevice(device));
   ec2d_ctx *c = new ec2d_ctx();
   c->device = device;
+  if (const char *e = getenv("EC2D_LUSGS_CLUSTER")) c->lusgs_cs = std::max(1, std::min(8, atoi(e)));
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { delete c; return EC2D_ERR_CUDA; }
   *out = c;
   return EC2D_OK;
@@ -1144,7 +1162,9 @@ int ec2d_update_buffer(ec2d_ctx *ctx, int mesh) {
 int ec2d_du_lusgs(ec2d_ctx *ctx, int mesh, double alfa1) {
   if (!ctx || !ctx->setup_done || mesh < 1 || mesh > ctx->num_mesh) return EC2D_ERR_ARG;
   cudaSetDevice(ctx->device);
-  launch_lusgs(ctx->lv[mesh].L, alfa1, ctx->stream);
+  const Lvl &L = ctx->lv[mesh].L;
+  if (L.rec) launch_lusgs_fast(L, alfa1, 0, ctx->lv[mesh].max_rows, ctx->lusgs_cs, ctx->stream);
+  else launch_lusgs(L, alfa1, ctx->stream);
   return check_launch(ctx);
 }
 int ec2d_time_advance(ec2d_ctx *ctx, int mesh) {

@@ -43,6 +43,7 @@ struct BlkDev {
   int nsub, sub0;           // subfaces [sub0, sub0+nsub) in Lvl::sub
   int tile0;                // first extended-range tile of this block
   int lsub0, lsubn;         // fine-mesh wall faces (forces), unused on coarse levels
+  int cell0;                // dense index of cell (1,1) among the level's interior cells
 };
 
 struct SubDev {
@@ -72,6 +73,9 @@ struct Lvl {
   double *tb;               // turbulence scratch planes
   double *met;              // FDM metrics Akx,Aky,Aix,Aiy,Ajac
   double *fdm;              // FDM scratch planes
+  double *lu;               // LU-SGS pre-pass planes (4 NV + 10)
+  double *rec;              // LU-SGS per-cell sweep records: [2 passes][ncell][4 NV + 10]
+  int ncell;                // interior cells of the level (all blocks of all cases)
   double *npart;            // norm partials: per tile 2*6 doubles
   double *norms;            // per case: max[6], rms[6]
   int *status;              // per case: code, block, i, j

@@ -24,6 +24,9 @@ void launch_dual_term(const Lvl &L, double sfac, cudaStream_t s);
 void launch_bc(const Lvl &L, int phases, cudaStream_t s);
 // k_lusgs.cu
 void launch_lusgs(const Lvl &L, double alfa1, cudaStream_t s);
+// k_sweep.cu
+int lusgs_planes(int nv);
+void launch_lusgs_fast(const Lvl &L, double alfa1, int update, int max_rows, int cs, cudaStream_t s);
 void launch_add_du(const Lvl &L, cudaStream_t s);
 void launch_euler(const Lvl &L, int force, cudaStream_t s);
 void launch_rk3(const Lvl &L, int stage, int force, cudaStream_t s);

@@ -1,0 +1,331 @@
+// k_sweep.cu -- the LU-SGS operator (du_LU_SGS_2D, sub_LU_SGS.f90:4-108) as a
+// latency-optimised wavefront.
+//
+// The Gauss-Seidel order of the reference is kept exactly: the forward sweep
+// visits hyperplanes p = i+j = 2..nx+ny-2, the backward sweep p = nx+ny-2..2,
+// and every cell reads only neighbours on plane p-1 (p+1).  The work is split
+// so that only the dependency chain sits between two planes:
+//   k_lusgs_prep  (all cells in parallel) evaluates everything that does not
+//                 depend on the sweep -- 1/alfa, the normal fluxes F_n(U_nb)
+//                 of the upstream neighbours with this cell's face normals,
+//                 the coefficient products 0.5 s and 0.5 Lc + Lv -- and packs
+//                 them with U and Res into one 16-byte-aligned record per cell
+//                 and pass;
+//   k_lusgs_sweep (one CTA or one thread-block cluster per block; thread j
+//                 owns row j) fetches the NEXT cell's record into shared memory
+//                 with cp.async while it computes the current cell, takes the
+//                 own row's previous cell from registers and the neighbouring
+//                 row from a double-buffered shared slot, and forms
+//                 F_n(U_nb + dU_nb) - F_n(U_nb), the sum and the 1/alfa scaling.
+// The producer of a state also ships 1/rho and p of U + dU, so each of its two
+// consumers needs no division.  The backward sweep writes U + dU (the update
+// of NS_Time_advance_LU_SGS, sub_NS_singlegrid.f90:203-211): a neighbour needs
+// U_old + dU_final of this cell, which is exactly the new U, and F_n(U_old)
+// was taken in the pre-pass before any U changed.
+#include <algorithm>
+
+#include "ec2d_dev.cuh"
+#include "ec2d_internal.h"
+
+namespace ec2d {
+
+constexpr int TILE = 256;
+
+// record layout (doubles), identical for both passes:
+//  A    Res (forward) or the forward dU (backward)
+//  U    U_old of the cell
+//  FI   F_n(U_nb) of the i-neighbour (west forward, east backward), normal of face i
+//  FJ   the same for the j-neighbour (south / north), normal of face j
+//  CI, CJ  0.5 Lc_nb (+ Lv_nb when viscous)
+//  HI, HJ  0.5 s of the face the reference multiplies the flux difference by
+//  IA, IA5 1/alfa and, for the SA row, 1/(alfa + Lvi + Lvj)
+//  N1I..N2J  face normals of face i and face j of the cell
+template <int NV>
+struct Rec {
+  static constexpr int A = 0, U = NV, FI = 2 * NV, FJ = 3 * NV, CI = 4 * NV, CJ = CI + 1, HI = CI + 2,
+                       HJ = CI + 3, IA = CI + 4, IA5 = CI + 5, N1I = CI + 6, N2I = CI + 7, N1J = CI + 8,
+                       N2J = CI + 9, N = CI + 10;
+  static_assert(N % 2 == 0, "records are whole 16-byte units");
+};
+
+// state shipped between neighbours: U2 = U + dU, 1/rho2, p2, dU
+template <int NV>
+struct Slot {
+  static constexpr int R = NV, P = NV + 1, D = NV + 2, S = 2 * NV + 2;
+  static_assert(S % 2 == 0, "slots are whole 16-byte units");
+};
+
+int lusgs_planes(int nv) { return 4 * nv + 10; }
+
+// normal flux of the Euler part (+ convected turbulence variables), the F(U)
+// half of comput_DFn (sub_LU_SGS.f90:122-137)
+template <int NV>
+__device__ __forceinline__ void fn(const double *U, double n1, double n2, double gm1, double *Fo) {
+  double r = 1.0 / U[0];
+  double un = (U[1] * n1 + U[2] * n2) * r;
+  double p = gm1 * (U[3] - 0.5 * (U[1] * U[1] + U[2] * U[2]) * r);
+  Fo[0] = U[0] * un;
+  Fo[1] = U[1] * un + p * n1;
+  Fo[2] = U[2] * un + p * n2;
+  Fo[3] = (U[3] + p) * un;
+#pragma unroll
+  for (int m = 4; m < NV; m++) Fo[m] = U[m] * un;
+}
+
+// the same from a shipped state (1/rho and p precomputed by the producer)
+template <int NV>
+__device__ __forceinline__ void fn_shipped(const double *st, double n1, double n2, double *Fo) {
+  using SL = Slot<NV>;
+  double un = (st[1] * n1 + st[2] * n2) * st[SL::R];
+  double p = st[SL::P];
+  Fo[0] = st[0] * un;
+  Fo[1] = st[1] * un + p * n1;
+  Fo[2] = st[2] * un + p * n2;
+  Fo[3] = (st[3] + p) * un;
+#pragma unroll
+  for (int m = 4; m < NV; m++) Fo[m] = st[m] * un;
+}
+
+template <int NV>
+__global__ void __launch_bounds__(TILE) k_lusgs_prep(Lvl L, double alfa1) {
+  using RC = Rec<NV>;
+  int2 t = L.tiles[blockIdx.x];
+  const BlkDev &b = L.blk[t.x];
+  int W = b.nx + 3, lin = t.y + threadIdx.x;
+  if (lin >= W * (b.ny + 3)) return;
+  int i = lin % W - 1, j = lin / W - 1;
+  if (i < 1 || i > b.nx - 1 || j < 1 || j > b.ny - 1) return;
+  const CaseDev &c = L.cs[b.cas];
+  const long long F = L.F, P = b.P;
+  const long long id = fidx(b, i, j);
+  const double gm1 = c.gamma - 1.0;
+  const double *g = L.geo, *lc = L.lc;
+  const bool visc = L.visc != 0;
+  const size_t cell = (size_t)b.cell0 + (size_t)(j - 1) * (b.nx - 1) + (i - 1);
+  double *rf = L.rec + cell * RC::N;                          // forward record
+  double *rb = L.rec + ((size_t)L.ncell + cell) * RC::N;      // backward record
+  double vol = g[G_VOL * F + id];
+  double Lv = lc[L_VI * F + id] + lc[L_VJ * F + id];
+  double alfa = vol / lc[L_DT * F + id] + 1.0 * (lc[L_CI * F + id] + lc[L_CJ * F + id]) + vol * alfa1;
+  if (visc) alfa += 2.0 * Lv;
+  double ia = 1.0 / alfa, ia5 = (NV == 5) ? 1.0 / (alfa + Lv) : ia;
+  double ni1 = g[G_NI1 * F + id], ni2 = g[G_NI2 * F + id], nj1 = g[G_NJ1 * F + id], nj2 = g[G_NJ2 * F + id];
+#pragma unroll
+  for (int m = 0; m < NV; m++) {
+    double u = L.U[m * F + id];
+    rf[RC::A + m] = L.res[m * F + id];
+    rb[RC::A + m] = 0.0;
+    rf[RC::U + m] = u;
+    rb[RC::U + m] = u;
+  }
+  double *rr[2] = {rf, rb};
+#pragma unroll
+  for (int pass = 0; pass < 2; pass++) {
+    double *r = rr[pass];
+    r[RC::IA] = ia; r[RC::IA5] = ia5;
+    r[RC::N1I] = ni1; r[RC::N2I] = ni2; r[RC::N1J] = nj1; r[RC::N2J] = nj2;
+#pragma unroll
+    for (int dir = 0; dir < 2; dir++) {  // 0: i-neighbour, 1: j-neighbour
+      const bool fwd = pass == 0;
+      const long long step = dir == 0 ? 1 : P;
+      const long long nb = fwd ? id - step : id + step;
+      const bool has = dir == 0 ? (fwd ? i > 1 : i < b.nx - 1) : (fwd ? j > 1 : j < b.ny - 1);
+      double Un[NV], Fo[NV], cc = 0.0, hh = 0.0;
+      if (has) {
+#pragma unroll
+        for (int m = 0; m < NV; m++) Un[m] = L.U[m * F + nb];
+        fn<NV>(Un, dir == 0 ? ni1 : nj1, dir == 0 ? ni2 : nj2, gm1, Fo);
+        cc = 0.5 * lc[(dir == 0 ? L_CI : L_CJ) * F + nb];
+        if (visc) cc += lc[(dir == 0 ? L_VI : L_VJ) * F + nb];
+        // forward: this cell's face length; backward: the neighbour's (the
+        // reference pairs the normal of face i with the length of face i+1,
+        // sub_LU_SGS.f90:87-88,95-96)
+        hh = 0.5 * g[(dir == 0 ? G_SI : G_SJ) * F + (fwd ? id : nb)];
+      } else {
+#pragma unroll
+        for (int m = 0; m < NV; m++) Fo[m] = 0.0;
+      }
+#pragma unroll
+      for (int m = 0; m < NV; m++) r[(dir == 0 ? RC::FI : RC::FJ) + m] = Fo[m];
+      r[dir == 0 ? RC::CI : RC::CJ] = cc;
+      r[dir == 0 ? RC::HI : RC::HJ] = hh;
+    }
+  }
+}
+
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// address of the same shared-memory location in CTA `rank` of the cluster
+__device__ __forceinline__ unsigned remote_smem(const void *p, unsigned rank) {
+  unsigned local = (unsigned)__cvta_generic_to_shared(p), remote;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(local), "r"(rank));
+  return remote;
+}
+__device__ __forceinline__ void st_remote2(unsigned addr, double a, double b) {
+  asm volatile("st.shared::cluster.v2.f64 [%0], {%1, %2};" ::"r"(addr), "d"(a), "d"(b) : "memory");
+}
+__device__ __forceinline__ void cp16(double *dst, const double *src) {
+  unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+template <int NV>
+__device__ __forceinline__ void fetch(double *dst, const double *src) {
+#pragma unroll
+  for (int k = 0; k < Rec<NV>::N; k += 2) cp16(dst + k, src + k);
+}
+
+// CS == 1: one CTA per block, planes separated by __syncthreads.
+// CS > 1: a cluster of CS CTAs per block, CTA r owns rows r*R+1..r*R+R; the
+// edge rows write into the neighbour CTA's halo slot through distributed
+// shared memory and planes are separated by a cluster barrier.
+template <int NV>
+__global__ void __launch_bounds__(1024) k_lusgs_sweep(Lvl L, int update, int R, int CS) {
+  using SL = Slot<NV>;
+  using RC = Rec<NV>;
+  constexpr int S = SL::S;
+  extern __shared__ __align__(16) double sh[];  // [2][R+2][S] slots, then [blockDim][2][RC::N] records
+  const unsigned rank = CS > 1 ? cluster_rank() : 0u;
+  const BlkDev bd = L.blk[blockIdx.x / CS];  // by value: no re-reads after global stores
+  const int nx = bd.nx, ny = bd.ny, rows = ny - 1, ni = nx - 1;
+  const long long off = bd.off, P = bd.P;
+  const int rl = threadIdx.x;
+  const int j = (int)rank * R + rl + 1;
+  const bool row_ok = rl < R && j <= rows;
+  const long long F = L.F;
+  const double gm1 = L.cs[bd.cas].gamma - 1.0;
+  double *rec = sh + (size_t)2 * (R + 2) * S + (size_t)threadIdx.x * 2 * RC::N;
+  const double *recF = L.rec + ((size_t)bd.cell0 + (size_t)(j - 1) * ni) * RC::N;   // row j, i = 1
+  const double *recB = recF + (size_t)L.ncell * RC::N;
+  double *recBw = L.rec + ((size_t)L.ncell + bd.cell0 + (size_t)(j - 1) * ni) * RC::N;
+  double st[S];
+#pragma unroll
+  for (int m = 0; m < S; m++) st[m] = 0.0;
+  for (int pass = 0; pass < 2; pass++) {
+    const bool fwd = pass == 0;
+    const double *rsrc = fwd ? recF : recB;
+    if (row_ok) fetch<NV>(rec, rsrc + (size_t)(fwd ? 0 : ni - 1) * RC::N);
+    cp_commit();
+    int k = 0;
+    for (int pp = 2; pp <= nx + ny - 2; pp++) {
+      const int p = fwd ? pp : nx + ny - pp;
+      const int i = p - j;
+      const int buf = p & 1;
+      if (row_ok && i >= 1 && i <= ni) {
+        const double *cur = rec + (k & 1) * RC::N;
+        const int inx = fwd ? i + 1 : i - 1;
+        if (inx >= 1 && inx <= ni) fetch<NV>(rec + ((k + 1) & 1) * RC::N, rsrc + (size_t)(inx - 1) * RC::N);
+        cp_commit();
+        cp_wait1();
+        double acc[NV], F2[NV];
+#pragma unroll
+        for (int m = 0; m < NV; m++) acc[m] = fwd ? cur[RC::A + m] : 0.0;
+        if (fwd ? (i > 1) : (i < ni)) {
+          fn_shipped<NV>(st, cur[RC::N1I], cur[RC::N2I], F2);
+          const double hh = cur[RC::HI], cc = cur[RC::CI];
+#pragma unroll
+          for (int m = 0; m < NV; m++) {
+            double DF = F2[m] - cur[RC::FI + m];
+            acc[m] = acc[m] + (fwd ? hh * DF : -hh * DF) + cc * st[SL::D + m];
+          }
+        }
+        if (fwd ? (j > 1) : (j < rows)) {
+          const double2 *s2 = reinterpret_cast<const double2 *>(sh + ((size_t)(buf ^ 1) * (R + 2) + (fwd ? rl : rl + 2)) * S);
+          double sn[S];
+#pragma unroll
+          for (int m = 0; m < S / 2; m++) { double2 v = s2[m]; sn[2 * m] = v.x; sn[2 * m + 1] = v.y; }
+          fn_shipped<NV>(sn, cur[RC::N1J], cur[RC::N2J], F2);
+          const double hh = cur[RC::HJ], cc = cur[RC::CJ];
+#pragma unroll
+          for (int m = 0; m < NV; m++) {
+            double DF = F2[m] - cur[RC::FJ + m];
+            acc[m] = acc[m] + (fwd ? hh * DF : -hh * DF) + cc * sn[SL::D + m];
+          }
+        }
+        const double ia = cur[RC::IA], ia5 = cur[RC::IA5];
+#pragma unroll
+        for (int m = 0; m < NV; m++) {
+          double inv = (NV == 5 && m == 4) ? ia5 : ia;
+          double d = fwd ? acc[m] * inv : cur[RC::A + m] + acc[m] * inv;
+          st[m] = cur[RC::U + m] + d;
+          st[SL::D + m] = d;
+        }
+        st[SL::R] = 1.0 / st[0];
+        st[SL::P] = gm1 * (st[3] - 0.5 * (st[1] * st[1] + st[2] * st[2]) * st[SL::R]);
+        double2 *own = reinterpret_cast<double2 *>(sh + ((size_t)buf * (R + 2) + rl + 1) * S);
+#pragma unroll
+        for (int m = 0; m < S / 2; m++) own[m] = make_double2(st[2 * m], st[2 * m + 1]);
+        if (CS > 1) {
+          if (fwd && rl == R - 1 && (int)rank + 1 < CS) {
+            unsigned a = remote_smem(sh + ((size_t)buf * (R + 2) + 0) * S, rank + 1);
+#pragma unroll
+            for (int m = 0; m < S / 2; m++) st_remote2(a + 16u * m, st[2 * m], st[2 * m + 1]);
+          }
+          if (!fwd && rl == 0 && rank > 0) {
+            unsigned a = remote_smem(sh + ((size_t)buf * (R + 2) + R + 1) * S, rank - 1);
+#pragma unroll
+            for (int m = 0; m < S / 2; m++) st_remote2(a + 16u * m, st[2 * m], st[2 * m + 1]);
+          }
+        }
+        if (fwd) {
+          // the forward dU becomes the A field of this cell's backward record
+          double *w = recBw + (size_t)(i - 1) * RC::N;
+#pragma unroll
+          for (int m = 0; m < NV; m++) w[RC::A + m] = st[SL::D + m];
+        } else {
+          const long long id = off + (long long)(j + 2) * P + (i + 2);
+#pragma unroll
+          for (int m = 0; m < NV; m++) {
+            L.du[m * F + id] = st[SL::D + m];
+            if (update) L.U[m * F + id] = st[m];
+          }
+        }
+        k++;
+      }
+      if (CS > 1) cluster_barrier();
+      else __syncthreads();
+    }
+    cp_wait0();
+  }
+}
+
+template <int NV>
+void sweep_nv(const Lvl &L, double alfa1, int update, int max_rows, int cs, cudaStream_t s) {
+  k_lusgs_prep<NV><<<L.ntiles, TILE, 0, s>>>(L, alfa1);
+  int CS = std::max(1, std::min(cs, std::min(8, (max_rows + 7) / 8)));
+  int R = (max_rows + CS - 1) / CS;
+  int th = ((R + 31) / 32) * 32;
+  size_t smem = ((size_t)2 * (R + 2) * Slot<NV>::S + (size_t)th * 2 * Rec<NV>::N) * sizeof(double);
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(k_lusgs_sweep<NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(L.nblk * CS);
+  cfg.blockDim = dim3(th);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CS;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_lusgs_sweep<NV>, L, update, R, CS);
+}
+
+void launch_lusgs_fast(const Lvl &L, double alfa1, int update, int max_rows, int cs, cudaStream_t s) {
+  if (L.nvar == 4) sweep_nv<4>(L, alfa1, update, max_rows, cs, s);
+  else if (L.nvar == 5) sweep_nv<5>(L, alfa1, update, max_rows, cs, s);
+  else sweep_nv<6>(L, alfa1, update, max_rows, cs, s);
+}
+
+}  // namespace ec2d

@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "lib", "libec2d_gpu.so")
-SOURCES = ["ec2d_api.cu", "k_residual.cu", "k_turb.cu", "k_bc.cu", "k_lusgs.cu", "k_misc.cu", "k_noalloc.cu"]
+SOURCES = ["ec2d_api.cu", "k_residual.cu", "k_turb.cu", "k_bc.cu", "k_lusgs.cu", "k_sweep.cu", "k_misc.cu", "k_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
