@@ -191,6 +191,14 @@ int ec2d_kernel_times(ec2d_ctx *ctx, char *buf, int buflen);
 #define EC2D_NOALLOC_MAX_CELLS 2097152
 int ec2d_residual_norms_noalloc(const double *res, int nvar, int ncell, double *out, void *stream);
 
+/* CUDA graphs for ec2d_step.  No counterpart in the reference.  When enabled
+ * (the default), the first ec2d_step records one pseudo-time step (single
+ * grid or V-cycle) as a CUDA graph and every step replays it: one launch per
+ * step instead of one per kernel, same kernels, same order, same results.
+ * Steps with dual time stepping or with kernel timing enabled launch kernels
+ * one by one.  enable = 0 switches to one-by-one launches. */
+int ec2d_set_graphs(ec2d_ctx *ctx, int enable);
+
 /* Wait for all queued work of the context. */
 int ec2d_sync(ec2d_ctx *ctx);
 

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -104,6 +105,13 @@ struct ec2d_ctx {
   long long launches = 0;
   int lusgs_cs = 1;  // CTAs per block in the LU-SGS wavefront (1: one CTA, >1: a cluster)
   bool timing = false;
+  // one pseudo-time step (single grid or V-cycle) captured as a CUDA graph:
+  // the replay stands for graph_launches kernel launches and advances the
+  // host step counters of level l graph_adv[l] times
+  bool use_graphs = true;
+  cudaGraphExec_t step_graph = nullptr;
+  long long graph_launches = 0;
+  int graph_adv[4] = {0, 0, 0, 0};
   struct KRec { const char *name; int level, nk; cudaEvent_t a, b; };
   std::vector<KRec> krec;
   std::vector<cudaEvent_t> evpool;
@@ -438,7 +446,7 @@ int build_level(ec2d_ctx *ctx, int l) {
   L.un1 = (P.Time_Method == Time_Dual && l == 1) ? dalloc<double>(lv, nv * F) : nullptr;
   L.fi = dalloc<double>(lv, 6 * F);
   L.fj = dalloc<double>(lv, 6 * F);
-  L.tb = (L.turb == Turb_SST) ? dalloc<double>(lv, 5 * F) : nullptr;
+  L.tb = (L.turb == Turb_SST) ? dalloc<double>(lv, 5 * F) : (L.turb == Turb_BL) ? dalloc<double>(lv, F) : nullptr;
   bool anyfdm = false;
   for (auto &B : lv.hb) anyfdm |= B.fdm;
   L.met = anyfdm ? dalloc<double>(lv, 5 * F) : nullptr;
@@ -562,6 +570,7 @@ void residual(ec2d_ctx *ctx, int l) {
   if (L.visc) {
     if (L.turb == Turb_SA) K(ctx, "sa", l, 4, [&] { launch_sa(L, s); });
     else if (L.turb == Turb_SST) K(ctx, "sst", l, 4, [&] { launch_sst(L, s); });
+    else if (L.turb == Turb_BL) K(ctx, "bl", l, 2, [&] { launch_bl(L, s); });
   }
   K(ctx, "k_flux_i", l, 1, [&] { launch_flux_i(L, s); });
   K(ctx, "k_flux_j", l, 1, [&] { launch_flux_j(L, s); });
@@ -730,6 +739,45 @@ void mg3(ec2d_ctx *ctx) {
   bc_all(ctx, 1);
 }
 
+int one_step(ec2d_ctx *ctx) {
+  if (ctx->num_mesh == 1) return time_advance(ctx, 1);
+  if (ctx->num_mesh == 2) mg2(ctx);
+  else mg3(ctx);
+  return EC2D_OK;
+}
+
+// Records one step into ctx->step_graph.  The orchestration runs once on the
+// host with the stream in capture mode, so its host-side effects (launch count,
+// step counters) are measured, undone, and re-applied on every replay.  If the
+// capture fails the context keeps launching kernels one by one.
+int capture_step(ec2d_ctx *ctx) {
+  std::vector<std::array<int, 4>> ks(ctx->cases.size());
+  std::vector<std::array<double, 4>> ts(ctx->cases.size());
+  for (size_t c = 0; c < ctx->cases.size(); c++)
+    for (int l = 0; l < 4; l++) { ks[c][l] = ctx->cases[c].kstep[l]; ts[c][l] = ctx->cases[c].tt[l]; }
+  long long n0 = ctx->launches;
+  CK(cudaGetLastError());
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  int r = one_step(ctx);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  if (r == EC2D_OK && e == cudaSuccess && g) e = cudaGraphInstantiate(&ctx->step_graph, g, 0);
+  if (g) cudaGraphDestroy(g);
+  ctx->graph_launches = ctx->launches - n0;
+  ctx->launches = n0;
+  for (int l = 1; l <= 3; l++) ctx->graph_adv[l] = ctx->cases.empty() ? 0 : ctx->cases[0].kstep[l] - ks[0][l];
+  for (size_t c = 0; c < ctx->cases.size(); c++)
+    for (int l = 0; l < 4; l++) { ctx->cases[c].kstep[l] = ks[c][l]; ctx->cases[c].tt[l] = ts[c][l]; }
+  if (r != EC2D_OK) return r;
+  if (e != cudaSuccess || !ctx->step_graph) {
+    fprintf(stderr, "ec2d: step capture failed (%s); launching kernels directly\n", cudaGetErrorString(e));
+    cudaGetLastError();
+    ctx->step_graph = nullptr;
+    ctx->use_graphs = false;
+  }
+  return EC2D_OK;
+}
+
 bool valid_case(ec2d_ctx *ctx, int c) { return ctx && c >= 1 && c <= (int)ctx->cases.size(); }
 
 // Fortran extents of the fields of ec2d_get_field
@@ -827,6 +875,7 @@ void ec2d_destroy(ec2d_ctx *ctx) {
   for (auto e : ctx->evpool) cudaEventDestroy(e);
   if (ctx->d_cases) cudaFree(ctx->d_cases);
   if (ctx->d_stage) cudaFree(ctx->d_stage);
+  if (ctx->step_graph) cudaGraphExecDestroy(ctx->step_graph);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -894,7 +943,6 @@ int ec2d_setup(ec2d_ctx *ctx) {
   if ((P.Time_Method == Time_LU_SGS && P.Num_Mesh != 1 && !P.mg_lusgs) ||
       (P.Time_Method == Time_Dual && P.Num_Mesh != 1))
     return EC2D_ERR_UNSUPPORTED;
-  if (P.If_viscous && P.Iflag_turbulence_model == Turb_BL) return EC2D_ERR_UNSUPPORTED;
   if (P.Iflag_turbulence_model != Turb_NONE && !P.If_viscous) return EC2D_ERR_UNSUPPORTED;
   int nm = 3;
   for (auto &c : ctx->cases) nm = std::min(nm, mg_depth(c));
@@ -994,12 +1042,30 @@ int ec2d_download_U(ec2d_ctx *ctx, int case_id, int mesh, int block, double *U) 
 int ec2d_step(ec2d_ctx *ctx, int nsteps) {
   if (!ctx || !ctx->setup_done || nsteps < 0) return EC2D_ERR_ARG;
   cudaSetDevice(ctx->device);
+  // dual time reads norms on the host inside the step; timing records events
+  bool graph = ctx->use_graphs && !ctx->timing && ctx->P.Time_Method != Time_Dual && nsteps > 0;
+  if (graph && !ctx->step_graph) {
+    int r = capture_step(ctx);
+    if (r) return r;
+  }
   for (int n = 0; n < nsteps; n++) {
-    if (ctx->num_mesh == 1) { int r = time_advance(ctx, 1); if (r) return r; }
-    else if (ctx->num_mesh == 2) mg2(ctx);
-    else mg3(ctx);
+    if (graph && ctx->step_graph) {
+      CK(cudaGraphLaunch(ctx->step_graph, ctx->stream));
+      ctx->launches += ctx->graph_launches;
+      for (int l = 1; l <= 3; l++)
+        for (int k = 0; k < ctx->graph_adv[l]; k++) advance_counters(ctx, l);
+      continue;
+    }
+    int r = one_step(ctx);
+    if (r) return r;
   }
   return check_launch(ctx);
+}
+
+int ec2d_set_graphs(ec2d_ctx *ctx, int enable) {
+  if (!ctx) return EC2D_ERR_ARG;
+  ctx->use_graphs = enable != 0;
+  return EC2D_OK;
 }
 
 int ec2d_residual(ec2d_ctx *ctx, int case_id, int mesh, double res_max[6], double res_rms[6], int *kstep,

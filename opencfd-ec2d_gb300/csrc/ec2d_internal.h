@@ -17,6 +17,7 @@ void launch_norms(const Lvl &L, const int *case_tile0, const int *case_ntile, co
 // k_turb.cu
 void launch_sa(const Lvl &L, cudaStream_t s);
 void launch_sst(const Lvl &L, cudaStream_t s);
+void launch_bl(const Lvl &L, cudaStream_t s);
 void launch_amut_boundary(const Lvl &L, cudaStream_t s);
 void launch_fdm(const Lvl &L, cudaStream_t s);
 void launch_dual_term(const Lvl &L, double sfac, cudaStream_t s);

@@ -111,6 +111,7 @@ def lib():
         "ec2d_launch_count": ([vp, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
         "ec2d_kernel_timing": ([vp, ctypes.c_int], ctypes.c_int),
         "ec2d_kernel_times": ([vp, ctypes.c_char_p, ctypes.c_int], ctypes.c_int),
+        "ec2d_set_graphs": ([vp, ctypes.c_int], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -273,6 +274,10 @@ class Solver:
         n = ctypes.c_longlong()
         _ck(self.L.ec2d_launch_count(self.h, ctypes.byref(n)), "ec2d_launch_count")
         return n.value
+
+    def set_graphs(self, enable=True):
+        """Replay each step as one CUDA graph (default) or launch kernels one by one."""
+        _ck(self.L.ec2d_set_graphs(self.h, 1 if enable else 0), "ec2d_set_graphs")
 
     def kernel_timing(self, enable=True):
         _ck(self.L.ec2d_kernel_timing(self.h, 1 if enable else 0), "ec2d_kernel_timing")

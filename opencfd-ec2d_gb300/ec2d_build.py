@@ -12,7 +12,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "lib", "libec2d_gpu.so")
-SOURCES = ["ec2d_api.cu", "k_residual.cu", "k_turb.cu", "k_bc.cu", "k_lusgs.cu", "k_sweep.cu", "k_misc.cu", "k_noalloc.cu"]
+SOURCES = ["ec2d_api.cu", "k_residual.cu", "k_turb.cu", "k_bl.cu", "k_bc.cu", "k_lusgs.cu", "k_sweep.cu", "k_misc.cu",
+           "k_noalloc.cu"]
+# per-file flags: the Baldwin-Lomax switch is discrete, so its products and
+# sums are rounded one by one like the reference's
+FILE_FLAGS = {"k_bl.cu": ["-fmad=false"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
@@ -43,7 +47,7 @@ def build(verbose: bool = False, extra=()) -> str:
         obj = os.path.join(OUT, s.replace(".cu", ".o"))
         objs.append(obj)
         if _stale(obj, [src] + headers):
-            jobs.append([nvcc(), *ARCH, *FLAGS, *extra, "-c", src, "-o", obj])
+            jobs.append([nvcc(), *ARCH, *FLAGS, *FILE_FLAGS.get(s, []), *extra, "-c", src, "-o", obj])
 
     def run(cmd):
         if verbose:
