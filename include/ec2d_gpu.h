@@ -199,6 +199,15 @@ int ec2d_residual_norms_noalloc(const double *res, int nvar, int ncell, double *
  * one by one.  enable = 0 switches to one-by-one launches. */
 int ec2d_set_graphs(ec2d_ctx *ctx, int enable);
 
+/* Precision of the LU-SGS sweeps (du_LU_SGS_2D) on every level: 64 (the
+ * default, the reference's arithmetic) or 32.  No counterpart in the
+ * reference.  With 32 the sweeps run in float from records built in FP64
+ * (Res, 1/alfa, spectral radii and the state rounded to float, the flux
+ * difference in increment form), and U stays FP64 (U += (double)dU); the
+ * residual, boundary conditions, multigrid transfers, norms and forces stay
+ * FP64, so the converged state is that of the FP64 discretisation. */
+int ec2d_set_lusgs_precision(ec2d_ctx *ctx, int bits);
+
 /* Wait for all queued work of the context. */
 int ec2d_sync(ec2d_ctx *ctx);
 

@@ -78,6 +78,7 @@ struct Level {
   std::vector<int> case_face0, case_nface;
   long long F = 0;
   int max_rows = 0;   // widest block (ny-1) of the level: LU-SGS threads per CTA
+  bool fast64 = false, fast32 = false;  // wavefront LU-SGS fits one CTA (FP64 / FP32 records)
   Lvl L{};
   int *d_case_tile0 = nullptr, *d_case_ntile = nullptr, *d_case_ncell = nullptr;
   int4 *d_faces = nullptr;
@@ -104,6 +105,7 @@ struct ec2d_ctx {
   // launch accounting and optional per-kernel event timing
   long long launches = 0;
   int lusgs_cs = 1;  // CTAs per block in the LU-SGS wavefront (1: one CTA, >1: a cluster)
+  bool lusgs_fp32 = false;  // LU-SGS sweeps in FP32 (mixed-precision mode)
   bool timing = false;
   // one pseudo-time step (single grid or V-cycle) captured as a CUDA graph:
   // the replay stands for graph_launches kernel launches and advances the
@@ -452,7 +454,11 @@ int build_level(ec2d_ctx *ctx, int l) {
   L.met = anyfdm ? dalloc<double>(lv, 5 * F) : nullptr;
   L.fdm = anyfdm ? dalloc<double>(lv, 30 * F) : nullptr;
   for (auto &B : lv.hb) lv.max_rows = std::max(lv.max_rows, B.ny - 1);
-  L.rec = (lv.max_rows <= 1024) ? dalloc<double>(lv, (size_t)2 * L.ncell * lusgs_planes(nv)) : nullptr;
+  // wavefront LU-SGS: one thread per row, its shared memory must fit one CTA
+  const size_t smem_max = 227 * 1024;
+  lv.fast64 = lv.max_rows <= 1024 && lusgs_smem(nv, lv.max_rows) <= smem_max;
+  lv.fast32 = lv.max_rows <= 1024 && lusgs32_smem(nv, lv.max_rows) <= smem_max;
+  L.rec = (lv.fast64 || lv.fast32) ? dalloc<double>(lv, (size_t)2 * L.ncell * lusgs_planes(nv)) : nullptr;
   L.npart = dalloc<double>(lv, lv.tiles.size() * 12);
   L.norms = dalloc<double>(lv, ncase * 12);
   L.status = dalloc<int>(lv, ncase * 4);
@@ -615,9 +621,12 @@ void step_rk3(ec2d_ctx *ctx, int l) {
 // (sub_NS_singlegrid.f90:196-213): the wavefront kernels fuse the update into
 // the backward sweep; blocks wider than 1024 rows take the generic kernel
 void lusgs_update(ec2d_ctx *ctx, int l, double alfa1) {
-  const Lvl &L = ctx->lv[l].L;
-  if (L.rec) {
-    K(ctx, "k_lusgs", l, 2, [&] { launch_lusgs_fast(L, alfa1, 1, ctx->lv[l].max_rows, ctx->lusgs_cs, ctx->stream); });
+  const Level &lv = ctx->lv[l];
+  const Lvl &L = lv.L;
+  if (ctx->lusgs_fp32 && lv.fast32) {
+    K(ctx, "k_lusgs32", l, 2, [&] { launch_lusgs_fast32(L, alfa1, 1, lv.max_rows, ctx->stream); });
+  } else if (lv.fast64) {
+    K(ctx, "k_lusgs", l, 2, [&] { launch_lusgs_fast(L, alfa1, 1, lv.max_rows, ctx->lusgs_cs, ctx->stream); });
   } else {
     K(ctx, "k_lusgs_generic", l, 1, [&] { launch_lusgs(L, alfa1, ctx->stream); });
     K(ctx, "k_add_du", l, 1, [&] { launch_add_du(L, ctx->stream); });
@@ -1068,6 +1077,19 @@ int ec2d_set_graphs(ec2d_ctx *ctx, int enable) {
   return EC2D_OK;
 }
 
+int ec2d_set_lusgs_precision(ec2d_ctx *ctx, int bits) {
+  if (!ctx || (bits != 32 && bits != 64)) return EC2D_ERR_ARG;
+  bool fp32 = bits == 32;
+  if (fp32 != ctx->lusgs_fp32 && ctx->step_graph) {
+    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaGraphExecDestroy(ctx->step_graph);
+    ctx->step_graph = nullptr;
+  }
+  ctx->lusgs_fp32 = fp32;
+  return EC2D_OK;
+}
+
 int ec2d_residual(ec2d_ctx *ctx, int case_id, int mesh, double res_max[6], double res_rms[6], int *kstep,
                   double *tt) {
   if (!ctx || !ctx->setup_done || !valid_case(ctx, case_id) || mesh < 1 || mesh > ctx->num_mesh) return EC2D_ERR_ARG;
@@ -1228,8 +1250,10 @@ int ec2d_update_buffer(ec2d_ctx *ctx, int mesh) {
 int ec2d_du_lusgs(ec2d_ctx *ctx, int mesh, double alfa1) {
   if (!ctx || !ctx->setup_done || mesh < 1 || mesh > ctx->num_mesh) return EC2D_ERR_ARG;
   cudaSetDevice(ctx->device);
-  const Lvl &L = ctx->lv[mesh].L;
-  if (L.rec) launch_lusgs_fast(L, alfa1, 0, ctx->lv[mesh].max_rows, ctx->lusgs_cs, ctx->stream);
+  const Level &lv = ctx->lv[mesh];
+  const Lvl &L = lv.L;
+  if (ctx->lusgs_fp32 && lv.fast32) launch_lusgs_fast32(L, alfa1, 0, lv.max_rows, ctx->stream);
+  else if (lv.fast64) launch_lusgs_fast(L, alfa1, 0, lv.max_rows, ctx->lusgs_cs, ctx->stream);
   else launch_lusgs(L, alfa1, ctx->stream);
   return check_launch(ctx);
 }

@@ -28,6 +28,10 @@ void launch_lusgs(const Lvl &L, double alfa1, cudaStream_t s);
 // k_sweep.cu
 int lusgs_planes(int nv);
 void launch_lusgs_fast(const Lvl &L, double alfa1, int update, int max_rows, int cs, cudaStream_t s);
+size_t lusgs_smem(int nv, int rows);  // dynamic shared memory of the one-CTA FP64 sweep
+void launch_lusgs_fast32(const Lvl &L, double alfa1, int update, int max_rows, cudaStream_t s);
+size_t lusgs32_smem(int nv, int rows);
+size_t lusgs32_record_bytes(int nv);
 void launch_add_du(const Lvl &L, cudaStream_t s);
 void launch_euler(const Lvl &L, int force, cudaStream_t s);
 void launch_rk3(const Lvl &L, int stage, int force, cudaStream_t s);

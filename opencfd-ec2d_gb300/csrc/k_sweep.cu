@@ -322,6 +322,13 @@ void sweep_nv(const Lvl &L, double alfa1, int update, int max_rows, int cs, cuda
   cudaLaunchKernelEx(&cfg, k_lusgs_sweep<NV>, L, update, R, CS);
 }
 
+template <int NV>
+size_t smem_nv(int rows) {
+  int th = ((rows + 31) / 32) * 32;
+  return ((size_t)2 * (rows + 2) * Slot<NV>::S + (size_t)th * 2 * Rec<NV>::N) * sizeof(double);
+}
+size_t lusgs_smem(int nv, int rows) { return nv == 4 ? smem_nv<4>(rows) : nv == 5 ? smem_nv<5>(rows) : smem_nv<6>(rows); }
+
 void launch_lusgs_fast(const Lvl &L, double alfa1, int update, int max_rows, int cs, cudaStream_t s) {
   if (L.nvar == 4) sweep_nv<4>(L, alfa1, update, max_rows, cs, s);
   else if (L.nvar == 5) sweep_nv<5>(L, alfa1, update, max_rows, cs, s);

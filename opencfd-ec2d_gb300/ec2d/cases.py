@@ -35,9 +35,10 @@ def euler_naca0012(nx=257, ny=65):
 def laminar_flat_plate(nxb=97, ny=97, num_mesh=3):
     """Laminar flat plate, 2-block 193x97 H-grid, dy1 = 1e-4, ratio 1.1,
     M 0.3, Re 1e4, adiabatic wall, AUSM+ + MUSCL, 3-level V-cycle with
-    LU-SGS smoothing."""
+    LU-SGS smoothing; free-stream back pressure at the exit face."""
     p = Params(Ma=0.3, AoA=0.0, Re=1.0e4, Pr=0.72, If_viscous=1, Iflag_turbulence_model=TURB_NONE,
                Iflag_local_dt=1, CFL=10.0, dtmax=1.0e3, dtmin=1.0e-12, Time_Method=TIME_LUSGS,
+               P_outlet=1.0 / (1.4 * 0.3 ** 2),
                Iflag_Scheme=SCHEME["MUSCL3"], Iflag_flux=FLUX["AUSM"], IFlag_Reconstruction=0,
                Num_Mesh=num_mesh, Twall=-1.0, T_inf=288.15, mg_lusgs=1, xaxis=0.0, yaxis=0.0)
     blocks = grids.flat_plate(nxb, ny, first=1.0e-4, ratio=1.1, x_lead=0.5, plate=1.0)

@@ -112,6 +112,7 @@ def lib():
         "ec2d_kernel_timing": ([vp, ctypes.c_int], ctypes.c_int),
         "ec2d_kernel_times": ([vp, ctypes.c_char_p, ctypes.c_int], ctypes.c_int),
         "ec2d_set_graphs": ([vp, ctypes.c_int], ctypes.c_int),
+        "ec2d_set_lusgs_precision": ([vp, ctypes.c_int], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -278,6 +279,10 @@ class Solver:
     def set_graphs(self, enable=True):
         """Replay each step as one CUDA graph (default) or launch kernels one by one."""
         _ck(self.L.ec2d_set_graphs(self.h, 1 if enable else 0), "ec2d_set_graphs")
+
+    def set_lusgs_precision(self, bits):
+        """64 (default) or 32: arithmetic of the LU-SGS sweeps on every level."""
+        _ck(self.L.ec2d_set_lusgs_precision(self.h, int(bits)), "ec2d_set_lusgs_precision")
 
     def kernel_timing(self, enable=True):
         _ck(self.L.ec2d_kernel_timing(self.h, 1 if enable else 0), "ec2d_kernel_timing")

@@ -20,7 +20,7 @@ from typing import List, Tuple
 
 import numpy as np
 
-from .inputs import BC_FARFIELD, BC_SYMMETRY, BC_WALL, Block
+from .inputs import BC_FARFIELD, BC_OUTLET, BC_SYMMETRY, BC_WALL, Block
 
 
 def naca4(m: float, p: float, t: float, xc: np.ndarray) -> Tuple[np.ndarray, np.ndarray]:
@@ -206,9 +206,12 @@ def split_cgrid(X: np.ndarray, Y: np.ndarray, n_wake: int, nblocks: int) -> List
 
 
 def flat_plate(nx_block: int = 97, ny: int = 97, first: float = 1.0e-4, ratio: float = 1.1,
-               x_lead: float = 0.5, plate: float = 1.0) -> List[Block]:
+               x_lead: float = 0.5, plate: float = 1.0, outlet: int = BC_OUTLET) -> List[Block]:
     """2-block H-grid: block 1 over [-x_lead, 0] (symmetry floor), block 2 over
-    [0, plate] (no-slip wall); geometric wall-normal stretching."""
+    [0, plate] (no-slip wall); geometric wall-normal stretching.  The exit face
+    is a back-pressure outlet (BC_OUTLET, with P_outlet > 0 in control.in): a
+    far-field face there extrapolates every variable on subsonic outflow
+    (sub_boundary.f90:529-531), which leaves the exit pressure floating."""
     yj = np.concatenate([[0.0], np.cumsum(first * ratio ** np.arange(ny - 1))])
     # streamwise: cluster at the leading edge x=0 from both sides
     s = _tanh_dist(nx_block, 2.0e-3)
@@ -223,7 +226,7 @@ def flat_plate(nx_block: int = 97, ny: int = 97, first: float = 1.0e-4, ratio: f
              [4, 4, 1, n, ny, ny, BC_FARFIELD, 0, 0]]
     b2.bc = [[1, 1, 1, 1, 1, ny, 1, 3, 2],
              [2, 2, 1, n, 1, 1, BC_WALL, 0, 0],
-             [3, 3, n, n, 1, ny, BC_FARFIELD, 0, 0],
+             [3, 3, n, n, 1, ny, outlet, 0, 0],
              [4, 4, 1, n, ny, ny, BC_FARFIELD, 0, 0]]
     return [b1, b2]
 
