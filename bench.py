@@ -155,36 +155,124 @@ def run_reference(args, rank, world):
     dt = time.perf_counter() - t0
     cells = fine_cells(blocks)
     v = cells * args.steps / dt
+    ttd = None
+    if args.drop_cap > 0:
+        # the same freestream-start drop as the GPU arm, bounded by 2x the cap
+        cap = 2.0 * args.drop_cap
+        orc.init_flow()
+        t0 = time.perf_counter()
+        orc.step(1)
+        r0 = orc.norms()[1][0]
+        it, r = 1, r0
+        while r > 1e-8 * r0 and time.perf_counter() - t0 < cap:
+            orc.step(25)
+            it += 25
+            r = orc.norms()[1][0]
+        tdrop = time.perf_counter() - t0
+        ttd = {"fp64": {"target": 1e-8, "iterations": it, "seconds": tdrop, "drop": r / r0,
+                        "reached": bool(r <= 1e-8 * r0), "cap_s": cap}}
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "cells": cells, "step": "one 3-level V-cycle"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{args.steps} V-cycles after {args.warmup} warm-up cycles"},
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "time_to_drop": ttd}
     print(json.dumps(line), flush=True)
 
 
-def time_to_drop(g, cells, cap_s=30.0, check=25, target=1e-8):
+def time_to_drop(g, cells, cap_s=60.0, target=1e-8, check=25):
     """Iterations and wall time from the freestream start until the
-    continuity RMS residual drops below target x its first-iteration value."""
+    continuity RMS residual drops below target x its first-iteration value,
+    through the library's own iterate-to-drop call (ec2d_run_to_drop)."""
     g.init_flow()
     g.sync()
     t0 = time.perf_counter()
-    g.step(1)
-    r0 = g.norms()[1][0]
-    it, r = 1, r0
-    while r > target * r0 and time.perf_counter() - t0 < cap_s:
-        g.step(check)
-        it += check
-        r = g.norms()[1][0]
+    it, ratio, _ = g.run_to_drop(drop=target, max_seconds=cap_s, check_every=check)
     dt = time.perf_counter() - t0
-    return {"iterations": it, "seconds": dt, "drop": r / r0, "reached": bool(r <= target * r0),
-            "cell_updates_per_s": cells * it / dt}
+    return {"target": target, "iterations": it, "seconds": dt, "drop": ratio, "reached": bool(ratio <= target),
+            "cell_updates_per_s": cells * it / dt, "cap_s": cap_s}
+
+
+# DRAM bytes per launch measured by ncu for the dominant kernel on this
+# workload (profiles/lusgs_sweep_flat_plate_97x97.md: dram__bytes_read.sum +
+# dram__bytes_write.sum of k_lusgs_sweep<4> on the fine level)
+PROFILED_TRAFFIC = {("k_lusgs", 1): 7388928.0}
+SWEEP_PLANES = lambda blocks, lev: 2 * max((b.nx - 1) // 2 ** (lev - 1) + (b.ny - 1) // 2 ** (lev - 1) - 1
+                                         for b in blocks)
+
+
+def timed_steps(torch, g, stream, flush, steps):
+    """K steps, each bracketed by CUDA events on the solver's stream, with a
+    512 MiB L2 flush before each.  Returns total ms and launches per step."""
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    n0 = g.launch_count()
+    for k in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ev[k][0].record(stream)
+        g.step(1)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in ev), (g.launch_count() - n0) // steps
+
+
+def kernel_table(g, torch, flush, steps):
+    """Per-kernel CUDA-event times of `steps` steps (launched one by one)."""
+    g.kernel_timing(True)
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        g.step(1)
+    kt = g.kernel_times()
+    g.kernel_timing(False)
+    return kt
+
+
+def residual_hbm(torch, gpu, dev, reps=10):
+    """Residual evaluation (Comput_Residual_one_mesh) on a grid far larger
+    than L2: 2 blocks of 2049x1025 nodes (4.19 M cells), laminar flat-plate
+    physics, a perturbed state.  Achieved = algorithmic bytes of the
+    residual (176 B per cell: read U, 7 metrics, x1, y1; write Res, dt and
+    the 4 spectral radii) / CUDA-event time of the whole residual stage."""
+    import numpy as np
+    from ec2d import cases, grids
+    p, _ = cases.laminar_flat_plate(33, 33, num_mesh=1)
+    blocks = grids.flat_plate(2049, 1025, first=1.0e-4, ratio=1.0065)
+    cells = fine_cells(blocks)
+    g = gpu.Solver([(p, blocks)], device=dev)
+    g.init_flow()
+    rng = np.random.default_rng(7)
+    for b in range(1, len(blocks) + 1):
+        U = g.download_U(1, 1, b)
+        U *= 1.0 + 0.01 * rng.standard_normal(U.shape[1:])[None]
+        g.upload_U(1, 1, b, U)
+    g.bc()
+    for _ in range(2):
+        g.residual()
+    g.sync()
+    g.kernel_timing(True)
+    for _ in range(reps):
+        g.residual()
+    kt = g.kernel_times()
+    g.kernel_timing(False)
+    g.close()
+    total_ms = sum(v[2] for v in kt.values()) / reps
+    hbm, kind = peaks()
+    achieved = 176.0 * cells / (total_ms / 1e3) / 1e9
+    per = {}
+    for (name, lev), (calls, _, ms) in kt.items():
+        bpu = BYTES_PER_UNIT.get(name)
+        t = ms / calls
+        per[name] = {"us": round(t * 1e3, 1), "gbs": round(bpu * cells / (t / 1e3) / 1e9, 1) if bpu else None}
+    return {"cells": cells, "grid": "2 x 2049x1025 (flat plate, 4.19 M cells)", "ms": total_ms,
+            "algorithmic_bytes_per_cell": 176, "achieved_gbs": achieved, "peak_gbs": hbm, "frac": achieved / hbm,
+            "peak_source": f"{kind} hbm_gbs", "kernels": per,
+            "note": "FP64 arithmetic bounds this stage: see the per-kernel FP64-pipe utilisation in profiles/"}
 
 
 def run_gb300(args, rank, world):
-    import numpy as np
     import torch
     from ec2d import gpu
 
@@ -197,6 +285,7 @@ def run_gb300(args, rank, world):
     p, blocks = build_case()
     cells = fine_cells(blocks)
     g = gpu.Solver([(p, blocks)], device=dev)
+    g.set_lusgs_precision(64)
     g.init_flow()
     stream = torch.cuda.ExternalStream(g.stream_handle())
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
@@ -210,36 +299,24 @@ def run_gb300(args, rank, world):
             dist.barrier()
         torch.cuda.synchronize()
 
-    # ---- device-timed region: K V-cycles, L2 flushed before each ----------
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    n0 = g.launch_count()
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], device=f"cuda:{dev}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- device-timed region: K V-cycles (FP64), L2 flushed before each -----
     barrier()
     with ClockSampler(dev) as clk:
-        for k in range(args.steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            ev[k][0].record(stream)
-            g.step(1)
-            ev[k][1].record(stream)
-        torch.cuda.synchronize()
+        ms, launches = timed_steps(torch, g, stream, flush, args.steps)
     barrier()
-    launches = (g.launch_count() - n0) // args.steps
-    ms = sum(a.elapsed_time(b) for a, b in ev)
     clocks = clk.summary()
-    if dist is not None:
-        t = torch.tensor([ms], device=f"cuda:{dev}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms)
     value = cells * args.steps * world / (ms / 1e3)
 
-    # ---- per-kernel event timing (same K cycles, separate pass) -----------
-    g.kernel_timing(True)
-    for k in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        g.step(1)
-    kt = g.kernel_times()
-    g.kernel_timing(False)
+    # ---- per-kernel event timing (same K cycles, separate pass) -------------
+    kt = kernel_table(g, torch, flush, args.steps)
     hbm, peak_kind = peaks()
     best = max(kt.items(), key=lambda kv: kv[1][2])
     (kname, klev), (kcalls, knk, kms) = best
@@ -254,12 +331,34 @@ def run_gb300(args, rank, world):
     avg_ms = kms / kcalls
     achieved = bpu * units / (avg_ms / 1e3) / 1e9 if bpu else None
     roofline = {"bound": "hbm", "kernel": f"{kname} (mesh {klev})", "achieved": achieved, "peak": hbm,
-                "unit": "GB/s", "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                "unit": "GB/s", "frac": (achieved / hbm) if achieved else None,
+                "traffic": PROFILED_TRAFFIC.get((kname, klev)),
                 "peak_source": f"{peak_kind} hbm_gbs", "avg_launch_us": avg_ms * 1e3,
                 "bytes_per_launch": bpu * units,
                 "share_of_step": kms / sum(v[2] for v in kt.values()),
                 "kernels": {f"{n}@{l}": {"calls": c, "ms_total": round(m, 4)} for (n, l), (c, _, m) in
                             sorted(kt.items(), key=lambda kv: -kv[1][2])[:12]}}
+    if kname == "k_lusgs":
+        mhz = clocks.get("sm_mhz") or 2070.0
+        roofline["cycles_per_plane"] = avg_ms * 1e-3 * mhz * 1e6 / SWEEP_PLANES(blocks, klev)
+        roofline["latency_note"] = ("wavefront sweep: one dependent chain of FP64 operations per hyperplane, "
+                                    "FP64 warp instruction latency 64 cycles on this part")
+
+    # ---- mixed precision: the same V-cycle with FP32 LU-SGS sweeps ----------
+    g.set_lusgs_precision(32)
+    for _ in range(3):
+        g.step(1)
+    g.sync()
+    barrier()
+    ms32, launches32 = timed_steps(torch, g, stream, flush, args.steps)
+    barrier()
+    ms32 = max_over_ranks(ms32)
+    kt32 = kernel_table(g, torch, flush, args.steps)
+    mixed = {"value": cells * args.steps * world / (ms32 / 1e3), "ms_per_step": ms32 / args.steps,
+             "lusgs": "fp32", "residual": "fp64",
+             "kernels": {f"{n}@{l}": round(m / args.steps, 4) for (n, l), (c, _, m) in
+                         sorted(kt32.items(), key=lambda kv: -kv[1][2])[:8]}}
+    g.set_lusgs_precision(64)
 
     # ---- end to end through the C-ABI with host buffers --------------------
     nbl = len(blocks)
@@ -281,23 +380,40 @@ def run_gb300(args, rank, world):
             g.upload_U(1, 1, b, host[b - 1][1])
         g.step(1)
         g.norms(1, 1)
-    t_e2e = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([t_e2e], device=f"cuda:{dev}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e = float(t.item())
+    t_e2e = max_over_ranks(time.perf_counter() - t0)
     e2e = {"value": cells * args.steps * world / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h}
 
-    ttd = time_to_drop(g, cells, cap_s=args.drop_cap) if args.drop_cap > 0 else None
+    # ---- time to a 1e-8 drop from the freestream start ----------------------
+    ttd = None
+    if args.drop_cap > 0:
+        ttd = {"fp64": time_to_drop(g, cells, cap_s=args.drop_cap)}
+        cl, cd, cm = g.forces(1)
+        ttd["fp64"]["forces"] = {"cl": cl, "cd": cd, "cm": cm}
+        g.set_lusgs_precision(32)
+        ttd["mixed"] = time_to_drop(g, cells, cap_s=args.drop_cap)
+        cl2, cd2, cm2 = g.forces(1)
+        ttd["mixed"]["forces"] = {"cl": cl2, "cd": cd2, "cm": cm2}
+        ttd["mixed"]["force_error_vs_fp64"] = max(abs(cl2 - cl), abs(cd2 - cd), abs(cm2 - cm))
+        g.set_lusgs_precision(64)
     cl, cd, cm = g.forces(1)
+    g.close()
+
+    big = None
+    if args.residual_hbm and rank == 0:
+        big = residual_hbm(torch, gpu, dev)
 
     if rank == 0:
         cpu = None
         if world == 1 and not args.no_cpu_baseline:
             rate, thr, n, dt = cpu_port_rate(p, blocks, seconds=args.cpu_seconds)
             cpu = {"value": rate, "unit": UNIT, "cores": thr, "kind": "port",
-                   "sample": f"{n} V-cycles of the same workload ({dt:.1f} s) on the C++ restatement"}
+                   "sample": f"{n} V-cycles of the same workload ({dt:.1f} s) on the C++ restatement",
+                   "seconds_per_step": dt / n}
+            if ttd and ttd["fp64"]["reached"]:
+                cpu["time_to_drop_estimate_s"] = dt / n * ttd["fp64"]["iterations"]
+                cpu["time_to_drop_basis"] = ("CPU seconds per V-cycle x the V-cycles the FP64 GPU run needed "
+                                             "(same arithmetic, same iteration count)")
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -305,9 +421,9 @@ def run_gb300(args, rank, world):
                            "l2": "flushed before every timed step (512 MiB write)", "parallelism": f"replicas{world}"},
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
                 "gpu_launches": launches * args.steps, "launches_per_step": launches,
-                "time_to_drop": ttd, "forces": {"cl": cl, "cd": cd, "cm": cm}}
+                "mixed_precision": mixed, "time_to_drop": ttd, "residual_hbm": big,
+                "forces": {"cl": cl, "cd": cd, "cm": cm}}
         print(json.dumps(line), flush=True)
-    g.close()
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()
@@ -321,10 +437,19 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--drop-cap", type=float, default=30.0)
+    ap.add_argument("--drop-cap", type=float, default=60.0, help="seconds per time-to-drop run (0: skip)")
+    ap.add_argument("--no-residual-hbm", dest="residual_hbm", action="store_false",
+                    help="skip the residual bandwidth measurement on the 4.19 M-cell grid")
+    ap.add_argument("--leg", default="all", choices=["all", "residual_hbm"],
+                    help="residual_hbm: only the 4.19 M-cell residual measurement (for profiling)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if args.leg == "residual_hbm":
+        import torch
+        from ec2d import gpu
+        print(json.dumps({"residual_hbm": residual_hbm(torch, gpu, 0)}), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
     else:

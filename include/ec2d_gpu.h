@@ -136,6 +136,19 @@ int ec2d_step(ec2d_ctx *ctx, int nsteps);
 int ec2d_residual(ec2d_ctx *ctx, int case_id, int mesh, double res_max[6], double res_rms[6],
                   int *kstep, double *tt);
 
+/* Iterate to a residual drop.  No counterpart in the reference, whose main
+ * loop runs to t_end (opencfd_ec2d_v1.5.4.f90:172-186).  Steps until every
+ * case's continuity RMS residual MP%Res_rms(1) of the fine mesh is at most
+ * `drop` times its reference value, checking every `check_every` steps (one
+ * device-to-host read of the norms per check).  r0: per-case reference
+ * values (ncase doubles), or NULL to take the residual of the first step of
+ * this call.  Stops early after max_steps steps or max_seconds of wall time
+ * (<= 0: no limit).  Outputs: steps taken, the worst case's Res_rms(1)/r0,
+ * and the wall time in seconds.  Returns EC2D_ERR_STATE if a case hit the
+ * T<1e-5 stop. */
+int ec2d_run_to_drop(ec2d_ctx *ctx, double drop, const double *r0, int max_steps, double max_seconds,
+                     int check_every, int *steps, double *worst_ratio, double *seconds);
+
 /* Status word of a case: code (0 ok, 3 = T<1e-5) and the block/cell. */
 int ec2d_status(ec2d_ctx *ctx, int case_id, int *code, int *block, int *i, int *j);
 

@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -624,7 +625,7 @@ void lusgs_update(ec2d_ctx *ctx, int l, double alfa1) {
   const Level &lv = ctx->lv[l];
   const Lvl &L = lv.L;
   if (ctx->lusgs_fp32 && lv.fast32) {
-    K(ctx, "k_lusgs32", l, 2, [&] { launch_lusgs_fast32(L, alfa1, 1, lv.max_rows, ctx->stream); });
+    K(ctx, "k_lusgs32", l, 3, [&] { launch_lusgs_fast32(L, alfa1, 1, lv.max_rows, ctx->stream); });
   } else if (lv.fast64) {
     K(ctx, "k_lusgs", l, 2, [&] { launch_lusgs_fast(L, alfa1, 1, lv.max_rows, ctx->lusgs_cs, ctx->stream); });
   } else {
@@ -1105,6 +1106,52 @@ int ec2d_residual(ec2d_ctx *ctx, int case_id, int mesh, double res_max[6], doubl
   if (kstep) *kstep = ctx->cases[case_id - 1].kstep[mesh];
   if (tt) *tt = ctx->cases[case_id - 1].tt[mesh];
   return st[0] ? EC2D_ERR_STATE : EC2D_OK;
+}
+
+int ec2d_run_to_drop(ec2d_ctx *ctx, double drop, const double *r0, int max_steps, double max_seconds,
+                     int check_every, int *steps, double *worst_ratio, double *seconds) {
+  if (!ctx || !ctx->setup_done || !(drop > 0.0) || max_steps < 1 || check_every < 1) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  const auto t0 = std::chrono::steady_clock::now();
+  auto elapsed = [&] { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); };
+  const Lvl &L = ctx->lv[1].L;
+  const int nc = L.ncase;
+  std::vector<double> nm(12 * (size_t)nc), ref(nc);
+  std::vector<int> st(4 * (size_t)nc);
+  // Res_rms(1) of every case after the last step; false if a case stopped
+  auto read = [&]() -> int {
+    CK(cudaMemcpyAsync(nm.data(), L.norms, nm.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(st.data(), L.status, st.size() * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int c = 0; c < nc; c++) if (st[4 * c]) return EC2D_ERR_STATE;
+    return EC2D_OK;
+  };
+  int n = 0, r;
+  double worst = 1.0;
+  if (r0) {
+    for (int c = 0; c < nc; c++) ref[c] = r0[c];
+  } else {
+    if ((r = ec2d_step(ctx, 1)) != EC2D_OK) return r;
+    n = 1;
+    if ((r = read()) != EC2D_OK) return r;
+    for (int c = 0; c < nc; c++) ref[c] = nm[12 * c + 6];
+  }
+  while (true) {
+    if (n > 0) {
+      worst = 0.0;
+      for (int c = 0; c < nc; c++) worst = std::max(worst, ref[c] > 0.0 ? nm[12 * c + 6] / ref[c] : 0.0);
+      if (worst <= drop) break;
+    }
+    if (n >= max_steps || (max_seconds > 0.0 && elapsed() >= max_seconds)) break;
+    int k = std::min(check_every, max_steps - n);
+    if ((r = ec2d_step(ctx, k)) != EC2D_OK) return r;
+    n += k;
+    if ((r = read()) != EC2D_OK) return r;
+  }
+  if (steps) *steps = n;
+  if (worst_ratio) *worst_ratio = worst;
+  if (seconds) *seconds = elapsed();
+  return EC2D_OK;
 }
 
 int ec2d_status(ec2d_ctx *ctx, int case_id, int *code, int *block, int *i, int *j) {

@@ -1,7 +1,7 @@
 // k_sweep32.cu -- the LU-SGS operator (du_LU_SGS_2D, sub_LU_SGS.f90:4-108) in
 // FP32, for the mixed-precision mode in which the sweeps only precondition:
 // the residual stays FP64, Res is rounded to float when the records are built,
-// U stays FP64 and receives U += (double)dU.
+// U stays FP64 and receives U += (double)dU in a separate all-cells kernel.
 //
 // Same wavefront as the FP64 sweep (k_sweep.cu): hyperplanes p = i+j in the
 // reference's Gauss-Seidel order, one CTA per block, thread j owns row j, the
@@ -35,7 +35,7 @@ constexpr int TILE = 256;
 
 constexpr int pad4(int n) { return (n + 3) / 4 * 4; }
 
-// record (floats, then the FP64 U_old), identical for both passes:
+// record (floats), identical for both passes:
 //  A        Res (forward) or the forward dU (backward)
 //  B        base state of the cell: rho, rho u, rho v, E + p, U_5.., then u, v
 //  CI, CJ   0.5 Lc_nb (+ Lv_nb when viscous) of the upstream neighbours
@@ -45,9 +45,8 @@ template <int NV>
 struct R32 {
   static constexpr int A = 0, B = NV, BU = 2 * NV, BV = 2 * NV + 1, CI = 2 * NV + 2, CJ = CI + 1, N1I = CI + 2,
                        N2I = CI + 3, N1J = CI + 4, N2J = CI + 5, IA = CI + 6, IA5 = CI + 7;
-  static constexpr int NF = pad4(CI + 8);         // floats
-  static constexpr int NU = (NV + 1) / 2 * 2;     // doubles of U_old (whole 16-byte units)
-  static constexpr int BYTES = NF * 4 + NU * 8;
+  static constexpr int NF = pad4(CI + 8);
+  static constexpr int BYTES = NF * 4;
   static_assert(BYTES % 16 == 0, "records are whole 16-byte units");
 };
 
@@ -77,7 +76,6 @@ __global__ void __launch_bounds__(TILE) k_lusgs_prep32(Lvl L, double alfa1) {
   char *base = reinterpret_cast<char *>(L.rec);
   float *rf = reinterpret_cast<float *>(base + cell * RC::BYTES);
   float *rb = reinterpret_cast<float *>(base + ((size_t)L.ncell + cell) * RC::BYTES);
-  double *uf = reinterpret_cast<double *>(rf + RC::NF), *ub = reinterpret_cast<double *>(rb + RC::NF);
   double vol = g[G_VOL * F + id];
   double Lv = lc[L_VI * F + id] + lc[L_VJ * F + id];
   double alfa = vol / lc[L_DT * F + id] + 1.0 * (lc[L_CI * F + id] + lc[L_CJ * F + id]) + vol * alfa1;
@@ -93,8 +91,6 @@ __global__ void __launch_bounds__(TILE) k_lusgs_prep32(Lvl L, double alfa1) {
   for (int m = 0; m < NV; m++) {
     rf[RC::A + m] = (float)L.res[m * F + id];
     rb[RC::A + m] = 0.0f;
-    uf[m] = U[m];
-    ub[m] = U[m];
   }
   float *rr[2] = {rf, rb};
 #pragma unroll
@@ -156,28 +152,23 @@ __device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1
 __device__ __forceinline__ void cp_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 template <int NV>
-__device__ __forceinline__ void fetch32(char *dst, const char *src, bool with_u) {
-  using RC = R32<NV>;
-  const int n = with_u ? RC::BYTES : RC::NF * 4;
+__device__ __forceinline__ void fetch32(char *dst, const char *src) {
 #pragma unroll
-  for (int k = 0; k < RC::BYTES; k += 16)
-    if (k < n) cp16(dst + k, src + k);
+  for (int k = 0; k < R32<NV>::BYTES; k += 16) cp16(dst + k, src + k);
 }
 
 template <int NV>
-__global__ void __launch_bounds__(1024) k_lusgs_sweep32(Lvl L, int update) {
+__global__ void __launch_bounds__(1024) k_lusgs_sweep32(Lvl L) {
   using SL = S32<NV>;
   using RC = R32<NV>;
   constexpr int S = SL::S;
   extern __shared__ __align__(16) float shf[];  // [2][rows+2][S] slots, then [blockDim][2] records
   const BlkDev bd = L.blk[blockIdx.x];
   const int nx = bd.nx, ny = bd.ny, rows = ny - 1, ni = nx - 1;
-  const long long off = bd.off, P = bd.P;
   const int rl = threadIdx.x;
   const int j = rl + 1;
   const int R = blockDim.x;
   const bool row_ok = j <= rows;
-  const long long F = L.F;
   const float gm1 = (float)(L.cs[bd.cas].gamma - 1.0);
   char *rec = reinterpret_cast<char *>(shf + (size_t)2 * (R + 2) * S) + (size_t)threadIdx.x * 2 * RC::BYTES;
   const char *recF = reinterpret_cast<const char *>(L.rec) + ((size_t)bd.cell0 + (size_t)(j - 1) * ni) * RC::BYTES;
@@ -189,7 +180,7 @@ __global__ void __launch_bounds__(1024) k_lusgs_sweep32(Lvl L, int update) {
   for (int pass = 0; pass < 2; pass++) {
     const bool fwd = pass == 0;
     const char *rsrc = fwd ? recF : recB;
-    if (row_ok) fetch32<NV>(rec, rsrc + (size_t)(fwd ? 0 : ni - 1) * RC::BYTES, !fwd);
+    if (row_ok) fetch32<NV>(rec, rsrc + (size_t)(fwd ? 0 : ni - 1) * RC::BYTES);
     cp_commit();
     int k = 0;
     for (int pp = 2; pp <= nx + ny - 2; pp++) {
@@ -199,7 +190,7 @@ __global__ void __launch_bounds__(1024) k_lusgs_sweep32(Lvl L, int update) {
       if (row_ok && i >= 1 && i <= ni) {
         const float *cur = reinterpret_cast<const float *>(rec + (k & 1) * RC::BYTES);
         const int inx = fwd ? i + 1 : i - 1;
-        if (inx >= 1 && inx <= ni) fetch32<NV>(rec + ((k + 1) & 1) * RC::BYTES, rsrc + (size_t)(inx - 1) * RC::BYTES, !fwd);
+        if (inx >= 1 && inx <= ni) fetch32<NV>(rec + ((k + 1) & 1) * RC::BYTES, rsrc + (size_t)(inx - 1) * RC::BYTES);
         cp_commit();
         cp_wait1();
         float acc[NV];
@@ -241,26 +232,41 @@ __global__ void __launch_bounds__(1024) k_lusgs_sweep32(Lvl L, int update) {
         float4 *own = reinterpret_cast<float4 *>(shf + ((size_t)buf * (R + 2) + rl + 1) * S);
 #pragma unroll
         for (int m = 0; m < S / 4; m++) own[m] = make_float4(st[4 * m], st[4 * m + 1], st[4 * m + 2], st[4 * m + 3]);
-        if (fwd) {
-          // the forward dU becomes the A field of this cell's backward record
-          float *w = reinterpret_cast<float *>(recBw + (size_t)(i - 1) * RC::BYTES);
+        // forward: the forward dU becomes the A field of this cell's backward
+        // record; backward: the final dU replaces it there, and k_apply32
+        // widens it to FP64 afterwards (FP64 instructions hold a warp for
+        // about 64 cycles each, so they stay off the wavefront)
+        float *w = reinterpret_cast<float *>(recBw + (size_t)(i - 1) * RC::BYTES);
 #pragma unroll
-          for (int m = 0; m < NV; m++) w[RC::A + m] = st[SL::D + m];
-        } else {
-          const double *uo = reinterpret_cast<const double *>(cur + RC::NF);
-          const long long id = off + (long long)(j + 2) * P + (i + 2);
-#pragma unroll
-          for (int m = 0; m < NV; m++) {
-            double d = (double)st[SL::D + m];
-            L.du[m * F + id] = d;
-            if (update) L.U[m * F + id] = uo[m] + d;
-          }
-        }
+        for (int m = 0; m < NV; m++) w[RC::A + m] = st[SL::D + m];
         k++;
       }
       __syncthreads();
     }
     cp_wait0();
+  }
+}
+
+// dU (FP32, in the backward records) -> L.du, and U += dU in FP64
+// (NS_Time_advance_LU_SGS, sub_NS_singlegrid.f90:203-211)
+template <int NV>
+__global__ void __launch_bounds__(TILE) k_apply32(Lvl L, int update) {
+  using RC = R32<NV>;
+  int2 t = L.tiles[blockIdx.x];
+  const BlkDev &b = L.blk[t.x];
+  int W = b.nx + 3, lin = t.y + threadIdx.x;
+  if (lin >= W * (b.ny + 3)) return;
+  int i = lin % W - 1, j = lin / W - 1;
+  if (i < 1 || i > b.nx - 1 || j < 1 || j > b.ny - 1) return;
+  const long long F = L.F, id = fidx(b, i, j);
+  const size_t cell = (size_t)b.cell0 + (size_t)(j - 1) * (b.nx - 1) + (i - 1);
+  const float *rb = reinterpret_cast<const float *>(reinterpret_cast<const char *>(L.rec) +
+                                                    ((size_t)L.ncell + cell) * RC::BYTES);
+#pragma unroll
+  for (int m = 0; m < NV; m++) {
+    double d = (double)rb[RC::A + m];
+    L.du[m * F + id] = d;
+    if (update) L.U[m * F + id] += d;
   }
 }
 
@@ -277,7 +283,8 @@ void sweep32_nv(const Lvl &L, double alfa1, int update, int max_rows, cudaStream
   size_t smem = smem32<NV>(max_rows);
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(k_lusgs_sweep32<NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_lusgs_sweep32<NV><<<L.nblk, th, smem, s>>>(L, update);
+  k_lusgs_sweep32<NV><<<L.nblk, th, smem, s>>>(L);
+  k_apply32<NV><<<L.ntiles, TILE, 0, s>>>(L, update);
 }
 
 }  // namespace

@@ -113,6 +113,8 @@ def lib():
         "ec2d_kernel_times": ([vp, ctypes.c_char_p, ctypes.c_int], ctypes.c_int),
         "ec2d_set_graphs": ([vp, ctypes.c_int], ctypes.c_int),
         "ec2d_set_lusgs_precision": ([vp, ctypes.c_int], ctypes.c_int),
+        "ec2d_run_to_drop": ([vp, ctypes.c_double, dp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ip, dp, dp],
+                             ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -279,6 +281,16 @@ class Solver:
     def set_graphs(self, enable=True):
         """Replay each step as one CUDA graph (default) or launch kernels one by one."""
         _ck(self.L.ec2d_set_graphs(self.h, 1 if enable else 0), "ec2d_set_graphs")
+
+    def run_to_drop(self, drop=1e-8, r0=None, max_steps=1000000, max_seconds=0.0, check_every=25):
+        """Iterate until every case's Res_rms(1) <= drop * r0 (r0: the first
+        step's residual unless given).  Returns (steps, worst ratio, seconds)."""
+        n = ctypes.c_int(); w = ctypes.c_double(); t = ctypes.c_double()
+        r0a = None if r0 is None else np.ascontiguousarray(r0, dtype=np.float64)
+        r0p = None if r0a is None else _dp(r0a)
+        _ck(self.L.ec2d_run_to_drop(self.h, drop, r0p, int(max_steps), float(max_seconds), int(check_every),
+                                    ctypes.byref(n), ctypes.byref(w), ctypes.byref(t)), "ec2d_run_to_drop")
+        return n.value, w.value, t.value
 
     def set_lusgs_precision(self, bits):
         """64 (default) or 32: arithmetic of the LU-SGS sweeps on every level."""

@@ -1,0 +1,37 @@
+"""ec2d_run_to_drop (iterate to a residual drop, with timers): the steps it
+takes are ordinary ec2d_step calls, so a second solver stepped by hand the
+same number of times must hold the identical state and norms."""
+import numpy as np
+import pytest
+
+from helpers import make_gpu, small_case
+
+pytestmark = pytest.mark.gpu
+
+
+def test_run_to_drop_matches_manual_stepping(gpu_lib):
+    p, bl = small_case(Ma=0.5, AoA=2.0, Iflag_flux=4, Iflag_Scheme=5, CFL=5.0)
+    a = make_gpu(p, bl)
+    a.init_flow()
+    n, ratio, secs = a.run_to_drop(drop=0.2, max_steps=400, check_every=10)
+    assert 1 < n <= 400 and secs > 0.0
+    assert ratio <= 0.2 or n == 400
+    b = make_gpu(p, bl)
+    b.init_flow()
+    b.step(1)
+    r0 = b.norms()[1][0]
+    b.step(n - 1)
+    np.testing.assert_array_equal(a.norms()[1], b.norms()[1])
+    assert b.norms()[1][0] / r0 == ratio
+    np.testing.assert_array_equal(a.download_U(1, 1, 1), b.download_U(1, 1, 1))
+
+
+def test_run_to_drop_limits(gpu_lib):
+    p, bl = small_case(Ma=0.5, AoA=2.0, Iflag_flux=4, Iflag_Scheme=5, CFL=5.0)
+    g = make_gpu(p, bl)
+    g.init_flow()
+    n, ratio, _ = g.run_to_drop(drop=1e-30, max_steps=37, check_every=10)
+    assert n == 37 and ratio > 1e-30
+    # a given reference residual: one check, no step needed when already below
+    n2, ratio2, _ = g.run_to_drop(drop=1.0, r0=[1e30], max_steps=5, check_every=5)
+    assert n2 == 5 or ratio2 <= 1.0
