@@ -221,6 +221,50 @@ int ec2d_set_graphs(ec2d_ctx *ctx, int enable);
  * FP64, so the converged state is that of the FP64 discretisation. */
 int ec2d_set_lusgs_precision(ec2d_ctx *ctx, int bits);
 
+/* ---- Learned warm start (no counterpart in the reference) ----------------
+ * A coordinate-conditioned MLP predicts the initial conservative (and SA)
+ * field of a case -- its departure from the case's freestream, and
+ * log1p(nu_tilde Re) -- from (x, y, log10 wall distance, M, AoA [deg],
+ * log10 Re, shape) per cell, where `shape` is a per-case geometry parameter the host
+ * supplies (the airfoil's t/c).  Training data are the fields of solved
+ * cases; training and inference run in the library's own kernels (BF16
+ * weights and activations, FP32 accumulation and Adam).  The freestream start
+ * of ec2d_init_flow stays the fallback: a case whose predicted field has any
+ * cell with rho <= 0, p <= 0 or T < 1e-5 keeps the freestream. */
+typedef struct ec2d_mlp ec2d_mlp;
+/* hidden_layers hidden layers of `width` (a multiple of 128) neurons */
+int ec2d_mlp_create(int device, int hidden_layers, int width, unsigned long long seed, ec2d_mlp **out);
+void ec2d_mlp_destroy(ec2d_mlp *m);
+/* per-case shape feature (default 0); call any time after ec2d_setup */
+int ec2d_set_case_shape(ec2d_ctx *ctx, int case_id, double shape);
+/* append one sample per fine-mesh cell of every case of ctx (its current U) */
+int ec2d_mlp_add_samples(ec2d_mlp *m, ec2d_ctx *ctx);
+int ec2d_mlp_num_samples(ec2d_mlp *m, long long *n);
+int ec2d_mlp_clear_samples(ec2d_mlp *m);
+/* standardisation of features and targets from the current samples */
+int ec2d_mlp_fit_normalization(ec2d_mlp *m);
+/* `steps` Adam steps on minibatches of `batch` (a multiple of 256) random
+ * samples; loss_out (may be NULL): the MSE of the last step (standardised) */
+int ec2d_mlp_train(ec2d_mlp *m, int steps, int batch, double lr, double *loss_out);
+/* predict the fine-mesh field of every case of ctx and write it into U
+ * (interior cells, then the boundary conditions and halos); n_fallback: the
+ * number of cases that kept the freestream */
+int ec2d_mlp_warm_start(ec2d_mlp *m, ec2d_ctx *ctx, int *n_fallback);
+/* test and persistence access: layer shapes, FP32 weights, gradients of the
+ * last training step or of ec2d_mlp_loss_grad, predictions from host features */
+int ec2d_mlp_num_layers(ec2d_mlp *m, int *nlin);
+int ec2d_mlp_layer_shape(ec2d_mlp *m, int layer, int *rows, int *cols);
+int ec2d_mlp_get_weights(ec2d_mlp *m, int layer, float *w, float *b);
+int ec2d_mlp_set_weights(ec2d_mlp *m, int layer, const float *w, const float *b);
+int ec2d_mlp_get_grads(ec2d_mlp *m, int layer, float *gw, float *gb);
+int ec2d_mlp_get_normalization(ec2d_mlp *m, float *nrm);  /* 2*7 + 2*5 floats */
+int ec2d_mlp_set_normalization(ec2d_mlp *m, const float *nrm);
+/* loss and gradients for B standardised rows (x: B x 7, y: B x 5, B a multiple
+ * of 256) */
+int ec2d_mlp_loss_grad(ec2d_mlp *m, const float *x, const float *y, int B, double *loss);
+/* un-standardised predictions (n x 5) for raw features (n x 7), host arrays */
+int ec2d_mlp_predict(ec2d_mlp *m, const float *feat, long long n, float *pred);
+
 /* Wait for all queued work of the context. */
 int ec2d_sync(ec2d_ctx *ctx);
 

@@ -19,6 +19,7 @@
 #include "../../include/ec2d_gpu.h"
 #include "ec2d_dev.cuh"
 #include "ec2d_internal.h"
+#include "ec2d_mlp.h"
 
 using namespace ec2d;
 
@@ -100,6 +101,7 @@ struct ec2d_ctx {
   Level lv[4];
   CaseDev *d_cases = nullptr;
   double *d_stage = nullptr;  // staging for U upload/download
+  double *d_shape = nullptr;  // per-case shape feature of the warm-start network
   size_t stage_n = 0;
   int dual_iflag1 = 0, dual_iflag = 0;
   int last_err = 0;
@@ -885,6 +887,7 @@ void ec2d_destroy(ec2d_ctx *ctx) {
   for (auto e : ctx->evpool) cudaEventDestroy(e);
   if (ctx->d_cases) cudaFree(ctx->d_cases);
   if (ctx->d_stage) cudaFree(ctx->d_stage);
+  if (ctx->d_shape) cudaFree(ctx->d_shape);
   if (ctx->step_graph) cudaGraphExecDestroy(ctx->step_graph);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -960,6 +963,8 @@ int ec2d_setup(ec2d_ctx *ctx) {
   ctx->nvar = ctx->cases[0].nvar;
   std::vector<CaseDev> cd;
   for (auto &c : ctx->cases) cd.push_back(make_casedev(c.p));
+  CK(cudaMalloc(&ctx->d_shape, ctx->cases.size() * sizeof(double)));
+  CK(cudaMemset(ctx->d_shape, 0, ctx->cases.size() * sizeof(double)));
   CK(cudaMalloc(&ctx->d_cases, cd.size() * sizeof(CaseDev)));
   CK(cudaMemcpy(ctx->d_cases, cd.data(), cd.size() * sizeof(CaseDev), cudaMemcpyHostToDevice));
   for (int l = 1; l <= nm; l++) {
@@ -1374,6 +1379,227 @@ int ec2d_kernel_times(ec2d_ctx *ctx, char *buf, int buflen) {
   }
   snprintf(buf, buflen, "%s", out.c_str());
   return (int)out.size() < buflen ? EC2D_OK : EC2D_ERR_ARG;
+}
+
+int ec2d_set_case_shape(ec2d_ctx *ctx, int case_id, double shape) {
+  if (!ctx || !ctx->setup_done || !valid_case(ctx, case_id)) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  CK(cudaMemcpyAsync(ctx->d_shape + (case_id - 1), &shape, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return EC2D_OK;
+}
+
+}  // extern "C"
+
+struct ec2d_mlp {
+  ec2d::Net net;
+};
+
+extern "C" {
+
+int ec2d_mlp_create(int device, int hidden_layers, int width, unsigned long long seed, ec2d_mlp **out) {
+  if (!out || width % 128 != 0) return EC2D_ERR_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return EC2D_ERR_CUDA;
+  ec2d_mlp *m = new ec2d_mlp();
+  int r = m->net.init(device, hidden_layers, width, seed);
+  if (r) {
+    m->net.destroy();
+    delete m;
+    return r == 1 ? EC2D_ERR_ARG : EC2D_ERR_CUDA;
+  }
+  *out = m;
+  return EC2D_OK;
+}
+
+void ec2d_mlp_destroy(ec2d_mlp *m) {
+  if (!m) return;
+  m->net.destroy();
+  delete m;
+}
+
+int ec2d_mlp_add_samples(ec2d_mlp *m, ec2d_ctx *ctx) {
+  if (!m || !ctx || !ctx->setup_done) return EC2D_ERR_ARG;
+  Net &net = m->net;
+  if (net.device != ctx->device) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  const Lvl &L = ctx->lv[1].L;
+  long long n0 = net.nsamp, n = L.ncell;
+  if (net.reserve_samples(n0 + n)) return EC2D_ERR_NOMEM;
+  CK(cudaStreamSynchronize(net.stream));
+  launch_features(L, ctx->d_shape, net.feat + n0 * NIN, net.targ + n0 * NOUT, ctx->stream);
+  CK(cudaStreamSynchronize(ctx->stream));
+  net.nsamp = n0 + n;
+  return check_launch(ctx);
+}
+
+int ec2d_mlp_num_samples(ec2d_mlp *m, long long *n) {
+  if (!m || !n) return EC2D_ERR_ARG;
+  *n = m->net.nsamp;
+  return EC2D_OK;
+}
+
+int ec2d_mlp_clear_samples(ec2d_mlp *m) {
+  if (!m) return EC2D_ERR_ARG;
+  m->net.nsamp = 0;
+  return EC2D_OK;
+}
+
+int ec2d_mlp_fit_normalization(ec2d_mlp *m) {
+  if (!m || m->net.nsamp < 2) return EC2D_ERR_ARG;
+  cudaSetDevice(m->net.device);
+  return m->net.fit_normalization() ? EC2D_ERR_CUDA : EC2D_OK;
+}
+
+int ec2d_mlp_train(ec2d_mlp *m, int steps, int batch, double lr, double *loss_out) {
+  if (!m || steps < 0 || batch < 256 || batch % 256 || !(lr > 0.0) || m->net.nsamp < 1) return EC2D_ERR_ARG;
+  Net &net = m->net;
+  cudaSetDevice(net.device);
+  if (net.ensure_batch(batch)) return EC2D_ERR_NOMEM;
+  for (int k = 0; k < steps; k++) {
+    net.gather(batch);
+    net.forward(batch);
+    net.backward(batch);
+    net.adam((float)lr);
+  }
+  float l = 0.0f;
+  CK(cudaMemcpyAsync(&l, net.d_loss, sizeof(float), cudaMemcpyDeviceToHost, net.stream));
+  CK(cudaStreamSynchronize(net.stream));
+  if (loss_out) *loss_out = l;
+  return cudaGetLastError() == cudaSuccess ? EC2D_OK : EC2D_ERR_CUDA;
+}
+
+int ec2d_mlp_warm_start(ec2d_mlp *m, ec2d_ctx *ctx, int *n_fallback) {
+  if (!m || !ctx || !ctx->setup_done || m->net.device != ctx->device) return EC2D_ERR_ARG;
+  Net &net = m->net;
+  cudaSetDevice(ctx->device);
+  int r = ec2d_init_flow(ctx);
+  if (r) return r;
+  const Level &lv = ctx->lv[1];
+  const Lvl &L = lv.L;
+  const long long n = L.ncell;
+  float *feat = nullptr, *pred = nullptr;
+  int *bad = nullptr;
+  CK(cudaMalloc(&feat, (size_t)n * NIN * sizeof(float)));
+  CK(cudaMalloc(&pred, (size_t)n * NOUT * sizeof(float)));
+  CK(cudaMalloc(&bad, ctx->cases.size() * sizeof(int)));
+  CK(cudaMemsetAsync(bad, 0, ctx->cases.size() * sizeof(int), ctx->stream));
+  launch_features(L, ctx->d_shape, feat, nullptr, ctx->stream);
+  CK(cudaStreamSynchronize(ctx->stream));
+  r = net.predict(feat, n, pred);
+  CK(cudaStreamSynchronize(net.stream));
+  if (r == EC2D_OK) {
+    launch_warm_start(L, pred, bad, ctx->stream);
+    launch_bc(L, 1 | 2 | 4, ctx->stream);
+    if (L.nvar >= 5) launch_bc(L, 8, ctx->stream);
+  }
+  std::vector<int> hb(ctx->cases.size());
+  CK(cudaMemcpyAsync(hb.data(), bad, hb.size() * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  cudaFree(feat);
+  cudaFree(pred);
+  cudaFree(bad);
+  if (r) return EC2D_ERR_CUDA;
+  if (n_fallback) {
+    int c = 0;
+    for (int v : hb) c += v != 0;
+    *n_fallback = c;
+  }
+  return check_launch(ctx);
+}
+
+int ec2d_mlp_num_layers(ec2d_mlp *m, int *nlin) {
+  if (!m || !nlin) return EC2D_ERR_ARG;
+  *nlin = m->net.nlin;
+  return EC2D_OK;
+}
+
+int ec2d_mlp_layer_shape(ec2d_mlp *m, int layer, int *rows, int *cols) {
+  if (!m || layer < 0 || layer >= m->net.nlin || !rows || !cols) return EC2D_ERR_ARG;
+  *rows = m->net.layer_out(layer);
+  *cols = m->net.layer_in(layer);
+  return EC2D_OK;
+}
+
+static int mlp_copy(ec2d_mlp *m, int layer, float *dw, float *db, const float *sw, const float *sb, bool grads) {
+  if (!m || layer < 0 || layer >= m->net.nlin) return EC2D_ERR_ARG;
+  Net &net = m->net;
+  cudaSetDevice(net.device);
+  Layer &Ly = net.L[layer];
+  size_t nw = (size_t)net.layer_out(layer) * net.layer_in(layer), nb = net.layer_out(layer);
+  CK(cudaStreamSynchronize(net.stream));
+  if (sw || sb) {
+    if (sw) CK(cudaMemcpy(Ly.w, sw, nw * sizeof(float), cudaMemcpyHostToDevice));
+    if (sb) CK(cudaMemcpy(Ly.b, sb, nb * sizeof(float), cudaMemcpyHostToDevice));
+    net.refresh_bf16();
+    CK(cudaStreamSynchronize(net.stream));
+  } else {
+    if (dw) CK(cudaMemcpy(dw, grads ? Ly.gw : Ly.w, nw * sizeof(float), cudaMemcpyDeviceToHost));
+    if (db) CK(cudaMemcpy(db, grads ? Ly.gb : Ly.b, nb * sizeof(float), cudaMemcpyDeviceToHost));
+  }
+  return EC2D_OK;
+}
+
+int ec2d_mlp_get_weights(ec2d_mlp *m, int layer, float *w, float *b) {
+  return mlp_copy(m, layer, w, b, nullptr, nullptr, false);
+}
+int ec2d_mlp_set_weights(ec2d_mlp *m, int layer, const float *w, const float *b) {
+  if (!w && !b) return EC2D_ERR_ARG;
+  return mlp_copy(m, layer, nullptr, nullptr, w, b, false);
+}
+int ec2d_mlp_get_grads(ec2d_mlp *m, int layer, float *gw, float *gb) {
+  return mlp_copy(m, layer, gw, gb, nullptr, nullptr, true);
+}
+
+int ec2d_mlp_get_normalization(ec2d_mlp *m, float *nrm) {
+  if (!m || !nrm) return EC2D_ERR_ARG;
+  cudaSetDevice(m->net.device);
+  CK(cudaStreamSynchronize(m->net.stream));
+  CK(cudaMemcpy(nrm, m->net.nrm, (2 * NIN + 2 * NOUT) * sizeof(float), cudaMemcpyDeviceToHost));
+  return EC2D_OK;
+}
+int ec2d_mlp_set_normalization(ec2d_mlp *m, const float *nrm) {
+  if (!m || !nrm) return EC2D_ERR_ARG;
+  cudaSetDevice(m->net.device);
+  CK(cudaStreamSynchronize(m->net.stream));
+  CK(cudaMemcpy(m->net.nrm, nrm, (2 * NIN + 2 * NOUT) * sizeof(float), cudaMemcpyHostToDevice));
+  return EC2D_OK;
+}
+
+int ec2d_mlp_loss_grad(ec2d_mlp *m, const float *x, const float *y, int B, double *loss) {
+  if (!m || !x || !y || B < 256 || B % 256) return EC2D_ERR_ARG;
+  Net &net = m->net;
+  cudaSetDevice(net.device);
+  if (net.ensure_batch(B)) return EC2D_ERR_NOMEM;
+  std::vector<__nv_bfloat16> xb((size_t)B * NIN_PAD, __float2bfloat16(0.0f));
+  for (int r = 0; r < B; r++)
+    for (int c = 0; c < NIN; c++) xb[(size_t)r * NIN_PAD + c] = __float2bfloat16(x[(size_t)r * NIN + c]);
+  CK(cudaMemcpyAsync(net.X, xb.data(), xb.size() * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice, net.stream));
+  CK(cudaMemcpyAsync(net.Y, y, (size_t)B * NOUT * sizeof(float), cudaMemcpyHostToDevice, net.stream));
+  net.forward(B);
+  net.backward(B);
+  float l = 0.0f;
+  CK(cudaMemcpyAsync(&l, net.d_loss, sizeof(float), cudaMemcpyDeviceToHost, net.stream));
+  CK(cudaStreamSynchronize(net.stream));
+  if (loss) *loss = l;
+  return cudaGetLastError() == cudaSuccess ? EC2D_OK : EC2D_ERR_CUDA;
+}
+
+int ec2d_mlp_predict(ec2d_mlp *m, const float *feat, long long n, float *pred) {
+  if (!m || !feat || !pred || n < 1) return EC2D_ERR_ARG;
+  Net &net = m->net;
+  cudaSetDevice(net.device);
+  float *df = nullptr, *dp = nullptr;
+  CK(cudaMalloc(&df, (size_t)n * NIN * sizeof(float)));
+  CK(cudaMalloc(&dp, (size_t)n * NOUT * sizeof(float)));
+  CK(cudaMemcpy(df, feat, (size_t)n * NIN * sizeof(float), cudaMemcpyHostToDevice));
+  int r = net.predict(df, n, dp);
+  cudaStreamSynchronize(net.stream);
+  if (r == 0) cudaMemcpy(pred, dp, (size_t)n * NOUT * sizeof(float), cudaMemcpyDeviceToHost);
+  cudaFree(df);
+  cudaFree(dp);
+  return r ? EC2D_ERR_CUDA : EC2D_OK;
 }
 
 int ec2d_sync(ec2d_ctx *ctx) {

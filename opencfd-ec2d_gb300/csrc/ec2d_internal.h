@@ -32,6 +32,9 @@ size_t lusgs_smem(int nv, int rows);  // dynamic shared memory of the one-CTA FP
 void launch_lusgs_fast32(const Lvl &L, double alfa1, int update, int max_rows, cudaStream_t s);
 size_t lusgs32_smem(int nv, int rows);
 size_t lusgs32_record_bytes(int nv);
+// warm-start network <-> solver level (k_mlp.cu)
+void launch_features(const Lvl &L, const double *shape, float *feat, float *targ, cudaStream_t s);
+void launch_warm_start(const Lvl &L, const float *pred, int *bad, cudaStream_t s);
 void launch_add_du(const Lvl &L, cudaStream_t s);
 void launch_euler(const Lvl &L, int force, cudaStream_t s);
 void launch_rk3(const Lvl &L, int stage, int force, cudaStream_t s);

@@ -74,6 +74,7 @@ def lib():
         raise OSError(f"{LIB} not built; run ec2d_build.py")
     L = ctypes.CDLL(LIB)
     vp, ip, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
+    fp = ctypes.POINTER(ctypes.c_float)
     cpp = ctypes.POINTER(ctypes.c_void_p)
     sig = {
         "ec2d_version": ([], ctypes.c_int),
@@ -115,6 +116,24 @@ def lib():
         "ec2d_set_lusgs_precision": ([vp, ctypes.c_int], ctypes.c_int),
         "ec2d_run_to_drop": ([vp, ctypes.c_double, dp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ip, dp, dp],
                              ctypes.c_int),
+        "ec2d_set_case_shape": ([vp, ctypes.c_int, ctypes.c_double], ctypes.c_int),
+        "ec2d_mlp_create": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, cpp], ctypes.c_int),
+        "ec2d_mlp_destroy": ([vp], None),
+        "ec2d_mlp_add_samples": ([vp, vp], ctypes.c_int),
+        "ec2d_mlp_num_samples": ([vp, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
+        "ec2d_mlp_clear_samples": ([vp], ctypes.c_int),
+        "ec2d_mlp_fit_normalization": ([vp], ctypes.c_int),
+        "ec2d_mlp_train": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, dp], ctypes.c_int),
+        "ec2d_mlp_warm_start": ([vp, vp, ip], ctypes.c_int),
+        "ec2d_mlp_num_layers": ([vp, ip], ctypes.c_int),
+        "ec2d_mlp_layer_shape": ([vp, ctypes.c_int, ip, ip], ctypes.c_int),
+        "ec2d_mlp_get_weights": ([vp, ctypes.c_int, fp, fp], ctypes.c_int),
+        "ec2d_mlp_set_weights": ([vp, ctypes.c_int, fp, fp], ctypes.c_int),
+        "ec2d_mlp_get_grads": ([vp, ctypes.c_int, fp, fp], ctypes.c_int),
+        "ec2d_mlp_get_normalization": ([vp, fp], ctypes.c_int),
+        "ec2d_mlp_set_normalization": ([vp, fp], ctypes.c_int),
+        "ec2d_mlp_loss_grad": ([vp, fp, fp, ctypes.c_int, dp], ctypes.c_int),
+        "ec2d_mlp_predict": ([vp, fp, ctypes.c_longlong, fp], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -126,6 +145,10 @@ def lib():
 
 def _dp(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _fp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
 
 
 def _ck(r, what):
@@ -292,6 +315,10 @@ class Solver:
                                     ctypes.byref(n), ctypes.byref(w), ctypes.byref(t)), "ec2d_run_to_drop")
         return n.value, w.value, t.value
 
+    def set_case_shape(self, case, shape):
+        """Per-case shape feature of the warm-start network (the airfoil t/c)."""
+        _ck(self.L.ec2d_set_case_shape(self.h, case, float(shape)), "ec2d_set_case_shape")
+
     def set_lusgs_precision(self, bits):
         """64 (default) or 32: arithmetic of the LU-SGS sweeps on every level."""
         _ck(self.L.ec2d_set_lusgs_precision(self.h, int(bits)), "ec2d_set_lusgs_precision")
@@ -307,4 +334,100 @@ class Solver:
         for line in buf.value.decode().splitlines():
             name, lvl, calls, nk, ms = line.split()
             out[(name, int(lvl))] = (int(calls), int(nk), float(ms))
+        return out
+
+
+class WarmStartNet:
+    """The learned warm start (ec2d_mlp_*): a coordinate-conditioned MLP over
+    (x, y, log10 dw, M, AoA, log10 Re, shape) -> (rho, rho u, rho v, E,
+    log1p(nu_tilde Re)), trained on solved fields by the library's kernels."""
+
+    NIN, NOUT = 7, 5
+
+    def __init__(self, hidden=6, width=256, seed=1, device=0):
+        self.L = lib()
+        h = ctypes.c_void_p()
+        _ck(self.L.ec2d_mlp_create(device, hidden, width, seed, ctypes.byref(h)), "ec2d_mlp_create")
+        self.h = h
+        n = ctypes.c_int()
+        _ck(self.L.ec2d_mlp_num_layers(self.h, ctypes.byref(n)), "ec2d_mlp_num_layers")
+        self.nlin = n.value
+
+    def close(self):
+        if self.h:
+            self.L.ec2d_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_samples(self, solver):
+        _ck(self.L.ec2d_mlp_add_samples(self.h, solver.h), "ec2d_mlp_add_samples")
+
+    def num_samples(self):
+        n = ctypes.c_longlong()
+        _ck(self.L.ec2d_mlp_num_samples(self.h, ctypes.byref(n)), "ec2d_mlp_num_samples")
+        return n.value
+
+    def clear_samples(self):
+        _ck(self.L.ec2d_mlp_clear_samples(self.h), "ec2d_mlp_clear_samples")
+
+    def fit_normalization(self):
+        _ck(self.L.ec2d_mlp_fit_normalization(self.h), "ec2d_mlp_fit_normalization")
+
+    def train(self, steps, batch=16384, lr=1e-3):
+        l = ctypes.c_double()
+        _ck(self.L.ec2d_mlp_train(self.h, int(steps), int(batch), float(lr), ctypes.byref(l)), "ec2d_mlp_train")
+        return l.value
+
+    def warm_start(self, solver):
+        """Write the predicted field into every case of `solver`; returns the
+        number of cases that kept the freestream."""
+        n = ctypes.c_int()
+        _ck(self.L.ec2d_mlp_warm_start(self.h, solver.h, ctypes.byref(n)), "ec2d_mlp_warm_start")
+        return n.value
+
+    def layer_shape(self, layer):
+        r, c = ctypes.c_int(), ctypes.c_int()
+        _ck(self.L.ec2d_mlp_layer_shape(self.h, layer, ctypes.byref(r), ctypes.byref(c)), "ec2d_mlp_layer_shape")
+        return r.value, c.value
+
+    def get_weights(self, layer):
+        r, c = self.layer_shape(layer)
+        w = np.zeros((r, c), np.float32); b = np.zeros(r, np.float32)
+        _ck(self.L.ec2d_mlp_get_weights(self.h, layer, _fp(w), _fp(b)), "ec2d_mlp_get_weights")
+        return w, b
+
+    def set_weights(self, layer, w, b):
+        w = np.ascontiguousarray(w, np.float32); b = np.ascontiguousarray(b, np.float32)
+        _ck(self.L.ec2d_mlp_set_weights(self.h, layer, _fp(w), _fp(b)), "ec2d_mlp_set_weights")
+
+    def get_grads(self, layer):
+        r, c = self.layer_shape(layer)
+        w = np.zeros((r, c), np.float32); b = np.zeros(r, np.float32)
+        _ck(self.L.ec2d_mlp_get_grads(self.h, layer, _fp(w), _fp(b)), "ec2d_mlp_get_grads")
+        return w, b
+
+    def get_normalization(self):
+        a = np.zeros(2 * self.NIN + 2 * self.NOUT, np.float32)
+        _ck(self.L.ec2d_mlp_get_normalization(self.h, _fp(a)), "ec2d_mlp_get_normalization")
+        return a
+
+    def set_normalization(self, a):
+        a = np.ascontiguousarray(a, np.float32)
+        _ck(self.L.ec2d_mlp_set_normalization(self.h, _fp(a)), "ec2d_mlp_set_normalization")
+
+    def loss_grad(self, x, y):
+        x = np.ascontiguousarray(x, np.float32); y = np.ascontiguousarray(y, np.float32)
+        l = ctypes.c_double()
+        _ck(self.L.ec2d_mlp_loss_grad(self.h, _fp(x), _fp(y), x.shape[0], ctypes.byref(l)), "ec2d_mlp_loss_grad")
+        return l.value
+
+    def predict(self, feat):
+        feat = np.ascontiguousarray(feat, np.float32)
+        out = np.zeros((feat.shape[0], self.NOUT), np.float32)
+        _ck(self.L.ec2d_mlp_predict(self.h, _fp(feat), feat.shape[0], _fp(out)), "ec2d_mlp_predict")
         return out
