@@ -272,6 +272,64 @@ def residual_hbm(torch, gpu, dev, reps=10):
             "note": "FP64 arithmetic bounds this stage: see the per-kernel FP64-pipe utilisation in profiles/"}
 
 
+def leg_polar(args):
+    """The batched polar (64 SA RANS cases from a seed, 257x65 to 513x129,
+    1-4 blocks, 3-level V-cycle): V-cycle throughput of the whole batch in one
+    context (FP64 and with FP32 LU-SGS) against the plain drop-in, one case
+    per context in FP64, timed on a sample of the same cases."""
+    import torch
+    from ec2d import cases, gpu
+    pc = cases.polar_cases(64)
+    cells = sum(fine_cells(bl) for _, bl in pc)
+    res = {"cases": len(pc), "cells": cells, "step": "one 3-level V-cycle of every case"}
+    g = gpu.Solver(pc)
+    stream = torch.cuda.ExternalStream(g.stream_handle())
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:0")
+    for bits in (64, 32):
+        g.set_lusgs_precision(bits)
+        g.init_flow()
+        g.step(3)
+        g.sync()
+        ms, launches = timed_steps(torch, g, stream, flush, args.steps)
+        res[f"batched_fp{bits}"] = {"value": cells * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+                                    "launches_per_step": launches}
+    g.close()
+    plain = []
+    for k in range(4):
+        p1 = gpu.Solver([pc[k]])
+        s1 = torch.cuda.ExternalStream(p1.stream_handle())
+        p1.init_flow()
+        p1.step(3)
+        p1.sync()
+        ms, _ = timed_steps(torch, p1, s1, flush, args.steps)
+        plain.append((fine_cells(pc[k][1]), ms / args.steps))
+        p1.close()
+    rate = sum(c for c, _ in plain) / (sum(t for _, t in plain) / 1e3)
+    res["plain_fp64_one_case_per_context"] = {"value": rate, "sample_cases": 4,
+                                              "ms_per_step": [t for _, t in plain]}
+    res["batched_mixed_vs_plain"] = res["batched_fp32"]["value"] / rate
+    res["unit"] = UNIT
+    return res
+
+
+def leg_learned(args):
+    """Learned warm start (512 training + 64 held-out SA cases on a 257x65
+    C-grid): data generation, training, and the held-out polar to a 1e-8 drop
+    -- warm-started, batched, FP32 LU-SGS against the freestream start and the
+    plain drop-in (one case per context, FP64)."""
+    from ec2d import gpu, learn
+    train_cases = learn.warmstart_cases(args.ws_train, seed=20261203)
+    held = learn.warmstart_cases(args.ws_held, seed=20261204)
+    net = gpu.WarmStartNet(hidden=6, width=256, seed=1)
+    gen = learn.generate(gpu, net, train_cases, steps=args.ws_gen_steps)
+    tr = learn.train(net, steps=args.ws_train_steps)
+    ev = learn.evaluate(gpu, net, held, targets=(1e-4, 1e-6, args.ws_target), max_steps=args.ws_max_steps,
+                        plain_sample=args.ws_plain)
+    net.close()
+    return {"network": "6 hidden layers x 256, SiLU, BF16 weights/activations, FP32 accumulate",
+            "generate": gen, "train": tr, "evaluate": ev}
+
+
 def run_gb300(args, rank, world):
     import torch
     from ec2d import gpu
@@ -440,15 +498,29 @@ def main():
     ap.add_argument("--drop-cap", type=float, default=60.0, help="seconds per time-to-drop run (0: skip)")
     ap.add_argument("--no-residual-hbm", dest="residual_hbm", action="store_false",
                     help="skip the residual bandwidth measurement on the 4.19 M-cell grid")
-    ap.add_argument("--leg", default="all", choices=["all", "residual_hbm"],
-                    help="residual_hbm: only the 4.19 M-cell residual measurement (for profiling)")
+    ap.add_argument("--leg", default="all", choices=["all", "residual_hbm", "polar", "learned"],
+                    help="residual_hbm: the 4.19 M-cell residual alone (for profiling); polar: the 64-case "
+                         "batched polar; learned: the learned warm start end to end")
+    ap.add_argument("--ws-train", type=int, default=512)
+    ap.add_argument("--ws-held", type=int, default=64)
+    ap.add_argument("--ws-gen-steps", type=int, default=3000)
+    ap.add_argument("--ws-train-steps", type=int, default=6000)
+    ap.add_argument("--ws-target", type=float, default=1e-8)
+    ap.add_argument("--ws-max-steps", type=int, default=30000)
+    ap.add_argument("--ws-plain", type=int, default=4, help="held-out cases also run one per context in FP64")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
-    if args.leg == "residual_hbm":
+    if args.leg != "all":
         import torch
         from ec2d import gpu
-        print(json.dumps({"residual_hbm": residual_hbm(torch, gpu, 0)}), flush=True)
+        if args.leg == "residual_hbm":
+            out = residual_hbm(torch, gpu, 0)
+        elif args.leg == "polar":
+            out = leg_polar(args)
+        else:
+            out = leg_learned(args)
+        print(json.dumps({args.leg: out}, default=float), flush=True)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)

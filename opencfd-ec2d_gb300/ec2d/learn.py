@@ -1,0 +1,171 @@
+"""Learned warm start: dataset generation from solved fields, training, and
+the comparison of warm-started against freestream-started runs.
+
+The case family is the polar box of the batched configuration -- M ~ U[0.3,
+0.8], AoA ~ U[-2, 8] deg, log10 Re ~ U[6, 7], t/c ~ U[0.09, 0.15] -- on a
+fixed 257x65 single-block C-grid topology around a symmetric four-digit
+airfoil (the geometry follows t/c), Spalart-Allmaras, Roe + MUSCL, LU-SGS.
+The family runs on a single grid: with the turbulence equation on the fine
+mesh only, the three-level V-cycle loses stability on most of these cases
+(the coarse levels carry no eddy viscosity), while the single-grid LU-SGS
+iteration converges monotonically.
+
+Every solver call goes through the C-ABI (`gpu.Solver`, `gpu.WarmStartNet`);
+cases run in batches of up to 64 per context (one launch per stage for the
+whole batch).
+"""
+from __future__ import annotations
+
+import time
+from typing import Dict, List, Sequence, Tuple
+
+import numpy as np
+
+from . import grids
+from .inputs import FLUX, SCHEME, TIME_LUSGS, TURB_SA, Params
+
+
+def warmstart_cases(n: int, seed: int, nx: int = 257, ny: int = 65) -> List[Tuple[Params, list, float]]:
+    """n cases drawn from the polar box: (params, blocks, t/c)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        M = rng.uniform(0.3, 0.8)
+        aoa = rng.uniform(-2.0, 8.0)
+        re = 10.0 ** rng.uniform(6.0, 7.0)
+        tc = rng.uniform(0.09, 0.15)
+        p = Params(Ma=M, AoA=aoa, Re=re, Pr=0.72, If_viscous=1, Iflag_turbulence_model=TURB_SA,
+                   Iflag_local_dt=1, CFL=5.0, dtmax=1.0e3, dtmin=1.0e-12, Time_Method=TIME_LUSGS,
+                   Iflag_Scheme=SCHEME["MUSCL3"], Iflag_flux=FLUX["ROE"], IFlag_Reconstruction=0,
+                   Num_Mesh=1, Twall=-1.0, vt_inf=3.0, mg_lusgs=1, xaxis=0.25)
+        first = 1.0e-6 * 6.5e6 / re * 4.0
+        blocks = grids.naca_cgrid(nx, ny, m=0.0, p=0.0, t=tc, radius=20.0, n_wake=(nx - 1) // 8 + 1,
+                                  first=first, nblocks=1)
+        out.append((p, blocks, tc))
+    return out
+
+
+def _solver(gpu, chunk, bits):
+    s = gpu.Solver([(p, b) for p, b, _ in chunk])
+    s.set_lusgs_precision(bits)
+    for c, (_, _, tc) in enumerate(chunk, start=1):
+        s.set_case_shape(c, tc)
+    return s
+
+
+def generate(gpu, net, cases, steps: int, batch: int = 64, bits: int = 32) -> Dict:
+    """Solve the cases in batches for `steps` iterations from the freestream
+    and add every fine-mesh cell of the result to the network's samples."""
+    t0 = time.perf_counter()
+    drops = []
+    for k in range(0, len(cases), batch):
+        chunk = cases[k:k + batch]
+        s = _solver(gpu, chunk, bits)
+        s.init_flow()
+        s.step(1)
+        r0 = np.array([_rms(s, c) for c in range(1, len(chunk) + 1)])
+        s.step(steps - 1)
+        r = np.array([_rms(s, c) for c in range(1, len(chunk) + 1)])
+        drops.extend(list(r / r0))
+        net.add_samples(s)
+        s.close()
+    d = np.array(drops)
+    return {"cases": len(cases), "steps": steps, "seconds": time.perf_counter() - t0,
+            "samples": net.num_samples(), "drop_median": float(np.nanmedian(d)),
+            "drop_max": float(np.nanmax(d))}
+
+
+def train(net, steps: int, batch: int = 16384, lr: float = 1e-3) -> Dict:
+    """Adam with the learning rate cut by 10 for the last 30 % of the steps."""
+    t0 = time.perf_counter()
+    net.fit_normalization()
+    first = net.train(1, batch=batch, lr=lr)
+    k1 = int(0.7 * steps)
+    mid = net.train(max(k1 - 1, 1), batch=batch, lr=lr)
+    last = net.train(max(steps - k1, 1), batch=batch, lr=lr * 0.1)
+    return {"steps": steps, "batch": batch, "seconds": time.perf_counter() - t0, "loss_first": first,
+            "loss_mid": mid, "loss_last": last}
+
+
+def _rms(s, c):
+    try:
+        return s.norms(c)[1][0]
+    except Exception:
+        return float("nan")
+
+
+def converge(gpu, cases, start: str, bits: int, r0=None, net=None, targets=(1e-4, 1e-6, 1e-8),
+             max_steps: int = 30000, check: int = 50) -> Dict:
+    """Run all cases of `cases` in one context until every case's
+    Res_rms(1) <= min(targets) x r0 or max_steps (r0: each case's
+    freestream-start first residual, measured here when not given).
+    start: 'freestream' or 'warm' (the network's prediction).  Records per
+    case and target the first step and wall time at which it was reached."""
+    s = _solver(gpu, cases, bits)
+    n = len(cases)
+    if r0 is None:
+        s.init_flow()
+        s.step(1)
+        r0 = np.array([_rms(s, c) for c in range(1, n + 1)])
+    s.sync()
+    t0 = time.perf_counter()
+    fallback = 0
+    if start == "warm":
+        fallback = net.warm_start(s)
+    else:
+        s.init_flow()
+    t_start = time.perf_counter() - t0
+    first = {t: np.full(n, -1) for t in targets}
+    when = {t: np.full(n, np.nan) for t in targets}
+    steps = 0
+    ratio = np.ones(n)
+    while steps < max_steps:
+        s.step(check)
+        steps += check
+        ratio = np.array([_rms(s, c) for c in range(1, n + 1)]) / r0
+        el = time.perf_counter() - t0
+        for t in targets:
+            new = (ratio <= t) & (first[t] < 0)
+            first[t][new] = steps
+            when[t][new] = el
+        if np.all(first[min(targets)] >= 0):
+            break
+    wall = time.perf_counter() - t0
+    forces = np.array([s.forces(c) for c in range(1, n + 1)])
+    s.close()
+    per = {}
+    for t in targets:
+        ok = first[t] >= 0
+        per[f"{t:.0e}"] = {"reached": int(ok.sum()),
+                           "steps_median": float(np.median(first[t][ok])) if ok.any() else None,
+                           "seconds_all": float(np.max(when[t])) if ok.all() else None,
+                           "seconds_p90": float(np.sort(when[t][ok])[int(0.9 * n) - 1]) if ok.sum() >= int(0.9 * n)
+                           and int(0.9 * n) >= 1 else None,
+                           "steps_per_case": first[t].tolist()}
+    return {"start": start, "bits": bits, "cases": n, "steps": steps, "seconds": wall, "start_seconds": t_start,
+            "fallback": fallback, "final_drop_max": float(np.nanmax(ratio)), "targets": per,
+            "forces": forces, "r0": r0}
+
+
+def evaluate(gpu, net, held, targets=(1e-4, 1e-6, 1e-8), max_steps=30000, plain_sample=4) -> Dict:
+    """The held-out cases three ways: (1) batched, FP32 LU-SGS, warm start;
+    (2) batched, FP32 LU-SGS, freestream; (3) the plain drop-in -- one case
+    per context, FP64, freestream -- on the first `plain_sample` cases.  The
+    force differences of (1) against (3) on those cases are reported."""
+    free = converge(gpu, held, "freestream", 32, targets=targets, max_steps=max_steps)
+    warm = converge(gpu, held, "warm", 32, r0=free["r0"], net=net, targets=targets, max_steps=max_steps)
+    plain = []
+    for k in range(min(plain_sample, len(held))):
+        plain.append(converge(gpu, [held[k]], "freestream", 64, r0=free["r0"][k:k + 1], targets=targets,
+                              max_steps=max_steps))
+    ferr = max(float(np.max(np.abs(warm["forces"][k] - plain[k]["forces"][0]))) for k in range(len(plain)))
+    ms_plain = float(np.mean([p["seconds"] / max(p["steps"], 1) for p in plain])) * 1e3
+    ms_batch = warm["seconds"] / max(warm["steps"], 1) * 1e3
+
+    def strip(d):
+        return {k: v for k, v in d.items() if k not in ("forces", "r0")}
+
+    return {"targets": [f"{t:.0e}" for t in targets], "warm_batched_mixed": strip(warm),
+            "freestream_batched_mixed": strip(free), "plain_sample": [strip(p) for p in plain],
+            "ms_per_step_plain_one_case_fp64": ms_plain, "ms_per_step_batched_mixed_all_cases": ms_batch,
+            "force_error_vs_plain_fp64": ferr}
