@@ -262,8 +262,21 @@ int ec2d_mlp_set_normalization(ec2d_mlp *m, const float *nrm);
 /* loss and gradients for B standardised rows (x: B x 7, y: B x 5, B a multiple
  * of 256) */
 int ec2d_mlp_loss_grad(ec2d_mlp *m, const float *x, const float *y, int B, double *loss);
+/* GEMM path of the network: 1 = tcgen05 kernels (accumulators in tensor
+ * memory, the default), 0 = mma.sync kernels.  A tcgen05 wait that times out makes the
+ * call return EC2D_ERR_TIMEOUT. */
+int ec2d_mlp_set_gemm(ec2d_mlp *m, int kind);
 /* un-standardised predictions (n x 5) for raw features (n x 7), host arrays */
 int ec2d_mlp_predict(ec2d_mlp *m, const float *feat, long long n, float *pred);
+
+/* Autotuner.  No counterpart in the reference.  Times `trial_steps` steps of
+ * every candidate launch configuration on the context's own cases and keeps
+ * the fastest: CTAs per block of the FP64 LU-SGS wavefront (1, or a thread-
+ * block cluster of 2, 4, 8 CTAs splitting the rows) and whether the i- and
+ * j-face flux kernels run concurrently on two streams.  The fine-mesh U and
+ * the step counters are restored afterwards.  Outputs (may be NULL): the
+ * choices and the winner's milliseconds per step. */
+int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *concurrent, double *ms_per_step);
 
 /* Wait for all queued work of the context. */
 int ec2d_sync(ec2d_ctx *ctx);

@@ -93,6 +93,8 @@ struct Level {
 struct ec2d_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;           // second stream for concurrent independent kernels
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::vector<HCase> cases;
   bool setup_done = false;
   int num_mesh = 1;
@@ -109,6 +111,7 @@ struct ec2d_ctx {
   long long launches = 0;
   int lusgs_cs = 1;  // CTAs per block in the LU-SGS wavefront (1: one CTA, >1: a cluster)
   bool lusgs_fp32 = false;  // LU-SGS sweeps in FP32 (mixed-precision mode)
+  bool concurrent = true;   // i- and j-face flux kernels on two streams
   bool timing = false;
   // one pseudo-time step (single grid or V-cycle) captured as a CUDA graph:
   // the replay stands for graph_launches kernel launches and advances the
@@ -581,17 +584,33 @@ void residual(ec2d_ctx *ctx, int l) {
     else if (L.turb == Turb_SST) K(ctx, "sst", l, 4, [&] { launch_sst(L, s); });
     else if (L.turb == Turb_BL) K(ctx, "bl", l, 2, [&] { launch_bl(L, s); });
   }
-  K(ctx, "k_flux_i", l, 1, [&] { launch_flux_i(L, s); });
-  K(ctx, "k_flux_j", l, 1, [&] { launch_flux_j(L, s); });
-  K(ctx, "k_res", l, 1, [&] { launch_res(L, s); });
+  // the i- and j-face kernels read the same primitives and write separate
+  // planes: they run concurrently on two streams (graph branches); with
+  // kernel timing on they run one after the other
+  if (!ctx->timing && ctx->concurrent) {
+    ctx->launches += 2;
+    cudaEventRecord(ctx->ev_fork, s);
+    cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0);
+    launch_flux_j(L, ctx->side);
+    launch_flux_i(L, s);
+    cudaEventRecord(ctx->ev_join, ctx->side);
+    cudaStreamWaitEvent(s, ctx->ev_join, 0);
+  } else {
+    K(ctx, "k_flux_i", l, 1, [&] { launch_flux_i(L, s); });
+    K(ctx, "k_flux_j", l, 1, [&] { launch_flux_j(L, s); });
+  }
+  const bool dual = ctx->P.Time_Method == Time_Dual && l == 1;
+  const bool fused = !L.fdm && !dual;  // Res final after k_res: norm partials fused into it
+  K(ctx, "k_res", l, 1, [&] { launch_res(L, fused, s); });
   if (L.fdm) K(ctx, "fdm", l, 3, [&] { launch_fdm(L, s); });
-  if (ctx->P.Time_Method == Time_Dual && l == 1) {
+  if (dual) {
     double sfac;
     if (ctx->dual_iflag1 == 0) { ctx->dual_iflag1 = 1; sfac = 1.0 / (3.0 * ctx->P.dt_global); }
     else sfac = 1.0 / (2.0 * ctx->P.dt_global);
     K(ctx, "k_dual", l, 1, [&] { launch_dual_term(L, sfac, s); });
   }
-  K(ctx, "norms", l, 2, [&] { launch_norms(L, lv.d_case_tile0, lv.d_case_ntile, lv.d_case_ncell, s); });
+  K(ctx, "norms", l, fused ? 1 : 2,
+    [&] { launch_norms(L, lv.d_case_tile0, lv.d_case_ntile, lv.d_case_ncell, !fused, s); });
 }
 
 void bc_all(ec2d_ctx *ctx, int l) {
@@ -873,7 +892,13 @@ int ec2d_create(int device, ec2d_ctx **out) {
   ec2d_ctx *c = new ec2d_ctx();
   c->device = device;
   if (const char *e = getenv("EC2D_LUSGS_CLUSTER")) c->lusgs_cs = std::max(1, std::min(8, atoi(e)));
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { delete c; return EC2D_ERR_CUDA; }
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+    delete c;
+    return EC2D_ERR_CUDA;
+  }
   *out = c;
   return EC2D_OK;
 }
@@ -889,6 +914,10 @@ void ec2d_destroy(ec2d_ctx *ctx) {
   if (ctx->d_stage) cudaFree(ctx->d_stage);
   if (ctx->d_shape) cudaFree(ctx->d_shape);
   if (ctx->step_graph) cudaGraphExecDestroy(ctx->step_graph);
+  cudaStreamSynchronize(ctx->side);
+  cudaEventDestroy(ctx->ev_fork);
+  cudaEventDestroy(ctx->ev_join);
+  cudaStreamDestroy(ctx->side);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -1081,6 +1110,72 @@ int ec2d_set_graphs(ec2d_ctx *ctx, int enable) {
   if (!ctx) return EC2D_ERR_ARG;
   ctx->use_graphs = enable != 0;
   return EC2D_OK;
+}
+
+static void drop_graph(ec2d_ctx *ctx) {
+  if (ctx->step_graph) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaGraphExecDestroy(ctx->step_graph);
+    ctx->step_graph = nullptr;
+  }
+}
+
+int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *concurrent, double *ms_per_step) {
+  if (!ctx || !ctx->setup_done || trial_steps < 1) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  // snapshot of the state a trial changes: fine-mesh U and the step counters
+  // (coarse levels are rebuilt from the fine mesh by every V-cycle)
+  const Level &lv = ctx->lv[1];
+  const size_t bytes = (size_t)lv.L.nvar * lv.F * sizeof(double);
+  double *snap = nullptr;
+  CK(cudaMalloc(&snap, bytes));
+  CK(cudaMemcpyAsync(snap, lv.L.U, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+  std::vector<std::array<int, 4>> ks(ctx->cases.size());
+  std::vector<std::array<double, 4>> ts(ctx->cases.size());
+  for (size_t c = 0; c < ctx->cases.size(); c++)
+    for (int l = 0; l < 4; l++) { ks[c][l] = ctx->cases[c].kstep[l]; ts[c][l] = ctx->cases[c].tt[l]; }
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  // candidates: CTAs per block of the FP64 wavefront (a cluster when > 1;
+  // the FP32 sweep is one CTA per block) x concurrent face kernels
+  std::vector<int> css = {1};
+  if (!ctx->lusgs_fp32 && ctx->P.Time_Method == Time_LU_SGS)
+    for (int c : {2, 4, 8}) css.push_back(c);
+  const int old_cs = ctx->lusgs_cs;
+  const bool old_cc = ctx->concurrent;
+  double best = 1e30;
+  int best_cs = old_cs, best_cc = old_cc ? 1 : 0, r = EC2D_OK;
+  for (int cs : css) {
+    for (int cc = 0; cc < 2 && r == EC2D_OK; cc++) {
+      ctx->lusgs_cs = cs;
+      ctx->concurrent = cc != 0;
+      drop_graph(ctx);
+      if ((r = ec2d_step(ctx, 1)) != EC2D_OK) break;
+      cudaEventRecord(a, ctx->stream);
+      if ((r = ec2d_step(ctx, trial_steps)) != EC2D_OK) break;
+      cudaEventRecord(b, ctx->stream);
+      cudaEventSynchronize(b);
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, a, b);
+      if (ms / trial_steps < best) { best = ms / trial_steps; best_cs = cs; best_cc = cc; }
+    }
+  }
+  ctx->lusgs_cs = r == EC2D_OK ? best_cs : old_cs;
+  ctx->concurrent = r == EC2D_OK ? best_cc != 0 : old_cc;
+  drop_graph(ctx);
+  cudaMemcpyAsync(lv.L.U, snap, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(snap);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  for (size_t c = 0; c < ctx->cases.size(); c++)
+    for (int l = 0; l < 4; l++) { ctx->cases[c].kstep[l] = ks[c][l]; ctx->cases[c].tt[l] = ts[c][l]; }
+  if (r) return r;
+  if (lusgs_cs) *lusgs_cs = ctx->lusgs_cs;
+  if (concurrent) *concurrent = ctx->concurrent ? 1 : 0;
+  if (ms_per_step) *ms_per_step = best;
+  return check_launch(ctx);
 }
 
 int ec2d_set_lusgs_precision(ec2d_ctx *ctx, int bits) {
@@ -1467,7 +1562,8 @@ int ec2d_mlp_train(ec2d_mlp *m, int steps, int batch, double lr, double *loss_ou
   CK(cudaMemcpyAsync(&l, net.d_loss, sizeof(float), cudaMemcpyDeviceToHost, net.stream));
   CK(cudaStreamSynchronize(net.stream));
   if (loss_out) *loss_out = l;
-  return cudaGetLastError() == cudaSuccess ? EC2D_OK : EC2D_ERR_CUDA;
+  if (cudaGetLastError() != cudaSuccess) return EC2D_ERR_CUDA;
+  return net.check_err() ? EC2D_ERR_TIMEOUT : EC2D_OK;
 }
 
 int ec2d_mlp_warm_start(ec2d_mlp *m, ec2d_ctx *ctx, int *n_fallback) {
@@ -1489,6 +1585,7 @@ int ec2d_mlp_warm_start(ec2d_mlp *m, ec2d_ctx *ctx, int *n_fallback) {
   CK(cudaStreamSynchronize(ctx->stream));
   r = net.predict(feat, n, pred);
   CK(cudaStreamSynchronize(net.stream));
+  if (r == EC2D_OK && net.check_err()) r = EC2D_ERR_TIMEOUT;
   if (r == EC2D_OK) {
     launch_warm_start(L, pred, bad, ctx->stream);
     launch_bc(L, 1 | 2 | 4, ctx->stream);
@@ -1500,7 +1597,7 @@ int ec2d_mlp_warm_start(ec2d_mlp *m, ec2d_ctx *ctx, int *n_fallback) {
   cudaFree(feat);
   cudaFree(pred);
   cudaFree(bad);
-  if (r) return EC2D_ERR_CUDA;
+  if (r) return r == EC2D_ERR_TIMEOUT ? r : EC2D_ERR_CUDA;
   if (n_fallback) {
     int c = 0;
     for (int v : hb) c += v != 0;
@@ -1583,7 +1680,14 @@ int ec2d_mlp_loss_grad(ec2d_mlp *m, const float *x, const float *y, int B, doubl
   CK(cudaMemcpyAsync(&l, net.d_loss, sizeof(float), cudaMemcpyDeviceToHost, net.stream));
   CK(cudaStreamSynchronize(net.stream));
   if (loss) *loss = l;
-  return cudaGetLastError() == cudaSuccess ? EC2D_OK : EC2D_ERR_CUDA;
+  if (cudaGetLastError() != cudaSuccess) return EC2D_ERR_CUDA;
+  return net.check_err() ? EC2D_ERR_TIMEOUT : EC2D_OK;
+}
+
+int ec2d_mlp_set_gemm(ec2d_mlp *m, int kind) {
+  if (!m || (kind != 0 && kind != 1)) return EC2D_ERR_ARG;
+  m->net.gemm_kind = kind;
+  return EC2D_OK;
 }
 
 int ec2d_mlp_predict(ec2d_mlp *m, const float *feat, long long n, float *pred) {
@@ -1599,7 +1703,8 @@ int ec2d_mlp_predict(ec2d_mlp *m, const float *feat, long long n, float *pred) {
   if (r == 0) cudaMemcpy(pred, dp, (size_t)n * NOUT * sizeof(float), cudaMemcpyDeviceToHost);
   cudaFree(df);
   cudaFree(dp);
-  return r ? EC2D_ERR_CUDA : EC2D_OK;
+  if (r) return EC2D_ERR_CUDA;
+  return net.check_err() ? EC2D_ERR_TIMEOUT : EC2D_OK;
 }
 
 int ec2d_sync(ec2d_ctx *ctx) {

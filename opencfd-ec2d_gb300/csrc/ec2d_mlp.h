@@ -16,6 +16,24 @@ constexpr int KSPLIT = 32;    // K splits of the weight-gradient GEMM
 
 enum { EPI_F32 = 0, EPI_BIAS = 1, EPI_BIAS_SILU = 2, EPI_DSILU = 3, EPI_BF16 = 4 };
 
+// epilogue of C[M x N] = A[M x K] . B[N x K]^T
+struct Epi {
+  int mode;                 // EPI_*
+  const float *bias;        // [N] (bias modes)
+  float *zout;              // pre-activation out (EPI_BIAS_SILU), [M x ldz]
+  const float *zin;         // pre-activation in (EPI_DSILU), [M x ldz]
+  int ldz;
+  __nv_bfloat16 *hout;      // bf16 out (EPI_BIAS_SILU, EPI_DSILU, EPI_BF16)
+  float *fout;              // fp32 out (EPI_BIAS, EPI_F32)
+  int ldc;
+  long long split_stride;   // EPI_F32: offset between the K-split partial tiles
+};
+
+// tcgen05 (TMEM accumulator) GEMM, k_gemm_tc.cu: M % 128 == 0, N % 64 == 0,
+// (K / ksplit) % 64 == 0.  err: device flag set if an mbarrier wait timed out.
+void launch_gemm_tc(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, int M, int N, int K,
+                    int ksplit, const Epi &e, int *err, cudaStream_t s);
+
 struct Layer {
   float *w = nullptr, *b = nullptr;    // FP32 masters [out x in], [out]
   float *mw = nullptr, *vw = nullptr, *mb = nullptr, *vb = nullptr;  // Adam moments
@@ -30,6 +48,8 @@ struct Net {
   Layer L[MAX_HIDDEN + 1];
   float *nrm = nullptr;  // feature mean[NIN], std[NIN], target mean[NOUT], std[NOUT]
   int *d_step = nullptr;
+  int *d_err = nullptr;   // set by a tcgen05 GEMM whose mbarrier wait timed out
+  int gemm_kind = 1;      // 1: tcgen05 GEMMs (default), 0: mma.sync GEMMs
   float *d_loss = nullptr;
   double *d_moments = nullptr;
   // batch buffers
@@ -48,6 +68,8 @@ struct Net {
   int layer_in(int l) const;
   int layer_out(int l) const;
   void refresh_bf16();
+  void gemm(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, int M, int N, int K, int ksplit,
+            const Epi &e);
   int ensure_batch(int B);
   void forward(int B);
   void backward(int B);
@@ -56,6 +78,7 @@ struct Net {
   int fit_normalization();
   int reserve_samples(long long n);
   int predict(const float *feat, long long n, float *pred);
+  int check_err();  // 0, or 1 if a tcgen05 wait timed out since the last call
 };
 
 }  // namespace ec2d

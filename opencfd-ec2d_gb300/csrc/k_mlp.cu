@@ -65,18 +65,6 @@ __device__ __forceinline__ float dsilu(float z) {
   return s * (1.0f + z * (1.0f - s));
 }
 
-struct Epi {
-  int mode;                 // EPI_*
-  const float *bias;        // [N] (bias modes)
-  float *zout;              // pre-activation out (EPI_BIAS_SILU), [M x ldz]
-  const float *zin;         // pre-activation in (EPI_DSILU), [M x ldz]
-  int ldz;
-  __nv_bfloat16 *hout;      // bf16 out (EPI_BIAS_SILU, EPI_DSILU, EPI_BF16)
-  float *fout;              // fp32 out (EPI_BIAS, EPI_F32)
-  int ldc;
-  long long split_stride;   // EPI_F32: offset between the K-split partial tiles
-};
-
 // A: [M x K] (lda), B: [N x K] (ldb); K range of this CTA: blockIdx.z
 __global__ void __launch_bounds__(256) k_gemm_tn(const __nv_bfloat16 *__restrict__ A, int lda,
                                                  const __nv_bfloat16 *__restrict__ B, int ldb, int K, int ksplit,
@@ -454,10 +442,15 @@ void launch_warm_start(const Lvl &L, const float *pred, int *bad, cudaStream_t s
 // ---------------------------------------------------------------------------
 using namespace mlp;
 
-static void launch_gemm(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, int M, int N, int K,
-                        int ksplit, const Epi &e, cudaStream_t s) {
+// tcgen05 kernel when selected and the shape fits its tiles, else mma.sync
+void Net::gemm(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, int M, int N, int K, int ksplit,
+               const Epi &e) {
+  if (gemm_kind == 1 && M % 128 == 0 && N % 64 == 0 && (K / ksplit) % 64 == 0) {
+    launch_gemm_tc(A, lda, B, ldb, M, N, K, ksplit, e, d_err, stream);
+    return;
+  }
   dim3 grid(M / BM, N / BN, ksplit);
-  k_gemm_tn<<<grid, 256, 0, s>>>(A, lda, B, ldb, K, ksplit, e);
+  k_gemm_tn<<<grid, 256, 0, stream>>>(A, lda, B, ldb, K, ksplit, e);
 }
 
 static void transpose(const __nv_bfloat16 *in, int rows, int cols, int ldi, __nv_bfloat16 *out, int ldo,
@@ -523,6 +516,7 @@ int Net::init(int dev, int hidden, int w, unsigned long long seed_) {
   for (int c = 0; c < NOUT; c++) one[2 * NIN + NOUT + c] = 1.0f;
   cudaMemcpy(nrm, one.data(), one.size() * sizeof(float), cudaMemcpyHostToDevice);
   d_step = dev_alloc<int>(owned, 4);
+  d_err = dev_alloc<int>(owned, 4);
   d_loss = dev_alloc<float>(owned, 4);
   d_moments = dev_alloc<double>(owned, 2 * (NIN + NOUT));
   refresh_bf16();
@@ -571,7 +565,7 @@ void Net::forward(int B) {
     } else {
       e.mode = EPI_BIAS; e.bias = L[l].b; e.fout = out; e.ldc = NOUT_PAD;
     }
-    launch_gemm(in, ldin, L[l].wb, ni, B, no, ni, 1, e, stream);
+    gemm(in, ldin, L[l].wb, ni, B, no, ni, 1, e);
     in = H[l < nlin - 1 ? l : 0];
     ldin = width;
   }
@@ -594,8 +588,8 @@ void Net::backward(int B) {
     Epi e{};
     e.mode = EPI_F32; e.fout = part; e.ldc = ni; e.split_stride = (long long)no * ni;
     int ks = KSPLIT;
-    while (ks > 1 && (B / ks) % BK) ks >>= 1;
-    launch_gemm(T2, B, T1, B, no, ni, B, ks, e, stream);
+    while (ks > 1 && (B / ks) % 64) ks >>= 1;
+    gemm(T2, B, T1, B, no, ni, B, ks, e);
     long long n = (long long)no * ni;
     k_split_sum<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(part, ks, n, L[l].gw);
     // db = column sums of dz
@@ -606,7 +600,7 @@ void Net::backward(int B) {
     // dH_{l-1} = dz . W_l, times silu'(Z_{l-1}) : A = dz [B x no], B = W_l^T [ni x no]
     Epi d{};
     d.mode = EPI_DSILU; d.zin = Z[l - 1]; d.ldz = width; d.hout = bufs[l & 1]; d.ldc = width;
-    launch_gemm(dz, ldz, L[l].wt, no, B, ni, no, 1, d, stream);
+    gemm(dz, ldz, L[l].wt, no, B, ni, no, 1, d);
     dz = bufs[l & 1];
     ldz = width;
   }
@@ -680,6 +674,14 @@ int Net::predict(const float *f, long long n, float *pred) {
     k_unstage_rows<<<B / 256, 256, 0, stream>>>(out, NOUT_PAD, r0, B, n, nrm, pred);
   }
   return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+int Net::check_err() {
+  int h = 0;
+  cudaMemcpyAsync(&h, d_err, sizeof(int), cudaMemcpyDeviceToHost, stream);
+  cudaMemsetAsync(d_err, 0, sizeof(int), stream);
+  cudaStreamSynchronize(stream);
+  return h;
 }
 
 void Net::destroy() {

@@ -186,46 +186,84 @@ __global__ void __launch_bounds__(TILE) k_flux_j(Lvl L) {
 
 // flux differences (sub_Residual.f90:460-468), comput_Lvc (sub_NS_singlegrid.f90:352-388)
 // and comput_dt (sub_NS_singlegrid.f90:324-348) for interior cells
+// NORM: also the tile's partial norms of Res (the work of k_norm_partial,
+// same cells, same reduction tree, so the norms are bit-identical); only when
+// no later kernel of the residual stage changes Res (no FDM patch, no
+// dual-time term)
+template <bool NORM>
 __global__ void __launch_bounds__(TILE) k_res(Lvl L) {
   int bk, i, j;
-  if (!tile_ij(L, bk, i, j)) return;
-  const BlkDev &b = L.blk[bk];
-  if (i < 1 || i > b.nx - 1 || j < 1 || j > b.ny - 1) return;
-  const CaseDev &c = L.cs[b.cas];
-  const long long F = L.F, P = b.P;
-  long long id = fidx(b, i, j);
-  bool fdm = b.fdm && (i >= LFDM + 1 && i <= b.nx - LFDM - 1) && (j >= LFDM + 1 && j <= b.ny - LFDM - 1);
-  if (!fdm) {
+  bool act = tile_ij(L, bk, i, j);
+  if (act) {
+    const BlkDev &b0 = L.blk[bk];
+    act = i >= 1 && i <= b0.nx - 1 && j >= 1 && j <= b0.ny - 1;
+  }
+  if (!NORM && !act) return;
+  double vres[6] = {0, 0, 0, 0, 0, 0};
+  if (act) {
+    const BlkDev &b = L.blk[bk];
+    const CaseDev &c = L.cs[b.cas];
+    const long long F = L.F, P = b.P;
+    long long id = fidx(b, i, j);
+    bool fdm = b.fdm && (i >= LFDM + 1 && i <= b.nx - LFDM - 1) && (j >= LFDM + 1 && j <= b.ny - LFDM - 1);
+    if (!fdm) {
 #pragma unroll
-    for (int m = 0; m < 4; m++)
-      L.res[m * F + id] = L.fi[m * F + id + 1] - L.fi[m * F + id] + L.fj[m * F + id + P] - L.fj[m * F + id];
+      for (int m = 0; m < 4; m++) {
+        double r = L.fi[m * F + id + 1] - L.fi[m * F + id] + L.fj[m * F + id + P] - L.fj[m * F + id];
+        L.res[m * F + id] = r;
+        vres[m] = r;
+      }
+    }
+    if (NORM)
+      for (int m = 4; m < L.nvar; m++) vres[m] = L.res[m * F + id];
+    const double *g = L.geo;
+    double s0 = g[G_VOL * F + id];
+    double si = 0.5 * (g[G_SI * F + id] + g[G_SI * F + id + 1]);
+    double ni1 = 0.5 * (g[G_NI1 * F + id] + g[G_NI1 * F + id + 1]);
+    double ni2 = 0.5 * (g[G_NI2 * F + id] + g[G_NI2 * F + id + 1]);
+    double sj = 0.5 * (g[G_SJ * F + id] + g[G_SJ * F + id + P]);
+    double nj1 = 0.5 * (g[G_NJ1 * F + id] + g[G_NJ1 * F + id + P]);
+    double nj2 = 0.5 * (g[G_NJ2 * F + id] + g[G_NJ2 * F + id + P]);
+    double uu = L.q[Q_U * F + id], vv = L.q[Q_V * F + id], cc = L.q[Q_C * F + id], d = L.q[Q_D * F + id];
+    double uni = uu * ni1 + vv * ni2, unj = uu * nj1 + vv * nj2;
+    double Lci = (fabs(uni) + cc) * si, Lcj = (fabs(unj) + cc) * sj;
+    double amu = L.visc ? L.amu[id] : 0.0, amut = L.visc ? L.amut[id] : 0.0;
+    double tmp1 = c.gamma / d * (amu / c.Pr + amut / PrT);
+    double Lvi = tmp1 * si * si / s0, Lvj = tmp1 * sj * sj / s0;
+    L.lc[L_CI * F + id] = Lci;
+    L.lc[L_CJ * F + id] = Lcj;
+    L.lc[L_VI * F + id] = Lvi;
+    L.lc[L_VJ * F + id] = Lvj;
+    double dt;
+    if (c.local_dt == 0) dt = c.dt_global;
+    else {
+      dt = c.CFL * s0 / (Lci + Lcj + 1.0 * (Lvi + Lvj));
+      if (dt > c.dtmax) dt = c.dtmax;
+      if (dt < c.dtmin) dt = c.dtmin;
+    }
+    L.lc[L_DT * F + id] = dt;
   }
-  const double *g = L.geo;
-  double s0 = g[G_VOL * F + id];
-  double si = 0.5 * (g[G_SI * F + id] + g[G_SI * F + id + 1]);
-  double ni1 = 0.5 * (g[G_NI1 * F + id] + g[G_NI1 * F + id + 1]);
-  double ni2 = 0.5 * (g[G_NI2 * F + id] + g[G_NI2 * F + id + 1]);
-  double sj = 0.5 * (g[G_SJ * F + id] + g[G_SJ * F + id + P]);
-  double nj1 = 0.5 * (g[G_NJ1 * F + id] + g[G_NJ1 * F + id + P]);
-  double nj2 = 0.5 * (g[G_NJ2 * F + id] + g[G_NJ2 * F + id + P]);
-  double uu = L.q[Q_U * F + id], vv = L.q[Q_V * F + id], cc = L.q[Q_C * F + id], d = L.q[Q_D * F + id];
-  double uni = uu * ni1 + vv * ni2, unj = uu * nj1 + vv * nj2;
-  double Lci = (fabs(uni) + cc) * si, Lcj = (fabs(unj) + cc) * sj;
-  double amu = L.visc ? L.amu[id] : 0.0, amut = L.visc ? L.amut[id] : 0.0;
-  double tmp1 = c.gamma / d * (amu / c.Pr + amut / PrT);
-  double Lvi = tmp1 * si * si / s0, Lvj = tmp1 * sj * sj / s0;
-  L.lc[L_CI * F + id] = Lci;
-  L.lc[L_CJ * F + id] = Lcj;
-  L.lc[L_VI * F + id] = Lvi;
-  L.lc[L_VJ * F + id] = Lvj;
-  double dt;
-  if (c.local_dt == 0) dt = c.dt_global;
-  else {
-    dt = c.CFL * s0 / (Lci + Lcj + 1.0 * (Lvi + Lvj));
-    if (dt > c.dtmax) dt = c.dtmax;
-    if (dt < c.dtmin) dt = c.dtmin;
+  if (NORM) {
+    __shared__ double smax[6][TILE / 32], ssum[6][TILE / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int m = 0; m < 6; m++) {
+      double a = act && m < L.nvar ? fabs(vres[m]) : 0.0, q = act && m < L.nvar ? vres[m] * vres[m] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) {
+        a = fmax(a, __shfl_down_sync(0xffffffffu, a, o));
+        q += __shfl_down_sync(0xffffffffu, q, o);
+      }
+      if (lane == 0) { smax[m][w] = a; ssum[m][w] = q; }
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+      int m = threadIdx.x;
+      double a = 0.0, q = 0.0;
+      for (int k = 0; k < TILE / 32; k++) { a = fmax(a, smax[m][k]); q += ssum[m][k]; }
+      L.npart[(size_t)blockIdx.x * 12 + m] = a;
+      L.npart[(size_t)blockIdx.x * 12 + 6 + m] = q;
+    }
   }
-  L.lc[L_DT * F + id] = dt;
 }
 
 // per-tile partial norms of Res (max |Res| and sum Res^2 per variable)
@@ -289,10 +327,13 @@ __global__ void k_norm_final(Lvl L, const int *case_tile0, const int *case_ntile
 void launch_prim(const Lvl &L, cudaStream_t s) { k_prim<<<L.ntiles, TILE, 0, s>>>(L); }
 void launch_flux_i(const Lvl &L, cudaStream_t s) { k_flux_i<<<L.ntiles, TILE, 0, s>>>(L); }
 void launch_flux_j(const Lvl &L, cudaStream_t s) { k_flux_j<<<L.ntiles, TILE, 0, s>>>(L); }
-void launch_res(const Lvl &L, cudaStream_t s) { k_res<<<L.ntiles, TILE, 0, s>>>(L); }
-void launch_norms(const Lvl &L, const int *case_tile0, const int *case_ntile, const int *case_ncell,
+void launch_res(const Lvl &L, bool with_norms, cudaStream_t s) {
+  if (with_norms) k_res<true><<<L.ntiles, TILE, 0, s>>>(L);
+  else k_res<false><<<L.ntiles, TILE, 0, s>>>(L);
+}
+void launch_norms(const Lvl &L, const int *case_tile0, const int *case_ntile, const int *case_ncell, bool partials,
                   cudaStream_t s) {
-  k_norm_partial<<<L.ntiles, TILE, 0, s>>>(L);
+  if (partials) k_norm_partial<<<L.ntiles, TILE, 0, s>>>(L);
   k_norm_final<<<L.ncase, dim3(32, 12), 0, s>>>(L, case_tile0, case_ntile, case_ncell);
 }
 

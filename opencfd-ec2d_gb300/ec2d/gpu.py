@@ -117,6 +117,7 @@ def lib():
         "ec2d_run_to_drop": ([vp, ctypes.c_double, dp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ip, dp, dp],
                              ctypes.c_int),
         "ec2d_set_case_shape": ([vp, ctypes.c_int, ctypes.c_double], ctypes.c_int),
+        "ec2d_autotune": ([vp, ctypes.c_int, ip, ip, dp], ctypes.c_int),
         "ec2d_mlp_create": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, cpp], ctypes.c_int),
         "ec2d_mlp_destroy": ([vp], None),
         "ec2d_mlp_add_samples": ([vp, vp], ctypes.c_int),
@@ -134,6 +135,7 @@ def lib():
         "ec2d_mlp_set_normalization": ([vp, fp], ctypes.c_int),
         "ec2d_mlp_loss_grad": ([vp, fp, fp, ctypes.c_int, dp], ctypes.c_int),
         "ec2d_mlp_predict": ([vp, fp, ctypes.c_longlong, fp], ctypes.c_int),
+        "ec2d_mlp_set_gemm": ([vp, ctypes.c_int], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -315,6 +317,14 @@ class Solver:
                                     ctypes.byref(n), ctypes.byref(w), ctypes.byref(t)), "ec2d_run_to_drop")
         return n.value, w.value, t.value
 
+    def autotune(self, trial_steps=5):
+        """Pick the fastest launch configuration; returns (cluster CTAs,
+        concurrent flux kernels, ms per step)."""
+        cs, cc, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        _ck(self.L.ec2d_autotune(self.h, int(trial_steps), ctypes.byref(cs), ctypes.byref(cc), ctypes.byref(ms)),
+            "ec2d_autotune")
+        return cs.value, cc.value, ms.value
+
     def set_case_shape(self, case, shape):
         """Per-case shape feature of the warm-start network (the airfoil t/c)."""
         _ck(self.L.ec2d_set_case_shape(self.h, case, float(shape)), "ec2d_set_case_shape")
@@ -363,6 +373,10 @@ class WarmStartNet:
             self.close()
         except Exception:
             pass
+
+    def set_gemm(self, kind):
+        """1: tcgen05 GEMM kernels, 0: mma.sync GEMM kernels."""
+        _ck(self.L.ec2d_mlp_set_gemm(self.h, int(kind)), "ec2d_mlp_set_gemm")
 
     def add_samples(self, solver):
         _ck(self.L.ec2d_mlp_add_samples(self.h, solver.h), "ec2d_mlp_add_samples")

@@ -32,3 +32,27 @@ def test_graph_replay_equals_direct(gpu_lib, tm, num_mesh):
     np.testing.assert_array_equal(rb[1], ra[1])
     assert rb[2] == ra[2] == 7
     assert rb[3] == ra[3]
+
+
+def test_autotune_keeps_state_and_results(gpu_lib):
+    """The autotuner restores U and the counters, and its choice changes only
+    the launch configuration: the steps after it match an untuned solver."""
+    p, bl = small_case(nx=65, ny=17, Ma=0.6, AoA=2.0, Iflag_flux=4, Iflag_Scheme=5, Time_Method=0,
+                       Num_Mesh=3, CFL=4.0, Pre_Step_Mesh=(0, 5, 5), mg_lusgs=1, nblocks=2)
+    a = make_gpu(p, bl)
+    a.init_flow()
+    a.step(2)
+    u0 = [a.download_U(1, 1, b) for b in (1, 2)]
+    k0 = a.norms(1)[2]
+    cs, cc, ms = a.autotune(trial_steps=3)
+    assert cs in (1, 2, 4, 8) and cc in (0, 1) and ms > 0.0
+    for b in (1, 2):
+        np.testing.assert_array_equal(a.download_U(1, 1, b), u0[b - 1])
+    assert a.norms(1)[2] == k0
+    ref = make_gpu(p, bl)
+    ref.init_flow()
+    ref.step(2)
+    a.step(4)
+    ref.step(4)
+    for b in (1, 2):
+        np.testing.assert_allclose(a.download_U(1, 1, b), ref.download_U(1, 1, b), rtol=1e-13, atol=1e-15)

@@ -80,3 +80,24 @@ def test_training_on_solved_fields_and_warm_start_gain(gpu_lib):
     n_warm, ratio_b, _ = b.run_to_drop(drop=1e-4, r0=r0, max_steps=20000, check_every=10)
     assert ratio_a <= 1e-4 and ratio_b <= 1e-4
     assert n_warm <= 0.7 * (n_free + 1), (n_warm, n_free)
+
+
+def test_tcgen05_gemm_matches_mma_sync(gpu_lib):
+    """The tcgen05 GEMM path (TMEM accumulators) against the mma.sync path on
+    the same weights and batch: loss and every gradient agree to FP32
+    accumulation-order round-off (BF16 activations may differ by one ulp)."""
+    rng = np.random.default_rng(9)
+    x = rng.normal(size=(1024, mo.NIN)).astype(np.float32)
+    y = rng.normal(size=(1024, mo.NOUT)).astype(np.float32)
+    res = []
+    for kind in (0, 1):
+        net = gpu_lib.WarmStartNet(hidden=3, width=256, seed=3)
+        net.set_gemm(kind)
+        loss = net.loss_grad(x, y)
+        res.append((loss, [net.get_grads(l) for l in range(net.nlin)]))
+        net.close()
+    (l0, g0), (l1, g1) = res
+    assert abs(l1 - l0) <= 1e-4 * abs(l0), (l0, l1)
+    for (a, ab), (b, bb) in zip(g0, g1):
+        assert np.linalg.norm(a - b) <= 5e-3 * np.linalg.norm(a)
+        assert np.linalg.norm(ab - bb) <= 5e-3 * np.linalg.norm(ab) + 1e-12
