@@ -263,8 +263,8 @@ int ec2d_mlp_set_normalization(ec2d_mlp *m, const float *nrm);
  * of 256) */
 int ec2d_mlp_loss_grad(ec2d_mlp *m, const float *x, const float *y, int B, double *loss);
 /* GEMM path of the network: 1 = tcgen05 kernels (accumulators in tensor
- * memory, the default), 0 = mma.sync kernels.  A tcgen05 wait that times out makes the
- * call return EC2D_ERR_TIMEOUT. */
+ * memory; the default), 0 = mma.sync kernels.  A tcgen05 wait that times
+ * out makes the call return EC2D_ERR_TIMEOUT. */
 int ec2d_mlp_set_gemm(ec2d_mlp *m, int kind);
 /* un-standardised predictions (n x 5) for raw features (n x 7), host arrays */
 int ec2d_mlp_predict(ec2d_mlp *m, const float *feat, long long n, float *pred);
