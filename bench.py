@@ -312,6 +312,45 @@ def leg_polar(args):
     return res
 
 
+def leg_mlp(args):
+    """Training-step throughput of the warm-start network (6 hidden layers of
+    256, batch 16,384) with the tcgen05 GEMM kernels and with the mma.sync
+    ones.  Samples: one 257x65 SA case after 50 steps (the values do not
+    change the work).  Algorithmic FLOPs of a step: forward 2 B (7x256 +
+    5x256^2 + 256x5), backward twice that less the input-gradient product of
+    the first layer."""
+    from ec2d import gpu, learn
+    case = learn.warmstart_cases(1, seed=5)
+    s = gpu.Solver([(case[0][0], case[0][1])])
+    s.init_flow()
+    s.step(50)
+    B, steps = 16384, max(args.steps, 50)
+    fwd = 2.0 * B * (7 * 256 + 5 * 256 * 256 + 256 * 5)
+    flops = fwd + 2.0 * fwd - 2.0 * B * 7 * 256
+    out = {"batch": B, "hidden": "6 x 256", "algorithmic_gflop_per_step": flops / 1e9}
+    hbm_peak, _ = peaks()
+    try:
+        with open(PEAKS) as fh:
+            bf16 = float(json.load(fh)["bf16_tflops"])
+    except Exception:
+        bf16 = 1900.0
+    for kind, name in ((1, "tcgen05"), (0, "mma_sync")):
+        net = gpu.WarmStartNet(hidden=6, width=256, seed=1)
+        net.set_gemm(kind)
+        net.add_samples(s)
+        net.fit_normalization()
+        net.train(20, batch=B)
+        t0 = time.perf_counter()
+        loss = net.train(steps, batch=B)
+        dt = (time.perf_counter() - t0) / steps
+        out[name] = {"ms_per_step": dt * 1e3, "tflops": flops / dt / 1e12, "frac_of_bf16_peak": flops / dt / 1e12 / bf16,
+                     "loss": loss}
+        net.close()
+    s.close()
+    out["bf16_peak_tflops"] = bf16
+    return out
+
+
 def leg_learned(args):
     """Learned warm start (512 training + 64 held-out SA cases on a 257x65
     C-grid): data generation, training, and the held-out polar to a 1e-8 drop
@@ -498,7 +537,7 @@ def main():
     ap.add_argument("--drop-cap", type=float, default=60.0, help="seconds per time-to-drop run (0: skip)")
     ap.add_argument("--no-residual-hbm", dest="residual_hbm", action="store_false",
                     help="skip the residual bandwidth measurement on the 4.19 M-cell grid")
-    ap.add_argument("--leg", default="all", choices=["all", "residual_hbm", "polar", "learned"],
+    ap.add_argument("--leg", default="all", choices=["all", "residual_hbm", "polar", "learned", "mlp"],
                     help="residual_hbm: the 4.19 M-cell residual alone (for profiling); polar: the 64-case "
                          "batched polar; learned: the learned warm start end to end")
     ap.add_argument("--ws-train", type=int, default=512)
@@ -518,6 +557,8 @@ def main():
             out = residual_hbm(torch, gpu, 0)
         elif args.leg == "polar":
             out = leg_polar(args)
+        elif args.leg == "mlp":
+            out = leg_mlp(args)
         else:
             out = leg_learned(args)
         print(json.dumps({args.leg: out}, default=float), flush=True)
