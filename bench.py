@@ -389,6 +389,7 @@ def run_gb300(args, rank, world):
     for _ in range(max(3, args.warmup)):
         g.step(1)
     g.sync()
+    tuned = {"fp64": dict(zip(("lusgs_ctas", "rows_per_warp", "concurrent_faces", "ms"), g.autotune(3)))}
 
     def barrier():
         torch.cuda.synchronize()
@@ -446,6 +447,7 @@ def run_gb300(args, rank, world):
     for _ in range(3):
         g.step(1)
     g.sync()
+    tuned["mixed"] = dict(zip(("lusgs_ctas", "rows_per_warp", "concurrent_faces", "ms"), g.autotune(3)))
     barrier()
     ms32, launches32 = timed_steps(torch, g, stream, flush, args.steps)
     barrier()
@@ -456,6 +458,7 @@ def run_gb300(args, rank, world):
              "kernels": {f"{n}@{l}": round(m / args.steps, 4) for (n, l), (c, _, m) in
                          sorted(kt32.items(), key=lambda kv: -kv[1][2])[:8]}}
     g.set_lusgs_precision(64)
+    g.autotune(3)
 
     # ---- end to end through the C-ABI with host buffers --------------------
     nbl = len(blocks)
@@ -488,6 +491,7 @@ def run_gb300(args, rank, world):
         cl, cd, cm = g.forces(1)
         ttd["fp64"]["forces"] = {"cl": cl, "cd": cd, "cm": cm}
         g.set_lusgs_precision(32)
+        g.autotune(3)
         ttd["mixed"] = time_to_drop(g, cells, cap_s=args.drop_cap)
         cl2, cd2, cm2 = g.forces(1)
         ttd["mixed"]["forces"] = {"cl": cl2, "cd": cd2, "cm": cm2}
@@ -515,7 +519,8 @@ def run_gb300(args, rank, world):
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": {"workload": WORKLOAD, "cells": cells, "step": "one 3-level V-cycle",
-                           "l2": "flushed before every timed step (512 MiB write)", "parallelism": f"replicas{world}"},
+                           "l2": "flushed before every timed step (512 MiB write)", "parallelism": f"replicas{world}",
+                           "autotuned": tuned},
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
                 "gpu_launches": launches * args.steps, "launches_per_step": launches,
                 "mixed_precision": mixed, "time_to_drop": ttd, "residual_hbm": big,

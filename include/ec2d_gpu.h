@@ -271,12 +271,14 @@ int ec2d_mlp_predict(ec2d_mlp *m, const float *feat, long long n, float *pred);
 
 /* Autotuner.  No counterpart in the reference.  Times `trial_steps` steps of
  * every candidate launch configuration on the context's own cases and keeps
- * the fastest: CTAs per block of the FP64 LU-SGS wavefront (1, or a thread-
- * block cluster of 2, 4, 8 CTAs splitting the rows) and whether the i- and
- * j-face flux kernels run concurrently on two streams.  The fine-mesh U and
- * the step counters are restored afterwards.  Outputs (may be NULL): the
- * choices and the winner's milliseconds per step. */
-int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *concurrent, double *ms_per_step);
+ * the fastest: the shape of the FP64 LU-SGS wavefront (one CTA per block
+ * with 32, 24 or 16 rows per warp, or a thread-block cluster of 2, 4, 8 CTAs
+ * splitting the rows) and whether the i- and j-face flux kernels run
+ * concurrently on two streams.  The fine-mesh U and the step counters are
+ * restored afterwards.  Outputs (may be NULL): the choices and the winner's
+ * milliseconds per step. */
+int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *rows_per_warp, int *concurrent,
+                  double *ms_per_step);
 
 /* Wait for all queued work of the context. */
 int ec2d_sync(ec2d_ctx *ctx);

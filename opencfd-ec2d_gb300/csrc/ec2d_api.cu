@@ -13,7 +13,9 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <set>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/ec2d_gpu.h"
@@ -112,6 +114,7 @@ struct ec2d_ctx {
   int lusgs_cs = 1;  // CTAs per block in the LU-SGS wavefront (1: one CTA, >1: a cluster)
   bool lusgs_fp32 = false;  // LU-SGS sweeps in FP32 (mixed-precision mode)
   bool concurrent = true;   // i- and j-face flux kernels on two streams
+  int lusgs_rpw = 32;       // rows per warp of the FP64 wavefront (one CTA per block)
   bool timing = false;
   // one pseudo-time step (single grid or V-cycle) captured as a CUDA graph:
   // the replay stands for graph_launches kernel launches and advances the
@@ -394,6 +397,48 @@ int build_level(ec2d_ctx *ctx, int l) {
       sd.nbk = nb; sd.nface = c1[1]; sd.nist = c1[2]; sd.niend = c1[3]; sd.njst = c1[4]; sd.njend = c1[5];
     }
   }
+  // physical boundary conditions: a subface joins the earliest barrier phase
+  // after every earlier subface of the block whose cells (ghosts written,
+  // cells read) meet its own; far-field items cover all ghost layers of a
+  // boundary node, wall and symmetry items one layer
+  for (int k = 0; k < (int)lv.hb.size(); k++) {
+    BlkDev &d = lv.blk[k];
+    std::vector<std::set<long long>> rd(d.nsub), wr(d.nsub);
+    auto key = [](int i, int j) { return (long long)(i + 8) * 1000003LL + (j + 8); };
+    int nph = 0;
+    for (int s = 0; s < d.nsub; s++) {
+      SubDev &sd = lv.sub[d.sub0 + s];
+      sd.phase = -1;
+      if (sd.neighb >= 0) continue;
+      int ni = sd.iend - sd.ist + 1, nj = sd.jend - sd.jst + 1;
+      bool ff = sd.neighb == BC_Farfield || sd.neighb == BC_Inlet || sd.neighb == BC_Outlet;
+      sd.nitem = ff ? ni * nj : ni * nj * LAP;
+      for (int j = sd.jst; j <= sd.jend; j++)
+        for (int i = sd.ist; i <= sd.iend; i++)
+          for (int q = 1; q <= LAP; q++) {
+            int i1 = i, j1 = j, i2 = i, j2 = j;
+            if (sd.face == 1) { i1 = i + q - 1; i2 = i - q; }
+            else if (sd.face == 2) { j1 = j + q - 1; j2 = j - q; }
+            else if (sd.face == 3) { i1 = i - q; i2 = i + q - 1; }
+            else { j1 = j - q; j2 = j + q - 1; }
+            rd[s].insert(key(i1, j1));
+            wr[s].insert(key(i2, j2));
+          }
+      auto meet = [](const std::set<long long> &a, const std::set<long long> &b) {
+        for (long long v : a) if (b.count(v)) return true;
+        return false;
+      };
+      int ph = 0;
+      for (int e = 0; e < s; e++) {
+        const SubDev &se = lv.sub[d.sub0 + e];
+        if (se.phase < 0) continue;
+        if (meet(wr[e], rd[s]) || meet(wr[e], wr[s]) || meet(rd[e], wr[s])) ph = std::max(ph, se.phase + 1);
+      }
+      sd.phase = ph;
+      nph = std::max(nph, ph + 1);
+    }
+    d.nphase = nph;
+  }
   // wall faces for forces (fine level only)
   if (l == 1) {
     lv.case_face0.assign(ncase, 0); lv.case_nface.assign(ncase, 0);
@@ -648,7 +693,7 @@ void lusgs_update(ec2d_ctx *ctx, int l, double alfa1) {
   if (ctx->lusgs_fp32 && lv.fast32) {
     K(ctx, "k_lusgs32", l, 3, [&] { launch_lusgs_fast32(L, alfa1, 1, lv.max_rows, ctx->stream); });
   } else if (lv.fast64) {
-    K(ctx, "k_lusgs", l, 2, [&] { launch_lusgs_fast(L, alfa1, 1, lv.max_rows, ctx->lusgs_cs, ctx->stream); });
+    K(ctx, "k_lusgs", l, 2, [&] { launch_lusgs_fast(L, alfa1, 1, lv.max_rows, ctx->lusgs_cs, ctx->lusgs_rpw, ctx->stream); });
   } else {
     K(ctx, "k_lusgs_generic", l, 1, [&] { launch_lusgs(L, alfa1, ctx->stream); });
     K(ctx, "k_add_du", l, 1, [&] { launch_add_du(L, ctx->stream); });
@@ -1120,7 +1165,8 @@ static void drop_graph(ec2d_ctx *ctx) {
   }
 }
 
-int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *concurrent, double *ms_per_step) {
+int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *rows_per_warp, int *concurrent,
+                  double *ms_per_step) {
   if (!ctx || !ctx->setup_done || trial_steps < 1) return EC2D_ERR_ARG;
   cudaSetDevice(ctx->device);
   // snapshot of the state a trial changes: fine-mesh U and the step counters
@@ -1137,18 +1183,22 @@ int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *concurrent
   cudaEvent_t a, b;
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
-  // candidates: CTAs per block of the FP64 wavefront (a cluster when > 1;
-  // the FP32 sweep is one CTA per block) x concurrent face kernels
-  std::vector<int> css = {1};
+  // candidates: the FP64 wavefront's shape -- one CTA per block with 32, 24
+  // or 16 rows per warp, or a cluster of 2, 4, 8 CTAs (the FP32 sweep has
+  // one shape) -- x concurrent face kernels
+  std::vector<std::pair<int, int>> shapes = {{1, 32}};
   if (!ctx->lusgs_fp32 && ctx->P.Time_Method == Time_LU_SGS)
-    for (int c : {2, 4, 8}) css.push_back(c);
-  const int old_cs = ctx->lusgs_cs;
+    for (auto sh : {std::make_pair(1, 24), std::make_pair(1, 16), std::make_pair(2, 32), std::make_pair(4, 32),
+                    std::make_pair(8, 32)})
+      shapes.push_back(sh);
+  const int old_cs = ctx->lusgs_cs, old_rpw = ctx->lusgs_rpw;
   const bool old_cc = ctx->concurrent;
   double best = 1e30;
-  int best_cs = old_cs, best_cc = old_cc ? 1 : 0, r = EC2D_OK;
-  for (int cs : css) {
+  int best_cs = old_cs, best_rpw = old_rpw, best_cc = old_cc ? 1 : 0, r = EC2D_OK;
+  for (auto sh : shapes) {
     for (int cc = 0; cc < 2 && r == EC2D_OK; cc++) {
-      ctx->lusgs_cs = cs;
+      ctx->lusgs_cs = sh.first;
+      ctx->lusgs_rpw = sh.second;
       ctx->concurrent = cc != 0;
       drop_graph(ctx);
       if ((r = ec2d_step(ctx, 1)) != EC2D_OK) break;
@@ -1158,10 +1208,16 @@ int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *concurrent
       cudaEventSynchronize(b);
       float ms = 0.0f;
       cudaEventElapsedTime(&ms, a, b);
-      if (ms / trial_steps < best) { best = ms / trial_steps; best_cs = cs; best_cc = cc; }
+      if (ms / trial_steps < best) {
+        best = ms / trial_steps;
+        best_cs = sh.first;
+        best_rpw = sh.second;
+        best_cc = cc;
+      }
     }
   }
   ctx->lusgs_cs = r == EC2D_OK ? best_cs : old_cs;
+  ctx->lusgs_rpw = r == EC2D_OK ? best_rpw : old_rpw;
   ctx->concurrent = r == EC2D_OK ? best_cc != 0 : old_cc;
   drop_graph(ctx);
   cudaMemcpyAsync(lv.L.U, snap, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
@@ -1173,6 +1229,7 @@ int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *concurrent
     for (int l = 0; l < 4; l++) { ctx->cases[c].kstep[l] = ks[c][l]; ctx->cases[c].tt[l] = ts[c][l]; }
   if (r) return r;
   if (lusgs_cs) *lusgs_cs = ctx->lusgs_cs;
+  if (rows_per_warp) *rows_per_warp = ctx->lusgs_rpw;
   if (concurrent) *concurrent = ctx->concurrent ? 1 : 0;
   if (ms_per_step) *ms_per_step = best;
   return check_launch(ctx);
@@ -1400,7 +1457,7 @@ int ec2d_du_lusgs(ec2d_ctx *ctx, int mesh, double alfa1) {
   const Level &lv = ctx->lv[mesh];
   const Lvl &L = lv.L;
   if (ctx->lusgs_fp32 && lv.fast32) launch_lusgs_fast32(L, alfa1, 0, lv.max_rows, ctx->stream);
-  else if (lv.fast64) launch_lusgs_fast(L, alfa1, 0, lv.max_rows, ctx->lusgs_cs, ctx->stream);
+  else if (lv.fast64) launch_lusgs_fast(L, alfa1, 0, lv.max_rows, ctx->lusgs_cs, ctx->lusgs_rpw, ctx->stream);
   else launch_lusgs(L, alfa1, ctx->stream);
   return check_launch(ctx);
 }

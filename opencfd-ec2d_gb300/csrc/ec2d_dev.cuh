@@ -44,10 +44,12 @@ struct BlkDev {
   int tile0;                // first extended-range tile of this block
   int lsub0, lsubn;         // fine-mesh wall faces (forces), unused on coarse levels
   int cell0;                // dense index of cell (1,1) among the level's interior cells
+  int nphase;               // barrier phases of the physical boundary conditions
 };
 
 struct SubDev {
   int face, ist, iend, jst, jend, neighb, orient;
+  int phase, nitem;         // physical BC: barrier phase within the block, work items
   int nbk;                  // level-global index of the neighbour block (-1: physical)
   int nface, nist, niend, njst, njend;  // the neighbour subface it reads
 };

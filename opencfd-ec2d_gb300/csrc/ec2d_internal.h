@@ -27,7 +27,7 @@ void launch_bc(const Lvl &L, int phases, cudaStream_t s);
 void launch_lusgs(const Lvl &L, double alfa1, cudaStream_t s);
 // k_sweep.cu
 int lusgs_planes(int nv);
-void launch_lusgs_fast(const Lvl &L, double alfa1, int update, int max_rows, int cs, cudaStream_t s);
+void launch_lusgs_fast(const Lvl &L, double alfa1, int update, int max_rows, int cs, int rpw, cudaStream_t s);
 size_t lusgs_smem(int nv, int rows);  // dynamic shared memory of the one-CTA FP64 sweep
 void launch_lusgs_fast32(const Lvl &L, double alfa1, int update, int max_rows, cudaStream_t s);
 size_t lusgs32_smem(int nv, int rows);

@@ -11,7 +11,9 @@
 // only interior cells, and corners read only the block's own ghosts.  Hence
 // one CTA per block reproduces the reference exactly: subfaces of phase 1 in
 // order with a barrier between them, all halo items of phase 2 in parallel,
-// then the corners.
+// then the corners.  Physical subfaces whose read and write sets do not meet
+// those of any earlier subface of the block share a barrier phase (the
+// grouping is computed at set-up from the index rectangles).
 #include "ec2d_dev.cuh"
 #include "ec2d_internal.h"
 
@@ -94,7 +96,7 @@ __device__ void bc_symmetry(const Lvl &L, const BlkDev &b, const SubDev &s, int 
 // outflow switch is a sign test on a computed normal Mach number, so this
 // routine is evaluated with separately rounded operations (no contraction)
 // to take the same branch as the reference on every cell.
-__device__ void bc_farfield(const Lvl &L, const BlkDev &b, const CaseDev &c, const SubDev &s, int i, int j, int k) {
+__device__ void bc_farfield(const Lvl &L, const BlkDev &b, const CaseDev &c, const SubDev &s, int i, int j) {
   const long long F = L.F;
   double *U = L.U;
   const double *x = L.geo + G_X * F, *y = L.geo + G_Y * F;
@@ -121,6 +123,9 @@ __device__ void bc_farfield(const Lvl &L, const BlkDev &b, const CaseDev &c, con
   if (s.face == 1 || s.face == 4) { n1 = __ddiv_rn(-dy, sl); n2 = __ddiv_rn(dx, sl); }
   else { n1 = __ddiv_rn(dy, sl); n2 = __ddiv_rn(-dx, sl); }
   double Ma_n = __ddiv_rn(__dadd_rn(__dmul_rn(u1, n1), __dmul_rn(v1, n2)), c1);
+  // every ghost layer k takes the same interior state and normal, so one item
+  // writes all LAP layers (the reference recomputes them per k: same values)
+  for (int k = 1; k <= LAP; k++) {
   int i2, j2;
   if (s.face == 1) { i2 = i - k; j2 = j; }
   else if (s.face == 2) { i2 = i; j2 = j - k; }
@@ -158,6 +163,7 @@ __device__ void bc_farfield(const Lvl &L, const BlkDev &b, const CaseDev &c, con
     if (L.nvar == 5) U[4 * F + g] = c.vt_inf / c.Re;
     else if (L.nvar == 6) { U[4 * F + g] = d_inf * c.Kt_inf; U[5 * F + g] = d_inf * c.Wt_inf; }
   }
+  }
 }
 
 // U_average_conner, sub_boundary.f90:595-612
@@ -186,17 +192,30 @@ __global__ void __launch_bounds__(256) k_bc(Lvl L, int phases) {
   const CaseDev &c = L.cs[b.cas];
   const long long F = L.F;
   if (phases & 1) {
-    for (int ks = 0; ks < b.nsub; ks++) {
-      const SubDev s = L.sub[b.sub0 + ks];
-      if (s.neighb < 0) {
-        int ni = s.iend - s.ist + 1, nj = s.jend - s.jst + 1;
-        int nitem = ni * nj * LAP;
-        for (int t = threadIdx.x; t < nitem; t += blockDim.x) {
-          int k = t % LAP + 1, r = t / LAP;
+    // subfaces of one phase touch disjoint cells (grouped at set-up in
+    // subface order): their items are spread over the CTA together
+    for (int ph = 0; ph < b.nphase; ph++) {
+      int total = 0;
+      for (int ks = 0; ks < b.nsub; ks++) {
+        const SubDev &s = L.sub[b.sub0 + ks];
+        if (s.neighb < 0 && s.phase == ph) total += s.nitem;
+      }
+      for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        int u = t, ks = 0;
+        for (; ks < b.nsub; ks++) {
+          const SubDev &s = L.sub[b.sub0 + ks];
+          if (s.neighb >= 0 || s.phase != ph) continue;
+          if (u < s.nitem) break;
+          u -= s.nitem;
+        }
+        const SubDev s = L.sub[b.sub0 + ks];
+        int ni = s.iend - s.ist + 1;
+        if (s.neighb == BC_Farfield || s.neighb == BC_Inlet || s.neighb == BC_Outlet) {
+          bc_farfield(L, b, c, s, s.ist + u % ni, s.jst + u / ni);
+        } else {
+          int k = u % LAP + 1, r = u / LAP;
           int i = s.ist + r % ni, j = s.jst + r / ni;
           if (s.neighb == BC_Wall) bc_wall(L, b, c, s, i, j, k);
-          else if (s.neighb == BC_Farfield || s.neighb == BC_Inlet || s.neighb == BC_Outlet)
-            bc_farfield(L, b, c, s, i, j, k);
           else if (s.neighb == BC_Symmetry) bc_symmetry(L, b, s, i, j, k);
         }
       }

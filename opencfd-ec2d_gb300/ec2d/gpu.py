@@ -117,7 +117,7 @@ def lib():
         "ec2d_run_to_drop": ([vp, ctypes.c_double, dp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ip, dp, dp],
                              ctypes.c_int),
         "ec2d_set_case_shape": ([vp, ctypes.c_int, ctypes.c_double], ctypes.c_int),
-        "ec2d_autotune": ([vp, ctypes.c_int, ip, ip, dp], ctypes.c_int),
+        "ec2d_autotune": ([vp, ctypes.c_int, ip, ip, ip, dp], ctypes.c_int),
         "ec2d_mlp_create": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, cpp], ctypes.c_int),
         "ec2d_mlp_destroy": ([vp], None),
         "ec2d_mlp_add_samples": ([vp, vp], ctypes.c_int),
@@ -318,12 +318,12 @@ class Solver:
         return n.value, w.value, t.value
 
     def autotune(self, trial_steps=5):
-        """Pick the fastest launch configuration; returns (cluster CTAs,
-        concurrent flux kernels, ms per step)."""
-        cs, cc, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
-        _ck(self.L.ec2d_autotune(self.h, int(trial_steps), ctypes.byref(cs), ctypes.byref(cc), ctypes.byref(ms)),
-            "ec2d_autotune")
-        return cs.value, cc.value, ms.value
+        """Pick the fastest launch configuration; returns (cluster CTAs, rows
+        per warp, concurrent flux kernels, ms per step)."""
+        cs, rpw, cc, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        _ck(self.L.ec2d_autotune(self.h, int(trial_steps), ctypes.byref(cs), ctypes.byref(rpw), ctypes.byref(cc),
+                                 ctypes.byref(ms)), "ec2d_autotune")
+        return cs.value, rpw.value, cc.value, ms.value
 
     def set_case_shape(self, case, shape):
         """Per-case shape feature of the warm-start network (the airfoil t/c)."""

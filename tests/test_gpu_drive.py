@@ -1,6 +1,8 @@
 """ec2d_run_to_drop (iterate to a residual drop, with timers): the steps it
 takes are ordinary ec2d_step calls, so a second solver stepped by hand the
 same number of times must hold the identical state and norms."""
+import os
+
 import numpy as np
 import pytest
 
@@ -35,3 +37,19 @@ def test_run_to_drop_limits(gpu_lib):
     # a given reference residual: one check, no step needed when already below
     n2, ratio2, _ = g.run_to_drop(drop=1.0, r0=[1e30], max_steps=5, check_every=5)
     assert n2 == 5 or ratio2 <= 1.0
+
+
+def test_output_files_from_the_device(gpu_lib, tmp_path):
+    from ec2d import outputs
+    p, bl = small_case(Ma=0.5, AoA=2.0, Re=1e6, If_viscous=1, Iflag_turbulence_model=2, Iflag_flux=4,
+                       Iflag_Scheme=5, CFL=5.0, first=2e-4, nblocks=2)
+    g = make_gpu(p, bl)
+    g.init_flow()
+    g.step(20)
+    paths = outputs.write_output(str(tmp_path), g, p, kstep=20)
+    assert [os.path.basename(x) for x in paths] == ["flow2d-0000020.dat", "flow2d.dat", "SA2d.dat"]
+    names, zones = outputs.parse_tecplot(open(paths[1]).read())
+    assert len(zones) == 2 and names[-1] == "Amut"
+    U = g.download_U(1, 1, 2)
+    nx, ny, _ = g.dims(1, 1, 2)
+    np.testing.assert_allclose(zones[1][:, 2].reshape(ny + 1, nx + 1), U[0, 1:nx + 2, 1:ny + 2].T, atol=1e-10)

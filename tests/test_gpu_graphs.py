@@ -44,8 +44,8 @@ def test_autotune_keeps_state_and_results(gpu_lib):
     a.step(2)
     u0 = [a.download_U(1, 1, b) for b in (1, 2)]
     k0 = a.norms(1)[2]
-    cs, cc, ms = a.autotune(trial_steps=3)
-    assert cs in (1, 2, 4, 8) and cc in (0, 1) and ms > 0.0
+    cs, rpw, cc, ms = a.autotune(trial_steps=3)
+    assert cs in (1, 2, 4, 8) and rpw in (16, 24, 32) and cc in (0, 1) and ms > 0.0
     for b in (1, 2):
         np.testing.assert_array_equal(a.download_U(1, 1, b), u0[b - 1])
     assert a.norms(1)[2] == k0

@@ -1,0 +1,48 @@
+"""Tecplot writers of `output` (opencfd_ec2d_v1.5.4.f90:284-371): layout,
+variables and values, checked by parsing the text back."""
+import numpy as np
+
+from ec2d import outputs
+
+
+def _block(nx, ny, nv, seed):
+    rng = np.random.default_rng(seed)
+    U = np.zeros((nv, nx + 3, ny + 3))
+    d = 1.0 + 0.1 * rng.random((nx + 3, ny + 3))
+    u, v = 0.5 + 0.1 * rng.random(d.shape), 0.1 * rng.random(d.shape)
+    p = 1.0 / (1.4 * 0.5 ** 2) * (1.0 + 0.05 * rng.random(d.shape))
+    U[0], U[1], U[2] = d, d * u, d * v
+    U[3] = p / 0.4 + 0.5 * d * (u * u + v * v)
+    for m in range(4, nv):
+        U[m] = rng.random(d.shape)
+    x1 = np.add.outer(np.arange(-1, nx + 2), np.zeros(ny + 3)) * 0.1
+    y1 = np.add.outer(np.zeros(nx + 3), np.arange(-1, ny + 2)) * 0.2
+    return {"nx": nx, "ny": ny, "U": U, "x1": x1, "y1": y1, "amut": 1e-6 * rng.random(d.shape)}, (d, u, v, p)
+
+
+def test_flow2d_layout_and_values():
+    b1, (d, u, v, p) = _block(5, 4, 4, 0)
+    b2, _ = _block(3, 6, 4, 1)
+    txt = outputs.format_blocks([b1, b2], gamma=1.4, Ma=0.5, Re=1e6)
+    names, zones = outputs.parse_tecplot(txt)
+    assert names == ["x", "y", "d", "u", "v", "T", "p", "Amut"]
+    assert [z.shape for z in zones] == [(6 * 5, 8), (4 * 7, 8)]
+    z = zones[0]
+    # row r = j*(nx+1) + i for i, j = 0..nx, 0..ny: array index (i+1, j+1)
+    for (i, j) in [(0, 0), (5, 0), (2, 3), (5, 4)]:
+        r = j * 6 + i
+        np.testing.assert_allclose(z[r, 0], b1["x1"][i + 1, j + 1], atol=1e-10)
+        np.testing.assert_allclose(z[r, 2], d[i + 1, j + 1], atol=1e-10)
+        np.testing.assert_allclose(z[r, 3], u[i + 1, j + 1], atol=1e-10)
+        np.testing.assert_allclose(z[r, 6], p[i + 1, j + 1], atol=1e-9)
+        np.testing.assert_allclose(z[r, 7], b1["amut"][i + 1, j + 1] * 1e6, atol=1e-10)
+
+
+def test_turbulence_files():
+    b, _ = _block(4, 3, 5, 2)
+    names, zones = outputs.parse_tecplot(outputs.format_turbulence([b]))
+    assert names == ["x", "y", "vt"] and zones[0].shape == (5 * 4, 3)
+    np.testing.assert_allclose(zones[0][7, 2], b["U"][4][7 % 5 + 1, 7 // 5 + 1], atol=1e-10)
+    b6, _ = _block(4, 3, 6, 3)
+    names, zones = outputs.parse_tecplot(outputs.format_turbulence([b6]))
+    assert names == ["x", "y", "Kt", "Wt"] and zones[0].shape == (20, 4)
