@@ -1609,11 +1609,38 @@ int ec2d_mlp_train(ec2d_mlp *m, int steps, int batch, double lr, double *loss_ou
   Net &net = m->net;
   cudaSetDevice(net.device);
   if (net.ensure_batch(batch)) return EC2D_ERR_NOMEM;
-  for (int k = 0; k < steps; k++) {
+  // one training step as a CUDA graph (its minibatch seed and Adam step count
+  // live in device memory), re-recorded when batch, rate or GEMM path change
+  if (!net.train_graph || net.graph_batch != batch || net.graph_lr != (float)lr || net.graph_kind != net.gemm_kind) {
+    if (net.train_graph) cudaGraphExecDestroy(net.train_graph);
+    net.train_graph = nullptr;
+    CK(cudaStreamSynchronize(net.stream));
+    CK(cudaStreamBeginCapture(net.stream, cudaStreamCaptureModeThreadLocal));
     net.gather(batch);
     net.forward(batch);
     net.backward(batch);
     net.adam((float)lr);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(net.stream, &g);
+    if (e == cudaSuccess && g) e = cudaGraphInstantiate(&net.train_graph, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      net.train_graph = nullptr;
+    }
+    net.graph_batch = batch;
+    net.graph_lr = (float)lr;
+    net.graph_kind = net.gemm_kind;
+  }
+  for (int k = 0; k < steps; k++) {
+    if (net.train_graph) {
+      CK(cudaGraphLaunch(net.train_graph, net.stream));
+    } else {
+      net.gather(batch);
+      net.forward(batch);
+      net.backward(batch);
+      net.adam((float)lr);
+    }
   }
   float l = 0.0f;
   CK(cudaMemcpyAsync(&l, net.d_loss, sizeof(float), cudaMemcpyDeviceToHost, net.stream));

@@ -60,7 +60,9 @@ struct Net {
   // samples (device): features n x NIN, targets n x NOUT
   float *feat = nullptr, *targ = nullptr;
   long long nsamp = 0, cap_samp = 0;
-  cudaGraphExec_t train_graph = nullptr;
+  cudaGraphExec_t train_graph = nullptr;  // one training step (gather, forward, backward, Adam)
+  int graph_batch = 0, graph_kind = -1;
+  float graph_lr = 0.0f;
   std::vector<void *> owned;
 
   int init(int dev, int hidden, int width, unsigned long long seed);

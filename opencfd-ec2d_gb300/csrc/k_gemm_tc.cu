@@ -13,7 +13,8 @@
 //    commits them to the chunk buffer's mbarrier; two buffers let the next
 //    chunk load while the tensor cores work;
 //  * after the last commit each warp reads its 32 accumulator rows with
-//    tcgen05.ld (32 columns at a time) and applies the epilogue.
+//    tcgen05.ld (32 columns at a time), stages them in shared memory and
+//    applies the epilogue row by row with coalesced global accesses.
 // Every mbarrier wait is bounded: on timeout the kernel sets *err, issues no
 // further MMA, waits (bounded) for the ones in flight and still frees its
 // TMEM.  The timeout decision is made CTA-wide (__syncthreads_and), so all
@@ -178,7 +179,11 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const __nv_bfloat16 *__restrict
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
   if (ok) {
-    const int row = m0 + warp * 32 + lane;
+    // epilogue through shared memory (the operand buffers are free now): each
+    // warp stages its 32 accumulator rows x 32 columns, then walks the rows
+    // with lane = column, so every global load and store of a warp covers
+    // consecutive columns of one row
+    float *stage = reinterpret_cast<float *>(smem) + warp * (32 * 33);
 #pragma unroll 1
     for (int c0 = 0; c0 < BN; c0 += 32) {
       uint32_t v[32];
@@ -193,28 +198,28 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const __nv_bfloat16 *__restrict
           : "r"(ta));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-      for (int j = 0; j < 32; j += 2) {
-        const int col = n0 + c0 + j;
-        float v0 = __uint_as_float(v[j]), v1 = __uint_as_float(v[j + 1]);
+      for (int j = 0; j < 32; j++) stage[lane * 33 + j] = __uint_as_float(v[j]);
+      __syncwarp();
+      const int col = n0 + c0 + lane;
+#pragma unroll 4
+      for (int r = 0; r < 32; r++) {
+        const size_t row = (size_t)(m0 + warp * 32 + r);
+        const float a = stage[r * 33 + lane];
         if (e.mode == EPI_F32) {
-          *reinterpret_cast<float2 *>(e.fout + blockIdx.z * e.split_stride + (size_t)row * e.ldc + col) =
-              make_float2(v0, v1);
+          e.fout[blockIdx.z * e.split_stride + row * e.ldc + col] = a;
         } else if (e.mode == EPI_BIAS) {
-          *reinterpret_cast<float2 *>(e.fout + (size_t)row * e.ldc + col) =
-              make_float2(v0 + e.bias[col], v1 + e.bias[col + 1]);
+          e.fout[row * e.ldc + col] = a + e.bias[col];
         } else if (e.mode == EPI_BIAS_SILU) {
-          float z0 = v0 + e.bias[col], z1 = v1 + e.bias[col + 1];
-          *reinterpret_cast<float2 *>(e.zout + (size_t)row * e.ldz + col) = make_float2(z0, z1);
-          *reinterpret_cast<__nv_bfloat162 *>(e.hout + (size_t)row * e.ldc + col) =
-              __floats2bfloat162_rn(silu(z0), silu(z1));
+          const float z = a + e.bias[col];
+          e.zout[row * e.ldz + col] = z;
+          e.hout[row * e.ldc + col] = __float2bfloat16_rn(silu(z));
         } else if (e.mode == EPI_DSILU) {
-          float2 z = *reinterpret_cast<const float2 *>(e.zin + (size_t)row * e.ldz + col);
-          *reinterpret_cast<__nv_bfloat162 *>(e.hout + (size_t)row * e.ldc + col) =
-              __floats2bfloat162_rn(v0 * dsilu(z.x), v1 * dsilu(z.y));
+          e.hout[row * e.ldc + col] = __float2bfloat16_rn(a * dsilu(e.zin[row * e.ldz + col]));
         } else {
-          *reinterpret_cast<__nv_bfloat162 *>(e.hout + (size_t)row * e.ldc + col) = __floats2bfloat162_rn(v0, v1);
+          e.hout[row * e.ldc + col] = __float2bfloat16_rn(a);
         }
       }
+      __syncwarp();
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
