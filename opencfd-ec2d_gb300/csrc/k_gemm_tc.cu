@@ -2,7 +2,7 @@
 // C[M x N] = A[M x K] . B[N x K]^T, both operands K-major, FP32 accumulators
 // in tensor memory, the epilogues of the warm-start network (k_mlp.cu).
 //
-// One CTA of 128 threads computes a 128 x BN tile (BN = 128 or 64):
+// One CTA of 256 threads computes a 128 x BN tile (BN = 128 or 64):
 //  * warp 0 allocates BN TMEM columns (128 lanes x BN x 32 bit: the tile);
 //  * all threads stage 64-wide K chunks of A and B into shared memory with
 //    16-byte cp.async, in the canonical no-swizzle K-major layout of the MMA
@@ -10,11 +10,12 @@
 //    a row group adjacent (leading byte offset 128 B), row groups 1024 B apart
 //    (stride byte offset);
 //  * thread 0 issues four tcgen05.mma (M=128, N=BN, K=16 each) per chunk and
-//    commits them to the chunk buffer's mbarrier; two buffers let the next
-//    chunk load while the tensor cores work;
-//  * after the last commit each warp reads its 32 accumulator rows with
-//    tcgen05.ld (32 columns at a time), stages them in shared memory and
-//    applies the epilogue row by row with coalesced global accesses.
+//    commits them to the chunk buffer's mbarrier; a three-buffer ring keeps
+//    two chunks loading while the tensor cores work on the third;
+//  * after the last commit each warp reads 32 accumulator rows of one column
+//    half with tcgen05.ld (32 columns at a time), stages them in shared
+//    memory and applies the epilogue row by row with coalesced global
+//    accesses (eight warps keep the epilogue's memory latency covered).
 // Every mbarrier wait is bounded: on timeout the kernel sets *err, issues no
 // further MMA, waits (bounded) for the ones in flight and still frees its
 // TMEM.  The timeout decision is made CTA-wide (__syncthreads_and), so all
@@ -29,7 +30,7 @@
 namespace ec2d {
 namespace tc {
 
-constexpr int BM = 128, BK = 64;
+constexpr int BM = 128, BK = 64, NS = 3;  // tile rows, K chunk, pipeline stages
 constexpr long long WAIT_LIMIT = 1ll << 24;  // try_wait polls before giving up
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -82,12 +83,12 @@ __device__ __forceinline__ float dsilu(float z) {
 }
 
 template <int BN>
-__global__ void __launch_bounds__(128) k_gemm_tc(const __nv_bfloat16 *__restrict__ A, int lda,
+__global__ void __launch_bounds__(256) k_gemm_tc(const __nv_bfloat16 *__restrict__ A, int lda,
                                                  const __nv_bfloat16 *__restrict__ B, int ldb, int K, int ksplit,
                                                  Epi e, int *err) {
   constexpr int ABYTES = BM * BK * 2, BBYTES = BN * BK * 2, STAGE = ABYTES + BBYTES;
   extern __shared__ __align__(1024) uint8_t smem[];
-  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ __align__(8) uint64_t mbar[NS];
   __shared__ uint32_t tmem_sh;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
@@ -101,8 +102,7 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const __nv_bfloat16 *__restrict
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    mbar_init(smem_u32(&mbar[0]), 1);
-    mbar_init(smem_u32(&mbar[1]), 1);
+    for (int q = 0; q < NS; q++) mbar_init(smem_u32(&mbar[q]), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -117,14 +117,14 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const __nv_bfloat16 *__restrict
     const int k0 = kb + kt * BK;
     const uint32_t sa = s0 + buf * STAGE, sb = sa + ABYTES;
 #pragma unroll
-    for (int q = 0; q < BM * 8 / 128; q++) {
-      int c = tid + q * 128;
+    for (int q = 0; q < BM * 8 / 256; q++) {
+      int c = tid + q * 256;
       int r = (c & 7) + ((c >> 6) << 3), p = (c >> 3) & 7;
       cp16(sa + (uint32_t)(((r >> 3) * 8 + p) * 128 + (r & 7) * 16), A + (size_t)(m0 + r) * lda + k0 + p * 8);
     }
 #pragma unroll
-    for (int q = 0; q < BN * 8 / 128; q++) {
-      int c = tid + q * 128;
+    for (int q = 0; q < BN * 8 / 256; q++) {
+      int c = tid + q * 256;
       int r = (c & 7) + ((c >> 6) << 3), p = (c >> 3) & 7;
       cp16(sb + (uint32_t)(((r >> 3) * 8 + p) * 128 + (r & 7) * 16), B + (size_t)(n0 + r) * ldb + k0 + p * 8);
     }
@@ -134,17 +134,24 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const __nv_bfloat16 *__restrict
   bool ok = true;
   int last = -1;  // last chunk whose MMAs were committed
   constexpr uint32_t IDESC = idesc_bf16(BM, BN);
-  load(0, 0);
+  // NS-stage ring: chunk c lives in buffer c % NS; one cp.async group is
+  // committed per chunk slot (empty past the end) so that wait_group<NS-1>
+  // always means "chunk kt has landed"
+#pragma unroll
+  for (int c = 0; c < NS - 1; c++) {
+    if (c < nk) load(c, c);
+    else cp_commit();
+  }
   for (int kt = 0; kt < nk; kt++) {
-    const int buf = kt & 1;
-    if (kt + 1 < nk) {
-      // the other buffer is free once the MMAs of chunk kt-1 completed
-      if (kt >= 1 && ok) ok = mbar_wait(smem_u32(&mbar[buf ^ 1]), ((kt - 1) >> 1) & 1);
-      load(buf ^ 1, kt + 1);
-      cp_wait<1>();
+    const int buf = kt % NS, c = kt + NS - 1;
+    if (c < nk) {
+      // buffer c % NS last held chunk kt-1: free once its MMAs completed
+      if (kt >= 1 && ok) ok = mbar_wait(smem_u32(&mbar[(kt - 1) % NS]), ((kt - 1) / NS) & 1);
+      load(c % NS, c);
     } else {
-      cp_wait<0>();
+      cp_commit();
     }
+    cp_wait<NS - 1>();
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     ok = __syncthreads_and(ok) != 0;
     if (!ok) break;
@@ -171,7 +178,7 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const __nv_bfloat16 *__restrict
   // the accumulators are complete (after a timeout: no MMA is in flight any
   // more) once the last committed chunk's barrier completes
   if (last >= 0) {
-    bool f = mbar_wait(smem_u32(&mbar[last & 1]), (last >> 1) & 1);
+    bool f = mbar_wait(smem_u32(&mbar[last % NS]), (last / NS) & 1);
     ok = ok && f;
   }
   ok = __syncthreads_and(ok) != 0;
@@ -183,11 +190,14 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const __nv_bfloat16 *__restrict
     // warp stages its 32 accumulator rows x 32 columns, then walks the rows
     // with lane = column, so every global load and store of a warp covers
     // consecutive columns of one row
+    // warp w reads TMEM lanes 32 (w % 4) .. +31 (the rows it may access) and
+    // the column half w / 4
     float *stage = reinterpret_cast<float *>(smem) + warp * (32 * 33);
+    const int wl = warp & 3, half = warp >> 2;
 #pragma unroll 1
-    for (int c0 = 0; c0 < BN; c0 += 32) {
+    for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 32) {
       uint32_t v[32];
-      const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      const uint32_t ta = tmem + ((uint32_t)(wl * 32) << 16) + (uint32_t)c0;
       asm volatile(
           "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
           "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
@@ -201,23 +211,40 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const __nv_bfloat16 *__restrict
       for (int j = 0; j < 32; j++) stage[lane * 33 + j] = __uint_as_float(v[j]);
       __syncwarp();
       const int col = n0 + c0 + lane;
-#pragma unroll 4
-      for (int r = 0; r < 32; r++) {
-        const size_t row = (size_t)(m0 + warp * 32 + r);
-        const float a = stage[r * 33 + lane];
-        if (e.mode == EPI_F32) {
-          e.fout[blockIdx.z * e.split_stride + row * e.ldc + col] = a;
-        } else if (e.mode == EPI_BIAS) {
-          e.fout[row * e.ldc + col] = a + e.bias[col];
-        } else if (e.mode == EPI_BIAS_SILU) {
-          const float z = a + e.bias[col];
-          e.zout[row * e.ldz + col] = z;
-          e.hout[row * e.ldc + col] = __float2bfloat16_rn(silu(z));
-        } else if (e.mode == EPI_DSILU) {
-          e.hout[row * e.ldc + col] = __float2bfloat16_rn(a * dsilu(e.zin[row * e.ldz + col]));
-        } else {
-          e.hout[row * e.ldc + col] = __float2bfloat16_rn(a);
+      const size_t row0 = (size_t)(m0 + wl * 32);
+      // the mode is uniform: one fully unrolled row loop per mode, so the 32
+      // rows' loads and stores of a lane are all in flight together
+      if (e.mode == EPI_F32) {
+        float *o = e.fout + blockIdx.z * e.split_stride + row0 * e.ldc + col;
+#pragma unroll
+        for (int r = 0; r < 32; r++) o[(size_t)r * e.ldc] = stage[r * 33 + lane];
+      } else if (e.mode == EPI_BIAS) {
+        const float bc = e.bias[col];
+        float *o = e.fout + row0 * e.ldc + col;
+#pragma unroll
+        for (int r = 0; r < 32; r++) o[(size_t)r * e.ldc] = stage[r * 33 + lane] + bc;
+      } else if (e.mode == EPI_BIAS_SILU) {
+        const float bc = e.bias[col];
+        float *zo = e.zout + row0 * e.ldz + col;
+        __nv_bfloat16 *ho = e.hout + row0 * e.ldc + col;
+#pragma unroll
+        for (int r = 0; r < 32; r++) {
+          const float z = stage[r * 33 + lane] + bc;
+          zo[(size_t)r * e.ldz] = z;
+          ho[(size_t)r * e.ldc] = __float2bfloat16_rn(silu(z));
         }
+      } else if (e.mode == EPI_DSILU) {
+        const float *zi = e.zin + row0 * e.ldz + col;
+        float z[32];
+#pragma unroll
+        for (int r = 0; r < 32; r++) z[r] = zi[(size_t)r * e.ldz];
+        __nv_bfloat16 *ho = e.hout + row0 * e.ldc + col;
+#pragma unroll
+        for (int r = 0; r < 32; r++) ho[(size_t)r * e.ldc] = __float2bfloat16_rn(stage[r * 33 + lane] * dsilu(z[r]));
+      } else {
+        __nv_bfloat16 *ho = e.hout + row0 * e.ldc + col;
+#pragma unroll
+        for (int r = 0; r < 32; r++) ho[(size_t)r * e.ldc] = __float2bfloat16_rn(stage[r * 33 + lane]);
       }
       __syncwarp();
     }
@@ -229,11 +256,11 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const __nv_bfloat16 *__restrict
 
 }  // namespace tc
 
-// shared memory: two stages of A (16 KB) and B (BN x 128 B), plus a spare
-// stage so that no descriptor walk can leave the CTA's allocation
+// shared memory: NS stages of A (16 KB) and B (BN x 128 B), 1 KB alignment
+// slack; the epilogue reuses the first 17 KB
 template <int BN>
 static size_t tc_smem() {
-  return (size_t)3 * (tc::BM * tc::BK * 2 + BN * tc::BK * 2) + 1024;
+  return (size_t)tc::NS * (tc::BM * tc::BK * 2 + BN * tc::BK * 2) + 1024;
 }
 
 void launch_gemm_tc(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, int M, int N, int K,
@@ -241,11 +268,11 @@ void launch_gemm_tc(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int
   if (N % 128 == 0) {
     size_t sm = tc_smem<128>();
     cudaFuncSetAttribute(tc::k_gemm_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    tc::k_gemm_tc<128><<<dim3(M / tc::BM, N / 128, ksplit), 128, sm, s>>>(A, lda, B, ldb, K, ksplit, e, err);
+    tc::k_gemm_tc<128><<<dim3(M / tc::BM, N / 128, ksplit), 256, sm, s>>>(A, lda, B, ldb, K, ksplit, e, err);
   } else {
     size_t sm = tc_smem<64>();
     cudaFuncSetAttribute(tc::k_gemm_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    tc::k_gemm_tc<64><<<dim3(M / tc::BM, N / 64, ksplit), 128, sm, s>>>(A, lda, B, ldb, K, ksplit, e, err);
+    tc::k_gemm_tc<64><<<dim3(M / tc::BM, N / 64, ksplit), 256, sm, s>>>(A, lda, B, ldb, K, ksplit, e, err);
   }
 }
 
