@@ -6,17 +6,19 @@
 // and every cell reads only neighbours on plane p-1 (p+1).  The work is split
 // so that only the dependency chain sits between two planes:
 //   k_lusgs_prep  (all cells in parallel) evaluates everything that does not
-//                 depend on the sweep -- 1/alfa, the normal fluxes F_n(U_nb)
-//                 of the upstream neighbours with this cell's face normals,
-//                 the coefficient products 0.5 s and 0.5 Lc + Lv -- and packs
-//                 them with U and Res into one 16-byte-aligned record per cell
-//                 and pass;
+//                 depend on the sweep -- 1/alfa, 0.5 Lc + Lv, the face normals
+//                 scaled by the reference's +-0.5 s, and the constant half of
+//                 the flux difference, -F_n(U_nb, s) of both upstream
+//                 neighbours, folded into Res -- and packs them with U into
+//                 one 16-byte-aligned record per cell and pass;
 //   k_lusgs_sweep (one CTA or one thread-block cluster per block; thread j
 //                 owns row j) fetches the NEXT cell's record into shared memory
 //                 with cp.async while it computes the current cell, takes the
 //                 own row's previous cell from registers and the neighbouring
-//                 row from a double-buffered shared slot, and forms
-//                 F_n(U_nb + dU_nb) - F_n(U_nb), the sum and the 1/alfa scaling.
+//                 row from a double-buffered shared slot, and adds
+//                 F_n(U_nb + dU_nb, s) and (0.5 Lc + Lv) dU_nb to the record's
+//                 constant term before the 1/alfa scaling (the same sum as
+//                 the reference, F_n being linear in the normal).
 // The producer of a state also ships 1/rho and p of U + dU, so each of its two
 // consumers needs no division.  The backward sweep writes U + dU (the update
 // of NS_Time_advance_LU_SGS, sub_NS_singlegrid.f90:203-211): a neighbour needs
@@ -32,19 +34,20 @@ namespace ec2d {
 constexpr int TILE = 256;
 
 // record layout (doubles), identical for both passes:
-//  A    Res (forward) or the forward dU (backward)
+//  A    forward: Res - F_n(U_i-nb, s_i) - F_n(U_j-nb, s_j); backward: the
+//       forward dU (written by the forward sweep)
 //  U    U_old of the cell
-//  FI   F_n(U_nb) of the i-neighbour (west forward, east backward), normal of face i
-//  FJ   the same for the j-neighbour (south / north), normal of face j
+//  C0   backward only: -F_n(U_i-nb, s_i) - F_n(U_j-nb, s_j)
 //  CI, CJ  0.5 Lc_nb (+ Lv_nb when viscous)
-//  HI, HJ  0.5 s of the face the reference multiplies the flux difference by
 //  IA, IA5 1/alfa and, for the SA row, 1/(alfa + Lvi + Lvj)
-//  N1I..N2J  face normals of face i and face j of the cell
+//  N1I..N2J  scaled normals s = +-0.5 (face length) n of face i and face j:
+//       the reference multiplies the flux difference by +-0.5 s, and the
+//       normal flux is linear in n, so F_n(W, s) = 0.5 s F_n(W, n) and the
+//       constant half F_n(U_nb) of the difference moves into the record
 template <int NV>
 struct Rec {
-  static constexpr int A = 0, U = NV, FI = 2 * NV, FJ = 3 * NV, CI = 4 * NV, CJ = CI + 1, HI = CI + 2,
-                       HJ = CI + 3, IA = CI + 4, IA5 = CI + 5, N1I = CI + 6, N2I = CI + 7, N1J = CI + 8,
-                       N2J = CI + 9, N = CI + 10;
+  static constexpr int A = 0, U = NV, C0 = 2 * NV, CI = 3 * NV, CJ = CI + 1, IA = CI + 2, IA5 = CI + 3,
+                       N1I = CI + 4, N2I = CI + 5, N1J = CI + 6, N2J = CI + 7, N = (CI + 8 + 1) / 2 * 2;
   static_assert(N % 2 == 0, "records are whole 16-byte units");
 };
 
@@ -55,7 +58,7 @@ struct Slot {
   static_assert(S % 2 == 0, "slots are whole 16-byte units");
 };
 
-int lusgs_planes(int nv) { return 4 * nv + 10; }
+int lusgs_planes(int nv) { return 3 * nv + 10; }  // at least Rec<NV>::N and the FP32 record
 
 // normal flux of the Euler part (+ convected turbulence variables), the F(U)
 // half of comput_DFn (sub_LU_SGS.f90:122-137)
@@ -110,46 +113,56 @@ __global__ void __launch_bounds__(TILE) k_lusgs_prep(Lvl L, double alfa1) {
   if (visc) alfa += 2.0 * Lv;
   double ia = 1.0 / alfa, ia5 = (NV == 5) ? 1.0 / (alfa + Lv) : ia;
   double ni1 = g[G_NI1 * F + id], ni2 = g[G_NI2 * F + id], nj1 = g[G_NJ1 * F + id], nj2 = g[G_NJ2 * F + id];
+  double res[NV], K[2][NV];  // K[pass]: -(sum over directions of F_n(U_nb, s))
 #pragma unroll
   for (int m = 0; m < NV; m++) {
     double u = L.U[m * F + id];
-    rf[RC::A + m] = L.res[m * F + id];
-    rb[RC::A + m] = 0.0;
+    res[m] = L.res[m * F + id];
     rf[RC::U + m] = u;
     rb[RC::U + m] = u;
+    K[0][m] = 0.0;
+    K[1][m] = 0.0;
   }
   double *rr[2] = {rf, rb};
 #pragma unroll
   for (int pass = 0; pass < 2; pass++) {
     double *r = rr[pass];
+    const bool fwd = pass == 0;
     r[RC::IA] = ia; r[RC::IA5] = ia5;
-    r[RC::N1I] = ni1; r[RC::N2I] = ni2; r[RC::N1J] = nj1; r[RC::N2J] = nj2;
 #pragma unroll
     for (int dir = 0; dir < 2; dir++) {  // 0: i-neighbour, 1: j-neighbour
-      const bool fwd = pass == 0;
       const long long step = dir == 0 ? 1 : P;
       const long long nb = fwd ? id - step : id + step;
       const bool has = dir == 0 ? (fwd ? i > 1 : i < b.nx - 1) : (fwd ? j > 1 : j < b.ny - 1);
-      double Un[NV], Fo[NV], cc = 0.0, hh = 0.0;
+      double cc = 0.0, s1 = 0.0, s2 = 0.0;
       if (has) {
+        double Un[NV], Fo[NV];
 #pragma unroll
         for (int m = 0; m < NV; m++) Un[m] = L.U[m * F + nb];
-        fn<NV>(Un, dir == 0 ? ni1 : nj1, dir == 0 ? ni2 : nj2, gm1, Fo);
         cc = 0.5 * lc[(dir == 0 ? L_CI : L_CJ) * F + nb];
         if (visc) cc += lc[(dir == 0 ? L_VI : L_VJ) * F + nb];
-        // forward: this cell's face length; backward: the neighbour's (the
-        // reference pairs the normal of face i with the length of face i+1,
-        // sub_LU_SGS.f90:87-88,95-96)
-        hh = 0.5 * g[(dir == 0 ? G_SI : G_SJ) * F + (fwd ? id : nb)];
-      } else {
+        // forward: +0.5 s of this cell's face; backward: -0.5 s of the
+        // neighbour's face with this cell's normal (the reference pairs the
+        // normal of face i with the length of face i+1, sub_LU_SGS.f90:87-88,95-96)
+        double hh = 0.5 * g[(dir == 0 ? G_SI : G_SJ) * F + (fwd ? id : nb)];
+        if (!fwd) hh = -hh;
+        s1 = hh * (dir == 0 ? ni1 : nj1);
+        s2 = hh * (dir == 0 ? ni2 : nj2);
+        fn<NV>(Un, s1, s2, gm1, Fo);
 #pragma unroll
-        for (int m = 0; m < NV; m++) Fo[m] = 0.0;
+        for (int m = 0; m < NV; m++) K[pass][m] -= Fo[m];
       }
-#pragma unroll
-      for (int m = 0; m < NV; m++) r[(dir == 0 ? RC::FI : RC::FJ) + m] = Fo[m];
       r[dir == 0 ? RC::CI : RC::CJ] = cc;
-      r[dir == 0 ? RC::HI : RC::HJ] = hh;
+      r[dir == 0 ? RC::N1I : RC::N1J] = s1;
+      r[dir == 0 ? RC::N2I : RC::N2J] = s2;
     }
+  }
+#pragma unroll
+  for (int m = 0; m < NV; m++) {
+    rf[RC::A + m] = res[m] + K[0][m];
+    rf[RC::C0 + m] = 0.0;
+    rb[RC::A + m] = 0.0;
+    rb[RC::C0 + m] = K[1][m];
   }
 }
 
@@ -245,15 +258,12 @@ __global__ void __launch_bounds__(1024) k_lusgs_sweep(Lvl L, int update, int R, 
         cp_wait1();
         double acc[NV], F2[NV];
 #pragma unroll
-        for (int m = 0; m < NV; m++) acc[m] = fwd ? cur[RC::A + m] : 0.0;
+        for (int m = 0; m < NV; m++) acc[m] = fwd ? cur[RC::A + m] : cur[RC::C0 + m];
         if (fwd ? (i > 1) : (i < ni)) {
           fn_shipped<NV>(st, cur[RC::N1I], cur[RC::N2I], F2);
-          const double hh = cur[RC::HI], cc = cur[RC::CI];
+          const double cc = cur[RC::CI];
 #pragma unroll
-          for (int m = 0; m < NV; m++) {
-            double DF = F2[m] - cur[RC::FI + m];
-            acc[m] = acc[m] + (fwd ? hh * DF : -hh * DF) + cc * st[SL::D + m];
-          }
+          for (int m = 0; m < NV; m++) acc[m] = fma(cc, st[SL::D + m], acc[m] + F2[m]);
         }
         if (fwd ? (j > 1) : (j < rows)) {
           const double2 *s2 = reinterpret_cast<const double2 *>(sh + ((size_t)(buf ^ 1) * (R + 2) + (fwd ? rl : rl + 2)) * S);
@@ -261,12 +271,9 @@ __global__ void __launch_bounds__(1024) k_lusgs_sweep(Lvl L, int update, int R, 
 #pragma unroll
           for (int m = 0; m < S / 2; m++) { double2 v = s2[m]; sn[2 * m] = v.x; sn[2 * m + 1] = v.y; }
           fn_shipped<NV>(sn, cur[RC::N1J], cur[RC::N2J], F2);
-          const double hh = cur[RC::HJ], cc = cur[RC::CJ];
+          const double cc = cur[RC::CJ];
 #pragma unroll
-          for (int m = 0; m < NV; m++) {
-            double DF = F2[m] - cur[RC::FJ + m];
-            acc[m] = acc[m] + (fwd ? hh * DF : -hh * DF) + cc * sn[SL::D + m];
-          }
+          for (int m = 0; m < NV; m++) acc[m] = fma(cc, sn[SL::D + m], acc[m] + F2[m]);
         }
         const double ia = cur[RC::IA], ia5 = cur[RC::IA5];
 #pragma unroll
