@@ -280,6 +280,15 @@ int ec2d_mlp_predict(ec2d_mlp *m, const float *feat, long long n, float *pred);
 int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *rows_per_warp, int *concurrent,
                   double *ms_per_step);
 
+/* Precision of the face fluxes (reconstruction, Riemann solver, viscous
+ * stress) on the coarse multigrid levels: 64 (the default) or 32.  No
+ * counterpart in the reference.  The coarse levels only smooth the
+ * fine-level correction and their forcing is formed from the same FP32
+ * residual, so early convergence follows the FP64 run; the FP32 rounding
+ * the forcing carries limits the attainable drop to about 1e-7 of the first
+ * residual (measured on the flat plate), so deep convergence wants 64. */
+int ec2d_set_coarse_precision(ec2d_ctx *ctx, int bits);
+
 /* Wait for all queued work of the context. */
 int ec2d_sync(ec2d_ctx *ctx);
 

@@ -115,6 +115,7 @@ struct ec2d_ctx {
   bool lusgs_fp32 = false;  // LU-SGS sweeps in FP32 (mixed-precision mode)
   bool concurrent = true;   // i- and j-face flux kernels on two streams
   int lusgs_rpw = 32;       // rows per warp of the FP64 wavefront (one CTA per block)
+  bool coarse_fp32 = false; // face fluxes of multigrid levels >= 2 in FP32
   bool timing = false;
   // one pseudo-time step (single grid or V-cycle) captured as a CUDA graph:
   // the replay stands for graph_launches kernel launches and advances the
@@ -632,17 +633,20 @@ void residual(ec2d_ctx *ctx, int l) {
   // the i- and j-face kernels read the same primitives and write separate
   // planes: they run concurrently on two streams (graph branches); with
   // kernel timing on they run one after the other
+  // face fluxes of a coarse level in FP32 when selected (the coarse levels
+  // only smooth the fine-level correction)
+  const bool f32 = ctx->coarse_fp32 && l >= 2;
   if (!ctx->timing && ctx->concurrent) {
     ctx->launches += 2;
     cudaEventRecord(ctx->ev_fork, s);
     cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0);
-    launch_flux_j(L, ctx->side);
-    launch_flux_i(L, s);
+    launch_flux_j(L, f32, ctx->side);
+    launch_flux_i(L, f32, s);
     cudaEventRecord(ctx->ev_join, ctx->side);
     cudaStreamWaitEvent(s, ctx->ev_join, 0);
   } else {
-    K(ctx, "k_flux_i", l, 1, [&] { launch_flux_i(L, s); });
-    K(ctx, "k_flux_j", l, 1, [&] { launch_flux_j(L, s); });
+    K(ctx, "k_flux_i", l, 1, [&] { launch_flux_i(L, f32, s); });
+    K(ctx, "k_flux_j", l, 1, [&] { launch_flux_j(L, f32, s); });
   }
   const bool dual = ctx->P.Time_Method == Time_Dual && l == 1;
   const bool fused = !L.fdm && !dual;  // Res final after k_res: norm partials fused into it
@@ -1233,6 +1237,14 @@ int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *rows_per_w
   if (concurrent) *concurrent = ctx->concurrent ? 1 : 0;
   if (ms_per_step) *ms_per_step = best;
   return check_launch(ctx);
+}
+
+int ec2d_set_coarse_precision(ec2d_ctx *ctx, int bits) {
+  if (!ctx || (bits != 32 && bits != 64)) return EC2D_ERR_ARG;
+  bool fp32 = bits == 32;
+  if (fp32 != ctx->coarse_fp32) drop_graph(ctx);
+  ctx->coarse_fp32 = fp32;
+  return EC2D_OK;
 }
 
 int ec2d_set_lusgs_precision(ec2d_ctx *ctx, int bits) {

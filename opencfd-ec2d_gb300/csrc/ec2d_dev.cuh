@@ -87,88 +87,97 @@ __host__ __device__ __forceinline__ long long fidx(const BlkDev &b, int i, int j
   return b.off + (long long)(j + 2) * b.P + (i + 2);
 }
 
+// The face physics below is written once for the arithmetic type T: double
+// is the reference's arithmetic (every literal T(x) is then the same double
+// constant), float serves the FP32 coarse multigrid levels.
+
 // ---- reconstruction, sub_Residual.f90:477-659 --------------------------------
-__device__ __forceinline__ double minmod(double a, double b) {
-  if (a * b <= 0.0) return 0.0;
+template <typename T>
+__device__ __forceinline__ T minmod(T a, T b) {
+  if (a * b <= T(0.0)) return T(0.0);
   return (fabs(a) <= fabs(b)) ? a : b;
 }
 
 // scheme_fP (sub_Residual.f90:591-623): left state at the face between u2 and u3
-__device__ __forceinline__ double scheme_fp(double u1, double u2, double u3, double u4, int flag) {
-  const double ep = 1.0e-6, k3 = 1.0 / 3.0;
+template <typename T>
+__device__ __forceinline__ T scheme_fp(T u1, T u2, T u3, T u4, int flag) {
+  const T ep = T(1.0e-6), k3 = T(1.0) / T(3.0);
   switch (flag) {
     case Scheme_UD1: return u2;
-    case Scheme_UD3: return (-u1 + 5.0 * u2 + 2.0 * u3) / 6.0;
-    case Scheme_NND2: return u2 + 0.5 * minmod(u2 - u1, u3 - u2);
+    case Scheme_UD3: return (-u1 + T(5.0) * u2 + T(2.0) * u3) / T(6.0);
+    case Scheme_NND2: return u2 + T(0.5) * minmod(u2 - u1, u3 - u2);
     case Scheme_WENO3: {
-      double IS1 = (u2 - u1) * (u2 - u1), IS2 = (u3 - u2) * (u3 - u2);
-      double e1 = 1.0e-6 + IS1, e2 = 1.0e-6 + IS2;
-      double a1 = 1.0 / (3.0 * (e1 * e1)), a2 = 2.0 / (3.0 * (e2 * e2));
-      double w1 = a1 / (a1 + a2), w2 = a2 / (a1 + a2);
-      return w1 * (-u1 / 2.0 + 3.0 * u2 / 2.0) + w2 * (u2 / 2.0 + u3 / 2.0);
+      T IS1 = (u2 - u1) * (u2 - u1), IS2 = (u3 - u2) * (u3 - u2);
+      T e1 = T(1.0e-6) + IS1, e2 = T(1.0e-6) + IS2;
+      T a1 = T(1.0) / (T(3.0) * (e1 * e1)), a2 = T(2.0) / (T(3.0) * (e2 * e2));
+      T w1 = a1 / (a1 + a2), w2 = a2 / (a1 + a2);
+      return w1 * (-u1 / T(2.0) + T(3.0) * u2 / T(2.0)) + w2 * (u2 / T(2.0) + u3 / T(2.0));
     }
     case Scheme_MUSCL2:  // k=1, b=2
-      return u2 + 0.25 * ((1.0 - 1.0) * minmod(u2 - u1, 2.0 * (u3 - u2)) + (1.0 + 1.0) * minmod(u3 - u2, 2.0 * (u2 - u1)));
+      return u2 + T(0.25) * ((T(1.0) - T(1.0)) * minmod(u2 - u1, T(2.0) * (u3 - u2)) + (T(1.0) + T(1.0)) * minmod(u3 - u2, T(2.0) * (u2 - u1)));
     case Scheme_MUSCL3: {
-      double up = u3 - u2, um = u2 - u1;
-      double s = (2.0 * up * um + ep) / (up * up + um * um + ep);
-      return u2 + 0.25 * s * ((1.0 - k3 * s) * um + (1.0 + k3 * s) * up);
+      T up = u3 - u2, um = u2 - u1;
+      T s = (T(2.0) * up * um + ep) / (up * up + um * um + ep);
+      return u2 + T(0.25) * s * ((T(1.0) - k3 * s) * um + (T(1.0) + k3 * s) * up);
     }
     case Scheme_OMUSCL2: {
-      double r1 = (u2 - u1 + ep) / (u3 - u2 + ep), r2 = (u3 - u2 + ep) / (u4 - u3 + ep);
-      double f1 = 0.8 - 0.175 / r2 + 0.375 * r1;
-      double f = fmax(0.0, fmin(fmin(2.0, f1), 2.0 * r1));
-      return u2 + 0.5 * f * (u3 - u2);
+      T r1 = (u2 - u1 + ep) / (u3 - u2 + ep), r2 = (u3 - u2 + ep) / (u4 - u3 + ep);
+      T f1 = T(0.8) - T(0.175) / r2 + T(0.375) * r1;
+      T f = fmax(T(0.0), fmin(fmin(T(2.0), f1), T(2.0) * r1));
+      return u2 + T(0.5) * f * (u3 - u2);
     }
   }
-  return 0.0;
+  return T(0.0);
 }
 // scheme_fm (sub_Residual.f90:626-659): right state at the face between u2 and u3
-__device__ __forceinline__ double scheme_fm(double u1, double u2, double u3, double u4, int flag) {
-  const double ep = 1.0e-6, k3 = 1.0 / 3.0;
+template <typename T>
+__device__ __forceinline__ T scheme_fm(T u1, T u2, T u3, T u4, int flag) {
+  const T ep = T(1.0e-6), k3 = T(1.0) / T(3.0);
   switch (flag) {
     case Scheme_UD1: return u3;
-    case Scheme_UD3: return (2.0 * u2 + 5.0 * u3 - u4) / 6.0;
-    case Scheme_NND2: return u3 - 0.5 * minmod(u3 - u2, u4 - u3);
+    case Scheme_UD3: return (T(2.0) * u2 + T(5.0) * u3 - u4) / T(6.0);
+    case Scheme_NND2: return u3 - T(0.5) * minmod(u3 - u2, u4 - u3);
     case Scheme_WENO3: {
-      double IS1 = (u3 - u4) * (u3 - u4), IS2 = (u2 - u3) * (u2 - u3);
-      double e1 = 1.0e-6 + IS1, e2 = 1.0e-6 + IS2;
-      double a1 = 1.0 / (3.0 * (e1 * e1)), a2 = 2.0 / (3.0 * (e2 * e2));
-      double w1 = a1 / (a1 + a2), w2 = a2 / (a1 + a2);
-      return w1 * (-u4 / 2.0 + 3.0 * u3 / 2.0) + w2 * (u3 / 2.0 + u2 / 2.0);
+      T IS1 = (u3 - u4) * (u3 - u4), IS2 = (u2 - u3) * (u2 - u3);
+      T e1 = T(1.0e-6) + IS1, e2 = T(1.0e-6) + IS2;
+      T a1 = T(1.0) / (T(3.0) * (e1 * e1)), a2 = T(2.0) / (T(3.0) * (e2 * e2));
+      T w1 = a1 / (a1 + a2), w2 = a2 / (a1 + a2);
+      return w1 * (-u4 / T(2.0) + T(3.0) * u3 / T(2.0)) + w2 * (u3 / T(2.0) + u2 / T(2.0));
     }
     case Scheme_MUSCL2: {  // k=1/3, b=1
-      const double k = 1.0 / 3.0;
-      return u3 - 0.25 * ((1.0 - k) * minmod(u4 - u3, (u3 - u2)) + (1.0 + k) * minmod(u3 - u2, (u4 - u3)));
+      const T k = T(1.0) / T(3.0);
+      return u3 - T(0.25) * ((T(1.0) - k) * minmod(u4 - u3, (u3 - u2)) + (T(1.0) + k) * minmod(u3 - u2, (u4 - u3)));
     }
     case Scheme_MUSCL3: {
-      double up = u4 - u3, um = u3 - u2;
-      double s = (2.0 * up * um + ep) / (up * up + um * um + ep);
-      return u3 - 0.25 * s * ((1.0 - k3 * s) * up + (1.0 + k3 * s) * um);
+      T up = u4 - u3, um = u3 - u2;
+      T s = (T(2.0) * up * um + ep) / (up * up + um * um + ep);
+      return u3 - T(0.25) * s * ((T(1.0) - k3 * s) * up + (T(1.0) + k3 * s) * um);
     }
     case Scheme_OMUSCL2: {
-      double r1 = (u4 - u3 + ep) / (u3 - u2 + ep), r2 = (u3 - u2 + ep) / (u2 - u1 + ep);
-      double f1 = 0.8 - 0.175 / r2 + 0.375 * r1;
-      double f = fmax(0.0, fmin(fmin(2.0, f1), 2.0 * r1));
-      return u3 - 0.5 * f * (u3 - u2);
+      T r1 = (u4 - u3 + ep) / (u3 - u2 + ep), r2 = (u3 - u2 + ep) / (u2 - u1 + ep);
+      T f1 = T(0.8) - T(0.175) / r2 + T(0.375) * r1;
+      T f = fmax(T(0.0), fmin(fmin(T(2.0), f1), T(2.0) * r1));
+      return u3 - T(0.5) * f * (u3 - u2);
     }
   }
-  return 0.0;
+  return T(0.0);
 }
 
 // conservative (rho, rho u, rho v, E) -> primitive (rho, u, v, p), as at the
 // end of Reconstuction_conservative/Characteristic (sub_Residual.f90:526-527)
-__device__ __forceinline__ void cons_to_prim(const double Q[4], double W[4], double gm1) {
+template <typename T>
+__device__ __forceinline__ void cons_to_prim(const T Q[4], T W[4], T gm1) {
   W[0] = Q[0];
   W[1] = Q[1] / W[0];
   W[2] = Q[2] / W[0];
-  W[3] = (Q[3] - (W[1] * Q[1] + W[2] * Q[2]) * 0.5) * gm1;
+  W[3] = (Q[3] - (W[1] * Q[1] + W[2] * Q[2]) * T(0.5)) * gm1;
 }
 
 // S0[k][m]: stencil points k = i-2..i+1 (or j-2..j+1), variable m.
 // Reconstuction_original/conservative/Characteristic (sub_Residual.f90:505-586)
-__device__ __forceinline__ void reconstruct(int recon, int scheme, double S0[4][4], double gamma,
-                                            double UL[4], double UR[4]) {
+template <typename T>
+__device__ __forceinline__ void reconstruct(int recon, int scheme, T S0[4][4], T gamma,
+                                            T UL[4], T UR[4]) {
   if (recon == Recon_Original) {
 #pragma unroll
     for (int m = 0; m < 4; m++) {
@@ -177,9 +186,9 @@ __device__ __forceinline__ void reconstruct(int recon, int scheme, double S0[4][
     }
     return;
   }
-  double gm1 = gamma - 1.0;
+  T gm1 = gamma - T(1.0);
   if (recon == Recon_Conservative) {
-    double QL[4], QR[4];
+    T QL[4], QR[4];
 #pragma unroll
     for (int m = 0; m < 4; m++) {
       QL[m] = scheme_fp(S0[0][m], S0[1][m], S0[2][m], S0[3][m], scheme);
@@ -191,35 +200,35 @@ __device__ __forceinline__ void reconstruct(int recon, int scheme, double S0[4][
   }
   // characteristic: project on the left eigenvectors at the arithmetic
   // mid-state, limit each characteristic variable, project back
-  double Uh[4];
+  T Uh[4];
 #pragma unroll
-  for (int m = 0; m < 4; m++) Uh[m] = 0.5 * (S0[1][m] + S0[2][m]);
-  double d1 = Uh[0], u1 = Uh[1] / d1, v1 = Uh[2] / d1;
-  double p1 = (Uh[3] - (Uh[1] * u1 + Uh[2] * v1) * 0.5) * gm1;
-  double c1 = sqrt(gamma * p1 / d1);
-  double V2 = (u1 * u1 + v1 * v1) * 0.5;
-  double tmp1 = gm1 / c1, tmp3 = gm1 / (c1 * c1), tmp5 = 1.0 / (2.0 * c1), tmp0 = 1.0 / tmp3;
-  const double Sm[4][4] = {{V2 - tmp0, -u1, -v1, 1.0},
-                           {-v1, 0.0, 1.0, 0.0},
-                           {-u1 - V2 * tmp1, 1.0 + tmp1 * u1, tmp1 * v1, -tmp1},
-                           {-u1 + V2 * tmp1, 1.0 - tmp1 * u1, -tmp1 * v1, tmp1}};
-  double V0[4][4];
+  for (int m = 0; m < 4; m++) Uh[m] = T(0.5) * (S0[1][m] + S0[2][m]);
+  T d1 = Uh[0], u1 = Uh[1] / d1, v1 = Uh[2] / d1;
+  T p1 = (Uh[3] - (Uh[1] * u1 + Uh[2] * v1) * T(0.5)) * gm1;
+  T c1 = sqrt(gamma * p1 / d1);
+  T V2 = (u1 * u1 + v1 * v1) * T(0.5);
+  T tmp1 = gm1 / c1, tmp3 = gm1 / (c1 * c1), tmp5 = T(1.0) / (T(2.0) * c1), tmp0 = T(1.0) / tmp3;
+  const T Sm[4][4] = {{V2 - tmp0, -u1, -v1, T(1.0)},
+                           {-v1, T(0.0), T(1.0), T(0.0)},
+                           {-u1 - V2 * tmp1, T(1.0) + tmp1 * u1, tmp1 * v1, -tmp1},
+                           {-u1 + V2 * tmp1, T(1.0) - tmp1 * u1, -tmp1 * v1, tmp1}};
+  T V0[4][4];
 #pragma unroll
   for (int k = 0; k < 4; k++)
 #pragma unroll
     for (int m = 0; m < 4; m++)
       V0[k][m] = Sm[m][0] * S0[k][0] + Sm[m][1] * S0[k][1] + Sm[m][2] * S0[k][2] + Sm[m][3] * S0[k][3];
-  double VL[4], VR[4];
+  T VL[4], VR[4];
 #pragma unroll
   for (int m = 0; m < 4; m++) {
     VL[m] = scheme_fp(V0[0][m], V0[1][m], V0[2][m], V0[3][m], scheme);
     VR[m] = scheme_fm(V0[0][m], V0[1][m], V0[2][m], V0[3][m], scheme);
   }
-  const double S1[4][4] = {{-tmp3, 0.0, -tmp5, tmp5},
-                           {-tmp3 * u1, 0.0, 0.5 - u1 * tmp5, 0.5 + u1 * tmp5},
-                           {-tmp3 * v1, 1.0, -v1 * tmp5, v1 * tmp5},
+  const T S1[4][4] = {{-tmp3, T(0.0), -tmp5, tmp5},
+                           {-tmp3 * u1, T(0.0), T(0.5) - u1 * tmp5, T(0.5) + u1 * tmp5},
+                           {-tmp3 * v1, T(1.0), -v1 * tmp5, v1 * tmp5},
                            {-tmp3 * V2, v1, (c1 * u1 - V2 - tmp0) * tmp5, (c1 * u1 + V2 + tmp0) * tmp5}};
-  double QL[4], QR[4];
+  T QL[4], QR[4];
 #pragma unroll
   for (int m = 0; m < 4; m++) {
     QL[m] = S1[m][0] * VL[0] + S1[m][1] * VL[1] + S1[m][2] * VL[2] + S1[m][3] * VL[3];
@@ -231,161 +240,166 @@ __device__ __forceinline__ void reconstruct(int recon, int scheme, double S0[4][
 
 // ---- 1-D face fluxes on rotated primitive states (rho, u_n, u_t, p) ----------
 // Flux_Roe_1D, sub_flux_split.f90:265-324 (Harten entropy fix, delta = 0.1)
-__device__ __forceinline__ void flux_roe(const double *QL, const double *QR, double *F, double gamma) {
-  const double delt = 0.1;
-  double dl = QL[0], uul = QL[1], vvl = QL[2], pl = QL[3];
-  double dr = QR[0], uur = QR[1], vvr = QR[2], pr = QR[3];
-  double gm1 = gamma - 1.0;
-  double hl = gamma * pl / (gm1 * dl) + 0.5 * (uul * uul + vvl * vvl);
-  double hr = gamma * pr / (gm1 * dr) + 0.5 * (uur * uur + vvr * vvr);
-  double Fl0 = dl * uul, Fl1 = dl * uul * uul + pl, Fl2 = dl * uul * vvl, Fl3 = uul * dl * hl;
-  double Fr0 = dr * uur, Fr1 = dr * uur * uur + pr, Fr2 = dr * uur * vvr, Fr3 = uur * dr * hr;
-  double tmpp = sqrt(dr / dl);
-  double inv = 1.0 / (1.0 + tmpp);
-  double avd = 0.25 * dl * (1.0 + tmpp) * (1.0 + tmpp);
-  double avu = (uul + tmpp * uur) * inv;
-  double avv = (vvl + tmpp * vvr) * inv;
-  double avh = (hl + tmpp * hr) * inv;
-  double ava = sqrt(gm1 * (avh - 0.5 * (avu * avu + avv * avv)));
-  double l0 = fabs(avu - ava), l1 = fabs(avu), l3 = fabs(avu + ava);
-  const double i2d = 1.0 / (2.0 * delt);
+template <typename T>
+__device__ __forceinline__ void flux_roe(const T *QL, const T *QR, T *F, T gamma) {
+  const T delt = T(0.1);
+  T dl = QL[0], uul = QL[1], vvl = QL[2], pl = QL[3];
+  T dr = QR[0], uur = QR[1], vvr = QR[2], pr = QR[3];
+  T gm1 = gamma - T(1.0);
+  T hl = gamma * pl / (gm1 * dl) + T(0.5) * (uul * uul + vvl * vvl);
+  T hr = gamma * pr / (gm1 * dr) + T(0.5) * (uur * uur + vvr * vvr);
+  T Fl0 = dl * uul, Fl1 = dl * uul * uul + pl, Fl2 = dl * uul * vvl, Fl3 = uul * dl * hl;
+  T Fr0 = dr * uur, Fr1 = dr * uur * uur + pr, Fr2 = dr * uur * vvr, Fr3 = uur * dr * hr;
+  T tmpp = sqrt(dr / dl);
+  T inv = T(1.0) / (T(1.0) + tmpp);
+  T avd = T(0.25) * dl * (T(1.0) + tmpp) * (T(1.0) + tmpp);
+  T avu = (uul + tmpp * uur) * inv;
+  T avv = (vvl + tmpp * vvr) * inv;
+  T avh = (hl + tmpp * hr) * inv;
+  T ava = sqrt(gm1 * (avh - T(0.5) * (avu * avu + avv * avv)));
+  T l0 = fabs(avu - ava), l1 = fabs(avu), l3 = fabs(avu + ava);
+  const T i2d = T(1.0) / (T(2.0) * delt);
   if (l0 < delt) l0 = (l0 * l0 + delt * delt) * i2d;
   if (l1 < delt) l1 = (l1 * l1 + delt * delt) * i2d;
-  double l2 = l1;
+  T l2 = l1;
   if (l3 < delt) l3 = (l3 * l3 + delt * delt) * i2d;
-  double ia = 1.0 / ava;
-  double i2aa = 0.5 * ia * ia;
-  double dp = pr - pl;
-  double a0 = (avd * ava * (-uur + uul) + dp) * i2aa;
-  double a1 = dr - dl - dp * (ia * ia);
-  double a2 = avd * (vvr - vvl) * ia;
-  double a3 = (avd * ava * (uur - uul) + dp) * i2aa;
-  F[0] = 0.5 * (Fl0 + Fr0) - 0.5 * (l0 * a0 + l1 * a1 + l3 * a3);
-  F[1] = 0.5 * (Fl1 + Fr1) - 0.5 * (l0 * a0 * (avu - ava) + l1 * a1 * avu + l3 * a3 * (avu + ava));
-  F[2] = 0.5 * (Fl2 + Fr2) - 0.5 * (l0 * a0 * avv + l1 * a1 * avv + l2 * a2 + l3 * a3 * avv);
-  F[3] = 0.5 * (Fl3 + Fr3) - 0.5 * (l0 * a0 * (avh - avu * ava) + l1 * a1 * 0.5 * (avu * avu + avv * avv) +
+  T ia = T(1.0) / ava;
+  T i2aa = T(0.5) * ia * ia;
+  T dp = pr - pl;
+  T a0 = (avd * ava * (-uur + uul) + dp) * i2aa;
+  T a1 = dr - dl - dp * (ia * ia);
+  T a2 = avd * (vvr - vvl) * ia;
+  T a3 = (avd * ava * (uur - uul) + dp) * i2aa;
+  F[0] = T(0.5) * (Fl0 + Fr0) - T(0.5) * (l0 * a0 + l1 * a1 + l3 * a3);
+  F[1] = T(0.5) * (Fl1 + Fr1) - T(0.5) * (l0 * a0 * (avu - ava) + l1 * a1 * avu + l3 * a3 * (avu + ava));
+  F[2] = T(0.5) * (Fl2 + Fr2) - T(0.5) * (l0 * a0 * avv + l1 * a1 * avv + l2 * a2 + l3 * a3 * avv);
+  F[3] = T(0.5) * (Fl3 + Fr3) - T(0.5) * (l0 * a0 * (avh - avu * ava) + l1 * a1 * T(0.5) * (avu * avu + avv * avv) +
                                     l2 * a2 * avv + l3 * a3 * (avh + avu * ava));
 }
 
 // Flux_Ausm_1Da (AUSM+), sub_flux_split.f90:195-261
-__device__ __forceinline__ void flux_ausm(const double *QL, const double *QR, double *F, double gamma) {
-  double dl = QL[0], uul = QL[1], vvl = QL[2], pl = QL[3];
-  double dr = QR[0], uur = QR[1], vvr = QR[2], pr = QR[3];
-  double gm1 = gamma - 1.0;
-  double hl = gamma * pl / (gm1 * dl) + 0.5 * (uul * uul + vvl * vvl);
-  double hr = gamma * pr / (gm1 * dr) + 0.5 * (uur * uur + vvr * vvr);
-  double al = sqrt(gamma * pl / dl), ar = sqrt(gamma * pr / dr);
-  double a = 0.5 * (al + ar);
-  double ia = 1.0 / a;
-  double Ml = uul * ia, Mr = uur * ia;
-  double Mp4, Mm4, Pp5, Pm5;
-  double ml2 = Ml * Ml - 1.0, mr2 = Mr * Mr - 1.0;
-  if (fabs(Ml) >= 1.0) { Mp4 = 0.5 * (Ml + fabs(Ml)); Pp5 = 0.5 * (Ml + fabs(Ml)) / Ml; }
-  else { Mp4 = 0.25 * (Ml + 1.0) * (Ml + 1.0) + 0.125 * ml2 * ml2;
-         Pp5 = 0.25 * (Ml + 1.0) * (Ml + 1.0) * (2.0 - Ml) + 3.0 * Ml * ml2 * ml2 / 16.0; }
-  if (fabs(Mr) >= 1.0) { Mm4 = 0.5 * (Mr - fabs(Mr)); Pm5 = 0.5 * (Mr - fabs(Mr)) / Mr; }
-  else { Mm4 = -0.25 * (Mr - 1.0) * (Mr - 1.0) - 0.125 * mr2 * mr2;
-         Pm5 = 0.25 * (Mr - 1.0) * (Mr - 1.0) * (2.0 + Mr) - 3.0 * Mr * mr2 * mr2 / 16.0; }
-  double M = Mp4 + Mm4;
-  double xm = dl * a * fmax(0.0, M) + dr * a * fmin(0.0, M);
-  double dm = (M >= 0.0) ? a * fabs(M) * dl : a * fabs(M) * dr;
-  double p = pl * Pp5 + pr * Pm5;
-  F[0] = 0.5 * xm * (1.0 + 1.0) - 0.5 * dm * (1.0 - 1.0);
-  F[1] = 0.5 * xm * (uul + uur) - 0.5 * dm * (uur - uul) + p;
-  F[2] = 0.5 * xm * (vvl + vvr) - 0.5 * dm * (vvr - vvl);
-  F[3] = 0.5 * xm * (hl + hr) - 0.5 * dm * (hr - hl);
+template <typename T>
+__device__ __forceinline__ void flux_ausm(const T *QL, const T *QR, T *F, T gamma) {
+  T dl = QL[0], uul = QL[1], vvl = QL[2], pl = QL[3];
+  T dr = QR[0], uur = QR[1], vvr = QR[2], pr = QR[3];
+  T gm1 = gamma - T(1.0);
+  T hl = gamma * pl / (gm1 * dl) + T(0.5) * (uul * uul + vvl * vvl);
+  T hr = gamma * pr / (gm1 * dr) + T(0.5) * (uur * uur + vvr * vvr);
+  T al = sqrt(gamma * pl / dl), ar = sqrt(gamma * pr / dr);
+  T a = T(0.5) * (al + ar);
+  T ia = T(1.0) / a;
+  T Ml = uul * ia, Mr = uur * ia;
+  T Mp4, Mm4, Pp5, Pm5;
+  T ml2 = Ml * Ml - T(1.0), mr2 = Mr * Mr - T(1.0);
+  if (fabs(Ml) >= T(1.0)) { Mp4 = T(0.5) * (Ml + fabs(Ml)); Pp5 = T(0.5) * (Ml + fabs(Ml)) / Ml; }
+  else { Mp4 = T(0.25) * (Ml + T(1.0)) * (Ml + T(1.0)) + T(0.125) * ml2 * ml2;
+         Pp5 = T(0.25) * (Ml + T(1.0)) * (Ml + T(1.0)) * (T(2.0) - Ml) + T(3.0) * Ml * ml2 * ml2 / T(16.0); }
+  if (fabs(Mr) >= T(1.0)) { Mm4 = T(0.5) * (Mr - fabs(Mr)); Pm5 = T(0.5) * (Mr - fabs(Mr)) / Mr; }
+  else { Mm4 = -T(0.25) * (Mr - T(1.0)) * (Mr - T(1.0)) - T(0.125) * mr2 * mr2;
+         Pm5 = T(0.25) * (Mr - T(1.0)) * (Mr - T(1.0)) * (T(2.0) + Mr) - T(3.0) * Mr * mr2 * mr2 / T(16.0); }
+  T M = Mp4 + Mm4;
+  T xm = dl * a * fmax(T(0.0), M) + dr * a * fmin(T(0.0), M);
+  T dm = (M >= T(0.0)) ? a * fabs(M) * dl : a * fabs(M) * dr;
+  T p = pl * Pp5 + pr * Pm5;
+  F[0] = T(0.5) * xm * (T(1.0) + T(1.0)) - T(0.5) * dm * (T(1.0) - T(1.0));
+  F[1] = T(0.5) * xm * (uul + uur) - T(0.5) * dm * (uur - uul) + p;
+  F[2] = T(0.5) * xm * (vvl + vvr) - T(0.5) * dm * (vvr - vvl);
+  F[3] = T(0.5) * xm * (hl + hr) - T(0.5) * dm * (hr - hl);
 }
 
 // Flux_Van_Leer_1Da, sub_flux_split.f90:139-189
-__device__ __forceinline__ void flux_vanleer(const double *QL, const double *QR, double *F, double gamma) {
-  double dl = QL[0], uul = QL[1], vvl = QL[2], pl = QL[3];
-  double dr = QR[0], uur = QR[1], vvr = QR[2], pr = QR[3];
-  double gm1 = gamma - 1.0;
-  double al = sqrt(gamma * pl / dl), ar = sqrt(gamma * pr / dr);
-  double Ml = uul / al, Mr = uur / ar;
-  double fp0 = 0, fp1 = 0, fp2 = 0, fp3 = 0, fm0 = 0, fm1 = 0, fm2 = 0, fm3 = 0;
-  if (Ml >= 1.0) {
+template <typename T>
+__device__ __forceinline__ void flux_vanleer(const T *QL, const T *QR, T *F, T gamma) {
+  T dl = QL[0], uul = QL[1], vvl = QL[2], pl = QL[3];
+  T dr = QR[0], uur = QR[1], vvr = QR[2], pr = QR[3];
+  T gm1 = gamma - T(1.0);
+  T al = sqrt(gamma * pl / dl), ar = sqrt(gamma * pr / dr);
+  T Ml = uul / al, Mr = uur / ar;
+  T fp0 = 0, fp1 = 0, fp2 = 0, fp3 = 0, fm0 = 0, fm1 = 0, fm2 = 0, fm3 = 0;
+  if (Ml >= T(1.0)) {
     fp0 = dl * uul; fp1 = dl * uul * uul + pl; fp2 = dl * uul * vvl;
-    fp3 = uul * (gamma * pl / gm1 + 0.5 * dl * (uul * uul + vvl * vvl));
-  } else if (fabs(Ml) < 1.0) {
-    double tmp0 = dl * al * (0.25 * (1.0 + Ml) * (1.0 + Ml));
-    double w = gm1 * uul + 2.0 * al;
+    fp3 = uul * (gamma * pl / gm1 + T(0.5) * dl * (uul * uul + vvl * vvl));
+  } else if (fabs(Ml) < T(1.0)) {
+    T tmp0 = dl * al * (T(0.25) * (T(1.0) + Ml) * (T(1.0) + Ml));
+    T w = gm1 * uul + T(2.0) * al;
     fp0 = tmp0; fp1 = tmp0 * w / gamma; fp2 = tmp0 * vvl;
-    fp3 = tmp0 * (w * w * 0.5 / (gamma * gamma - 1.0) + 0.5 * (vvl * vvl));
+    fp3 = tmp0 * (w * w * T(0.5) / (gamma * gamma - T(1.0)) + T(0.5) * (vvl * vvl));
   }
-  if (Mr >= 1.0) {
-  } else if (fabs(Mr) < 1.0) {
-    double tmp0 = dr * ar * (-0.25 * (Mr - 1.0) * (Mr - 1.0));
-    double w = gm1 * uur - 2.0 * ar;
+  if (Mr >= T(1.0)) {
+  } else if (fabs(Mr) < T(1.0)) {
+    T tmp0 = dr * ar * (-T(0.25) * (Mr - T(1.0)) * (Mr - T(1.0)));
+    T w = gm1 * uur - T(2.0) * ar;
     fm0 = tmp0; fm1 = tmp0 * w / gamma; fm2 = tmp0 * vvr;
-    fm3 = tmp0 * (w * w * 0.5 / (gamma * gamma - 1.0) + 0.5 * (vvr * vvr));
-  } else if (Mr <= -1.0) {
+    fm3 = tmp0 * (w * w * T(0.5) / (gamma * gamma - T(1.0)) + T(0.5) * (vvr * vvr));
+  } else if (Mr <= -T(1.0)) {
     fm0 = dr * uur; fm1 = dr * uur * uur + pr; fm2 = dr * uur * vvr;
-    fm3 = uur * (gamma * pr / gm1 + 0.5 * dr * (uur * uur + vvr * vvr));
+    fm3 = uur * (gamma * pr / gm1 + T(0.5) * dr * (uur * uur + vvr * vvr));
   }
   F[0] = fp0 + fm0; F[1] = fp1 + fm1; F[2] = fp2 + fm2; F[3] = fp3 + fm3;
 }
 
 // Flux_steger_warming_1Da, sub_flux_split.f90:99-136
-__device__ __forceinline__ void flux_sw(const double *QL, const double *QR, double *F, double gamma) {
-  double dl = QL[0], uul = QL[1], vvl = QL[2], pl = QL[3];
-  double dr = QR[0], uur = QR[1], vvr = QR[2], pr = QR[3];
-  double al = sqrt(gamma * pl / dl), ar = sqrt(gamma * pr / dr);
-  double gm1 = gamma - 1.0;
-  double tmp1 = 2.0 * gm1, tmp3 = (3.0 - gamma) / (2.0 * gm1);
-  double E1P = (uul + fabs(uul)) * 0.5, E2P = (uul - al + fabs(uul - al)) * 0.5, E3P = (uul + al + fabs(uul + al)) * 0.5;
-  double t0 = dl / (2.0 * gamma);
-  double p0 = t0 * (tmp1 * E1P + E2P + E3P);
-  double p1 = t0 * (tmp1 * E1P * uul + E2P * (uul - al) + E3P * (uul + al));
-  double p2 = t0 * (tmp1 * E1P * vvl + E2P * vvl + E3P * vvl);
-  double p3 = t0 * (E1P * gm1 * (uul * uul + vvl * vvl) + E2P * ((uul - al) * (uul - al) + vvl * vvl) * 0.5 +
-                    E3P * ((uul + al) * (uul + al) + vvl * vvl) * 0.5 + tmp3 * al * al * (E2P + E3P));
-  double E1M = (uur - fabs(uur)) * 0.5, E2M = (uur - ar - fabs(uur - ar)) * 0.5, E3M = (uur + ar - fabs(uur + ar)) * 0.5;
-  t0 = dr / (2.0 * gamma);
-  double m0 = t0 * (tmp1 * E1M + E2M + E3M);
-  double m1 = t0 * (tmp1 * E1M * uur + E2M * (uur - ar) + E3M * (uur + ar));
-  double m2 = t0 * (tmp1 * E1M * vvr + E2M * vvr + E3M * vvr);
-  double m3 = t0 * (E1M * gm1 * (uur * uur + vvr * vvr) + E2M * ((uur - ar) * (uur - ar) + vvr * vvr) * 0.5 +
-                    E3M * ((uur + ar) * (uur + ar) + vvr * vvr) * 0.5 + tmp3 * ar * ar * (E2M + E3M));
+template <typename T>
+__device__ __forceinline__ void flux_sw(const T *QL, const T *QR, T *F, T gamma) {
+  T dl = QL[0], uul = QL[1], vvl = QL[2], pl = QL[3];
+  T dr = QR[0], uur = QR[1], vvr = QR[2], pr = QR[3];
+  T al = sqrt(gamma * pl / dl), ar = sqrt(gamma * pr / dr);
+  T gm1 = gamma - T(1.0);
+  T tmp1 = T(2.0) * gm1, tmp3 = (T(3.0) - gamma) / (T(2.0) * gm1);
+  T E1P = (uul + fabs(uul)) * T(0.5), E2P = (uul - al + fabs(uul - al)) * T(0.5), E3P = (uul + al + fabs(uul + al)) * T(0.5);
+  T t0 = dl / (T(2.0) * gamma);
+  T p0 = t0 * (tmp1 * E1P + E2P + E3P);
+  T p1 = t0 * (tmp1 * E1P * uul + E2P * (uul - al) + E3P * (uul + al));
+  T p2 = t0 * (tmp1 * E1P * vvl + E2P * vvl + E3P * vvl);
+  T p3 = t0 * (E1P * gm1 * (uul * uul + vvl * vvl) + E2P * ((uul - al) * (uul - al) + vvl * vvl) * T(0.5) +
+                    E3P * ((uul + al) * (uul + al) + vvl * vvl) * T(0.5) + tmp3 * al * al * (E2P + E3P));
+  T E1M = (uur - fabs(uur)) * T(0.5), E2M = (uur - ar - fabs(uur - ar)) * T(0.5), E3M = (uur + ar - fabs(uur + ar)) * T(0.5);
+  t0 = dr / (T(2.0) * gamma);
+  T m0 = t0 * (tmp1 * E1M + E2M + E3M);
+  T m1 = t0 * (tmp1 * E1M * uur + E2M * (uur - ar) + E3M * (uur + ar));
+  T m2 = t0 * (tmp1 * E1M * vvr + E2M * vvr + E3M * vvr);
+  T m3 = t0 * (E1M * gm1 * (uur * uur + vvr * vvr) + E2M * ((uur - ar) * (uur - ar) + vvr * vvr) * T(0.5) +
+                    E3M * ((uur + ar) * (uur + ar) + vvr * vvr) * T(0.5) + tmp3 * ar * ar * (E2M + E3M));
   F[0] = p0 + m0; F[1] = p1 + m1; F[2] = p2 + m2; F[3] = p3 + m3;
 }
 
 // Flux_HLL_HLLC_1D, sub_flux_split.f90:16-93
-__device__ __forceinline__ void flux_hll(const double *QL, const double *QR, double *F, double gamma, bool hllc) {
-  double dl = QL[0], uul = QL[1], vvl = QL[2], pl = QL[3];
-  double dr = QR[0], uur = QR[1], vvr = QR[2], pr = QR[3];
-  double gm1 = gamma - 1.0;
-  double UL[4] = {dl, dl * uul, dl * vvl, pl / gm1 + dl * (uul * uul + vvl * vvl) * 0.5};
-  double UR[4] = {dr, dr * uur, dr * vvr, pr / gm1 + dr * (uur * uur + vvr * vvr) * 0.5};
-  double al = sqrt(gamma * pl / dl), ar = sqrt(gamma * pr / dr);
-  double p_pvrs = 0.5 * (pl + pr) - (uur - uul) * (dl + dr) * (al + ar) * 0.125;
-  double p_star = fmax(0.0, p_pvrs);
-  double g2 = (gamma + 1.0) / (2.0 * gamma);
-  double qql = (p_star <= pl) ? 1.0 : sqrt(1.0 + g2 * (p_star / pl - 1.0));
-  double qqr = (p_star <= pr) ? 1.0 : sqrt(1.0 + g2 * (p_star / pr - 1.0));
-  double Sl = uul - al * qql, Sr = uur + ar * qqr;
-  double Fl[4] = {UL[1], UL[1] * uul + pl, UL[2] * uul, uul * (UL[3] + pl)};
-  double Fr[4] = {UR[1], UR[1] * uur + pr, UR[2] * uur, uur * (UR[3] + pr)};
+template <typename T>
+__device__ __forceinline__ void flux_hll(const T *QL, const T *QR, T *F, T gamma, bool hllc) {
+  T dl = QL[0], uul = QL[1], vvl = QL[2], pl = QL[3];
+  T dr = QR[0], uur = QR[1], vvr = QR[2], pr = QR[3];
+  T gm1 = gamma - T(1.0);
+  T UL[4] = {dl, dl * uul, dl * vvl, pl / gm1 + dl * (uul * uul + vvl * vvl) * T(0.5)};
+  T UR[4] = {dr, dr * uur, dr * vvr, pr / gm1 + dr * (uur * uur + vvr * vvr) * T(0.5)};
+  T al = sqrt(gamma * pl / dl), ar = sqrt(gamma * pr / dr);
+  T p_pvrs = T(0.5) * (pl + pr) - (uur - uul) * (dl + dr) * (al + ar) * T(0.125);
+  T p_star = fmax(T(0.0), p_pvrs);
+  T g2 = (gamma + T(1.0)) / (T(2.0) * gamma);
+  T qql = (p_star <= pl) ? T(1.0) : sqrt(T(1.0) + g2 * (p_star / pl - T(1.0)));
+  T qqr = (p_star <= pr) ? T(1.0) : sqrt(T(1.0) + g2 * (p_star / pr - T(1.0)));
+  T Sl = uul - al * qql, Sr = uur + ar * qqr;
+  T Fl[4] = {UL[1], UL[1] * uul + pl, UL[2] * uul, uul * (UL[3] + pl)};
+  T Fr[4] = {UR[1], UR[1] * uur + pr, UR[2] * uur, uur * (UR[3] + pr)};
   if (!hllc) {
     if (Sl >= 0) { for (int m = 0; m < 4; m++) F[m] = Fl[m]; }
     else if (Sr <= 0) { for (int m = 0; m < 4; m++) F[m] = Fr[m]; }
-    else { double inv = 1.0 / (Sr - Sl);
+    else { T inv = T(1.0) / (Sr - Sl);
       for (int m = 0; m < 4; m++) F[m] = (Sr * Fl[m] - Sl * Fr[m] + Sl * Sr * (UR[m] - UL[m])) * inv; }
     return;
   }
-  double S_star = (pr - pl + dl * uul * (Sl - uul) - dr * uur * (Sr - uur)) / (dl * (Sl - uul) - dr * (Sr - uur));
+  T S_star = (pr - pl + dl * uul * (Sl - uul) - dr * uur * (Sr - uur)) / (dl * (Sl - uul) - dr * (Sr - uur));
   if (Sl >= 0) { for (int m = 0; m < 4; m++) F[m] = Fl[m]; return; }
   if (Sr <= 0) { for (int m = 0; m < 4; m++) F[m] = Fr[m]; return; }
   if (S_star >= 0) {
-    double tmpl = dl * (Sl - uul) / (Sl - S_star);
-    double tmp = UL[3] / dl + (S_star - uul) * (S_star + pl / (dl * (Sl - uul)));
+    T tmpl = dl * (Sl - uul) / (Sl - S_star);
+    T tmp = UL[3] / dl + (S_star - uul) * (S_star + pl / (dl * (Sl - uul)));
     F[0] = Fl[0] + Sl * (tmpl - UL[0]);
     F[1] = Fl[1] + Sl * (tmpl * S_star - UL[1]);
     F[2] = Fl[2] + Sl * (tmpl * vvl - UL[2]);
     F[3] = Fl[3] + Sl * (tmpl * tmp - UL[3]);
   } else {
-    double tmpr = dr * (Sr - uur) / (Sr - S_star);
-    double tmp = UR[3] / dr + (S_star - uur) * (S_star + pr / (dr * (Sr - uur)));
+    T tmpr = dr * (Sr - uur) / (Sr - S_star);
+    T tmp = UR[3] / dr + (S_star - uur) * (S_star + pr / (dr * (Sr - uur)));
     F[0] = Fr[0] + Sr * (tmpr - UR[0]);
     F[1] = Fr[1] + Sr * (tmpr * S_star - UR[1]);
     F[2] = Fr[2] + Sr * (tmpr * vvr - UR[2]);
@@ -393,7 +407,8 @@ __device__ __forceinline__ void flux_hll(const double *QL, const double *QR, dou
   }
 }
 
-__device__ __forceinline__ void face_flux(int iflux, const double *QL, const double *QR, double *F, double gamma) {
+template <typename T>
+__device__ __forceinline__ void face_flux(int iflux, const T *QL, const T *QR, T *F, T gamma) {
   switch (iflux) {
     case Flux_Roe: flux_roe(QL, QR, F, gamma); return;
     case Flux_Ausm: flux_ausm(QL, QR, F, gamma); return;
@@ -402,22 +417,23 @@ __device__ __forceinline__ void face_flux(int iflux, const double *QL, const dou
     case Flux_HLL: flux_hll(QL, QR, F, gamma, false); return;
     case Flux_HLLC: flux_hll(QL, QR, F, gamma, true); return;
   }
-  F[0] = F[1] = F[2] = F[3] = 0.0;
+  F[0] = F[1] = F[2] = F[3] = T(0.0);
 }
 
 // viscous stress and heat flux through a face from the face-local 2x2
 // Jacobian of cell centres, sub_Residual.f90:313-343 / 419-450
-__device__ __forceinline__ void viscous_face(double Dix, double Diy, double Djx, double Djy, double Diu, double Div,
-                                             double DiT, double Dju, double Djv, double DjT, double Amu1, double Amk1,
-                                             double u1, double v1, double n1, double n2, double s, double &F2,
-                                             double &F3, double &F4) {
-  double Ds = 1.0 / (Dix * Djy - Djx * Diy);
-  double ux = (Diu * Djy - Dju * Diy) * Ds, vx = (Div * Djy - Djv * Diy) * Ds, Tx = (DiT * Djy - DjT * Diy) * Ds;
-  double uy = (-Diu * Djx + Dju * Dix) * Ds, vy = (-Div * Djx + Djv * Dix) * Ds, Ty = (-DiT * Djx + DjT * Dix) * Ds;
-  double t11 = ((4.0 / 3.0) * ux - (2.0 / 3.0) * vy) * Amu1;
-  double t22 = ((4.0 / 3.0) * vy - (2.0 / 3.0) * ux) * Amu1;
-  double t12 = (uy + vx) * Amu1;
-  double E1 = u1 * t11 + v1 * t12 + Amk1 * Tx, E2 = u1 * t12 + v1 * t22 + Amk1 * Ty;
+template <typename T>
+__device__ __forceinline__ void viscous_face(T Dix, T Diy, T Djx, T Djy, T Diu, T Div,
+                                             T DiT, T Dju, T Djv, T DjT, T Amu1, T Amk1,
+                                             T u1, T v1, T n1, T n2, T s, T &F2,
+                                             T &F3, T &F4) {
+  T Ds = T(1.0) / (Dix * Djy - Djx * Diy);
+  T ux = (Diu * Djy - Dju * Diy) * Ds, vx = (Div * Djy - Djv * Diy) * Ds, Tx = (DiT * Djy - DjT * Diy) * Ds;
+  T uy = (-Diu * Djx + Dju * Dix) * Ds, vy = (-Div * Djx + Djv * Dix) * Ds, Ty = (-DiT * Djx + DjT * Dix) * Ds;
+  T t11 = ((T(4.0) / T(3.0)) * ux - (T(2.0) / T(3.0)) * vy) * Amu1;
+  T t22 = ((T(4.0) / T(3.0)) * vy - (T(2.0) / T(3.0)) * ux) * Amu1;
+  T t12 = (uy + vx) * Amu1;
+  T E1 = u1 * t11 + v1 * t12 + Amk1 * Tx, E2 = u1 * t12 + v1 * t22 + Amk1 * Ty;
   F2 += (t11 * n1 + t12 * n2) * s;
   F3 += (t12 * n1 + t22 * n2) * s;
   F4 += (E1 * n1 + E2 * n2) * s;

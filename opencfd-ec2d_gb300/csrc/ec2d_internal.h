@@ -9,8 +9,8 @@ namespace ec2d {
 
 // k_residual.cu
 void launch_prim(const Lvl &L, cudaStream_t s);
-void launch_flux_i(const Lvl &L, cudaStream_t s);
-void launch_flux_j(const Lvl &L, cudaStream_t s);
+void launch_flux_i(const Lvl &L, bool fp32, cudaStream_t s);
+void launch_flux_j(const Lvl &L, bool fp32, cudaStream_t s);
 void launch_res(const Lvl &L, bool with_norms, cudaStream_t s);
 void launch_norms(const Lvl &L, const int *case_tile0, const int *case_ntile, const int *case_ncell, bool partials,
                   cudaStream_t s);

@@ -63,6 +63,7 @@ __device__ __forceinline__ bool in_fdm_core(const BlkDev &b, int i, int j) {
 
 // i-direction face loop of Residual_FVM (sub_Residual.f90:238-346): face (i,j),
 // i=1..nx, j=1..ny-1, between cells (i-1,j) and (i,j).
+template <typename T>
 __global__ void __launch_bounds__(TILE) k_flux_i(Lvl L) {
   int bk, i, j;
   if (!tile_ij(L, bk, i, j)) return;
@@ -72,50 +73,50 @@ __global__ void __launch_bounds__(TILE) k_flux_i(Lvl L) {
   const CaseDev &c = L.cs[b.cas];
   const long long F = L.F;
   long long id = fidx(b, i, j);
-  double si = L.geo[G_SI * F + id], n1 = L.geo[G_NI1 * F + id], n2 = L.geo[G_NI2 * F + id];
-  double S0[4][4], UL[4], UR[4];
+  T si = (T)L.geo[G_SI * F + id], n1 = (T)L.geo[G_NI1 * F + id], n2 = (T)L.geo[G_NI2 * F + id];
+  T S0[4][4], UL[4], UR[4];
   if (L.recon == Recon_Original) {
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       long long s = id + (k - 2);
-      S0[k][0] = L.q[Q_D * F + s]; S0[k][1] = L.q[Q_U * F + s];
-      S0[k][2] = L.q[Q_V * F + s]; S0[k][3] = L.q[Q_P * F + s];
+      S0[k][0] = (T)L.q[Q_D * F + s]; S0[k][1] = (T)L.q[Q_U * F + s];
+      S0[k][2] = (T)L.q[Q_V * F + s]; S0[k][3] = (T)L.q[Q_P * F + s];
     }
   } else {
 #pragma unroll
     for (int k = 0; k < 4; k++)
 #pragma unroll
-      for (int m = 0; m < 4; m++) S0[k][m] = L.U[m * F + id + (k - 2)];
+      for (int m = 0; m < 4; m++) S0[k][m] = (T)L.U[m * F + id + (k - 2)];
   }
-  reconstruct(L.recon, L.scheme, S0, c.gamma, UL, UR);
-  double QL[4] = {UL[0], UL[1] * n1 + UL[2] * n2, -UL[1] * n2 + UL[2] * n1, UL[3]};
-  double QR[4] = {UR[0], UR[1] * n1 + UR[2] * n2, -UR[1] * n2 + UR[2] * n1, UR[3]};
-  double Fl[4];
-  face_flux(L.flux, QL, QR, Fl, c.gamma);
-  double F0 = -Fl[0] * si, F1 = -(Fl[1] * n1 - Fl[2] * n2) * si, F2 = -(Fl[1] * n2 + Fl[2] * n1) * si, F3 = -Fl[3] * si;
+  reconstruct(L.recon, L.scheme, S0, (T)c.gamma, UL, UR);
+  T QL[4] = {UL[0], UL[1] * n1 + UL[2] * n2, -UL[1] * n2 + UL[2] * n1, UL[3]};
+  T QR[4] = {UR[0], UR[1] * n1 + UR[2] * n2, -UR[1] * n2 + UR[2] * n1, UR[3]};
+  T Fl[4];
+  face_flux(L.flux, QL, QR, Fl, (T)c.gamma);
+  T F0 = -Fl[0] * si, F1 = -(Fl[1] * n1 - Fl[2] * n2) * si, F2 = -(Fl[1] * n2 + Fl[2] * n1) * si, F3 = -Fl[3] * si;
   if (L.visc) {
     long long w = id - 1, nN = id + b.P, nS = id - b.P;
-    double Amu1, Amk1;
+    T Amu1, Amk1;
     if (i == 1) {
-      Amu1 = L.amu[id] + L.amut[id];
-      Amk1 = c.Cp * (L.amu[id] / c.Pr + L.amut[id] / PrT);
+      Amu1 = (T)L.amu[id] + (T)L.amut[id];
+      Amk1 = (T)c.Cp * ((T)L.amu[id] / (T)c.Pr + (T)L.amut[id] / (T)PrT);
     } else if (i == b.nx) {
-      Amu1 = L.amu[w] + L.amut[w];
-      Amk1 = c.Cp * (L.amu[w] / c.Pr + L.amut[w] / PrT);
+      Amu1 = (T)L.amu[w] + (T)L.amut[w];
+      Amk1 = (T)c.Cp * ((T)L.amu[w] / (T)c.Pr + (T)L.amut[w] / (T)PrT);
     } else {
-      Amu1 = (L.amu[w] + L.amu[id] + L.amut[w] + L.amut[id]) * 0.5;
-      Amk1 = c.Cp * ((L.amu[w] + L.amu[id]) / c.Pr + (L.amut[w] + L.amut[id]) / PrT) * 0.5;
+      Amu1 = ((T)L.amu[w] + (T)L.amu[id] + (T)L.amut[w] + (T)L.amut[id]) * T(0.5);
+      Amk1 = (T)c.Cp * (((T)L.amu[w] + (T)L.amu[id]) / (T)c.Pr + ((T)L.amut[w] + (T)L.amut[id]) / (T)PrT) * T(0.5);
     }
     const double *x1 = L.geo + G_X1 * F, *y1 = L.geo + G_Y1 * F;
     const double *uu = L.q + Q_U * F, *vv = L.q + Q_V * F, *TT = L.q + Q_T * F;
-    double Dix = x1[id] - x1[w], Diy = y1[id] - y1[w];
-    double Djx = (x1[nN - 1] + x1[nN] - x1[nS - 1] - x1[nS]) * 0.25;
-    double Djy = (y1[nN - 1] + y1[nN] - y1[nS - 1] - y1[nS]) * 0.25;
-    double Diu = uu[id] - uu[w], Div = vv[id] - vv[w], DiT = TT[id] - TT[w];
-    double Dju = (uu[nN - 1] + uu[nN] - uu[nS - 1] - uu[nS]) * 0.25;
-    double Djv = (vv[nN - 1] + vv[nN] - vv[nS - 1] - vv[nS]) * 0.25;
-    double DjT = (TT[nN - 1] + TT[nN] - TT[nS - 1] - TT[nS]) * 0.25;
-    double u1 = (uu[id] + uu[w]) * 0.5, v1 = (vv[id] + vv[w]) * 0.5;
+    T Dix = (T)x1[id] - (T)x1[w], Diy = (T)y1[id] - (T)y1[w];
+    T Djx = ((T)x1[nN - 1] + (T)x1[nN] - (T)x1[nS - 1] - (T)x1[nS]) * T(0.25);
+    T Djy = ((T)y1[nN - 1] + (T)y1[nN] - (T)y1[nS - 1] - (T)y1[nS]) * T(0.25);
+    T Diu = (T)uu[id] - (T)uu[w], Div = (T)vv[id] - (T)vv[w], DiT = (T)TT[id] - (T)TT[w];
+    T Dju = ((T)uu[nN - 1] + (T)uu[nN] - (T)uu[nS - 1] - (T)uu[nS]) * T(0.25);
+    T Djv = ((T)vv[nN - 1] + (T)vv[nN] - (T)vv[nS - 1] - (T)vv[nS]) * T(0.25);
+    T DjT = ((T)TT[nN - 1] + (T)TT[nN] - (T)TT[nS - 1] - (T)TT[nS]) * T(0.25);
+    T u1 = ((T)uu[id] + (T)uu[w]) * T(0.5), v1 = ((T)vv[id] + (T)vv[w]) * T(0.5);
     viscous_face(Dix, Diy, Djx, Djy, Diu, Div, DiT, Dju, Djv, DjT, Amu1, Amk1, u1, v1, n1, n2, si, F1, F2, F3);
   }
   L.fi[id] = F0; L.fi[F + id] = F1; L.fi[2 * F + id] = F2; L.fi[3 * F + id] = F3;
@@ -123,6 +124,7 @@ __global__ void __launch_bounds__(TILE) k_flux_i(Lvl L) {
 
 // j-direction face loop of Residual_FVM (sub_Residual.f90:352-455): face (i,j),
 // i=1..nx-1, j=1..ny, between cells (i,j-1) and (i,j).
+template <typename T>
 __global__ void __launch_bounds__(TILE) k_flux_j(Lvl L) {
   int bk, i, j;
   if (!tile_ij(L, bk, i, j)) return;
@@ -133,52 +135,52 @@ __global__ void __launch_bounds__(TILE) k_flux_j(Lvl L) {
   const long long F = L.F;
   const long long P = b.P;
   long long id = fidx(b, i, j);
-  double sj = L.geo[G_SJ * F + id], n1 = L.geo[G_NJ1 * F + id], n2 = L.geo[G_NJ2 * F + id];
-  double S0[4][4], UL[4], UR[4];
+  T sj = (T)L.geo[G_SJ * F + id], n1 = (T)L.geo[G_NJ1 * F + id], n2 = (T)L.geo[G_NJ2 * F + id];
+  T S0[4][4], UL[4], UR[4];
   int scheme = L.scheme;
   if (L.recon == Recon_Original) {
     scheme = L.gscheme;  // the reference passes the global Iflag_Scheme here (sub_Residual.f90:367)
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       long long s = id + (k - 2) * P;
-      S0[k][0] = L.q[Q_D * F + s]; S0[k][1] = L.q[Q_U * F + s];
-      S0[k][2] = L.q[Q_V * F + s]; S0[k][3] = L.q[Q_P * F + s];
+      S0[k][0] = (T)L.q[Q_D * F + s]; S0[k][1] = (T)L.q[Q_U * F + s];
+      S0[k][2] = (T)L.q[Q_V * F + s]; S0[k][3] = (T)L.q[Q_P * F + s];
     }
   } else {
 #pragma unroll
     for (int k = 0; k < 4; k++)
 #pragma unroll
-      for (int m = 0; m < 4; m++) S0[k][m] = L.U[m * F + id + (k - 2) * P];
+      for (int m = 0; m < 4; m++) S0[k][m] = (T)L.U[m * F + id + (k - 2) * P];
   }
-  reconstruct(L.recon, scheme, S0, c.gamma, UL, UR);
-  double QL[4] = {UL[0], UL[1] * n1 + UL[2] * n2, -UL[1] * n2 + UL[2] * n1, UL[3]};
-  double QR[4] = {UR[0], UR[1] * n1 + UR[2] * n2, -UR[1] * n2 + UR[2] * n1, UR[3]};
-  double Fl[4];
-  face_flux(L.flux, QL, QR, Fl, c.gamma);
-  double F0 = -Fl[0] * sj, F1 = -(Fl[1] * n1 - Fl[2] * n2) * sj, F2 = -(Fl[1] * n2 + Fl[2] * n1) * sj, F3 = -Fl[3] * sj;
+  reconstruct(L.recon, scheme, S0, (T)c.gamma, UL, UR);
+  T QL[4] = {UL[0], UL[1] * n1 + UL[2] * n2, -UL[1] * n2 + UL[2] * n1, UL[3]};
+  T QR[4] = {UR[0], UR[1] * n1 + UR[2] * n2, -UR[1] * n2 + UR[2] * n1, UR[3]};
+  T Fl[4];
+  face_flux(L.flux, QL, QR, Fl, (T)c.gamma);
+  T F0 = -Fl[0] * sj, F1 = -(Fl[1] * n1 - Fl[2] * n2) * sj, F2 = -(Fl[1] * n2 + Fl[2] * n1) * sj, F3 = -Fl[3] * sj;
   if (L.visc) {
     long long s = id - P;
-    double Amu1, Amk1;
+    T Amu1, Amk1;
     if (j == 1) {
-      Amu1 = L.amu[id] + L.amut[id];
-      Amk1 = c.Cp * (L.amu[id] / c.Pr + L.amut[id] / PrT);
+      Amu1 = (T)L.amu[id] + (T)L.amut[id];
+      Amk1 = (T)c.Cp * ((T)L.amu[id] / (T)c.Pr + (T)L.amut[id] / (T)PrT);
     } else if (j == b.ny) {
-      Amu1 = L.amu[s] + L.amut[s];
-      Amk1 = c.Cp * (L.amu[s] / c.Pr + L.amut[s] / PrT);
+      Amu1 = (T)L.amu[s] + (T)L.amut[s];
+      Amk1 = (T)c.Cp * ((T)L.amu[s] / (T)c.Pr + (T)L.amut[s] / (T)PrT);
     } else {
-      Amu1 = (L.amu[id] + L.amu[s] + L.amut[id] + L.amut[s]) * 0.5;
-      Amk1 = c.Cp * ((L.amu[s] + L.amu[id]) / c.Pr + (L.amut[s] + L.amut[id]) / PrT) * 0.5;
+      Amu1 = ((T)L.amu[id] + (T)L.amu[s] + (T)L.amut[id] + (T)L.amut[s]) * T(0.5);
+      Amk1 = (T)c.Cp * (((T)L.amu[s] + (T)L.amu[id]) / (T)c.Pr + ((T)L.amut[s] + (T)L.amut[id]) / (T)PrT) * T(0.5);
     }
     const double *x1 = L.geo + G_X1 * F, *y1 = L.geo + G_Y1 * F;
     const double *uu = L.q + Q_U * F, *vv = L.q + Q_V * F, *TT = L.q + Q_T * F;
-    double Dix = (x1[s + 1] + x1[id + 1] - x1[s - 1] - x1[id - 1]) * 0.25;
-    double Diy = (y1[s + 1] + y1[id + 1] - y1[s - 1] - y1[id - 1]) * 0.25;
-    double Djx = x1[id] - x1[s], Djy = y1[id] - y1[s];
-    double Diu = (uu[s + 1] + uu[id + 1] - uu[s - 1] - uu[id - 1]) * 0.25;
-    double Div = (vv[s + 1] + vv[id + 1] - vv[s - 1] - vv[id - 1]) * 0.25;
-    double DiT = (TT[s + 1] + TT[id + 1] - TT[s - 1] - TT[id - 1]) * 0.25;
-    double Dju = uu[id] - uu[s], Djv = vv[id] - vv[s], DjT = TT[id] - TT[s];
-    double u1 = (uu[id] + uu[s]) * 0.5, v1 = (vv[id] + vv[s]) * 0.5;
+    T Dix = ((T)x1[s + 1] + (T)x1[id + 1] - (T)x1[s - 1] - (T)x1[id - 1]) * T(0.25);
+    T Diy = ((T)y1[s + 1] + (T)y1[id + 1] - (T)y1[s - 1] - (T)y1[id - 1]) * T(0.25);
+    T Djx = (T)x1[id] - (T)x1[s], Djy = (T)y1[id] - (T)y1[s];
+    T Diu = ((T)uu[s + 1] + (T)uu[id + 1] - (T)uu[s - 1] - (T)uu[id - 1]) * T(0.25);
+    T Div = ((T)vv[s + 1] + (T)vv[id + 1] - (T)vv[s - 1] - (T)vv[id - 1]) * T(0.25);
+    T DiT = ((T)TT[s + 1] + (T)TT[id + 1] - (T)TT[s - 1] - (T)TT[id - 1]) * T(0.25);
+    T Dju = (T)uu[id] - (T)uu[s], Djv = (T)vv[id] - (T)vv[s], DjT = (T)TT[id] - (T)TT[s];
+    T u1 = ((T)uu[id] + (T)uu[s]) * T(0.5), v1 = ((T)vv[id] + (T)vv[s]) * T(0.5);
     viscous_face(Dix, Diy, Djx, Djy, Diu, Div, DiT, Dju, Djv, DjT, Amu1, Amk1, u1, v1, n1, n2, sj, F1, F2, F3);
   }
   L.fj[id] = F0; L.fj[F + id] = F1; L.fj[2 * F + id] = F2; L.fj[3 * F + id] = F3;
@@ -325,8 +327,14 @@ __global__ void k_norm_final(Lvl L, const int *case_tile0, const int *case_ntile
 }
 
 void launch_prim(const Lvl &L, cudaStream_t s) { k_prim<<<L.ntiles, TILE, 0, s>>>(L); }
-void launch_flux_i(const Lvl &L, cudaStream_t s) { k_flux_i<<<L.ntiles, TILE, 0, s>>>(L); }
-void launch_flux_j(const Lvl &L, cudaStream_t s) { k_flux_j<<<L.ntiles, TILE, 0, s>>>(L); }
+void launch_flux_i(const Lvl &L, bool fp32, cudaStream_t s) {
+  if (fp32) k_flux_i<float><<<L.ntiles, TILE, 0, s>>>(L);
+  else k_flux_i<double><<<L.ntiles, TILE, 0, s>>>(L);
+}
+void launch_flux_j(const Lvl &L, bool fp32, cudaStream_t s) {
+  if (fp32) k_flux_j<float><<<L.ntiles, TILE, 0, s>>>(L);
+  else k_flux_j<double><<<L.ntiles, TILE, 0, s>>>(L);
+}
 void launch_res(const Lvl &L, bool with_norms, cudaStream_t s) {
   if (with_norms) k_res<true><<<L.ntiles, TILE, 0, s>>>(L);
   else k_res<false><<<L.ntiles, TILE, 0, s>>>(L);

@@ -114,6 +114,7 @@ def lib():
         "ec2d_kernel_times": ([vp, ctypes.c_char_p, ctypes.c_int], ctypes.c_int),
         "ec2d_set_graphs": ([vp, ctypes.c_int], ctypes.c_int),
         "ec2d_set_lusgs_precision": ([vp, ctypes.c_int], ctypes.c_int),
+        "ec2d_set_coarse_precision": ([vp, ctypes.c_int], ctypes.c_int),
         "ec2d_run_to_drop": ([vp, ctypes.c_double, dp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ip, dp, dp],
                              ctypes.c_int),
         "ec2d_set_case_shape": ([vp, ctypes.c_int, ctypes.c_double], ctypes.c_int),
@@ -328,6 +329,10 @@ class Solver:
     def set_case_shape(self, case, shape):
         """Per-case shape feature of the warm-start network (the airfoil t/c)."""
         _ck(self.L.ec2d_set_case_shape(self.h, case, float(shape)), "ec2d_set_case_shape")
+
+    def set_coarse_precision(self, bits):
+        """64 (default) or 32: arithmetic of the coarse multigrid levels' face fluxes."""
+        _ck(self.L.ec2d_set_coarse_precision(self.h, int(bits)), "ec2d_set_coarse_precision")
 
     def set_lusgs_precision(self, bits):
         """64 (default) or 32: arithmetic of the LU-SGS sweeps on every level."""
