@@ -369,6 +369,22 @@ def leg_learned(args):
             "generate": gen, "train": tr, "evaluate": ev}
 
 
+def reduce_max(dist, x: float, device: str) -> float:
+    """The slowest rank's time: every rank of a replica run gets the maximum
+    of x over all ranks (x itself without a process group)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(units_per_rank: float, steps: int, world: int, ms: float) -> float:
+    """Whole-job rate: all ranks' units x steps over the slowest rank's time."""
+    return units_per_rank * steps * world / (ms / 1e3)
+
+
 def run_gb300(args, rank, world):
     import torch
     from ec2d import gpu
@@ -398,11 +414,7 @@ def run_gb300(args, rank, world):
         torch.cuda.synchronize()
 
     def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], device=f"cuda:{dev}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return reduce_max(dist, x, f"cuda:{dev}")
 
     # ---- device-timed region: K V-cycles (FP64), L2 flushed before each -----
     barrier()
@@ -411,7 +423,7 @@ def run_gb300(args, rank, world):
     barrier()
     clocks = clk.summary()
     ms = max_over_ranks(ms)
-    value = cells * args.steps * world / (ms / 1e3)
+    value = aggregate_rate(cells, args.steps, world, ms)
 
     # ---- per-kernel event timing (same K cycles, separate pass) -------------
     kt = kernel_table(g, torch, flush, args.steps)
