@@ -295,6 +295,7 @@ void fdm_metrics(HLevelBlock &B) {
 CaseDev make_casedev(const ec2d_params &p) {
   CaseDev c{};
   c.gamma = p.gamma; c.Ma = p.Ma; c.Re = p.Re; c.Pr = p.Pr;
+  c.rPr = 1.0 / p.Pr;
   c.Cv = 1.0 / (p.gamma * (p.gamma - 1.0) * p.Ma * p.Ma);
   c.Cp = c.Cv * p.gamma;
   double aoa = p.AoA * PI / 180.0;

@@ -58,6 +58,7 @@ struct CaseDev {
   double gamma, Ma, Re, Pr, Cv, Cp, cosA, sinA, p00, Tsb, Twall, p_outlet;
   double vt_inf, Kt_inf, Wt_inf, CFL, dtmax, dtmin, dt_global, T_inf;
   double xaxis, yaxis;
+  double rPr;               // 1 / Pr
   int local_dt, pad;
 };
 
@@ -86,6 +87,26 @@ struct Lvl {
 __host__ __device__ __forceinline__ long long fidx(const BlkDev &b, int i, int j) {
   return b.off + (long long)(j + 2) * b.P + (i + 2);
 }
+
+// Reciprocal on the face and wavefront paths.  FP64: the hardware's
+// approximate reciprocal refined by two Newton-Raphson steps
+// r <- r + r (1 - x r), each squaring the relative error (on 2^20 samples in
+// [0.05, 20] it equals the rounded quotient 1/x), about half the dependent
+// FP64 operations of a divide; a / b becomes a * rcp(b), within an ulp of the
+// quotient.  FP32: the division.
+template <typename T>
+__device__ __forceinline__ T rcp(T x);
+template <>
+__device__ __forceinline__ double rcp<double>(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
+}
+template <>
+__device__ __forceinline__ float rcp<float>(float x) { return 1.0f / x; }
 
 // The face physics below is written once for the arithmetic type T: double
 // is the reference's arithmetic (every literal T(x) is then the same double
@@ -117,7 +138,7 @@ __device__ __forceinline__ T scheme_fp(T u1, T u2, T u3, T u4, int flag) {
       return u2 + T(0.25) * ((T(1.0) - T(1.0)) * minmod(u2 - u1, T(2.0) * (u3 - u2)) + (T(1.0) + T(1.0)) * minmod(u3 - u2, T(2.0) * (u2 - u1)));
     case Scheme_MUSCL3: {
       T up = u3 - u2, um = u2 - u1;
-      T s = (T(2.0) * up * um + ep) / (up * up + um * um + ep);
+      T s = (T(2.0) * up * um + ep) * rcp(up * up + um * um + ep);
       return u2 + T(0.25) * s * ((T(1.0) - k3 * s) * um + (T(1.0) + k3 * s) * up);
     }
     case Scheme_OMUSCL2: {
@@ -150,7 +171,7 @@ __device__ __forceinline__ T scheme_fm(T u1, T u2, T u3, T u4, int flag) {
     }
     case Scheme_MUSCL3: {
       T up = u4 - u3, um = u3 - u2;
-      T s = (T(2.0) * up * um + ep) / (up * up + um * um + ep);
+      T s = (T(2.0) * up * um + ep) * rcp(up * up + um * um + ep);
       return u3 - T(0.25) * s * ((T(1.0) - k3 * s) * up + (T(1.0) + k3 * s) * um);
     }
     case Scheme_OMUSCL2: {
@@ -246,12 +267,13 @@ __device__ __forceinline__ void flux_roe(const T *QL, const T *QR, T *F, T gamma
   T dl = QL[0], uul = QL[1], vvl = QL[2], pl = QL[3];
   T dr = QR[0], uur = QR[1], vvr = QR[2], pr = QR[3];
   T gm1 = gamma - T(1.0);
-  T hl = gamma * pl / (gm1 * dl) + T(0.5) * (uul * uul + vvl * vvl);
-  T hr = gamma * pr / (gm1 * dr) + T(0.5) * (uur * uur + vvr * vvr);
+  const T rdl = rcp(dl), rdr = rcp(dr), ggm1 = gamma * rcp(gm1);
+  T hl = ggm1 * pl * rdl + T(0.5) * (uul * uul + vvl * vvl);
+  T hr = ggm1 * pr * rdr + T(0.5) * (uur * uur + vvr * vvr);
   T Fl0 = dl * uul, Fl1 = dl * uul * uul + pl, Fl2 = dl * uul * vvl, Fl3 = uul * dl * hl;
   T Fr0 = dr * uur, Fr1 = dr * uur * uur + pr, Fr2 = dr * uur * vvr, Fr3 = uur * dr * hr;
-  T tmpp = sqrt(dr / dl);
-  T inv = T(1.0) / (T(1.0) + tmpp);
+  T tmpp = sqrt(dr * rdl);
+  T inv = rcp(T(1.0) + tmpp);
   T avd = T(0.25) * dl * (T(1.0) + tmpp) * (T(1.0) + tmpp);
   T avu = (uul + tmpp * uur) * inv;
   T avv = (vvl + tmpp * vvr) * inv;
@@ -263,7 +285,7 @@ __device__ __forceinline__ void flux_roe(const T *QL, const T *QR, T *F, T gamma
   if (l1 < delt) l1 = (l1 * l1 + delt * delt) * i2d;
   T l2 = l1;
   if (l3 < delt) l3 = (l3 * l3 + delt * delt) * i2d;
-  T ia = T(1.0) / ava;
+  T ia = rcp(ava);
   T i2aa = T(0.5) * ia * ia;
   T dp = pr - pl;
   T a0 = (avd * ava * (-uur + uul) + dp) * i2aa;
@@ -283,11 +305,12 @@ __device__ __forceinline__ void flux_ausm(const T *QL, const T *QR, T *F, T gamm
   T dl = QL[0], uul = QL[1], vvl = QL[2], pl = QL[3];
   T dr = QR[0], uur = QR[1], vvr = QR[2], pr = QR[3];
   T gm1 = gamma - T(1.0);
-  T hl = gamma * pl / (gm1 * dl) + T(0.5) * (uul * uul + vvl * vvl);
-  T hr = gamma * pr / (gm1 * dr) + T(0.5) * (uur * uur + vvr * vvr);
-  T al = sqrt(gamma * pl / dl), ar = sqrt(gamma * pr / dr);
+  const T rdl = rcp(dl), rdr = rcp(dr), ggm1 = gamma * rcp(gm1);
+  T hl = ggm1 * pl * rdl + T(0.5) * (uul * uul + vvl * vvl);
+  T hr = ggm1 * pr * rdr + T(0.5) * (uur * uur + vvr * vvr);
+  T al = sqrt(gamma * pl * rdl), ar = sqrt(gamma * pr * rdr);
   T a = T(0.5) * (al + ar);
-  T ia = T(1.0) / a;
+  T ia = rcp(a);
   T Ml = uul * ia, Mr = uur * ia;
   T Mp4, Mm4, Pp5, Pm5;
   T ml2 = Ml * Ml - T(1.0), mr2 = Mr * Mr - T(1.0);
@@ -427,7 +450,7 @@ __device__ __forceinline__ void viscous_face(T Dix, T Diy, T Djx, T Djy, T Diu, 
                                              T DiT, T Dju, T Djv, T DjT, T Amu1, T Amk1,
                                              T u1, T v1, T n1, T n2, T s, T &F2,
                                              T &F3, T &F4) {
-  T Ds = T(1.0) / (Dix * Djy - Djx * Diy);
+  T Ds = rcp(Dix * Djy - Djx * Diy);
   T ux = (Diu * Djy - Dju * Diy) * Ds, vx = (Div * Djy - Djv * Diy) * Ds, Tx = (DiT * Djy - DjT * Diy) * Ds;
   T uy = (-Diu * Djx + Dju * Dix) * Ds, vy = (-Div * Djx + Djv * Dix) * Ds, Ty = (-DiT * Djx + DjT * Dix) * Ds;
   T t11 = ((T(4.0) / T(3.0)) * ux - (T(2.0) / T(3.0)) * vy) * Amu1;

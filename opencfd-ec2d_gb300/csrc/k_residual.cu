@@ -99,13 +99,13 @@ __global__ void __launch_bounds__(TILE) k_flux_i(Lvl L) {
     T Amu1, Amk1;
     if (i == 1) {
       Amu1 = (T)L.amu[id] + (T)L.amut[id];
-      Amk1 = (T)c.Cp * ((T)L.amu[id] / (T)c.Pr + (T)L.amut[id] / (T)PrT);
+      Amk1 = (T)c.Cp * ((T)L.amu[id] * (T)c.rPr + (T)L.amut[id] * (T)(1.0 / PrT));
     } else if (i == b.nx) {
       Amu1 = (T)L.amu[w] + (T)L.amut[w];
-      Amk1 = (T)c.Cp * ((T)L.amu[w] / (T)c.Pr + (T)L.amut[w] / (T)PrT);
+      Amk1 = (T)c.Cp * ((T)L.amu[w] * (T)c.rPr + (T)L.amut[w] * (T)(1.0 / PrT));
     } else {
       Amu1 = ((T)L.amu[w] + (T)L.amu[id] + (T)L.amut[w] + (T)L.amut[id]) * T(0.5);
-      Amk1 = (T)c.Cp * (((T)L.amu[w] + (T)L.amu[id]) / (T)c.Pr + ((T)L.amut[w] + (T)L.amut[id]) / (T)PrT) * T(0.5);
+      Amk1 = (T)c.Cp * (((T)L.amu[w] + (T)L.amu[id]) * (T)c.rPr + ((T)L.amut[w] + (T)L.amut[id]) * (T)(1.0 / PrT)) * T(0.5);
     }
     const double *x1 = L.geo + G_X1 * F, *y1 = L.geo + G_Y1 * F;
     const double *uu = L.q + Q_U * F, *vv = L.q + Q_V * F, *TT = L.q + Q_T * F;
@@ -163,13 +163,13 @@ __global__ void __launch_bounds__(TILE) k_flux_j(Lvl L) {
     T Amu1, Amk1;
     if (j == 1) {
       Amu1 = (T)L.amu[id] + (T)L.amut[id];
-      Amk1 = (T)c.Cp * ((T)L.amu[id] / (T)c.Pr + (T)L.amut[id] / (T)PrT);
+      Amk1 = (T)c.Cp * ((T)L.amu[id] * (T)c.rPr + (T)L.amut[id] * (T)(1.0 / PrT));
     } else if (j == b.ny) {
       Amu1 = (T)L.amu[s] + (T)L.amut[s];
-      Amk1 = (T)c.Cp * ((T)L.amu[s] / (T)c.Pr + (T)L.amut[s] / (T)PrT);
+      Amk1 = (T)c.Cp * ((T)L.amu[s] * (T)c.rPr + (T)L.amut[s] * (T)(1.0 / PrT));
     } else {
       Amu1 = ((T)L.amu[id] + (T)L.amu[s] + (T)L.amut[id] + (T)L.amut[s]) * T(0.5);
-      Amk1 = (T)c.Cp * (((T)L.amu[s] + (T)L.amu[id]) / (T)c.Pr + ((T)L.amut[s] + (T)L.amut[id]) / (T)PrT) * T(0.5);
+      Amk1 = (T)c.Cp * (((T)L.amu[s] + (T)L.amu[id]) * (T)c.rPr + ((T)L.amut[s] + (T)L.amut[id]) * (T)(1.0 / PrT)) * T(0.5);
     }
     const double *x1 = L.geo + G_X1 * F, *y1 = L.geo + G_Y1 * F;
     const double *uu = L.q + Q_U * F, *vv = L.q + Q_V * F, *TT = L.q + Q_T * F;

@@ -166,20 +166,6 @@ __global__ void __launch_bounds__(TILE) k_lusgs_prep(Lvl L, double alfa1) {
   }
 }
 
-// 1/x on the wavefront's critical path: the hardware's approximate FP64
-// reciprocal refined by two Newton-Raphson steps r <- r + r (1 - x r) (each
-// squares the relative error); on 2^20 samples in [0.05, 20] it equals the
-// rounded quotient, with about half the dependent FP64 operations of a
-// full-precision divide
-__device__ __forceinline__ double rcp_nr(double x) {
-  double r;
-  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
-  double e = fma(-x, r, 1.0);
-  r = fma(r, e, r);
-  e = fma(-x, r, 1.0);
-  return fma(r, e, r);
-}
-
 __device__ __forceinline__ unsigned cluster_rank() {
   unsigned r;
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
@@ -283,7 +269,7 @@ __global__ void __launch_bounds__(1024) k_lusgs_sweep(Lvl L, int update, int R, 
           st[m] = cur[RC::U + m] + d;
           st[SL::D + m] = d;
         }
-        st[SL::R] = rcp_nr(st[0]);
+        st[SL::R] = rcp(st[0]);
         st[SL::P] = gm1 * (st[3] - 0.5 * (st[1] * st[1] + st[2] * st[2]) * st[SL::R]);
         double2 *own = reinterpret_cast<double2 *>(sh + ((size_t)buf * (R + 2) + rl + 1) * S);
 #pragma unroll
