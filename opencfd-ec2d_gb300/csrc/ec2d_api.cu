@@ -296,7 +296,10 @@ CaseDev make_casedev(const ec2d_params &p) {
   CaseDev c{};
   c.gamma = p.gamma; c.Ma = p.Ma; c.Re = p.Re; c.Pr = p.Pr;
   c.rPr = 1.0 / p.Pr;
+  c.rMa = 1.0 / p.Ma;
+  c.rRe = 1.0 / p.Re;
   c.Cv = 1.0 / (p.gamma * (p.gamma - 1.0) * p.Ma * p.Ma);
+  c.rCv = p.gamma * (p.gamma - 1.0) * p.Ma * p.Ma;
   c.Cp = c.Cv * p.gamma;
   double aoa = p.AoA * PI / 180.0;
   c.cosA = 1.0 * std::cos(aoa); c.sinA = 1.0 * std::sin(aoa);

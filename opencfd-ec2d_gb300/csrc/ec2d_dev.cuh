@@ -58,7 +58,7 @@ struct CaseDev {
   double gamma, Ma, Re, Pr, Cv, Cp, cosA, sinA, p00, Tsb, Twall, p_outlet;
   double vt_inf, Kt_inf, Wt_inf, CFL, dtmax, dtmin, dt_global, T_inf;
   double xaxis, yaxis;
-  double rPr;               // 1 / Pr
+  double rPr, rCv, rMa, rRe;  // 1/Pr, 1/Cv, 1/Ma, 1/Re
   int local_dt, pad;
 };
 

@@ -37,8 +37,9 @@ __global__ void __launch_bounds__(TILE) k_prim(Lvl L) {
   long long id = fidx(b, i, j);
   const long long F = L.F;
   double d = L.U[id], ru = L.U[F + id], rv = L.U[2 * F + id], E = L.U[3 * F + id];
-  double uu = ru / d, v = rv / d;
-  double T = (E - 0.5 * d * (uu * uu + v * v)) / (c.Cv * d);
+  const double rd = rcp(d);
+  double uu = ru * rd, v = rv * rd;
+  double T = (E - 0.5 * d * (uu * uu + v * v)) * (rd * c.rCv);
   double p = c.p00 * d * T;
   L.q[Q_D * F + id] = d;
   L.q[Q_U * F + id] = uu;
@@ -48,11 +49,11 @@ __global__ void __launch_bounds__(TILE) k_prim(Lvl L) {
   bool interior = (i >= 1 && i <= b.nx - 1 && j >= 1 && j <= b.ny - 1);
   if (interior) {
     if (!(T >= 1.0e-5)) set_status(L.status + 4 * b.cas, 3, bk, i, j);
-    L.q[Q_C * F + id] = sqrt(T) / c.Ma;
+    L.q[Q_C * F + id] = sqrt(T) * c.rMa;
   }
   if (L.visc) {
     if (i >= 0 && i <= b.nx && j >= 0 && j <= b.ny)
-      L.amu[id] = 1.0 / c.Re * (1.0 + c.Tsb) * sqrt(T * T * T) / (c.Tsb + T);
+      L.amu[id] = c.rRe * (1.0 + c.Tsb) * sqrt(T * T * T) * rcp(c.Tsb + T);
     L.amut[id] = 0.0;
   }
 }
@@ -230,8 +231,9 @@ __global__ void __launch_bounds__(TILE) k_res(Lvl L) {
     double uni = uu * ni1 + vv * ni2, unj = uu * nj1 + vv * nj2;
     double Lci = (fabs(uni) + cc) * si, Lcj = (fabs(unj) + cc) * sj;
     double amu = L.visc ? L.amu[id] : 0.0, amut = L.visc ? L.amut[id] : 0.0;
-    double tmp1 = c.gamma / d * (amu / c.Pr + amut / PrT);
-    double Lvi = tmp1 * si * si / s0, Lvj = tmp1 * sj * sj / s0;
+    const double rs0 = rcp(s0);
+    double tmp1 = c.gamma * rcp(d) * (amu * c.rPr + amut * (1.0 / PrT));
+    double Lvi = tmp1 * si * si * rs0, Lvj = tmp1 * sj * sj * rs0;
     L.lc[L_CI * F + id] = Lci;
     L.lc[L_CJ * F + id] = Lcj;
     L.lc[L_VI * F + id] = Lvi;
@@ -239,7 +241,7 @@ __global__ void __launch_bounds__(TILE) k_res(Lvl L) {
     double dt;
     if (c.local_dt == 0) dt = c.dt_global;
     else {
-      dt = c.CFL * s0 / (Lci + Lcj + 1.0 * (Lvi + Lvj));
+      dt = c.CFL * s0 * rcp(Lci + Lcj + 1.0 * (Lvi + Lvj));
       if (dt > c.dtmax) dt = c.dtmax;
       if (dt < c.dtmin) dt = c.dtmin;
     }

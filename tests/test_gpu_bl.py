@@ -6,9 +6,11 @@ same channel with the index directions swapped (walls on faces 1 and 3), the
 C-grid airfoil (partial wall on face 2, two blocks) and the flat plate (wall
 and symmetry floor in different blocks).  Two wall subfaces in one block
 exercise the minimum taken where a second wall's lines cross cells set by the
-first.  Amu_t must match to 1e-12 relative (the model's branches are discrete,
-so a mismatch shows up as an O(1) jump, not as round-off), and the residual
-to the standard 1e-12 face-flux-scaled bound."""
+first.  Amu_t must match to 1e-10 relative (the model's branches are discrete,
+so a mismatch shows up as an O(1) jump, not as round-off; the primitives come
+from a Newton-refined reciprocal of the density, an ulp or two from the
+oracle's divide, and the F_max search and the Klebanoff factor carry that to
+about 1e-11), and the residual to the standard 1e-12 face-flux-scaled bound."""
 import numpy as np
 import pytest
 
@@ -61,7 +63,7 @@ def _check(p, blocks, steps=4, seed=3):
     copy_state(orc, g)
     orc.residual(); g.residual()
     compare_fields(orc, g, [AMU], tol=1e-13)
-    compare_fields(orc, g, [AMUT], tol=1e-12)
+    compare_fields(orc, g, [AMUT], tol=1e-10)
     compare_residual(orc, g)
     return orc, g
 

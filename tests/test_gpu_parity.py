@@ -82,7 +82,11 @@ def test_residual_sst(gpu_lib):
     orc, g = _pair(p, bl, steps=5)
     orc.residual(); g.residual()
     compare_residual(orc, g)
-    compare_fields(orc, g, [1, 2, 3, 4, 5, 7, 8])
+    compare_fields(orc, g, [1, 2, 3, 7])
+    # mu_t from k, omega, the blending F2 and the vorticity limiter: the
+    # primitives' last-ulp differences (reciprocal-multiply against the
+    # oracle's divides) grow to ~1e-11 there, and to ~1e-12 in Lv = f(mu_t)
+    compare_fields(orc, g, [4, 5, 8], tol=1e-10)
 
 
 @pytest.mark.parametrize("visc", [0, 1])
