@@ -16,11 +16,18 @@
 //                 with cp.async while it computes the current cell, takes the
 //                 own row's previous cell from registers and the neighbouring
 //                 row from a double-buffered shared slot, and adds
-//                 F_n(U_nb + dU_nb, s) and (0.5 Lc + Lv) dU_nb to the record's
-//                 constant term before the 1/alfa scaling (the same sum as
-//                 the reference, F_n being linear in the normal).
-// The producer of a state also ships 1/rho and p of U + dU, so each of its two
-// consumers needs no division.  The backward sweep writes U + dU (the update
+//                 F_n(U_nb + dU_nb, s) + (0.5 Lc + Lv) (U_nb + dU_nb) to the
+//                 record's constant term before the 1/alfa scaling (the same
+//                 sum as the reference: F_n is linear in the normal, and the
+//                 -(0.5 Lc + Lv) U_nb half of the dissipation term is constant
+//                 too, so it sits in the record beside -F_n(U_nb, s)).
+// The producer of a state also ships u, v and p of U + dU, so each of its two
+// consumers needs no division, and the flux plus dissipation of one neighbour
+// folds into seven FMAs: with un = u n1 + v n2 and w = un + cc,
+//   rho w,  rho u w + p n1,  rho v w + p n2,  E w + p un  (+ U_m w).
+// The FP64 pipe issues one warp instruction per 64 cycles per sub-partition on
+// this part, so the operation count per cell, not the dependency depth, sets
+// the time per plane.  The backward sweep writes U + dU (the update
 // of NS_Time_advance_LU_SGS, sub_NS_singlegrid.f90:203-211): a neighbour needs
 // U_old + dU_final of this cell, which is exactly the new U, and F_n(U_old)
 // was taken in the pre-pass before any U changed.
@@ -34,10 +41,11 @@ namespace ec2d {
 constexpr int TILE = 256;
 
 // record layout (doubles), identical for both passes:
-//  A    forward: Res - F_n(U_i-nb, s_i) - F_n(U_j-nb, s_j); backward: the
-//       forward dU (written by the forward sweep)
+//  A    forward: Res + K; backward: the forward dU, or U + dU when the sweep
+//       updates U (written by the forward sweep); K = -sum over the upstream
+//       neighbours of F_n(U_nb, s) + cc U_nb
 //  U    U_old of the cell
-//  C0   backward only: -F_n(U_i-nb, s_i) - F_n(U_j-nb, s_j)
+//  C0   backward only: K of the downstream neighbours
 //  CI, CJ  0.5 Lc_nb (+ Lv_nb when viscous)
 //  IA, IA5 1/alfa and, for the SA row, 1/(alfa + Lvi + Lvj)
 //  N1I..N2J  scaled normals s = +-0.5 (face length) n of face i and face j:
@@ -51,10 +59,10 @@ struct Rec {
   static_assert(N % 2 == 0, "records are whole 16-byte units");
 };
 
-// state shipped between neighbours: U2 = U + dU, 1/rho2, p2, dU
+// state shipped between neighbours: U2 = U + dU, then u2, v2, p2
 template <int NV>
 struct Slot {
-  static constexpr int R = NV, P = NV + 1, D = NV + 2, S = 2 * NV + 2;
+  static constexpr int U = NV, V = NV + 1, P = NV + 2, S = (NV + 3 + 1) / 2 * 2;
   static_assert(S % 2 == 0, "slots are whole 16-byte units");
 };
 
@@ -75,18 +83,20 @@ __device__ __forceinline__ void fn(const double *U, double n1, double n2, double
   for (int m = 4; m < NV; m++) Fo[m] = U[m] * un;
 }
 
-// the same from a shipped state (1/rho and p precomputed by the producer)
+// acc += F_n(U2, s) + cc U2 from a shipped state (u, v, p of U2 precomputed
+// by the producer)
 template <int NV>
-__device__ __forceinline__ void fn_shipped(const double *st, double n1, double n2, double *Fo) {
+__device__ __forceinline__ void add_shipped(const double *st, double n1, double n2, double cc, double *acc) {
   using SL = Slot<NV>;
-  double un = (st[1] * n1 + st[2] * n2) * st[SL::R];
-  double p = st[SL::P];
-  Fo[0] = st[0] * un;
-  Fo[1] = st[1] * un + p * n1;
-  Fo[2] = st[2] * un + p * n2;
-  Fo[3] = (st[3] + p) * un;
+  const double p = st[SL::P];
+  const double un = fma(st[SL::U], n1, st[SL::V] * n2);
+  const double w = un + cc;
+  acc[0] = fma(st[0], w, acc[0]);
+  acc[1] = fma(st[1], w, fma(p, n1, acc[1]));
+  acc[2] = fma(st[2], w, fma(p, n2, acc[2]));
+  acc[3] = fma(st[3], w, fma(p, un, acc[3]));
 #pragma unroll
-  for (int m = 4; m < NV; m++) Fo[m] = st[m] * un;
+  for (int m = 4; m < NV; m++) acc[m] = fma(st[m], w, acc[m]);
 }
 
 template <int NV>
@@ -150,7 +160,7 @@ __global__ void __launch_bounds__(TILE) k_lusgs_prep(Lvl L, double alfa1) {
         s2 = hh * (dir == 0 ? ni2 : nj2);
         fn<NV>(Un, s1, s2, gm1, Fo);
 #pragma unroll
-        for (int m = 0; m < NV; m++) K[pass][m] -= Fo[m];
+        for (int m = 0; m < NV; m++) K[pass][m] -= fma(cc, Un[m], Fo[m]);
       }
       r[dir == 0 ? RC::CI : RC::CJ] = cc;
       r[dir == 0 ? RC::N1I : RC::N1J] = s1;
@@ -201,8 +211,8 @@ __device__ __forceinline__ void fetch(double *dst, const double *src) {
 // CS > 1: a cluster of CS CTAs per block, CTA r owns rows r*R+1..r*R+R; the
 // edge rows write into the neighbour CTA's halo slot through distributed
 // shared memory and planes are separated by a cluster barrier.
-template <int NV>
-__global__ void __launch_bounds__(1024) k_lusgs_sweep(Lvl L, int update, int R, int CS, int RPW) {
+template <int NV, bool update>
+__global__ void __launch_bounds__(1024) k_lusgs_sweep(Lvl L, int R, int CS, int RPW) {
   using SL = Slot<NV>;
   using RC = Rec<NV>;
   constexpr int S = SL::S;
@@ -242,35 +252,34 @@ __global__ void __launch_bounds__(1024) k_lusgs_sweep(Lvl L, int update, int R, 
         if (inx >= 1 && inx <= ni) fetch<NV>(rec + ((k + 1) & 1) * RC::N, rsrc + (size_t)(inx - 1) * RC::N);
         cp_commit();
         cp_wait1();
-        double acc[NV], F2[NV];
+        double acc[NV], dn[NV];
 #pragma unroll
         for (int m = 0; m < NV; m++) acc[m] = fwd ? cur[RC::A + m] : cur[RC::C0 + m];
-        if (fwd ? (i > 1) : (i < ni)) {
-          fn_shipped<NV>(st, cur[RC::N1I], cur[RC::N2I], F2);
-          const double cc = cur[RC::CI];
-#pragma unroll
-          for (int m = 0; m < NV; m++) acc[m] = fma(cc, st[SL::D + m], acc[m] + F2[m]);
-        }
+        if (fwd ? (i > 1) : (i < ni)) add_shipped<NV>(st, cur[RC::N1I], cur[RC::N2I], cur[RC::CI], acc);
         if (fwd ? (j > 1) : (j < rows)) {
           const double2 *s2 = reinterpret_cast<const double2 *>(sh + ((size_t)(buf ^ 1) * (R + 2) + (fwd ? rl : rl + 2)) * S);
           double sn[S];
 #pragma unroll
           for (int m = 0; m < S / 2; m++) { double2 v = s2[m]; sn[2 * m] = v.x; sn[2 * m + 1] = v.y; }
-          fn_shipped<NV>(sn, cur[RC::N1J], cur[RC::N2J], F2);
-          const double cc = cur[RC::CJ];
-#pragma unroll
-          for (int m = 0; m < NV; m++) acc[m] = fma(cc, sn[SL::D + m], acc[m] + F2[m]);
+          add_shipped<NV>(sn, cur[RC::N1J], cur[RC::N2J], cur[RC::CJ], acc);
         }
         const double ia = cur[RC::IA], ia5 = cur[RC::IA5];
 #pragma unroll
         for (int m = 0; m < NV; m++) {
           double inv = (NV == 5 && m == 4) ? ia5 : ia;
-          double d = fwd ? acc[m] * inv : cur[RC::A + m] + acc[m] * inv;
-          st[m] = cur[RC::U + m] + d;
-          st[SL::D + m] = d;
+          if (update) {
+            // fused: U + dU* in one fma going forward, carried in the backward
+            // record, and U + dU* + dU** in one fma going backward
+            st[m] = fma(acc[m], inv, fwd ? cur[RC::U + m] : cur[RC::A + m]);
+          } else {
+            dn[m] = fwd ? acc[m] * inv : fma(acc[m], inv, cur[RC::A + m]);
+            st[m] = cur[RC::U + m] + dn[m];
+          }
         }
-        st[SL::R] = rcp(st[0]);
-        st[SL::P] = gm1 * (st[3] - 0.5 * (st[1] * st[1] + st[2] * st[2]) * st[SL::R]);
+        const double rd = rcp(st[0]);
+        st[SL::U] = st[1] * rd;
+        st[SL::V] = st[2] * rd;
+        st[SL::P] = gm1 * fma(-0.5, fma(st[2], st[SL::V], st[1] * st[SL::U]), st[3]);
         double2 *own = reinterpret_cast<double2 *>(sh + ((size_t)buf * (R + 2) + rl + 1) * S);
 #pragma unroll
         for (int m = 0; m < S / 2; m++) own[m] = make_double2(st[2 * m], st[2 * m + 1]);
@@ -290,12 +299,12 @@ __global__ void __launch_bounds__(1024) k_lusgs_sweep(Lvl L, int update, int R, 
           // the forward dU becomes the A field of this cell's backward record
           double *w = recBw + (size_t)(i - 1) * RC::N;
 #pragma unroll
-          for (int m = 0; m < NV; m++) w[RC::A + m] = st[SL::D + m];
+          for (int m = 0; m < NV; m++) w[RC::A + m] = update ? st[m] : dn[m];
         } else {
           const long long id = off + (long long)(j + 2) * P + (i + 2);
 #pragma unroll
           for (int m = 0; m < NV; m++) {
-            L.du[m * F + id] = st[SL::D + m];
+            L.du[m * F + id] = update ? st[m] - cur[RC::U + m] : dn[m];
             if (update) L.U[m * F + id] = st[m];
           }
         }
@@ -321,8 +330,8 @@ void sweep_nv(const Lvl &L, double alfa1, int update, int max_rows, int cs, int 
     th = ((R + 31) / 32) * 32;
     smem = ((size_t)2 * (R + 2) * Slot<NV>::S + (size_t)th * 2 * Rec<NV>::N) * sizeof(double);
   }
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(k_lusgs_sweep<NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  auto kern = update ? k_lusgs_sweep<NV, true> : k_lusgs_sweep<NV, false>;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(L.nblk * CS);
   cfg.blockDim = dim3(th);
@@ -335,7 +344,7 @@ void sweep_nv(const Lvl &L, double alfa1, int update, int max_rows, int cs, int 
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, k_lusgs_sweep<NV>, L, update, R, CS, rpw);
+  cudaLaunchKernelEx(&cfg, kern, L, R, CS, rpw);
 }
 
 template <int NV>

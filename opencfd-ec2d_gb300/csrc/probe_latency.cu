@@ -5,7 +5,9 @@
 // floor of the per-plane cost of the LU-SGS wavefront sweep, whose critical
 // path is a chain of dependent arithmetic plus one barrier per plane.
 // Build and run: nvcc -gencode arch=compute_103a,code=sm_103a -O3 -o lat probe_latency.cu && ./lat
+#include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <cuda_runtime.h>
 __global__ void k_dfma(double *out, long long *cyc, double a, double b, int n) {
   double x = a + threadIdx.x;
@@ -61,6 +63,75 @@ __global__ void k_cluster(double *out, long long *cyc, double a, double b, int n
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   out[t] = a; cyc[t] = t1 - t0;
 }
+// ILP independent chains per thread: does one warp overlap independent FP64
+// instructions, or does each occupy the sub-partition for its full latency?
+template <int ILP>
+__global__ void k_dfma_ilp(double *out, long long *cyc, double a, double b, int n) {
+  double x[ILP];
+#pragma unroll
+  for (int q = 0; q < ILP; q++) x[q] = a + threadIdx.x + q;
+  long long t0 = clock64();
+  for (int k = 0; k < n; k++) {
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+#pragma unroll
+      for (int q = 0; q < ILP; q++) x[q] = fma(x[q], b, a);
+  }
+  long long t1 = clock64();
+  double s = 0.0;
+#pragma unroll
+  for (int q = 0; q < ILP; q++) s += x[q];
+  out[threadIdx.x] = s; cyc[threadIdx.x] = t1 - t0;
+}
+// the same with only `lanes` lanes of each warp active
+__global__ void k_dfma_lanes(double *out, long long *cyc, double a, double b, int n, int lanes) {
+  double x = a + threadIdx.x;
+  long long t0 = clock64();
+  if ((threadIdx.x & 31) < lanes)
+    for (int k = 0; k < n; k++) {
+#pragma unroll
+      for (int u = 0; u < 8; u++) x = fma(x, b, a);
+    }
+  long long t1 = clock64();
+  out[threadIdx.x] = x; cyc[threadIdx.x] = t1 - t0;
+}
+// largest |x * rcp.approx.ftz.f64(x) - 1| over mantissas in [1, 2) (exact
+// residual by fma), as the bit pattern of a non-negative double
+__global__ void k_rcp_err(unsigned long long *worst, int per_thread) {
+  unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double m = 0.0;
+  for (int k = 0; k < per_thread; k++) {
+    unsigned long long h = (t * per_thread + k) * 0x9E3779B97F4A7C15ull;
+    h ^= h >> 29;
+    double x = __longlong_as_double((long long)(0x3FF0000000000000ull | (h & 0x000FFFFFFFFFFFFFull)));
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    double e = fabs(fma(-x, r, 1.0));
+    m = e > m ? e : m;
+  }
+  atomicMax(worst, (unsigned long long)__double_as_longlong(m));
+}
+// largest distance in ulps between 1/x (IEEE divide) and the reciprocal used
+// by the solver kernels (approximate reciprocal + one third-order step), over
+// x = mantissa * 2^k, k in [-8, 8]
+__global__ void k_rcp3_ulps(unsigned long long *worst, int per_thread) {
+  unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long m = 0;
+  for (int k = 0; k < per_thread; k++) {
+    unsigned long long h = (t * per_thread + k) * 0xD1B54A32D192ED03ull;
+    h ^= h >> 31;
+    int ex = (int)((h >> 52) % 17) - 8;
+    double x = ldexp(__longlong_as_double((long long)(0x3FF0000000000000ull | (h & 0x000FFFFFFFFFFFFFull))), ex);
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    const double e = fma(-x, r, 1.0);
+    r = fma(r, fma(e, e, e), r);
+    long long d = __double_as_longlong(r) - __double_as_longlong(1.0 / x);
+    d = d < 0 ? -d : d;
+    m = d > m ? d : m;
+  }
+  atomicMax(worst, (unsigned long long)m);
+}
 int main() {
   const int n = 1000, T = 256;
   double *out; long long *cyc; long long h[T];
@@ -89,6 +160,41 @@ int main() {
     cudaDeviceSynchronize();
     cudaMemcpy(h, cyc, 8 * sizeof(long long), cudaMemcpyDeviceToHost);
     printf("cluster barrier cs=%d  cycles each = %.2f\n", cs, h[0] / (8.0 * n));
+  }
+  for (int warps : {1, 4}) {
+    k_dfma_ilp<2><<<1, 32 * warps>>>(out, cyc, 0.5, 0.999, n);
+    cudaMemcpy(h, cyc, 8 * sizeof(long long), cudaMemcpyDeviceToHost);
+    printf("dfma ILP2 warps=%d  cycles per instruction = %.2f\n", warps, h[0] / (16.0 * n));
+    k_dfma_ilp<4><<<1, 32 * warps>>>(out, cyc, 0.5, 0.999, n);
+    cudaMemcpy(h, cyc, 8 * sizeof(long long), cudaMemcpyDeviceToHost);
+    printf("dfma ILP4 warps=%d  cycles per instruction = %.2f\n", warps, h[0] / (32.0 * n));
+    k_dfma_ilp<8><<<1, 32 * warps>>>(out, cyc, 0.5, 0.999, n);
+    cudaMemcpy(h, cyc, 8 * sizeof(long long), cudaMemcpyDeviceToHost);
+    printf("dfma ILP8 warps=%d  cycles per instruction = %.2f\n", warps, h[0] / (64.0 * n));
+  }
+  for (int lanes : {1, 8, 16}) {
+    k_dfma_lanes<<<1, 32>>>(out, cyc, 0.5, 0.999, n, lanes);
+    cudaMemcpy(h, cyc, 8 * sizeof(long long), cudaMemcpyDeviceToHost);
+    printf("dfma lanes=%d  cycles/op = %.2f\n", lanes, h[0] / (8.0 * n));
+  }
+  {
+    unsigned long long *w, hw = 0;
+    cudaMalloc(&w, sizeof(unsigned long long));
+    cudaMemset(w, 0, sizeof(unsigned long long));
+    k_rcp_err<<<608, 256>>>(w, 256);  // 40 M mantissas
+    cudaMemcpy(&hw, w, sizeof(hw), cudaMemcpyDeviceToHost);
+    double e; memcpy(&e, &hw, sizeof(e));
+    printf("rcp.approx.ftz.f64 max relative error over 4.0e7 mantissas = %.3e (2^%.2f)\n", e, log2(e));
+    cudaFree(w);
+  }
+  {
+    unsigned long long *w, hw = 0;
+    cudaMalloc(&w, sizeof(unsigned long long));
+    cudaMemset(w, 0, sizeof(unsigned long long));
+    k_rcp3_ulps<<<608, 256>>>(w, 256);
+    cudaMemcpy(&hw, w, sizeof(hw), cudaMemcpyDeviceToHost);
+    printf("third-order reciprocal: max distance from 1/x over 4.0e7 samples = %llu ulp\n", hw);
+    cudaFree(w);
   }
   cudaError_t e = cudaDeviceSynchronize();
   printf("status %s\n", cudaGetErrorString(e));
