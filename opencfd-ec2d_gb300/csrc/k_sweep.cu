@@ -12,8 +12,8 @@
 //                 neighbours, folded into Res -- and packs them with U into
 //                 one 16-byte-aligned record per cell and pass;
 //   k_lusgs_sweep (one CTA or one thread-block cluster per block; thread j
-//                 owns row j) fetches the NEXT cell's record into shared memory
-//                 with cp.async while it computes the current cell, takes the
+//                 owns row j) loads the NEXT cell's record into registers
+//                 while it computes the current cell, takes the
 //                 own row's previous cell from registers and the neighbouring
 //                 row from a double-buffered shared slot, and adds
 //                 F_n(U_nb + dU_nb, s) + (0.5 Lc + Lv) (U_nb + dU_nb) to the
@@ -193,18 +193,139 @@ __device__ __forceinline__ unsigned remote_smem(const void *p, unsigned rank) {
 __device__ __forceinline__ void st_remote2(unsigned addr, double a, double b) {
   asm volatile("st.shared::cluster.v2.f64 [%0], {%1, %2};" ::"r"(addr), "d"(a), "d"(b) : "memory");
 }
-__device__ __forceinline__ void cp16(double *dst, const double *src) {
-  unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
-__device__ __forceinline__ void cp_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-
+// the fields of one record a row needs for its update, held in registers
 template <int NV>
-__device__ __forceinline__ void fetch(double *dst, const double *src) {
+struct Cur {
+  double a[NV], u[NV], c0[NV];
+  double ci, cj, ia, ia5, n1i, n2i, n1j, n2j;
+};
+// a record as it arrives from memory: the 16-byte pairs one pass needs, loaded
+// straight into registers (L2 only: the backward records are written by the
+// forward pass of the same kernel)
+template <int NV>
+struct Raw {
+  double2 v[Rec<NV>::N / 2];
+};
+template <int NV, bool FWD>
+__device__ __forceinline__ constexpr bool pair_used(int q) {
+  // the forward pass does not read C0
+  return !FWD ? true : !(2 * q >= Rec<NV>::C0 && 2 * q + 1 < Rec<NV>::CI);
+}
+template <int NV, bool FWD>
+__device__ __forceinline__ void load_raw(Raw<NV> &r, const double *src) {
+  const double2 *s2 = reinterpret_cast<const double2 *>(src);
 #pragma unroll
-  for (int k = 0; k < Rec<NV>::N; k += 2) cp16(dst + k, src + k);
+  for (int q = 0; q < Rec<NV>::N / 2; q++)
+    if (pair_used<NV, FWD>(q)) r.v[q] = __ldcg(s2 + q);
+}
+template <int NV>
+__device__ __forceinline__ double field(const Raw<NV> &r, int k) { return (k & 1) ? r.v[k >> 1].y : r.v[k >> 1].x; }
+template <int NV, bool FWD>
+__device__ __forceinline__ void unpack(Cur<NV> &c, const Raw<NV> &r) {
+  using RC = Rec<NV>;
+#pragma unroll
+  for (int m = 0; m < NV; m++) {
+    c.a[m] = field(r, RC::A + m);
+    c.u[m] = field(r, RC::U + m);
+    if (!FWD) c.c0[m] = field(r, RC::C0 + m);
+  }
+  c.ci = field(r, RC::CI); c.cj = field(r, RC::CJ); c.ia = field(r, RC::IA); c.ia5 = field(r, RC::IA5);
+  c.n1i = field(r, RC::N1I); c.n2i = field(r, RC::N2I); c.n1j = field(r, RC::N1J); c.n2j = field(r, RC::N2J);
+}
+
+constexpr int SWEEP_MAX_THREADS = 384;
+
+// One pass (forward or backward) of a row.  The record of the next cell the
+// row visits is loaded into registers while the current cell is computed,
+// so between two barriers only the neighbouring row's state (one
+// shared-memory read) sits in front of the FP64 chain.
+template <int NV, bool update, bool FWD>
+__device__ __forceinline__ void sweep_pass(const Lvl &L, const BlkDev &bd, double *sh, const double *rsrc, double *recBw, double *st, int R, int CS,
+                                           unsigned rank, int rl, int j, bool row_ok, double gm1) {
+  using SL = Slot<NV>;
+  using RC = Rec<NV>;
+  constexpr int S = SL::S;
+  const int nx = bd.nx, ny = bd.ny, rows = ny - 1, ni = nx - 1;
+  const long long F = L.F;
+  // record of the k-th visited cell: forward i = 1 + k, backward i = ni - k
+  auto src = [&](int k) { return rsrc + (size_t)(FWD ? k : ni - 1 - k) * RC::N; };
+  Raw<NV> raw;
+  Cur<NV> cur;
+  if (row_ok) {
+    load_raw<NV, FWD>(raw, src(0));
+    unpack<NV, FWD>(cur, raw);
+  }
+  int k = 0;
+  for (int pp = 2; pp <= nx + ny - 2; pp++) {
+    const int p = FWD ? pp : nx + ny - pp;
+    const int i = p - j;
+    const int buf = p & 1;
+    if (row_ok && i >= 1 && i <= ni) {
+      const bool more = k + 1 < ni;
+      if (more) load_raw<NV, FWD>(raw, src(k + 1));
+      double acc[NV], dn[NV];
+#pragma unroll
+      for (int m = 0; m < NV; m++) acc[m] = FWD ? cur.a[m] : cur.c0[m];
+      if (FWD ? (i > 1) : (i < ni)) add_shipped<NV>(st, cur.n1i, cur.n2i, cur.ci, acc);
+      if (FWD ? (j > 1) : (j < rows)) {
+        const double2 *s2 = reinterpret_cast<const double2 *>(sh + ((size_t)(buf ^ 1) * (R + 2) + (FWD ? rl : rl + 2)) * S);
+        double sn[S];
+#pragma unroll
+        for (int m = 0; m < S / 2; m++) { double2 v = s2[m]; sn[2 * m] = v.x; sn[2 * m + 1] = v.y; }
+        add_shipped<NV>(sn, cur.n1j, cur.n2j, cur.cj, acc);
+      }
+#pragma unroll
+      for (int m = 0; m < NV; m++) {
+        const double inv = (NV == 5 && m == 4) ? cur.ia5 : cur.ia;
+        if (update) {
+          // fused: U + dU* in one fma going forward, carried in the backward
+          // record, and U + dU* + dU** in one fma going backward
+          st[m] = fma(acc[m], inv, FWD ? cur.u[m] : cur.a[m]);
+        } else {
+          dn[m] = FWD ? acc[m] * inv : fma(acc[m], inv, cur.a[m]);
+          st[m] = cur.u[m] + dn[m];
+        }
+      }
+      const double rd = rcp(st[0]);
+      st[SL::U] = st[1] * rd;
+      st[SL::V] = st[2] * rd;
+      st[SL::P] = gm1 * fma(-0.5, fma(st[2], st[SL::V], st[1] * st[SL::U]), st[3]);
+      double2 *own = reinterpret_cast<double2 *>(sh + ((size_t)buf * (R + 2) + rl + 1) * S);
+#pragma unroll
+      for (int m = 0; m < S / 2; m++) own[m] = make_double2(st[2 * m], st[2 * m + 1]);
+      if (CS > 1) {
+        if (FWD && rl == R - 1 && (int)rank + 1 < CS) {
+          unsigned a = remote_smem(sh + ((size_t)buf * (R + 2) + 0) * S, rank + 1);
+#pragma unroll
+          for (int m = 0; m < S / 2; m++) st_remote2(a + 16u * m, st[2 * m], st[2 * m + 1]);
+        }
+        if (!FWD && rl == 0 && rank > 0) {
+          unsigned a = remote_smem(sh + ((size_t)buf * (R + 2) + R + 1) * S, rank - 1);
+#pragma unroll
+          for (int m = 0; m < S / 2; m++) st_remote2(a + 16u * m, st[2 * m], st[2 * m + 1]);
+        }
+      }
+      if (FWD) {
+        // the forward result becomes the A field of this cell's backward record
+        double *w = recBw + (size_t)(i - 1) * RC::N;
+        const double *val = update ? st : dn;
+#pragma unroll
+        for (int m = 0; m + 1 < NV; m += 2) reinterpret_cast<double2 *>(w + RC::A)[m / 2] = make_double2(val[m], val[m + 1]);
+        if (NV & 1) w[RC::A + NV - 1] = val[NV - 1];
+      } else {
+        const long long id = bd.off + (long long)(j + 2) * bd.P + (i + 2);
+#pragma unroll
+        for (int m = 0; m < NV; m++) {
+          L.du[m * F + id] = update ? st[m] - cur.u[m] : dn[m];
+          if (update) L.U[m * F + id] = st[m];
+        }
+      }
+      if (more) unpack<NV, FWD>(cur, raw);
+      k++;
+    }
+    if (CS > 1) cluster_barrier();
+    else __syncthreads();
+  }
 }
 
 // CS == 1: one CTA per block, planes separated by __syncthreads.
@@ -212,109 +333,35 @@ __device__ __forceinline__ void fetch(double *dst, const double *src) {
 // edge rows write into the neighbour CTA's halo slot through distributed
 // shared memory and planes are separated by a cluster barrier.
 template <int NV, bool update>
-__global__ void __launch_bounds__(1024) k_lusgs_sweep(Lvl L, int R, int CS, int RPW) {
+__global__ void __launch_bounds__(SWEEP_MAX_THREADS) k_lusgs_sweep(Lvl L, int R, int CS, int RPW) {
   using SL = Slot<NV>;
   using RC = Rec<NV>;
   constexpr int S = SL::S;
-  extern __shared__ __align__(16) double sh[];  // [2][R+2][S] slots, then [blockDim][2][RC::N] records
+  extern __shared__ __align__(16) double sh[];  // [2][R+2][S] slots
   const unsigned rank = CS > 1 ? cluster_rank() : 0u;
   const BlkDev bd = L.blk[blockIdx.x / CS];  // by value: no re-reads after global stores
-  const int nx = bd.nx, ny = bd.ny, rows = ny - 1, ni = nx - 1;
-  const long long off = bd.off, P = bd.P;
+  const int rows = bd.ny - 1, ni = bd.nx - 1;
   // RPW rows per warp (lanes RPW..31 idle): fewer rows per warp spread a
   // plane's work over more SM sub-partitions
   const int lane_w = threadIdx.x & 31;
   const int rl = lane_w < RPW ? (int)(threadIdx.x >> 5) * RPW + lane_w : R;
   const int j = (int)rank * R + rl + 1;
   const bool row_ok = rl < R && j <= rows;
-  const long long F = L.F;
   const double gm1 = L.cs[bd.cas].gamma - 1.0;
-  double *rec = sh + (size_t)2 * (R + 2) * S + (size_t)threadIdx.x * 2 * RC::N;
   const double *recF = L.rec + ((size_t)bd.cell0 + (size_t)(j - 1) * ni) * RC::N;   // row j, i = 1
   const double *recB = recF + (size_t)L.ncell * RC::N;
   double *recBw = L.rec + ((size_t)L.ncell + bd.cell0 + (size_t)(j - 1) * ni) * RC::N;
   double st[S];
 #pragma unroll
   for (int m = 0; m < S; m++) st[m] = 0.0;
-  for (int pass = 0; pass < 2; pass++) {
-    const bool fwd = pass == 0;
-    const double *rsrc = fwd ? recF : recB;
-    if (row_ok) fetch<NV>(rec, rsrc + (size_t)(fwd ? 0 : ni - 1) * RC::N);
-    cp_commit();
-    int k = 0;
-    for (int pp = 2; pp <= nx + ny - 2; pp++) {
-      const int p = fwd ? pp : nx + ny - pp;
-      const int i = p - j;
-      const int buf = p & 1;
-      if (row_ok && i >= 1 && i <= ni) {
-        const double *cur = rec + (k & 1) * RC::N;
-        const int inx = fwd ? i + 1 : i - 1;
-        if (inx >= 1 && inx <= ni) fetch<NV>(rec + ((k + 1) & 1) * RC::N, rsrc + (size_t)(inx - 1) * RC::N);
-        cp_commit();
-        cp_wait1();
-        double acc[NV], dn[NV];
-#pragma unroll
-        for (int m = 0; m < NV; m++) acc[m] = fwd ? cur[RC::A + m] : cur[RC::C0 + m];
-        if (fwd ? (i > 1) : (i < ni)) add_shipped<NV>(st, cur[RC::N1I], cur[RC::N2I], cur[RC::CI], acc);
-        if (fwd ? (j > 1) : (j < rows)) {
-          const double2 *s2 = reinterpret_cast<const double2 *>(sh + ((size_t)(buf ^ 1) * (R + 2) + (fwd ? rl : rl + 2)) * S);
-          double sn[S];
-#pragma unroll
-          for (int m = 0; m < S / 2; m++) { double2 v = s2[m]; sn[2 * m] = v.x; sn[2 * m + 1] = v.y; }
-          add_shipped<NV>(sn, cur[RC::N1J], cur[RC::N2J], cur[RC::CJ], acc);
-        }
-        const double ia = cur[RC::IA], ia5 = cur[RC::IA5];
-#pragma unroll
-        for (int m = 0; m < NV; m++) {
-          double inv = (NV == 5 && m == 4) ? ia5 : ia;
-          if (update) {
-            // fused: U + dU* in one fma going forward, carried in the backward
-            // record, and U + dU* + dU** in one fma going backward
-            st[m] = fma(acc[m], inv, fwd ? cur[RC::U + m] : cur[RC::A + m]);
-          } else {
-            dn[m] = fwd ? acc[m] * inv : fma(acc[m], inv, cur[RC::A + m]);
-            st[m] = cur[RC::U + m] + dn[m];
-          }
-        }
-        const double rd = rcp(st[0]);
-        st[SL::U] = st[1] * rd;
-        st[SL::V] = st[2] * rd;
-        st[SL::P] = gm1 * fma(-0.5, fma(st[2], st[SL::V], st[1] * st[SL::U]), st[3]);
-        double2 *own = reinterpret_cast<double2 *>(sh + ((size_t)buf * (R + 2) + rl + 1) * S);
-#pragma unroll
-        for (int m = 0; m < S / 2; m++) own[m] = make_double2(st[2 * m], st[2 * m + 1]);
-        if (CS > 1) {
-          if (fwd && rl == R - 1 && (int)rank + 1 < CS) {
-            unsigned a = remote_smem(sh + ((size_t)buf * (R + 2) + 0) * S, rank + 1);
-#pragma unroll
-            for (int m = 0; m < S / 2; m++) st_remote2(a + 16u * m, st[2 * m], st[2 * m + 1]);
-          }
-          if (!fwd && rl == 0 && rank > 0) {
-            unsigned a = remote_smem(sh + ((size_t)buf * (R + 2) + R + 1) * S, rank - 1);
-#pragma unroll
-            for (int m = 0; m < S / 2; m++) st_remote2(a + 16u * m, st[2 * m], st[2 * m + 1]);
-          }
-        }
-        if (fwd) {
-          // the forward dU becomes the A field of this cell's backward record
-          double *w = recBw + (size_t)(i - 1) * RC::N;
-#pragma unroll
-          for (int m = 0; m < NV; m++) w[RC::A + m] = update ? st[m] : dn[m];
-        } else {
-          const long long id = off + (long long)(j + 2) * P + (i + 2);
-#pragma unroll
-          for (int m = 0; m < NV; m++) {
-            L.du[m * F + id] = update ? st[m] - cur[RC::U + m] : dn[m];
-            if (update) L.U[m * F + id] = st[m];
-          }
-        }
-        k++;
-      }
-      if (CS > 1) cluster_barrier();
-      else __syncthreads();
-    }
-    cp_wait0();
-  }
+  sweep_pass<NV, update, true>(L, bd, sh, recF, recBw, st, R, CS, rank, rl, j, row_ok, gm1);
+  sweep_pass<NV, update, false>(L, bd, sh, recB, recBw, st, R, CS, rank, rl, j, row_ok, gm1);
+}
+
+template <int NV>
+size_t smem_bytes(int R, int th) {
+  (void)th;
+  return (size_t)2 * (R + 2) * Slot<NV>::S * sizeof(double);
 }
 
 template <int NV>
@@ -324,11 +371,11 @@ void sweep_nv(const Lvl &L, double alfa1, int update, int max_rows, int cs, int 
   int R = (max_rows + CS - 1) / CS;
   if (rpw < 1 || rpw > 32) rpw = 32;
   int th = ((R + rpw - 1) / rpw) * 32;
-  size_t smem = ((size_t)2 * (R + 2) * Slot<NV>::S + (size_t)th * 2 * Rec<NV>::N) * sizeof(double);
-  if (smem > 227 * 1024 || th > 1024) {  // fall back to full warps
+  size_t smem = smem_bytes<NV>(R, th);
+  if (smem > 227 * 1024 || th > SWEEP_MAX_THREADS) {  // fall back to full warps
     rpw = 32;
     th = ((R + 31) / 32) * 32;
-    smem = ((size_t)2 * (R + 2) * Slot<NV>::S + (size_t)th * 2 * Rec<NV>::N) * sizeof(double);
+    smem = smem_bytes<NV>(R, th);
   }
   auto kern = update ? k_lusgs_sweep<NV, true> : k_lusgs_sweep<NV, false>;
   if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -347,10 +394,13 @@ void sweep_nv(const Lvl &L, double alfa1, int update, int max_rows, int cs, int 
   cudaLaunchKernelEx(&cfg, kern, L, R, CS, rpw);
 }
 
+// one CTA holding every row of the widest block, or SIZE_MAX when the rows
+// exceed the CTA's thread limit
 template <int NV>
 size_t smem_nv(int rows) {
   int th = ((rows + 31) / 32) * 32;
-  return ((size_t)2 * (rows + 2) * Slot<NV>::S + (size_t)th * 2 * Rec<NV>::N) * sizeof(double);
+  if (th > SWEEP_MAX_THREADS) return (size_t)-1;
+  return smem_bytes<NV>(rows, th);
 }
 size_t lusgs_smem(int nv, int rows) { return nv == 4 ? smem_nv<4>(rows) : nv == 5 ? smem_nv<5>(rows) : smem_nv<6>(rows); }
 
