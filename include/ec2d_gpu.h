@@ -68,7 +68,12 @@ typedef struct ec2d_ctx ec2d_ctx;
  *  DU (NVAR,1:nx,1:ny)  AMU, AMUT, X1, Y1 (-1:nx+1,-1:ny+1)
  *  VOL,SI,SJ,NI1,NI2,NJ1,NJ2 (1:nx,1:ny)  DW (0:nx,0:ny)
  *  QF (4,1:nx-1,1:ny-1)  DELTU (4,-1:nx+1,-1:ny+1)  UN (NVAR,0:nx,0:ny)
- *  X, Y (-1:nx+2,-1:ny+2) */
+ *  X, Y (-1:nx+2,-1:ny+2)
+ * DU holds the LU-SGS increment after ec2d_du_lusgs and after steps of
+ * levels that take the general LU-SGS kernel; the wavefront sweep of a step
+ * adds the increment to U directly and leaves DU as scratch (the reference
+ * reads DU only inside du_LU_SGS_2D and the update after it,
+ * sub_LU_SGS.f90:44-95, sub_NS_singlegrid.f90:197-211). */
 enum {
   EC2D_F_RES = 0, EC2D_F_DT = 1, EC2D_F_LCI = 2, EC2D_F_LCJ = 3, EC2D_F_LVI = 4,
   EC2D_F_LVJ = 5, EC2D_F_DU = 6, EC2D_F_AMU = 7, EC2D_F_AMUT = 8, EC2D_F_X1 = 9,

@@ -313,11 +313,13 @@ __device__ __forceinline__ void sweep_pass(const Lvl &L, const BlkDev &bd, doubl
         for (int m = 0; m + 1 < NV; m += 2) reinterpret_cast<double2 *>(w + RC::A)[m / 2] = make_double2(val[m], val[m + 1]);
         if (NV & 1) w[RC::A + NV - 1] = val[NV - 1];
       } else {
+        // an updating sweep writes U only: the reference reads DU nowhere but
+        // inside du_LU_SGS_2D and the update that follows it
         const long long id = bd.off + (long long)(j + 2) * bd.P + (i + 2);
 #pragma unroll
         for (int m = 0; m < NV; m++) {
-          L.du[m * F + id] = update ? st[m] - cur.u[m] : dn[m];
           if (update) L.U[m * F + id] = st[m];
+          else L.du[m * F + id] = dn[m];
         }
       }
       if (more) unpack<NV, FWD>(cur, raw);
