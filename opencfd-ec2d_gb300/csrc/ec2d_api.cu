@@ -82,6 +82,7 @@ struct Level {
   std::vector<int> case_face0, case_nface;
   long long F = 0;
   int max_rows = 0;   // widest block (ny-1) of the level: LU-SGS threads per CTA
+  int bc_max_nodes = 0;  // most boundary nodes of one far-field / symmetry subface
   bool fast64 = false, fast32 = false;  // wavefront LU-SGS fits one CTA (FP64 / FP32 records)
   Lvl L{};
   int *d_case_tile0 = nullptr, *d_case_ntile = nullptr, *d_case_ncell = nullptr;
@@ -444,6 +445,18 @@ int build_level(ec2d_ctx *ctx, int l) {
     }
     d.nphase = nph;
   }
+  // far-field and symmetry subfaces: one edge normal per boundary node,
+  // filled on the device once the coordinates are there
+  int nbcn = 0;
+  for (auto &sd : lv.sub) {
+    sd.nrm0 = -1;
+    bool need = sd.neighb == BC_Farfield || sd.neighb == BC_Inlet || sd.neighb == BC_Outlet || sd.neighb == BC_Symmetry;
+    if (!need) continue;
+    int nn = (sd.iend - sd.ist + 1) * (sd.jend - sd.jst + 1);
+    sd.nrm0 = nbcn;
+    nbcn += nn;
+    lv.bc_max_nodes = std::max(lv.bc_max_nodes, nn);
+  }
   // wall faces for forces (fine level only)
   if (l == 1) {
     lv.case_face0.assign(ncase, 0); lv.case_nface.assign(ncase, 0);
@@ -515,6 +528,13 @@ int build_level(ec2d_ctx *ctx, int l) {
   lv.fast64 = lv.max_rows <= 1024 && lusgs_smem(nv, lv.max_rows) <= smem_max;
   lv.fast32 = lv.max_rows <= 1024 && lusgs32_smem(nv, lv.max_rows) <= smem_max;
   L.rec = (lv.fast64 || lv.fast32) ? dalloc<double>(lv, (size_t)2 * L.ncell * lusgs_planes(nv)) : nullptr;
+  {
+    size_t nbcn = 0;
+    for (auto &sd : lv.sub)
+      if (sd.nrm0 >= 0) nbcn = std::max(nbcn, (size_t)sd.nrm0 + (size_t)(sd.iend - sd.ist + 1) * (sd.jend - sd.jst + 1));
+    L.bcn = nbcn ? dalloc<double2>(lv, nbcn) : nullptr;
+    if (nbcn && !L.bcn) return EC2D_ERR_NOMEM;
+  }
   L.npart = dalloc<double>(lv, lv.tiles.size() * 12);
   L.norms = dalloc<double>(lv, ncase * 12);
   L.status = dalloc<int>(lv, ncase * 4);
@@ -560,6 +580,11 @@ int build_level(ec2d_ctx *ctx, int l) {
     CK(cudaMemcpy(L.U, u.data(), u.size() * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(L.un, un.data(), un.size() * sizeof(double), cudaMemcpyHostToDevice));
     if (anyfdm) CK(cudaMemcpy(L.met, met.data(), met.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  if (L.bcn) {
+    launch_bc_normals(L, lv.bc_max_nodes, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->stream));
   }
   return EC2D_OK;
 }

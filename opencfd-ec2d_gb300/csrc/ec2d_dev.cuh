@@ -52,6 +52,7 @@ struct SubDev {
   int phase, nitem;         // physical BC: barrier phase within the block, work items
   int nbk;                  // level-global index of the neighbour block (-1: physical)
   int nface, nist, niend, njst, njend;  // the neighbour subface it reads
+  int nrm0;                 // far-field / symmetry: first node's entry in Lvl::bcn (-1: none)
 };
 
 struct CaseDev {
@@ -78,6 +79,7 @@ struct Lvl {
   double *fdm;              // FDM scratch planes
   double *lu;               // LU-SGS pre-pass planes (4 NV + 10)
   double *rec;              // LU-SGS per-cell sweep records: [2 passes][ncell][4 NV + 10]
+  double2 *bcn;             // unit normals of the far-field and symmetry boundary nodes
   int ncell;                // interior cells of the level (all blocks of all cases)
   double *npart;            // norm partials: per tile 2*6 doubles
   double *norms;            // per case: max[6], rms[6]

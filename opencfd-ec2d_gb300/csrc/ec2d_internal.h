@@ -23,6 +23,7 @@ void launch_fdm(const Lvl &L, cudaStream_t s);
 void launch_dual_term(const Lvl &L, double sfac, cudaStream_t s);
 // k_bc.cu
 void launch_bc(const Lvl &L, int phases, cudaStream_t s);
+void launch_bc_normals(const Lvl &L, int max_nodes, cudaStream_t s);
 // k_lusgs.cu
 void launch_lusgs(const Lvl &L, double alfa1, cudaStream_t s);
 // k_sweep.cu

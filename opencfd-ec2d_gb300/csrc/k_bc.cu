@@ -64,22 +64,12 @@ __device__ void bc_wall(const Lvl &L, const BlkDev &b, const CaseDev &c, const S
   }
 }
 
-// Symmetry_or_slidewall, sub_boundary.f90:391-451
-__device__ void bc_symmetry(const Lvl &L, const BlkDev &b, const SubDev &s, int i, int j, int k) {
+// Symmetry_or_slidewall, sub_boundary.f90:391-451.  The reflection
+// U - 2 (U.n) n does not depend on the sign of n, so the far-field edge
+// normal serves.
+__device__ void bc_symmetry(const Lvl &L, const BlkDev &b, const SubDev &s, int i, int j, int k, double2 nrm) {
   const long long F = L.F;
-  const double *x = L.geo + G_X * F, *y = L.geo + G_Y * F;
-  double n1, n2;
-  if (s.face == 1 || s.face == 3) {
-    long long p0 = fidx(b, i, j), p1 = fidx(b, i, j + 1);
-    double dx = x[p1] - x[p0], dy = y[p1] - y[p0];
-    double si = sqrt(dx * dx + dy * dy);
-    n1 = dy / si; n2 = -dx / si;
-  } else {
-    long long p0 = fidx(b, i, j), p1 = fidx(b, i + 1, j);
-    double dx = x[p1] - x[p0], dy = y[p1] - y[p0];
-    double si = sqrt(dx * dx + dy * dy);
-    n1 = -dy / si; n2 = dx / si;
-  }
+  const double n1 = nrm.x, n2 = nrm.y;
   int i1, j1, i2, j2;
   ghost_pair(s.face, i, j, k, i1, j1, i2, j2);
   long long a = fidx(b, i1, j1), g = fidx(b, i2, j2);
@@ -92,15 +82,35 @@ __device__ void bc_symmetry(const Lvl &L, const BlkDev &b, const SubDev &s, int 
   for (int m = 4; m < L.nvar; m++) U[m * F + g] = U[m * F + a];
 }
 
+// Outward unit normal of a boundary node's edge, as boundary_Farfield_inlet_outlet
+// (sub_boundary.f90:484-497) and Symmetry_or_slidewall (:400-412) form it: the
+// edge from node (i,j) to (i,j+1) on faces 1 and 3, to (i+1,j) on faces 2 and
+// 4, rotated by the face's sign.  Geometry only, so it is evaluated once at
+// set-up (k_bc_normals), in separately rounded operations: the far-field
+// inflow/outflow switch is a sign test on u.n.
+__device__ __forceinline__ double2 edge_normal(const Lvl &L, const BlkDev &b, int face, int i, int j) {
+  const long long F = L.F;
+  const double *x = L.geo + G_X * F, *y = L.geo + G_Y * F;
+  const long long p0 = fidx(b, i, j), p1 = (face == 1 || face == 3) ? fidx(b, i, j + 1) : fidx(b, i + 1, j);
+  const double dx = __dsub_rn(x[p1], x[p0]), dy = __dsub_rn(y[p1], y[p0]);
+  const double sl = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+  if (face == 1 || face == 4) return make_double2(__ddiv_rn(-dy, sl), __ddiv_rn(dx, sl));
+  return make_double2(__ddiv_rn(dy, sl), __ddiv_rn(-dx, sl));
+}
+
 // boundary_Farfield_inlet_outlet, sub_boundary.f90:457-581.  The inflow /
 // outflow switch is a sign test on a computed normal Mach number, so this
 // routine is evaluated with separately rounded operations (no contraction)
-// to take the same branch as the reference on every cell.
-__device__ void bc_farfield(const Lvl &L, const BlkDev &b, const CaseDev &c, const SubDev &s, int i, int j) {
+// to take the same branch as the reference on every cell.  Every ghost layer
+// takes the same interior state and normal (the reference recomputes the
+// same values per layer), so the ghost state is formed once and written to
+// all LAP layers.
+__device__ void bc_farfield(const Lvl &L, const BlkDev &b, const CaseDev &c, const SubDev &s, int i, int j,
+                            double2 nrm) {
   const long long F = L.F;
   double *U = L.U;
-  const double *x = L.geo + G_X * F, *y = L.geo + G_Y * F;
   const double gamma = c.gamma, gm1 = gamma - 1.0;
+  const double n1 = nrm.x, n2 = nrm.y;
   int i1, j1;
   if (s.face == 1 || s.face == 2) { i1 = i; j1 = j; }
   else if (s.face == 3) { i1 = i - 1; j1 = j; }
@@ -111,58 +121,47 @@ __device__ void bc_farfield(const Lvl &L, const BlkDev &b, const CaseDev &c, con
   double ke = __dmul_rn(__dmul_rn(0.5, d1), __dadd_rn(__dmul_rn(u1, u1), __dmul_rn(v1, v1)));
   double p1 = __dmul_rn(__dsub_rn(U[3 * F + a], ke), gm1);
   double c1 = __dsqrt_rn(__ddiv_rn(__dmul_rn(gamma, p1), d1));
-  double dx, dy, n1, n2;
-  if (s.face == 1 || s.face == 3) {
-    long long p0 = fidx(b, i, j), p1i = fidx(b, i, j + 1);
-    dx = __dsub_rn(x[p1i], x[p0]); dy = __dsub_rn(y[p1i], y[p0]);
-  } else {
-    long long p0 = fidx(b, i, j), p1i = fidx(b, i + 1, j);
-    dx = __dsub_rn(x[p1i], x[p0]); dy = __dsub_rn(y[p1i], y[p0]);
-  }
-  double sl = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
-  if (s.face == 1 || s.face == 4) { n1 = __ddiv_rn(-dy, sl); n2 = __ddiv_rn(dx, sl); }
-  else { n1 = __ddiv_rn(dy, sl); n2 = __ddiv_rn(-dx, sl); }
   double Ma_n = __ddiv_rn(__dadd_rn(__dmul_rn(u1, n1), __dmul_rn(v1, n2)), c1);
-  // every ghost layer k takes the same interior state and normal, so one item
-  // writes all LAP layers (the reference recomputes them per k: same values)
-  for (int k = 1; k <= LAP; k++) {
-  int i2, j2;
-  if (s.face == 1) { i2 = i - k; j2 = j; }
-  else if (s.face == 2) { i2 = i; j2 = j - k; }
-  else if (s.face == 3) { i2 = i + k - 1; j2 = j; }
-  else { i2 = i; j2 = j + k - 1; }
-  long long g = fidx(b, i2, j2);
-  int type = s.neighb;
+  double G[6];
+  const int type = s.neighb;
   if (type == BC_Outlet || (type == BC_Farfield && Ma_n >= 0.0)) {
     if (Ma_n > 1.0 || c.p_outlet < 0 || type == BC_Farfield) {
-      for (int m = 0; m < L.nvar; m++) U[m * F + g] = U[m * F + a];
+      for (int m = 0; m < L.nvar; m++) G[m] = U[m * F + a];
     } else {
       double pb = c.p_outlet;
       double db = d1 + (c.p_outlet - p1) / (c1 * c1);
       double ub = u1 + (p1 - c.p_outlet) / (d1 * c1) * n1;
       double vb = v1 + (p1 - c.p_outlet) / (d1 * c1) * n2;
       double p2 = 2.0 * pb - p1, d2 = 2.0 * db - d1, u2 = 2.0 * ub - u1, v2 = 2.0 * vb - v1;
-      U[g] = d2; U[F + g] = d2 * u2; U[2 * F + g] = d2 * v2;
-      U[3 * F + g] = p2 / gm1 + 0.5 * d2 * (u2 * u2 + v2 * v2);
-      for (int m = 4; m < L.nvar; m++) U[m * F + g] = U[m * F + a];
+      G[0] = d2; G[1] = d2 * u2; G[2] = d2 * v2;
+      G[3] = p2 / gm1 + 0.5 * d2 * (u2 * u2 + v2 * v2);
+      for (int m = 4; m < L.nvar; m++) G[m] = U[m * F + a];
     }
   } else {
     const double d_inf = 1.0, u_inf = c.cosA, v_inf = c.sinA, p_inf = c.p00;
     if (c.p_outlet < 0 || Ma_n <= -1.0) {
-      U[g] = d_inf; U[F + g] = d_inf * u_inf; U[2 * F + g] = d_inf * v_inf;
-      U[3 * F + g] = p_inf / gm1 + 0.5 * d_inf * (u_inf * u_inf + v_inf * v_inf);
+      G[0] = d_inf; G[1] = d_inf * u_inf; G[2] = d_inf * v_inf;
+      G[3] = p_inf / gm1 + 0.5 * d_inf * (u_inf * u_inf + v_inf * v_inf);
     } else {
       double pb = 0.5 * (p1 + p_inf - d1 * c1 * ((u_inf - u1) * n1 + (v_inf - v1) * n2));
       double db = d_inf + (pb - p_inf) / (c1 * c1);
       double ub = u_inf - (p_inf - pb) / (d1 * c1) * n1;
       double vb = v_inf - (p_inf - pb) / (d1 * c1) * n2;
       double p2 = 2.0 * pb - p1, d2 = 2.0 * db - d1, u2 = 2.0 * ub - u1, v2 = 2.0 * vb - v1;
-      U[g] = d2; U[F + g] = d2 * u2; U[2 * F + g] = d2 * v2;
-      U[3 * F + g] = p2 / gm1 + 0.5 * d2 * (u2 * u2 + v2 * v2);
+      G[0] = d2; G[1] = d2 * u2; G[2] = d2 * v2;
+      G[3] = p2 / gm1 + 0.5 * d2 * (u2 * u2 + v2 * v2);
     }
-    if (L.nvar == 5) U[4 * F + g] = c.vt_inf / c.Re;
-    else if (L.nvar == 6) { U[4 * F + g] = d_inf * c.Kt_inf; U[5 * F + g] = d_inf * c.Wt_inf; }
+    if (L.nvar == 5) G[4] = c.vt_inf / c.Re;
+    else if (L.nvar == 6) { G[4] = d_inf * c.Kt_inf; G[5] = d_inf * c.Wt_inf; }
   }
+  for (int k = 1; k <= LAP; k++) {
+    int i2, j2;
+    if (s.face == 1) { i2 = i - k; j2 = j; }
+    else if (s.face == 2) { i2 = i; j2 = j - k; }
+    else if (s.face == 3) { i2 = i + k - 1; j2 = j; }
+    else { i2 = i; j2 = j + k - 1; }
+    const long long g = fidx(b, i2, j2);
+    for (int m = 0; m < L.nvar; m++) U[m * F + g] = G[m];
   }
 }
 
@@ -186,37 +185,45 @@ __device__ void corner(const Lvl &L, const CaseDev &c, long long i1, long long i
 }
 
 // phases: 1 physical BCs, 2 halo copy, 4 corners, 8 nu~/k/omega clip
+constexpr int BC_SMEM_SUBS = 32;  // subfaces of a block staged in shared memory
+
 __global__ void __launch_bounds__(256) k_bc(Lvl L, int phases) {
   const int bk = blockIdx.x;
   const BlkDev &b = L.blk[bk];
   const CaseDev &c = L.cs[b.cas];
   const long long F = L.F;
   if (phases & 1) {
+    // the block's subface table in shared memory (global beyond 32)
+    __shared__ SubDev ssub[BC_SMEM_SUBS];
+    const int nsub = b.nsub;
+    for (int ks = threadIdx.x; ks < min(nsub, BC_SMEM_SUBS); ks += blockDim.x) ssub[ks] = L.sub[b.sub0 + ks];
+    __syncthreads();
+    auto sub = [&](int ks) -> const SubDev & { return ks < BC_SMEM_SUBS ? ssub[ks] : L.sub[b.sub0 + ks]; };
     // subfaces of one phase touch disjoint cells (grouped at set-up in
     // subface order): their items are spread over the CTA together
     for (int ph = 0; ph < b.nphase; ph++) {
       int total = 0;
-      for (int ks = 0; ks < b.nsub; ks++) {
-        const SubDev &s = L.sub[b.sub0 + ks];
+      for (int ks = 0; ks < nsub; ks++) {
+        const SubDev &s = sub(ks);
         if (s.neighb < 0 && s.phase == ph) total += s.nitem;
       }
       for (int t = threadIdx.x; t < total; t += blockDim.x) {
         int u = t, ks = 0;
-        for (; ks < b.nsub; ks++) {
-          const SubDev &s = L.sub[b.sub0 + ks];
+        for (; ks < nsub; ks++) {
+          const SubDev &s = sub(ks);
           if (s.neighb >= 0 || s.phase != ph) continue;
           if (u < s.nitem) break;
           u -= s.nitem;
         }
-        const SubDev s = L.sub[b.sub0 + ks];
+        const SubDev &s = sub(ks);
         int ni = s.iend - s.ist + 1;
         if (s.neighb == BC_Farfield || s.neighb == BC_Inlet || s.neighb == BC_Outlet) {
-          bc_farfield(L, b, c, s, s.ist + u % ni, s.jst + u / ni);
+          bc_farfield(L, b, c, s, s.ist + u % ni, s.jst + u / ni, L.bcn[s.nrm0 + u]);
         } else {
           int k = u % LAP + 1, r = u / LAP;
           int i = s.ist + r % ni, j = s.jst + r / ni;
           if (s.neighb == BC_Wall) bc_wall(L, b, c, s, i, j, k);
-          else if (s.neighb == BC_Symmetry) bc_symmetry(L, b, s, i, j, k);
+          else if (s.neighb == BC_Symmetry) bc_symmetry(L, b, s, i, j, k, L.bcn[s.nrm0 + r]);
         }
       }
       __syncthreads();
@@ -267,5 +274,20 @@ __global__ void __launch_bounds__(256) k_bc(Lvl L, int phases) {
 }
 
 void launch_bc(const Lvl &L, int phases, cudaStream_t s) { k_bc<<<L.nblk, 256, 0, s>>>(L, phases); }
+
+// set-up: the edge normals of every far-field and symmetry node (grid y: block)
+__global__ void __launch_bounds__(256) k_bc_normals(Lvl L) {
+  const BlkDev &b = L.blk[blockIdx.y];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int ks = 0; ks < b.nsub; ks++) {
+    const SubDev &s = L.sub[b.sub0 + ks];
+    const int ni = s.iend - s.ist + 1, nn = ni * (s.jend - s.jst + 1);
+    if (s.nrm0 < 0 || t >= nn) continue;
+    L.bcn[s.nrm0 + t] = edge_normal(L, b, s.face, s.ist + t % ni, s.jst + t / ni);
+  }
+}
+void launch_bc_normals(const Lvl &L, int max_nodes, cudaStream_t s) {
+  if (max_nodes > 0) k_bc_normals<<<dim3((max_nodes + 255) / 256, L.nblk), 256, 0, s>>>(L);
+}
 
 }  // namespace ec2d
