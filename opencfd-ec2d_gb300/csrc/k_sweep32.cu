@@ -5,7 +5,7 @@
 //
 // Same wavefront as the FP64 sweep (k_sweep.cu): hyperplanes p = i+j in the
 // reference's Gauss-Seidel order, one CTA per block, thread j owns row j, the
-// next cell's record is prefetched with cp.async, the neighbouring row's
+// next three cells' records are in flight by cp.async, the neighbouring row's
 // state comes through a double-buffered shared slot.  One difference in
 // arithmetic, not in the operator: the flux difference of comput_DFn
 // (sub_LU_SGS.f90:117-138), F_n(U + dU) - F_n(U), is evaluated in the
@@ -148,7 +148,11 @@ __device__ __forceinline__ void cp16(void *dst, const void *src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_ring() { asm volatile("cp.async.wait_group 3;" ::: "memory"); }
+// record buffers per thread: the record of the cell three planes ahead is in
+// flight while the current one is computed (an FP32 plane is short next to
+// the L2 latency)
+constexpr int RING32 = 4;
 __device__ __forceinline__ void cp_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 template <int NV>
@@ -170,7 +174,7 @@ __global__ void __launch_bounds__(1024) k_lusgs_sweep32(Lvl L) {
   const int R = blockDim.x;
   const bool row_ok = j <= rows;
   const float gm1 = (float)(L.cs[bd.cas].gamma - 1.0);
-  char *rec = reinterpret_cast<char *>(shf + (size_t)2 * (R + 2) * S) + (size_t)threadIdx.x * 2 * RC::BYTES;
+  char *rec = reinterpret_cast<char *>(shf + (size_t)2 * (R + 2) * S) + (size_t)threadIdx.x * RING32 * RC::BYTES;
   const char *recF = reinterpret_cast<const char *>(L.rec) + ((size_t)bd.cell0 + (size_t)(j - 1) * ni) * RC::BYTES;
   const char *recB = recF + (size_t)L.ncell * RC::BYTES;
   char *recBw = reinterpret_cast<char *>(L.rec) + ((size_t)L.ncell + bd.cell0 + (size_t)(j - 1) * ni) * RC::BYTES;
@@ -180,19 +184,22 @@ __global__ void __launch_bounds__(1024) k_lusgs_sweep32(Lvl L) {
   for (int pass = 0; pass < 2; pass++) {
     const bool fwd = pass == 0;
     const char *rsrc = fwd ? recF : recB;
-    if (row_ok) fetch32<NV>(rec, rsrc + (size_t)(fwd ? 0 : ni - 1) * RC::BYTES);
-    cp_commit();
+    // record of the k-th visited cell: forward i = 1 + k, backward i = ni - k
+    auto src = [&](int k) { return rsrc + (size_t)(fwd ? k : ni - 1 - k) * RC::BYTES; };
+    for (int q = 0; q < RING32 - 1; q++) {
+      if (row_ok && q < ni) fetch32<NV>(rec + q * RC::BYTES, src(q));
+      cp_commit();
+    }
     int k = 0;
     for (int pp = 2; pp <= nx + ny - 2; pp++) {
       const int p = fwd ? pp : nx + ny - pp;
       const int i = p - j;
       const int buf = p & 1;
       if (row_ok && i >= 1 && i <= ni) {
-        const float *cur = reinterpret_cast<const float *>(rec + (k & 1) * RC::BYTES);
-        const int inx = fwd ? i + 1 : i - 1;
-        if (inx >= 1 && inx <= ni) fetch32<NV>(rec + ((k + 1) & 1) * RC::BYTES, rsrc + (size_t)(inx - 1) * RC::BYTES);
+        const float *cur = reinterpret_cast<const float *>(rec + (k % RING32) * RC::BYTES);
+        if (k + RING32 - 1 < ni) fetch32<NV>(rec + ((k + RING32 - 1) % RING32) * RC::BYTES, src(k + RING32 - 1));
         cp_commit();
-        cp_wait1();
+        cp_wait_ring();
         float acc[NV];
 #pragma unroll
         for (int m = 0; m < NV; m++) acc[m] = fwd ? cur[RC::A + m] : 0.0f;
@@ -247,7 +254,7 @@ __global__ void __launch_bounds__(1024) k_lusgs_sweep32(Lvl L) {
   }
 }
 
-// dU (FP32, in the backward records) -> L.du, and U += dU in FP64
+// dU (FP32, in the backward records) -> U += dU in FP64, or -> L.du
 // (NS_Time_advance_LU_SGS, sub_NS_singlegrid.f90:203-211)
 template <int NV>
 __global__ void __launch_bounds__(TILE) k_apply32(Lvl L, int update) {
@@ -262,18 +269,20 @@ __global__ void __launch_bounds__(TILE) k_apply32(Lvl L, int update) {
   const size_t cell = (size_t)b.cell0 + (size_t)(j - 1) * (b.nx - 1) + (i - 1);
   const float *rb = reinterpret_cast<const float *>(reinterpret_cast<const char *>(L.rec) +
                                                     ((size_t)L.ncell + cell) * RC::BYTES);
+  // an updating sweep keeps no DU, as the FP64 sweep (the reference reads DU
+  // only inside du_LU_SGS_2D and the update after it)
 #pragma unroll
   for (int m = 0; m < NV; m++) {
     double d = (double)rb[RC::A + m];
-    L.du[m * F + id] = d;
     if (update) L.U[m * F + id] += d;
+    else L.du[m * F + id] = d;
   }
 }
 
 template <int NV>
 size_t smem32(int rows) {
   int th = ((rows + 31) / 32) * 32;
-  return (size_t)2 * (th + 2) * S32<NV>::S * sizeof(float) + (size_t)th * 2 * R32<NV>::BYTES;
+  return (size_t)2 * (th + 2) * S32<NV>::S * sizeof(float) + (size_t)th * RING32 * R32<NV>::BYTES;
 }
 
 template <int NV>
