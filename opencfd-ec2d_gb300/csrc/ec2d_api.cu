@@ -299,6 +299,7 @@ CaseDev make_casedev(const ec2d_params &p) {
   c.rPr = 1.0 / p.Pr;
   c.rMa = 1.0 / p.Ma;
   c.rRe = 1.0 / p.Re;
+  c.rgm1 = 1.0 / (p.gamma - 1.0);
   c.Cv = 1.0 / (p.gamma * (p.gamma - 1.0) * p.Ma * p.Ma);
   c.rCv = p.gamma * (p.gamma - 1.0) * p.Ma * p.Ma;
   c.Cp = c.Cv * p.gamma;

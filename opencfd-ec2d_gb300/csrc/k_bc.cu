@@ -98,13 +98,16 @@ __device__ __forceinline__ double2 edge_normal(const Lvl &L, const BlkDev &b, in
   return make_double2(__ddiv_rn(dy, sl), __ddiv_rn(-dx, sl));
 }
 
-// boundary_Farfield_inlet_outlet, sub_boundary.f90:457-581.  The inflow /
-// outflow switch is a sign test on a computed normal Mach number, so this
-// routine is evaluated with separately rounded operations (no contraction)
-// to take the same branch as the reference on every cell.  Every ghost layer
-// takes the same interior state and normal (the reference recomputes the
-// same values per layer), so the ghost state is formed once and written to
-// all LAP layers.
+// boundary_Farfield_inlet_outlet, sub_boundary.f90:457-581.  The state is
+// formed by reciprocal-multiply and a refined reciprocal square root (each
+// within an ulp or two of the reference's divides and square root).  The
+// inflow / outflow switch is a comparison of the normal Mach number with 0
+// and +-1: where the fast value lies within its error bound of a threshold,
+// the switch is decided on the value the reference computes, in separately
+// rounded correctly rounded operations, so every cell takes the reference's
+// branch.  Every ghost layer takes the same interior state and normal (the
+// reference recomputes the same values per layer), so the ghost state is
+// formed once and written to all LAP layers.
 __device__ void bc_farfield(const Lvl &L, const BlkDev &b, const CaseDev &c, const SubDev &s, int i, int j,
                             double2 nrm) {
   const long long F = L.F;
@@ -116,25 +119,36 @@ __device__ void bc_farfield(const Lvl &L, const BlkDev &b, const CaseDev &c, con
   else if (s.face == 3) { i1 = i - 1; j1 = j; }
   else { i1 = i; j1 = j - 1; }
   long long a = fidx(b, i1, j1);
-  double d1 = U[a];
-  double u1 = __ddiv_rn(U[F + a], d1), v1 = __ddiv_rn(U[2 * F + a], d1);
-  double ke = __dmul_rn(__dmul_rn(0.5, d1), __dadd_rn(__dmul_rn(u1, u1), __dmul_rn(v1, v1)));
-  double p1 = __dmul_rn(__dsub_rn(U[3 * F + a], ke), gm1);
-  double c1 = __dsqrt_rn(__ddiv_rn(__dmul_rn(gamma, p1), d1));
-  double Ma_n = __ddiv_rn(__dadd_rn(__dmul_rn(u1, n1), __dmul_rn(v1, n2)), c1);
+  const double d1 = U[a], m1 = U[F + a], m2 = U[2 * F + a], E1 = U[3 * F + a];
+  const double rd = rcp(d1);
+  const double u1 = m1 * rd, v1 = m2 * rd;
+  const double p1 = (E1 - 0.5 * d1 * (u1 * u1 + v1 * v1)) * gm1;
+  const double c2 = gamma * p1 * rd;
+  const double rc = rsqrt_d(c2);  // 1 / c1
+  const double c1 = c2 * rc;
+  double Ma_n = (u1 * n1 + v1 * n2) * rc;
+  // a few ulps of |u| / c bound the fast value's error
+  const double tol = 1.0e-12 * (fabs(u1) + fabs(v1)) * rc;
+  if (fabs(Ma_n) <= tol || fabs(fabs(Ma_n) - 1.0) <= tol + 1.0e-12) {
+    const double ux = __ddiv_rn(m1, d1), vx = __ddiv_rn(m2, d1);
+    const double ke = __dmul_rn(__dmul_rn(0.5, d1), __dadd_rn(__dmul_rn(ux, ux), __dmul_rn(vx, vx)));
+    const double px = __dmul_rn(__dsub_rn(E1, ke), gm1);
+    const double cx = __dsqrt_rn(__ddiv_rn(__dmul_rn(gamma, px), d1));
+    Ma_n = __ddiv_rn(__dadd_rn(__dmul_rn(ux, n1), __dmul_rn(vx, n2)), cx);
+  }
   double G[6];
   const int type = s.neighb;
   if (type == BC_Outlet || (type == BC_Farfield && Ma_n >= 0.0)) {
     if (Ma_n > 1.0 || c.p_outlet < 0 || type == BC_Farfield) {
       for (int m = 0; m < L.nvar; m++) G[m] = U[m * F + a];
     } else {
-      double pb = c.p_outlet;
-      double db = d1 + (c.p_outlet - p1) / (c1 * c1);
-      double ub = u1 + (p1 - c.p_outlet) / (d1 * c1) * n1;
-      double vb = v1 + (p1 - c.p_outlet) / (d1 * c1) * n2;
-      double p2 = 2.0 * pb - p1, d2 = 2.0 * db - d1, u2 = 2.0 * ub - u1, v2 = 2.0 * vb - v1;
+      const double pb = c.p_outlet;
+      const double db = d1 + (c.p_outlet - p1) * (rc * rc);
+      const double t = (p1 - c.p_outlet) * (rd * rc);
+      const double ub = u1 + t * n1, vb = v1 + t * n2;
+      const double p2 = 2.0 * pb - p1, d2 = 2.0 * db - d1, u2 = 2.0 * ub - u1, v2 = 2.0 * vb - v1;
       G[0] = d2; G[1] = d2 * u2; G[2] = d2 * v2;
-      G[3] = p2 / gm1 + 0.5 * d2 * (u2 * u2 + v2 * v2);
+      G[3] = p2 * c.rgm1 + 0.5 * d2 * (u2 * u2 + v2 * v2);
       for (int m = 4; m < L.nvar; m++) G[m] = U[m * F + a];
     }
   } else {
@@ -143,13 +157,13 @@ __device__ void bc_farfield(const Lvl &L, const BlkDev &b, const CaseDev &c, con
       G[0] = d_inf; G[1] = d_inf * u_inf; G[2] = d_inf * v_inf;
       G[3] = p_inf / gm1 + 0.5 * d_inf * (u_inf * u_inf + v_inf * v_inf);
     } else {
-      double pb = 0.5 * (p1 + p_inf - d1 * c1 * ((u_inf - u1) * n1 + (v_inf - v1) * n2));
-      double db = d_inf + (pb - p_inf) / (c1 * c1);
-      double ub = u_inf - (p_inf - pb) / (d1 * c1) * n1;
-      double vb = v_inf - (p_inf - pb) / (d1 * c1) * n2;
-      double p2 = 2.0 * pb - p1, d2 = 2.0 * db - d1, u2 = 2.0 * ub - u1, v2 = 2.0 * vb - v1;
+      const double pb = 0.5 * (p1 + p_inf - d1 * c1 * ((u_inf - u1) * n1 + (v_inf - v1) * n2));
+      const double db = d_inf + (pb - p_inf) * (rc * rc);
+      const double t = (p_inf - pb) * (rd * rc);
+      const double ub = u_inf - t * n1, vb = v_inf - t * n2;
+      const double p2 = 2.0 * pb - p1, d2 = 2.0 * db - d1, u2 = 2.0 * ub - u1, v2 = 2.0 * vb - v1;
       G[0] = d2; G[1] = d2 * u2; G[2] = d2 * v2;
-      G[3] = p2 / gm1 + 0.5 * d2 * (u2 * u2 + v2 * v2);
+      G[3] = p2 * c.rgm1 + 0.5 * d2 * (u2 * u2 + v2 * v2);
     }
     if (L.nvar == 5) G[4] = c.vt_inf / c.Re;
     else if (L.nvar == 6) { G[4] = d_inf * c.Kt_inf; G[5] = d_inf * c.Wt_inf; }

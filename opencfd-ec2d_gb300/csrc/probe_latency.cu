@@ -132,6 +132,35 @@ __global__ void k_rcp3_ulps(unsigned long long *worst, int per_thread) {
   }
   atomicMax(worst, (unsigned long long)m);
 }
+// rsqrt.approx.ftz.f64: largest relative error of y^2 x - 1 (half of it is
+// the error of y), and the reciprocal square root refined by one third-order
+// step: distance of x * y from the IEEE square root in ulps, and of y from
+// 1 / (IEEE square root) in ulps
+__global__ void k_rsqrt_err(unsigned long long *worst, int per_thread) {
+  unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double m0 = 0.0;
+  long long m1 = 0, m2 = 0;
+  for (int k = 0; k < per_thread; k++) {
+    unsigned long long h = (t * per_thread + k) * 0x9E3779B97F4A7C15ull;
+    h ^= h >> 29;
+    int ex = (int)((h >> 52) % 17) - 8;
+    double x = ldexp(__longlong_as_double((long long)(0x3FF0000000000000ull | (h & 0x000FFFFFFFFFFFFFull))), ex);
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double e0 = fabs(fma(-x, y * y, 1.0));
+    m0 = e0 > m0 ? e0 : m0;
+    const double e = fma(-x, y * y, 1.0);
+    const double y3 = fma(y, e * fma(0.375, e, 0.5), y);
+    const double sq = __dsqrt_rn(x);
+    long long d1 = __double_as_longlong(x * y3) - __double_as_longlong(sq);
+    long long d2 = __double_as_longlong(y3) - __double_as_longlong(__ddiv_rn(1.0, sq));
+    d1 = d1 < 0 ? -d1 : d1; d2 = d2 < 0 ? -d2 : d2;
+    m1 = d1 > m1 ? d1 : m1; m2 = d2 > m2 ? d2 : m2;
+  }
+  atomicMax(worst, (unsigned long long)__double_as_longlong(m0));
+  atomicMax(worst + 1, (unsigned long long)m1);
+  atomicMax(worst + 2, (unsigned long long)m2);
+}
 int main() {
   const int n = 1000, T = 256;
   double *out; long long *cyc; long long h[T];
@@ -194,6 +223,17 @@ int main() {
     k_rcp3_ulps<<<608, 256>>>(w, 256);
     cudaMemcpy(&hw, w, sizeof(hw), cudaMemcpyDeviceToHost);
     printf("third-order reciprocal: max distance from 1/x over 4.0e7 samples = %llu ulp\n", hw);
+    cudaFree(w);
+  }
+  {
+    unsigned long long *w, hw[3] = {0, 0, 0};
+    cudaMalloc(&w, 3 * sizeof(unsigned long long));
+    cudaMemset(w, 0, 3 * sizeof(unsigned long long));
+    k_rsqrt_err<<<608, 256>>>(w, 256);
+    cudaMemcpy(hw, w, sizeof(hw), cudaMemcpyDeviceToHost);
+    double e; memcpy(&e, &hw[0], sizeof(e));
+    printf("rsqrt.approx.ftz.f64: max |x y^2 - 1| over 4.0e7 samples = %.3e (2^%.2f)\n", e, log2(e));
+    printf("third-order rsqrt: x*y vs sqrt(x) max %llu ulp, y vs 1/sqrt(x) max %llu ulp\n", hw[1], hw[2]);
     cudaFree(w);
   }
   cudaError_t e = cudaDeviceSynchronize();
