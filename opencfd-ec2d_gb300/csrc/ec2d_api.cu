@@ -548,6 +548,9 @@ int build_level(ec2d_ctx *ctx, int l) {
   CK(cudaMemcpy(lv.d_case_tile0, lv.case_tile0.data(), ncase * sizeof(int), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(lv.d_case_ntile, lv.case_ntile.data(), ncase * sizeof(int), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(lv.d_case_ncell, lv.case_ncell.data(), ncase * sizeof(int), cudaMemcpyHostToDevice));
+  L.case_tile0 = lv.d_case_tile0; L.case_ntile = lv.d_case_ntile; L.case_ncell = lv.d_case_ncell;
+  L.nctr = dalloc<unsigned>(lv, 1);  // zeroed; the last CTA of k_res resets it
+  if (!L.nctr) return EC2D_ERR_NOMEM;
   if (!lv.wall_faces.empty()) {
     lv.d_faces = dalloc<int4>(lv, lv.wall_faces.size());
     lv.d_face_out = dalloc<double>(lv, lv.wall_faces.size() * 5);
@@ -688,8 +691,8 @@ void residual(ec2d_ctx *ctx, int l) {
     else sfac = 1.0 / (2.0 * ctx->P.dt_global);
     K(ctx, "k_dual", l, 1, [&] { launch_dual_term(L, sfac, s); });
   }
-  K(ctx, "norms", l, fused ? 1 : 2,
-    [&] { launch_norms(L, lv.d_case_tile0, lv.d_case_ntile, lv.d_case_ncell, !fused, s); });
+  if (!(fused && norms_fused_final(L)))
+    K(ctx, "norms", l, fused ? 1 : 2, [&] { launch_norms(L, !fused, s); });
 }
 
 void bc_all(ec2d_ctx *ctx, int l) {

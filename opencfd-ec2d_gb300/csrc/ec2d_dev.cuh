@@ -84,6 +84,8 @@ struct Lvl {
   int ncell;                // interior cells of the level (all blocks of all cases)
   double *npart;            // norm partials: per tile 2*6 doubles
   double *norms;            // per case: max[6], rms[6]
+  const int *case_tile0, *case_ntile, *case_ncell;  // per case: first tile, tiles, interior cells
+  unsigned *nctr;           // tiles of k_res done (the last one reduces the partials)
   int *status;              // per case: code, block, i, j
 };
 

@@ -12,8 +12,8 @@ void launch_prim(const Lvl &L, cudaStream_t s);
 void launch_flux_i(const Lvl &L, bool fp32, cudaStream_t s);
 void launch_flux_j(const Lvl &L, bool fp32, cudaStream_t s);
 void launch_res(const Lvl &L, bool with_norms, cudaStream_t s);
-void launch_norms(const Lvl &L, const int *case_tile0, const int *case_ntile, const int *case_ncell, bool partials,
-                  cudaStream_t s);
+void launch_norms(const Lvl &L, bool partials, cudaStream_t s);
+bool norms_fused_final(const Lvl &L);
 // k_turb.cu
 void launch_sa(const Lvl &L, cudaStream_t s);
 void launch_sst(const Lvl &L, cudaStream_t s);

@@ -193,7 +193,66 @@ __global__ void __launch_bounds__(TILE) k_flux_j(Lvl L) {
 // same cells, same reduction tree, so the norms are bit-identical); only when
 // no later kernel of the residual stage changes Res (no FDM patch, no
 // dual-time term)
-template <bool NORM>
+// Norm reductions.  max |Res| is reduced on the bit patterns: for
+// non-negative doubles the order of the patterns as signed 64-bit integers is
+// the order of the values, so the maxima run on the integer pipes (an FP64
+// warp instruction holds its sub-partition for 64 cycles on this part) and
+// are exact in any order.  Sums of Res^2 run in a fixed tree order.
+__device__ __forceinline__ long long warp_max_bits(long long a) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a = max(a, __shfl_xor_sync(0xffffffffu, a, o));
+  return a;
+}
+__device__ __forceinline__ double warp_sum(double q) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+  return q;
+}
+
+// one CTA's partials: per variable the max |Res| and sum Res^2 of its cells
+__device__ __forceinline__ void tile_partials(const Lvl &L, bool act, const double *vres) {
+  __shared__ long long smax[6][TILE / 32];
+  __shared__ double ssum[6][TILE / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nv = L.nvar;
+#pragma unroll
+  for (int m = 0; m < 6; m++) {
+    if (m >= nv) break;
+    const long long a = warp_max_bits(act ? __double_as_longlong(fabs(vres[m])) : 0ll);
+    const double q = warp_sum(act ? vres[m] * vres[m] : 0.0);
+    if (lane == 0) { smax[m][w] = a; ssum[m][w] = q; }
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    const int m = threadIdx.x;
+    long long a = 0;
+    double q = 0.0;
+    if (m < nv)
+      for (int k = 0; k < TILE / 32; k++) { a = max(a, smax[m][k]); q += ssum[m][k]; }
+    L.npart[(size_t)blockIdx.x * 12 + m] = __longlong_as_double(a);
+    L.npart[(size_t)blockIdx.x * 12 + 6 + m] = q;
+  }
+}
+
+// per case and quantity (max[6], rms[6]) from the tile partials: one warp per
+// (case, quantity), lanes over tiles, then the warp tree
+__device__ __forceinline__ void final_norm(const Lvl &L, int cs, int m) {
+  const int lane = threadIdx.x & 31;
+  const int t0 = L.case_tile0[cs], nt = L.case_ntile[cs];
+  double out = 0.0;
+  if (m < 6) {
+    long long a = 0;
+    for (int t = lane; t < nt; t += 32) a = max(a, __double_as_longlong(L.npart[(size_t)(t0 + t) * 12 + m]));
+    out = __longlong_as_double(warp_max_bits(a));
+  } else {
+    double q = 0.0;
+    for (int t = lane; t < nt; t += 32) q += L.npart[(size_t)(t0 + t) * 12 + m];
+    q = warp_sum(q);
+    out = (m - 6 < L.nvar) ? sqrt(q / (1.0 * L.case_ncell[cs])) : 0.0;
+  }
+  if (lane == 0) L.norms[cs * 12 + m] = out;
+}
+
+template <bool NORM, bool FINAL>
 __global__ void __launch_bounds__(TILE) k_res(Lvl L) {
   int bk, i, j;
   bool act = tile_ij(L, bk, i, j);
@@ -248,84 +307,44 @@ __global__ void __launch_bounds__(TILE) k_res(Lvl L) {
     L.lc[L_DT * F + id] = dt;
   }
   if (NORM) {
-    __shared__ double smax[6][TILE / 32], ssum[6][TILE / 32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-    for (int m = 0; m < 6; m++) {
-      double a = act && m < L.nvar ? fabs(vres[m]) : 0.0, q = act && m < L.nvar ? vres[m] * vres[m] : 0.0;
-      for (int o = 16; o > 0; o >>= 1) {
-        a = fmax(a, __shfl_down_sync(0xffffffffu, a, o));
-        q += __shfl_down_sync(0xffffffffu, q, o);
+    tile_partials(L, act, vres);
+    if (FINAL) {
+      // the last CTA to finish reduces every tile's partials (few cases)
+      __shared__ int last;
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) last = atomicAdd(L.nctr, 1u) == gridDim.x - 1;
+      __syncthreads();
+      if (last) {
+        __threadfence();
+        const int w = threadIdx.x >> 5;
+        for (int k = w; k < L.ncase * 12; k += TILE / 32) final_norm(L, k / 12, k % 12);
+        if (threadIdx.x == 0) *L.nctr = 0u;
       }
-      if (lane == 0) { smax[m][w] = a; ssum[m][w] = q; }
-    }
-    __syncthreads();
-    if (threadIdx.x < 6) {
-      int m = threadIdx.x;
-      double a = 0.0, q = 0.0;
-      for (int k = 0; k < TILE / 32; k++) { a = fmax(a, smax[m][k]); q += ssum[m][k]; }
-      L.npart[(size_t)blockIdx.x * 12 + m] = a;
-      L.npart[(size_t)blockIdx.x * 12 + 6 + m] = q;
     }
   }
 }
 
 // per-tile partial norms of Res (max |Res| and sum Res^2 per variable)
 __global__ void __launch_bounds__(TILE) k_norm_partial(Lvl L) {
-  __shared__ double smax[6][TILE / 32], ssum[6][TILE / 32];
   int bk, i, j;
-  double vmax[6] = {0, 0, 0, 0, 0, 0}, vsum[6] = {0, 0, 0, 0, 0, 0};
+  double vres[6] = {0, 0, 0, 0, 0, 0};
+  bool act = false;
   if (tile_ij(L, bk, i, j)) {
     const BlkDev &b = L.blk[bk];
     if (i >= 1 && i <= b.nx - 1 && j >= 1 && j <= b.ny - 1) {
+      act = true;
       long long id = fidx(b, i, j);
-      for (int m = 0; m < L.nvar; m++) {
-        double r = L.res[m * L.F + id];
-        vmax[m] = fabs(r);
-        vsum[m] = r * r;
-      }
+      for (int m = 0; m < L.nvar; m++) vres[m] = L.res[m * L.F + id];
     }
   }
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-  for (int m = 0; m < 6; m++) {
-    double a = vmax[m], s = vsum[m];
-    for (int o = 16; o > 0; o >>= 1) {
-      a = fmax(a, __shfl_down_sync(0xffffffffu, a, o));
-      s += __shfl_down_sync(0xffffffffu, s, o);
-    }
-    if (lane == 0) { smax[m][w] = a; ssum[m][w] = s; }
-  }
-  __syncthreads();
-  if (threadIdx.x < 6) {
-    int m = threadIdx.x;
-    double a = 0.0, s = 0.0;
-    for (int k = 0; k < TILE / 32; k++) { a = fmax(a, smax[m][k]); s += ssum[m][k]; }
-    L.npart[(size_t)blockIdx.x * 12 + m] = a;
-    L.npart[(size_t)blockIdx.x * 12 + 6 + m] = s;
-  }
+  tile_partials(L, act, vres);
 }
 
-// per-case reduction of the tile partials in a fixed order
-__global__ void k_norm_final(Lvl L, const int *case_tile0, const int *case_ntile, const int *case_ncell) {
-  int cs = blockIdx.x;
-  int t0 = case_tile0[cs], nt = case_ntile[cs];
-  __shared__ double sm[12][32];
-  int m = threadIdx.y;  // 0..11
-  int lane = threadIdx.x;  // 0..31
-  double acc = 0.0;
-  for (int t = lane; t < nt; t += 32) {
-    double v = L.npart[(size_t)(t0 + t) * 12 + m];
-    acc = (m < 6) ? fmax(acc, v) : acc + v;
-  }
-  sm[m][lane] = acc;
-  __syncthreads();
-  if (lane == 0) {
-    double a = 0.0;
-    for (int k = 0; k < 32; k++) a = (m < 6) ? fmax(a, sm[m][k]) : a + sm[m][k];
-    if (m >= 6) a = (m - 6 < L.nvar) ? sqrt(a / (1.0 * case_ncell[cs])) : 0.0;
-    L.norms[cs * 12 + m] = a;
-  }
+// per-case reduction of the tile partials (one warp per case and quantity)
+__global__ void __launch_bounds__(384) k_norm_final(Lvl L) {
+  const int k = blockIdx.x * 12 + (threadIdx.x >> 5);
+  final_norm(L, k / 12, k % 12);
 }
 
 void launch_prim(const Lvl &L, cudaStream_t s) { k_prim<<<L.ntiles, TILE, 0, s>>>(L); }
@@ -337,14 +356,17 @@ void launch_flux_j(const Lvl &L, bool fp32, cudaStream_t s) {
   if (fp32) k_flux_j<float><<<L.ntiles, TILE, 0, s>>>(L);
   else k_flux_j<double><<<L.ntiles, TILE, 0, s>>>(L);
 }
+// with_norms: the tile partials inside k_res; with few cases the last CTA of
+// k_res also forms the per-case norms (fused_final() tells the caller)
+bool norms_fused_final(const Lvl &L) { return L.ncase <= 8; }
 void launch_res(const Lvl &L, bool with_norms, cudaStream_t s) {
-  if (with_norms) k_res<true><<<L.ntiles, TILE, 0, s>>>(L);
-  else k_res<false><<<L.ntiles, TILE, 0, s>>>(L);
+  if (!with_norms) k_res<false, false><<<L.ntiles, TILE, 0, s>>>(L);
+  else if (norms_fused_final(L)) k_res<true, true><<<L.ntiles, TILE, 0, s>>>(L);
+  else k_res<true, false><<<L.ntiles, TILE, 0, s>>>(L);
 }
-void launch_norms(const Lvl &L, const int *case_tile0, const int *case_ntile, const int *case_ncell, bool partials,
-                  cudaStream_t s) {
+void launch_norms(const Lvl &L, bool partials, cudaStream_t s) {
   if (partials) k_norm_partial<<<L.ntiles, TILE, 0, s>>>(L);
-  k_norm_final<<<L.ncase, dim3(32, 12), 0, s>>>(L, case_tile0, case_ntile, case_ncell);
+  k_norm_final<<<L.ncase, 384, 0, s>>>(L);
 }
 
 }  // namespace ec2d
