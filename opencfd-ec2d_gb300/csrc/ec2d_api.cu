@@ -28,7 +28,7 @@ using namespace ec2d;
 namespace {
 
 const double PI = 3.1415926535897932;
-constexpr int TILE = 256;
+constexpr int TILE = EC2D_TILE;
 
 struct HBlock {
   int nx = 0, ny = 0;

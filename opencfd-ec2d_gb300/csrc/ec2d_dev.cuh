@@ -89,6 +89,14 @@ struct Lvl {
   int *status;              // per case: code, block, i, j
 };
 
+// Items (cells, faces or nodes of a block's padded index range) per tile of
+// the level's tile list, and threads per CTA of the kernels that walk it.
+// Most of those kernels are chains of FP64 operations on this part, so their
+// time is the chain length times the warps that share a sub-partition: 128
+// gives every warp of the 2 x 48 x 48 and 2 x 24 x 24 multigrid levels its
+// own sub-partition, where 256 put two on each.
+constexpr int EC2D_TILE = 128;
+
 __host__ __device__ __forceinline__ long long fidx(const BlkDev &b, int i, int j) {
   return b.off + (long long)(j + 2) * b.P + (i + 2);
 }

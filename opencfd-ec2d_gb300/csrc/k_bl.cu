@@ -20,7 +20,7 @@
 namespace ec2d {
 namespace {
 
-constexpr int TILE = 256;
+constexpr int TILE = EC2D_TILE;
 // single-precision literals of sub_turbulence_BL.f90:215 promoted to double
 constexpr double AP = (double)26.f, Ccp = (double)1.6f, Ckleb = (double)0.3f, Cwk = 0.25, AKT = (double)0.4f,
                  AK = (double)0.0168f;

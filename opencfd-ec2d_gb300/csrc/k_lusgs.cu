@@ -248,7 +248,7 @@ __global__ void k_freestream(Lvl L, int flow, int turb) {
   }
 }
 
-constexpr int TILE = 256;
+constexpr int TILE = EC2D_TILE;
 void launch_lusgs(const Lvl &L, double alfa1, cudaStream_t s) { k_lusgs<<<L.nblk, 128, 0, s>>>(L, alfa1); }
 void launch_add_du(const Lvl &L, cudaStream_t s) { k_add_du<<<L.ntiles, TILE, 0, s>>>(L); }
 void launch_euler(const Lvl &L, int force, cudaStream_t s) { k_euler<<<L.ntiles, TILE, 0, s>>>(L, force); }

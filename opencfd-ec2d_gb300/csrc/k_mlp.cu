@@ -430,11 +430,11 @@ __global__ void k_warm_apply(Lvl L, const float *__restrict__ pred, const int *_
 }  // namespace mlp
 
 void launch_features(const Lvl &L, const double *shape, float *feat, float *targ, cudaStream_t s) {
-  mlp::k_features<<<L.ntiles, 256, 0, s>>>(L, shape, feat, targ);
+  mlp::k_features<<<L.ntiles, EC2D_TILE, 0, s>>>(L, shape, feat, targ);
 }
 void launch_warm_start(const Lvl &L, const float *pred, int *bad, cudaStream_t s) {
-  mlp::k_warm_check<<<L.ntiles, 256, 0, s>>>(L, pred, bad);
-  mlp::k_warm_apply<<<L.ntiles, 256, 0, s>>>(L, pred, bad);
+  mlp::k_warm_check<<<L.ntiles, EC2D_TILE, 0, s>>>(L, pred, bad);
+  mlp::k_warm_apply<<<L.ntiles, EC2D_TILE, 0, s>>>(L, pred, bad);
 }
 
 // ---------------------------------------------------------------------------

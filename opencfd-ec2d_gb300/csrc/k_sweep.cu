@@ -38,7 +38,7 @@
 
 namespace ec2d {
 
-constexpr int TILE = 256;
+constexpr int TILE = EC2D_TILE;
 
 // record layout (doubles), identical for both passes:
 //  A    forward: Res + K; backward: the forward dU, or U + dU when the sweep
@@ -72,7 +72,7 @@ int lusgs_planes(int nv) { return 3 * nv + 10; }  // at least Rec<NV>::N and the
 // half of comput_DFn (sub_LU_SGS.f90:122-137)
 template <int NV>
 __device__ __forceinline__ void fn(const double *U, double n1, double n2, double gm1, double *Fo) {
-  double r = 1.0 / U[0];
+  double r = rcp(U[0]);
   double un = (U[1] * n1 + U[2] * n2) * r;
   double p = gm1 * (U[3] - 0.5 * (U[1] * U[1] + U[2] * U[2]) * r);
   Fo[0] = U[0] * un;
@@ -119,9 +119,9 @@ __global__ void __launch_bounds__(TILE) k_lusgs_prep(Lvl L, double alfa1) {
   double *rb = L.rec + ((size_t)L.ncell + cell) * RC::N;      // backward record
   double vol = g[G_VOL * F + id];
   double Lv = lc[L_VI * F + id] + lc[L_VJ * F + id];
-  double alfa = vol / lc[L_DT * F + id] + 1.0 * (lc[L_CI * F + id] + lc[L_CJ * F + id]) + vol * alfa1;
+  double alfa = vol * rcp(lc[L_DT * F + id]) + 1.0 * (lc[L_CI * F + id] + lc[L_CJ * F + id]) + vol * alfa1;
   if (visc) alfa += 2.0 * Lv;
-  double ia = 1.0 / alfa, ia5 = (NV == 5) ? 1.0 / (alfa + Lv) : ia;
+  double ia = rcp(alfa), ia5 = (NV == 5) ? rcp(alfa + Lv) : ia;
   double ni1 = g[G_NI1 * F + id], ni2 = g[G_NI2 * F + id], nj1 = g[G_NJ1 * F + id], nj2 = g[G_NJ2 * F + id];
   double res[NV], K[2][NV];  // K[pass]: -(sum over directions of F_n(U_nb, s))
 #pragma unroll

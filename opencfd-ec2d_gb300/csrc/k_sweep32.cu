@@ -31,7 +31,7 @@ namespace ec2d {
 
 namespace {
 
-constexpr int TILE = 256;
+constexpr int TILE = EC2D_TILE;
 
 constexpr int pad4(int n) { return (n + 3) / 4 * 4; }
 
@@ -78,13 +78,13 @@ __global__ void __launch_bounds__(TILE) k_lusgs_prep32(Lvl L, double alfa1) {
   float *rb = reinterpret_cast<float *>(base + ((size_t)L.ncell + cell) * RC::BYTES);
   double vol = g[G_VOL * F + id];
   double Lv = lc[L_VI * F + id] + lc[L_VJ * F + id];
-  double alfa = vol / lc[L_DT * F + id] + 1.0 * (lc[L_CI * F + id] + lc[L_CJ * F + id]) + vol * alfa1;
+  double alfa = vol * rcp(lc[L_DT * F + id]) + 1.0 * (lc[L_CI * F + id] + lc[L_CJ * F + id]) + vol * alfa1;
   if (visc) alfa += 2.0 * Lv;
-  double ia = 1.0 / alfa, ia5 = (NV == 5) ? 1.0 / (alfa + Lv) : ia;
+  double ia = rcp(alfa), ia5 = (NV == 5) ? rcp(alfa + Lv) : ia;
   double U[NV];
 #pragma unroll
   for (int m = 0; m < NV; m++) U[m] = L.U[m * F + id];
-  double r = 1.0 / U[0], u = U[1] * r, v = U[2] * r;
+  double r = rcp(U[0]), u = U[1] * r, v = U[2] * r;
   double p = gm1 * (U[3] - 0.5 * (U[1] * u + U[2] * v));
   double ni1 = g[G_NI1 * F + id], ni2 = g[G_NI2 * F + id], nj1 = g[G_NJ1 * F + id], nj2 = g[G_NJ2 * F + id];
 #pragma unroll

@@ -7,7 +7,7 @@
 
 namespace ec2d {
 
-constexpr int TILE = 256;
+constexpr int TILE = EC2D_TILE;
 
 __device__ __forceinline__ bool tile_xy(const Lvl &L, int &bk, int &i, int &j) {
   int2 t = L.tiles[blockIdx.x];
