@@ -653,7 +653,10 @@ void K(ec2d_ctx *ctx, const char *name, int level, int nk, Fn fn) {
 }
 
 // Comput_Residual_one_mesh (sub_Residual.f90:13-107) for all blocks of a level
-void residual(ec2d_ctx *ctx, int l) {
+// post: RES_ADD_FORCE / RES_FORCE_FN / RES_SET_UN steps that follow the
+// residual in the caller's sequence, done inside k_res when the norms are
+// final there, as separate kernels otherwise
+void residual(ec2d_ctx *ctx, int l, int post = 0) {
   Level &lv = ctx->lv[l];
   const Lvl &L = lv.L;
   cudaStream_t s = ctx->stream;
@@ -683,7 +686,8 @@ void residual(ec2d_ctx *ctx, int l) {
   }
   const bool dual = ctx->P.Time_Method == Time_Dual && l == 1;
   const bool fused = !L.fdm && !dual;  // Res final after k_res: norm partials fused into it
-  K(ctx, "k_res", l, 1, [&] { launch_res(L, fused, s); });
+  const int inpass = (fused && norms_fused_final(L)) ? post : 0;
+  K(ctx, "k_res", l, 1, [&] { launch_res(L, fused, inpass, s); });
   if (L.fdm) K(ctx, "fdm", l, 3, [&] { launch_fdm(L, s); });
   if (dual) {
     double sfac;
@@ -693,6 +697,10 @@ void residual(ec2d_ctx *ctx, int l) {
   }
   if (!(fused && norms_fused_final(L)))
     K(ctx, "norms", l, fused ? 1 : 2, [&] { launch_norms(L, !fused, s); });
+  const int rest = post & ~inpass;
+  if (rest & RES_ADD_FORCE) K(ctx, "k_add_force", l, 1, [&] { launch_add_force(L, s); });
+  if (rest & RES_FORCE_FN) K(ctx, "k_force_fn", l, 1, [&] { launch_force_fn(L, s); });
+  if (rest & RES_SET_UN) K(ctx, "k_set_un", l, 1, [&] { launch_set_un(L, 4, s); });
 }
 
 void bc_all(ec2d_ctx *ctx, int l) {
@@ -739,9 +747,7 @@ void lusgs_update(ec2d_ctx *ctx, int l, double alfa1) {
 // NS_Time_advance_LU_SGS (sub_NS_singlegrid.f90:185-224); on a coarse level of
 // an LU-SGS-smoothed multigrid cycle the forcing is added after the residual
 void step_lusgs(ec2d_ctx *ctx, int l, double alfa1 = 0.0) {
-  const Lvl &L = ctx->lv[l].L;
-  residual(ctx, l);
-  if (l != 1) K(ctx, "k_add_force", l, 1, [&] { launch_add_force(L, ctx->stream); });
+  residual(ctx, l, l != 1 ? RES_ADD_FORCE : 0);
   lusgs_update(ctx, l, alfa1);
   bc_all(ctx, l);
   advance_counters(ctx, l);
@@ -795,29 +801,33 @@ void mg_smooth_fine(ec2d_ctx *ctx) {
   else if (tm == Time_LU_SGS) { step_lusgs(ctx, 1); clip(ctx, 1); }
   else step_rk3(ctx, 1);
 }
+// Un = U of the coarse level (Euler and LU-SGS smoothing) is taken by the
+// residual evaluation just before (RES_SET_UN, see coarse_entry)
 void mg_smooth_coarse(ec2d_ctx *ctx, int l) {
   const int Time_step_coarse_mesh = 3;
   int tm = ctx->P.Time_Method;
   if (tm == Time_Euler1) {
-    K(ctx, "k_set_un", l, 1, [&] { launch_set_un(ctx->lv[l].L, 4, ctx->stream); });
     for (int m = 0; m < Time_step_coarse_mesh; m++) step_euler(ctx, l);
   } else if (tm == Time_LU_SGS) {
-    K(ctx, "k_set_un", l, 1, [&] { launch_set_un(ctx->lv[l].L, 4, ctx->stream); });
     step_lusgs(ctx, l);
   } else step_rk3(ctx, l);
+}
+// residual of a coarse level right after restriction, QF -= Res
+// (comput_force_function), and Un = U for the smoothing that follows
+void coarse_entry(ec2d_ctx *ctx, int l) {
+  const int tm = ctx->P.Time_Method;
+  residual(ctx, l, RES_FORCE_FN | ((tm == Time_Euler1 || tm == Time_LU_SGS) ? RES_SET_UN : 0));
 }
 // restriction of the residual (flag 2) and of U (flag 1) from level f to f+1
 void restrict_both(ec2d_ctx *ctx, int f) {
   const Lvl &Lf = ctx->lv[f].L, &Lc = ctx->lv[f + 1].L;
-  K(ctx, "k_restrict", f + 1, 1, [&] { launch_restrict(Lf, Lc, 2, ctx->stream); });
-  K(ctx, "k_restrict", f + 1, 1, [&] { launch_restrict(Lf, Lc, 1, ctx->stream); });
+  K(ctx, "k_restrict", f + 1, 1, [&] { launch_restrict(Lf, Lc, 3, ctx->stream); });
 }
 // deltU = U - Un on level c, prolonged to level c-1 and added there
 void correct_from(ec2d_ctx *ctx, int c) {
   const Lvl &Lc = ctx->lv[c].L, &Lf = ctx->lv[c - 1].L;
   K(ctx, "k_delt_u", c, 1, [&] { launch_delt_u(Lc, ctx->stream); });
-  K(ctx, "k_prolong", c - 1, 1, [&] { launch_prolong(Lc, Lf, 2, ctx->stream); });
-  K(ctx, "k_new_u", c - 1, 1, [&] { launch_new_u(Lf, ctx->stream); });
+  K(ctx, "k_prolong", c - 1, 1, [&] { launch_prolong(Lc, Lf, 3, ctx->stream); });
 }
 // NS_2stge_multigrid (sub_NS_multigrid.f90:14-58)
 void mg2(ec2d_ctx *ctx) {
@@ -825,8 +835,7 @@ void mg2(ec2d_ctx *ctx) {
   residual(ctx, 1);
   restrict_both(ctx, 1);
   bc_all(ctx, 2);
-  residual(ctx, 2);
-  K(ctx, "k_force_fn", 2, 1, [&] { launch_force_fn(ctx->lv[2].L, ctx->stream); });
+  coarse_entry(ctx, 2);
   mg_smooth_coarse(ctx, 2);
   correct_from(ctx, 2);
   bc_all(ctx, 1);
@@ -837,15 +846,12 @@ void mg3(ec2d_ctx *ctx) {
   residual(ctx, 1);
   restrict_both(ctx, 1);
   bc_all(ctx, 2);
-  residual(ctx, 2);
-  K(ctx, "k_force_fn", 2, 1, [&] { launch_force_fn(ctx->lv[2].L, ctx->stream); });
+  coarse_entry(ctx, 2);
   mg_smooth_coarse(ctx, 2);
-  residual(ctx, 2);
-  K(ctx, "k_add_force", 2, 1, [&] { launch_add_force(ctx->lv[2].L, ctx->stream); });
+  residual(ctx, 2, RES_ADD_FORCE);
   restrict_both(ctx, 2);
   bc_all(ctx, 3);
-  residual(ctx, 3);
-  K(ctx, "k_force_fn", 3, 1, [&] { launch_force_fn(ctx->lv[3].L, ctx->stream); });
+  coarse_entry(ctx, 3);
   mg_smooth_coarse(ctx, 3);
   correct_from(ctx, 3);
   correct_from(ctx, 2);

@@ -179,18 +179,30 @@ __device__ void bc_farfield(const Lvl &L, const BlkDev &b, const CaseDev &c, con
   }
 }
 
-// U_average_conner, sub_boundary.f90:595-612
+// U_average_conner, sub_boundary.f90:595-612: the corner ghost cell i4 takes
+// rho, u, v, T extrapolated from its neighbours i1, i3 across the corner of
+// i2.  One warp per corner; lanes 0..2 form the primitives of i1, i2, i3 side
+// by side (the divisions by rho as reciprocal-multiplies), lane 0 combines.
 __device__ void corner(const Lvl &L, const CaseDev &c, long long i1, long long i2, long long i3, long long i4) {
   const long long F = L.F;
   double *U = L.U;
-  double Cv = c.Cv;
-  double d1 = U[i1], uu1 = U[F + i1] / d1, v1 = U[2 * F + i1] / d1;
-  double T1 = (U[3 * F + i1] - (uu1 * U[F + i1] + v1 * U[2 * F + i1]) * 0.5) / (d1 * Cv);
-  double d2 = U[i2], uu2 = U[F + i2] / d2, v2 = U[2 * F + i2] / d2;
-  double T2 = (U[3 * F + i2] - (uu2 * U[F + i2] + v2 * U[2 * F + i2]) * 0.5) / (d2 * Cv);
-  double d3 = U[i3], uu3 = U[F + i3] / d3, v3 = U[2 * F + i3] / d3;
-  double T3 = (U[3 * F + i3] - (uu3 * U[F + i3] + v3 * U[2 * F + i3]) * 0.5) / (d3 * Cv);
-  double d4 = d1 + d3 - d2, uu4 = uu1 + uu3 - uu2, v4 = v1 + v3 - v2, T4 = T1 + T3 - T2;
+  const int lane = threadIdx.x & 31;
+  const long long src = lane == 0 ? i1 : lane == 1 ? i2 : i3;
+  double d = 0.0, uu = 0.0, v = 0.0, T = 0.0;
+  if (lane < 3) {
+    d = U[src];
+    const double rd = rcp(d);
+    uu = U[F + src] * rd;
+    v = U[2 * F + src] * rd;
+    T = (U[3 * F + src] - (uu * U[F + src] + v * U[2 * F + src]) * 0.5) * (rd * c.rCv);
+  }
+  const double d2 = __shfl_sync(0xffffffffu, d, 1), u2 = __shfl_sync(0xffffffffu, uu, 1);
+  const double v2 = __shfl_sync(0xffffffffu, v, 1), T2 = __shfl_sync(0xffffffffu, T, 1);
+  const double d3 = __shfl_sync(0xffffffffu, d, 2), u3 = __shfl_sync(0xffffffffu, uu, 2);
+  const double v3 = __shfl_sync(0xffffffffu, v, 2), T3 = __shfl_sync(0xffffffffu, T, 2);
+  if (lane != 0) return;
+  const double Cv = c.Cv;
+  double d4 = d + d3 - d2, uu4 = uu + u3 - u2, v4 = v + v3 - v2, T4 = T + T3 - T2;
   U[i4] = d4;
   U[F + i4] = d4 * uu4;
   U[2 * F + i4] = d4 * v4;
@@ -270,10 +282,11 @@ __global__ void __launch_bounds__(256) k_bc(Lvl L, int phases) {
   }
   if (phases & 4) {
     int nx = b.nx, ny = b.ny;
-    if (threadIdx.x == 0) corner(L, c, fidx(b, 1, 0), fidx(b, 1, 1), fidx(b, 0, 1), fidx(b, 0, 0));
-    if (threadIdx.x == 32) corner(L, c, fidx(b, 1, ny), fidx(b, 1, ny - 1), fidx(b, 0, ny - 1), fidx(b, 0, ny));
-    if (threadIdx.x == 64) corner(L, c, fidx(b, nx - 1, 0), fidx(b, nx - 1, 1), fidx(b, nx, 1), fidx(b, nx, 0));
-    if (threadIdx.x == 96) corner(L, c, fidx(b, nx - 1, ny), fidx(b, nx - 1, ny - 1), fidx(b, nx, ny - 1), fidx(b, nx, ny));
+    const int w = threadIdx.x >> 5;
+    if (w == 0) corner(L, c, fidx(b, 1, 0), fidx(b, 1, 1), fidx(b, 0, 1), fidx(b, 0, 0));
+    else if (w == 1) corner(L, c, fidx(b, 1, ny), fidx(b, 1, ny - 1), fidx(b, 0, ny - 1), fidx(b, 0, ny));
+    else if (w == 2) corner(L, c, fidx(b, nx - 1, 0), fidx(b, nx - 1, 1), fidx(b, nx, 1), fidx(b, nx, 0));
+    else if (w == 3) corner(L, c, fidx(b, nx - 1, ny), fidx(b, nx - 1, ny - 1), fidx(b, nx, ny - 1), fidx(b, nx, ny));
     __syncthreads();
   }
   if ((phases & 8) && L.nvar >= 5) {

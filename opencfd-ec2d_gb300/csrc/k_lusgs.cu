@@ -184,8 +184,8 @@ __global__ void k_new_u(Lvl L) {
 }
 
 // restriction fine -> coarse (interpolation2h, sub_NS_multigrid.f90:349-398):
-// flag 1 volume-weighted U, flag 2 residual sum into QF.  Runs over the
-// coarse level's tiles.
+// flag 1 volume-weighted U, flag 2 residual sum into QF, 3 both.  Runs over
+// the coarse level's tiles.
 __global__ void k_restrict(Lvl Lf, Lvl Lc, int flag) {
   int bk, i, j;
   if (!tile_cell(Lc, bk, i, j, 1, 1)) return;
@@ -194,14 +194,15 @@ __global__ void k_restrict(Lvl Lf, Lvl Lc, int flag) {
   long long f11 = fidx(bf, 2 * i - 1, 2 * j - 1), f12 = fidx(bf, 2 * i - 1, 2 * j);
   long long f21 = fidx(bf, 2 * i, 2 * j - 1), f22 = fidx(bf, 2 * i, 2 * j);
   const long long FF = Lf.F, FC = Lc.F;
-  if (flag == 1) {
+  if (flag & 1) {
     const double *vf = Lf.geo + G_VOL * FF;
     double vc = Lc.geo[G_VOL * FC + ic];
     for (int m = 0; m < 4; m++) {
       const double *u = Lf.U + m * FF;
       Lc.U[m * FC + ic] = (u[f11] * vf[f11] + u[f12] * vf[f12] + u[f21] * vf[f21] + u[f22] * vf[f22]) / vc;
     }
-  } else {
+  }
+  if (flag & 2) {
     for (int m = 0; m < 4; m++) {
       const double *r = Lf.res + m * FF;
       Lc.qf[m * FC + ic] = r[f11] + r[f12] + r[f21] + r[f22];
@@ -210,7 +211,9 @@ __global__ void k_restrict(Lvl Lf, Lvl Lc, int flag) {
 }
 
 // prolongation coarse -> fine (prolong_U, sub_NS_multigrid.f90:271-343), over
-// fine cells 0..nx2, 0..ny2; flag 1 interpolates U, flag 2 deltU.
+// fine cells 0..nx2, 0..ny2; flag 1 interpolates U, flag 2 deltU, flag 3
+// deltU and then U += deltU on the fine interior (comput_new_U,
+// sub_NS_multigrid.f90:240-260) in the same pass.
 __global__ void k_prolong(Lvl Lc, Lvl Lf, int flag) {
   int bk, i, j;
   if (!tile_cell(Lf, bk, i, j, 0, 0)) return;
@@ -222,9 +225,12 @@ __global__ void k_prolong(Lvl Lc, Lvl Lf, int flag) {
   long long id = fidx(bf, i, j);
   const double *src = (flag == 1) ? Lc.U : Lc.deltu;
   double *dst = (flag == 1) ? Lf.U : Lf.deltu;
+  const bool add = flag == 3 && i >= 1 && i <= bf.nx - 1 && j >= 1 && j <= bf.ny - 1;
   for (int m = 0; m < 4; m++) {
     const double *s = src + m * Lc.F;
-    dst[m * Lf.F + id] = a1 * s[c11] + a2 * (s[c21] + s[c12]) + a3 * s[c22];
+    const double v = a1 * s[c11] + a2 * (s[c21] + s[c12]) + a3 * s[c22];
+    dst[m * Lf.F + id] = v;
+    if (add) Lf.U[m * Lf.F + id] = Lf.U[m * Lf.F + id] + v;
   }
 }
 

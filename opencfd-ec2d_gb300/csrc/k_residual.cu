@@ -252,12 +252,20 @@ __device__ __forceinline__ void final_norm(const Lvl &L, int cs, int m) {
   if (lane == 0) L.norms[cs * 12 + m] = out;
 }
 
+// post: RES_ADD_FORCE (Res += QF once the norms are taken), RES_FORCE_FN
+// (QF -= Res), RES_SET_UN (Un = U over 0..nx, 0..ny): the multigrid steps
+// that follow a residual evaluation, done in the same pass
 template <bool NORM, bool FINAL>
-__global__ void __launch_bounds__(TILE) k_res(Lvl L) {
+__global__ void __launch_bounds__(TILE) k_res(Lvl L, int post) {
   int bk, i, j;
   bool act = tile_ij(L, bk, i, j);
   if (act) {
     const BlkDev &b0 = L.blk[bk];
+    if ((post & RES_SET_UN) && i >= 0 && i <= b0.nx && j >= 0 && j <= b0.ny) {
+      const long long id = fidx(b0, i, j);
+#pragma unroll
+      for (int m = 0; m < 4; m++) L.un[m * L.F + id] = L.U[m * L.F + id];
+    }
     act = i >= 1 && i <= b0.nx - 1 && j >= 1 && j <= b0.ny - 1;
   }
   if (!NORM && !act) return;
@@ -272,8 +280,13 @@ __global__ void __launch_bounds__(TILE) k_res(Lvl L) {
 #pragma unroll
       for (int m = 0; m < 4; m++) {
         double r = L.fi[m * F + id + 1] - L.fi[m * F + id] + L.fj[m * F + id + P] - L.fj[m * F + id];
-        L.res[m * F + id] = r;
         vres[m] = r;
+        if (post & (RES_ADD_FORCE | RES_FORCE_FN)) {
+          const double qf = L.qf[m * F + id];
+          if (post & RES_FORCE_FN) L.qf[m * F + id] = qf - r;
+          if (post & RES_ADD_FORCE) r = r + qf;
+        }
+        L.res[m * F + id] = r;
       }
     }
     if (NORM)
@@ -357,12 +370,12 @@ void launch_flux_j(const Lvl &L, bool fp32, cudaStream_t s) {
   else k_flux_j<double><<<L.ntiles, TILE, 0, s>>>(L);
 }
 // with_norms: the tile partials inside k_res; with few cases the last CTA of
-// k_res also forms the per-case norms (fused_final() tells the caller)
+// k_res also forms the per-case norms (norms_fused_final() tells the caller)
 bool norms_fused_final(const Lvl &L) { return L.ncase <= 8; }
-void launch_res(const Lvl &L, bool with_norms, cudaStream_t s) {
-  if (!with_norms) k_res<false, false><<<L.ntiles, TILE, 0, s>>>(L);
-  else if (norms_fused_final(L)) k_res<true, true><<<L.ntiles, TILE, 0, s>>>(L);
-  else k_res<true, false><<<L.ntiles, TILE, 0, s>>>(L);
+void launch_res(const Lvl &L, bool with_norms, int post, cudaStream_t s) {
+  if (!with_norms) k_res<false, false><<<L.ntiles, TILE, 0, s>>>(L, post);
+  else if (norms_fused_final(L)) k_res<true, true><<<L.ntiles, TILE, 0, s>>>(L, post);
+  else k_res<true, false><<<L.ntiles, TILE, 0, s>>>(L, post);
 }
 void launch_norms(const Lvl &L, bool partials, cudaStream_t s) {
   if (partials) k_norm_partial<<<L.ntiles, TILE, 0, s>>>(L);
