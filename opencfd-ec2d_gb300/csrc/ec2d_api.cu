@@ -300,6 +300,7 @@ CaseDev make_casedev(const ec2d_params &p) {
   c.rMa = 1.0 / p.Ma;
   c.rRe = 1.0 / p.Re;
   c.rgm1 = 1.0 / (p.gamma - 1.0);
+  c.ggm1 = p.gamma / (p.gamma - 1.0);
   c.Cv = 1.0 / (p.gamma * (p.gamma - 1.0) * p.Ma * p.Ma);
   c.rCv = p.gamma * (p.gamma - 1.0) * p.Ma * p.Ma;
   c.Cp = c.Cv * p.gamma;
@@ -585,6 +586,8 @@ int build_level(ec2d_ctx *ctx, int l) {
     CK(cudaMemcpy(L.un, un.data(), un.size() * sizeof(double), cudaMemcpyHostToDevice));
     if (anyfdm) CK(cudaMemcpy(L.met, met.data(), met.size() * sizeof(double), cudaMemcpyHostToDevice));
   }
+  launch_face_metrics(L, ctx->stream);
+  CK(cudaGetLastError());
   if (L.bcn) {
     launch_bc_normals(L, lv.bc_max_nodes, ctx->stream);
     CK(cudaGetLastError());

@@ -31,8 +31,13 @@ enum { Turb_NONE = 0, Turb_BL = 1, Turb_SA = 2, Turb_SST = 3 };
 // primitive planes in Lvl::q
 enum { Q_D = 0, Q_U = 1, Q_V = 2, Q_T = 3, Q_P = 4, Q_C = 5, NQ = 6 };
 // geometry planes in Lvl::geo
+// G_VI*, G_VJ*: the face-local inverse Jacobian of the viscous terms of an i-
+// or j-face, (Djy, Diy, Djx, Dix) / (Dix Djy - Djx Diy), formed at set-up
+// (k_face_metrics) from the cell centres
 enum { G_VOL = 0, G_SI = 1, G_SJ = 2, G_NI1 = 3, G_NI2 = 4, G_NJ1 = 5, G_NJ2 = 6,
-       G_X = 7, G_Y = 8, G_X1 = 9, G_Y1 = 10, G_DW = 11, NG = 12 };
+       G_X = 7, G_Y = 8, G_X1 = 9, G_Y1 = 10, G_DW = 11,
+       G_VIA = 12, G_VIB = 13, G_VIC = 14, G_VID = 15, G_VJA = 16, G_VJB = 17, G_VJC = 18, G_VJD = 19,
+       NG = 20 };
 // spectral-radius / time-step planes in Lvl::lc
 enum { L_CI = 0, L_CJ = 1, L_VI = 2, L_VJ = 3, L_DT = 4, NL = 5 };
 
@@ -61,6 +66,7 @@ struct CaseDev {
   double xaxis, yaxis;
   double rPr, rCv, rMa, rRe;  // 1/Pr, 1/Cv, 1/Ma, 1/Re
   double rgm1;                // 1/(gamma - 1)
+  double ggm1;                // gamma/(gamma - 1)
   int local_dt, pad;
 };
 
@@ -286,12 +292,12 @@ __device__ __forceinline__ void reconstruct(int recon, int scheme, T S0[4][4], T
 // ---- 1-D face fluxes on rotated primitive states (rho, u_n, u_t, p) ----------
 // Flux_Roe_1D, sub_flux_split.f90:265-324 (Harten entropy fix, delta = 0.1)
 template <typename T>
-__device__ __forceinline__ void flux_roe(const T *QL, const T *QR, T *F, T gamma) {
+__device__ __forceinline__ void flux_roe(const T *QL, const T *QR, T *F, T gamma, T ggm1) {
   const T delt = T(0.1);
   T dl = QL[0], uul = QL[1], vvl = QL[2], pl = QL[3];
   T dr = QR[0], uur = QR[1], vvr = QR[2], pr = QR[3];
   T gm1 = gamma - T(1.0);
-  const T rdl = rcp(dl), rdr = rcp(dr), ggm1 = gamma * rcp(gm1);
+  const T rdl = rcp(dl), rdr = rcp(dr);
   T hl = ggm1 * pl * rdl + T(0.5) * (uul * uul + vvl * vvl);
   T hr = ggm1 * pr * rdr + T(0.5) * (uur * uur + vvr * vvr);
   T Fl0 = dl * uul, Fl1 = dl * uul * uul + pl, Fl2 = dl * uul * vvl, Fl3 = uul * dl * hl;
@@ -325,14 +331,14 @@ __device__ __forceinline__ void flux_roe(const T *QL, const T *QR, T *F, T gamma
 
 // Flux_Ausm_1Da (AUSM+), sub_flux_split.f90:195-261
 template <typename T>
-__device__ __forceinline__ void flux_ausm(const T *QL, const T *QR, T *F, T gamma) {
+__device__ __forceinline__ void flux_ausm(const T *QL, const T *QR, T *F, T gamma, T ggm1) {
   T dl = QL[0], uul = QL[1], vvl = QL[2], pl = QL[3];
   T dr = QR[0], uur = QR[1], vvr = QR[2], pr = QR[3];
-  T gm1 = gamma - T(1.0);
-  const T rdl = rcp(dl), rdr = rcp(dr), ggm1 = gamma * rcp(gm1);
-  T hl = ggm1 * pl * rdl + T(0.5) * (uul * uul + vvl * vvl);
-  T hr = ggm1 * pr * rdr + T(0.5) * (uur * uur + vvr * vvr);
-  T al = sqrt(gamma * pl * rdl), ar = sqrt(gamma * pr * rdr);
+  const T rdl = rcp(dl), rdr = rcp(dr);
+  const T prl = pl * rdl, prr = pr * rdr;  // p / rho
+  T hl = ggm1 * prl + T(0.5) * (uul * uul + vvl * vvl);
+  T hr = ggm1 * prr + T(0.5) * (uur * uur + vvr * vvr);
+  T al = sqrt(gamma * prl), ar = sqrt(gamma * prr);
   T a = T(0.5) * (al + ar);
   T ia = rcp(a);
   T Ml = uul * ia, Mr = uur * ia;
@@ -348,7 +354,7 @@ __device__ __forceinline__ void flux_ausm(const T *QL, const T *QR, T *F, T gamm
   T xm = dl * a * fmax(T(0.0), M) + dr * a * fmin(T(0.0), M);
   T dm = (M >= T(0.0)) ? a * fabs(M) * dl : a * fabs(M) * dr;
   T p = pl * Pp5 + pr * Pm5;
-  F[0] = T(0.5) * xm * (T(1.0) + T(1.0)) - T(0.5) * dm * (T(1.0) - T(1.0));
+  F[0] = xm;  // 0.5 xm (1 + 1) - 0.5 dm (1 - 1): the same value for finite xm, dm
   F[1] = T(0.5) * xm * (uul + uur) - T(0.5) * dm * (uur - uul) + p;
   F[2] = T(0.5) * xm * (vvl + vvr) - T(0.5) * dm * (vvr - vvl);
   F[3] = T(0.5) * xm * (hl + hr) - T(0.5) * dm * (hr - hl);
@@ -455,10 +461,10 @@ __device__ __forceinline__ void flux_hll(const T *QL, const T *QR, T *F, T gamma
 }
 
 template <typename T>
-__device__ __forceinline__ void face_flux(int iflux, const T *QL, const T *QR, T *F, T gamma) {
+__device__ __forceinline__ void face_flux(int iflux, const T *QL, const T *QR, T *F, T gamma, T ggm1) {
   switch (iflux) {
-    case Flux_Roe: flux_roe(QL, QR, F, gamma); return;
-    case Flux_Ausm: flux_ausm(QL, QR, F, gamma); return;
+    case Flux_Roe: flux_roe(QL, QR, F, gamma, ggm1); return;
+    case Flux_Ausm: flux_ausm(QL, QR, F, gamma, ggm1); return;
     case Flux_VanLeer: flux_vanleer(QL, QR, F, gamma); return;
     case Flux_SW: flux_sw(QL, QR, F, gamma); return;
     case Flux_HLL: flux_hll(QL, QR, F, gamma, false); return;
@@ -477,6 +483,23 @@ __device__ __forceinline__ void viscous_face(T Dix, T Diy, T Djx, T Djy, T Diu, 
   T Ds = rcp(Dix * Djy - Djx * Diy);
   T ux = (Diu * Djy - Dju * Diy) * Ds, vx = (Div * Djy - Djv * Diy) * Ds, Tx = (DiT * Djy - DjT * Diy) * Ds;
   T uy = (-Diu * Djx + Dju * Dix) * Ds, vy = (-Div * Djx + Djv * Dix) * Ds, Ty = (-DiT * Djx + DjT * Dix) * Ds;
+  T t11 = ((T(4.0) / T(3.0)) * ux - (T(2.0) / T(3.0)) * vy) * Amu1;
+  T t22 = ((T(4.0) / T(3.0)) * vy - (T(2.0) / T(3.0)) * ux) * Amu1;
+  T t12 = (uy + vx) * Amu1;
+  T E1 = u1 * t11 + v1 * t12 + Amk1 * Tx, E2 = u1 * t12 + v1 * t22 + Amk1 * Ty;
+  F2 += (t11 * n1 + t12 * n2) * s;
+  F3 += (t12 * n1 + t22 * n2) * s;
+  F4 += (E1 * n1 + E2 * n2) * s;
+}
+
+// the same from the face's precomputed inverse Jacobian (A, B, C, D) =
+// (Djy, Diy, Djx, Dix) / (Dix Djy - Djx Diy): u_x = Diu A - Dju B,
+// u_y = Dju D - Diu C
+template <typename T>
+__device__ __forceinline__ void viscous_face_m(T A, T B, T C, T D, T Diu, T Div, T DiT, T Dju, T Djv, T DjT,
+                                               T Amu1, T Amk1, T u1, T v1, T n1, T n2, T s, T &F2, T &F3, T &F4) {
+  T ux = fma(Diu, A, -Dju * B), vx = fma(Div, A, -Djv * B), Tx = fma(DiT, A, -DjT * B);
+  T uy = fma(Dju, D, -Diu * C), vy = fma(Djv, D, -Div * C), Ty = fma(DjT, D, -DiT * C);
   T t11 = ((T(4.0) / T(3.0)) * ux - (T(2.0) / T(3.0)) * vy) * Amu1;
   T t22 = ((T(4.0) / T(3.0)) * vy - (T(2.0) / T(3.0)) * ux) * Amu1;
   T t12 = (uy + vx) * Amu1;

@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(TILE) k_flux_i(Lvl L) {
   T QL[4] = {UL[0], UL[1] * n1 + UL[2] * n2, -UL[1] * n2 + UL[2] * n1, UL[3]};
   T QR[4] = {UR[0], UR[1] * n1 + UR[2] * n2, -UR[1] * n2 + UR[2] * n1, UR[3]};
   T Fl[4];
-  face_flux(L.flux, QL, QR, Fl, (T)c.gamma);
+  face_flux(L.flux, QL, QR, Fl, (T)c.gamma, (T)c.ggm1);
   T F0 = -Fl[0] * si, F1 = -(Fl[1] * n1 - Fl[2] * n2) * si, F2 = -(Fl[1] * n2 + Fl[2] * n1) * si, F3 = -Fl[3] * si;
   if (L.visc) {
     long long w = id - 1, nN = id + b.P, nS = id - b.P;
@@ -108,17 +108,15 @@ __global__ void __launch_bounds__(TILE) k_flux_i(Lvl L) {
       Amu1 = ((T)L.amu[w] + (T)L.amu[id] + (T)L.amut[w] + (T)L.amut[id]) * T(0.5);
       Amk1 = (T)c.Cp * (((T)L.amu[w] + (T)L.amu[id]) * (T)c.rPr + ((T)L.amut[w] + (T)L.amut[id]) * (T)(1.0 / PrT)) * T(0.5);
     }
-    const double *x1 = L.geo + G_X1 * F, *y1 = L.geo + G_Y1 * F;
     const double *uu = L.q + Q_U * F, *vv = L.q + Q_V * F, *TT = L.q + Q_T * F;
-    T Dix = (T)x1[id] - (T)x1[w], Diy = (T)y1[id] - (T)y1[w];
-    T Djx = ((T)x1[nN - 1] + (T)x1[nN] - (T)x1[nS - 1] - (T)x1[nS]) * T(0.25);
-    T Djy = ((T)y1[nN - 1] + (T)y1[nN] - (T)y1[nS - 1] - (T)y1[nS]) * T(0.25);
+    const double *g = L.geo + id;
     T Diu = (T)uu[id] - (T)uu[w], Div = (T)vv[id] - (T)vv[w], DiT = (T)TT[id] - (T)TT[w];
     T Dju = ((T)uu[nN - 1] + (T)uu[nN] - (T)uu[nS - 1] - (T)uu[nS]) * T(0.25);
     T Djv = ((T)vv[nN - 1] + (T)vv[nN] - (T)vv[nS - 1] - (T)vv[nS]) * T(0.25);
     T DjT = ((T)TT[nN - 1] + (T)TT[nN] - (T)TT[nS - 1] - (T)TT[nS]) * T(0.25);
     T u1 = ((T)uu[id] + (T)uu[w]) * T(0.5), v1 = ((T)vv[id] + (T)vv[w]) * T(0.5);
-    viscous_face(Dix, Diy, Djx, Djy, Diu, Div, DiT, Dju, Djv, DjT, Amu1, Amk1, u1, v1, n1, n2, si, F1, F2, F3);
+    viscous_face_m((T)g[G_VIA * F], (T)g[G_VIB * F], (T)g[G_VIC * F], (T)g[G_VID * F], Diu, Div, DiT, Dju, Djv, DjT,
+                   Amu1, Amk1, u1, v1, n1, n2, si, F1, F2, F3);
   }
   L.fi[id] = F0; L.fi[F + id] = F1; L.fi[2 * F + id] = F2; L.fi[3 * F + id] = F3;
 }
@@ -157,7 +155,7 @@ __global__ void __launch_bounds__(TILE) k_flux_j(Lvl L) {
   T QL[4] = {UL[0], UL[1] * n1 + UL[2] * n2, -UL[1] * n2 + UL[2] * n1, UL[3]};
   T QR[4] = {UR[0], UR[1] * n1 + UR[2] * n2, -UR[1] * n2 + UR[2] * n1, UR[3]};
   T Fl[4];
-  face_flux(L.flux, QL, QR, Fl, (T)c.gamma);
+  face_flux(L.flux, QL, QR, Fl, (T)c.gamma, (T)c.ggm1);
   T F0 = -Fl[0] * sj, F1 = -(Fl[1] * n1 - Fl[2] * n2) * sj, F2 = -(Fl[1] * n2 + Fl[2] * n1) * sj, F3 = -Fl[3] * sj;
   if (L.visc) {
     long long s = id - P;
@@ -172,27 +170,19 @@ __global__ void __launch_bounds__(TILE) k_flux_j(Lvl L) {
       Amu1 = ((T)L.amu[id] + (T)L.amu[s] + (T)L.amut[id] + (T)L.amut[s]) * T(0.5);
       Amk1 = (T)c.Cp * (((T)L.amu[s] + (T)L.amu[id]) * (T)c.rPr + ((T)L.amut[s] + (T)L.amut[id]) * (T)(1.0 / PrT)) * T(0.5);
     }
-    const double *x1 = L.geo + G_X1 * F, *y1 = L.geo + G_Y1 * F;
     const double *uu = L.q + Q_U * F, *vv = L.q + Q_V * F, *TT = L.q + Q_T * F;
-    T Dix = ((T)x1[s + 1] + (T)x1[id + 1] - (T)x1[s - 1] - (T)x1[id - 1]) * T(0.25);
-    T Diy = ((T)y1[s + 1] + (T)y1[id + 1] - (T)y1[s - 1] - (T)y1[id - 1]) * T(0.25);
-    T Djx = (T)x1[id] - (T)x1[s], Djy = (T)y1[id] - (T)y1[s];
+    const double *g = L.geo + id;
     T Diu = ((T)uu[s + 1] + (T)uu[id + 1] - (T)uu[s - 1] - (T)uu[id - 1]) * T(0.25);
     T Div = ((T)vv[s + 1] + (T)vv[id + 1] - (T)vv[s - 1] - (T)vv[id - 1]) * T(0.25);
     T DiT = ((T)TT[s + 1] + (T)TT[id + 1] - (T)TT[s - 1] - (T)TT[id - 1]) * T(0.25);
     T Dju = (T)uu[id] - (T)uu[s], Djv = (T)vv[id] - (T)vv[s], DjT = (T)TT[id] - (T)TT[s];
     T u1 = ((T)uu[id] + (T)uu[s]) * T(0.5), v1 = ((T)vv[id] + (T)vv[s]) * T(0.5);
-    viscous_face(Dix, Diy, Djx, Djy, Diu, Div, DiT, Dju, Djv, DjT, Amu1, Amk1, u1, v1, n1, n2, sj, F1, F2, F3);
+    viscous_face_m((T)g[G_VJA * F], (T)g[G_VJB * F], (T)g[G_VJC * F], (T)g[G_VJD * F], Diu, Div, DiT, Dju, Djv, DjT,
+                   Amu1, Amk1, u1, v1, n1, n2, sj, F1, F2, F3);
   }
   L.fj[id] = F0; L.fj[F + id] = F1; L.fj[2 * F + id] = F2; L.fj[3 * F + id] = F3;
 }
 
-// flux differences (sub_Residual.f90:460-468), comput_Lvc (sub_NS_singlegrid.f90:352-388)
-// and comput_dt (sub_NS_singlegrid.f90:324-348) for interior cells
-// NORM: also the tile's partial norms of Res (the work of k_norm_partial,
-// same cells, same reduction tree, so the norms are bit-identical); only when
-// no later kernel of the residual stage changes Res (no FDM patch, no
-// dual-time term)
 // Norm reductions.  max |Res| is reduced on the bit patterns: for
 // non-negative doubles the order of the patterns as signed 64-bit integers is
 // the order of the values, so the maxima run on the integer pipes (an FP64
@@ -252,6 +242,12 @@ __device__ __forceinline__ void final_norm(const Lvl &L, int cs, int m) {
   if (lane == 0) L.norms[cs * 12 + m] = out;
 }
 
+// flux differences (sub_Residual.f90:460-468), comput_Lvc (sub_NS_singlegrid.f90:352-388)
+// and comput_dt (sub_NS_singlegrid.f90:324-348) for interior cells
+// NORM: also the tile's partial norms of Res (the work of k_norm_partial,
+// same cells, same reduction tree, so the norms are bit-identical); only when
+// no later kernel of the residual stage changes Res (no FDM patch, no
+// dual-time term)
 // post: RES_ADD_FORCE (Res += QF once the norms are taken), RES_FORCE_FN
 // (QF -= Res), RES_SET_UN (Un = U over 0..nx, 0..ny): the multigrid steps
 // that follow a residual evaluation, done in the same pass
@@ -359,6 +355,35 @@ __global__ void __launch_bounds__(384) k_norm_final(Lvl L) {
   const int k = blockIdx.x * 12 + (threadIdx.x >> 5);
   final_norm(L, k / 12, k % 12);
 }
+
+// set-up: the viscous inverse Jacobians of the i-faces (i = 1..nx, j =
+// 1..ny-1) and j-faces (i = 1..nx-1, j = 1..ny) from the cell centres, with the
+// stencils of Residual_FVM (sub_Residual.f90:313-330, 419-436)
+__global__ void __launch_bounds__(TILE) k_face_metrics(Lvl L) {
+  int bk, i, j;
+  if (!tile_ij(L, bk, i, j)) return;
+  const BlkDev &b = L.blk[bk];
+  const long long F = L.F, P = b.P, id = fidx(b, i, j);
+  const double *x1 = L.geo + G_X1 * F, *y1 = L.geo + G_Y1 * F;
+  double *g = L.geo + id;
+  if (i >= 1 && i <= b.nx && j >= 1 && j <= b.ny - 1) {
+    const long long w = id - 1, nN = id + P, nS = id - P;
+    const double Dix = x1[id] - x1[w], Diy = y1[id] - y1[w];
+    const double Djx = (x1[nN - 1] + x1[nN] - x1[nS - 1] - x1[nS]) * 0.25;
+    const double Djy = (y1[nN - 1] + y1[nN] - y1[nS - 1] - y1[nS]) * 0.25;
+    const double Ds = 1.0 / (Dix * Djy - Djx * Diy);
+    g[G_VIA * F] = Djy * Ds; g[G_VIB * F] = Diy * Ds; g[G_VIC * F] = Djx * Ds; g[G_VID * F] = Dix * Ds;
+  }
+  if (i >= 1 && i <= b.nx - 1 && j >= 1 && j <= b.ny) {
+    const long long s = id - P;
+    const double Dix = (x1[s + 1] + x1[id + 1] - x1[s - 1] - x1[id - 1]) * 0.25;
+    const double Diy = (y1[s + 1] + y1[id + 1] - y1[s - 1] - y1[id - 1]) * 0.25;
+    const double Djx = x1[id] - x1[s], Djy = y1[id] - y1[s];
+    const double Ds = 1.0 / (Dix * Djy - Djx * Diy);
+    g[G_VJA * F] = Djy * Ds; g[G_VJB * F] = Diy * Ds; g[G_VJC * F] = Djx * Ds; g[G_VJD * F] = Dix * Ds;
+  }
+}
+void launch_face_metrics(const Lvl &L, cudaStream_t s) { k_face_metrics<<<L.ntiles, TILE, 0, s>>>(L); }
 
 void launch_prim(const Lvl &L, cudaStream_t s) { k_prim<<<L.ntiles, TILE, 0, s>>>(L); }
 void launch_flux_i(const Lvl &L, bool fp32, cudaStream_t s) {
