@@ -330,6 +330,170 @@ __device__ __forceinline__ void sweep_pass(const Lvl &L, const BlkDev &bd, doubl
   }
 }
 
+// Narrow blocks (the coarse multigrid levels): LPR lanes per row, each lane
+// owning some of the row's variables.  An FP64 warp instruction costs the
+// same whatever the number of active lanes, so spreading one cell's
+// accumulation over 2 or 4 lanes of the same instruction stream shortens the
+// chain per plane (21 FP64 operations instead of 31 with four lanes) as long
+// as the rows times LPR still fit one warp per SM sub-partition.  Lane q of a row owns
+// the variables var(q, k); both neighbours' states come from the shared
+// slots (the own row's previous cell included), the mean flow of U + dU is
+// gathered across the row's lanes by shuffles, and every lane forms u, v, p.
+template <int NV, int LPR>
+struct Lanes {
+  static constexpr int MV = 4 / LPR;                    // mean-flow variables per lane
+  static constexpr int TV = (NV - 4 + LPR - 1) / LPR;   // turbulence variables per lane
+  static constexpr int VPL = MV + TV;
+  __device__ static int var(int q, int k) { return k < MV ? q * MV + k : 4 + (k - MV) * LPR + q; }
+  __host__ __device__ static constexpr int lane_of(int m) { return m < 4 ? m / MV : (m - 4) % LPR; }
+  __host__ __device__ static constexpr int reg_of(int m) { return m < 4 ? m % MV : MV + (m - 4) / LPR; }
+};
+template <int NV, int LPR>
+struct CurL {
+  double a[Lanes<NV, LPR>::VPL], u[Lanes<NV, LPR>::VPL], c0[Lanes<NV, LPR>::VPL];
+  double ci, cj, ia, ia5, n1i, n2i, n1j, n2j;
+};
+
+template <int NV, bool update, bool FWD, int LPR>
+__device__ __forceinline__ void sweep_pass_lanes(const Lvl &L, const BlkDev &bd, double *sh, const double *rsrc,
+                                                 double *recBw, int R, int rl, int q, int gbase, int j, bool row_ok,
+                                                 double gm1) {
+  using SL = Slot<NV>;
+  using RC = Rec<NV>;
+  using LN = Lanes<NV, LPR>;
+  constexpr int S = SL::S, VPL = LN::VPL;
+  const int nx = bd.nx, ny = bd.ny, rows = ny - 1, ni = nx - 1;
+  const long long F = L.F;
+  int mv[VPL];
+  bool ok[VPL];
+#pragma unroll
+  for (int k = 0; k < VPL; k++) {
+    const int m = LN::var(q, k);
+    ok[k] = m < NV;
+    mv[k] = ok[k] ? m : 0;
+  }
+  auto src = [&](int k) { return rsrc + (size_t)(FWD ? k : ni - 1 - k) * RC::N; };
+  auto load = [&](CurL<NV, LPR> &c, const double *r) {
+#pragma unroll
+    for (int k = 0; k < VPL; k++) {
+      c.a[k] = __ldcg(r + RC::A + mv[k]);
+      c.u[k] = __ldcg(r + RC::U + mv[k]);
+      if (!FWD) c.c0[k] = __ldcg(r + RC::C0 + mv[k]);
+    }
+    c.ci = __ldcg(r + RC::CI); c.cj = __ldcg(r + RC::CJ); c.ia = __ldcg(r + RC::IA); c.ia5 = __ldcg(r + RC::IA5);
+    c.n1i = __ldcg(r + RC::N1I); c.n2i = __ldcg(r + RC::N2I); c.n1j = __ldcg(r + RC::N1J); c.n2j = __ldcg(r + RC::N2J);
+  };
+  CurL<NV, LPR> cur, nxt;
+  if (row_ok) load(cur, src(0));
+  int k = 0;
+  for (int pp = 2; pp <= nx + ny - 2; pp++) {
+    const int p = FWD ? pp : nx + ny - pp;
+    const int i = p - j;
+    const int buf = p & 1;
+    const bool act = row_ok && i >= 1 && i <= ni;
+    const bool more = act && k + 1 < ni;
+    double myst[VPL], dn[VPL];
+#pragma unroll
+    for (int kk = 0; kk < VPL; kk++) myst[kk] = dn[kk] = 0.0;
+    if (act) {
+      if (more) load(nxt, src(k + 1));
+      double acc[VPL];
+#pragma unroll
+      for (int kk = 0; kk < VPL; kk++) acc[kk] = FWD ? cur.a[kk] : cur.c0[kk];
+      // acc += F_n(U2, s) + cc U2 of a neighbour from its shared slot, own variables only
+      auto add_nb = [&](const double *sl, double n1, double n2, double cc) {
+        const double pn = sl[SL::P];
+        const double un = fma(sl[SL::U], n1, sl[SL::V] * n2), w = un + cc;
+#pragma unroll
+        for (int kk = 0; kk < VPL; kk++) {
+          const int m = mv[kk];
+          const double coef = m == 1 ? n1 : m == 2 ? n2 : m == 3 ? un : 0.0;
+          acc[kk] = fma(sl[m], w, fma(pn, coef, acc[kk]));
+        }
+      };
+      if (FWD ? (i > 1) : (i < ni)) add_nb(sh + ((size_t)(buf ^ 1) * (R + 2) + rl + 1) * S, cur.n1i, cur.n2i, cur.ci);
+      if (FWD ? (j > 1) : (j < rows))
+        add_nb(sh + ((size_t)(buf ^ 1) * (R + 2) + (FWD ? rl : rl + 2)) * S, cur.n1j, cur.n2j, cur.cj);
+#pragma unroll
+      for (int kk = 0; kk < VPL; kk++) {
+        const double inv = (NV == 5 && mv[kk] == 4) ? cur.ia5 : cur.ia;
+        if (update) {
+          myst[kk] = fma(acc[kk], inv, FWD ? cur.u[kk] : cur.a[kk]);
+        } else {
+          dn[kk] = FWD ? acc[kk] * inv : fma(acc[kk], inv, cur.a[kk]);
+          myst[kk] = cur.u[kk] + dn[kk];
+        }
+      }
+    }
+    // every lane of the warp takes part in the gathers
+    double s4[4];
+#pragma unroll
+    for (int m = 0; m < 4; m++) s4[m] = __shfl_sync(0xffffffffu, myst[LN::reg_of(m)], gbase + LN::lane_of(m));
+    if (act) {
+      const double rd = rcp(s4[0]);
+      const double u = s4[1] * rd, v = s4[2] * rd;
+      const double pr = gm1 * fma(-0.5, fma(s4[2], v, s4[1] * u), s4[3]);
+      double *own = sh + ((size_t)buf * (R + 2) + rl + 1) * S;
+#pragma unroll
+      for (int kk = 0; kk < VPL; kk++)
+        if (ok[kk]) own[mv[kk]] = myst[kk];
+      if (q == 0) { own[SL::U] = u; own[SL::V] = v; own[SL::P] = pr; }
+      if (FWD) {
+        double *w = recBw + (size_t)(i - 1) * RC::N;
+#pragma unroll
+        for (int kk = 0; kk < VPL; kk++)
+          if (ok[kk]) w[RC::A + mv[kk]] = update ? myst[kk] : dn[kk];
+      } else {
+        const long long id = bd.off + (long long)(j + 2) * bd.P + (i + 2);
+#pragma unroll
+        for (int kk = 0; kk < VPL; kk++) {
+          if (!ok[kk]) continue;
+          if (update) L.U[mv[kk] * F + id] = myst[kk];
+          else L.du[mv[kk] * F + id] = dn[kk];
+        }
+      }
+      if (more) cur = nxt;
+      k++;
+    }
+    __syncthreads();
+  }
+}
+
+template <int NV, bool update, int LPR>
+__global__ void __launch_bounds__(128) k_lusgs_sweep_lanes(Lvl L, int R) {
+  constexpr int S = Slot<NV>::S;
+  extern __shared__ __align__(16) double sh[];  // [2][R+2][S] slots
+  const BlkDev bd = L.blk[blockIdx.x];
+  const int rows = bd.ny - 1, ni = bd.nx - 1;
+  const int rl = threadIdx.x / LPR, q = threadIdx.x % LPR;
+  const int gbase = (threadIdx.x & 31) / LPR * LPR;
+  const int j = rl + 1;
+  const bool row_ok = rl < R && j <= rows;
+  const double gm1 = L.cs[bd.cas].gamma - 1.0;
+  const int jr = row_ok ? j : 1;  // record pointers of idle lanes stay in the array
+  const double *recF = L.rec + ((size_t)bd.cell0 + (size_t)(jr - 1) * ni) * Rec<NV>::N;
+  const double *recB = recF + (size_t)L.ncell * Rec<NV>::N;
+  double *recBw = L.rec + ((size_t)L.ncell + bd.cell0 + (size_t)(jr - 1) * ni) * Rec<NV>::N;
+  (void)S;
+  sweep_pass_lanes<NV, update, true, LPR>(L, bd, sh, recF, recBw, R, rl, q, gbase, j, row_ok, gm1);
+  sweep_pass_lanes<NV, update, false, LPR>(L, bd, sh, recB, recBw, R, rl, q, gbase, j, row_ok, gm1);
+}
+
+// lanes per row for a level whose widest block has `rows` rows: 4 when
+// rows x 4 fits one warp per sub-partition of one SM (128 lanes).  Two lanes
+// per row save 5 of 31 FP64 operations, less than the added loads, shuffles
+// and selects cost (2 x 48 x 48 level: 283 us against 276 us for one lane);
+// four save 10 (2 x 24 x 24 level: 124 us against 146 us).
+int sweep_lanes_per_row(int rows) { return rows * 4 <= 128 ? 4 : 1; }
+
+template <int NV, int LPR>
+void launch_lanes(const Lvl &L, int update, int R, cudaStream_t s) {
+  const int th = (R * LPR + 31) / 32 * 32;
+  const size_t smem = (size_t)2 * (R + 2) * Slot<NV>::S * sizeof(double);
+  if (update) k_lusgs_sweep_lanes<NV, true, LPR><<<L.nblk, th, smem, s>>>(L, R);
+  else k_lusgs_sweep_lanes<NV, false, LPR><<<L.nblk, th, smem, s>>>(L, R);
+}
+
 // CS == 1: one CTA per block, planes separated by __syncthreads.
 // CS > 1: a cluster of CS CTAs per block, CTA r owns rows r*R+1..r*R+R; the
 // edge rows write into the neighbour CTA's halo slot through distributed
@@ -369,6 +533,8 @@ size_t smem_bytes(int R, int th) {
 template <int NV>
 void sweep_nv(const Lvl &L, double alfa1, int update, int max_rows, int cs, int rpw, cudaStream_t s) {
   k_lusgs_prep<NV><<<L.ntiles, TILE, 0, s>>>(L, alfa1);
+  const int lpr = sweep_lanes_per_row(max_rows);
+  if (lpr == 4) { launch_lanes<NV, 4>(L, update, max_rows, s); return; }
   int CS = std::max(1, std::min(cs, std::min(8, (max_rows + 7) / 8)));
   int R = (max_rows + CS - 1) / CS;
   if (rpw < 1 || rpw > 32) rpw = 32;
