@@ -33,11 +33,14 @@ enum { Q_D = 0, Q_U = 1, Q_V = 2, Q_T = 3, Q_P = 4, Q_C = 5, NQ = 6 };
 // geometry planes in Lvl::geo
 // G_VI*, G_VJ*: the face-local inverse Jacobian of the viscous terms of an i-
 // or j-face, (Djy, Diy, Djx, Dix) / (Dix Djy - Djx Diy), formed at set-up
-// (k_face_metrics) from the cell centres
+// (k_face_metrics) from the cell centres; G_SIA..G_NJ2A: the cell's face
+// length and normal averaged over its two i- (j-) faces, G_VI2 / G_VJ2 their
+// squared length over the cell volume (the metric factors of comput_Lvc)
 enum { G_VOL = 0, G_SI = 1, G_SJ = 2, G_NI1 = 3, G_NI2 = 4, G_NJ1 = 5, G_NJ2 = 6,
        G_X = 7, G_Y = 8, G_X1 = 9, G_Y1 = 10, G_DW = 11,
        G_VIA = 12, G_VIB = 13, G_VIC = 14, G_VID = 15, G_VJA = 16, G_VJB = 17, G_VJC = 18, G_VJD = 19,
-       NG = 20 };
+       G_SIA = 20, G_NI1A = 21, G_NI2A = 22, G_SJA = 23, G_NJ1A = 24, G_NJ2A = 25, G_VI2 = 26, G_VJ2 = 27,
+       NG = 28 };
 // spectral-radius / time-step planes in Lvl::lc
 enum { L_CI = 0, L_CJ = 1, L_VI = 2, L_VJ = 3, L_DT = 4, NL = 5 };
 

@@ -41,6 +41,7 @@ __global__ void __launch_bounds__(TILE) k_prim(Lvl L) {
   double uu = ru * rd, v = rv * rd;
   double T = (E - 0.5 * d * (uu * uu + v * v)) * (rd * c.rCv);
   double p = c.p00 * d * T;
+  const double sT = sqrt(T);
   L.q[Q_D * F + id] = d;
   L.q[Q_U * F + id] = uu;
   L.q[Q_V * F + id] = v;
@@ -49,11 +50,11 @@ __global__ void __launch_bounds__(TILE) k_prim(Lvl L) {
   bool interior = (i >= 1 && i <= b.nx - 1 && j >= 1 && j <= b.ny - 1);
   if (interior) {
     if (!(T >= 1.0e-5)) set_status(L.status + 4 * b.cas, 3, bk, i, j);
-    L.q[Q_C * F + id] = sqrt(T) * c.rMa;
+    L.q[Q_C * F + id] = sT * c.rMa;
   }
   if (L.visc) {
     if (i >= 0 && i <= b.nx && j >= 0 && j <= b.ny)
-      L.amu[id] = c.rRe * (1.0 + c.Tsb) * sqrt(T * T * T) * rcp(c.Tsb + T);
+      L.amu[id] = c.rRe * (1.0 + c.Tsb) * (T * sT) * rcp(c.Tsb + T);  // T^1.5 = T sqrt(T)
     L.amut[id] = 0.0;
   }
 }
@@ -287,21 +288,16 @@ __global__ void __launch_bounds__(TILE) k_res(Lvl L, int post) {
     }
     if (NORM)
       for (int m = 4; m < L.nvar; m++) vres[m] = L.res[m * F + id];
-    const double *g = L.geo;
-    double s0 = g[G_VOL * F + id];
-    double si = 0.5 * (g[G_SI * F + id] + g[G_SI * F + id + 1]);
-    double ni1 = 0.5 * (g[G_NI1 * F + id] + g[G_NI1 * F + id + 1]);
-    double ni2 = 0.5 * (g[G_NI2 * F + id] + g[G_NI2 * F + id + 1]);
-    double sj = 0.5 * (g[G_SJ * F + id] + g[G_SJ * F + id + P]);
-    double nj1 = 0.5 * (g[G_NJ1 * F + id] + g[G_NJ1 * F + id + P]);
-    double nj2 = 0.5 * (g[G_NJ2 * F + id] + g[G_NJ2 * F + id + P]);
+    const double *g = L.geo + id;
+    const double s0 = g[G_VOL * F];
+    const double si = g[G_SIA * F], ni1 = g[G_NI1A * F], ni2 = g[G_NI2A * F];
+    const double sj = g[G_SJA * F], nj1 = g[G_NJ1A * F], nj2 = g[G_NJ2A * F];
     double uu = L.q[Q_U * F + id], vv = L.q[Q_V * F + id], cc = L.q[Q_C * F + id], d = L.q[Q_D * F + id];
     double uni = uu * ni1 + vv * ni2, unj = uu * nj1 + vv * nj2;
     double Lci = (fabs(uni) + cc) * si, Lcj = (fabs(unj) + cc) * sj;
     double amu = L.visc ? L.amu[id] : 0.0, amut = L.visc ? L.amut[id] : 0.0;
-    const double rs0 = rcp(s0);
     double tmp1 = c.gamma * rcp(d) * (amu * c.rPr + amut * (1.0 / PrT));
-    double Lvi = tmp1 * si * si * rs0, Lvj = tmp1 * sj * sj * rs0;
+    double Lvi = tmp1 * g[G_VI2 * F], Lvj = tmp1 * g[G_VJ2 * F];
     L.lc[L_CI * F + id] = Lci;
     L.lc[L_CJ * F + id] = Lcj;
     L.lc[L_VI * F + id] = Lvi;
@@ -358,7 +354,8 @@ __global__ void __launch_bounds__(384) k_norm_final(Lvl L) {
 
 // set-up: the viscous inverse Jacobians of the i-faces (i = 1..nx, j =
 // 1..ny-1) and j-faces (i = 1..nx-1, j = 1..ny) from the cell centres, with the
-// stencils of Residual_FVM (sub_Residual.f90:313-330, 419-436)
+// stencils of Residual_FVM (sub_Residual.f90:313-330, 419-436), and the cell
+// metric factors of the spectral radii
 __global__ void __launch_bounds__(TILE) k_face_metrics(Lvl L) {
   int bk, i, j;
   if (!tile_ij(L, bk, i, j)) return;
@@ -381,6 +378,22 @@ __global__ void __launch_bounds__(TILE) k_face_metrics(Lvl L) {
     const double Djx = x1[id] - x1[s], Djy = y1[id] - y1[s];
     const double Ds = 1.0 / (Dix * Djy - Djx * Diy);
     g[G_VJA * F] = Djy * Ds; g[G_VJB * F] = Diy * Ds; g[G_VJC * F] = Djx * Ds; g[G_VJD * F] = Dix * Ds;
+  }
+  if (i >= 1 && i <= b.nx - 1 && j >= 1 && j <= b.ny - 1) {
+    // comput_Lvc (sub_NS_singlegrid.f90:352-388): face metrics averaged over
+    // the cell's two faces of each family
+    const double *gg = L.geo;
+    const double si = 0.5 * (gg[G_SI * F + id] + gg[G_SI * F + id + 1]);
+    const double sj = 0.5 * (gg[G_SJ * F + id] + gg[G_SJ * F + id + P]);
+    const double rs0 = 1.0 / gg[G_VOL * F + id];
+    g[G_SIA * F] = si;
+    g[G_NI1A * F] = 0.5 * (gg[G_NI1 * F + id] + gg[G_NI1 * F + id + 1]);
+    g[G_NI2A * F] = 0.5 * (gg[G_NI2 * F + id] + gg[G_NI2 * F + id + 1]);
+    g[G_SJA * F] = sj;
+    g[G_NJ1A * F] = 0.5 * (gg[G_NJ1 * F + id] + gg[G_NJ1 * F + id + P]);
+    g[G_NJ2A * F] = 0.5 * (gg[G_NJ2 * F + id] + gg[G_NJ2 * F + id + P]);
+    g[G_VI2 * F] = si * si * rs0;
+    g[G_VJ2 * F] = sj * sj * rs0;
   }
 }
 void launch_face_metrics(const Lvl &L, cudaStream_t s) { k_face_metrics<<<L.ntiles, TILE, 0, s>>>(L); }
