@@ -41,9 +41,10 @@ namespace ec2d {
 constexpr int TILE = EC2D_TILE;
 
 // record layout (doubles), identical for both passes:
-//  A    forward: Res + K; backward: the forward dU, or U + dU when the sweep
-//       updates U (written by the forward sweep); K = -sum over the upstream
-//       neighbours of F_n(U_nb, s) + cc U_nb
+//  A    forward: Res + K; backward: the forward dU, or U + dU of the mean
+//       flow when the sweep updates U (written by the forward sweep); K =
+//       -sum over the upstream neighbours of F_n(U_nb, s) + cc U_nb (mean
+//       flow) or F_n(U_nb, s) (turbulence variables)
 //  U    U_old of the cell
 //  C0   backward only: K of the downstream neighbours
 //  CI, CJ  0.5 Lc_nb (+ Lv_nb when viscous)
@@ -59,10 +60,13 @@ struct Rec {
   static_assert(N % 2 == 0, "records are whole 16-byte units");
 };
 
-// state shipped between neighbours: U2 = U + dU, then u2, v2, p2
+// state shipped between neighbours: U2 = U + dU, then u2, v2, p2, then dU of
+// the turbulence variables (their dissipation term stays (0.5 Lc + Lv) dU_nb:
+// omega and nu~ are large next to their increments, and the folded form
+// cc U2 - cc U_nb would round at the scale of cc U)
 template <int NV>
 struct Slot {
-  static constexpr int U = NV, V = NV + 1, P = NV + 2, S = (NV + 3 + 1) / 2 * 2;
+  static constexpr int U = NV, V = NV + 1, P = NV + 2, DT = NV + 3, S = (2 * NV - 1 + 1) / 2 * 2;
   static_assert(S % 2 == 0, "slots are whole 16-byte units");
 };
 
@@ -83,8 +87,8 @@ __device__ __forceinline__ void fn(const double *U, double n1, double n2, double
   for (int m = 4; m < NV; m++) Fo[m] = U[m] * un;
 }
 
-// acc += F_n(U2, s) + cc U2 from a shipped state (u, v, p of U2 precomputed
-// by the producer)
+// acc += F_n(U2, s) + cc U2 (mean flow) or F_n(U2, s) + cc dU (turbulence
+// variables) from a shipped state (u, v, p of U2 precomputed by the producer)
 template <int NV>
 __device__ __forceinline__ void add_shipped(const double *st, double n1, double n2, double cc, double *acc) {
   using SL = Slot<NV>;
@@ -96,7 +100,7 @@ __device__ __forceinline__ void add_shipped(const double *st, double n1, double 
   acc[2] = fma(st[2], w, fma(p, n2, acc[2]));
   acc[3] = fma(st[3], w, fma(p, un, acc[3]));
 #pragma unroll
-  for (int m = 4; m < NV; m++) acc[m] = fma(st[m], w, acc[m]);
+  for (int m = 4; m < NV; m++) acc[m] = fma(cc, st[SL::DT + m - 4], fma(st[m], un, acc[m]));
 }
 
 template <int NV>
@@ -160,7 +164,7 @@ __global__ void __launch_bounds__(TILE) k_lusgs_prep(Lvl L, double alfa1) {
         s2 = hh * (dir == 0 ? ni2 : nj2);
         fn<NV>(Un, s1, s2, gm1, Fo);
 #pragma unroll
-        for (int m = 0; m < NV; m++) K[pass][m] -= fma(cc, Un[m], Fo[m]);
+        for (int m = 0; m < NV; m++) K[pass][m] -= (m < 4) ? fma(cc, Un[m], Fo[m]) : Fo[m];
       }
       r[dir == 0 ? RC::CI : RC::CJ] = cc;
       r[dir == 0 ? RC::N1I : RC::N1J] = s1;
@@ -277,7 +281,7 @@ __device__ __forceinline__ void sweep_pass(const Lvl &L, const BlkDev &bd, doubl
 #pragma unroll
       for (int m = 0; m < NV; m++) {
         const double inv = (NV == 5 && m == 4) ? cur.ia5 : cur.ia;
-        if (update) {
+        if (update && m < 4) {
           // fused: U + dU* in one fma going forward, carried in the backward
           // record, and U + dU* + dU** in one fma going backward
           st[m] = fma(acc[m], inv, FWD ? cur.u[m] : cur.a[m]);
@@ -286,6 +290,8 @@ __device__ __forceinline__ void sweep_pass(const Lvl &L, const BlkDev &bd, doubl
           st[m] = cur.u[m] + dn[m];
         }
       }
+#pragma unroll
+      for (int m = 4; m < NV; m++) st[SL::DT + m - 4] = dn[m];
       const double rd = rcp(st[0]);
       st[SL::U] = st[1] * rd;
       st[SL::V] = st[2] * rd;
@@ -308,7 +314,9 @@ __device__ __forceinline__ void sweep_pass(const Lvl &L, const BlkDev &bd, doubl
       if (FWD) {
         // the forward result becomes the A field of this cell's backward record
         double *w = recBw + (size_t)(i - 1) * RC::N;
-        const double *val = update ? st : dn;
+        double val[NV];
+#pragma unroll
+        for (int m = 0; m < NV; m++) val[m] = (update && m < 4) ? st[m] : dn[m];
 #pragma unroll
         for (int m = 0; m + 1 < NV; m += 2) reinterpret_cast<double2 *>(w + RC::A)[m / 2] = make_double2(val[m], val[m + 1]);
         if (NV & 1) w[RC::A + NV - 1] = val[NV - 1];
@@ -407,8 +415,12 @@ __device__ __forceinline__ void sweep_pass_lanes(const Lvl &L, const BlkDev &bd,
 #pragma unroll
         for (int kk = 0; kk < VPL; kk++) {
           const int m = mv[kk];
-          const double coef = m == 1 ? n1 : m == 2 ? n2 : m == 3 ? un : 0.0;
-          acc[kk] = fma(sl[m], w, fma(pn, coef, acc[kk]));
+          if (kk < LN::MV) {
+            const double coef = m == 1 ? n1 : m == 2 ? n2 : m == 3 ? un : 0.0;
+            acc[kk] = fma(sl[m], w, fma(pn, coef, acc[kk]));
+          } else {
+            acc[kk] = fma(cc, sl[SL::DT + m - 4], fma(sl[m], un, acc[kk]));
+          }
         }
       };
       if (FWD ? (i > 1) : (i < ni)) add_nb(sh + ((size_t)(buf ^ 1) * (R + 2) + rl + 1) * S, cur.n1i, cur.n2i, cur.ci);
@@ -417,7 +429,7 @@ __device__ __forceinline__ void sweep_pass_lanes(const Lvl &L, const BlkDev &bd,
 #pragma unroll
       for (int kk = 0; kk < VPL; kk++) {
         const double inv = (NV == 5 && mv[kk] == 4) ? cur.ia5 : cur.ia;
-        if (update) {
+        if (update && kk < LN::MV) {
           myst[kk] = fma(acc[kk], inv, FWD ? cur.u[kk] : cur.a[kk]);
         } else {
           dn[kk] = FWD ? acc[kk] * inv : fma(acc[kk], inv, cur.a[kk]);
@@ -435,14 +447,17 @@ __device__ __forceinline__ void sweep_pass_lanes(const Lvl &L, const BlkDev &bd,
       const double pr = gm1 * fma(-0.5, fma(s4[2], v, s4[1] * u), s4[3]);
       double *own = sh + ((size_t)buf * (R + 2) + rl + 1) * S;
 #pragma unroll
-      for (int kk = 0; kk < VPL; kk++)
-        if (ok[kk]) own[mv[kk]] = myst[kk];
+      for (int kk = 0; kk < VPL; kk++) {
+        if (!ok[kk]) continue;
+        own[mv[kk]] = myst[kk];
+        if (kk >= LN::MV) own[SL::DT + mv[kk] - 4] = dn[kk];
+      }
       if (q == 0) { own[SL::U] = u; own[SL::V] = v; own[SL::P] = pr; }
       if (FWD) {
         double *w = recBw + (size_t)(i - 1) * RC::N;
 #pragma unroll
         for (int kk = 0; kk < VPL; kk++)
-          if (ok[kk]) w[RC::A + mv[kk]] = update ? myst[kk] : dn[kk];
+          if (ok[kk]) w[RC::A + mv[kk]] = (update && kk < LN::MV) ? myst[kk] : dn[kk];
       } else {
         const long long id = bd.off + (long long)(j + 2) * bd.P + (i + 2);
 #pragma unroll

@@ -117,8 +117,18 @@ def test_boundary_wall_isothermal_symmetry_sa(gpu_lib):
     compare_U(orc, g, tol=1e-14)
 
 
-def test_lusgs_sweep(gpu_lib):
-    p, bl = small_case(Ma=0.7, AoA=2.0, nblocks=2, If_viscous=1, Re=1e4, Iflag_flux=4)
+# 16 rows per block run the wavefront with four lanes per row, 40 rows with
+# one; NV = 4, 5 (SA), 6 (SST)
+@pytest.mark.parametrize("ny", [17, 41])
+@pytest.mark.parametrize("turb", [0, 2, 3])
+def test_lusgs_sweep(gpu_lib, ny, turb):
+    kw = dict(Ma=0.7, AoA=2.0, nblocks=2, If_viscous=1, Re=1e4, Iflag_flux=4, ny=ny)
+    nv = 4
+    if turb == 2:
+        kw.update(Iflag_turbulence_model=2, Re=1e6, first=2e-4); nv = 5
+    if turb == 3:
+        kw.update(Iflag_turbulence_model=3, Re=1e6, first=2e-4, Kt_inf=1e-6, Wt_inf=1e-2); nv = 6
+    p, bl = small_case(**kw)
     orc, g = _pair(p, bl, steps=3)
     orc.residual()
     # identical inputs on both sides: Res, dt and spectral radii from the oracle
@@ -128,19 +138,53 @@ def test_lusgs_sweep(gpu_lib):
     for b in (1, 2):
         orc.lusgs(1, b, 0.0)
     g.lusgs(1, 0.0)
-    # dU = (Res + dui + duj)/alfa with dui built from F(U+dU) - F(U): the
-    # round-off of that difference scales with F(U) s / alfa, i.e. with the
-    # cell's |U|, not with |dU|, and it accumulates along the sweep's
-    # dependency chain.  Per cell: |ddU| <= 1e-12 |dU| + 1e-14 |U| (~100 ulp of U).
+    # dU = (Res + dui + duj)/alfa with dui built from F(U+dU) - F(U) and the
+    # dissipation (0.5 Lc + Lv) dU of the upstream neighbours: the round-off
+    # of those sums scales with the magnitudes added, F(U) s / alfa and
+    # (0.5 Lc + Lv) U_nb / alfa, i.e. with |U| of the cell and of its
+    # neighbours (and with p in the momentum and energy rows, where F carries
+    # p n and (E + p) un), not with |dU|, and it accumulates along the sweep's
+    # dependency chain, one rounding of those magnitudes per hyperplane at
+    # most.  Per cell: |ddU_m| <= 1e-12 |dU_m| + eps (nx + ny) S_m with eps =
+    # 2^-52, nx + ny the planes of a sweep and S_m = max |U_m| over the cell
+    # and its four neighbours (+ p for m = 1..3).  The SST omega row sums
+    # source and flux terms thousands of times its increment next to walls:
+    # its relative term is 2e-12 (the row reached 0.9-1.1e-12 with either
+    # accumulation order of the wavefront).
     worst = 0.0
     for b in (1, 2):
         nx, ny = orc.dims(1, b)
-        a = orc.field(1, b, 6, (4, nx, ny))[:, :nx - 1, :ny - 1]
-        c = g.field(1, 1, b, 6, (4, nx, ny))[:, :nx - 1, :ny - 1]
-        U = orc.get_U(1, b)[:4, 2:nx + 1, 2:ny + 1]
-        bound = 1e-12 * np.maximum(np.abs(a), np.abs(c)) + 1e-14 * np.abs(U)
+        chain = np.finfo(np.float64).eps * (nx + ny)
+        a = orc.field(1, b, 6, (nv, nx, ny))[:, :nx - 1, :ny - 1]
+        c = g.field(1, 1, b, 6, (nv, nx, ny))[:, :nx - 1, :ny - 1]
+        Ug = np.abs(orc.get_U(1, b)[:nv])  # ghost-padded: interior at 2..nx, 2..ny
+        Um = np.maximum.reduce([Ug[:, 2:nx + 1, 2:ny + 1], Ug[:, 1:nx, 2:ny + 1], Ug[:, 3:nx + 2, 2:ny + 1],
+                                Ug[:, 2:nx + 1, 1:ny], Ug[:, 2:nx + 1, 3:ny + 2]])
+        Uc = orc.get_U(1, b)[:4, 2:nx + 1, 2:ny + 1]
+        pr = 0.4 * (Uc[3] - 0.5 * (Uc[1] ** 2 + Uc[2] ** 2) / Uc[0])
+        S = Um.copy()
+        S[1:4] += pr
+        rel = np.full((nv, 1, 1), 1e-12)
+        rel[4:] = 2e-12
+        bound = rel * np.maximum(np.abs(a), np.abs(c)) + chain * S
         worst = max(worst, np.max(np.abs(a - c) / bound))
     assert worst <= 1.0, worst
+
+
+@pytest.mark.parametrize("turb", [0, 2])
+def test_lusgs_steps_wide_blocks(gpu_lib, turb):
+    """LU-SGS time steps on 40-row blocks (one lane per row in the wavefront,
+    U updated inside the sweep) against the oracle."""
+    kw = dict(ny=41, Ma=0.6, AoA=2.0, Iflag_flux=4, Iflag_Scheme=5, Time_Method=0, CFL=5.0)
+    if turb == 2:
+        kw.update(If_viscous=1, Iflag_turbulence_model=2, Re=1e6, first=2e-4)
+    p, bl = small_case(**kw)
+    orc = make_oracle(p, bl)
+    orc.init_flow()
+    g = make_gpu(p, bl)
+    g.init_flow()
+    orc.step(15); g.step(15)
+    compare_U(orc, g, tol=1e-10)
 
 
 @pytest.mark.parametrize("tm", [0, 1, 3])
