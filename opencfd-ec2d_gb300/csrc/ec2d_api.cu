@@ -714,9 +714,13 @@ void advance_counters(ec2d_ctx *ctx, int l) {
   for (auto &c : ctx->cases) { c.tt[l] += c.p.dt_global; c.kstep[l] += 1; }
 }
 
-// NS_Time_advance_1Euler (sub_NS_singlegrid.f90:67-106)
-void step_euler(ec2d_ctx *ctx, int l) {
-  residual(ctx, l);
+// NS_Time_advance_1Euler (sub_NS_singlegrid.f90:67-106).  fresh: U has not
+// changed since the last residual evaluation of this level (the first
+// smoothing step after coarse_entry), so Res, the spectral radii, dt and the
+// norms of that evaluation stand; the reference evaluates them again with the
+// same result.
+void step_euler(ec2d_ctx *ctx, int l, bool fresh = false) {
+  if (!fresh) residual(ctx, l);
   K(ctx, "k_euler", l, 1, [&] { launch_euler(ctx->lv[l].L, l != 1, ctx->stream); });
   bc_all(ctx, l);
   advance_counters(ctx, l);
@@ -749,8 +753,9 @@ void lusgs_update(ec2d_ctx *ctx, int l, double alfa1) {
 }
 // NS_Time_advance_LU_SGS (sub_NS_singlegrid.f90:185-224); on a coarse level of
 // an LU-SGS-smoothed multigrid cycle the forcing is added after the residual
-void step_lusgs(ec2d_ctx *ctx, int l, double alfa1 = 0.0) {
-  residual(ctx, l, l != 1 ? RES_ADD_FORCE : 0);
+void step_lusgs(ec2d_ctx *ctx, int l, double alfa1 = 0.0, bool fresh = false) {
+  if (!fresh) residual(ctx, l, l != 1 ? RES_ADD_FORCE : 0);
+  else if (l != 1) K(ctx, "k_add_force", l, 1, [&] { launch_add_force(ctx->lv[l].L, ctx->stream); });
   lusgs_update(ctx, l, alfa1);
   bc_all(ctx, l);
   advance_counters(ctx, l);
@@ -805,14 +810,15 @@ void mg_smooth_fine(ec2d_ctx *ctx) {
   else step_rk3(ctx, 1);
 }
 // Un = U of the coarse level (Euler and LU-SGS smoothing) is taken by the
-// residual evaluation just before (RES_SET_UN, see coarse_entry)
+// residual evaluation just before (RES_SET_UN, see coarse_entry), and the
+// first smoothing step reuses that evaluation (U is unchanged since)
 void mg_smooth_coarse(ec2d_ctx *ctx, int l) {
   const int Time_step_coarse_mesh = 3;
   int tm = ctx->P.Time_Method;
   if (tm == Time_Euler1) {
-    for (int m = 0; m < Time_step_coarse_mesh; m++) step_euler(ctx, l);
+    for (int m = 0; m < Time_step_coarse_mesh; m++) step_euler(ctx, l, m == 0);
   } else if (tm == Time_LU_SGS) {
-    step_lusgs(ctx, l);
+    step_lusgs(ctx, l, 0.0, true);
   } else step_rk3(ctx, l);
 }
 // residual of a coarse level right after restriction, QF -= Res
