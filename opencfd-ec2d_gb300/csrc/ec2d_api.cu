@@ -739,14 +739,18 @@ void step_rk3(ec2d_ctx *ctx, int l) {
 // du_LU_SGS_2D for every block of the level followed by U += dU
 // (sub_NS_singlegrid.f90:196-213): the wavefront kernels fuse the update into
 // the backward sweep; blocks wider than 1024 rows take the generic kernel
-void lusgs_update(ec2d_ctx *ctx, int l, double alfa1) {
+// force: Res + QF stands for Res (forcing of a coarse level whose residual
+// evaluated on entry is reused); the wavefront record builders add it
+void lusgs_update(ec2d_ctx *ctx, int l, double alfa1, bool force = false) {
   const Level &lv = ctx->lv[l];
   const Lvl &L = lv.L;
+  const int mode = LUSGS_UPDATE | (force ? LUSGS_FORCE : 0);
   if (ctx->lusgs_fp32 && lv.fast32) {
-    K(ctx, "k_lusgs32", l, 3, [&] { launch_lusgs_fast32(L, alfa1, 1, lv.max_rows, ctx->stream); });
+    K(ctx, "k_lusgs32", l, 3, [&] { launch_lusgs_fast32(L, alfa1, mode, lv.max_rows, ctx->stream); });
   } else if (lv.fast64) {
-    K(ctx, "k_lusgs", l, 2, [&] { launch_lusgs_fast(L, alfa1, 1, lv.max_rows, ctx->lusgs_cs, ctx->lusgs_rpw, ctx->stream); });
+    K(ctx, "k_lusgs", l, 2, [&] { launch_lusgs_fast(L, alfa1, mode, lv.max_rows, ctx->lusgs_cs, ctx->lusgs_rpw, ctx->stream); });
   } else {
+    if (force) K(ctx, "k_add_force", l, 1, [&] { launch_add_force(L, ctx->stream); });
     K(ctx, "k_lusgs_generic", l, 1, [&] { launch_lusgs(L, alfa1, ctx->stream); });
     K(ctx, "k_add_du", l, 1, [&] { launch_add_du(L, ctx->stream); });
   }
@@ -755,8 +759,7 @@ void lusgs_update(ec2d_ctx *ctx, int l, double alfa1) {
 // an LU-SGS-smoothed multigrid cycle the forcing is added after the residual
 void step_lusgs(ec2d_ctx *ctx, int l, double alfa1 = 0.0, bool fresh = false) {
   if (!fresh) residual(ctx, l, l != 1 ? RES_ADD_FORCE : 0);
-  else if (l != 1) K(ctx, "k_add_force", l, 1, [&] { launch_add_force(ctx->lv[l].L, ctx->stream); });
-  lusgs_update(ctx, l, alfa1);
+  lusgs_update(ctx, l, alfa1, fresh && l != 1);
   bc_all(ctx, l);
   advance_counters(ctx, l);
 }
@@ -832,10 +835,10 @@ void restrict_both(ec2d_ctx *ctx, int f) {
   const Lvl &Lf = ctx->lv[f].L, &Lc = ctx->lv[f + 1].L;
   K(ctx, "k_restrict", f + 1, 1, [&] { launch_restrict(Lf, Lc, 3, ctx->stream); });
 }
-// deltU = U - Un on level c, prolonged to level c-1 and added there
+// deltU = U - Un on level c, prolonged to level c-1 and added there (one
+// kernel: the coarse deltU is formed where it is interpolated)
 void correct_from(ec2d_ctx *ctx, int c) {
   const Lvl &Lc = ctx->lv[c].L, &Lf = ctx->lv[c - 1].L;
-  K(ctx, "k_delt_u", c, 1, [&] { launch_delt_u(Lc, ctx->stream); });
   K(ctx, "k_prolong", c - 1, 1, [&] { launch_prolong(Lc, Lf, 3, ctx->stream); });
 }
 // NS_2stge_multigrid (sub_NS_multigrid.f90:14-58)

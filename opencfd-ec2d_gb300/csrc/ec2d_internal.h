@@ -31,9 +31,12 @@ void launch_bc_normals(const Lvl &L, int max_nodes, cudaStream_t s);
 void launch_lusgs(const Lvl &L, double alfa1, cudaStream_t s);
 // k_sweep.cu
 int lusgs_planes(int nv);
-void launch_lusgs_fast(const Lvl &L, double alfa1, int update, int max_rows, int cs, int rpw, cudaStream_t s);
+// mode bits of the wavefront launchers: update U in the sweep, and take
+// Res + QF for Res (a coarse level's forcing when its residual is reused)
+enum { LUSGS_UPDATE = 1, LUSGS_FORCE = 2 };
+void launch_lusgs_fast(const Lvl &L, double alfa1, int mode, int max_rows, int cs, int rpw, cudaStream_t s);
 size_t lusgs_smem(int nv, int rows);  // dynamic shared memory of the one-CTA FP64 sweep
-void launch_lusgs_fast32(const Lvl &L, double alfa1, int update, int max_rows, cudaStream_t s);
+void launch_lusgs_fast32(const Lvl &L, double alfa1, int mode, int max_rows, cudaStream_t s);
 size_t lusgs32_smem(int nv, int rows);
 size_t lusgs32_record_bytes(int nv);
 // warm-start network <-> solver level (k_mlp.cu)

@@ -212,8 +212,9 @@ __global__ void k_restrict(Lvl Lf, Lvl Lc, int flag) {
 
 // prolongation coarse -> fine (prolong_U, sub_NS_multigrid.f90:271-343), over
 // fine cells 0..nx2, 0..ny2; flag 1 interpolates U, flag 2 deltU, flag 3
-// deltU and then U += deltU on the fine interior (comput_new_U,
-// sub_NS_multigrid.f90:240-260) in the same pass.
+// deltU formed on the fly from the coarse U - Un (comput_delt_U,
+// sub_NS_multigrid.f90:199-216, the same subtraction) and then U += deltU on
+// the fine interior (comput_new_U, sub_NS_multigrid.f90:240-260), one pass.
 __global__ void k_prolong(Lvl Lc, Lvl Lf, int flag) {
   int bk, i, j;
   if (!tile_cell(Lf, bk, i, j, 0, 0)) return;
@@ -227,8 +228,15 @@ __global__ void k_prolong(Lvl Lc, Lvl Lf, int flag) {
   double *dst = (flag == 1) ? Lf.U : Lf.deltu;
   const bool add = flag == 3 && i >= 1 && i <= bf.nx - 1 && j >= 1 && j <= bf.ny - 1;
   for (int m = 0; m < 4; m++) {
-    const double *s = src + m * Lc.F;
-    const double v = a1 * s[c11] + a2 * (s[c21] + s[c12]) + a3 * s[c22];
+    double s11, s21, s12, s22;
+    if (flag == 3) {
+      const double *u = Lc.U + m * Lc.F, *un = Lc.un + m * Lc.F;
+      s11 = u[c11] - un[c11]; s21 = u[c21] - un[c21]; s12 = u[c12] - un[c12]; s22 = u[c22] - un[c22];
+    } else {
+      const double *s = src + m * Lc.F;
+      s11 = s[c11]; s21 = s[c21]; s12 = s[c12]; s22 = s[c22];
+    }
+    const double v = a1 * s11 + a2 * (s21 + s12) + a3 * s22;
     dst[m * Lf.F + id] = v;
     if (add) Lf.U[m * Lf.F + id] = Lf.U[m * Lf.F + id] + v;
   }

@@ -104,7 +104,9 @@ __device__ __forceinline__ void add_shipped(const double *st, double n1, double 
 }
 
 template <int NV>
-__global__ void __launch_bounds__(TILE) k_lusgs_prep(Lvl L, double alfa1) {
+// force: Res + QF in place of Res (the multigrid forcing of a coarse level
+// whose residual was evaluated on entry, Add_force_function)
+__global__ void __launch_bounds__(TILE) k_lusgs_prep(Lvl L, double alfa1, int force) {
   using RC = Rec<NV>;
   int2 t = L.tiles[blockIdx.x];
   const BlkDev &b = L.blk[t.x];
@@ -132,6 +134,7 @@ __global__ void __launch_bounds__(TILE) k_lusgs_prep(Lvl L, double alfa1) {
   for (int m = 0; m < NV; m++) {
     double u = L.U[m * F + id];
     res[m] = L.res[m * F + id];
+    if (force && m < 4) res[m] = res[m] + L.qf[m * F + id];
     rf[RC::U + m] = u;
     rb[RC::U + m] = u;
     K[0][m] = 0.0;
@@ -546,8 +549,9 @@ size_t smem_bytes(int R, int th) {
 }
 
 template <int NV>
-void sweep_nv(const Lvl &L, double alfa1, int update, int max_rows, int cs, int rpw, cudaStream_t s) {
-  k_lusgs_prep<NV><<<L.ntiles, TILE, 0, s>>>(L, alfa1);
+void sweep_nv(const Lvl &L, double alfa1, int mode, int max_rows, int cs, int rpw, cudaStream_t s) {
+  k_lusgs_prep<NV><<<L.ntiles, TILE, 0, s>>>(L, alfa1, mode & LUSGS_FORCE);
+  const int update = mode & LUSGS_UPDATE;
   const int lpr = sweep_lanes_per_row(max_rows);
   if (lpr == 4) { launch_lanes<NV, 4>(L, update, max_rows, s); return; }
   int CS = std::max(1, std::min(cs, std::min(8, (max_rows + 7) / 8)));
@@ -587,10 +591,10 @@ size_t smem_nv(int rows) {
 }
 size_t lusgs_smem(int nv, int rows) { return nv == 4 ? smem_nv<4>(rows) : nv == 5 ? smem_nv<5>(rows) : smem_nv<6>(rows); }
 
-void launch_lusgs_fast(const Lvl &L, double alfa1, int update, int max_rows, int cs, int rpw, cudaStream_t s) {
-  if (L.nvar == 4) sweep_nv<4>(L, alfa1, update, max_rows, cs, rpw, s);
-  else if (L.nvar == 5) sweep_nv<5>(L, alfa1, update, max_rows, cs, rpw, s);
-  else sweep_nv<6>(L, alfa1, update, max_rows, cs, rpw, s);
+void launch_lusgs_fast(const Lvl &L, double alfa1, int mode, int max_rows, int cs, int rpw, cudaStream_t s) {
+  if (L.nvar == 4) sweep_nv<4>(L, alfa1, mode, max_rows, cs, rpw, s);
+  else if (L.nvar == 5) sweep_nv<5>(L, alfa1, mode, max_rows, cs, rpw, s);
+  else sweep_nv<6>(L, alfa1, mode, max_rows, cs, rpw, s);
 }
 
 }  // namespace ec2d

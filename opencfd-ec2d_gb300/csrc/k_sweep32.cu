@@ -58,7 +58,7 @@ struct S32 {
 };
 
 template <int NV>
-__global__ void __launch_bounds__(TILE) k_lusgs_prep32(Lvl L, double alfa1) {
+__global__ void __launch_bounds__(TILE) k_lusgs_prep32(Lvl L, double alfa1, int force) {
   using RC = R32<NV>;
   int2 t = L.tiles[blockIdx.x];
   const BlkDev &b = L.blk[t.x];
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(TILE) k_lusgs_prep32(Lvl L, double alfa1) {
   double ni1 = g[G_NI1 * F + id], ni2 = g[G_NI2 * F + id], nj1 = g[G_NJ1 * F + id], nj2 = g[G_NJ2 * F + id];
 #pragma unroll
   for (int m = 0; m < NV; m++) {
-    rf[RC::A + m] = (float)L.res[m * F + id];
+    rf[RC::A + m] = (float)((force && m < 4) ? L.res[m * F + id] + L.qf[m * F + id] : L.res[m * F + id]);
     rb[RC::A + m] = 0.0f;
   }
   float *rr[2] = {rf, rb};
@@ -286,8 +286,9 @@ size_t smem32(int rows) {
 }
 
 template <int NV>
-void sweep32_nv(const Lvl &L, double alfa1, int update, int max_rows, cudaStream_t s) {
-  k_lusgs_prep32<NV><<<L.ntiles, TILE, 0, s>>>(L, alfa1);
+void sweep32_nv(const Lvl &L, double alfa1, int mode, int max_rows, cudaStream_t s) {
+  k_lusgs_prep32<NV><<<L.ntiles, TILE, 0, s>>>(L, alfa1, mode & LUSGS_FORCE);
+  const int update = mode & LUSGS_UPDATE;
   int th = ((max_rows + 31) / 32) * 32;
   size_t smem = smem32<NV>(max_rows);
   if (smem > 48 * 1024)
@@ -305,10 +306,10 @@ size_t lusgs32_record_bytes(int nv) {
   return nv == 4 ? R32<4>::BYTES : nv == 5 ? R32<5>::BYTES : R32<6>::BYTES;
 }
 
-void launch_lusgs_fast32(const Lvl &L, double alfa1, int update, int max_rows, cudaStream_t s) {
-  if (L.nvar == 4) sweep32_nv<4>(L, alfa1, update, max_rows, s);
-  else if (L.nvar == 5) sweep32_nv<5>(L, alfa1, update, max_rows, s);
-  else sweep32_nv<6>(L, alfa1, update, max_rows, s);
+void launch_lusgs_fast32(const Lvl &L, double alfa1, int mode, int max_rows, cudaStream_t s) {
+  if (L.nvar == 4) sweep32_nv<4>(L, alfa1, mode, max_rows, s);
+  else if (L.nvar == 5) sweep32_nv<5>(L, alfa1, mode, max_rows, s);
+  else sweep32_nv<6>(L, alfa1, mode, max_rows, s);
 }
 
 }  // namespace ec2d
