@@ -73,7 +73,9 @@ typedef struct ec2d_ctx ec2d_ctx;
  * levels that take the general LU-SGS kernel; the wavefront sweep of a step
  * adds the increment to U directly and leaves DU as scratch (the reference
  * reads DU only inside du_LU_SGS_2D and the update after it,
- * sub_LU_SGS.f90:44-95, sub_NS_singlegrid.f90:197-211). */
+ * sub_LU_SGS.f90:44-95, sub_NS_singlegrid.f90:197-211).  Likewise a
+ * multigrid cycle fills DELTU of the finer level of each prolongation; the
+ * coarse increment U - Un is formed where it is interpolated and not stored. */
 enum {
   EC2D_F_RES = 0, EC2D_F_DT = 1, EC2D_F_LCI = 2, EC2D_F_LCJ = 3, EC2D_F_LVI = 4,
   EC2D_F_LVJ = 5, EC2D_F_DU = 6, EC2D_F_AMU = 7, EC2D_F_AMUT = 8, EC2D_F_X1 = 9,

@@ -38,7 +38,6 @@ void launch_lusgs_fast(const Lvl &L, double alfa1, int mode, int max_rows, int c
 size_t lusgs_smem(int nv, int rows);  // dynamic shared memory of the one-CTA FP64 sweep
 void launch_lusgs_fast32(const Lvl &L, double alfa1, int mode, int max_rows, cudaStream_t s);
 size_t lusgs32_smem(int nv, int rows);
-size_t lusgs32_record_bytes(int nv);
 // warm-start network <-> solver level (k_mlp.cu)
 void launch_features(const Lvl &L, const double *shape, float *feat, float *targ, cudaStream_t s);
 void launch_warm_start(const Lvl &L, const float *pred, int *bad, cudaStream_t s);
@@ -48,8 +47,6 @@ void launch_rk3(const Lvl &L, int stage, int force, cudaStream_t s);
 void launch_add_force(const Lvl &L, cudaStream_t s);
 void launch_force_fn(const Lvl &L, cudaStream_t s);
 void launch_set_un(const Lvl &L, int nv, cudaStream_t s);
-void launch_delt_u(const Lvl &L, cudaStream_t s);
-void launch_new_u(const Lvl &L, cudaStream_t s);
 void launch_restrict(const Lvl &Lf, const Lvl &Lc, int flag, cudaStream_t s);
 void launch_prolong(const Lvl &Lc, const Lvl &Lf, int flag, cudaStream_t s);
 void launch_freestream(const Lvl &L, int flow, int turb, cudaStream_t s);

@@ -168,21 +168,6 @@ __global__ void k_set_un(Lvl L, int nv) {
   long long id = fidx(L.blk[bk], i, j);
   for (int m = 0; m < nv; m++) L.un[m * L.F + id] = L.U[m * L.F + id];
 }
-// deltU = U - Un over 0..nx, 0..ny (comput_delt_U, sub_NS_multigrid.f90:199-216)
-__global__ void k_delt_u(Lvl L) {
-  int bk, i, j;
-  if (!tile_cell(L, bk, i, j, 0, 0)) return;
-  long long id = fidx(L.blk[bk], i, j);
-  for (int m = 0; m < 4; m++) L.deltu[m * L.F + id] = L.U[m * L.F + id] - L.un[m * L.F + id];
-}
-// U += deltU (comput_new_U, sub_NS_multigrid.f90:240-260)
-__global__ void k_new_u(Lvl L) {
-  int bk, i, j;
-  if (!tile_cell(L, bk, i, j, 1, 1)) return;
-  long long id = fidx(L.blk[bk], i, j);
-  for (int m = 0; m < 4; m++) L.U[m * L.F + id] = L.U[m * L.F + id] + L.deltu[m * L.F + id];
-}
-
 // restriction fine -> coarse (interpolation2h, sub_NS_multigrid.f90:349-398):
 // flag 1 volume-weighted U, flag 2 residual sum into QF, 3 both.  Runs over
 // the coarse level's tiles.
@@ -270,8 +255,6 @@ void launch_rk3(const Lvl &L, int stage, int force, cudaStream_t s) { k_rk3<<<L.
 void launch_add_force(const Lvl &L, cudaStream_t s) { k_add_force<<<L.ntiles, TILE, 0, s>>>(L); }
 void launch_force_fn(const Lvl &L, cudaStream_t s) { k_force_fn<<<L.ntiles, TILE, 0, s>>>(L); }
 void launch_set_un(const Lvl &L, int nv, cudaStream_t s) { k_set_un<<<L.ntiles, TILE, 0, s>>>(L, nv); }
-void launch_delt_u(const Lvl &L, cudaStream_t s) { k_delt_u<<<L.ntiles, TILE, 0, s>>>(L); }
-void launch_new_u(const Lvl &L, cudaStream_t s) { k_new_u<<<L.ntiles, TILE, 0, s>>>(L); }
 void launch_restrict(const Lvl &Lf, const Lvl &Lc, int flag, cudaStream_t s) {
   k_restrict<<<Lc.ntiles, TILE, 0, s>>>(Lf, Lc, flag);
 }

@@ -302,9 +302,6 @@ void sweep32_nv(const Lvl &L, double alfa1, int mode, int max_rows, cudaStream_t
 size_t lusgs32_smem(int nv, int rows) {
   return nv == 4 ? smem32<4>(rows) : nv == 5 ? smem32<5>(rows) : smem32<6>(rows);
 }
-size_t lusgs32_record_bytes(int nv) {
-  return nv == 4 ? R32<4>::BYTES : nv == 5 ? R32<5>::BYTES : R32<6>::BYTES;
-}
 
 void launch_lusgs_fast32(const Lvl &L, double alfa1, int mode, int max_rows, cudaStream_t s) {
   if (L.nvar == 4) sweep32_nv<4>(L, alfa1, mode, max_rows, s);
