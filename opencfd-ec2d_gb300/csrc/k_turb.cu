@@ -36,9 +36,9 @@ __global__ void k_sa_mut(Lvl L) {
   const long long F = L.F;
   long long id = fidx(b, i, j);
   double vt = L.U[4 * F + id], d = L.q[Q_D * F + id];
-  double X = d * vt / L.amu[id];
+  double X = d * vt * rcp(L.amu[id]);
   double X3 = X * X * X;
-  double fv1 = X3 / (X3 + sa::Cv1 * sa::Cv1 * sa::Cv1);
+  double fv1 = X3 * rcp(X3 + sa::Cv1 * sa::Cv1 * sa::Cv1);
   L.amut[id] = fv1 * d * vt;
 }
 
@@ -74,21 +74,19 @@ __global__ void k_sa_faces(Lvl L) {
   const long long F = L.F, P = b.P;
   long long id = fidx(b, i, j);
   const double *vt = L.U + 4 * F, *d = L.q + Q_D * F, *uu = L.q + Q_U * F, *vv = L.q + Q_V * F;
-  const double *x1 = L.geo + G_X1 * F, *y1 = L.geo + G_Y1 * F, *amu = L.amu;
+  const double *amu = L.amu;
   const double c0 = 0.5 * (1.0 + sa::Cb2) / sa::sigma;
   if (i >= 1 && i <= b.nx && j >= 1 && j <= b.ny - 1) {
     long long w = id - 1, nN = id + P, nS = id - P;
     double s0 = L.geo[G_SI * F + id], n1 = L.geo[G_NI1 * F + id], n2 = L.geo[G_NI2 * F + id];
     double vn1 = uu[w] * n1 + vv[w] * n2, vn2 = uu[id] * n1 + vv[id] * n2;
     double vfi = -0.5 * ((vn1 + fabs(vn1)) * vt[w] + (vn2 - fabs(vn2)) * vt[id]) * s0;
-    double v0 = c0 * (vt[id] + amu[id] / d[id] + vt[w] + amu[w] / d[w]);
-    double Dix = x1[id] - x1[w], Diy = y1[id] - y1[w];
-    double Djx = (x1[nN - 1] + x1[nN] - x1[nS - 1] - x1[nS]) * 0.25;
-    double Djy = (y1[nN - 1] + y1[nN] - y1[nS - 1] - y1[nS]) * 0.25;
-    double Ds = 1.0 / (Dix * Djy - Djx * Diy);
+    double v0 = c0 * (vt[id] + amu[id] * rcp(d[id]) + vt[w] + amu[w] * rcp(d[w]));
+    // the face's inverse Jacobian, formed at set-up (k_face_metrics)
+    const double *gm = L.geo + id;
     double Div = vt[id] - vt[w];
     double Djv = (vt[nN - 1] + vt[nN] - vt[nS - 1] - vt[nS]) * 0.25;
-    double vtx = (Div * Djy - Djv * Diy) * Ds, vty = (-Div * Djx + Djv * Dix) * Ds;
+    double vtx = fma(Div, gm[G_VIA * F], -Djv * gm[G_VIB * F]), vty = fma(Djv, gm[G_VID * F], -Div * gm[G_VIC * F]);
     double g = (vtx * n1 + vty * n2) * s0;
     L.fi[4 * F + id] = vfi + v0 * g;
     L.fi[5 * F + id] = g;
@@ -98,14 +96,11 @@ __global__ void k_sa_faces(Lvl L) {
     double s0 = L.geo[G_SJ * F + id], n1 = L.geo[G_NJ1 * F + id], n2 = L.geo[G_NJ2 * F + id];
     double vn1 = uu[s] * n1 + vv[s] * n2, vn2 = uu[id] * n1 + vv[id] * n2;
     double vfi = -0.5 * ((vn1 + fabs(vn1)) * vt[s] + (vn2 - fabs(vn2)) * vt[id]) * s0;
-    double v0 = c0 * (vt[id] + amu[id] / d[id] + vt[s] + amu[s] / d[s]);
-    double Dix = (x1[s + 1] + x1[id + 1] - x1[s - 1] - x1[id - 1]) * 0.25;
-    double Diy = (y1[s + 1] + y1[id + 1] - y1[s - 1] - y1[id - 1]) * 0.25;
-    double Djx = x1[id] - x1[s], Djy = y1[id] - y1[s];
-    double Ds = 1.0 / (Dix * Djy - Djx * Diy);
+    double v0 = c0 * (vt[id] + amu[id] * rcp(d[id]) + vt[s] + amu[s] * rcp(d[s]));
+    const double *gm = L.geo + id;
     double Div = (vt[s + 1] + vt[id + 1] - vt[s - 1] - vt[id - 1]) * 0.25;
     double Djv = vt[id] - vt[s];
-    double vtx = (Div * Djy - Djv * Diy) * Ds, vty = (-Div * Djx + Djv * Dix) * Ds;
+    double vtx = fma(Div, gm[G_VJA * F], -Djv * gm[G_VJB * F]), vty = fma(Djv, gm[G_VJD * F], -Div * gm[G_VJC * F]);
     double g = (vtx * n1 + vty * n2) * s0;
     L.fj[4 * F + id] = vfi + v0 * g;
     L.fj[5 * F + id] = g;
@@ -123,7 +118,8 @@ __global__ void k_sa_res(Lvl L) {
   long long id = fidx(b, i, j);
   const double *x1 = L.geo + G_X1 * F, *y1 = L.geo + G_Y1 * F, *uu = L.q + Q_U * F, *vv = L.q + Q_V * F;
   double vt = L.U[4 * F + id], d = L.q[Q_D * F + id], amu = L.amu[id];
-  double v0 = (vt + amu / d) * sa::Cb2 / sa::sigma;
+  const double ramu = rcp(amu);
+  double v0 = (vt + amu * rcp(d)) * (sa::Cb2 / sa::sigma);
   double r = L.fi[4 * F + id + 1] - L.fi[4 * F + id] - v0 * (L.fi[5 * F + id + 1] - L.fi[5 * F + id]);
   r = r + L.fj[4 * F + id + P] - L.fj[4 * F + id] - v0 * (L.fj[5 * F + id + P] - L.fj[5 * F + id]);
   double Dix = (x1[id + 1] - x1[id - 1]) * 0.5, Diy = (y1[id + 1] - y1[id - 1]) * 0.5;
@@ -135,21 +131,23 @@ __global__ void k_sa_res(Lvl L) {
   double uy = (-Diu * Djx + Dju * Dix) * Ds;
   double S = fabs(vx - uy);
   double dw = L.geo[G_DW * F + id];
-  double X = d * vt / amu;
+  double X = d * vt * ramu;
   double X3 = X * X * X;
-  double fv1 = X3 / (X3 + sa::Cv1 * sa::Cv1 * sa::Cv1);
-  double fv2 = 1.0 - X / (1.0 + X * fv1);
+  double fv1 = X3 * rcp(X3 + sa::Cv1 * sa::Cv1 * sa::Cv1);
+  double fv2 = 1.0 - X * rcp(1.0 + X * fv1);
   double kd = sa::kap * dw;
-  double S1 = fmax(S + fv2 * vt / (kd * kd), (double)0.3f * S);  // 0.3 is a single-precision literal
-  double rr = fmin(vt / (S1 * sa::kap * sa::kap * dw * dw), 10.0);
+  const double rkd2 = rcp(kd * kd);  // 1 / (kappa d)^2
+  double S1 = fmax(S + fv2 * vt * rkd2, (double)0.3f * S);  // 0.3 is a single-precision literal
+  double rr = fmin(vt * rcp(S1) * rkd2, 10.0);
   double r2 = rr * rr, r6 = r2 * r2 * r2;
   double g = rr + sa::Cw2 * (r6 - rr);
   double g2 = g * g, g6 = g2 * g2 * g2;
   const double c36 = sa::Cw3 * sa::Cw3 * sa::Cw3 * sa::Cw3 * sa::Cw3 * sa::Cw3;
-  double fw = g * pow((1.0 + c36) / (g6 + c36), 1.0 / 6.0);
+  // x^(1/6) as cbrt(sqrt(x)): both within an ulp, cheaper than pow
+  double fw = g * cbrt(sqrt((1.0 + c36) * rcp(g6 + c36)));
   double ft2 = sa::Ct3 * exp(-sa::Ct4 * X * X);
   const double Cw1 = sa::Cb1 / (sa::kap * sa::kap) + (1.0 + sa::Cb2) / sa::sigma;
-  double q = vt / dw;
+  double q = vt * rcp(dw);
   double Q = sa::Cb1 * (1.0 - ft2) * S1 * vt - (Cw1 * fw - sa::Cb1 * ft2 / (sa::kap * sa::kap)) * (q * q);
   L.res[4 * F + id] = r + Q * L.geo[G_VOL * F + id];
 }
