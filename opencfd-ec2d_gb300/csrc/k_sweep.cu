@@ -121,8 +121,8 @@ __global__ void __launch_bounds__(TILE) k_lusgs_prep(Lvl L, double alfa1, int fo
   const double *g = L.geo, *lc = L.lc;
   const bool visc = L.visc != 0;
   const size_t cell = (size_t)b.cell0 + (size_t)(j - 1) * (b.nx - 1) + (i - 1);
-  double *rf = L.rec + cell * RC::N;                          // forward record
-  double *rb = L.rec + ((size_t)L.ncell + cell) * RC::N;      // backward record
+  // the two records are assembled in registers and written 16 bytes at a time
+  double rf[RC::N], rb[RC::N];  // forward and backward record
   double vol = g[G_VOL * F + id];
   double Lv = lc[L_VI * F + id] + lc[L_VJ * F + id];
   double alfa = vol * rcp(lc[L_DT * F + id]) + 1.0 * (lc[L_CI * F + id] + lc[L_CJ * F + id]) + vol * alfa1;
@@ -180,6 +180,15 @@ __global__ void __launch_bounds__(TILE) k_lusgs_prep(Lvl L, double alfa1, int fo
     rf[RC::C0 + m] = 0.0;
     rb[RC::A + m] = 0.0;
     rb[RC::C0 + m] = K[1][m];
+  }
+#pragma unroll
+  for (int k = RC::CI + 8; k < RC::N; k++) rf[k] = rb[k] = 0.0;
+  double2 *wf = reinterpret_cast<double2 *>(L.rec + cell * RC::N);
+  double2 *wb = reinterpret_cast<double2 *>(L.rec + ((size_t)L.ncell + cell) * RC::N);
+#pragma unroll
+  for (int q = 0; q < RC::N / 2; q++) {
+    wf[q] = make_double2(rf[2 * q], rf[2 * q + 1]);
+    wb[q] = make_double2(rb[2 * q], rb[2 * q + 1]);
   }
 }
 
