@@ -73,9 +73,10 @@ __global__ void __launch_bounds__(TILE) k_lusgs_prep32(Lvl L, double alfa1, int 
   const double *g = L.geo, *lc = L.lc;
   const bool visc = L.visc != 0;
   const size_t cell = (size_t)b.cell0 + (size_t)(j - 1) * (b.nx - 1) + (i - 1);
-  char *base = reinterpret_cast<char *>(L.rec);
-  float *rf = reinterpret_cast<float *>(base + cell * RC::BYTES);
-  float *rb = reinterpret_cast<float *>(base + ((size_t)L.ncell + cell) * RC::BYTES);
+  // the two records are assembled in registers and written 16 bytes at a time
+  float rf[RC::NF], rb[RC::NF];
+#pragma unroll
+  for (int k = RC::CI + 8; k < RC::NF; k++) rf[k] = rb[k] = 0.0f;
   double vol = g[G_VOL * F + id];
   double Lv = lc[L_VI * F + id] + lc[L_VJ * F + id];
   double alfa = vol * rcp(lc[L_DT * F + id]) + 1.0 * (lc[L_CI * F + id] + lc[L_CJ * F + id]) + vol * alfa1;
@@ -125,6 +126,14 @@ __global__ void __launch_bounds__(TILE) k_lusgs_prep32(Lvl L, double alfa1, int 
       q[dir == 0 ? RC::N1I : RC::N1J] = (float)(hh * (dir == 0 ? ni1 : nj1));
       q[dir == 0 ? RC::N2I : RC::N2J] = (float)(hh * (dir == 0 ? ni2 : nj2));
     }
+  }
+  char *base = reinterpret_cast<char *>(L.rec);
+  float4 *wf = reinterpret_cast<float4 *>(base + cell * RC::BYTES);
+  float4 *wb = reinterpret_cast<float4 *>(base + ((size_t)L.ncell + cell) * RC::BYTES);
+#pragma unroll
+  for (int k = 0; k < RC::NF / 4; k++) {
+    wf[k] = make_float4(rf[4 * k], rf[4 * k + 1], rf[4 * k + 2], rf[4 * k + 3]);
+    wb[k] = make_float4(rb[4 * k], rb[4 * k + 1], rb[4 * k + 2], rb[4 * k + 3]);
   }
 }
 
