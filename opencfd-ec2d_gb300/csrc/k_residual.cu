@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(TILE) k_prim(Lvl L) {
   double uu = ru * rd, v = rv * rd;
   double T = (E - 0.5 * d * (uu * uu + v * v)) * (rd * c.rCv);
   double p = c.p00 * d * T;
-  const double sT = sqrt(T);
+  const double sT = T > 0.0 ? sqrt_p(T) : sqrt(T);  // the reference's sqrt, NaN for T < 0
   L.q[Q_D * F + id] = d;
   L.q[Q_U * F + id] = uu;
   L.q[Q_V * F + id] = v;
