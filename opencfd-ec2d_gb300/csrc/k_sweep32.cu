@@ -205,10 +205,17 @@ __global__ void __launch_bounds__(1024) k_lusgs_sweep32(Lvl L) {
       const int i = p - j;
       const int buf = p & 1;
       if (row_ok && i >= 1 && i <= ni) {
-        const float *cur = reinterpret_cast<const float *>(rec + (k % RING32) * RC::BYTES);
+        const float4 *cur4 = reinterpret_cast<const float4 *>(rec + (k % RING32) * RC::BYTES);
         if (k + RING32 - 1 < ni) fetch32<NV>(rec + ((k + RING32 - 1) % RING32) * RC::BYTES, src(k + RING32 - 1));
         cp_commit();
         cp_wait_ring();
+        // the whole record into registers with 16-byte shared loads at once
+        float cur[RC::NF];
+#pragma unroll
+        for (int q = 0; q < RC::NF / 4; q++) {
+          const float4 v = cur4[q];
+          cur[4 * q] = v.x; cur[4 * q + 1] = v.y; cur[4 * q + 2] = v.z; cur[4 * q + 3] = v.w;
+        }
         float acc[NV];
 #pragma unroll
         for (int m = 0; m < NV; m++) acc[m] = fwd ? cur[RC::A + m] : 0.0f;
