@@ -243,7 +243,8 @@ __global__ void __launch_bounds__(1024) k_lusgs_sweep32(Lvl L) {
           const float rho = cur[RC::B + 0], m1 = cur[RC::B + 1], m2 = cur[RC::B + 2];
           const float u = cur[RC::BU], v = cur[RC::BV];
           const float dr = st[SL::D + 0], dm1 = st[SL::D + 1], dm2 = st[SL::D + 2], dE = st[SL::D + 3];
-          const float rr = __frcp_rn(rho + dr);
+          float rr;  // 1 / (rho + d rho): the approximate reciprocal (an FP32 preconditioner)
+          asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rr) : "f"(rho + dr));
           const float du = (dm1 - u * dr) * rr, dv = (dm2 - v * dr) * rr;
           const float up = u + du, vp = v + dv;
           st[SL::UP] = up;
@@ -260,8 +261,12 @@ __global__ void __launch_bounds__(1024) k_lusgs_sweep32(Lvl L) {
         // widens it to FP64 afterwards (FP64 instructions hold a warp for
         // about 64 cycles each, so they stay off the wavefront)
         float *w = reinterpret_cast<float *>(recBw + (size_t)(i - 1) * RC::BYTES);
+        static_assert(RC::A == 0 && SL::D == 0, "A and D open the record and the slot");
 #pragma unroll
-        for (int m = 0; m < NV; m++) w[RC::A + m] = st[SL::D + m];
+        for (int m = 0; m + 3 < NV; m += 4)
+          reinterpret_cast<float4 *>(w)[m / 4] = make_float4(st[m], st[m + 1], st[m + 2], st[m + 3]);
+#pragma unroll
+        for (int m = NV / 4 * 4; m < NV; m++) w[m] = st[m];
         k++;
       }
       __syncthreads();
