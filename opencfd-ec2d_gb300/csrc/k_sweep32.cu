@@ -170,14 +170,105 @@ __device__ __forceinline__ void fetch32(char *dst, const char *src) {
   for (int k = 0; k < R32<NV>::BYTES; k += 16) cp16(dst + k, src + k);
 }
 
+// One pass of a row, forward (FWD) or backward.
+template <int NV, bool fwd>
+__device__ __forceinline__ void sweep32_pass(const Lvl &L, float *shf, char *rec, const char *recF, const char *recB,
+                                             char *recBw, float *st, const BlkDev &bd, int R, int rl, int j,
+                                             bool row_ok, float gm1) {
+  using SL = S32<NV>;
+  using RC = R32<NV>;
+  constexpr int S = SL::S;
+  const int nx = bd.nx, ny = bd.ny, rows = ny - 1, ni = nx - 1;
+  const char *rsrc = fwd ? recF : recB;
+  // record of the k-th visited cell: forward i = 1 + k, backward i = ni - k
+  auto src = [&](int k) { return rsrc + (size_t)(fwd ? k : ni - 1 - k) * RC::BYTES; };
+  for (int q = 0; q < RING32 - 1; q++) {
+    if (row_ok && q < ni) fetch32<NV>(rec + q * RC::BYTES, src(q));
+    cp_commit();
+  }
+  int k = 0;
+  for (int pp = 2; pp <= nx + ny - 2; pp++) {
+    const int p = fwd ? pp : nx + ny - pp;
+    const int i = p - j;
+    const int buf = p & 1;
+    if (row_ok && i >= 1 && i <= ni) {
+      const float4 *cur4 = reinterpret_cast<const float4 *>(rec + (k % RING32) * RC::BYTES);
+      if (k + RING32 - 1 < ni) fetch32<NV>(rec + ((k + RING32 - 1) % RING32) * RC::BYTES, src(k + RING32 - 1));
+      cp_commit();
+      cp_wait_ring();
+      // the whole record into registers with 16-byte shared loads at once
+      float cur[RC::NF];
+#pragma unroll
+      for (int q = 0; q < RC::NF / 4; q++) {
+        const float4 v = cur4[q];
+        cur[4 * q] = v.x; cur[4 * q + 1] = v.y; cur[4 * q + 2] = v.z; cur[4 * q + 3] = v.w;
+      }
+      float acc[NV];
+#pragma unroll
+      for (int m = 0; m < NV; m++) acc[m] = fwd ? cur[RC::A + m] : 0.0f;
+      if (fwd ? (i > 1) : (i < ni)) dflux<NV>(st, cur[RC::N1I], cur[RC::N2I], cur[RC::CI], acc);
+      if (fwd ? (j > 1) : (j < rows)) {
+        const float4 *s4 = reinterpret_cast<const float4 *>(shf + ((size_t)(buf ^ 1) * (R + 2) + (fwd ? rl : rl + 2)) * S);
+        float sn[S];
+#pragma unroll
+        for (int m = 0; m < S / 4; m++) {
+          float4 v = s4[m];
+          sn[4 * m] = v.x; sn[4 * m + 1] = v.y; sn[4 * m + 2] = v.z; sn[4 * m + 3] = v.w;
+        }
+        dflux<NV>(sn, cur[RC::N1J], cur[RC::N2J], cur[RC::CJ], acc);
+      }
+      const float ia = cur[RC::IA], ia5 = cur[RC::IA5];
+#pragma unroll
+      for (int m = 0; m < NV; m++) {
+        float inv = (NV == 5 && m == 4) ? ia5 : ia;
+        st[SL::D + m] = fwd ? acc[m] * inv : cur[RC::A + m] + acc[m] * inv;
+      }
+      // state shipped to the two downstream neighbours
+#pragma unroll
+      for (int m = 0; m < NV; m++) st[SL::B + m] = cur[RC::B + m];
+      {
+        const float rho = cur[RC::B + 0], m1 = cur[RC::B + 1], m2 = cur[RC::B + 2];
+        const float u = cur[RC::BU], v = cur[RC::BV];
+        const float dr = st[SL::D + 0], dm1 = st[SL::D + 1], dm2 = st[SL::D + 2], dE = st[SL::D + 3];
+        float rr;  // 1 / (rho + d rho): the approximate reciprocal (an FP32 preconditioner)
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rr) : "f"(rho + dr));
+        const float du = (dm1 - u * dr) * rr, dv = (dm2 - v * dr) * rr;
+        const float up = u + du, vp = v + dv;
+        st[SL::UP] = up;
+        st[SL::VP] = vp;
+        st[SL::DU] = du;
+        st[SL::DV] = dv;
+        st[SL::DP] = gm1 * (dE - 0.5f * (dm1 * up + m1 * du + dm2 * vp + m2 * dv));
+      }
+      float4 *own = reinterpret_cast<float4 *>(shf + ((size_t)buf * (R + 2) + rl + 1) * S);
+#pragma unroll
+      for (int m = 0; m < S / 4; m++) own[m] = make_float4(st[4 * m], st[4 * m + 1], st[4 * m + 2], st[4 * m + 3]);
+      // forward: the forward dU becomes the A field of this cell's backward
+      // record; backward: the final dU replaces it there, and k_apply32
+      // widens it to FP64 afterwards (FP64 instructions hold a warp for
+      // about 64 cycles each, so they stay off the wavefront)
+      float *w = reinterpret_cast<float *>(recBw + (size_t)(i - 1) * RC::BYTES);
+      static_assert(RC::A == 0 && SL::D == 0, "A and D open the record and the slot");
+#pragma unroll
+      for (int m = 0; m + 3 < NV; m += 4)
+        reinterpret_cast<float4 *>(w)[m / 4] = make_float4(st[m], st[m + 1], st[m + 2], st[m + 3]);
+#pragma unroll
+      for (int m = NV / 4 * 4; m < NV; m++) w[m] = st[m];
+      k++;
+    }
+    __syncthreads();
+  }
+  cp_wait0();
+}
+
 template <int NV>
 __global__ void __launch_bounds__(1024) k_lusgs_sweep32(Lvl L) {
   using SL = S32<NV>;
   using RC = R32<NV>;
   constexpr int S = SL::S;
-  extern __shared__ __align__(16) float shf[];  // [2][rows+2][S] slots, then [blockDim][2] records
+  extern __shared__ __align__(16) float shf[];  // [2][rows+2][S] slots, then [blockDim][RING32] records
   const BlkDev bd = L.blk[blockIdx.x];
-  const int nx = bd.nx, ny = bd.ny, rows = ny - 1, ni = nx - 1;
+  const int rows = bd.ny - 1, ni = bd.nx - 1;
   const int rl = threadIdx.x;
   const int j = rl + 1;
   const int R = blockDim.x;
@@ -190,89 +281,8 @@ __global__ void __launch_bounds__(1024) k_lusgs_sweep32(Lvl L) {
   float st[S];
 #pragma unroll
   for (int m = 0; m < S; m++) st[m] = 0.0f;
-  for (int pass = 0; pass < 2; pass++) {
-    const bool fwd = pass == 0;
-    const char *rsrc = fwd ? recF : recB;
-    // record of the k-th visited cell: forward i = 1 + k, backward i = ni - k
-    auto src = [&](int k) { return rsrc + (size_t)(fwd ? k : ni - 1 - k) * RC::BYTES; };
-    for (int q = 0; q < RING32 - 1; q++) {
-      if (row_ok && q < ni) fetch32<NV>(rec + q * RC::BYTES, src(q));
-      cp_commit();
-    }
-    int k = 0;
-    for (int pp = 2; pp <= nx + ny - 2; pp++) {
-      const int p = fwd ? pp : nx + ny - pp;
-      const int i = p - j;
-      const int buf = p & 1;
-      if (row_ok && i >= 1 && i <= ni) {
-        const float4 *cur4 = reinterpret_cast<const float4 *>(rec + (k % RING32) * RC::BYTES);
-        if (k + RING32 - 1 < ni) fetch32<NV>(rec + ((k + RING32 - 1) % RING32) * RC::BYTES, src(k + RING32 - 1));
-        cp_commit();
-        cp_wait_ring();
-        // the whole record into registers with 16-byte shared loads at once
-        float cur[RC::NF];
-#pragma unroll
-        for (int q = 0; q < RC::NF / 4; q++) {
-          const float4 v = cur4[q];
-          cur[4 * q] = v.x; cur[4 * q + 1] = v.y; cur[4 * q + 2] = v.z; cur[4 * q + 3] = v.w;
-        }
-        float acc[NV];
-#pragma unroll
-        for (int m = 0; m < NV; m++) acc[m] = fwd ? cur[RC::A + m] : 0.0f;
-        if (fwd ? (i > 1) : (i < ni)) dflux<NV>(st, cur[RC::N1I], cur[RC::N2I], cur[RC::CI], acc);
-        if (fwd ? (j > 1) : (j < rows)) {
-          const float4 *s4 = reinterpret_cast<const float4 *>(shf + ((size_t)(buf ^ 1) * (R + 2) + (fwd ? rl : rl + 2)) * S);
-          float sn[S];
-#pragma unroll
-          for (int m = 0; m < S / 4; m++) {
-            float4 v = s4[m];
-            sn[4 * m] = v.x; sn[4 * m + 1] = v.y; sn[4 * m + 2] = v.z; sn[4 * m + 3] = v.w;
-          }
-          dflux<NV>(sn, cur[RC::N1J], cur[RC::N2J], cur[RC::CJ], acc);
-        }
-        const float ia = cur[RC::IA], ia5 = cur[RC::IA5];
-#pragma unroll
-        for (int m = 0; m < NV; m++) {
-          float inv = (NV == 5 && m == 4) ? ia5 : ia;
-          st[SL::D + m] = fwd ? acc[m] * inv : cur[RC::A + m] + acc[m] * inv;
-        }
-        // state shipped to the two downstream neighbours
-#pragma unroll
-        for (int m = 0; m < NV; m++) st[SL::B + m] = cur[RC::B + m];
-        {
-          const float rho = cur[RC::B + 0], m1 = cur[RC::B + 1], m2 = cur[RC::B + 2];
-          const float u = cur[RC::BU], v = cur[RC::BV];
-          const float dr = st[SL::D + 0], dm1 = st[SL::D + 1], dm2 = st[SL::D + 2], dE = st[SL::D + 3];
-          float rr;  // 1 / (rho + d rho): the approximate reciprocal (an FP32 preconditioner)
-          asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rr) : "f"(rho + dr));
-          const float du = (dm1 - u * dr) * rr, dv = (dm2 - v * dr) * rr;
-          const float up = u + du, vp = v + dv;
-          st[SL::UP] = up;
-          st[SL::VP] = vp;
-          st[SL::DU] = du;
-          st[SL::DV] = dv;
-          st[SL::DP] = gm1 * (dE - 0.5f * (dm1 * up + m1 * du + dm2 * vp + m2 * dv));
-        }
-        float4 *own = reinterpret_cast<float4 *>(shf + ((size_t)buf * (R + 2) + rl + 1) * S);
-#pragma unroll
-        for (int m = 0; m < S / 4; m++) own[m] = make_float4(st[4 * m], st[4 * m + 1], st[4 * m + 2], st[4 * m + 3]);
-        // forward: the forward dU becomes the A field of this cell's backward
-        // record; backward: the final dU replaces it there, and k_apply32
-        // widens it to FP64 afterwards (FP64 instructions hold a warp for
-        // about 64 cycles each, so they stay off the wavefront)
-        float *w = reinterpret_cast<float *>(recBw + (size_t)(i - 1) * RC::BYTES);
-        static_assert(RC::A == 0 && SL::D == 0, "A and D open the record and the slot");
-#pragma unroll
-        for (int m = 0; m + 3 < NV; m += 4)
-          reinterpret_cast<float4 *>(w)[m / 4] = make_float4(st[m], st[m + 1], st[m + 2], st[m + 3]);
-#pragma unroll
-        for (int m = NV / 4 * 4; m < NV; m++) w[m] = st[m];
-        k++;
-      }
-      __syncthreads();
-    }
-    cp_wait0();
-  }
+  sweep32_pass<NV, true>(L, shf, rec, recF, recB, recBw, st, bd, R, rl, j, row_ok, gm1);
+  sweep32_pass<NV, false>(L, shf, rec, recF, recB, recBw, st, bd, R, rl, j, row_ok, gm1);
 }
 
 // dU (FP32, in the backward records) -> U += dU in FP64, or -> L.du
