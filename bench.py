@@ -422,8 +422,17 @@ def run_gb300(args, rank, world):
     for _ in range(max(3, args.warmup)):
         g.step(1)
     g.sync()
-    tune = (lambda: g.autotune(3)) if args.autotune else (lambda: (1, 32, 1, None))
-    tuned = {"fp64": dict(zip(("lusgs_ctas", "rows_per_warp", "concurrent_faces", "ms"), tune()))}
+    tune = (lambda: g.autotune(3)) if args.autotune else (lambda: (0, 24, 1, None))
+
+    def shape(t):
+        # lusgs_ctas 0: four lanes per row, bands of at most `rows` rows on a
+        # cluster; 1: one CTA per block, `rows` rows per warp; >1: a cluster
+        # of that many CTAs with a barrier per plane
+        cs, rpw, cc, ms = t
+        return {"lusgs_kernel": "four-lane bands" if cs == 0 else "one-lane", "lusgs_ctas": cs, "rows": rpw,
+                "concurrent_faces": cc, "ms": ms}
+
+    tuned = {"fp64": shape(tune())}
 
     def barrier():
         torch.cuda.synchronize()
@@ -477,7 +486,7 @@ def run_gb300(args, rank, world):
     for _ in range(3):
         g.step(1)
     g.sync()
-    tuned["mixed"] = dict(zip(("lusgs_ctas", "rows_per_warp", "concurrent_faces", "ms"), tune()))
+    tuned["mixed"] = shape(tune())
     barrier()
     ms32, launches32 = timed_steps(torch, g, stream, flush, args.steps)
     barrier()

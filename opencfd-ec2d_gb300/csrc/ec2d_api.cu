@@ -82,6 +82,7 @@ struct Level {
   std::vector<int> case_face0, case_nface;
   long long F = 0;
   int max_rows = 0;   // widest block (ny-1) of the level: LU-SGS threads per CTA
+  int max_cols = 0;   // longest row of cells (nx-1) of the level's blocks
   int bc_max_nodes = 0;  // most boundary nodes of one far-field / symmetry subface
   bool fast64 = false, fast32 = false;  // wavefront LU-SGS fits one CTA (FP64 / FP32 records)
   Lvl L{};
@@ -112,10 +113,10 @@ struct ec2d_ctx {
   int last_err = 0;
   // launch accounting and optional per-kernel event timing
   long long launches = 0;
-  int lusgs_cs = 1;  // CTAs per block in the LU-SGS wavefront (1: one CTA, >1: a cluster)
+  int lusgs_cs = 0;  // LU-SGS wavefront shape: 0 four lanes per row where it fits, 1 one CTA per block, >1 a cluster
   bool lusgs_fp32 = false;  // LU-SGS sweeps in FP32 (mixed-precision mode)
   bool concurrent = true;   // i- and j-face flux kernels on two streams
-  int lusgs_rpw = 32;       // rows per warp of the FP64 wavefront (one CTA per block)
+  int lusgs_rpw = 24;       // most rows per CTA of the four-lane kernel, or rows per warp of the one-lane one
   bool coarse_fp32 = false; // face fluxes of multigrid levels >= 2 in FP32
   bool timing = false;
   // one pseudo-time step (single grid or V-cycle) captured as a CUDA graph:
@@ -525,6 +526,7 @@ int build_level(ec2d_ctx *ctx, int l) {
   L.met = anyfdm ? dalloc<double>(lv, 5 * F) : nullptr;
   L.fdm = anyfdm ? dalloc<double>(lv, 30 * F) : nullptr;
   for (auto &B : lv.hb) lv.max_rows = std::max(lv.max_rows, B.ny - 1);
+  for (auto &B : lv.hb) lv.max_cols = std::max(lv.max_cols, B.nx - 1);
   // wavefront LU-SGS: one thread per row, its shared memory must fit one CTA
   const size_t smem_max = 227 * 1024;
   lv.fast64 = lv.max_rows <= 1024 && lusgs_smem(nv, lv.max_rows) <= smem_max;
@@ -748,7 +750,7 @@ void lusgs_update(ec2d_ctx *ctx, int l, double alfa1, bool force = false) {
   if (ctx->lusgs_fp32 && lv.fast32) {
     K(ctx, "k_lusgs32", l, 3, [&] { launch_lusgs_fast32(L, alfa1, mode, lv.max_rows, ctx->stream); });
   } else if (lv.fast64) {
-    K(ctx, "k_lusgs", l, 2, [&] { launch_lusgs_fast(L, alfa1, mode, lv.max_rows, ctx->lusgs_cs, ctx->lusgs_rpw, ctx->stream); });
+    K(ctx, "k_lusgs", l, 2, [&] { launch_lusgs_fast(L, alfa1, mode, lv.max_rows, lv.max_cols, ctx->lusgs_cs, ctx->lusgs_rpw, ctx->stream); });
   } else {
     if (force) K(ctx, "k_add_force", l, 1, [&] { launch_add_force(L, ctx->stream); });
     K(ctx, "k_lusgs_generic", l, 1, [&] { launch_lusgs(L, alfa1, ctx->stream); });
@@ -963,6 +965,12 @@ int check_launch(ec2d_ctx *ctx) {
   return EC2D_OK;
 }
 
+// the error a case's device status code stands for: 3 the T < 1e-5 stop of
+// the primitives, 4 a wavefront wait that gave up
+int status_error(int code) {
+  return code == 0 ? EC2D_OK : code == EC2D_ERR_TIMEOUT ? EC2D_ERR_TIMEOUT : EC2D_ERR_STATE;
+}
+
 }  // namespace
 
 // =============================== C-ABI =====================================
@@ -991,7 +999,8 @@ int ec2d_create(int device, ec2d_ctx **out) {
   CK(cudaSetDevice(device));
   ec2d_ctx *c = new ec2d_ctx();
   c->device = device;
-  if (const char *e = getenv("EC2D_LUSGS_CLUSTER")) c->lusgs_cs = std::max(1, std::min(8, atoi(e)));
+  if (const char *e = getenv("EC2D_LUSGS_CLUSTER")) c->lusgs_cs = std::max(0, std::min(8, atoi(e)));
+  if (const char *e = getenv("EC2D_LUSGS_ROWS")) c->lusgs_rpw = std::max(8, std::min(32, atoi(e)));
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
@@ -1238,13 +1247,13 @@ int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *rows_per_w
   cudaEvent_t a, b;
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
-  // candidates: the FP64 wavefront's shape -- one CTA per block with 32, 24
-  // or 16 rows per warp, or a cluster of 2, 4, 8 CTAs (the FP32 sweep has
-  // one shape) -- x concurrent face kernels
-  std::vector<std::pair<int, int>> shapes = {{1, 32}};
+  // candidates: the FP64 wavefront's shape -- four lanes per row (where it
+  // fits), one CTA per block with 32, 24 or 16 rows per warp, or a cluster of
+  // 2, 4, 8 CTAs (the FP32 sweep has one shape) -- x concurrent face kernels
+  std::vector<std::pair<int, int>> shapes = {{0, 24}};
   if (!ctx->lusgs_fp32 && ctx->P.Time_Method == Time_LU_SGS)
-    for (auto sh : {std::make_pair(1, 24), std::make_pair(1, 16), std::make_pair(2, 32), std::make_pair(4, 32),
-                    std::make_pair(8, 32)})
+    for (auto sh : {std::make_pair(0, 32), std::make_pair(0, 16), std::make_pair(1, 32), std::make_pair(1, 24),
+                    std::make_pair(1, 16), std::make_pair(2, 32), std::make_pair(4, 32), std::make_pair(8, 32)})
       shapes.push_back(sh);
   const int old_cs = ctx->lusgs_cs, old_rpw = ctx->lusgs_rpw;
   const bool old_cc = ctx->concurrent;
@@ -1325,7 +1334,7 @@ int ec2d_residual(ec2d_ctx *ctx, int case_id, int mesh, double res_max[6], doubl
   if (res_rms) for (int m = 0; m < 6; m++) res_rms[m] = nm[6 + m];
   if (kstep) *kstep = ctx->cases[case_id - 1].kstep[mesh];
   if (tt) *tt = ctx->cases[case_id - 1].tt[mesh];
-  return st[0] ? EC2D_ERR_STATE : EC2D_OK;
+  return status_error(st[0]);
 }
 
 int ec2d_run_to_drop(ec2d_ctx *ctx, double drop, const double *r0, int max_steps, double max_seconds,
@@ -1343,7 +1352,7 @@ int ec2d_run_to_drop(ec2d_ctx *ctx, double drop, const double *r0, int max_steps
     CK(cudaMemcpyAsync(nm.data(), L.norms, nm.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(st.data(), L.status, st.size() * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    for (int c = 0; c < nc; c++) if (st[4 * c]) return EC2D_ERR_STATE;
+    for (int c = 0; c < nc; c++) if (st[4 * c]) return status_error(st[4 * c]);
     return EC2D_OK;
   };
   int n = 0, r;
@@ -1520,7 +1529,7 @@ int ec2d_du_lusgs(ec2d_ctx *ctx, int mesh, double alfa1) {
   const Level &lv = ctx->lv[mesh];
   const Lvl &L = lv.L;
   if (ctx->lusgs_fp32 && lv.fast32) launch_lusgs_fast32(L, alfa1, 0, lv.max_rows, ctx->stream);
-  else if (lv.fast64) launch_lusgs_fast(L, alfa1, 0, lv.max_rows, ctx->lusgs_cs, ctx->lusgs_rpw, ctx->stream);
+  else if (lv.fast64) launch_lusgs_fast(L, alfa1, 0, lv.max_rows, lv.max_cols, ctx->lusgs_cs, ctx->lusgs_rpw, ctx->stream);
   else launch_lusgs(L, alfa1, ctx->stream);
   return check_launch(ctx);
 }

@@ -34,7 +34,11 @@ int lusgs_planes(int nv);
 // mode bits of the wavefront launchers: update U in the sweep, and take
 // Res + QF for Res (a coarse level's forcing when its residual is reused)
 enum { LUSGS_UPDATE = 1, LUSGS_FORCE = 2 };
-void launch_lusgs_fast(const Lvl &L, double alfa1, int mode, int max_rows, int cs, int rpw, cudaStream_t s);
+// cs: 0 the four-lanes-per-row kernel where it fits, with at most rpw rows
+// per CTA (else one CTA per block), 1 one CTA per block with rpw rows per
+// warp, 2..8 a cluster of cs CTAs with a barrier per plane
+void launch_lusgs_fast(const Lvl &L, double alfa1, int mode, int max_rows, int max_cols, int cs, int rpw,
+                       cudaStream_t s);
 size_t lusgs_smem(int nv, int rows);  // dynamic shared memory of the one-CTA FP64 sweep
 void launch_lusgs_fast32(const Lvl &L, double alfa1, int mode, int max_rows, cudaStream_t s);
 size_t lusgs32_smem(int nv, int rows);

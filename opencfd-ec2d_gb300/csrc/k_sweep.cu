@@ -521,6 +521,291 @@ void launch_lanes(const Lvl &L, int update, int R, cudaStream_t s) {
   else k_lusgs_sweep_lanes<NV, false, LPR><<<L.nblk, th, smem, s>>>(L, R);
 }
 
+// ---- mean flow only (NV = 4): four lanes per row, row bands on a cluster -----
+//
+// Lane q of a row owns variable q.  A neighbour's state is held as
+// X = (rho, rho u, rho v, H = E + p) with u, v, p, so that its flux plus
+// dissipation in variable q is one pair of FMAs, X_q w + p c_q with
+// w = u n1 + v n2 + cc and c = (0, n1, n2, -cc) (E w + p un = H w - p cc).
+// Per cell and lane that leaves 19 FP64 operations: 2 x 4 for the two
+// neighbours, one for the update, and rcp(rho), u, v, p, H of the new state
+// (formed by every lane of the row after the four variables are gathered by
+// shuffles).  A CTA holds at most 32 rows (four warps, one per SM
+// sub-partition); a block with more rows is split into bands of R rows on
+// the CTAs of a cluster.  The band edge does not wait for a barrier: the edge
+// row of the upstream band writes each new state straight into the
+// downstream CTA's inbox (one 64-byte entry and one mbarrier per column,
+// through distributed shared memory), and the downstream edge row waits for
+// that column's entry only, so the bands run as a pipeline a few planes apart.
+// The per-lane pressure coefficient c_q is a record field picked by a
+// per-lane offset and masked or sign-flipped with integer operations, so
+// the lanes of a row run one instruction stream without branches or FP64
+// selects.
+constexpr int QROWS = 32;        // rows per CTA
+constexpr int QCOLS = 1024;      // cells per row the inboxes hold
+constexpr int QWAIT = 1 << 22;   // polls of an inbox mbarrier before the wait gives up
+
+struct QRec {
+  double a, u, c0, ki, kj;  // ki, kj: the lane's raw coefficient field of face i and j
+  double2 c, ia, ni, nj;    // (0.5 Lc + Lv) i / j, 1/alfa, scaled normals of face i and j
+};
+// per-lane record offsets of the pressure coefficient c_q: n1 (q = 1), n2
+// (q = 2), cc (q = 3, sign flipped below), any field for q = 0 (zeroed)
+struct QLane {
+  int offi, offj;
+  unsigned keep, sign;
+};
+__device__ __forceinline__ QLane qlane(int q) {
+  using RC = Rec<4>;
+  QLane l;
+  l.offi = q == 1 ? RC::N1I : q == 2 ? RC::N2I : RC::CI;
+  l.offj = q == 1 ? RC::N1J : q == 2 ? RC::N2J : RC::CJ;
+  l.keep = q == 0 ? 0u : 0xffffffffu;
+  l.sign = q == 3 ? 0x80000000u : 0u;
+  return l;
+}
+// c_q from the raw field by integer operations only (zero for q = 0, -cc for q = 3)
+__device__ __forceinline__ double qcoef(double x, const QLane &l) {
+  return __hiloint2double((__double2hiint(x) & (int)l.keep) ^ (int)l.sign, __double2loint(x) & (int)l.keep);
+}
+template <bool FWD, bool update>
+__device__ __forceinline__ void qload(QRec &r, const double *rec, int q, const QLane &l) {
+  using RC = Rec<4>;
+  r.a = __ldcg(rec + RC::A + q);
+  if (FWD || !update) r.u = __ldcg(rec + RC::U + q);
+  if (!FWD) r.c0 = __ldcg(rec + RC::C0 + q);
+  r.ki = __ldcg(rec + l.offi);
+  r.kj = __ldcg(rec + l.offj);
+  const double2 *p2 = reinterpret_cast<const double2 *>(rec + RC::CI);
+  r.c = __ldcg(p2);
+  r.ia = __ldcg(p2 + 1);
+  r.ni = __ldcg(p2 + 2);
+  r.nj = __ldcg(p2 + 3);
+}
+// Inbox entries arrive by st.async, each 16-byte store counting its bytes on
+// the entry's mbarrier in the receiving CTA: no fence on the sending side.
+// The receiver arms every entry's mbarrier at start-up (one arrival expecting
+// 64 bytes), so phase 0 completes when the entry has landed.
+__device__ __forceinline__ void qarm(unsigned long long *mb) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(mb);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(1) : "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(64) : "memory");
+}
+// bounded wait for an inbox entry (phase 0 of its mbarrier); false: gave up
+__device__ __forceinline__ bool qwait(const unsigned long long *mb) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(mb);
+  for (int n = 0; n < QWAIT; n++) {
+    unsigned done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], 0;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(a)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void qsend2(unsigned raddr, double x, double y, unsigned rmb) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f64 [%0], {%1, %2}, [%3];" ::"r"(raddr),
+               "d"(x), "d"(y), "r"(rmb)
+               : "memory");
+}
+
+struct QBand {
+  int R, CS, rl, q, j, rows, ni, bk;
+  unsigned rank;
+  bool row_ok;
+};
+
+// One pass of a band.  Records are requested two cells ahead into three
+// register sets used in turn by plane number mod 3 (the loop is unrolled by
+// three, so no set is ever copied while its loads are in flight): a record
+// has two planes to arrive, enough for a read that crosses to the other
+// die's L2.  The band-edge state goes to the next band before this plane's
+// global stores, so the release that publishes it waits only for stores of
+// earlier planes.
+template <bool update, bool FWD>
+__device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBand &B, double *slot, double *inbox,
+                                      unsigned long long *mbar, unsigned rbox, unsigned rmbar, const double *rsrc,
+                                      double *recBw, double gm1) {
+  using RC = Rec<4>;
+  const int R = B.R, rl = B.rl, q = B.q, j = B.j, rows = B.rows, ni = B.ni;
+  const long long F = L.F;
+  const QLane ln = qlane(q);
+  // this row's neighbour across the band edge comes through the inbox; the
+  // band's edge row feeds the next band's inbox
+  const bool from_box = B.row_ok && (FWD ? (rl == 0 && B.rank > 0) : (rl == R - 1 && (int)B.rank + 1 < B.CS && j < rows));
+  const bool to_box = B.row_ok && (FWD ? (rl == R - 1 && (int)B.rank + 1 < B.CS && j < rows) : (rl == 0 && B.rank > 0));
+  auto src = [&](int k) { return rsrc + (size_t)(FWD ? k : ni - 1 - k) * RC::N; };
+  const int j0 = (int)B.rank * R + 1, j1 = min((int)B.rank * R + R, rows);
+  const int plo = j0 + 1, phi = j1 + ni;  // planes holding a cell of this band
+  // plane p of this pass reads the record in set (pass position of p) mod 3
+  auto pos = [&](int p) { return FWD ? p - plo : phi - p; };
+  QRec r0, r1, r2;
+  if (B.row_ok) {
+    const int m0 = pos(FWD ? j + 1 : ni + j) % 3;  // set of the row's first cell
+    if (m0 == 0) { qload<FWD, update>(r0, src(0), q, ln); if (ni > 1) qload<FWD, update>(r1, src(1), q, ln); }
+    else if (m0 == 1) { qload<FWD, update>(r1, src(0), q, ln); if (ni > 1) qload<FWD, update>(r2, src(1), q, ln); }
+    else { qload<FWD, update>(r2, src(0), q, ln); if (ni > 1) qload<FWD, update>(r0, src(1), q, ln); }
+  }
+  double wx = 0.0, wu = 0.0, wv = 0.0, wp = 0.0;  // the row's previous cell
+  int gave_up = 0;                                 // first column whose inbox wait gave up
+  const int gl = (threadIdx.x & 31) & ~3;
+  // cur: this plane's record; ahead: the set two planes on (free since the last plane)
+  auto plane = [&](int p, const QRec &cur, QRec &ahead) {
+    const int i = p - j, buf = p & 1;
+    const bool act = B.row_ok && i >= 1 && i <= ni;
+    const int k = FWD ? i - 1 : ni - i;
+    if (act && k + 2 < ni) qload<FWD, update>(ahead, src(k + 2), q, ln);
+    double st = 0.0, dn = 0.0;
+    if (act) {
+      double acc = FWD ? cur.a : cur.c0;
+      if (FWD ? (i > 1) : (i < ni)) {
+        const double w = fma(wu, cur.ni.x, fma(wv, cur.ni.y, cur.c.x));
+        acc = fma(wx, w, fma(wp, qcoef(cur.ki, ln), acc));
+      }
+      if (FWD ? (j > 1) : (j < rows)) {
+        const double *s;
+        if (from_box) {
+          if (!qwait(mbar + i - 1) && !gave_up) gave_up = i;
+          s = inbox + (size_t)(i - 1) * 8;
+        } else {
+          s = slot + ((size_t)(buf ^ 1) * R + (FWD ? rl - 1 : rl + 1)) * 8;
+        }
+        const double2 uv = *reinterpret_cast<const double2 *>(s + 4);
+        const double sp = s[6], sx = s[q];
+        const double w = fma(uv.x, cur.nj.x, fma(uv.y, cur.nj.y, cur.c.y));
+        acc = fma(sx, w, fma(sp, qcoef(cur.kj, ln), acc));
+      }
+      if (update) {
+        // U + dU* going forward (carried in the backward record), U + dU* + dU** going backward
+        st = fma(acc, cur.ia.x, FWD ? cur.u : cur.a);
+      } else {
+        dn = FWD ? acc * cur.ia.x : fma(acc, cur.ia.x, cur.a);
+        st = cur.u + dn;
+      }
+    }
+    const double s0 = __shfl_sync(0xffffffffu, st, gl), s1 = __shfl_sync(0xffffffffu, st, gl + 1);
+    const double s2 = __shfl_sync(0xffffffffu, st, gl + 2), s3 = __shfl_sync(0xffffffffu, st, gl + 3);
+    if (act) {
+      const double rd = rcp(s0);
+      const double u = s1 * rd, v = s2 * rd;
+      const double pr = gm1 * fma(-0.5, fma(s2, v, s1 * u), s3);
+      const double H = s3 + pr;
+      const double x = q == 3 ? H : st;
+      if (to_box && q == 0) {
+        const unsigned a = rbox + 64u * (unsigned)(i - 1), m = rmbar + 8u * (unsigned)(i - 1);
+        qsend2(a, s0, s1, m);
+        qsend2(a + 16u, s2, H, m);
+        qsend2(a + 32u, u, v, m);
+        qsend2(a + 48u, pr, 0.0, m);
+      }
+      double *o = slot + ((size_t)buf * R + rl) * 8;
+      o[q] = x;
+      if (q == 0) *reinterpret_cast<double2 *>(o + 4) = make_double2(u, v);
+      if (q == 1) o[6] = pr;
+      wx = x; wu = u; wv = v; wp = pr;
+      if (FWD) {
+        recBw[(size_t)(i - 1) * RC::N + RC::A + q] = update ? st : dn;
+      } else {
+        // an updating sweep writes U only (DU is read nowhere but inside
+        // du_LU_SGS_2D and the update that follows it)
+        const long long id = bd.off + (long long)(j + 2) * bd.P + (i + 2);
+        if (update) L.U[q * F + id] = st;
+        else L.du[q * F + id] = dn;
+      }
+    }
+    __syncthreads();
+  };
+  const int np = phi - plo + 1;  // planes of the pass; positions past np - 1 hold no cell
+  for (int t = 0; t < np; t += 3) {
+    plane(FWD ? plo + t : phi - t, r0, r2);
+    plane(FWD ? plo + t + 1 : phi - t - 1, r1, r0);
+    plane(FWD ? plo + t + 2 : phi - t - 2, r2, r1);
+  }
+  if (gave_up) set_status(L.status + 4 * bd.cas, 4, B.bk, gave_up, j);
+}
+
+template <bool update>
+__global__ void __launch_bounds__(4 * QROWS, 1) k_lusgs_sweep_quad(Lvl L, int R, int CS) {
+  extern __shared__ __align__(16) double sh[];  // [2][R][8] slots | inbox F [ni][8] | inbox B | mbarriers F [ni] | B
+  QBand B;
+  B.rank = CS > 1 ? cluster_rank() : 0u;
+  B.bk = blockIdx.x / CS;
+  const BlkDev bd = L.blk[B.bk];  // by value: no re-reads after global stores
+  B.R = R; B.CS = CS;
+  B.rows = bd.ny - 1;
+  B.ni = bd.nx - 1;
+  B.rl = threadIdx.x >> 2;
+  B.q = threadIdx.x & 3;
+  B.j = (int)B.rank * R + B.rl + 1;
+  B.row_ok = B.rl < R && B.j <= B.rows;
+  const int ni = B.ni;
+  const double gm1 = L.cs[bd.cas].gamma - 1.0;
+  double *slot = sh;
+  double *inF = sh + (size_t)2 * R * 8, *inB = inF + (size_t)ni * 8;
+  unsigned long long *mbF = reinterpret_cast<unsigned long long *>(inB + (size_t)ni * 8), *mbB = mbF + ni;
+  unsigned rboxF = 0, rmbF = 0, rboxB = 0, rmbB = 0;
+  if (CS > 1) {
+    for (int t = threadIdx.x; t < 2 * ni; t += blockDim.x) qarm(mbF + t);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if ((int)B.rank + 1 < CS) { rboxF = remote_smem(inF, B.rank + 1); rmbF = remote_smem(mbF, B.rank + 1); }
+    if (B.rank > 0) { rboxB = remote_smem(inB, B.rank - 1); rmbB = remote_smem(mbB, B.rank - 1); }
+    cluster_barrier();  // every inbox armed before any CTA writes into one
+  }
+  const int jr = B.row_ok ? B.j : 1;  // record pointers of idle rows stay in the array
+  const double *recF = L.rec + ((size_t)bd.cell0 + (size_t)(jr - 1) * ni) * Rec<4>::N;
+  const double *recB = recF + (size_t)L.ncell * Rec<4>::N;
+  double *recBw = L.rec + ((size_t)L.ncell + bd.cell0 + (size_t)(jr - 1) * ni) * Rec<4>::N;
+  qpass<update, true>(L, bd, B, slot, inF, mbF, rboxF, rmbF, recF, recBw, gm1);
+  qpass<update, false>(L, bd, B, slot, inB, mbB, rboxB, rmbB, recB, recBw, gm1);
+  if (CS > 1) cluster_barrier();  // no CTA leaves while a neighbour may still write into it
+}
+
+// the four-lane kernel serves NV = 4 levels whose blocks have at most 8 x 32
+// rows and QCOLS cells per row, when every CTA of the launch gets an SM of
+// its own (with fewer SMs, one lane per row needs fewer FP64 instructions)
+// rmax: most rows per CTA (16, 24 or 32: four, three or two warps share an
+// SM's FP64 unit)
+int quad_ctas(int max_rows, int rmax) {
+  rmax = std::max(8, std::min(rmax, QROWS));
+  return (max_rows + rmax - 1) / rmax;
+}
+bool quad_fits(const Lvl &L, int max_rows, int max_cols, int rmax) {
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  }
+  const int CS = quad_ctas(max_rows, rmax);
+  return L.nvar == 4 && max_rows >= 1 && CS <= 8 && max_cols <= QCOLS && L.nblk * CS <= nsm;
+}
+
+void launch_quad(const Lvl &L, int update, int max_rows, int max_cols, int rmax, cudaStream_t s) {
+  const int CS = quad_ctas(max_rows, rmax);
+  const int R = (max_rows + CS - 1) / CS;
+  const int th = (4 * R + 31) / 32 * 32;
+  const size_t smem = (size_t)2 * R * 8 * sizeof(double) + (CS > 1 ? (size_t)max_cols * 2 * (8 * sizeof(double) + 8) : 0);
+  auto kern = update ? k_lusgs_sweep_quad<true> : k_lusgs_sweep_quad<false>;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(L.nblk * CS);
+  cfg.blockDim = dim3(th);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CS;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, L, R, CS);
+}
+
 // CS == 1: one CTA per block, planes separated by __syncthreads.
 // CS > 1: a cluster of CS CTAs per block, CTA r owns rows r*R+1..r*R+R; the
 // edge rows write into the neighbour CTA's halo slot through distributed
@@ -558,9 +843,17 @@ size_t smem_bytes(int R, int th) {
 }
 
 template <int NV>
-void sweep_nv(const Lvl &L, double alfa1, int mode, int max_rows, int cs, int rpw, cudaStream_t s) {
+void sweep_nv(const Lvl &L, double alfa1, int mode, int max_rows, int max_cols, int cs, int rpw, cudaStream_t s) {
   k_lusgs_prep<NV><<<L.ntiles, TILE, 0, s>>>(L, alfa1, mode & LUSGS_FORCE);
   const int update = mode & LUSGS_UPDATE;
+  if (cs == 0) {
+    if (quad_fits(L, max_rows, max_cols, rpw)) {
+      launch_quad(L, update, max_rows, max_cols, rpw, s);
+      return;
+    }
+    cs = 1;  // one CTA per block, full warps
+    rpw = 32;
+  }
   const int lpr = sweep_lanes_per_row(max_rows);
   if (lpr == 4) { launch_lanes<NV, 4>(L, update, max_rows, s); return; }
   int CS = std::max(1, std::min(cs, std::min(8, (max_rows + 7) / 8)));
@@ -600,10 +893,11 @@ size_t smem_nv(int rows) {
 }
 size_t lusgs_smem(int nv, int rows) { return nv == 4 ? smem_nv<4>(rows) : nv == 5 ? smem_nv<5>(rows) : smem_nv<6>(rows); }
 
-void launch_lusgs_fast(const Lvl &L, double alfa1, int mode, int max_rows, int cs, int rpw, cudaStream_t s) {
-  if (L.nvar == 4) sweep_nv<4>(L, alfa1, mode, max_rows, cs, rpw, s);
-  else if (L.nvar == 5) sweep_nv<5>(L, alfa1, mode, max_rows, cs, rpw, s);
-  else sweep_nv<6>(L, alfa1, mode, max_rows, cs, rpw, s);
+void launch_lusgs_fast(const Lvl &L, double alfa1, int mode, int max_rows, int max_cols, int cs, int rpw,
+                       cudaStream_t s) {
+  if (L.nvar == 4) sweep_nv<4>(L, alfa1, mode, max_rows, max_cols, cs, rpw, s);
+  else if (L.nvar == 5) sweep_nv<5>(L, alfa1, mode, max_rows, max_cols, cs, rpw, s);
+  else sweep_nv<6>(L, alfa1, mode, max_rows, max_cols, cs, rpw, s);
 }
 
 }  // namespace ec2d

@@ -117,9 +117,11 @@ def test_boundary_wall_isothermal_symmetry_sa(gpu_lib):
     compare_U(orc, g, tol=1e-14)
 
 
-# 16 rows per block run the wavefront with four lanes per row, 40 rows with
-# one; NV = 4, 5 (SA), 6 (SST)
-@pytest.mark.parametrize("ny", [17, 41])
+# NV = 4: 16 rows per block run the four-lane kernel in one CTA, 40 and 70
+# rows in bands of 20 and 24 rows on clusters of 2 and 3 CTAs (the last band
+# short).  NV = 5 (SA), 6 (SST): 16 rows run four lanes per row in one CTA,
+# 40 and 70 rows one lane per row.
+@pytest.mark.parametrize("ny", [17, 41, 71])
 @pytest.mark.parametrize("turb", [0, 2, 3])
 def test_lusgs_sweep(gpu_lib, ny, turb):
     kw = dict(Ma=0.7, AoA=2.0, nblocks=2, If_viscous=1, Re=1e4, Iflag_flux=4, ny=ny)
@@ -171,11 +173,16 @@ def test_lusgs_sweep(gpu_lib, ny, turb):
     assert worst <= 1.0, worst
 
 
-@pytest.mark.parametrize("turb", [0, 2])
-def test_lusgs_steps_wide_blocks(gpu_lib, turb):
-    """LU-SGS time steps on 40-row blocks (one lane per row in the wavefront,
-    U updated inside the sweep) against the oracle."""
-    kw = dict(ny=41, Ma=0.6, AoA=2.0, Iflag_flux=4, Iflag_Scheme=5, Time_Method=0, CFL=5.0)
+@pytest.mark.parametrize("turb,ny,shape", [(0, 41, "auto"), (0, 71, "auto"), (0, 41, "one"), (0, 41, "barrier"),
+                                           (2, 41, "auto")])
+def test_lusgs_steps_wide_blocks(gpu_lib, monkeypatch, turb, ny, shape):
+    """LU-SGS time steps on 40- and 70-row blocks (U updated inside the
+    sweep) against the oracle, with each wavefront shape: auto (four lanes per
+    row on a cluster of row bands for NV = 4, one lane per row otherwise), one
+    CTA per block with one lane per row, and a two-CTA cluster with a barrier
+    per plane."""
+    monkeypatch.setenv("EC2D_LUSGS_CLUSTER", {"auto": "0", "one": "1", "barrier": "2"}[shape])
+    kw = dict(ny=ny, Ma=0.6, AoA=2.0, Iflag_flux=4, Iflag_Scheme=5, Time_Method=0, CFL=5.0)
     if turb == 2:
         kw.update(If_viscous=1, Iflag_turbulence_model=2, Re=1e6, first=2e-4)
     p, bl = small_case(**kw)
