@@ -53,10 +53,15 @@ constexpr int TILE = EC2D_TILE;
 //       the reference multiplies the flux difference by +-0.5 s, and the
 //       normal flux is linear in n, so F_n(W, s) = 0.5 s F_n(W, n) and the
 //       constant half F_n(U_nb) of the difference moves into the record
+//  G1I..GCJ  NV = 4 only: (gamma - 1) times n1, n2 and cc of face i and j,
+//       the pressure coefficients of the four-lane sweep, which ships
+//       p / (gamma - 1)
 template <int NV>
 struct Rec {
   static constexpr int A = 0, U = NV, C0 = 2 * NV, CI = 3 * NV, CJ = CI + 1, IA = CI + 2, IA5 = CI + 3,
-                       N1I = CI + 4, N2I = CI + 5, N1J = CI + 6, N2J = CI + 7, N = (CI + 8 + 1) / 2 * 2;
+                       N1I = CI + 4, N2I = CI + 5, N1J = CI + 6, N2J = CI + 7, G1I = CI + 8, G2I = CI + 9,
+                       GCI = CI + 10, G1J = CI + 11, G2J = CI + 12, GCJ = CI + 13,
+                       N = (CI + 8 + (NV == 4 ? 6 : 0) + 1) / 2 * 2;
   static_assert(N % 2 == 0, "records are whole 16-byte units");
 };
 
@@ -70,7 +75,7 @@ struct Slot {
   static_assert(S % 2 == 0, "slots are whole 16-byte units");
 };
 
-int lusgs_planes(int nv) { return 3 * nv + 10; }  // at least Rec<NV>::N and the FP32 record
+int lusgs_planes(int nv) { return 3 * nv + 10 + (nv == 4 ? 4 : 0); }  // at least Rec<NV>::N and the FP32 record
 
 // normal flux of the Euler part (+ convected turbulence variables), the F(U)
 // half of comput_DFn (sub_LU_SGS.f90:122-137)
@@ -172,6 +177,11 @@ __global__ void __launch_bounds__(TILE) k_lusgs_prep(Lvl L, double alfa1, int fo
       r[dir == 0 ? RC::CI : RC::CJ] = cc;
       r[dir == 0 ? RC::N1I : RC::N1J] = s1;
       r[dir == 0 ? RC::N2I : RC::N2J] = s2;
+      if (NV == 4) {
+        r[dir == 0 ? RC::G1I : RC::G1J] = gm1 * s1;
+        r[dir == 0 ? RC::G2I : RC::G2J] = gm1 * s2;
+        r[dir == 0 ? RC::GCI : RC::GCJ] = gm1 * cc;
+      }
     }
   }
 #pragma unroll
@@ -182,7 +192,7 @@ __global__ void __launch_bounds__(TILE) k_lusgs_prep(Lvl L, double alfa1, int fo
     rb[RC::C0 + m] = K[1][m];
   }
 #pragma unroll
-  for (int k = RC::CI + 8; k < RC::N; k++) rf[k] = rb[k] = 0.0;
+  for (int k = RC::CI + 8 + (NV == 4 ? 6 : 0); k < RC::N; k++) rf[k] = rb[k] = 0.0;
   double2 *wf = reinterpret_cast<double2 *>(L.rec + cell * RC::N);
   double2 *wb = reinterpret_cast<double2 *>(L.rec + ((size_t)L.ncell + cell) * RC::N);
 #pragma unroll
@@ -224,8 +234,9 @@ struct Raw {
 };
 template <int NV, bool FWD>
 __device__ __forceinline__ constexpr bool pair_used(int q) {
-  // the forward pass does not read C0
-  return !FWD ? true : !(2 * q >= Rec<NV>::C0 && 2 * q + 1 < Rec<NV>::CI);
+  // the forward pass does not read C0; the pressure coefficients of the
+  // four-lane sweep are not read here
+  return 2 * q < Rec<NV>::CI + 8 && (!FWD ? true : !(2 * q >= Rec<NV>::C0 && 2 * q + 1 < Rec<NV>::CI));
 }
 template <int NV, bool FWD>
 __device__ __forceinline__ void load_raw(Raw<NV> &r, const double *src) {
@@ -524,20 +535,21 @@ void launch_lanes(const Lvl &L, int update, int R, cudaStream_t s) {
 // ---- mean flow only (NV = 4): four lanes per row, row bands on a cluster -----
 //
 // Lane q of a row owns variable q.  A neighbour's state is held as
-// X = (rho, rho u, rho v, H = E + p) with u, v, p, so that its flux plus
-// dissipation in variable q is one pair of FMAs, X_q w + p c_q with
-// w = u n1 + v n2 + cc and c = (0, n1, n2, -cc) (E w + p un = H w - p cc).
-// Per cell and lane that leaves 19 FP64 operations: 2 x 4 for the two
-// neighbours, one for the update, and rcp(rho), u, v, p, H of the new state
-// (formed by every lane of the row after the four variables are gathered by
-// shuffles).  A CTA holds at most 32 rows (four warps, one per SM
-// sub-partition); a block with more rows is split into bands of R rows on
+// X = (rho, rho u, rho v, H = E + p) with u, v and p' = p / (gamma - 1), so
+// that its flux plus dissipation in variable q is one pair of FMAs,
+// X_q w + p' g_q with w = u n1 + v n2 + cc and g = (gamma - 1) (0, n1, n2,
+// -cc) taken from the record (E w + p un = H w - p cc).  Per cell and lane
+// that leaves 18 FP64 operations: 2 x 4 for the two neighbours, one for the
+// update, and rcp(rho), u, v, p', H of the new state (formed by every lane of
+// the row after the four variables are gathered by shuffles).  A CTA holds
+// at most 32 rows (four warps, one per SM sub-partition); a block with more
+// rows is split into bands of R rows on
 // the CTAs of a cluster.  The band edge does not wait for a barrier: the edge
 // row of the upstream band writes each new state straight into the
 // downstream CTA's inbox (one 64-byte entry and one mbarrier per column,
 // through distributed shared memory), and the downstream edge row waits for
 // that column's entry only, so the bands run as a pipeline a few planes apart.
-// The per-lane pressure coefficient c_q is a record field picked by a
+// The per-lane pressure coefficient g_q is a record field picked by a
 // per-lane offset and masked or sign-flipped with integer operations, so
 // the lanes of a row run one instruction stream without branches or FP64
 // selects.
@@ -549,8 +561,9 @@ struct QRec {
   double a, u, c0, ki, kj;  // ki, kj: the lane's raw coefficient field of face i and j
   double2 c, ia, ni, nj;    // (0.5 Lc + Lv) i / j, 1/alfa, scaled normals of face i and j
 };
-// per-lane record offsets of the pressure coefficient c_q: n1 (q = 1), n2
-// (q = 2), cc (q = 3, sign flipped below), any field for q = 0 (zeroed)
+// per-lane record offsets of the pressure coefficient g_q: (gamma - 1) n1
+// (q = 1), n2 (q = 2), cc (q = 3, sign flipped below), any field for q = 0
+// (zeroed)
 struct QLane {
   int offi, offj;
   unsigned keep, sign;
@@ -558,13 +571,13 @@ struct QLane {
 __device__ __forceinline__ QLane qlane(int q) {
   using RC = Rec<4>;
   QLane l;
-  l.offi = q == 1 ? RC::N1I : q == 2 ? RC::N2I : RC::CI;
-  l.offj = q == 1 ? RC::N1J : q == 2 ? RC::N2J : RC::CJ;
+  l.offi = q == 1 ? RC::G1I : q == 2 ? RC::G2I : RC::GCI;
+  l.offj = q == 1 ? RC::G1J : q == 2 ? RC::G2J : RC::GCJ;
   l.keep = q == 0 ? 0u : 0xffffffffu;
   l.sign = q == 3 ? 0x80000000u : 0u;
   return l;
 }
-// c_q from the raw field by integer operations only (zero for q = 0, -cc for q = 3)
+// g_q from the raw field by integer operations only (zero for q = 0, negated for q = 3)
 __device__ __forceinline__ double qcoef(double x, const QLane &l) {
   return __hiloint2double((__double2hiint(x) & (int)l.keep) ^ (int)l.sign, __double2loint(x) & (int)l.keep);
 }
@@ -692,8 +705,8 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
     if (act) {
       const double rd = rcp(s0);
       const double u = s1 * rd, v = s2 * rd;
-      const double pr = gm1 * fma(-0.5, fma(s2, v, s1 * u), s3);
-      const double H = s3 + pr;
+      const double pr = fma(-0.5, fma(s2, v, s1 * u), s3);  // p / (gamma - 1)
+      const double H = fma(gm1, pr, s3);
       const double x = q == 3 ? H : st;
       if (to_box && q == 0) {
         const unsigned a = rbox + 64u * (unsigned)(i - 1), m = rmbar + 8u * (unsigned)(i - 1);
