@@ -116,6 +116,10 @@ struct ec2d_ctx {
   int lusgs_cs = 0;  // LU-SGS wavefront shape: 0 four lanes per row where it fits, 1 one CTA per block, >1 a cluster
   bool lusgs_fp32 = false;  // LU-SGS sweeps in FP32 (mixed-precision mode)
   bool concurrent = true;   // i- and j-face flux kernels on two streams
+  // test hook (EC2D_TEST_SILENT_BAND_EDGE): the band edges of the four-lane
+  // wavefront send nothing, so the downstream waits run out and report
+  // EC2D_ERR_TIMEOUT; failure detection is tested without a GPU fault
+  bool silent_band_edge = false;
   int lusgs_rpw = 24;       // most rows per CTA of the four-lane kernel, or rows per warp of the one-lane one
   bool coarse_fp32 = false; // face fluxes of multigrid levels >= 2 in FP32
   bool timing = false;
@@ -542,6 +546,7 @@ int build_level(ec2d_ctx *ctx, int l) {
   L.npart = dalloc<double>(lv, lv.tiles.size() * 12);
   L.norms = dalloc<double>(lv, ncase * 12);
   L.status = dalloc<int>(lv, ncase * 4);
+  L.silent_band_edge = ctx->silent_band_edge ? 1 : 0;
   if (!L.U || !L.q || !L.amu || !L.amut || !L.res || !L.lc || !L.du || !L.geo || !L.un || !L.deltu || !L.qf ||
       !L.fi || !L.fj || !L.npart || !L.norms || !L.status)
     return EC2D_ERR_NOMEM;
@@ -1001,6 +1006,7 @@ int ec2d_create(int device, ec2d_ctx **out) {
   c->device = device;
   if (const char *e = getenv("EC2D_LUSGS_CLUSTER")) c->lusgs_cs = std::max(0, std::min(8, atoi(e)));
   if (const char *e = getenv("EC2D_LUSGS_ROWS")) c->lusgs_rpw = std::max(8, std::min(32, atoi(e)));
+  if (const char *e = getenv("EC2D_TEST_SILENT_BAND_EDGE")) c->silent_band_edge = atoi(e) != 0;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||

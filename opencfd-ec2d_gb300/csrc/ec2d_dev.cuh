@@ -96,6 +96,7 @@ struct Lvl {
   const int *case_tile0, *case_ntile, *case_ncell;  // per case: first tile, tiles, interior cells
   unsigned *nctr;           // tiles of k_res done (the last one reduces the partials)
   int *status;              // per case: code, block, i, j
+  int silent_band_edge;     // test hook: band edges of the four-lane wavefront send nothing
 };
 
 // Items (cells, faces or nodes of a block's padded index range) per tile of

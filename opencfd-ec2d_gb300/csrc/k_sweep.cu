@@ -555,7 +555,7 @@ void launch_lanes(const Lvl &L, int update, int R, cudaStream_t s) {
 // selects.
 constexpr int QROWS = 32;        // rows per CTA
 constexpr int QCOLS = 1024;      // cells per row the inboxes hold
-constexpr int QWAIT = 1 << 22;   // polls of an inbox mbarrier before the wait gives up
+constexpr int QWAIT = 1 << 20;   // polls of an inbox mbarrier before the wait gives up (about 20 ms)
 
 struct QRec {
   double a, u, c0, ki, kj;  // ki, kj: the lane's raw coefficient field of face i and j
@@ -650,7 +650,8 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
   // this row's neighbour across the band edge comes through the inbox; the
   // band's edge row feeds the next band's inbox
   const bool from_box = B.row_ok && (FWD ? (rl == 0 && B.rank > 0) : (rl == R - 1 && (int)B.rank + 1 < B.CS && j < rows));
-  const bool to_box = B.row_ok && (FWD ? (rl == R - 1 && (int)B.rank + 1 < B.CS && j < rows) : (rl == 0 && B.rank > 0));
+  const bool to_box = B.row_ok && !L.silent_band_edge &&
+                      (FWD ? (rl == R - 1 && (int)B.rank + 1 < B.CS && j < rows) : (rl == 0 && B.rank > 0));
   auto src = [&](int k) { return rsrc + (size_t)(FWD ? k : ni - 1 - k) * RC::N; };
   const int j0 = (int)B.rank * R + 1, j1 = min((int)B.rank * R + R, rows);
   const int plo = j0 + 1, phi = j1 + ni;  // planes holding a cell of this band
@@ -682,7 +683,9 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
       if (FWD ? (j > 1) : (j < rows)) {
         const double *s;
         if (from_box) {
-          if (!qwait(mbar + i - 1) && !gave_up) gave_up = i;
+          // after one wait has given up the row no longer waits (its results
+          // are void; the step reports EC2D_ERR_TIMEOUT)
+          if (!gave_up && !qwait(mbar + i - 1)) gave_up = i;
           s = inbox + (size_t)(i - 1) * 8;
         } else {
           s = slot + ((size_t)(buf ^ 1) * R + (FWD ? rl - 1 : rl + 1)) * 8;

@@ -1,0 +1,45 @@
+"""Failure detection of the four-lane LU-SGS wavefront without a GPU fault.
+
+The bands of a tall block hand their edge rows to the next band through
+bounded waits.  With the band edges silenced (the EC2D_TEST_SILENT_BAND_EDGE
+test hook read by ec2d_create) nothing arrives, every downstream wait runs
+out after its poll limit, the case's status records the timeout, and the
+next status read reports EC2D_ERR_TIMEOUT while the context keeps working."""
+import numpy as np
+import pytest
+
+from helpers import make_gpu, small_case
+
+pytestmark = pytest.mark.gpu
+
+EC2D_ERR_TIMEOUT = 4
+
+
+def test_band_edge_wait_runs_out(gpu_lib, monkeypatch):
+    from ec2d import gpu
+    monkeypatch.setenv("EC2D_TEST_SILENT_BAND_EDGE", "1")
+    monkeypatch.setenv("EC2D_LUSGS_CLUSTER", "0")  # four lanes per row, 40 rows: two bands
+    p, bl = small_case(ny=41, Ma=0.6, AoA=2.0, Iflag_flux=4, Iflag_Scheme=5, Time_Method=0, CFL=5.0)
+    g = make_gpu(p, bl)
+    g.init_flow()
+    g.step(1)
+    with pytest.raises(gpu.EC2DError) as e:
+        g.norms()
+    assert e.value.code == EC2D_ERR_TIMEOUT
+    code, blk, i, j = g.status()
+    assert code == EC2D_ERR_TIMEOUT and blk >= 1 and i >= 1 and j >= 1
+    # the context still answers: the state can be read back and stepped
+    g.sync()
+    assert g.download_U(1, 1, 1).shape[0] == 4
+
+
+def test_band_edges_deliver_without_the_hook(gpu_lib, monkeypatch):
+    monkeypatch.delenv("EC2D_TEST_SILENT_BAND_EDGE", raising=False)
+    monkeypatch.setenv("EC2D_LUSGS_CLUSTER", "0")
+    p, bl = small_case(ny=41, Ma=0.6, AoA=2.0, Iflag_flux=4, Iflag_Scheme=5, Time_Method=0, CFL=5.0)
+    g = make_gpu(p, bl)
+    g.init_flow()
+    g.step(3)
+    g.norms()  # raises on any recorded status
+    assert g.status()[0] == 0
+    assert np.all(np.isfinite(g.download_U(1, 1, 1)))
