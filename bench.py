@@ -422,15 +422,15 @@ def run_gb300(args, rank, world):
     for _ in range(max(3, args.warmup)):
         g.step(1)
     g.sync()
-    tune = (lambda: g.autotune(3)) if args.autotune else (lambda: (0, 24, 1, None))
+    tune = (lambda: g.autotune(3)) if args.autotune else (lambda: (0, 12, 1, None))
 
     def shape(t):
-        # lusgs_ctas 0: four lanes per row, bands of at most `rows` rows on a
-        # cluster; 1: one CTA per block, `rows` rows per warp; >1: a cluster
-        # of that many CTAs with a barrier per plane
+        # lusgs_ctas 0: bands of at most `rows` rows on a cluster, eight lanes
+        # per row up to 16 rows, four above; 1: one CTA per block, `rows` rows
+        # per warp; >1: a cluster of that many CTAs with a barrier per plane
         cs, rpw, cc, ms = t
-        return {"lusgs_kernel": "four-lane bands" if cs == 0 else "one-lane", "lusgs_ctas": cs, "rows": rpw,
-                "concurrent_faces": cc, "ms": ms}
+        kind = "one-lane" if cs != 0 else ("eight-lane bands" if rpw <= 16 else "four-lane bands")
+        return {"lusgs_kernel": kind, "lusgs_ctas": cs, "rows": rpw, "concurrent_faces": cc, "ms": ms}
 
     tuned = {"fp64": shape(tune())}
 
@@ -477,9 +477,17 @@ def run_gb300(args, rank, world):
                             sorted(kt.items(), key=lambda kv: -kv[1][2])[:12]}}
     if kname == "k_lusgs":
         mhz = clocks.get("sm_mhz") or 2070.0
-        roofline["cycles_per_plane"] = avg_ms * 1e-3 * mhz * 1e6 / SWEEP_PLANES(blocks, klev)
-        roofline["latency_note"] = ("wavefront sweep: one dependent chain of FP64 operations per hyperplane, "
-                                    "FP64 warp instruction latency 64 cycles on this part")
+        cpp = avg_ms * 1e-3 * mhz * 1e6 / SWEEP_PLANES(blocks, klev)
+        # the FP64 chain of one plane: 15 operations per cell and lane with
+        # eight lanes per row, 18 with four, 31 per cell with one, 64 cycles each
+        kind = tuned["fp64"]["lusgs_kernel"]
+        floor = {"eight-lane bands": 15, "four-lane bands": 18}.get(kind, 31) * 64
+        roofline["cycles_per_plane"] = cpp
+        roofline["fp64_chain_floor_cycles_per_plane"] = floor
+        roofline["of_chain_floor"] = floor / cpp
+        roofline["latency_note"] = ("wavefront sweep (prep + sweep timed): one dependent chain of FP64 operations "
+                                    "per hyperplane, FP64 warp instruction latency 64 cycles on this part; "
+                                    "of_chain_floor = that chain's cycles / measured cycles per plane")
 
     # ---- mixed precision: the same V-cycle with FP32 LU-SGS sweeps ----------
     g.set_lusgs_precision(32)

@@ -278,16 +278,18 @@ int ec2d_mlp_predict(ec2d_mlp *m, const float *feat, long long n, float *pred);
 
 /* Autotuner.  No counterpart in the reference.  Times `trial_steps` steps of
  * every candidate launch configuration on the context's own cases and keeps
- * the fastest: the shape of the FP64 LU-SGS wavefront (lusgs_cs = 0: four
- * lanes per row, row bands of at most 32 rows on the CTAs of a cluster, where
- * the level has 4 variables and at most 256 rows and 1024 cells per row, else
- * as 1; 1: one CTA per block with 32, 24 or 16 rows per warp; 2, 4, 8: a
- * thread-block cluster of that many CTAs with a barrier per plane) and
+ * the fastest: the shape of the FP64 LU-SGS wavefront (lusgs_cs = 0: row
+ * bands of at most rows_per_warp rows on the CTAs of a cluster, eight lanes
+ * per row for bands of up to 16 rows and four for taller ones, where the
+ * level has 4 variables, at most 8 bands and 1024 cells per row, else as 1;
+ * 1: one CTA per block with rows_per_warp (32, 24 or 16) rows per warp; 2, 4,
+ * 8: a thread-block cluster of that many CTAs with a barrier per plane) and
  * whether the i- and j-face flux kernels run concurrently on two streams.
  * The fine-mesh U and the step counters are restored afterwards.  Outputs
  * (may be NULL): the choices and the winner's milliseconds per step.  The
- * default shape, before any autotune, is 0; the environment variable
- * EC2D_LUSGS_CLUSTER read by ec2d_create overrides it. */
+ * default shape, before any autotune, is 0 with 12-row bands; the
+ * environment variables EC2D_LUSGS_CLUSTER and EC2D_LUSGS_ROWS read by
+ * ec2d_create override it. */
 int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *rows_per_warp, int *concurrent,
                   double *ms_per_step);
 

@@ -120,7 +120,7 @@ struct ec2d_ctx {
   // wavefront send nothing, so the downstream waits run out and report
   // EC2D_ERR_TIMEOUT; failure detection is tested without a GPU fault
   bool silent_band_edge = false;
-  int lusgs_rpw = 24;       // most rows per CTA of the four-lane kernel, or rows per warp of the one-lane one
+  int lusgs_rpw = 12;       // most rows per CTA of the banded kernel (<= 16: eight lanes per row), or rows per warp of the one-lane one
   bool coarse_fp32 = false; // face fluxes of multigrid levels >= 2 in FP32
   bool timing = false;
   // one pseudo-time step (single grid or V-cycle) captured as a CUDA graph:
@@ -1253,12 +1253,14 @@ int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *rows_per_w
   cudaEvent_t a, b;
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
-  // candidates: the FP64 wavefront's shape -- four lanes per row (where it
-  // fits), one CTA per block with 32, 24 or 16 rows per warp, or a cluster of
-  // 2, 4, 8 CTAs (the FP32 sweep has one shape) -- x concurrent face kernels
-  std::vector<std::pair<int, int>> shapes = {{0, 24}};
+  // candidates: the FP64 wavefront's shape -- bands of 12 or 16 rows with
+  // eight lanes per row or of 24 or 32 rows with four (where they fit), one
+  // CTA per block with 32, 24 or 16 rows per warp, or a cluster of 2, 4, 8
+  // CTAs (the FP32 sweep has one shape) -- x concurrent face kernels
+  std::vector<std::pair<int, int>> shapes = {{0, 12}};
   if (!ctx->lusgs_fp32 && ctx->P.Time_Method == Time_LU_SGS)
-    for (auto sh : {std::make_pair(0, 32), std::make_pair(0, 16), std::make_pair(1, 32), std::make_pair(1, 24),
+    for (auto sh : {std::make_pair(0, 16), std::make_pair(0, 24), std::make_pair(0, 32), std::make_pair(1, 32),
+                    std::make_pair(1, 24),
                     std::make_pair(1, 16), std::make_pair(2, 32), std::make_pair(4, 32), std::make_pair(8, 32)})
       shapes.push_back(sh);
   const int old_cs = ctx->lusgs_cs, old_rpw = ctx->lusgs_rpw;

@@ -639,7 +639,7 @@ struct QBand {
 // die's L2.  The band-edge state goes to the next band before this plane's
 // global stores, so the release that publishes it waits only for stores of
 // earlier planes.
-template <bool update, bool FWD>
+template <bool update, bool FWD, int LPR>
 __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBand &B, double *slot, double *inbox,
                                       unsigned long long *mbar, unsigned rbox, unsigned rmbar, const double *rsrc,
                                       double *recBw, double gm1) {
@@ -666,35 +666,65 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
   }
   double wx = 0.0, wu = 0.0, wv = 0.0, wp = 0.0;  // the row's previous cell
   int gave_up = 0;                                 // first column whose inbox wait gave up
-  const int gl = (threadIdx.x & 31) & ~3;
+  const int gl = (threadIdx.x & 31) & ~(LPR - 1);  // the row's first lane
+  // eight lanes per row: lanes 0-3 take the row's own previous cell, lanes
+  // 4-7 the neighbouring row; four lanes per row take both
+  const bool own_nb = LPR == 4 || !((threadIdx.x >> 2) & 1), row_nb = LPR == 4 || !own_nb;
+  const bool lead = LPR == 4 || own_nb;  // stores and sends
   // cur: this plane's record; ahead: the set two planes on (free since the last plane)
   auto plane = [&](int p, const QRec &cur, QRec &ahead) {
     const int i = p - j, buf = p & 1;
     const bool act = B.row_ok && i >= 1 && i <= ni;
     const int k = FWD ? i - 1 : ni - i;
     if (act && k + 2 < ni) qload<FWD, update>(ahead, src(k + 2), q, ln);
-    double st = 0.0, dn = 0.0;
+    double acc = 0.0;
     if (act) {
-      double acc = FWD ? cur.a : cur.c0;
-      if (FWD ? (i > 1) : (i < ni)) {
-        const double w = fma(wu, cur.ni.x, fma(wv, cur.ni.y, cur.c.x));
-        acc = fma(wx, w, fma(wp, qcoef(cur.ki, ln), acc));
-      }
-      if (FWD ? (j > 1) : (j < rows)) {
-        const double *s;
-        if (from_box) {
-          // after one wait has given up the row no longer waits (its results
-          // are void; the step reports EC2D_ERR_TIMEOUT)
+      if (LPR == 4) {
+        acc = FWD ? cur.a : cur.c0;
+        if (FWD ? (i > 1) : (i < ni)) {
+          const double w = fma(wu, cur.ni.x, fma(wv, cur.ni.y, cur.c.x));
+          acc = fma(wx, w, fma(wp, qcoef(cur.ki, ln), acc));
+        }
+        if (FWD ? (j > 1) : (j < rows)) {
+          const double *s;
+          if (from_box) {
+            // after one wait has given up the row no longer waits (its results
+            // are void; the step reports EC2D_ERR_TIMEOUT)
+            if (!gave_up && !qwait(mbar + i - 1)) gave_up = i;
+            s = inbox + (size_t)(i - 1) * 8;
+          } else {
+            s = slot + ((size_t)(buf ^ 1) * R + (FWD ? rl - 1 : rl + 1)) * 8;
+          }
+          const double2 uv = *reinterpret_cast<const double2 *>(s + 4);
+          const double sp = s[6], sx = s[q];
+          const double w = fma(uv.x, cur.nj.x, fma(uv.y, cur.nj.y, cur.c.y));
+          acc = fma(sx, w, fma(sp, qcoef(cur.kj, ln), acc));
+        }
+      } else {
+        // both halves run the same FP64 instructions on their own operands
+        const double *s = slot + ((size_t)(buf ^ 1) * R + min(max(FWD ? rl - 1 : rl + 1, 0), R - 1)) * 8;
+        if (row_nb && from_box) {
           if (!gave_up && !qwait(mbar + i - 1)) gave_up = i;
           s = inbox + (size_t)(i - 1) * 8;
-        } else {
-          s = slot + ((size_t)(buf ^ 1) * R + (FWD ? rl - 1 : rl + 1)) * 8;
         }
         const double2 uv = *reinterpret_cast<const double2 *>(s + 4);
         const double sp = s[6], sx = s[q];
-        const double w = fma(uv.x, cur.nj.x, fma(uv.y, cur.nj.y, cur.c.y));
-        acc = fma(sx, w, fma(sp, qcoef(cur.kj, ln), acc));
+        const bool has = own_nb ? (FWD ? (i > 1) : (i < ni)) : (FWD ? (j > 1) : (j < rows));
+        const double X = own_nb ? wx : sx, Uu = own_nb ? wu : uv.x, Vv = own_nb ? wv : uv.y, P = own_nb ? wp : sp;
+        const double n1 = own_nb ? cur.ni.x : cur.nj.x, n2 = own_nb ? cur.ni.y : cur.nj.y;
+        const double cc = own_nb ? cur.c.x : cur.c.y, kk = own_nb ? cur.ki : cur.kj;
+        acc = own_nb ? (FWD ? cur.a : cur.c0) : 0.0;
+        if (has) {
+          const double w = fma(Uu, n1, fma(Vv, n2, cc));
+          acc = fma(X, w, fma(P, qcoef(kk, ln), acc));
+        }
       }
+    }
+    // eight lanes: the two halves of the row add their neighbours' terms
+    const double other = LPR == 8 ? __shfl_xor_sync(0xffffffffu, acc, 4) : 0.0;
+    double st = 0.0, dn = 0.0;
+    if (act) {
+      if (LPR == 8) acc = acc + other;
       if (update) {
         // U + dU* going forward (carried in the backward record), U + dU* + dU** going backward
         st = fma(acc, cur.ia.x, FWD ? cur.u : cur.a);
@@ -711,7 +741,7 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
       const double pr = fma(-0.5, fma(s2, v, s1 * u), s3);  // p / (gamma - 1)
       const double H = fma(gm1, pr, s3);
       const double x = q == 3 ? H : st;
-      if (to_box && q == 0) {
+      if (to_box && lead && q == 0) {
         const unsigned a = rbox + 64u * (unsigned)(i - 1), m = rmbar + 8u * (unsigned)(i - 1);
         qsend2(a, s0, s1, m);
         qsend2(a + 16u, s2, H, m);
@@ -719,18 +749,20 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
         qsend2(a + 48u, pr, 0.0, m);
       }
       double *o = slot + ((size_t)buf * R + rl) * 8;
-      o[q] = x;
-      if (q == 0) *reinterpret_cast<double2 *>(o + 4) = make_double2(u, v);
-      if (q == 1) o[6] = pr;
+      if (lead) o[q] = x;
+      if (lead && q == 0) *reinterpret_cast<double2 *>(o + 4) = make_double2(u, v);
+      if (lead && q == 1) o[6] = pr;
       wx = x; wu = u; wv = v; wp = pr;
-      if (FWD) {
-        recBw[(size_t)(i - 1) * RC::N + RC::A + q] = update ? st : dn;
-      } else {
-        // an updating sweep writes U only (DU is read nowhere but inside
-        // du_LU_SGS_2D and the update that follows it)
-        const long long id = bd.off + (long long)(j + 2) * bd.P + (i + 2);
-        if (update) L.U[q * F + id] = st;
-        else L.du[q * F + id] = dn;
+      if (lead) {
+        if (FWD) {
+          recBw[(size_t)(i - 1) * RC::N + RC::A + q] = update ? st : dn;
+        } else {
+          // an updating sweep writes U only (DU is read nowhere but inside
+          // du_LU_SGS_2D and the update that follows it)
+          const long long id = bd.off + (long long)(j + 2) * bd.P + (i + 2);
+          if (update) L.U[q * F + id] = st;
+          else L.du[q * F + id] = dn;
+        }
       }
     }
     __syncthreads();
@@ -744,7 +776,7 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
   if (gave_up) set_status(L.status + 4 * bd.cas, 4, B.bk, gave_up, j);
 }
 
-template <bool update>
+template <bool update, int LPR>
 __global__ void __launch_bounds__(4 * QROWS, 1) k_lusgs_sweep_quad(Lvl L, int R, int CS) {
   extern __shared__ __align__(16) double sh[];  // [2][R][8] slots | inbox F [ni][8] | inbox B | mbarriers F [ni] | B
   QBand B;
@@ -754,7 +786,7 @@ __global__ void __launch_bounds__(4 * QROWS, 1) k_lusgs_sweep_quad(Lvl L, int R,
   B.R = R; B.CS = CS;
   B.rows = bd.ny - 1;
   B.ni = bd.nx - 1;
-  B.rl = threadIdx.x >> 2;
+  B.rl = threadIdx.x / LPR;
   B.q = threadIdx.x & 3;
   B.j = (int)B.rank * R + B.rl + 1;
   B.row_ok = B.rl < R && B.j <= B.rows;
@@ -775,14 +807,15 @@ __global__ void __launch_bounds__(4 * QROWS, 1) k_lusgs_sweep_quad(Lvl L, int R,
   const double *recF = L.rec + ((size_t)bd.cell0 + (size_t)(jr - 1) * ni) * Rec<4>::N;
   const double *recB = recF + (size_t)L.ncell * Rec<4>::N;
   double *recBw = L.rec + ((size_t)L.ncell + bd.cell0 + (size_t)(jr - 1) * ni) * Rec<4>::N;
-  qpass<update, true>(L, bd, B, slot, inF, mbF, rboxF, rmbF, recF, recBw, gm1);
-  qpass<update, false>(L, bd, B, slot, inB, mbB, rboxB, rmbB, recB, recBw, gm1);
+  qpass<update, true, LPR>(L, bd, B, slot, inF, mbF, rboxF, rmbF, recF, recBw, gm1);
+  qpass<update, false, LPR>(L, bd, B, slot, inB, mbB, rboxB, rmbB, recB, recBw, gm1);
   if (CS > 1) cluster_barrier();  // no CTA leaves while a neighbour may still write into it
 }
 
-// the four-lane kernel serves NV = 4 levels whose blocks have at most 8 x 32
-// rows and QCOLS cells per row, when every CTA of the launch gets an SM of
-// its own (with fewer SMs, one lane per row needs fewer FP64 instructions)
+// the four- and eight-lane kernel serves NV = 4 levels whose blocks have at
+// most 8 bands of rows and QCOLS cells per row, when every CTA of the launch
+// gets an SM of its own (with fewer SMs, one lane per row needs fewer FP64
+// instructions)
 // rmax: most rows per CTA (16, 24 or 32: four, three or two warps share an
 // SM's FP64 unit)
 int quad_ctas(int max_rows, int rmax) {
@@ -800,12 +833,16 @@ bool quad_fits(const Lvl &L, int max_rows, int max_cols, int rmax) {
   return L.nvar == 4 && max_rows >= 1 && CS <= 8 && max_cols <= QCOLS && L.nblk * CS <= nsm;
 }
 
+// at most 16 rows per CTA: eight lanes per row (15 FP64 operations per cell
+// and lane instead of 18, in up to four warps); more: four lanes per row
 void launch_quad(const Lvl &L, int update, int max_rows, int max_cols, int rmax, cudaStream_t s) {
   const int CS = quad_ctas(max_rows, rmax);
   const int R = (max_rows + CS - 1) / CS;
-  const int th = (4 * R + 31) / 32 * 32;
+  const int lpr = rmax <= 16 ? 8 : 4;
+  const int th = (lpr * R + 31) / 32 * 32;
   const size_t smem = (size_t)2 * R * 8 * sizeof(double) + (CS > 1 ? (size_t)max_cols * 2 * (8 * sizeof(double) + 8) : 0);
-  auto kern = update ? k_lusgs_sweep_quad<true> : k_lusgs_sweep_quad<false>;
+  auto kern = lpr == 8 ? (update ? k_lusgs_sweep_quad<true, 8> : k_lusgs_sweep_quad<false, 8>)
+                       : (update ? k_lusgs_sweep_quad<true, 4> : k_lusgs_sweep_quad<false, 4>);
   if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(L.nblk * CS);
@@ -863,10 +900,12 @@ void sweep_nv(const Lvl &L, double alfa1, int mode, int max_rows, int max_cols, 
   k_lusgs_prep<NV><<<L.ntiles, TILE, 0, s>>>(L, alfa1, mode & LUSGS_FORCE);
   const int update = mode & LUSGS_UPDATE;
   if (cs == 0) {
-    if (quad_fits(L, max_rows, max_cols, rpw)) {
-      launch_quad(L, update, max_rows, max_cols, rpw, s);
-      return;
-    }
+    // the requested band height, else four-lane bands of 24 or 32 rows
+    for (int r : {rpw, 24, 32})
+      if (quad_fits(L, max_rows, max_cols, r)) {
+        launch_quad(L, update, max_rows, max_cols, r, s);
+        return;
+      }
     cs = 1;  // one CTA per block, full warps
     rpw = 32;
   }

@@ -117,10 +117,10 @@ def test_boundary_wall_isothermal_symmetry_sa(gpu_lib):
     compare_U(orc, g, tol=1e-14)
 
 
-# NV = 4: 16 rows per block run the four-lane kernel in one CTA, 40 and 70
-# rows in bands of 20 and 24 rows on clusters of 2 and 3 CTAs (the last band
-# short).  NV = 5 (SA), 6 (SST): 16 rows run four lanes per row in one CTA,
-# 40 and 70 rows one lane per row.
+# NV = 4 (default shape): 16, 40 and 70 rows per block run eight lanes per
+# row in bands of 8, 10 and 12 rows on clusters of 2, 4 and 6 CTAs (the last
+# band short).  NV = 5 (SA), 6 (SST): 16 rows run four lanes per row in one
+# CTA, 40 and 70 rows one lane per row.
 @pytest.mark.parametrize("ny", [17, 41, 71])
 @pytest.mark.parametrize("turb", [0, 2, 3])
 def test_lusgs_sweep(gpu_lib, ny, turb):
@@ -173,15 +173,17 @@ def test_lusgs_sweep(gpu_lib, ny, turb):
     assert worst <= 1.0, worst
 
 
-@pytest.mark.parametrize("turb,ny,shape", [(0, 41, "auto"), (0, 71, "auto"), (0, 41, "one"), (0, 41, "barrier"),
-                                           (2, 41, "auto")])
+@pytest.mark.parametrize("turb,ny,shape", [(0, 41, "auto"), (0, 71, "auto"), (0, 41, "four"), (0, 71, "four"),
+                                           (0, 41, "one"), (0, 41, "barrier"), (2, 41, "auto")])
 def test_lusgs_steps_wide_blocks(gpu_lib, monkeypatch, turb, ny, shape):
     """LU-SGS time steps on 40- and 70-row blocks (U updated inside the
-    sweep) against the oracle, with each wavefront shape: auto (four lanes per
-    row on a cluster of row bands for NV = 4, one lane per row otherwise), one
-    CTA per block with one lane per row, and a two-CTA cluster with a barrier
-    per plane."""
-    monkeypatch.setenv("EC2D_LUSGS_CLUSTER", {"auto": "0", "one": "1", "barrier": "2"}[shape])
+    sweep) against the oracle, with each wavefront shape: auto (eight lanes
+    per row in bands of at most 12 rows on a cluster for NV = 4, one lane per
+    row otherwise), four lanes per row in bands of at most 24 rows, one CTA
+    per block with one lane per row, and a two-CTA cluster with a barrier per
+    plane."""
+    monkeypatch.setenv("EC2D_LUSGS_CLUSTER", {"auto": "0", "four": "0", "one": "1", "barrier": "2"}[shape])
+    monkeypatch.setenv("EC2D_LUSGS_ROWS", {"four": "24", "one": "32", "barrier": "32"}.get(shape, "12"))
     kw = dict(ny=ny, Ma=0.6, AoA=2.0, Iflag_flux=4, Iflag_Scheme=5, Time_Method=0, CFL=5.0)
     if turb == 2:
         kw.update(If_viscous=1, Iflag_turbulence_model=2, Re=1e6, first=2e-4)

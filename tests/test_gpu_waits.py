@@ -18,7 +18,7 @@ EC2D_ERR_TIMEOUT = 4
 def test_band_edge_wait_runs_out(gpu_lib, monkeypatch):
     from ec2d import gpu
     monkeypatch.setenv("EC2D_TEST_SILENT_BAND_EDGE", "1")
-    monkeypatch.setenv("EC2D_LUSGS_CLUSTER", "0")  # four lanes per row, 40 rows: two bands
+    monkeypatch.setenv("EC2D_LUSGS_CLUSTER", "0")  # banded wavefront, 40 rows: four bands of 10
     p, bl = small_case(ny=41, Ma=0.6, AoA=2.0, Iflag_flux=4, Iflag_Scheme=5, Time_Method=0, CFL=5.0)
     g = make_gpu(p, bl)
     g.init_flow()
