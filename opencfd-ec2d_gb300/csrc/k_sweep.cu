@@ -532,27 +532,30 @@ void launch_lanes(const Lvl &L, int update, int R, cudaStream_t s) {
   else k_lusgs_sweep_lanes<NV, false, LPR><<<L.nblk, th, smem, s>>>(L, R);
 }
 
-// ---- mean flow only (NV = 4): four lanes per row, row bands on a cluster -----
+// ---- mean flow only (NV = 4): four or eight lanes per row, row bands -------
 //
 // Lane q of a row owns variable q.  A neighbour's state is held as
 // X = (rho, rho u, rho v, H = E + p) with u, v and p' = p / (gamma - 1), so
 // that its flux plus dissipation in variable q is one pair of FMAs,
 // X_q w + p' g_q with w = u n1 + v n2 + cc and g = (gamma - 1) (0, n1, n2,
-// -cc) taken from the record (E w + p un = H w - p cc).  Per cell and lane
-// that leaves 18 FP64 operations: 2 x 4 for the two neighbours, one for the
-// update, and rcp(rho), u, v, p', H of the new state (formed by every lane of
-// the row after the four variables are gathered by shuffles).  A CTA holds
-// at most 32 rows (four warps, one per SM sub-partition); a block with more
-// rows is split into bands of R rows on
-// the CTAs of a cluster.  The band edge does not wait for a barrier: the edge
-// row of the upstream band writes each new state straight into the
-// downstream CTA's inbox (one 64-byte entry and one mbarrier per column,
-// through distributed shared memory), and the downstream edge row waits for
-// that column's entry only, so the bands run as a pipeline a few planes apart.
-// The per-lane pressure coefficient g_q is a record field picked by a
-// per-lane offset and masked or sign-flipped with integer operations, so
-// the lanes of a row run one instruction stream without branches or FP64
-// selects.
+// -cc) taken from the record (E w + p un = H w - p cc).  With four lanes per
+// row a lane adds both neighbours: 18 FP64 operations per cell and lane (2 x
+// 4 for the neighbours, one for the update, and rcp(rho), u, v, p', H of the
+// new state, formed by every lane of the row after the four variables are
+// gathered by shuffles).  With eight, lanes 0-3 add the row's own previous
+// cell and lanes 4-7 the neighbouring row on operands selected per lane (one
+// FP64 instruction stream for both halves), and a shuffle-add joins them:
+// 15 operations.  A CTA holds at most 32 rows of four lanes or 16 of eight
+// (up to four warps, one per SM sub-partition); a block with more rows is
+// split into bands of R rows on the CTAs of a cluster.  The band edge does
+// not wait for a barrier: the edge row of the upstream band writes each new
+// state straight into the downstream CTA's inbox (one 64-byte entry and one
+// mbarrier per column, through distributed shared memory), and the
+// downstream edge row waits for that column's entry only, so the bands run
+// as a pipeline a few planes apart.  The per-lane pressure coefficient g_q
+// is a record field picked by a per-lane offset and masked or sign-flipped
+// with integer operations, so the lanes of a row need no branches or FP64
+// selects for it.
 constexpr int QROWS = 32;        // rows per CTA
 constexpr int QCOLS = 1024;      // cells per row the inboxes hold
 constexpr int QWAIT = 1 << 20;   // polls of an inbox mbarrier before the wait gives up (about 20 ms)
