@@ -213,9 +213,10 @@ def time_to_drop(g, cells, cap_s=60.0, target=1e-8, check=25):
 
 
 # DRAM bytes per launch of the dominant kernel on this workload, from one
-# ncu capture of k_lusgs_sweep<4> on the fine level (dram__bytes_read.sum +
-# dram__bytes_write.sum; the run is in the profiling summaries of the repo)
-PROFILED_TRAFFIC = {("k_lusgs", 1): 5320448.0}
+# ncu capture of the default wavefront (k_lusgs_sweep_quad<1, 8>) on the fine
+# level (dram__bytes_read.sum + dram__bytes_write.sum, caches flushed before
+# the launch; the run is in the profiling summaries of the repo)
+PROFILED_TRAFFIC = {("k_lusgs", 1): 7426816.0}
 SWEEP_PLANES = lambda blocks, lev: 2 * max((b.nx - 1) // 2 ** (lev - 1) + (b.ny - 1) // 2 ** (lev - 1) - 1
                                          for b in blocks)
 
