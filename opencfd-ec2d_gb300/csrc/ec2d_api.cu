@@ -99,6 +99,11 @@ struct ec2d_ctx {
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;           // second stream for concurrent independent kernels
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // a second stream pair (and its fork / join events) for the branch of a
+  // multigrid transfer that runs beside the fine residual, and the events
+  // that open and close that branch
+  cudaStream_t stream2 = nullptr, side2 = nullptr;
+  cudaEvent_t ev_fork2 = nullptr, ev_join2 = nullptr, ev_b0 = nullptr, ev_b1 = nullptr;
   std::vector<HCase> cases;
   bool setup_done = false;
   int num_mesh = 1;
@@ -723,7 +728,7 @@ void advance_counters(ec2d_ctx *ctx, int l) {
 
 // NS_Time_advance_1Euler (sub_NS_singlegrid.f90:67-106).  fresh: U has not
 // changed since the last residual evaluation of this level (the first
-// smoothing step after coarse_entry), so Res, the spectral radii, dt and the
+// smoothing step after transfer_down), so Res, the spectral radii, dt and the
 // norms of that evaluation stand; the reference evaluates them again with the
 // same result.
 void step_euler(ec2d_ctx *ctx, int l, bool fresh = false) {
@@ -820,7 +825,7 @@ void mg_smooth_fine(ec2d_ctx *ctx) {
   else step_rk3(ctx, 1);
 }
 // Un = U of the coarse level (Euler and LU-SGS smoothing) is taken by the
-// residual evaluation just before (RES_SET_UN, see coarse_entry), and the
+// residual evaluation just before (RES_SET_UN, see transfer_down), and the
 // first smoothing step reuses that evaluation (U is unchanged since)
 void mg_smooth_coarse(ec2d_ctx *ctx, int l) {
   const int Time_step_coarse_mesh = 3;
@@ -831,16 +836,42 @@ void mg_smooth_coarse(ec2d_ctx *ctx, int l) {
     step_lusgs(ctx, l, 0.0, true);
   } else step_rk3(ctx, l);
 }
-// residual of a coarse level right after restriction, QF -= Res
-// (comput_force_function), and Un = U for the smoothing that follows
-void coarse_entry(ec2d_ctx *ctx, int l) {
-  const int tm = ctx->P.Time_Method;
-  residual(ctx, l, RES_FORCE_FN | ((tm == Time_Euler1 || tm == Time_LU_SGS) ? RES_SET_UN : 0));
+// the work issued while it is in effect goes to the second stream pair
+void swap_branch(ec2d_ctx *ctx) {
+  std::swap(ctx->stream, ctx->stream2);
+  std::swap(ctx->side, ctx->side2);
+  std::swap(ctx->ev_fork, ctx->ev_fork2);
+  std::swap(ctx->ev_join, ctx->ev_join2);
 }
-// restriction of the residual (flag 2) and of U (flag 1) from level f to f+1
-void restrict_both(ec2d_ctx *ctx, int f) {
+// Transfer from level f to f + 1 (interpolation2h and comput_force_function,
+// sub_NS_multigrid.f90:349-398,156-173): the residual of level f, the
+// restriction of U with the coarse boundary conditions, and the coarse
+// residual on entry (with Un = U for the smoothing that follows).  The
+// residual of level f reads and writes level-f arrays only; the other chain
+// reads level-f U and writes level-(f + 1) arrays only, so with concurrent
+// kernels it runs on the second stream pair beside the first (graph
+// branches); the forcing QF = sum Res_h - R_2h(U_2h) is formed where the two
+// join, with the same two roundings as the reference's sum then subtract.
+void transfer_down(ec2d_ctx *ctx, int f, int fine_post) {
+  const int tm = ctx->P.Time_Method;
+  const int cpost = (tm == Time_Euler1 || tm == Time_LU_SGS) ? RES_SET_UN : 0;
   const Lvl &Lf = ctx->lv[f].L, &Lc = ctx->lv[f + 1].L;
-  K(ctx, "k_restrict", f + 1, 1, [&] { launch_restrict(Lf, Lc, 3, ctx->stream); });
+  const bool par = !ctx->timing && ctx->concurrent;
+  if (par) {
+    cudaEventRecord(ctx->ev_b0, ctx->stream);
+    cudaStreamWaitEvent(ctx->stream2, ctx->ev_b0, 0);
+    swap_branch(ctx);
+  }
+  K(ctx, "k_restrict", f + 1, 1, [&] { launch_restrict(Lf, Lc, 1, ctx->stream); });
+  bc_all(ctx, f + 1);
+  residual(ctx, f + 1, cpost);
+  if (par) {
+    swap_branch(ctx);
+    cudaEventRecord(ctx->ev_b1, ctx->stream2);
+  }
+  residual(ctx, f, fine_post);
+  if (par) cudaStreamWaitEvent(ctx->stream, ctx->ev_b1, 0);
+  K(ctx, "k_restrict", f + 1, 1, [&] { launch_restrict(Lf, Lc, 2 | 4, ctx->stream); });
 }
 // deltU = U - Un on level c, prolonged to level c-1 and added there (one
 // kernel: the coarse deltU is formed where it is interpolated)
@@ -851,10 +882,7 @@ void correct_from(ec2d_ctx *ctx, int c) {
 // NS_2stge_multigrid (sub_NS_multigrid.f90:14-58)
 void mg2(ec2d_ctx *ctx) {
   mg_smooth_fine(ctx);
-  residual(ctx, 1);
-  restrict_both(ctx, 1);
-  bc_all(ctx, 2);
-  coarse_entry(ctx, 2);
+  transfer_down(ctx, 1, 0);
   mg_smooth_coarse(ctx, 2);
   correct_from(ctx, 2);
   bc_all(ctx, 1);
@@ -862,15 +890,9 @@ void mg2(ec2d_ctx *ctx) {
 // NS_3stge_multigrid (sub_NS_multigrid.f90:66-142)
 void mg3(ec2d_ctx *ctx) {
   mg_smooth_fine(ctx);
-  residual(ctx, 1);
-  restrict_both(ctx, 1);
-  bc_all(ctx, 2);
-  coarse_entry(ctx, 2);
+  transfer_down(ctx, 1, 0);
   mg_smooth_coarse(ctx, 2);
-  residual(ctx, 2, RES_ADD_FORCE);
-  restrict_both(ctx, 2);
-  bc_all(ctx, 3);
-  coarse_entry(ctx, 3);
+  transfer_down(ctx, 2, RES_ADD_FORCE);
   mg_smooth_coarse(ctx, 3);
   correct_from(ctx, 3);
   correct_from(ctx, 2);
@@ -1010,7 +1032,13 @@ int ec2d_create(int device, ec2d_ctx **out) {
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->side2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_fork2, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_join2, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_b0, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_b1, cudaEventDisableTiming) != cudaSuccess) {
     delete c;
     return EC2D_ERR_CUDA;
   }
@@ -1030,8 +1058,13 @@ void ec2d_destroy(ec2d_ctx *ctx) {
   if (ctx->d_shape) cudaFree(ctx->d_shape);
   if (ctx->step_graph) cudaGraphExecDestroy(ctx->step_graph);
   cudaStreamSynchronize(ctx->side);
+  cudaStreamSynchronize(ctx->stream2);
+  cudaStreamSynchronize(ctx->side2);
   cudaEventDestroy(ctx->ev_fork);
   cudaEventDestroy(ctx->ev_join);
+  for (cudaEvent_t e : {ctx->ev_fork2, ctx->ev_join2, ctx->ev_b0, ctx->ev_b1}) cudaEventDestroy(e);
+  cudaStreamDestroy(ctx->side2);
+  cudaStreamDestroy(ctx->stream2);
   cudaStreamDestroy(ctx->side);
   cudaStreamDestroy(ctx->stream);
   delete ctx;

@@ -169,8 +169,11 @@ __global__ void k_set_un(Lvl L, int nv) {
   for (int m = 0; m < nv; m++) L.un[m * L.F + id] = L.U[m * L.F + id];
 }
 // restriction fine -> coarse (interpolation2h, sub_NS_multigrid.f90:349-398):
-// flag 1 volume-weighted U, flag 2 residual sum into QF, 3 both.  Runs over
-// the coarse level's tiles.
+// flag 1 volume-weighted U, flag 2 residual sum into QF, 3 both; with 4 the
+// coarse residual already evaluated on the restricted U is subtracted from
+// the sum (QF = sum Res_h - Res_2h, comput_force_function,
+// sub_NS_multigrid.f90:156-173: the sum is rounded first, as there).  Runs
+// over the coarse level's tiles.
 __global__ void k_restrict(Lvl Lf, Lvl Lc, int flag) {
   int bk, i, j;
   if (!tile_cell(Lc, bk, i, j, 1, 1)) return;
@@ -190,7 +193,8 @@ __global__ void k_restrict(Lvl Lf, Lvl Lc, int flag) {
   if (flag & 2) {
     for (int m = 0; m < 4; m++) {
       const double *r = Lf.res + m * FF;
-      Lc.qf[m * FC + ic] = r[f11] + r[f12] + r[f21] + r[f22];
+      const double sum = r[f11] + r[f12] + r[f21] + r[f22];
+      Lc.qf[m * FC + ic] = (flag & 4) ? sum - Lc.res[m * FC + ic] : sum;
     }
   }
 }
