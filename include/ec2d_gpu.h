@@ -284,7 +284,9 @@ int ec2d_mlp_predict(ec2d_mlp *m, const float *feat, long long n, float *pred);
  * level has 4 variables, at most 8 bands and 1024 cells per row, else as 1;
  * 1: one CTA per block with rows_per_warp (32, 24 or 16) rows per warp; 2, 4,
  * 8: a thread-block cluster of that many CTAs with a barrier per plane) and
- * whether the i- and j-face flux kernels run concurrently on two streams.
+ * whether independent kernels run concurrently on two stream pairs (the i-
+ * and j-face flux kernels; at a multigrid transfer the fine residual and the
+ * restriction + coarse boundary conditions + coarse entry residual).
  * The fine-mesh U and the step counters are restored afterwards.  Outputs
  * (may be NULL): the choices and the winner's milliseconds per step.  The
  * default shape, before any autotune, is 0 with 12-row bands; the
