@@ -1029,6 +1029,7 @@ int ec2d_create(int device, ec2d_ctx **out) {
   if (const char *e = getenv("EC2D_LUSGS_CLUSTER")) c->lusgs_cs = std::max(0, std::min(8, atoi(e)));
   if (const char *e = getenv("EC2D_LUSGS_ROWS")) c->lusgs_rpw = std::max(8, std::min(32, atoi(e)));
   if (const char *e = getenv("EC2D_TEST_SILENT_BAND_EDGE")) c->silent_band_edge = atoi(e) != 0;
+  if (const char *e = getenv("EC2D_CONCURRENT")) c->concurrent = atoi(e) != 0;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
