@@ -570,23 +570,42 @@ struct QRec {
 struct QLane {
   int offi, offj;
   unsigned keep, sign;
+  // eight lanes per row: the half's own face (i for lanes 0-3, j for 4-7)
+  int offk, offn, offc;
+  bool own;
 };
-__device__ __forceinline__ QLane qlane(int q) {
+__device__ __forceinline__ QLane qlane(int q, bool own = true) {
   using RC = Rec<4>;
   QLane l;
   l.offi = q == 1 ? RC::G1I : q == 2 ? RC::G2I : RC::GCI;
   l.offj = q == 1 ? RC::G1J : q == 2 ? RC::G2J : RC::GCJ;
   l.keep = q == 0 ? 0u : 0xffffffffu;
   l.sign = q == 3 ? 0x80000000u : 0u;
+  l.own = own;
+  l.offk = own ? l.offi : l.offj;
+  l.offn = own ? RC::N1I : RC::N1J;
+  l.offc = own ? RC::CI : RC::CJ;
   return l;
 }
 // g_q from the raw field by integer operations only (zero for q = 0, negated for q = 3)
 __device__ __forceinline__ double qcoef(double x, const QLane &l) {
   return __hiloint2double((__double2hiint(x) & (int)l.keep) ^ (int)l.sign, __double2loint(x) & (int)l.keep);
 }
-template <bool FWD, bool update>
+// four lanes per row load both faces' fields; eight load their half's face
+// only (into ki, ni, c.x) and the fields their half uses
+template <bool FWD, bool update, int LPR = 4>
 __device__ __forceinline__ void qload(QRec &r, const double *rec, int q, const QLane &l) {
   using RC = Rec<4>;
+  if (LPR == 8) {
+    if (!FWD || l.own) r.a = __ldcg(rec + RC::A + q);
+    if (FWD || !update) r.u = __ldcg(rec + RC::U + q);
+    if (!FWD && l.own) r.c0 = __ldcg(rec + RC::C0 + q);
+    r.ki = __ldcg(rec + l.offk);
+    r.ni = __ldcg(reinterpret_cast<const double2 *>(rec + l.offn));
+    r.c.x = __ldcg(rec + l.offc);
+    r.ia.x = __ldcg(rec + RC::IA);
+    return;
+  }
   r.a = __ldcg(rec + RC::A + q);
   if (FWD || !update) r.u = __ldcg(rec + RC::U + q);
   if (!FWD) r.c0 = __ldcg(rec + RC::C0 + q);
@@ -649,7 +668,7 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
   using RC = Rec<4>;
   const int R = B.R, rl = B.rl, q = B.q, j = B.j, rows = B.rows, ni = B.ni;
   const long long F = L.F;
-  const QLane ln = qlane(q);
+  const QLane ln = qlane(q, LPR == 4 || !((threadIdx.x >> 2) & 1));
   // this row's neighbour across the band edge comes through the inbox; the
   // band's edge row feeds the next band's inbox
   const bool from_box = B.row_ok && (FWD ? (rl == 0 && B.rank > 0) : (rl == R - 1 && (int)B.rank + 1 < B.CS && j < rows));
@@ -663,9 +682,9 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
   QRec r0, r1, r2;
   if (B.row_ok) {
     const int m0 = pos(FWD ? j + 1 : ni + j) % 3;  // set of the row's first cell
-    if (m0 == 0) { qload<FWD, update>(r0, src(0), q, ln); if (ni > 1) qload<FWD, update>(r1, src(1), q, ln); }
-    else if (m0 == 1) { qload<FWD, update>(r1, src(0), q, ln); if (ni > 1) qload<FWD, update>(r2, src(1), q, ln); }
-    else { qload<FWD, update>(r2, src(0), q, ln); if (ni > 1) qload<FWD, update>(r0, src(1), q, ln); }
+    if (m0 == 0) { qload<FWD, update, LPR>(r0, src(0), q, ln); if (ni > 1) qload<FWD, update, LPR>(r1, src(1), q, ln); }
+    else if (m0 == 1) { qload<FWD, update, LPR>(r1, src(0), q, ln); if (ni > 1) qload<FWD, update, LPR>(r2, src(1), q, ln); }
+    else { qload<FWD, update, LPR>(r2, src(0), q, ln); if (ni > 1) qload<FWD, update, LPR>(r0, src(1), q, ln); }
   }
   double wx = 0.0, wu = 0.0, wv = 0.0, wp = 0.0;  // the row's previous cell
   int gave_up = 0;                                 // first column whose inbox wait gave up
@@ -679,7 +698,7 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
     const int i = p - j, buf = p & 1;
     const bool act = B.row_ok && i >= 1 && i <= ni;
     const int k = FWD ? i - 1 : ni - i;
-    if (act && k + 2 < ni) qload<FWD, update>(ahead, src(k + 2), q, ln);
+    if (act && k + 2 < ni) qload<FWD, update, LPR>(ahead, src(k + 2), q, ln);
     double acc = 0.0;
     if (act) {
       if (LPR == 4) {
@@ -714,12 +733,11 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
         const double sp = s[6], sx = s[q];
         const bool has = own_nb ? (FWD ? (i > 1) : (i < ni)) : (FWD ? (j > 1) : (j < rows));
         const double X = own_nb ? wx : sx, Uu = own_nb ? wu : uv.x, Vv = own_nb ? wv : uv.y, P = own_nb ? wp : sp;
-        const double n1 = own_nb ? cur.ni.x : cur.nj.x, n2 = own_nb ? cur.ni.y : cur.nj.y;
-        const double cc = own_nb ? cur.c.x : cur.c.y, kk = own_nb ? cur.ki : cur.kj;
+        // the record fields of this half's face (loaded per half)
         acc = own_nb ? (FWD ? cur.a : cur.c0) : 0.0;
         if (has) {
-          const double w = fma(Uu, n1, fma(Vv, n2, cc));
-          acc = fma(X, w, fma(P, qcoef(kk, ln), acc));
+          const double w = fma(Uu, cur.ni.x, fma(Vv, cur.ni.y, cur.c.x));
+          acc = fma(X, w, fma(P, qcoef(cur.ki, ln), acc));
         }
       }
     }
