@@ -654,10 +654,10 @@ struct QBand {
   bool row_ok;
 };
 
-// One pass of a band.  Records are requested two cells ahead into three
-// register sets used in turn by plane number mod 3 (the loop is unrolled by
-// three, so no set is ever copied while its loads are in flight): a record
-// has two planes to arrive, enough for a read that crosses to the other
+// One pass of a band.  Records are requested three cells ahead into four
+// register sets used in turn by plane number mod 4 (the loop is unrolled by
+// four, so no set is ever copied while its loads are in flight): a record
+// has three planes to arrive, enough for a read that crosses to the other
 // die's L2.  The band-edge state goes to the next band before this plane's
 // global stores, so the release that publishes it waits only for stores of
 // earlier planes.
@@ -677,14 +677,21 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
   auto src = [&](int k) { return rsrc + (size_t)(FWD ? k : ni - 1 - k) * RC::N; };
   const int j0 = (int)B.rank * R + 1, j1 = min((int)B.rank * R + R, rows);
   const int plo = j0 + 1, phi = j1 + ni;  // planes holding a cell of this band
-  // plane p of this pass reads the record in set (pass position of p) mod 3
+  // plane p of this pass reads the record in set (pass position of p) mod 4
   auto pos = [&](int p) { return FWD ? p - plo : phi - p; };
-  QRec r0, r1, r2;
+  QRec r0, r1, r2, r3;
   if (B.row_ok) {
-    const int m0 = pos(FWD ? j + 1 : ni + j) % 3;  // set of the row's first cell
-    if (m0 == 0) { qload<FWD, update, LPR>(r0, src(0), q, ln); if (ni > 1) qload<FWD, update, LPR>(r1, src(1), q, ln); }
-    else if (m0 == 1) { qload<FWD, update, LPR>(r1, src(0), q, ln); if (ni > 1) qload<FWD, update, LPR>(r2, src(1), q, ln); }
-    else { qload<FWD, update, LPR>(r2, src(0), q, ln); if (ni > 1) qload<FWD, update, LPR>(r0, src(1), q, ln); }
+    // the row's first three cells into the sets of their planes
+    const int m0 = pos(FWD ? j + 1 : ni + j) % 4;  // set of the row's first cell
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      if (c >= ni) break;
+      const int m = (m0 + c) & 3;
+      if (m == 0) qload<FWD, update, LPR>(r0, src(c), q, ln);
+      else if (m == 1) qload<FWD, update, LPR>(r1, src(c), q, ln);
+      else if (m == 2) qload<FWD, update, LPR>(r2, src(c), q, ln);
+      else qload<FWD, update, LPR>(r3, src(c), q, ln);
+    }
   }
   double wx = 0.0, wu = 0.0, wv = 0.0, wp = 0.0;  // the row's previous cell
   int gave_up = 0;                                 // first column whose inbox wait gave up
@@ -693,12 +700,12 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
   // 4-7 the neighbouring row; four lanes per row take both
   const bool own_nb = LPR == 4 || !((threadIdx.x >> 2) & 1), row_nb = LPR == 4 || !own_nb;
   const bool lead = LPR == 4 || own_nb;  // stores and sends
-  // cur: this plane's record; ahead: the set two planes on (free since the last plane)
+  // cur: this plane's record; ahead: the set three planes on (free since the last plane)
   auto plane = [&](int p, const QRec &cur, QRec &ahead) {
     const int i = p - j, buf = p & 1;
     const bool act = B.row_ok && i >= 1 && i <= ni;
     const int k = FWD ? i - 1 : ni - i;
-    if (act && k + 2 < ni) qload<FWD, update, LPR>(ahead, src(k + 2), q, ln);
+    if (act && k + 3 < ni) qload<FWD, update, LPR>(ahead, src(k + 3), q, ln);
     double acc = 0.0;
     if (act) {
       if (LPR == 4) {
@@ -789,10 +796,11 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
     __syncthreads();
   };
   const int np = phi - plo + 1;  // planes of the pass; positions past np - 1 hold no cell
-  for (int t = 0; t < np; t += 3) {
-    plane(FWD ? plo + t : phi - t, r0, r2);
+  for (int t = 0; t < np; t += 4) {
+    plane(FWD ? plo + t : phi - t, r0, r3);
     plane(FWD ? plo + t + 1 : phi - t - 1, r1, r0);
     plane(FWD ? plo + t + 2 : phi - t - 2, r2, r1);
+    plane(FWD ? plo + t + 3 : phi - t - 3, r3, r2);
   }
   if (gave_up) set_status(L.status + 4 * bd.cas, 4, B.bk, gave_up, j);
 }
