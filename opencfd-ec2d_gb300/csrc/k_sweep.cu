@@ -658,9 +658,8 @@ struct QBand {
 // register sets used in turn by plane number mod 4 (the loop is unrolled by
 // four, so no set is ever copied while its loads are in flight): a record
 // has three planes to arrive, enough for a read that crosses to the other
-// die's L2.  The band-edge state goes to the next band before this plane's
-// global stores, so the release that publishes it waits only for stores of
-// earlier planes.
+// die's L2.  The band-edge state goes to the next band by st.async, its
+// bytes counted on the receiving entry's mbarrier (no fence on this side).
 template <bool update, bool FWD, int LPR>
 __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBand &B, double *slot, double *inbox,
                                       unsigned long long *mbar, unsigned rbox, unsigned rmbar, const double *rsrc,
