@@ -88,7 +88,16 @@ enum {
 int ec2d_version(void);
 const char *ec2d_error_string(int code);
 
-/* Create an empty context on CUDA device `device` (its own stream). */
+/* Create an empty context on CUDA device `device` (its own streams).
+ * Environment variables read here fix launch choices the autotuner would
+ * otherwise make (none changes the arithmetic of a kernel):
+ *   EC2D_LUSGS_CLUSTER  FP64 wavefront shape (see ec2d_autotune's lusgs_cs)
+ *   EC2D_LUSGS_ROWS     rows per band, or rows per warp of the one-CTA shape
+ *   EC2D_CONCURRENT     0: every kernel on one stream (no concurrent graph
+ *                       branches; results are bit-identical either way)
+ *   EC2D_TEST_SILENT_BAND_EDGE  test hook: band edges of the banded wavefront
+ *                       send nothing, so the downstream waits run out and the
+ *                       next status read returns EC2D_ERR_TIMEOUT */
 int ec2d_create(int device, ec2d_ctx **out);
 void ec2d_destroy(ec2d_ctx *ctx);
 
