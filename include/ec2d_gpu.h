@@ -215,8 +215,12 @@ int ec2d_kernel_times(ec2d_ctx *ctx, char *buf, int buflen);
  * The tile partials live in one file-scope __device__ array of 768 KiB per
  * GPU, so ncell is limited to EC2D_NOALLOC_MAX_CELLS (larger sizes return
  * EC2D_ERR_ARG).  All calls share that array: calls that overlap on the GPU
- * race.  The first call on a device looks up the array's address; make it
- * before any stream capture. */
+ * race.  The max is taken on the bit patterns of |Res|, so a NaN residual
+ * gives a NaN max, as in ec2d_residual.  The array's device address is looked
+ * up on every call made outside stream capture (a device reset therefore
+ * leaves no stale address); a call during capture reuses the last address
+ * found on that device, so make the first call on a device before any
+ * capture. */
 #define EC2D_NOALLOC_MAX_CELLS 2097152
 int ec2d_residual_norms_noalloc(const double *res, int nvar, int ncell, double *out, void *stream);
 

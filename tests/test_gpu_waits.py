@@ -28,9 +28,25 @@ def test_band_edge_wait_runs_out(gpu_lib, monkeypatch):
     assert e.value.code == EC2D_ERR_TIMEOUT
     code, blk, i, j = g.status()
     assert code == EC2D_ERR_TIMEOUT and blk >= 1 and i >= 1 and j >= 1
-    # the context still answers: the state can be read back and stepped
+    # the context still answers: the state can be read back
     g.sync()
     assert g.download_U(1, 1, 1).shape[0] == 4
+    g.close()
+    # and the process's GPU context stays usable: with the hook cleared, a new
+    # context in the same process steps with a clean status and finite U, and
+    # its sweeps agree with a context that never saw the hook
+    monkeypatch.delenv("EC2D_TEST_SILENT_BAND_EDGE")
+    outs = []
+    for _ in range(2):
+        h = make_gpu(p, bl)
+        h.init_flow()
+        h.step(3)
+        h.norms()
+        assert h.status()[0] == 0
+        outs.append(h.download_U(1, 1, 1))
+        h.close()
+    assert np.all(np.isfinite(outs[0]))
+    np.testing.assert_array_equal(outs[0], outs[1])
 
 
 def test_band_edges_deliver_without_the_hook(gpu_lib, monkeypatch):

@@ -46,9 +46,10 @@ def test_control_roundtrip(tmp_path):
     assert tuple(q.Pre_Step_Mesh) == (0, 100, 200)
 
 
-@pytest.mark.skipif(not os.path.exists("/root/reference/control.in"), reason="reference case not present")
 def test_reads_reference_inputs():
-    p, blocks = inputs.read_case("/root/reference")
+    from conftest import reference_file
+    reference_file("Mesh2d.dat")
+    p, blocks = inputs.read_case(os.path.dirname(reference_file("control.in")))
     assert p.Ma == 0.729 and p.Iflag_turbulence_model == 3 and p.Iflag_Scheme == 5
     assert len(blocks) == 3 and blocks[1].bc[1] == [2, 2, 1, 305, 1, 1, -10, 0, 0]
 

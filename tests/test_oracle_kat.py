@@ -157,15 +157,13 @@ def test_lusgs_converges_euler_small(oracle_lib):
     assert r1 < 1e-2 * r0
 
 
-RAE = "/root/reference"
-
-
-@pytest.mark.skipif(not os.path.exists(os.path.join(RAE, "Mesh2d.dat")), reason="reference case not present")
 def test_reference_rae2822_case_runs(oracle_lib):
     """The reference's own RAE2822 grid and connectivity (3 blocks, wake cut
     j-/j- reversed) parse and run: Euler LU-SGS drives the residual down."""
+    from conftest import reference_file
     from ec2d import inputs
-    p, blocks = inputs.read_case(RAE)
+    reference_file("Mesh2d.dat")
+    p, blocks = inputs.read_case(os.path.dirname(reference_file("control.in")))
     assert [b.nx for b in blocks] == [33, 305, 33] and all(b.ny == 65 for b in blocks)
     p = p.replace(If_viscous=0, Iflag_turbulence_model=0, Iflag_flux=4, IFlag_Reconstruction=0, CFL=3.0)
     orc = make_oracle(p, blocks, threads=8)

@@ -50,6 +50,27 @@ def test_noalloc_norms_match_context_entry_point(gpu_lib):
     g.close()
 
 
+def test_noalloc_max_carries_nan(gpu_lib):
+    """A host that watches max|Res| for divergence must see a NaN cell: the
+    max of a residual holding one NaN is NaN for that variable, finite for
+    the others, as in the context path."""
+    import torch
+    lib = gpu_lib.lib()
+    nv, ncell = 4, 3000
+    rng = np.random.default_rng(3)
+    res = rng.standard_normal((ncell, nv))
+    res[1234, 2] = np.nan
+    dres = torch.from_numpy(res.reshape(-1)).to("cuda")
+    out = torch.zeros(12, dtype=torch.float64, device="cuda")
+    assert _noalloc(lib, dres.data_ptr(), nv, ncell, out.data_ptr()) == 0
+    torch.cuda.synchronize()
+    o = out.cpu().numpy()
+    assert np.isnan(o[2]) and np.isnan(o[6 + 2])
+    for m in (0, 1, 3):
+        assert o[m] == np.max(np.abs(res[:, m]))
+        np.testing.assert_allclose(o[6 + m], np.sum(res[:, m] ** 2), rtol=1e-13)
+
+
 def test_noalloc_rejects_oversize(gpu_lib):
     import torch
     lib = gpu_lib.lib()
