@@ -118,16 +118,19 @@ def fine_cells(blocks):
     return sum(b.ncell for b in blocks)
 
 
-def best_threads(oracle, p, blocks, trials=4):
-    """Thread count at which the CPU port runs this workload fastest.  On the
+def thread_counts():
+    n = os.cpu_count() or 1
+    return sorted({t for t in (1, 2, 4, 8, n) if t <= n}), n
+
+
+def best_threads(oracle, p, blocks, trials=4, fast=False):
+    """Thread count at which a CPU build runs this workload fastest.  On the
     18,432-cell flat plate its OpenMP regions are short, so all host cores
     are not the fastest setting (measured on the 16-core Arm host: 7.5 ms
     per V-cycle on 4 threads, 12.5 ms on 16)."""
     best = None
-    n = os.cpu_count() or 1
-    cand = sorted({t for t in (1, 2, 4, 8, 12, 16, n) if t <= n})
-    for th in cand:
-        orc = oracle.Oracle(p, blocks, threads=th)
+    for th in thread_counts()[0]:
+        orc = oracle.Oracle(p, blocks, threads=th, fast=fast)
         orc.init_flow()
         orc.step(2)
         t0 = time.perf_counter(); orc.step(trials); dt = time.perf_counter() - t0
@@ -136,41 +139,95 @@ def best_threads(oracle, p, blocks, trials=4):
     return best[0]
 
 
-def cpu_port_rate(p, blocks, seconds=12.0, threads=None):
-    """Cell-updates/s of the CPU port (C++ restatement of the reference, the
-    only CPU implementation runnable here) at its fastest thread count on the
-    host cores."""
+def cpu_port_rates(p, blocks, seconds=16.0):
+    """Cell-updates/s of the CPU timing port (the C++ restatement of the
+    reference built -O3 with FMA contraction, the stand-in for gfortran -O3
+    -fopenmp on the reference, whose Fortran cannot be compiled here) on 1
+    thread, on every host core, and on the counts between; each count runs
+    for about seconds / (number of counts).  Returns the fastest count's
+    rate, that count, and the rate of every count."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
-    threads = threads or best_threads(oracle, p, blocks)
-    orc = oracle.Oracle(p, blocks, threads=threads)
+    counts, ncores = thread_counts()
+    per = seconds / len(counts)
+    by, best = {}, None
+    for th in counts:
+        orc = oracle.Oracle(p, blocks, threads=th, fast=True)
+        orc.init_flow()
+        orc.step(2)
+        t0 = time.perf_counter(); orc.step(2); t1 = (time.perf_counter() - t0) / 2
+        n = max(5, min(2000, int(per / max(t1, 1e-6))))
+        t0 = time.perf_counter(); orc.step(n); dt = time.perf_counter() - t0
+        rate = fine_cells(blocks) * n / dt
+        by[str(th)] = {"value": rate, "seconds_per_step": dt / n, "steps": n}
+        if best is None or rate > best[1]:
+            best = (th, rate)
+    return best[1], best[0], by, ncores
+
+
+def parity_record(p, blocks, gpu_hist, gpu_iters, gpu_forces, gpu_cf, mixed_forces=None, check=25, target=1e-8):
+    """The oracle (parity build, FP64, separately rounded like the reference)
+    run from the freestream start to the same residual drop, checked every
+    `check` V-cycles as the GPU run was: V-cycle counts, the differences of
+    CL, CD, CM and of every wall face's skin friction, and the largest
+    relative difference of the Res_rms(1) histories at the common checks."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    th = best_threads(oracle, p, blocks)
+    orc = oracle.Oracle(p, blocks, threads=th)
     orc.init_flow()
-    orc.step(2)
-    t0 = time.perf_counter(); orc.step(1); t1 = time.perf_counter() - t0
-    n = max(1, min(2000, int(seconds / max(t1, 1e-6))))
-    t0 = time.perf_counter(); orc.step(n); dt = time.perf_counter() - t0
-    return fine_cells(blocks) * n / dt, threads, n, dt
+    t0 = time.perf_counter()
+    orc.step(1)
+    r0 = orc.norms()[1][0]
+    hist, it = [r0], 1
+    while hist[-1] > target * r0 and it < 4 * gpu_iters:
+        orc.step(check)
+        it += check
+        hist.append(orc.norms()[1][0])
+    secs = time.perf_counter() - t0
+    cl, cd, cm = orc.forces()
+    cf, _ = orc.wall_cf(2, 2)
+    n = min(len(hist), len(gpu_hist))
+    h_o, h_g = np.array(hist[:n]), np.array(gpu_hist[:n])
+    rec = {"oracle": "C++ restatement of the reference, parity build (-O2, no FMA contraction)",
+           "oracle_threads": th, "oracle_seconds": secs, "target": target, "check_every": check,
+           "iterations_oracle": it, "iterations_gpu": gpu_iters,
+           "forces_oracle": {"cl": cl, "cd": cd, "cm": cm},
+           "dcl": gpu_forces[0] - cl, "dcd": gpu_forces[1] - cd, "dcm": gpu_forces[2] - cm,
+           "max_dcf": float(np.max(np.abs(np.asarray(gpu_cf) - cf))), "max_cf": float(np.max(np.abs(cf))),
+           "history_max_rel": float(np.max(np.abs(h_g - h_o) / h_o)), "history_points": n,
+           "bar": "|dCL|, |dCD|, |dCM| <= 1e-6 and Res_rms(1) history within 1e-6 relative"}
+    rec["within_1e-6"] = bool(max(abs(rec["dcl"]), abs(rec["dcd"]), abs(rec["dcm"])) <= 1e-6
+                              and rec["history_max_rel"] <= 1e-6 and it == gpu_iters)
+    if mixed_forces is not None:
+        rec["mixed_vs_oracle"] = {"dcl": mixed_forces[0] - cl, "dcd": mixed_forces[1] - cd,
+                                  "dcm": mixed_forces[2] - cm}
+    return rec
 
 
 def run_reference(args, rank, world):
-    """--impl reference: the CPU restatement of the reference timed on the
-    host cores (no Fortran compiler exists here or on the GPU machine, so the
-    reference itself cannot run; the port is its stand-in)."""
+    """--impl reference: the reference's CPU path on the host cores.  No
+    Fortran compiler exists here or on the GPU host, so the reference itself
+    cannot run; its stand-in is the C++ restatement built like gfortran -O3
+    -fopenmp would build it (the timing port), at its fastest thread count,
+    with the 1-thread and all-core rates beside it."""
     if rank != 0:
         return
     p, blocks = build_case()
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
-    threads = best_threads(oracle, p, blocks)
-    orc = oracle.Oracle(p, blocks, threads=threads)
+    cells = fine_cells(blocks)
+    best, threads, by, ncores = cpu_port_rates(p, blocks, seconds=args.cpu_seconds)
+    orc = oracle.Oracle(p, blocks, threads=threads, fast=True)
     orc.init_flow()
     orc.step(max(1, args.warmup))
     t0 = time.perf_counter()
     orc.step(args.steps)
     dt = time.perf_counter() - t0
-    cells = fine_cells(blocks)
     v = cells * args.steps / dt
     ttd = None
     if args.drop_cap > 0:
@@ -186,14 +243,17 @@ def run_reference(args, rank, world):
             it += 25
             r = orc.norms()[1][0]
         tdrop = time.perf_counter() - t0
+        cl, cd, cm = orc.forces()
         ttd = {"fp64": {"target": 1e-8, "iterations": it, "seconds": tdrop, "drop": r / r0,
-                        "reached": bool(r <= 1e-8 * r0), "cap_s": cap}}
+                        "reached": bool(r <= 1e-8 * r0), "cap_s": cap, "forces": {"cl": cl, "cd": cd, "cm": cm}}}
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "cells": cells, "step": "one 3-level V-cycle"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} V-cycles after {args.warmup} warm-up cycles"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port-O3",
+                             "host_cores": ncores, "by_cores": by,
+                             "sample": f"{args.steps} V-cycles after {args.warmup} warm-up cycles, "
+                                       f"{threads} of {ncores} host threads (fastest count)"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "time_to_drop": ttd}
     print(json.dumps(line), flush=True)
@@ -217,6 +277,11 @@ def time_to_drop(g, cells, cap_s=60.0, target=1e-8, check=25):
 # level (dram__bytes_read.sum + dram__bytes_write.sum, caches flushed before
 # the launch; the run is in the profiling summaries of the repo)
 PROFILED_TRAFFIC = {("k_lusgs", 1): 7426816.0}
+# FP64 FLOPs per fine cell of one laminar residual evaluation (k_prim,
+# k_flux_i, k_flux_j, k_res; AUSM+, MUSCL van Albada, primitive
+# reconstruction), from one ncu capture of those kernels:
+# (dadd + dmul + 2 dfma) thread instructions / cells
+FP64_FLOPS_PER_CELL_RESIDUAL = None
 SWEEP_PLANES = lambda blocks, lev: 2 * max((b.nx - 1) // 2 ** (lev - 1) + (b.ny - 1) // 2 ** (lev - 1) - 1
                                          for b in blocks)
 
@@ -246,6 +311,20 @@ def kernel_table(g, torch, flush, steps):
     kt = g.kernel_times()
     g.kernel_timing(False)
     return kt
+
+
+def merge_lusgs(kt):
+    """With kernel timing on, the FP64 wavefront's record builder and sweep
+    are timed apart (k_lusgs_prep, k_lusgs_sweep); fold them back into the
+    k_lusgs stage in place and return the sweep's (calls, ms) per level."""
+    sweep = {}
+    for (name, lev) in list(kt):
+        if name == "k_lusgs_sweep":
+            c, nk, ms = kt.pop((name, lev))
+            pc, pnk, pms = kt.pop(("k_lusgs_prep", lev), (0, 0, 0.0))
+            sweep[lev] = (c, ms)
+            kt[("k_lusgs", lev)] = (c, nk + pnk, ms + pms)
+    return sweep
 
 
 def residual_hbm(torch, gpu, dev, reps=10):
@@ -279,15 +358,27 @@ def residual_hbm(torch, gpu, dev, reps=10):
     total_ms = sum(v[2] for v in kt.values()) / reps
     hbm, kind = peaks()
     achieved = 176.0 * cells / (total_ms / 1e3) / 1e9
+    try:
+        fp64_peak = gpu.measure_fp64_peak()
+    except Exception:
+        fp64_peak = None
     per = {}
     for (name, lev), (calls, _, ms) in kt.items():
         bpu = BYTES_PER_UNIT.get(name)
         t = ms / calls
         per[name] = {"us": round(t * 1e3, 1), "gbs": round(bpu * cells / (t / 1e3) / 1e9, 1) if bpu else None}
-    return {"cells": cells, "grid": "2 x 2049x1025 (flat plate, 4.19 M cells)", "ms": total_ms,
-            "algorithmic_bytes_per_cell": 176, "achieved_gbs": achieved, "peak_gbs": hbm, "frac": achieved / hbm,
-            "peak_source": f"{kind} hbm_gbs", "kernels": per,
-            "note": "FP64 arithmetic bounds this stage (ncu: FP64 pipe 88-90 % busy in k_prim, k_flux_i, k_res)"}
+    out = {"cells": cells, "grid": "2 x 2049x1025 (flat plate, 4.19 M cells)", "ms": total_ms,
+           "algorithmic_bytes_per_cell": 176, "achieved_gbs": achieved, "peak_gbs": hbm, "frac": achieved / hbm,
+           "hbm_frac": achieved / hbm, "peak_source": f"{kind} hbm_gbs", "kernels": per}
+    out["fp64_peak_tflops"] = fp64_peak
+    if fp64_peak and FP64_FLOPS_PER_CELL_RESIDUAL:
+        # FP64 roofline: FLOPs executed per cell (ncu instruction counts of the
+        # residual kernels: dadd + dmul + 2 dfma per thread) / stage time
+        flops = FP64_FLOPS_PER_CELL_RESIDUAL * cells / (total_ms / 1e3) / 1e12
+        out.update({"bound": "fp64", "fp64_flops_per_cell": FP64_FLOPS_PER_CELL_RESIDUAL,
+                    "fp64_tflops": flops, "fp64_peak_tflops": fp64_peak, "fp64_frac": flops / fp64_peak,
+                    "fp64_peak_source": "measured in this run (ec2d_measure_fp64_peak: FMA chains on every SM)"})
+    return out
 
 
 def leg_polar(args):
@@ -455,6 +546,7 @@ def run_gb300(args, rank, world):
 
     # ---- per-kernel event timing (same K cycles, separate pass) -------------
     kt = kernel_table(g, torch, flush, args.steps)
+    sweep_ms = merge_lusgs(kt)
     hbm, peak_kind = peaks()
     best = max(kt.items(), key=lambda kv: kv[1][2])
     (kname, klev), (kcalls, knk, kms) = best
@@ -471,24 +563,34 @@ def run_gb300(args, rank, world):
     roofline = {"bound": "hbm", "kernel": f"{kname} (mesh {klev})", "achieved": achieved, "peak": hbm,
                 "unit": "GB/s", "frac": (achieved / hbm) if achieved else None,
                 "traffic": PROFILED_TRAFFIC.get((kname, klev)),
-                "peak_source": f"{peak_kind} hbm_gbs", "avg_launch_us": avg_ms * 1e3,
+                "peak_source": f"{peak_kind} hbm_gbs (of {peak_kind})", "avg_launch_us": avg_ms * 1e3,
                 "bytes_per_launch": bpu * units,
                 "share_of_step": kms / sum(v[2] for v in kt.values()),
                 "kernels": {f"{n}@{l}": {"calls": c, "ms_total": round(m, 4)} for (n, l), (c, _, m) in
                             sorted(kt.items(), key=lambda kv: -kv[1][2])[:12]}}
     if kname == "k_lusgs":
+        # the wavefront is bound by the latency of its per-plane FP64 chain, not
+        # by HBM: 2 (nx + ny - 3) dependent hyperplanes, each one cell update
         mhz = clocks.get("sm_mhz") or 2070.0
-        cpp = avg_ms * 1e-3 * mhz * 1e6 / SWEEP_PLANES(blocks, klev)
+        planes = SWEEP_PLANES(blocks, klev)
+        s_calls, s_ms = sweep_ms.get(klev, (kcalls, kms))
+        cpp = s_ms / s_calls * 1e-3 * mhz * 1e6 / planes
         # the FP64 chain of one plane: 15 operations per cell and lane with
         # eight lanes per row, 18 with four, 31 per cell with one, 64 cycles each
         kind = tuned["fp64"]["lusgs_kernel"]
         floor = {"eight-lane bands": 15, "four-lane bands": 18}.get(kind, 31) * 64
+        roofline["bound"] = "latency"
+        roofline["hbm_frac"] = roofline["frac"]
+        roofline["sweep_avg_launch_us"] = s_ms / s_calls * 1e3
         roofline["cycles_per_plane"] = cpp
+        roofline["cycles_per_plane_incl_prep"] = avg_ms * 1e-3 * mhz * 1e6 / planes
         roofline["fp64_chain_floor_cycles_per_plane"] = floor
         roofline["of_chain_floor"] = floor / cpp
-        roofline["latency_note"] = ("wavefront sweep (prep + sweep timed): one dependent chain of FP64 operations "
-                                    "per hyperplane, FP64 warp instruction latency 64 cycles on this part; "
-                                    "of_chain_floor = that chain's cycles / measured cycles per plane")
+        roofline["latency_note"] = ("wavefront sweep: one dependent chain of FP64 operations per hyperplane, FP64 "
+                                    "warp instruction latency 64 cycles on this part; cycles_per_plane = the sweep "
+                                    "kernel's event time x SM clock / planes; of_chain_floor = the chain's cycles / "
+                                    "cycles_per_plane; frac and hbm_frac = algorithmic bytes of prep + sweep "
+                                    "(256 B/cell) / their time / measured HBM bandwidth")
 
     # ---- mixed precision: the same V-cycle with FP32 LU-SGS sweeps ----------
     g.set_lusgs_precision(32)
@@ -534,10 +636,12 @@ def run_gb300(args, rank, world):
 
     # ---- time to a 1e-8 drop from the freestream start ----------------------
     ttd = None
+    hist = None
     if args.drop_cap > 0:
         ttd = {"fp64": time_to_drop(g, cells, cap_s=args.drop_cap)}
         cl, cd, cm = g.forces(1)
         ttd["fp64"]["forces"] = {"cl": cl, "cd": cd, "cm": cm}
+        cf_fp64, _ = g.wall_cf(1, 2, 2)
         g.set_lusgs_precision(32)
         tune()
         ttd["mixed"] = time_to_drop(g, cells, cap_s=args.drop_cap)
@@ -545,6 +649,18 @@ def run_gb300(args, rank, world):
         ttd["mixed"]["forces"] = {"cl": cl2, "cd": cd2, "cm": cm2}
         ttd["mixed"]["force_error_vs_fp64"] = max(abs(cl2 - cl), abs(cd2 - cd), abs(cm2 - cm))
         g.set_lusgs_precision(64)
+        tune()
+        if rank == 0 and world == 1 and args.parity:
+            # untimed: the FP64 residual history at every 25th V-cycle, the
+            # checks of the run above, for the comparison with the oracle
+            g.init_flow()
+            g.step(1)
+            r0 = g.norms(1, 1)[1][0]
+            hist, it = [r0], 1
+            while hist[-1] > 1e-8 * r0 and it < ttd["fp64"]["iterations"]:
+                g.step(25)
+                it += 25
+                hist.append(g.norms(1, 1)[1][0])
     cl, cd, cm = g.forces(1)
     g.close()
 
@@ -554,15 +670,25 @@ def run_gb300(args, rank, world):
 
     if rank == 0:
         cpu = None
+        parity = None
         if world == 1 and not args.no_cpu_baseline:
-            rate, thr, n, dt = cpu_port_rate(p, blocks, seconds=args.cpu_seconds)
-            cpu = {"value": rate, "unit": UNIT, "cores": thr, "kind": "port",
-                   "sample": f"{n} V-cycles of the same workload ({dt:.1f} s) on the C++ restatement",
-                   "seconds_per_step": dt / n}
+            rate, thr, by, ncores = cpu_port_rates(p, blocks, seconds=args.cpu_seconds)
+            cpu = {"value": rate, "unit": UNIT, "cores": thr, "kind": "port-O3", "host_cores": ncores,
+                   "by_cores": by,
+                   "sample": (f"V-cycles of the same workload on the C++ restatement built -O3 with FMA "
+                              f"contraction, {args.cpu_seconds:.0f} s over 1..{ncores} threads; value at the "
+                              f"fastest count ({thr})"),
+                   "seconds_per_step": by[str(thr)]["seconds_per_step"]}
             if ttd and ttd["fp64"]["reached"]:
-                cpu["time_to_drop_estimate_s"] = dt / n * ttd["fp64"]["iterations"]
-                cpu["time_to_drop_basis"] = ("CPU seconds per V-cycle x the V-cycles the FP64 GPU run needed "
-                                             "(same arithmetic, same iteration count)")
+                cpu["time_to_drop_estimate_s"] = cpu["seconds_per_step"] * ttd["fp64"]["iterations"]
+                cpu["time_to_drop_basis"] = ("CPU seconds per V-cycle x the V-cycles to the drop (the FP64 GPU "
+                                             "run and the oracle need the same count, see parity)")
+        if hist is not None:
+            parity = parity_record(p, blocks, hist, ttd["fp64"]["iterations"],
+                                   (ttd["fp64"]["forces"]["cl"], ttd["fp64"]["forces"]["cd"],
+                                    ttd["fp64"]["forces"]["cm"]), cf_fp64,
+                                   mixed_forces=(ttd["mixed"]["forces"]["cl"], ttd["mixed"]["forces"]["cd"],
+                                                 ttd["mixed"]["forces"]["cm"]))
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -571,7 +697,7 @@ def run_gb300(args, rank, world):
                            "autotuned": tuned},
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
                 "gpu_launches": launches * args.steps, "launches_per_step": launches,
-                "mixed_precision": mixed, "time_to_drop": ttd, "residual_hbm": big,
+                "mixed_precision": mixed, "time_to_drop": ttd, "parity": parity, "residual_hbm": big,
                 "forces": {"cl": cl, "cd": cd, "cm": cm}}
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -586,7 +712,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--cpu-seconds", type=float, default=16.0,
+                    help="seconds of the CPU timing port, spread over 1..all host threads")
+    ap.add_argument("--no-parity", dest="parity", action="store_false",
+                    help="skip the oracle run to the same drop (converged CL/CD/CM, Cf, residual history)")
     ap.add_argument("--drop-cap", type=float, default=60.0, help="seconds per time-to-drop run (0: skip)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="keep the default launch configuration (e.g. under a profiler, whose timing misleads it)")

@@ -204,6 +204,12 @@ int ec2d_launch_count(ec2d_ctx *ctx, long long *n);
 int ec2d_kernel_timing(ec2d_ctx *ctx, int enable);
 int ec2d_kernel_times(ec2d_ctx *ctx, char *buf, int buflen);
 
+/* Measured FP64 FMA throughput of the current device in TFLOP/s (2 FLOPs per
+ * FMA; independent FMA chains on every SM, best of five timed launches).  No
+ * counterpart in the reference: it is the denominator of the FP64 roofline
+ * that bounds the residual and LU-SGS kernels on this part. */
+int ec2d_measure_fp64_peak(double *tflops);
+
 /* Residual norms without any device allocation.  No counterpart in the
  * reference: it serves hosts that cannot call cudaMalloc (a Fortran/OpenACC
  * host whose device memory belongs to another allocator or memory pool, or a

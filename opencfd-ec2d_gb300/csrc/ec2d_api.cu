@@ -760,7 +760,15 @@ void lusgs_update(ec2d_ctx *ctx, int l, double alfa1, bool force = false) {
   if (ctx->lusgs_fp32 && lv.fast32) {
     K(ctx, "k_lusgs32", l, 3, [&] { launch_lusgs_fast32(L, alfa1, mode, lv.max_rows, ctx->stream); });
   } else if (lv.fast64) {
-    K(ctx, "k_lusgs", l, 2, [&] { launch_lusgs_fast(L, alfa1, mode, lv.max_rows, lv.max_cols, ctx->lusgs_cs, ctx->lusgs_rpw, ctx->stream); });
+    auto go = [&](int part) {
+      launch_lusgs_fast(L, alfa1, mode | part, lv.max_rows, lv.max_cols, ctx->lusgs_cs, ctx->lusgs_rpw, ctx->stream);
+    };
+    if (ctx->timing) {  // the record builder and the sweep timed apart (together: the k_lusgs stage)
+      K(ctx, "k_lusgs_prep", l, 1, [&] { go(LUSGS_PREP_ONLY); });
+      K(ctx, "k_lusgs_sweep", l, 1, [&] { go(LUSGS_SWEEP_ONLY); });
+    } else {
+      K(ctx, "k_lusgs", l, 2, [&] { go(0); });
+    }
   } else {
     if (force) K(ctx, "k_add_force", l, 1, [&] { launch_add_force(L, ctx->stream); });
     K(ctx, "k_lusgs_generic", l, 1, [&] { launch_lusgs(L, alfa1, ctx->stream); });

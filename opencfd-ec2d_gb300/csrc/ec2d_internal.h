@@ -33,7 +33,9 @@ void launch_lusgs(const Lvl &L, double alfa1, cudaStream_t s);
 int lusgs_planes(int nv);
 // mode bits of the wavefront launchers: update U in the sweep, and take
 // Res + QF for Res (a coarse level's forcing when its residual is reused)
-enum { LUSGS_UPDATE = 1, LUSGS_FORCE = 2 };
+// PREP_ONLY / SWEEP_ONLY launch one of the two kernels of the FP64 wavefront
+// (record builder, sweep), so that per-kernel timing can bracket each
+enum { LUSGS_UPDATE = 1, LUSGS_FORCE = 2, LUSGS_PREP_ONLY = 4, LUSGS_SWEEP_ONLY = 8 };
 // cs: 0 the four-lanes-per-row kernel where it fits, with at most rpw rows
 // per CTA (else one CTA per block), 1 one CTA per block with rpw rows per
 // warp, 2..8 a cluster of cs CTAs with a barrier per plane

@@ -925,7 +925,8 @@ size_t smem_bytes(int R, int th) {
 
 template <int NV>
 void sweep_nv(const Lvl &L, double alfa1, int mode, int max_rows, int max_cols, int cs, int rpw, cudaStream_t s) {
-  k_lusgs_prep<NV><<<L.ntiles, TILE, 0, s>>>(L, alfa1, mode & LUSGS_FORCE);
+  if (!(mode & LUSGS_SWEEP_ONLY)) k_lusgs_prep<NV><<<L.ntiles, TILE, 0, s>>>(L, alfa1, mode & LUSGS_FORCE);
+  if (mode & LUSGS_PREP_ONLY) return;
   const int update = mode & LUSGS_UPDATE;
   if (cs == 0) {
     // the requested band height, else four-lane bands of 24 or 32 rows

@@ -137,6 +137,7 @@ def lib():
         "ec2d_mlp_loss_grad": ([vp, fp, fp, ctypes.c_int, dp], ctypes.c_int),
         "ec2d_mlp_predict": ([vp, fp, ctypes.c_longlong, fp], ctypes.c_int),
         "ec2d_mlp_set_gemm": ([vp, ctypes.c_int], ctypes.c_int),
+        "ec2d_measure_fp64_peak": ([dp], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -148,6 +149,13 @@ def lib():
 
 def _dp(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def measure_fp64_peak():
+    """Measured FP64 FMA throughput of the current device, TFLOP/s."""
+    t = ctypes.c_double()
+    _ck(lib().ec2d_measure_fp64_peak(ctypes.byref(t)), "ec2d_measure_fp64_peak")
+    return t.value
 
 
 def _fp(a):

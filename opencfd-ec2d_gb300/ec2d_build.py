@@ -13,7 +13,7 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "lib", "libec2d_gpu.so")
 SOURCES = ["ec2d_api.cu", "k_residual.cu", "k_turb.cu", "k_bl.cu", "k_bc.cu", "k_lusgs.cu", "k_sweep.cu",
-           "k_sweep32.cu", "k_misc.cu", "k_noalloc.cu", "k_mlp.cu",
+           "k_sweep32.cu", "k_misc.cu", "k_noalloc.cu", "k_mlp.cu", "k_peak.cu",
            "k_gemm_tc.cu"]
 # per-file flags: the Baldwin-Lomax switch is discrete, so its products and
 # sums are rounded one by one like the reference's

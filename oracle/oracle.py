@@ -14,6 +14,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "libec2d_oracle.so")
+# the same source built -O3 with FMA contraction: the benchmark's CPU timing
+# baseline, never a parity reference
+LIB_FAST = os.path.join(HERE, "_build", "libec2d_oracle_fast.so")
 
 F_RES, F_DT, F_LCI, F_LCJ, F_LVI, F_LVJ, F_DU, F_AMU, F_AMUT, F_X1, F_Y1, F_VOL = range(12)
 F_SI, F_SJ, F_NI1, F_NI2, F_NJ1, F_NJ2, F_DW, F_QF, F_DELTU, F_UN, F_X, F_Y = range(12, 24)
@@ -53,19 +56,20 @@ def to_struct(p, cls=OrcParams):
     return s
 
 
-_lib = None
+_libs = {}
 
 
 def build():
     subprocess.run(["make", "-s", "-C", HERE], check=True)
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB):
+def lib(fast=False):
+    """The parity build (default) or, with fast=True, the timing build."""
+    path = LIB_FAST if fast else LIB
+    if path not in _libs:
+        if not os.path.exists(path):
             build()
-        L = ctypes.CDLL(LIB)
+        L = ctypes.CDLL(path)
         vp, ip, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
         L.orc_new.restype = vp
         L.orc_new.argtypes = [ctypes.POINTER(OrcParams)]
@@ -97,8 +101,8 @@ def lib():
         L.orc_scheme.argtypes = [ctypes.c_int] + [ctypes.c_double] * 4 + [ctypes.c_int]
         L.orc_scheme.restype = ctypes.c_double
         L.orc_set_field.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
-        _lib = L
-    return _lib
+        _libs[path] = L
+    return _libs[path]
 
 
 def flux(iflux, QL, QR, gamma=1.4):
@@ -119,8 +123,8 @@ def _dp(a):
 class Oracle:
     """One case on the CPU oracle, driven like the reference main program."""
 
-    def __init__(self, params, blocks, fdm_blocks=(), dw=None, threads=None):
-        L = lib()
+    def __init__(self, params, blocks, fdm_blocks=(), dw=None, threads=None, fast=False):
+        L = lib(fast)
         if threads is not None:
             L.orc_set_threads(int(threads))
         self.L = L

@@ -1,0 +1,179 @@
+"""Converged-answer parity on the benchmark workloads at their full sizes.
+
+The correctness bar for the drop-in: converged lift, drag and moment
+coefficients and the residual-history shape within 1e-6 of the FP64 oracle,
+and one residual evaluation within 1e-12 per cell.  Against the committed
+oracle fixtures (tests/golden/converged.json, made by
+tests/golden/make_converged.py) and against the oracle run live:
+
+* laminar flat plate, 2 x 97x97 blocks, 3-level V-cycle with LU-SGS
+  smoothing -- the benchmark's exact shape and launch configuration -- from
+  the freestream to a 1e-8 drop of Res_rms(1): the same V-cycle count, CL,
+  CD, CM and every wall face's Cf, and Res_rms(1) at every 25th V-cycle; in
+  FP64 and with the FP32 LU-SGS (mixed precision: the error against the FP64
+  oracle is stated per coefficient);
+* the same workload, 200 V-cycles against the oracle run live;
+* the 4-block 513x129 RANS C-grid (NACA 2412, M 0.73, Re 6.5e6, WENO5 patch
+  on every block, 3-level multigrid), SA and SST: one residual per cell and
+  100 V-cycles against the oracle run live;
+* the NACA 0012 Euler workload, which the reference discretisation does not
+  converge: the GPU follows the oracle's limit-cycle record until the
+  trajectories part (the cycle amplifies last-bit differences), keeps its
+  amplitude, and stops at T < 1e-5 where the oracle does.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from helpers import compare_fields, compare_residual, make_gpu, make_oracle
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "converged.json")
+
+# the contract: converged coefficients and Res_rms(1) history within 1e-6
+COEF_TOL = 1.0e-6
+HIST_TOL = 1.0e-6
+
+
+@pytest.fixture(scope="module")
+def gold():
+    with open(GOLD) as fh:
+        return json.load(fh)
+
+
+def _run_to_drop_with_history(g, check=25, target=1e-8, cap=20000):
+    g.init_flow()
+    g.step(1)
+    r0 = g.norms()[1][0]
+    hist, it = [r0], 1
+    while hist[-1] > target * r0 and it < cap:
+        g.step(check)
+        it += check
+        hist.append(g.norms()[1][0])
+    return it, np.array(hist)
+
+
+@pytest.mark.parametrize("bits", [64, 32])
+def test_flat_plate_converged_forces_and_history(gpu_lib, gold, bits):
+    from ec2d import cases
+    fx = gold["flat_plate"]
+    p, bl = cases.laminar_flat_plate(97, 97, num_mesh=3)
+    g = make_gpu(p, bl)
+    g.set_lusgs_precision(bits)
+    it, hist = _run_to_drop_with_history(g, fx["check_every"], fx["target"])
+    f = np.array(g.forces(1))
+    cf, _ = g.wall_cf(1, 2, 2)
+    g.close()
+    assert it == fx["iterations"]
+    fo = np.array([fx["forces"][k] for k in ("cl", "cd", "cm")])
+    # measured: |dCL|, |dCD|, |dCM| ~1e-15 in both precisions
+    assert np.max(np.abs(f - fo)) <= COEF_TOL
+    assert np.max(np.abs(f - fo)) <= 1e-12
+    cfo = np.array(fx["wall"]["cf"])
+    assert cf.shape == cfo.shape
+    assert np.max(np.abs(cf - cfo)) <= 1e-12 * np.max(np.abs(cfo))
+    ho = np.array(fx["history_res_rms1"])
+    assert hist.shape == ho.shape
+    # measured: at most 5.4e-7 (FP64) and 3.4e-7 (FP32 LU-SGS), at the last
+    # checks, where Res_rms(1) is 1e-8 of its start and carries the
+    # round-off of the flux differences
+    assert np.max(np.abs(hist - ho) / ho) <= HIST_TOL
+
+
+def test_flat_plate_bench_shape_tracks_oracle(gpu_lib):
+    """200 V-cycles of the benchmark workload from the freestream on the GPU
+    (eight-lane banded wavefront on an 8-CTA cluster for the 96-row fine
+    level) and on the oracle run live: U within 1e-11 (measured 3e-14)."""
+    from ec2d import cases
+    p, bl = cases.laminar_flat_plate(97, 97, num_mesh=3)
+    orc = make_oracle(p, bl, threads=8)
+    orc.init_flow()
+    g = make_gpu(p, bl)
+    g.init_flow()
+    orc.step(200)
+    g.step(200)
+    for b in (1, 2):
+        a, c = orc.get_U(1, b), g.download_U(1, 1, b)
+        for m in range(4):
+            assert np.max(np.abs(a[m] - c[m])) <= 1e-11 * np.abs(a[m]).max()
+    np.testing.assert_allclose(g.norms()[1][:4], orc.norms()[1][:4], rtol=1e-9)
+    g.close()
+
+
+@pytest.mark.parametrize("turb", [2, 3])
+def test_rans_4block_513x129_at_size(gpu_lib, turb):
+    """The RANS workload at its size (4 blocks of 129x129 nodes, 65,536
+    cells): wall distance, one residual per cell after 5 oracle V-cycles, the
+    primitive and viscous fields, then 100 V-cycles on both sides."""
+    from ec2d import cases
+    p, bl, fdm = cases.rans_naca2412(turb=turb)
+    orc = make_oracle(p, bl, fdm=fdm, threads=8)
+    orc.init_flow()
+    g = make_gpu(p, bl, fdm=fdm)
+    g.init_flow()
+    compare_fields(orc, g, [18], tol=1e-13)  # wall distance
+    orc.step(5)
+    for b in range(1, len(bl) + 1):
+        g.upload_U(1, 1, b, orc.get_U(1, b))
+    orc.residual()
+    g.residual()
+    compare_residual(orc, g)
+    compare_fields(orc, g, [1, 2, 3, 7])
+    if turb == 2:
+        compare_fields(orc, g, [4, 5, 8])
+    else:
+        # SST mu_t (F2 blending, vorticity limiter) and the viscous radii
+        # from it: the primitives' last-bit differences grow to ~1e-9 here
+        compare_fields(orc, g, [4, 5, 8], tol=1e-8)
+    orc.step(100)
+    g.step(100)
+    for b in range(1, len(bl) + 1):
+        a, c = orc.get_U(1, b), g.download_U(1, 1, b)
+        for m in range(a.shape[0]):
+            assert np.max(np.abs(a[m] - c[m])) <= 1e-10 * np.abs(a[m]).max(), (b, m)
+    np.testing.assert_allclose(g.forces(1), orc.forces(), rtol=1e-10, atol=1e-12)
+    g.close()
+
+
+def test_naca0012_euler_limit_cycle(gpu_lib, gold):
+    from ec2d import cases
+    fx = gold["naca0012_euler"]
+    rec = fx["record"]
+    p, bl = cases.euler_naca0012()
+    g = make_gpu(p, bl)
+    g.init_flow()
+    cl = []
+    for _ in rec["step"]:
+        g.step(fx["every"])
+        cl.append(g.forces(1)[0])
+    steps = np.array(rec["step"])
+    cl, clo = np.array(cl), np.array(rec["cl"])
+    d = np.abs(cl - clo)
+    # the trajectories agree to 1e-8 through step 5,000 and to 1e-6 through
+    # 7,000 (measured: first 1e-8 excess at 5,400, first 1e-6 at 8,120)
+    assert np.all(d[steps <= 5000] <= 1e-8)
+    assert np.all(d[steps <= 7000] <= 1e-6)
+    # once they part, the GPU stays on the same cycle: CL extremes within 0.1
+    # and its mean within 0.02 over steps 4,000..13,000 (measured 0.03 / 0.004)
+    late = steps >= 4000
+    assert abs(cl[late].min() - clo[late].min()) <= 0.1
+    assert abs(cl[late].max() - clo[late].max()) <= 0.1
+    assert abs(cl[late].mean() - clo[late].mean()) <= 0.02
+    # and, like the oracle, it stops on T < 1e-5 (oracle: step 13,244;
+    # GPU measured 13,249)
+    from ec2d import gpu
+    done, stop = fx["steps"], None
+    while done < fx["stop"]["step"] + 500:
+        g.step(1)
+        done += 1
+        try:
+            g.norms()
+        except gpu.EC2DError as e:
+            stop = done
+            assert e.code == 3
+            break
+    g.close()
+    assert stop is not None and abs(stop - fx["stop"]["step"]) <= 500
