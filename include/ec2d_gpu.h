@@ -141,6 +141,24 @@ int ec2d_init_flow(ec2d_ctx *ctx);
 int ec2d_upload_U(ec2d_ctx *ctx, int case_id, int mesh, int block, const double *U);
 int ec2d_download_U(ec2d_ctx *ctx, int case_id, int mesh, int block, double *U);
 
+/* Asynchronous snapshot of a case's fine-mesh U for `output` at Kstep_save
+ * (opencfd_ec2d_v1.5.4.f90:181,284-371), where ec2d_download_U would stall
+ * the loop.  ec2d_snapshot enqueues, after the work queued so far, a device
+ * copy of every block's U in the layout of ec2d_download_U, and the copy of
+ * it to pinned host memory on a stream of its own; it returns at once and
+ * later steps run while the copy proceeds (the block's eddy viscosity is
+ * copied with it).  ec2d_snapshot_wait waits for
+ * that copy and gives the case, Kstep and tt at which it was taken;
+ * ec2d_snapshot_U copies one block of it into U(NVAR,-1:nx+1,-1:ny+1)
+ * (waiting first).  One snapshot is held at a time: a new one replaces it
+ * (the main stream waits only if the previous copy is still running). */
+int ec2d_snapshot(ec2d_ctx *ctx, int case_id);
+int ec2d_snapshot_wait(ec2d_ctx *ctx, int *case_id, int *kstep, double *tt);
+int ec2d_snapshot_U(ec2d_ctx *ctx, int block, double *U);
+/* The eddy viscosity Amu_t(-1:nx+1,-1:ny+1) of one block at the snapshot
+ * (the Amut column of flow2d.dat is Amu_t * Re). */
+int ec2d_snapshot_amut(ec2d_ctx *ctx, int block, double *amut);
+
 /* Advance `nsteps` iterations of the main loop (opencfd_ec2d_v1.5.4.f90:174-180):
  * NS_Time_advance(1) when Num_Mesh==1, else one 2- or 3-level V-cycle. */
 int ec2d_step(ec2d_ctx *ctx, int nsteps);

@@ -138,6 +138,18 @@ struct ec2d_ctx {
   struct KRec { const char *name; int level, nk; cudaEvent_t a, b; };
   std::vector<KRec> krec;
   std::vector<cudaEvent_t> evpool;
+  // asynchronous snapshot of one case's fine-level U (ec2d_snapshot): the
+  // blocks in the reference's layout, packed on the device on the main
+  // stream, then copied to pinned host memory on the snapshot stream while
+  // the main stream runs on
+  cudaStream_t snap_stream = nullptr;
+  cudaEvent_t ev_snap = nullptr, ev_snap_done = nullptr;
+  double *d_snap = nullptr, *h_snap = nullptr;
+  size_t snap_cap = 0;
+  int snap_case = 0, snap_kstep = 0;
+  double snap_tt = 0.0;
+  bool snap_pending = false;
+  std::vector<size_t> snap_off;  // per block of the case: offset in the snapshot
 };
 
 namespace {
@@ -1059,6 +1071,14 @@ void ec2d_destroy(ec2d_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  if (ctx->snap_stream) {
+    cudaStreamSynchronize(ctx->snap_stream);
+    cudaStreamDestroy(ctx->snap_stream);
+    cudaEventDestroy(ctx->ev_snap);
+    cudaEventDestroy(ctx->ev_snap_done);
+  }
+  if (ctx->d_snap) cudaFree(ctx->d_snap);
+  if (ctx->h_snap) cudaFreeHost(ctx->h_snap);
   for (auto &lv : ctx->lv) lv.bufs.clear();
   for (auto &r : ctx->krec) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   for (auto e : ctx->evpool) cudaEventDestroy(e);
@@ -1237,6 +1257,100 @@ int ec2d_download_U(ec2d_ctx *ctx, int case_id, int mesh, int block, double *U) 
   launch_unpack_u(L, k, L.nvar, ctx->d_stage, items, ctx->stream);
   CK(cudaMemcpyAsync(U, ctx->d_stage, (size_t)items * L.nvar * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  return EC2D_OK;
+}
+
+int ec2d_snapshot(ec2d_ctx *ctx, int case_id) {
+  if (!ctx || !ctx->setup_done || !valid_case(ctx, case_id)) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  if (!ctx->snap_stream) {
+    CK(cudaStreamCreateWithFlags(&ctx->snap_stream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&ctx->ev_snap, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ctx->ev_snap_done, cudaEventDisableTiming));
+  }
+  const Level &lv = ctx->lv[1];
+  const Lvl &L = lv.L;
+  const HCase &hc = ctx->cases[case_id - 1];
+  // per block: U in the layout of ec2d_download_U, then the block's mu_t
+  // frame ((nx+5) x (ny+5), origin (-2,-2)) for the Amut column of flow2d.dat
+  std::vector<size_t> off;
+  size_t n = 0;
+  for (int b = 1; b <= (int)hc.blocks.size(); b++) {
+    int k = find_block(ctx, case_id, 1, b);
+    if (k < 0) return EC2D_ERR_ARG;
+    off.push_back(n);
+    n += (size_t)(lv.blk[k].nx + 3) * (lv.blk[k].ny + 3) * L.nvar;
+    n += (size_t)lv.blk[k].P * (lv.blk[k].ny + 5);
+  }
+  // the previous snapshot's copy reads the device buffer: the main stream
+  // waits for it before packing over it (only when snapshots come faster
+  // than their copies)
+  if (ctx->snap_pending) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_snap_done, 0));
+  if (n > ctx->snap_cap) {
+    CK(cudaStreamSynchronize(ctx->snap_stream));
+    if (ctx->d_snap) cudaFree(ctx->d_snap);
+    if (ctx->h_snap) cudaFreeHost(ctx->h_snap);
+    ctx->d_snap = nullptr;
+    ctx->h_snap = nullptr;
+    ctx->snap_cap = 0;
+    CK(cudaMalloc(&ctx->d_snap, n * sizeof(double)));
+    CK(cudaMallocHost(&ctx->h_snap, n * sizeof(double)));
+    ctx->snap_cap = n;
+  }
+  for (int b = 1; b <= (int)hc.blocks.size(); b++) {
+    int k = find_block(ctx, case_id, 1, b);
+    const BlkDev &bd = lv.blk[k];
+    int items = (bd.nx + 3) * (bd.ny + 3);
+    launch_unpack_u(L, k, L.nvar, ctx->d_snap + off[b - 1], items, ctx->stream);
+    CK(cudaMemcpyAsync(ctx->d_snap + off[b - 1] + (size_t)items * L.nvar, L.amut + bd.off,
+                       (size_t)bd.P * (bd.ny + 5) * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  ctx->launches += (long long)hc.blocks.size();
+  CK(cudaEventRecord(ctx->ev_snap, ctx->stream));
+  CK(cudaStreamWaitEvent(ctx->snap_stream, ctx->ev_snap, 0));
+  CK(cudaMemcpyAsync(ctx->h_snap, ctx->d_snap, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->snap_stream));
+  CK(cudaEventRecord(ctx->ev_snap_done, ctx->snap_stream));
+  ctx->snap_off = off;
+  ctx->snap_case = case_id;
+  ctx->snap_kstep = hc.kstep[1];
+  ctx->snap_tt = hc.tt[1];
+  ctx->snap_pending = true;
+  return check_launch(ctx);
+}
+
+int ec2d_snapshot_wait(ec2d_ctx *ctx, int *case_id, int *kstep, double *tt) {
+  if (!ctx || !ctx->snap_pending) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  CK(cudaEventSynchronize(ctx->ev_snap_done));
+  if (case_id) *case_id = ctx->snap_case;
+  if (kstep) *kstep = ctx->snap_kstep;
+  if (tt) *tt = ctx->snap_tt;
+  return EC2D_OK;
+}
+
+int ec2d_snapshot_U(ec2d_ctx *ctx, int block, double *U) {
+  if (!ctx || !ctx->snap_pending || !U || block < 1 || block > (int)ctx->snap_off.size()) return EC2D_ERR_ARG;
+  int r = ec2d_snapshot_wait(ctx, nullptr, nullptr, nullptr);
+  if (r) return r;
+  int k = find_block(ctx, ctx->snap_case, 1, block);
+  if (k < 0) return EC2D_ERR_ARG;
+  const BlkDev &b = ctx->lv[1].blk[k];
+  size_t n = (size_t)(b.nx + 3) * (b.ny + 3) * ctx->lv[1].L.nvar;
+  memcpy(U, ctx->h_snap + ctx->snap_off[block - 1], n * sizeof(double));
+  return EC2D_OK;
+}
+
+int ec2d_snapshot_amut(ec2d_ctx *ctx, int block, double *amut) {
+  if (!ctx || !ctx->snap_pending || !amut || block < 1 || block > (int)ctx->snap_off.size()) return EC2D_ERR_ARG;
+  int r = ec2d_snapshot_wait(ctx, nullptr, nullptr, nullptr);
+  if (r) return r;
+  int k = find_block(ctx, ctx->snap_case, 1, block);
+  if (k < 0) return EC2D_ERR_ARG;
+  const BlkDev &b = ctx->lv[1].blk[k];
+  const double *fr = ctx->h_snap + ctx->snap_off[block - 1] + (size_t)(b.nx + 3) * (b.ny + 3) * ctx->lv[1].L.nvar;
+  for (int j = -1; j <= b.ny + 1; j++)
+    for (int i = -1; i <= b.nx + 1; i++)
+      amut[(size_t)(i + 1) + (size_t)(b.nx + 3) * (j + 1)] = fr[(size_t)(j + 2) * b.P + (i + 2)];
   return EC2D_OK;
 }
 

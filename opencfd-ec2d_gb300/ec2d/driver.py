@@ -1,0 +1,84 @@
+"""The reference main program (opencfd_ec2d_v1.5.4.f90:142-186) as a Python
+host over the C-ABI: read the case directory, hand it to the library, march
+until t_end (or a step count), print and record the residuals every
+Kstep_show steps and write the flow files every Kstep_save steps and at the
+end.
+
+The flow files at Kstep_save come from asynchronous snapshots
+(ec2d_snapshot): the library copies U to pinned host memory on a stream of
+its own while the steps go on, and the files of a snapshot are written once
+the next snapshot is taken or the run ends, so the marching does not wait for
+the device-to-host copy.
+
+  python -m ec2d.driver <case_dir> [--steps N] [--fix-nvar-restart]
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import time
+
+from . import gpu, inputs, outputs
+
+
+def read_fdm(directory: str):
+    """Block numbers listed in FDM.in (sub_Finite_Difference.f90:287-308):
+    four comment lines, the count, one more line, one block per line."""
+    path = os.path.join(directory, "FDM.in")
+    if not os.path.exists(path):
+        return []
+    lines = open(path).read().splitlines()
+    n = int(lines[4].split()[0])
+    return [int(lines[6 + k].split()[0]) for k in range(n)]
+
+
+def run(directory: str, steps: int = None, device: int = 0, fix_nvar: bool = False, quiet: bool = False) -> dict:
+    p, blocks = inputs.read_case(directory)
+    fdm = read_fdm(directory)
+    s = gpu.Solver([(p, blocks)], device=device, fdm_blocks=[fdm])
+    if p.Iflag_init == 0:
+        s.init_flow()
+    else:
+        outputs.restart(s, directory, fix_nvar=fix_nvar)
+    geometry = outputs.read_blocks(s)  # x1, y1 (constant) for the snapshot files
+    res_path = os.path.join(directory, "Residual.dat")
+    pending, written, done, tt, kstep = None, [], 0, 0.0, 0
+    t0 = time.perf_counter()
+    while tt < p.t_end and (steps is None or done < steps):
+        s.step(1)
+        done += 1
+        rmax, rrms, kstep, tt = s.norms()
+        if kstep % max(1, p.Kstep_show) == 0:  # output_Res(1)
+            if not quiet:
+                print(f" Kstep, t= {kstep} {tt}  Res_rms(1:{p.nvar()}) = {rrms[:p.nvar()]}")
+            with open(res_path, "a") as fh:
+                fh.write(inputs.residual_record(kstep, rmax, rrms, p.nvar()))
+        if kstep % max(1, p.Kstep_save) == 0:  # output(1), from a snapshot
+            if pending is not None:
+                written += outputs.write_output(directory, s, p, kstep=pending,
+                                                blocks=outputs.snapshot_blocks(s, geometry))
+            s.snapshot(1)
+            pending = kstep
+    if pending is not None:
+        written += outputs.write_output(directory, s, p, kstep=pending, blocks=outputs.snapshot_blocks(s, geometry))
+    written += outputs.write_output(directory, s, p, kstep=kstep)  # the final output(1)
+    forces = s.forces(1)
+    s.close()
+    return {"steps": done, "kstep": kstep, "tt": tt, "seconds": time.perf_counter() - t0, "files": written,
+            "forces": forces}
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("case_dir")
+    ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--fix-nvar-restart", action="store_true",
+                    help="read SST2d.dat for 6-variable states on restart (the reference tests NVAR == 5)")
+    a = ap.parse_args()
+    r = run(a.case_dir, a.steps, a.device, a.fix_nvar_restart)
+    print(f"steps {r['steps']} Kstep {r['kstep']} tt {r['tt']} ({r['seconds']:.2f} s); CL CD CM {r['forces']}")
+
+
+if __name__ == "__main__":
+    main()

@@ -138,6 +138,10 @@ def lib():
         "ec2d_mlp_predict": ([vp, fp, ctypes.c_longlong, fp], ctypes.c_int),
         "ec2d_mlp_set_gemm": ([vp, ctypes.c_int], ctypes.c_int),
         "ec2d_measure_fp64_peak": ([dp], ctypes.c_int),
+        "ec2d_snapshot": ([vp, ctypes.c_int], ctypes.c_int),
+        "ec2d_snapshot_wait": ([vp, ip, ip, dp], ctypes.c_int),
+        "ec2d_snapshot_U": ([vp, ctypes.c_int, dp], ctypes.c_int),
+        "ec2d_snapshot_amut": ([vp, ctypes.c_int, dp], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -237,6 +241,35 @@ class Solver:
 
     def step(self, n=1):
         _ck(self.L.ec2d_step(self.h, n), "ec2d_step")
+
+    def snapshot(self, case=1):
+        """Enqueue an asynchronous copy of the case's fine-mesh U (returns at once)."""
+        _ck(self.L.ec2d_snapshot(self.h, case), "ec2d_snapshot")
+
+    def snapshot_wait(self):
+        """Wait for the last snapshot; returns (case, Kstep, tt) at which it was taken."""
+        c, k, t = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        _ck(self.L.ec2d_snapshot_wait(self.h, ctypes.byref(c), ctypes.byref(k), ctypes.byref(t)),
+            "ec2d_snapshot_wait")
+        return c.value, k.value, t.value
+
+    def snapshot_U(self, block, case=None):
+        """One block of the last snapshot, U(NVAR,-1:nx+1,-1:ny+1)."""
+        if case is None:
+            case = self.snapshot_wait()[0]
+        nx, ny, nv = self.dims(case, 1, block)
+        U = np.zeros((nv, nx + 3, ny + 3), order="F")
+        _ck(self.L.ec2d_snapshot_U(self.h, block, _dp(U)), "ec2d_snapshot_U")
+        return U
+
+    def snapshot_amut(self, block, case=None):
+        """Amu_t(-1:nx+1,-1:ny+1) of one block at the last snapshot."""
+        if case is None:
+            case = self.snapshot_wait()[0]
+        nx, ny, _ = self.dims(case, 1, block)
+        a = np.zeros((nx + 3, ny + 3), order="F")
+        _ck(self.L.ec2d_snapshot_amut(self.h, block, _dp(a)), "ec2d_snapshot_amut")
+        return a
 
     def norms(self, case=1, mesh=1):
         a = np.zeros(6); b = np.zeros(6)

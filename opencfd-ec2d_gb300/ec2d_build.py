@@ -63,7 +63,28 @@ def build(verbose: bool = False, extra=()) -> str:
         list(ex.map(run, jobs))
     if jobs or not os.path.exists(LIB):
         run([nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
+    build_host(verbose)
     return LIB
+
+
+HOST_SRC = os.path.join(HERE, "host", "ec2d_host.c")
+HOST = os.path.join(HERE, "lib", "ec2d_host")
+
+
+def build_host(verbose: bool = False) -> str:
+    """The C replica of the reference driver (host/ec2d_host.c), linked
+    against the library beside it (rpath $ORIGIN)."""
+    inc = os.path.join(HERE, "..", "include")
+    if os.path.exists(HOST) and not _stale(HOST, [HOST_SRC, LIB, os.path.join(inc, "ec2d_gpu.h")]):
+        return HOST
+    cmd = [os.environ.get("CC", "gcc"), "-O2", "-std=c11", "-Wall", "-I", inc, HOST_SRC, "-o", HOST,
+           "-L", os.path.dirname(LIB), "-lec2d_gpu", "-Wl,-rpath,$ORIGIN"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"host build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return HOST
 
 
 if __name__ == "__main__":

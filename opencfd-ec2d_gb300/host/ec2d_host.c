@@ -1,0 +1,284 @@
+/*
+ * ec2d_host.c -- a C replica of the OpenCFD-EC2D driver over the C-ABI of
+ * libec2d_gpu.so: the host a Fortran build would be, for machines without a
+ * Fortran compiler.
+ *
+ * It follows `program main` (opencfd_ec2d_v1.5.4.f90:142-186): read
+ * control.in (read_parameter, :197-235), Mesh2d.dat and bc2d_1.in
+ * (Creat_Mesh1 + read_bcin, sub_init.f90:111-251) and, when present, FDM.in
+ * (Init_FiniteDifference, sub_Finite_Difference.f90:278-311); hand them to
+ * the library; then the main loop
+ *
+ *     do while (tt < t_end)
+ *       NS_Time_advance(1) / NS_2stge_multigrid / NS_3stge_multigrid
+ *       if (mod(Kstep, Kstep_show) == 0) call output_Res(1)
+ *
+ * with the step body replaced by ec2d_step and output_Res writing the same
+ * Residual.dat record, format (I8,13E24.10) (opencfd_ec2d_v1.5.4.f90:266-279).
+ * The input files are read in the reference's formats, unchanged.
+ *
+ *   ec2d_host [case_dir] [--steps N] [--device D]
+ *
+ * --steps N stops after N steps (the reference stops only on tt >= t_end).
+ * At the end it prints the last step's residual norms and CL, CD, CM.
+ * Exit status: 0, or the EC2D_ERR_* code of the failing call (a T < 1e-5
+ * state prints the reference's message and stops, as sub_Residual.f90:143-146
+ * does).
+ */
+#include <ctype.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "ec2d_gpu.h"
+
+#define MAXB 64
+#define MAXLINE 4096
+
+typedef struct {
+  int nx, ny, nsub;
+  double *x, *y; /* x(1:nx,1:ny), column-major */
+  int *bc9;      /* nsub x 9 */
+} host_block;
+
+static char *path_in(const char *dir, const char *name) {
+  static char buf[4096];
+  snprintf(buf, sizeof(buf), "%s/%s", dir, name);
+  return buf;
+}
+
+/* Fortran list-directed reals accept d/D exponents */
+static double fnum(const char *tok) {
+  char t[128];
+  size_t n = strlen(tok);
+  if (n >= sizeof(t)) n = sizeof(t) - 1;
+  for (size_t k = 0; k < n; k++) t[k] = (tok[k] == 'd' || tok[k] == 'D') ? 'e' : tok[k];
+  t[n] = 0;
+  return strtod(t, NULL);
+}
+
+/* the whitespace-separated tokens of one line */
+static int split(char *line, char **tok, int maxtok) {
+  int n = 0;
+  char *s = line;
+  while (*s && n < maxtok) {
+    while (*s && (isspace((unsigned char)*s) || *s == ',')) s++;
+    if (!*s) break;
+    tok[n++] = s;
+    while (*s && !isspace((unsigned char)*s) && *s != ',') s++;
+    if (*s) *s++ = 0;
+  }
+  return n;
+}
+
+static int read_lines(const char *path, char lines[][MAXLINE], int maxl) {
+  FILE *f = fopen(path, "r");
+  if (!f) return -1;
+  int n = 0;
+  while (n < maxl && fgets(lines[n], MAXLINE, f)) n++;
+  fclose(f);
+  return n;
+}
+
+/* read_parameter: the data lines 2, 4, 6, 8, 10 (and 12: moment point) */
+static int read_control(const char *dir, ec2d_params *p) {
+  static char L[16][MAXLINE];
+  char *t[32];
+  int n = read_lines(path_in(dir, "control.in"), L, 16);
+  if (n < 10) return -1;
+  memset(p, 0, sizeof(*p));
+  if (split(L[1], t, 32) < 10) return -1;
+  p->Ma = fnum(t[0]); p->Re = fnum(t[1]); p->gamma = fnum(t[2]); p->AoA = fnum(t[3]);
+  p->Pr = fnum(t[4]); p->t_end = fnum(t[5]);
+  p->Kstep_save = (int)fnum(t[6]); p->If_viscous = (int)fnum(t[7]);
+  p->Iflag_turbulence_model = (int)fnum(t[8]); p->Iflag_init = (int)fnum(t[9]);
+  if (split(L[3], t, 32) < 12) return -1;
+  p->Iflag_local_dt = (int)fnum(t[0]); p->dt_global = fnum(t[1]); p->CFL = fnum(t[2]);
+  p->dtmax = fnum(t[3]); p->dtmin = fnum(t[4]); p->Time_Method = (int)fnum(t[5]);
+  p->P_outlet = fnum(t[6]); p->T_inf = fnum(t[7]); p->Twall = fnum(t[8]);
+  p->vt_inf = fnum(t[9]); p->Kt_inf = fnum(t[10]); p->Wt_inf = fnum(t[11]);
+  if (split(L[5], t, 32) < 4) return -1;
+  p->Iflag_Scheme = (int)fnum(t[0]); p->Iflag_flux = (int)fnum(t[1]);
+  p->IFlag_Reconstruction = (int)fnum(t[2]); p->Kstep_show = (int)fnum(t[3]);
+  if (split(L[7], t, 32) < 4) return -1;
+  p->Num_Mesh = (int)fnum(t[0]); p->Num_Threads = (int)fnum(t[1]);
+  p->Nstep_Inner_Limit = (int)fnum(t[2]); p->Res_Inner_Limit = fnum(t[3]);
+  int k = split(L[9], t, 32);
+  for (int m = 0; m < 3; m++) p->Pre_Step_Mesh[m] = (m < k && m < p->Num_Mesh) ? (int)fnum(t[m]) : 0;
+  p->xaxis = 0.25;
+  p->yaxis = 0.0;
+  if (n > 11 && split(L[11], t, 32) >= 2 && (isdigit((unsigned char)t[0][0]) || t[0][0] == '-' || t[0][0] == '.')) {
+    p->xaxis = fnum(t[0]);
+    p->yaxis = fnum(t[1]);
+  }
+  /* multigrid levels are smoothed by LU-SGS when the time method is LU-SGS
+   * (the reference refuses that combination, opencfd_ec2d_v1.5.4.f90:216-221) */
+  p->mg_lusgs = 1;
+  if (p->Kstep_show < 1) p->Kstep_show = 1;
+  return 0;
+}
+
+/* Mesh2d.dat: number of blocks, (nx, ny) per block, then per block x(:,:)
+ * and y(:,:) in Fortran order (sub_init.f90:121-127,176) */
+static int read_mesh(const char *dir, host_block *B, int *nb) {
+  FILE *f = fopen(path_in(dir, "Mesh2d.dat"), "r");
+  if (!f) return -1;
+  char tok[128];
+  if (fscanf(f, "%127s", tok) != 1) { fclose(f); return -1; }
+  *nb = (int)fnum(tok);
+  if (*nb < 1 || *nb > MAXB) { fclose(f); return -1; }
+  for (int m = 0; m < *nb; m++) {
+    if (fscanf(f, "%127s", tok) != 1) { fclose(f); return -1; }
+    B[m].nx = (int)fnum(tok);
+    if (fscanf(f, "%127s", tok) != 1) { fclose(f); return -1; }
+    B[m].ny = (int)fnum(tok);
+  }
+  for (int m = 0; m < *nb; m++) {
+    size_t n = (size_t)B[m].nx * B[m].ny;
+    B[m].x = (double *)malloc(n * sizeof(double));
+    B[m].y = (double *)malloc(n * sizeof(double));
+    for (int a = 0; a < 2; a++) {
+      double *v = a ? B[m].y : B[m].x;
+      for (size_t k = 0; k < n; k++) {
+        if (fscanf(f, "%127s", tok) != 1) { fclose(f); return -1; }
+        v[k] = fnum(tok);
+      }
+    }
+  }
+  fclose(f);
+  return 0;
+}
+
+/* bc2d_1.in: title, "# Blocks", count; per block "Block n", "Subface",
+ * count, a header line and one 9-integer row per subface (sub_init.f90:228-248) */
+static int read_bc(const char *dir, host_block *B, int nb) {
+  static char L[4096][MAXLINE];
+  char *t[32];
+  int n = read_lines(path_in(dir, "bc2d_1.in"), L, 4096);
+  if (n < 3) return -1;
+  int k = 2;
+  if (split(L[k++], t, 32) < 1 || (int)fnum(t[0]) != nb) {
+    fprintf(stderr, "Block number in bc2d.in is not equal to that in Mesh2d.dat\n");
+    return -1;
+  }
+  for (int m = 0; m < nb; m++) {
+    k += 2;
+    if (k >= n || split(L[k++], t, 32) < 1) return -1;
+    B[m].nsub = (int)fnum(t[0]);
+    k++;
+    B[m].bc9 = (int *)malloc((size_t)B[m].nsub * 9 * sizeof(int));
+    for (int s = 0; s < B[m].nsub; s++) {
+      if (k >= n || split(L[k++], t, 32) < 9) return -1;
+      for (int q = 0; q < 9; q++) B[m].bc9[s * 9 + q] = (int)fnum(t[q]);
+    }
+  }
+  return 0;
+}
+
+/* FDM.in: four comment lines, the block count, one more line, then one
+ * block number per line (sub_Finite_Difference.f90:287-308) */
+static int read_fdm(const char *dir, int *ids, int nb) {
+  static char L[MAXB + 16][MAXLINE];
+  char *t[8];
+  int n = read_lines(path_in(dir, "FDM.in"), L, MAXB + 16);
+  if (n < 0) return 0;
+  if (n < 5 || split(L[4], t, 8) < 1) return 0;
+  int cnt = (int)fnum(t[0]), got = 0;
+  for (int k = 0; k < cnt && 6 + k < n; k++) {
+    if (split(L[6 + k], t, 8) < 1) continue;
+    int md = (int)fnum(t[0]);
+    if (md > nb || md < 1) fprintf(stderr, "error in 'FDM.in'\n");
+    else ids[got++] = md;
+  }
+  return got;
+}
+
+/* Fortran E24.10: 0.dddddddddddE+xx right-justified in 24 columns */
+static void e24(FILE *f, double v) {
+  char m[64], out[64];
+  if (v == 0.0) { fprintf(f, "%24s", "0.0000000000E+00"); return; }
+  snprintf(m, sizeof(m), "%.9e", v < 0 ? -v : v); /* d.ddddddddde+xx */
+  char *e = strchr(m, 'e');
+  int ex = atoi(e + 1) + 1;
+  char digits[16];
+  digits[0] = m[0];
+  memcpy(digits + 1, m + 2, 9);
+  digits[10] = 0;
+  snprintf(out, sizeof(out), "%s0.%sE%c%02d", v < 0 ? "-" : "", digits, ex < 0 ? '-' : '+', ex < 0 ? -ex : ex);
+  fprintf(f, "%24s", out);
+}
+
+static int fail(const char *what, int r) {
+  fprintf(stderr, "%s: %s (%d)\n", what, ec2d_error_string(r), r);
+  return r;
+}
+
+int main(int argc, char **argv) {
+  const char *dir = ".";
+  long max_steps = -1;
+  int device = 0;
+  for (int a = 1; a < argc; a++) {
+    if (!strcmp(argv[a], "--steps") && a + 1 < argc) max_steps = atol(argv[++a]);
+    else if (!strcmp(argv[a], "--device") && a + 1 < argc) device = atoi(argv[++a]);
+    else dir = argv[a];
+  }
+  ec2d_params P;
+  if (read_control(dir, &P)) { fprintf(stderr, "cannot read %s\n", path_in(dir, "control.in")); return 1; }
+  static host_block B[MAXB];
+  int nb = 0;
+  if (read_mesh(dir, B, &nb)) { fprintf(stderr, "cannot read %s\n", path_in(dir, "Mesh2d.dat")); return 1; }
+  if (read_bc(dir, B, nb)) { fprintf(stderr, "cannot read %s\n", path_in(dir, "bc2d_1.in")); return 1; }
+  int fdm[MAXB], nfdm = read_fdm(dir, fdm, nb);
+  int nvar = P.Iflag_turbulence_model == 3 ? 6 : P.Iflag_turbulence_model == 2 ? 5 : 4;
+
+  ec2d_ctx *ctx = NULL;
+  int r, cs = 0;
+  if ((r = ec2d_create(device, &ctx))) return fail("ec2d_create", r);
+  if ((r = ec2d_add_case(ctx, &P, &cs))) return fail("ec2d_add_case", r);
+  for (int m = 0; m < nb; m++)
+    if ((r = ec2d_add_block(ctx, cs, B[m].nx, B[m].ny, B[m].x, B[m].y, B[m].nsub, B[m].bc9)))
+      return fail("ec2d_add_block", r);
+  for (int k = 0; k < nfdm; k++)
+    if ((r = ec2d_set_fdm_block(ctx, cs, fdm[k]))) return fail("ec2d_set_fdm_block", r);
+  if ((r = ec2d_setup(ctx))) return fail("ec2d_setup", r);
+  if ((r = ec2d_init_flow(ctx))) return fail("ec2d_init_flow", r);
+  printf(" Start ......\n");
+
+  double rmax[6] = {0}, rrms[6] = {0}, tt = 0.0;
+  int kstep = 0;
+  long done = 0;
+  char rpath[4096];
+  snprintf(rpath, sizeof(rpath), "%s/Residual.dat", dir);
+  while (tt < P.t_end && (max_steps < 0 || done < max_steps)) {
+    if ((r = ec2d_step(ctx, 1))) return fail("ec2d_step", r);
+    done++;
+    r = ec2d_residual(ctx, cs, 1, rmax, rrms, &kstep, &tt);
+    if (r == EC2D_ERR_STATE) {
+      int code, blk, i, j;
+      ec2d_status(ctx, cs, &code, &blk, &i, &j);
+      printf("T <1.d-5 ! at block %d cell (%d,%d)\n", blk, i, j);
+      ec2d_destroy(ctx);
+      return r;
+    }
+    if (r) return fail("ec2d_residual", r);
+    if (kstep % P.Kstep_show == 0) { /* output_Res(1) */
+      FILE *f = fopen(rpath, "a");
+      if (f) {
+        fprintf(f, "%8d", kstep);
+        for (int m = 0; m < 6; m++) e24(f, rmax[m]);
+        for (int m = 0; m < nvar; m++) e24(f, rrms[m]);
+        fprintf(f, "\n");
+        fclose(f);
+      }
+    }
+  }
+  double cl = 0, cd = 0, cm = 0;
+  if ((r = ec2d_forces(ctx, cs, &cl, &cd, &cm))) return fail("ec2d_forces", r);
+  printf("steps %ld kstep %d tt %.17g\n", done, kstep, tt);
+  printf("res_rms");
+  for (int m = 0; m < nvar; m++) printf(" %.17g", rrms[m]);
+  printf("\nforces %.17g %.17g %.17g\n", cl, cd, cm);
+  ec2d_destroy(ctx);
+  for (int m = 0; m < nb; m++) { free(B[m].x); free(B[m].y); free(B[m].bc9); }
+  return 0;
+}
