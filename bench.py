@@ -277,11 +277,14 @@ def time_to_drop(g, cells, cap_s=60.0, target=1e-8, check=25):
 # level (dram__bytes_read.sum + dram__bytes_write.sum, caches flushed before
 # the launch; the run is in the profiling summaries of the repo)
 PROFILED_TRAFFIC = {("k_lusgs", 1): 7426816.0}
-# FP64 FLOPs per fine cell of one laminar residual evaluation (k_prim,
+# FP64 work per fine cell of one laminar residual evaluation (k_prim,
 # k_flux_i, k_flux_j, k_res; AUSM+, MUSCL van Albada, primitive
-# reconstruction), from one ncu capture of those kernels:
-# (dadd + dmul + 2 dfma) thread instructions / cells
-FP64_FLOPS_PER_CELL_RESIDUAL = None
+# reconstruction) on the 4.19 M-cell grid, from one ncu capture of those
+# kernels (thread instructions executed / cells): FLOPs = dadd + dmul +
+# 2 dfma, instructions = dadd + dmul + dfma.  Every FP64 instruction takes
+# one issue slot of the FP64 pipe, whose rate is half the FMA FLOP rate.
+FP64_FLOPS_PER_CELL_RESIDUAL = 966.1
+FP64_INST_PER_CELL_RESIDUAL = 689.9
 SWEEP_PLANES = lambda blocks, lev: 2 * max((b.nx - 1) // 2 ** (lev - 1) + (b.ny - 1) // 2 ** (lev - 1) - 1
                                          for b in blocks)
 
@@ -375,9 +378,15 @@ def residual_hbm(torch, gpu, dev, reps=10):
         # FP64 roofline: FLOPs executed per cell (ncu instruction counts of the
         # residual kernels: dadd + dmul + 2 dfma per thread) / stage time
         flops = FP64_FLOPS_PER_CELL_RESIDUAL * cells / (total_ms / 1e3) / 1e12
+        inst = FP64_INST_PER_CELL_RESIDUAL * cells / (total_ms / 1e3) / 1e12
         out.update({"bound": "fp64", "fp64_flops_per_cell": FP64_FLOPS_PER_CELL_RESIDUAL,
+                    "fp64_inst_per_cell": FP64_INST_PER_CELL_RESIDUAL,
                     "fp64_tflops": flops, "fp64_peak_tflops": fp64_peak, "fp64_frac": flops / fp64_peak,
-                    "fp64_peak_source": "measured in this run (ec2d_measure_fp64_peak: FMA chains on every SM)"})
+                    "fp64_issue_frac": inst / (fp64_peak / 2.0),
+                    "fp64_peak_source": "measured in this run (ec2d_measure_fp64_peak: FMA chains on every SM)",
+                    "note": ("FP64 instruction issue bounds this stage: fp64_issue_frac = FP64 instructions per "
+                             "second / the FP64 pipe's instruction rate (measured FMA FLOP/s / 2); fp64_frac "
+                             "counts FLOPs, where a dadd or dmul is one FLOP in one issue slot")})
     return out
 
 
