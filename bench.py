@@ -390,44 +390,138 @@ def residual_hbm(torch, gpu, dev, reps=10):
     return out
 
 
-def leg_polar(args):
-    """The batched polar (64 SA RANS cases from a seed, 257x65 to 513x129,
-    1-4 blocks, 3-level V-cycle): V-cycle throughput of the whole batch in one
-    context (FP64 and with FP32 LU-SGS) against the plain drop-in, one case
-    per context in FP64, timed on a sample of the same cases."""
-    import torch
-    from ec2d import cases, gpu
-    pc = cases.polar_cases(64)
-    cells = sum(fine_cells(bl) for _, bl in pc)
-    res = {"cases": len(pc), "cells": cells, "step": "one 3-level V-cycle of every case"}
-    g = gpu.Solver(pc)
-    stream = torch.cuda.ExternalStream(g.stream_handle())
-    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:0")
-    for bits in (64, 32):
-        g.set_lusgs_precision(bits)
+def plain_step_ms(torch, gpu, pc, steps=10):
+    """Milliseconds per V-cycle of every case as the plain drop-in: one
+    context per case, FP64 LU-SGS, the step graph replayed, CUDA events on
+    the context's stream after three warm-up V-cycles."""
+    out = []
+    for case in pc:
+        g = gpu.Solver([case[:2]])
+        st = torch.cuda.ExternalStream(g.stream_handle())
         g.init_flow()
         g.step(3)
         g.sync()
-        ms, launches = timed_steps(torch, g, stream, flush, args.steps)
-        res[f"batched_fp{bits}"] = {"value": cells * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
-                                    "launches_per_step": launches}
-    g.close()
-    plain = []
-    for k in range(4):
-        p1 = gpu.Solver([pc[k]])
-        s1 = torch.cuda.ExternalStream(p1.stream_handle())
-        p1.init_flow()
-        p1.step(3)
-        p1.sync()
-        ms, _ = timed_steps(torch, p1, s1, flush, args.steps)
-        plain.append((fine_cells(pc[k][1]), ms / args.steps))
-        p1.close()
-    rate = sum(c for c, _ in plain) / (sum(t for _, t in plain) / 1e3)
-    res["plain_fp64_one_case_per_context"] = {"value": rate, "sample_cases": 4,
-                                              "ms_per_step": [t for _, t in plain]}
-    res["batched_mixed_vs_plain"] = res["batched_fp32"]["value"] / rate
-    res["unit"] = UNIT
-    return res
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        g.step(steps)
+        e1.record(st)
+        e1.synchronize()
+        out.append(e0.elapsed_time(e1) / steps)
+        g.close()
+    return out
+
+
+def polar_metric(args, torch, gpu):
+    """The metric's comparison on the 64-case polar (SA RANS cases from a
+    seed: M in [0.3, 0.8], AoA in [-2, 8] deg, Re in [1e6, 1e7], t/c in [0.09,
+    0.15], 257x65 to 513x129, 1-4 blocks, 3-level V-cycle, LU-SGS):
+
+    * plain: the GPU drop-in, one case per context, FP64.  Its time to a
+      drop D for case c is that case's V-cycles to D times its own ms per
+      V-cycle (plain_step_ms).  The V-cycle counts come from the FP64 batch,
+      whose per-case arithmetic is the plain drop-in's bit for bit (one launch
+      per stage covers every case; cases never read each other's data).
+    * batched_mixed: all 64 cases in one context, FP32 LU-SGS (FP64
+      residual, boundary conditions, transfers, norms), freestream start.
+    * learned_batched_mixed: the same from the warm-start network's
+      prediction (inference inside the timed region), the network trained
+      in this run on fields the solver generated (learned leg, below).
+
+    Every run is capped at args.polar_cap seconds; residuals are checked
+    every 25 V-cycles.  For each drop D the comparison uses the cases that
+    reached D in both arms: plain time = the sum of their plain times (one
+    context after the other), batched time = the wall time until the last of
+    them reached D."""
+    import numpy as np
+    from ec2d import cases, learn
+    pc = cases.polar_cases(64, with_tc=True)
+    cells = sum(fine_cells(bl) for _, bl, _ in pc)
+    targets = (1e-3, 1e-4, 1e-6, 1e-8)
+    out = {"cases": len(pc), "cells": cells, "cap_s": args.polar_cap, "check_every": 25,
+           "targets": [f"{t:.0e}" for t in targets]}
+    net, learned = None, None
+    if args.polar_learned:
+        net, learned = learned_leg(args, gpu)
+        out["learned_training"] = learned
+    t0 = time.perf_counter()
+    fp64 = learn.converge(gpu, pc, "freestream", 64, targets=targets, max_steps=10 ** 6, check=25,
+                          max_seconds=args.polar_cap)
+    r0 = fp64["r0"]
+    arms = {"batched_fp64": fp64,
+            "batched_mixed": learn.converge(gpu, pc, "freestream", 32, r0=r0, targets=targets, max_steps=10 ** 6,
+                                            check=25, max_seconds=args.polar_cap)}
+    if net is not None:
+        arms["learned_batched_mixed"] = learn.converge(gpu, pc, "warm", 32, r0=r0, net=net, targets=targets,
+                                                       max_steps=10 ** 6, check=25, max_seconds=args.polar_cap)
+        net.close()
+    plain_ms = plain_step_ms(torch, gpu, pc)
+    out["plain_ms_per_vcycle"] = {"median": float(np.median(plain_ms)), "min": float(np.min(plain_ms)),
+                                  "max": float(np.max(plain_ms)), "sum": float(np.sum(plain_ms))}
+    for name, r in arms.items():
+        out[name] = {"reached": {k: v["reached"] for k, v in r["targets"].items()}, "vcycles": r["steps"],
+                     "seconds": r["seconds"], "ms_per_vcycle": r["seconds"] / max(r["steps"], 1) * 1e3,
+                     "diverged": r["diverged"], "start_seconds": r["start_seconds"],
+                     "setup_seconds": r["setup_seconds"], "download_seconds": r["download_seconds"],
+                     "warm_start_fallback_cases": r["fallback"]}
+    plain_first = fp64["first"]
+    comp = {}
+    for t in targets:
+        key = f"{t:.0e}"
+        ok_plain = plain_first[t] >= 0
+        row = {"plain_reached": int(ok_plain.sum())}
+        for name in [n for n in arms if n != "batched_fp64"]:
+            r = arms[name]
+            both = ok_plain & (r["first"][t] >= 0)
+            if not both.any():
+                row[name] = {"common_cases": 0}
+                continue
+            plain_s = float(np.sum(np.array(plain_ms)[both] * plain_first[t][both]) / 1e3)
+            batch_s = float(np.max(r["when"][t][both]))
+            e2e_s = batch_s + r["setup_seconds"] + r["download_seconds"]
+            row[name] = {"reached": int((r["first"][t] >= 0).sum()), "common_cases": int(both.sum()),
+                         "plain_seconds": plain_s, "batched_seconds": batch_s, "speedup": plain_s / batch_s,
+                         "e2e_seconds": e2e_s, "e2e_speedup": plain_s / e2e_s}
+        comp[key] = row
+    out["comparison"] = comp
+    # the headline: the deepest drop that at least half of the cases reached
+    # in the plain run and in the learned (else the freestream) batch
+    head = "learned_batched_mixed" if "learned_batched_mixed" in arms else "batched_mixed"
+    out["headline"] = None
+    for t in targets:
+        row = comp[f"{t:.0e}"].get(head, {})
+        if row.get("common_cases", 0) >= len(pc) // 2:
+            out["headline"] = {"drop": f"{t:.0e}", "arm": head, **row}
+    out["seconds"] = time.perf_counter() - t0
+    out["unit"] = "wall seconds to the drop for the cases both arms reached"
+    return out
+
+
+def learned_leg(args, gpu):
+    """The warm-start network of the polar comparison: args.ws_train SA cases
+    of the learned family (257x65 C-grid, the polar box, seed 20261203) solved
+    in batches in FP32 LU-SGS from the freestream until every case's drop
+    reached args.ws_gen_target, or its plateau, or args.ws_gen_steps steps,
+    or args.ws_gen_cap seconds per batch; then args.ws_train_steps Adam steps
+    on all their cells.  Dataset generation and training are reported here
+    and are not part of the time-to-drop comparison."""
+    import numpy as np
+    from ec2d import learn
+    train_cases = learn.warmstart_cases(args.ws_train, seed=20261203)
+    net = gpu.WarmStartNet(hidden=6, width=256, seed=1)
+    gen = learn.generate(gpu, net, train_cases, steps=args.ws_gen_steps, target=args.ws_gen_target,
+                         max_seconds=args.ws_gen_cap)
+    tr = learn.train(net, steps=args.ws_train_steps)
+    drops = np.array(gen.pop("drops"))
+    gen["drops_quartiles"] = [float(x) for x in np.quantile(drops[np.isfinite(drops)], [0.25, 0.5, 0.75])]
+    return net, {"network": "6 hidden layers x 256, SiLU, BF16 weights/activations, FP32 accumulate",
+                 "generate": gen, "train": tr}
+
+
+def leg_polar(args):
+    """The batched polar, as the default run reports it."""
+    import torch
+    from ec2d import gpu
+    return polar_metric(args, torch, gpu)
 
 
 def leg_mlp(args):
@@ -478,7 +572,8 @@ def leg_learned(args):
     train_cases = learn.warmstart_cases(args.ws_train, seed=20261203)
     held = learn.warmstart_cases(args.ws_held, seed=20261204)
     net = gpu.WarmStartNet(hidden=6, width=256, seed=1)
-    gen = learn.generate(gpu, net, train_cases, steps=args.ws_gen_steps)
+    gen = learn.generate(gpu, net, train_cases, steps=args.ws_gen_steps, target=args.ws_gen_target,
+                         max_seconds=args.ws_gen_cap)
     tr = learn.train(net, steps=args.ws_train_steps)
     ev = learn.evaluate(gpu, net, held, targets=(1e-4, 1e-6, args.ws_target), max_steps=args.ws_max_steps,
                         plain_sample=args.ws_plain)
@@ -676,6 +771,9 @@ def run_gb300(args, rank, world):
     big = None
     if args.residual_hbm and rank == 0:
         big = residual_hbm(torch, gpu, dev)
+    polar = None
+    if args.polar and rank == 0 and world == 1:
+        polar = polar_metric(args, torch, gpu)
 
     if rank == 0:
         cpu = None
@@ -707,7 +805,12 @@ def run_gb300(args, rank, world):
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
                 "gpu_launches": launches * args.steps, "launches_per_step": launches,
                 "mixed_precision": mixed, "time_to_drop": ttd, "parity": parity, "residual_hbm": big,
+                "polar": polar, "learned_batched_vs_plain": polar["headline"] if polar else None,
                 "forces": {"cl": cl, "cd": cd, "cm": cm}}
+        if polar:
+            line["config"]["polar"] = (f"64 SA cases of the polar box (257x65..513x129, 1-4 blocks, 3-level "
+                                       f"V-cycle), each run capped at {args.polar_cap:g} s; warm-start network "
+                                       f"trained in this run on {args.ws_train} generated 257x65 fields")
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.barrier()
@@ -733,10 +836,17 @@ def main():
     ap.add_argument("--leg", default="all", choices=["all", "residual_hbm", "polar", "learned", "mlp"],
                     help="residual_hbm: the 4.19 M-cell residual alone (for profiling); polar: the 64-case "
                          "batched polar; learned: the learned warm start end to end")
-    ap.add_argument("--ws-train", type=int, default=512)
+    ap.add_argument("--no-polar", dest="polar", action="store_false",
+                    help="skip the 64-case polar comparison (learned+batched+mixed vs plain)")
+    ap.add_argument("--polar-cap", type=float, default=20.0, help="seconds per polar run")
+    ap.add_argument("--no-polar-learned", dest="polar_learned", action="store_false",
+                    help="polar comparison without the warm-start network")
+    ap.add_argument("--ws-gen-target", type=float, default=1e-6)
+    ap.add_argument("--ws-gen-cap", type=float, default=15.0, help="seconds per generation batch of 64 cases")
+    ap.add_argument("--ws-train", type=int, default=64)
     ap.add_argument("--ws-held", type=int, default=64)
-    ap.add_argument("--ws-gen-steps", type=int, default=3000)
-    ap.add_argument("--ws-train-steps", type=int, default=6000)
+    ap.add_argument("--ws-gen-steps", type=int, default=30000)
+    ap.add_argument("--ws-train-steps", type=int, default=2000)
     ap.add_argument("--ws-target", type=float, default=1e-8)
     ap.add_argument("--ws-max-steps", type=int, default=30000)
     ap.add_argument("--ws-plain", type=int, default=4, help="held-out cases also run one per context in FP64")

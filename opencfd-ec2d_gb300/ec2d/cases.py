@@ -61,11 +61,11 @@ def rans_naca2412(nx=513, ny=129, nblocks=4, turb=TURB_SA, num_mesh=3, weno5=Tru
     return p, blocks, fdm
 
 
-def polar_cases(n=64, seed=20261203, min_size=(257, 65), max_size=(513, 129)):
+def polar_cases(n=64, seed=20261203, min_size=(257, 65), max_size=(513, 129), with_tc=False):
     """Batched polar: n SA RANS cases drawn from a seed.  M ~ U[0.3,0.8],
     AoA ~ U[-2,8] deg, log10 Re ~ U[6,7], t/c ~ U[0.09,0.15], 1..4 blocks,
     grids between 257x65 and 513x129 (node counts that keep three multigrid
-    levels)."""
+    levels).  with_tc: (params, blocks, t/c) triples."""
     rng = np.random.default_rng(seed)
     sizes = [(257, 65), (385, 97), (513, 129)]
     sizes = [s for s in sizes if min_size[0] <= s[0] <= max_size[0]]
@@ -87,7 +87,7 @@ def polar_cases(n=64, seed=20261203, min_size=(257, 65), max_size=(513, 129)):
         first = 1.0e-6 * 6.5e6 / re * 4.0
         blocks = grids.naca_cgrid(nx, ny, m=0.0, p=0.0, t=tc, radius=20.0, n_wake=n_wake, first=first,
                                   nblocks=nb)
-        out.append((p, blocks))
+        out.append((p, blocks, tc) if with_tc else (p, blocks))
     return out
 
 

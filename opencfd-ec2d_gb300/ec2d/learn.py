@@ -53,26 +53,50 @@ def _solver(gpu, chunk, bits):
     return s
 
 
-def generate(gpu, net, cases, steps: int, batch: int = 64, bits: int = 32) -> Dict:
-    """Solve the cases in batches for `steps` iterations from the freestream
-    and add every fine-mesh cell of the result to the network's samples."""
+def generate(gpu, net, cases, steps: int, batch: int = 64, bits: int = 32, target: float = None,
+             check: int = 500, plateau: float = 0.8, max_seconds: float = None) -> Dict:
+    """Solve the cases in batches from the freestream and add every fine-mesh
+    cell of the result to the network's samples.  A batch runs until every
+    case's Res_rms(1) dropped below `target` x its first-iteration value, or
+    until no case improved its drop by more than the factor `plateau` over
+    the last four checks (`check` steps apart), or `steps` steps, or
+    `max_seconds` per batch.  Records each field's drop and where it
+    stopped."""
     t0 = time.perf_counter()
-    drops = []
+    drops, stopped = [], []
     for k in range(0, len(cases), batch):
         chunk = cases[k:k + batch]
         s = _solver(gpu, chunk, bits)
         s.init_flow()
         s.step(1)
         r0 = np.array([_rms(s, c) for c in range(1, len(chunk) + 1)])
-        s.step(steps - 1)
-        r = np.array([_rms(s, c) for c in range(1, len(chunk) + 1)])
-        drops.extend(list(r / r0))
+        tb, done, hist, why = time.perf_counter(), 1, [], "steps"
+        while done < steps:
+            n = min(check, steps - done)
+            s.step(n)
+            done += n
+            r = np.array([_rms(s, c) for c in range(1, len(chunk) + 1)]) / r0
+            hist.append(np.where(np.isfinite(r), r, np.inf))
+            if target is not None and np.all(hist[-1] <= target):
+                why = "target"
+                break
+            if len(hist) > 4 and np.all(hist[-1] > plateau * hist[-5]):
+                why = "plateau"
+                break
+            if max_seconds is not None and time.perf_counter() - tb > max_seconds:
+                why = "time"
+                break
+        drops.extend(list(hist[-1]) if hist else [1.0] * len(chunk))
+        stopped.append({"steps": done, "stop": why})
         net.add_samples(s)
         s.close()
     d = np.array(drops)
-    return {"cases": len(cases), "steps": steps, "seconds": time.perf_counter() - t0,
-            "samples": net.num_samples(), "drop_median": float(np.nanmedian(d)),
-            "drop_max": float(np.nanmax(d))}
+    ok = np.isfinite(d)
+    return {"cases": len(cases), "steps_cap": steps, "target": target, "batches": stopped,
+            "seconds": time.perf_counter() - t0, "samples": net.num_samples(),
+            "drop_median": float(np.median(d[ok])) if ok.any() else None,
+            "drop_max": float(np.max(d[ok])) if ok.any() else None, "diverged": int((~ok).sum()),
+            "drops": [float(x) for x in d]}
 
 
 def train(net, steps: int, batch: int = 16384, lr: float = 1e-3) -> Dict:
@@ -95,13 +119,15 @@ def _rms(s, c):
 
 
 def converge(gpu, cases, start: str, bits: int, r0=None, net=None, targets=(1e-4, 1e-6, 1e-8),
-             max_steps: int = 30000, check: int = 50) -> Dict:
+             max_steps: int = 30000, check: int = 50, max_seconds: float = None) -> Dict:
     """Run all cases of `cases` in one context until every case's
     Res_rms(1) <= min(targets) x r0 or max_steps (r0: each case's
     freestream-start first residual, measured here when not given).
     start: 'freestream' or 'warm' (the network's prediction).  Records per
     case and target the first step and wall time at which it was reached."""
+    ts = time.perf_counter()
     s = _solver(gpu, cases, bits)
+    setup_s = time.perf_counter() - ts  # context set-up: grids to the device, geometry
     n = len(cases)
     if r0 is None:
         s.init_flow()
@@ -130,7 +156,14 @@ def converge(gpu, cases, start: str, bits: int, r0=None, net=None, targets=(1e-4
             when[t][new] = el
         if np.all(first[min(targets)] >= 0):
             break
+        if max_seconds is not None and el > max_seconds:
+            break
     wall = time.perf_counter() - t0
+    td = time.perf_counter()
+    for c in range(1, n + 1):  # the converged fields back to the host
+        for b in range(1, len(cases[c - 1][1]) + 1):
+            s.download_U(c, 1, b)
+    d2h_s = time.perf_counter() - td
     forces = np.array([s.forces(c) for c in range(1, n + 1)])
     s.close()
     per = {}
@@ -143,8 +176,10 @@ def converge(gpu, cases, start: str, bits: int, r0=None, net=None, targets=(1e-4
                            and int(0.9 * n) >= 1 else None,
                            "steps_per_case": first[t].tolist()}
     return {"start": start, "bits": bits, "cases": n, "steps": steps, "seconds": wall, "start_seconds": t_start,
+            "setup_seconds": setup_s, "download_seconds": d2h_s,
             "fallback": fallback, "final_drop_max": float(np.nanmax(ratio)), "targets": per,
-            "forces": forces, "r0": r0}
+            "diverged": int(np.sum(~np.isfinite(ratio))),
+            "forces": forces, "r0": r0, "first": first, "when": when}
 
 
 def evaluate(gpu, net, held, targets=(1e-4, 1e-6, 1e-8), max_steps=30000, plain_sample=4) -> Dict:
@@ -163,7 +198,7 @@ def evaluate(gpu, net, held, targets=(1e-4, 1e-6, 1e-8), max_steps=30000, plain_
     ms_batch = warm["seconds"] / max(warm["steps"], 1) * 1e3
 
     def strip(d):
-        return {k: v for k, v in d.items() if k not in ("forces", "r0")}
+        return {k: v for k, v in d.items() if k not in ("forces", "r0", "first", "when")}
 
     return {"targets": [f"{t:.0e}" for t in targets], "warm_batched_mixed": strip(warm),
             "freestream_batched_mixed": strip(free), "plain_sample": [strip(p) for p in plain],
