@@ -1,6 +1,7 @@
-// ec2d_api.cu -- the C-ABI (include/ec2d_gpu.h): context, one-time setup on
-// the host (geometry, ghost coordinates, coarse meshes, FDM metrics, device
-// layout) and the orchestration of the pseudo-time-marching sequences of
+// ec2d_api.cu -- the C-ABI (include/ec2d_gpu.h): context, one-time setup
+// (block and subface tables, device layout on the host; the geometry of every
+// level, ghost coordinates, coarse meshes and FDM metrics by the set-up
+// kernels of k_setup.cu) and the orchestration of the pseudo-time-marching sequences of
 // sub_NS_singlegrid.f90 and sub_NS_multigrid.f90 as kernel launches on the
 // context's stream.
 #include <cuda_runtime.h>
@@ -63,8 +64,7 @@ struct HLevelBlock {
   std::vector<int> bc;   // 9 per subface (level indices)
   int nsub;
   bool fdm;
-  Frame x, y, x1, y1, vol, si, sj, ni1, ni2, nj1, nj2;
-  Frame akx, aky, aix, aiy, ajac;
+  Frame x, y;  // fine level: the nodes from Mesh2d.dat (geometry is formed on the device)
 };
 
 struct DevBuf {
@@ -201,120 +201,6 @@ int mg_depth(const HCase &c) {
   return std::min(3, std::min(Km_grid, c.p.Num_Mesh));
 }
 
-void geometry(HLevelBlock &B) {
-  int nx = B.nx, ny = B.ny;
-  // cell areas and face lengths/normals (sub_init.f90:180-204)
-  for (int j = 1; j <= ny - 1; j++)
-    for (int i = 1; i <= nx - 1; i++)
-      B.vol(i, j) = std::fabs((B.x(i, j) - B.x(i + 1, j + 1)) * (B.y(i + 1, j) - B.y(i, j + 1)) -
-                              (B.x(i + 1, j) - B.x(i, j + 1)) * (B.y(i, j) - B.y(i + 1, j + 1))) * 0.5;
-  for (int j = 1; j <= ny - 1; j++)
-    for (int i = 1; i <= nx; i++) {
-      double dx = B.x(i, j + 1) - B.x(i, j), dy = B.y(i, j + 1) - B.y(i, j);
-      double s = std::sqrt(dx * dx + dy * dy);
-      B.si(i, j) = s; B.ni1(i, j) = dy / s; B.ni2(i, j) = -dx / s;
-    }
-  for (int j = 1; j <= ny; j++)
-    for (int i = 1; i <= nx - 1; i++) {
-      double dx = B.x(i + 1, j) - B.x(i, j), dy = B.y(i + 1, j) - B.y(i, j);
-      double s = std::sqrt(dx * dx + dy * dy);
-      B.sj(i, j) = s; B.nj1(i, j) = -dy / s; B.nj2(i, j) = dx / s;
-    }
-}
-
-// ghost node coordinates and cell centres of one level of one case
-// (Update_coordinate_buffer_onemesh, sub_boundary.f90:174-282)
-void ghost_coordinates(std::vector<HLevelBlock *> &blocks) {
-  for (HLevelBlock *Bp : blocks) {
-    HLevelBlock &B = *Bp;
-    for (int ks = 0; ks < B.nsub; ks++) {
-      const int *c = &B.bc[9 * ks];
-      int face = c[1], ib2 = c[2], ie2 = c[3], jb2 = c[4], je2 = c[5], neighb = c[6], msub = c[7], orient = c[8];
-      if (neighb > 0) {
-        int n1 = ie2 - ib2 + je2 - jb2 + 1;
-        HLevelBlock &B1 = *blocks[neighb - 1];
-        const int *c1 = &B1.bc[9 * (msub - 1)];
-        int f1 = c1[1], ib1 = c1[2], ie1 = c1[3], jb1 = c1[4], je1 = c1[5];
-        std::vector<double> ux(2 * n1 * LAP);
-        auto UX = [&](int cc, int k, int l) -> double & { return ux[(cc - 1) + 2 * ((k - 1) + n1 * (l - 1))]; };
-        for (int l = 1; l <= LAP; l++) {
-          if (f1 == 1) for (int k = 1; k <= je1 - jb1 + 1; k++) { UX(1, k, l) = B1.x(ib1 + l, jb1 + k - 1); UX(2, k, l) = B1.y(ib1 + l, jb1 + k - 1); }
-          else if (f1 == 2) for (int k = 1; k <= ie1 - ib1 + 1; k++) { UX(1, k, l) = B1.x(ib1 + k - 1, jb1 + l); UX(2, k, l) = B1.y(ib1 + k - 1, jb1 + l); }
-          else if (f1 == 3) for (int k = 1; k <= je1 - jb1 + 1; k++) { UX(1, k, l) = B1.x(ie1 - LAP - 1 + l, jb1 + k - 1); UX(2, k, l) = B1.y(ie1 - LAP - 1 + l, jb1 + k - 1); }
-          else for (int k = 1; k <= ie1 - ib1 + 1; k++) { UX(1, k, l) = B1.x(ib1 + k - 1, je1 - LAP - 1 + l); UX(2, k, l) = B1.y(ib1 + k - 1, je1 - LAP - 1 + l); }
-        }
-        for (int k = 1; k <= n1; k++) {
-          int k1 = (orient == 2) ? k : n1 + 1 - k;
-          for (int l = 1; l <= LAP; l++) {
-            int di, dj;
-            if (face == 1) { di = ib2 - LAP - 1 + l; dj = jb2 + k - 1; }
-            else if (face == 2) { di = ib2 + k - 1; dj = jb2 - LAP - 1 + l; }
-            else if (face == 3) { di = ie2 + l; dj = jb2 + k - 1; }
-            else { di = ib2 + k - 1; dj = je2 + l; }
-            B.x(di, dj) = UX(1, k1, l);
-            B.y(di, dj) = UX(2, k1, l);
-          }
-        }
-      } else {
-        for (int l = 1; l <= LAP; l++) {
-          if (face == 1) for (int j = jb2; j <= je2; j++) { B.x(ib2 - l, j) = 2.0 * B.x(ib2, j) - B.x(ib2 + l, j); B.y(ib2 - l, j) = 2.0 * B.y(ib2, j) - B.y(ib2 + l, j); }
-          else if (face == 2) for (int i = ib2; i <= ie2; i++) { B.x(i, jb2 - l) = 2.0 * B.x(i, jb2) - B.x(i, jb2 + l); B.y(i, jb2 - l) = 2.0 * B.y(i, jb2) - B.y(i, jb2 + l); }
-          else if (face == 3) for (int j = jb2; j <= je2; j++) { B.x(ie2 + l, j) = 2.0 * B.x(ie2, j) - B.x(ie2 - l, j); B.y(ie2 + l, j) = 2.0 * B.y(ie2, j) - B.y(ie2 - l, j); }
-          else for (int i = ib2; i <= ie2; i++) { B.x(i, je2 + l) = 2.0 * B.x(i, je2) - B.x(i, je2 - l); B.y(i, je2 + l) = 2.0 * B.y(i, je2) - B.y(i, je2 - l); }
-        }
-      }
-    }
-    int nx = B.nx, ny = B.ny;
-    for (int j = 1; j <= LAP; j++)
-      for (int i = 1; i <= LAP; i++) {
-        int i1 = 1 - i, j1 = 1 - j, i2 = nx + i, j2 = ny + j;
-        B.x(i1, j1) = B.x(i1, 1) + B.x(1, j1) - B.x(1, 1); B.y(i1, j1) = B.y(i1, 1) + B.y(1, j1) - B.y(1, 1);
-        B.x(i2, j2) = B.x(i2, ny) + B.x(nx, j2) - B.x(nx, ny); B.y(i2, j2) = B.y(i2, ny) + B.y(nx, j2) - B.y(nx, ny);
-        B.x(i1, j2) = B.x(i1, ny) + B.x(1, j2) - B.x(1, ny); B.y(i1, j2) = B.y(i1, ny) + B.y(1, j2) - B.y(1, ny);
-        B.x(i2, j1) = B.x(i2, 1) + B.x(nx, j1) - B.x(nx, 1); B.y(i2, j1) = B.y(i2, 1) + B.y(nx, j1) - B.y(nx, 1);
-      }
-    for (int j = 1 - LAP; j <= ny + LAP - 1; j++)
-      for (int i = 1 - LAP; i <= nx + LAP - 1; i++) {
-        B.x1(i, j) = (B.x(i, j) + B.x(i + 1, j) + B.x(i, j + 1) + B.x(i + 1, j + 1)) * 0.25;
-        B.y1(i, j) = (B.y(i, j) + B.y(i + 1, j) + B.y(i, j + 1) + B.y(i + 1, j + 1)) * 0.25;
-      }
-  }
-}
-
-// 6th/4th-order metric derivatives (dx0/dy0, sub_Finite_Difference.f90:387-439)
-void fdm_metrics(HLevelBlock &B) {
-  int nx = B.nx - 1, ny = B.ny - 1;
-  auto d_i = [&](Frame &f, int i, int j) -> double {
-    const double b1 = 8.0 / 12.0, b2 = 1.0 / 12.0, a1 = 1.0 / 60.0, a2 = -3.0 / 20.0, a3 = 3.0 / 4.0;
-    if (i >= 4 && i <= nx - 3) return a1 * (f(i + 3, j) - f(i - 3, j)) + a2 * (f(i + 2, j) - f(i - 2, j)) + a3 * (f(i + 1, j) - f(i - 1, j));
-    if (i == 1) return (-3.0 * f(1, j) + 4.0 * f(2, j) - f(3, j)) / 2.0;
-    if (i == 2) return (-2.0 * f(1, j) - 3.0 * f(2, j) + 6.0 * f(3, j) - f(4, j)) / 6.0;
-    if (i == 3) return b1 * (f(4, j) - f(2, j)) - b2 * (f(5, j) - f(1, j));
-    if (i == nx - 2) return b1 * (f(nx - 1, j) - f(nx - 3, j)) - b2 * (f(nx, j) - f(nx - 4, j));
-    if (i == nx - 1) return (f(nx - 3, j) - 6.0 * f(nx - 2, j) + 3.0 * f(nx - 1, j) + 2.0 * f(nx, j)) / 6.0;
-    return (f(nx - 2, j) - 4.0 * f(nx - 1, j) + 3.0 * f(nx, j)) / 2.0;
-  };
-  auto d_j = [&](Frame &f, int i, int j) -> double {
-    const double b1 = 8.0 / 12.0, b2 = 1.0 / 12.0, a1 = 1.0 / 60.0, a2 = -3.0 / 20.0, a3 = 3.0 / 4.0;
-    if (j >= 4 && j <= ny - 3) return a1 * (f(i, j + 3) - f(i, j - 3)) + a2 * (f(i, j + 2) - f(i, j - 2)) + a3 * (f(i, j + 1) - f(i, j - 1));
-    if (j == 1) return (-3.0 * f(i, 1) + 4.0 * f(i, 2) - f(i, 3)) / 2.0;
-    if (j == 2) return (-2.0 * f(i, 1) - 3.0 * f(i, 2) + 6.0 * f(i, 3) - f(i, 4)) / 6.0;
-    if (j == 3) return b1 * (f(i, 4) - f(i, 2)) - b2 * (f(i, 5) - f(i, 1));
-    if (j == ny - 2) return b1 * (f(i, ny - 1) - f(i, ny - 3)) - b2 * (f(i, ny) - f(i, ny - 4));
-    if (j == ny - 1) return (f(i, ny - 3) - 6.0 * f(i, ny - 2) + 3.0 * f(i, ny - 1) + 2.0 * f(i, ny)) / 6.0;
-    return (f(i, ny - 2) - 4.0 * f(i, ny - 1) + 3.0 * f(i, ny)) / 2.0;
-  };
-  B.akx.init(B.nx, B.ny); B.aky.init(B.nx, B.ny); B.aix.init(B.nx, B.ny); B.aiy.init(B.nx, B.ny);
-  B.ajac.init(B.nx, B.ny, 1.0);
-  for (int j = 1; j <= ny; j++)
-    for (int i = 1; i <= nx; i++) {
-      double xk = d_i(B.x1, i, j), yk = d_i(B.y1, i, j), xi = d_j(B.x1, i, j), yi = d_j(B.y1, i, j);
-      double J = 1.0 / (xk * yi - xi * yk);
-      B.ajac(i, j) = J;
-      B.akx(i, j) = J * yi; B.aky(i, j) = -J * xi; B.aix(i, j) = -J * yk; B.aiy(i, j) = J * xk;
-    }
-}
-
 CaseDev make_casedev(const ec2d_params &p) {
   CaseDev c{};
   c.gamma = p.gamma; c.Ma = p.Ma; c.Re = p.Re; c.Pr = p.Pr;
@@ -342,15 +228,15 @@ int build_level(ec2d_ctx *ctx, int l) {
   Level &lv = ctx->lv[l];
   const ec2d_params &P = ctx->P;
   int ncase = (int)ctx->cases.size();
-  // host geometry
+  // block tables (and the fine level's nodes)
   if (l == 1) {
     for (int c = 0; c < ncase; c++)
       for (int m = 0; m < (int)ctx->cases[c].blocks.size(); m++) {
         const HBlock &hb = ctx->cases[c].blocks[m];
         HLevelBlock B;
         B.nx = hb.nx; B.ny = hb.ny; B.cas = c; B.blk = m; B.bc = hb.bc; B.nsub = hb.nsub; B.fdm = hb.fdm;
-        Frame *fr[] = {&B.x, &B.y, &B.x1, &B.y1, &B.vol, &B.si, &B.sj, &B.ni1, &B.ni2, &B.nj1, &B.nj2};
-        for (Frame *f : fr) f->init(B.nx, B.ny);
+        B.x.init(B.nx, B.ny);
+        B.y.init(B.nx, B.ny);
         for (int j = 1; j <= B.ny; j++)
           for (int i = 1; i <= B.nx; i++) {
             B.x(i, j) = hb.x[(i - 1) + (size_t)B.nx * (j - 1)];
@@ -359,28 +245,17 @@ int build_level(ec2d_ctx *ctx, int l) {
         lv.hb.push_back(std::move(B));
       }
   } else {
-    // coarse mesh by node skipping (Creat_Mesh, sub_init.f90:276-373)
+    // coarse mesh by node skipping (Creat_Mesh, sub_init.f90:276-373): the
+    // block list and subface indices here, the nodes on the device
     for (auto &B1 : ctx->lv[l - 1].hb) {
       HLevelBlock B;
       B.nx = (B1.nx - 1) / 2 + 1; B.ny = (B1.ny - 1) / 2 + 1; B.cas = B1.cas; B.blk = B1.blk;
       B.nsub = B1.nsub; B.fdm = false; B.bc = B1.bc;
       for (int k = 0; k < B.nsub; k++)
         for (int q = 2; q <= 5; q++) B.bc[9 * k + q] = (B1.bc[9 * k + q] - 1) / 2 + 1;
-      Frame *fr[] = {&B.x, &B.y, &B.x1, &B.y1, &B.vol, &B.si, &B.sj, &B.ni1, &B.ni2, &B.nj1, &B.nj2};
-      for (Frame *f : fr) f->init(B.nx, B.ny);
-      for (int j = 1; j <= B.ny; j++)
-        for (int i = 1; i <= B.nx; i++) { B.x(i, j) = B1.x(2 * i - 1, 2 * j - 1); B.y(i, j) = B1.y(2 * i - 1, 2 * j - 1); }
       lv.hb.push_back(std::move(B));
     }
   }
-  for (auto &B : lv.hb) geometry(B);
-  // ghost coordinates per case (neighbour numbers are case-local)
-  for (int c = 0; c < ncase; c++) {
-    std::vector<HLevelBlock *> bl;
-    for (auto &B : lv.hb) if (B.cas == c) bl.push_back(&B);
-    ghost_coordinates(bl);
-  }
-  for (auto &B : lv.hb) if (B.fdm) fdm_metrics(B);
   // device layout
   std::vector<int> case_first_block(ncase, -1);
   long long off = 0;
@@ -583,15 +458,18 @@ int build_level(ec2d_ctx *ctx, int l) {
   }
   // geometry planes and initial values
   {
+    // the fine mesh's nodes (the rest of the geometry is formed on the
+    // device below), the wall distance plane at 1 until comput_dw fills it
     std::vector<double> g((size_t)NG * F, 0.0);
     std::vector<double> u((size_t)nv * F, 0.0), un((size_t)nv * F, 0.0);
-    std::vector<double> met(anyfdm ? (size_t)5 * F : 0, 0.0);
     for (int k = 0; k < (int)lv.hb.size(); k++) {
       auto &B = lv.hb[k];
       long long o = lv.blk[k].off;
-      size_t n = B.x.v.size();
-      Frame *src[] = {&B.vol, &B.si, &B.sj, &B.ni1, &B.ni2, &B.nj1, &B.nj2, &B.x, &B.y, &B.x1, &B.y1};
-      for (int q = 0; q < 11; q++) std::copy(src[q]->v.begin(), src[q]->v.end(), g.begin() + (size_t)q * F + o);
+      size_t n = (size_t)(B.nx + 5) * (B.ny + 5);
+      if (l == 1) {
+        std::copy(B.x.v.begin(), B.x.v.end(), g.begin() + (size_t)G_X * F + o);
+        std::copy(B.y.v.begin(), B.y.v.end(), g.begin() + (size_t)G_Y * F + o);
+      }
       for (size_t t = 0; t < n; t++) g[(size_t)G_DW * F + o + t] = 1.0;
       // B%U(1)=1, U(2)=U(3)=0, U(4)=1 (+ turbulence) ; Un(4)=0 fine, 1 coarse (sub_init.f90:161-174, 311-312)
       for (size_t t = 0; t < n; t++) {
@@ -600,16 +478,14 @@ int build_level(ec2d_ctx *ctx, int l) {
         if (l == 1 && nv == 5) u[4 * F + o + t] = 1.0 / ctx->cases[B.cas].p.Re;
         if (l == 1 && nv == 6) { u[4 * F + o + t] = 0.0; u[5 * F + o + t] = 1.0; }
       }
-      if (B.fdm) {
-        Frame *ms[] = {&B.akx, &B.aky, &B.aix, &B.aiy, &B.ajac};
-        for (int q = 0; q < 5; q++) std::copy(ms[q]->v.begin(), ms[q]->v.end(), met.begin() + (size_t)q * F + o);
-      }
     }
     CK(cudaMemcpy(L.geo, g.data(), g.size() * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(L.U, u.data(), u.size() * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(L.un, un.data(), un.size() * sizeof(double), cudaMemcpyHostToDevice));
-    if (anyfdm) CK(cudaMemcpy(L.met, met.data(), met.size() * sizeof(double), cudaMemcpyHostToDevice));
   }
+  // coarse nodes, areas, faces, ghost nodes, cell centres, FDM metrics
+  launch_setup_geometry(L, l > 1 ? &ctx->lv[l - 1].L : nullptr, anyfdm, ctx->stream);
+  CK(cudaGetLastError());
   launch_face_metrics(L, ctx->stream);
   CK(cudaGetLastError());
   if (L.bcn) {

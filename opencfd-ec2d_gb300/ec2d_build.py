@@ -13,11 +13,12 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "lib", "libec2d_gpu.so")
 SOURCES = ["ec2d_api.cu", "k_residual.cu", "k_turb.cu", "k_bl.cu", "k_bc.cu", "k_lusgs.cu", "k_sweep.cu",
-           "k_sweep32.cu", "k_misc.cu", "k_noalloc.cu", "k_mlp.cu", "k_peak.cu",
+           "k_sweep32.cu", "k_misc.cu", "k_noalloc.cu", "k_mlp.cu", "k_peak.cu", "k_setup.cu",
            "k_gemm_tc.cu"]
-# per-file flags: the Baldwin-Lomax switch is discrete, so its products and
-# sums are rounded one by one like the reference's
-FILE_FLAGS = {"k_bl.cu": ["-fmad=false"]}
+# per-file flags: the Baldwin-Lomax switch is discrete, and the mesh set-up
+# must give the reference's geometry bit for bit, so their products and sums
+# are rounded one by one like the reference's
+FILE_FLAGS = {"k_bl.cu": ["-fmad=false"], "k_setup.cu": ["-fmad=false"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

@@ -38,6 +38,29 @@ def test_geometry_all_levels(gpu_lib):
         compare_fields(orc, g, GEOM, mesh=mesh, tol=1e-13)
 
 
+@pytest.mark.parametrize("case", ["cgrid4", "flat_plate", "rans513"])
+def test_device_setup_geometry_bit_identical(gpu_lib, case):
+    """The set-up kernels (node skipping, areas, faces, ghost nodes across
+    block interfaces and physical faces, corners, cell centres) reproduce the
+    oracle's geometry bit for bit on every multigrid level."""
+    from ec2d import cases
+    if case == "cgrid4":
+        p, bl = small_case(nx=129, ny=33, nblocks=4, Num_Mesh=3, Time_Method=1)
+    elif case == "flat_plate":
+        p, bl = cases.laminar_flat_plate(97, 97, num_mesh=3)
+    else:
+        p, bl, _ = cases.rans_naca2412()
+    orc = make_oracle(p, bl)
+    g = make_gpu(p, bl)
+    assert g.num_mesh == orc.num_mesh == 3
+    for mesh in (1, 2, 3):
+        for b in range(1, len(bl) + 1):
+            for f in GEOM:
+                np.testing.assert_array_equal(g.field(1, mesh, b, f), orc.field(mesh, b, f),
+                                              err_msg=f"mesh {mesh} block {b} field {f}")
+    g.close()
+
+
 @pytest.mark.parametrize("flux", [1, 2, 3, 4, 5, 6])
 @pytest.mark.parametrize("recon", [0, 1, 2])
 def test_residual_inviscid(gpu_lib, flux, recon):

@@ -105,8 +105,10 @@ def test_tecplot_restart_sst_keeps_reference_behaviour(gpu_lib, tmp_path):
     a = make_gpu(p, bl)
     a.init_flow()
     fs = a.download_U(1, 1, 1)
-    a.step(15)
-    outputs.write_output(str(tmp_path), a, p, kstep=15)
+    # two steps: on this coarse wall spacing the SST iteration grows omega
+    # without bound within ten steps (the oracle does the same)
+    a.step(2)
+    outputs.write_output(str(tmp_path), a, p, kstep=2)
     Ua = a.download_U(1, 1, 1)
     nx, ny = bl[0].nx, bl[0].ny
     sl = (slice(4, 6), slice(2, nx + 1), slice(2, ny + 1))
