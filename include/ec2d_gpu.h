@@ -95,6 +95,8 @@ const char *ec2d_error_string(int code);
  *   EC2D_LUSGS_ROWS     rows per band, or rows per warp of the one-CTA shape
  *   EC2D_CONCURRENT     0: every kernel on one stream (no concurrent graph
  *                       branches; results are bit-identical either way)
+ *   EC2D_TILE_RESIDUAL  0: the residual as the four-kernel chain (see
+ *                       ec2d_tile_residual)
  *   EC2D_TEST_SILENT_BAND_EDGE  test hook: band edges of the banded wavefront
  *                       send nothing, so the downstream waits run out and the
  *                       next status read returns EC2D_ERR_TIMEOUT */
@@ -132,7 +134,8 @@ int ec2d_num_mesh(ec2d_ctx *ctx, int *num_mesh);
 int ec2d_block_dims(ec2d_ctx *ctx, int case_id, int mesh, int block, int *nx, int *ny, int *nvar);
 
 /* Freestream start including the coarse-to-fine pre-iterations
- * (init_flow_zero, sub_init.f90:423-495) for every case. */
+ * (init_flow_zero, sub_init.f90:423-495) for every case; clears every
+ * case's status word. */
 int ec2d_init_flow(ec2d_ctx *ctx);
 
 /* Copy the conservative field of one block in or out, Fortran layout
@@ -185,6 +188,10 @@ int ec2d_run_to_drop(ec2d_ctx *ctx, double drop, const double *r0, int max_steps
 
 /* Status word of a case: code (0 ok, 3 = T<1e-5) and the block/cell. */
 int ec2d_status(ec2d_ctx *ctx, int case_id, int *code, int *block, int *i, int *j);
+/* Clear the status word of one case (case_id 0: every case), e.g. after the
+ * host replaced a failed case's state with ec2d_upload_U; ec2d_init_flow
+ * clears every case's.  No counterpart in the reference, which stops. */
+int ec2d_clear_status(ec2d_ctx *ctx, int case_id);
 
 /* Lift, drag and moment coefficients (about xaxis, yaxis) from the wall
  * pressure and viscous stress of mesh 1; no counterpart in the reference,
@@ -331,6 +338,17 @@ int ec2d_mlp_predict(ec2d_mlp *m, const float *feat, long long n, float *pred);
  * ec2d_create override it. */
 int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *rows_per_warp, int *concurrent,
                   double *ms_per_step);
+
+/* The residual of a level as one kernel over 2-D tiles of cells whose
+ * primitives and halo sit in shared memory (enable = 1, the default where a
+ * level has no turbulence model and no finite-difference patch and computes
+ * in FP64), or as the chain of four kernels through HBM planes (0); -1 only
+ * reads the setting into *current (may be NULL).  No counterpart in the
+ * reference; both forms evaluate Residual_FVM (sub_Residual.f90:200-472),
+ * comput_Lvc and comput_dt with the same face arithmetic.  ec2d_autotune
+ * picks the faster; EC2D_TILE_RESIDUAL=0 read by ec2d_create starts with the
+ * chain. */
+int ec2d_tile_residual(ec2d_ctx *ctx, int enable, int *current);
 
 /* Precision of the face fluxes (reconstruction, Riemann solver, viscous
  * stress) on the coarse multigrid levels: 64 (the default) or 32.  No

@@ -89,6 +89,13 @@ struct Level {
   int *d_case_tile0 = nullptr, *d_case_ntile = nullptr, *d_case_ncell = nullptr;
   int4 *d_faces = nullptr;
   double *d_face_out = nullptr;
+  // 2-D cell tiles of the one-kernel residual (k_residual_tile): (block, i0,
+  // j0), per-case ranges, norm partials and the last-tile counter
+  int n_rtiles = 0;
+  int4 *d_rtiles = nullptr;
+  int *d_rcase_tile0 = nullptr, *d_rcase_ntile = nullptr;
+  double *d_rnpart = nullptr;
+  unsigned *d_rnctr = nullptr;
   std::vector<std::unique_ptr<DevBuf>> bufs;
 };
 
@@ -127,6 +134,7 @@ struct ec2d_ctx {
   bool silent_band_edge = false;
   int lusgs_rpw = 12;       // most rows per CTA of the banded kernel (<= 16: eight lanes per row), or rows per warp of the one-lane one
   bool coarse_fp32 = false; // face fluxes of multigrid levels >= 2 in FP32
+  bool tile_residual = true; // the one-kernel residual where it applies (no turbulence model, no FDM patch, FP64)
   bool timing = false;
   // one pseudo-time step (single grid or V-cycle) captured as a CUDA graph:
   // the replay stands for graph_launches kernel launches and advances the
@@ -451,6 +459,28 @@ int build_level(ec2d_ctx *ctx, int l) {
   L.case_tile0 = lv.d_case_tile0; L.case_ntile = lv.d_case_ntile; L.case_ncell = lv.d_case_ncell;
   L.nctr = dalloc<unsigned>(lv, 1);  // zeroed; the last CTA of k_res resets it
   if (!L.nctr) return EC2D_ERR_NOMEM;
+  {
+    // 2-D cell tiles of the one-kernel residual, block after block (a case's
+    // tiles are contiguous, so its norm partials are too)
+    std::vector<int4> rt;
+    std::vector<int> rc0(ncase, 0), rcn(ncase, 0);
+    for (int k = 0; k < (int)lv.hb.size(); k++) {
+      const auto &B = lv.hb[k];
+      if (rcn[B.cas] == 0) rc0[B.cas] = (int)rt.size();
+      for (int j0 = 1; j0 <= B.ny - 1; j0 += RES_TILE_Y)
+        for (int i0 = 1; i0 <= B.nx - 1; i0 += RES_TILE_X) { rt.push_back(make_int4(k, i0, j0, 0)); rcn[B.cas]++; }
+    }
+    lv.n_rtiles = (int)rt.size();
+    lv.d_rtiles = dalloc<int4>(lv, rt.size());
+    lv.d_rcase_tile0 = dalloc<int>(lv, ncase);
+    lv.d_rcase_ntile = dalloc<int>(lv, ncase);
+    lv.d_rnpart = dalloc<double>(lv, rt.size() * 12);
+    lv.d_rnctr = dalloc<unsigned>(lv, 1);
+    if (!lv.d_rtiles || !lv.d_rcase_tile0 || !lv.d_rcase_ntile || !lv.d_rnpart || !lv.d_rnctr) return EC2D_ERR_NOMEM;
+    CK(cudaMemcpy(lv.d_rtiles, rt.data(), rt.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(lv.d_rcase_tile0, rc0.data(), ncase * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(lv.d_rcase_ntile, rcn.data(), ncase * sizeof(int), cudaMemcpyHostToDevice));
+  }
   if (!lv.wall_faces.empty()) {
     lv.d_faces = dalloc<int4>(lv, lv.wall_faces.size());
     lv.d_face_out = dalloc<double>(lv, lv.wall_faces.size() * 5);
@@ -563,6 +593,25 @@ void residual(ec2d_ctx *ctx, int l, int post = 0) {
   Level &lv = ctx->lv[l];
   const Lvl &L = lv.L;
   cudaStream_t s = ctx->stream;
+  const bool dual = ctx->P.Time_Method == Time_Dual && l == 1;
+  const bool f32 = ctx->coarse_fp32 && l >= 2;
+  if (ctx->tile_residual && lv.n_rtiles > 0 && L.turb == Turb_NONE && !L.fdm && !dual && !f32) {
+    // the whole residual in one kernel over 2-D tiles (norm partials inside;
+    // with few cases the per-case norms and the multigrid post-steps too)
+    Lvl Lr = L;
+    Lr.npart = lv.d_rnpart;
+    Lr.case_tile0 = lv.d_rcase_tile0;
+    Lr.case_ntile = lv.d_rcase_ntile;
+    Lr.nctr = lv.d_rnctr;
+    const int inpass = norms_fused_final(L) ? post : 0;
+    K(ctx, "k_residual_tile", l, 1, [&] { launch_residual_tile(Lr, lv.d_rtiles, lv.n_rtiles, true, inpass, s); });
+    if (!norms_fused_final(L)) K(ctx, "norms", l, 1, [&] { launch_norms(Lr, false, s); });
+    const int rest = post & ~inpass;
+    if (rest & RES_ADD_FORCE) K(ctx, "k_add_force", l, 1, [&] { launch_add_force(L, s); });
+    if (rest & RES_FORCE_FN) K(ctx, "k_force_fn", l, 1, [&] { launch_force_fn(L, s); });
+    if (rest & RES_SET_UN) K(ctx, "k_set_un", l, 1, [&] { launch_set_un(L, 4, s); });
+    return;
+  }
   K(ctx, "k_prim", l, 1, [&] { launch_prim(L, s); });
   if (L.visc) {
     if (L.turb == Turb_SA) K(ctx, "sa", l, 4, [&] { launch_sa(L, s); });
@@ -574,7 +623,6 @@ void residual(ec2d_ctx *ctx, int l, int post = 0) {
   // kernel timing on they run one after the other
   // face fluxes of a coarse level in FP32 when selected (the coarse levels
   // only smooth the fine-level correction)
-  const bool f32 = ctx->coarse_fp32 && l >= 2;
   if (!ctx->timing && ctx->concurrent) {
     ctx->launches += 2;
     cudaEventRecord(ctx->ev_fork, s);
@@ -587,7 +635,6 @@ void residual(ec2d_ctx *ctx, int l, int post = 0) {
     K(ctx, "k_flux_i", l, 1, [&] { launch_flux_i(L, f32, s); });
     K(ctx, "k_flux_j", l, 1, [&] { launch_flux_j(L, f32, s); });
   }
-  const bool dual = ctx->P.Time_Method == Time_Dual && l == 1;
   const bool fused = !L.fdm && !dual;  // Res final after k_res: norm partials fused into it
   const int inpass = (fused && norms_fused_final(L)) ? post : 0;
   K(ctx, "k_res", l, 1, [&] { launch_res(L, fused, inpass, s); });
@@ -926,6 +973,7 @@ int ec2d_create(int device, ec2d_ctx **out) {
   if (const char *e = getenv("EC2D_LUSGS_ROWS")) c->lusgs_rpw = std::max(8, std::min(32, atoi(e)));
   if (const char *e = getenv("EC2D_TEST_SILENT_BAND_EDGE")) c->silent_band_edge = atoi(e) != 0;
   if (const char *e = getenv("EC2D_CONCURRENT")) c->concurrent = atoi(e) != 0;
+  if (const char *e = getenv("EC2D_TILE_RESIDUAL")) c->tile_residual = atoi(e) != 0;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
@@ -1084,9 +1132,20 @@ int ec2d_block_dims(ec2d_ctx *ctx, int case_id, int mesh, int block, int *nx, in
 }
 
 // init_flow_zero (sub_init.f90:423-495)
+int ec2d_clear_status(ec2d_ctx *ctx, int case_id) {
+  if (!ctx || !ctx->setup_done || (case_id != 0 && !valid_case(ctx, case_id))) return EC2D_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  const int c0 = case_id ? case_id - 1 : 0, nc = case_id ? 1 : (int)ctx->cases.size();
+  for (int l = 1; l <= ctx->num_mesh; l++)
+    CK(cudaMemsetAsync(ctx->lv[l].L.status + 4 * c0, 0, (size_t)4 * nc * sizeof(int), ctx->stream));
+  return EC2D_OK;
+}
+
 int ec2d_init_flow(ec2d_ctx *ctx) {
   if (!ctx || !ctx->setup_done) return EC2D_ERR_ARG;
   cudaSetDevice(ctx->device);
+  int rc = ec2d_clear_status(ctx, 0);  // a fresh start: no case carries a stop
+  if (rc) return rc;
   int nm = ctx->num_mesh;
   if (ctx->nvar >= 5) launch_freestream(ctx->lv[1].L, 0, 1, ctx->stream);
   launch_freestream(ctx->lv[nm].L, 1, 0, ctx->stream);
@@ -1323,6 +1382,30 @@ int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *rows_per_w
   ctx->lusgs_cs = r == EC2D_OK ? best_cs : old_cs;
   ctx->lusgs_rpw = r == EC2D_OK ? best_rpw : old_rpw;
   ctx->concurrent = r == EC2D_OK ? best_cc != 0 : old_cc;
+  // then, with that shape, the one-kernel residual against the four-kernel
+  // chain (where some level can take it)
+  bool tile_applies = false;
+  for (int l = 1; l <= ctx->num_mesh; l++)
+    tile_applies |= ctx->lv[l].L.turb == Turb_NONE && !ctx->lv[l].L.fdm;
+  if (r == EC2D_OK && tile_applies) {
+    const bool old_tile = ctx->tile_residual;
+    double tbest = 1e30;
+    bool tpick = old_tile;
+    for (int tile = 0; tile < 2 && r == EC2D_OK; tile++) {
+      ctx->tile_residual = tile != 0;
+      drop_graph(ctx);
+      if ((r = ec2d_step(ctx, 1)) != EC2D_OK) break;
+      cudaEventRecord(a, ctx->stream);
+      if ((r = ec2d_step(ctx, trial_steps)) != EC2D_OK) break;
+      cudaEventRecord(b, ctx->stream);
+      cudaEventSynchronize(b);
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, a, b);
+      if (ms / trial_steps < tbest) { tbest = ms / trial_steps; tpick = tile != 0; }
+    }
+    ctx->tile_residual = r == EC2D_OK ? tpick : old_tile;
+    if (r == EC2D_OK) best = std::min(best, tbest);
+  }
   drop_graph(ctx);
   cudaMemcpyAsync(lv.L.U, snap, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
   cudaStreamSynchronize(ctx->stream);
@@ -1337,6 +1420,16 @@ int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *rows_per_w
   if (concurrent) *concurrent = ctx->concurrent ? 1 : 0;
   if (ms_per_step) *ms_per_step = best;
   return check_launch(ctx);
+}
+
+int ec2d_tile_residual(ec2d_ctx *ctx, int enable, int *current) {
+  if (!ctx || enable < -1 || enable > 1) return EC2D_ERR_ARG;
+  if (enable >= 0 && (enable != 0) != ctx->tile_residual) {
+    ctx->tile_residual = enable != 0;
+    drop_graph(ctx);
+  }
+  if (current) *current = ctx->tile_residual ? 1 : 0;
+  return EC2D_OK;
 }
 
 int ec2d_set_coarse_precision(ec2d_ctx *ctx, int bits) {

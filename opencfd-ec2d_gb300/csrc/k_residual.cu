@@ -330,6 +330,212 @@ __global__ void __launch_bounds__(TILE) k_res(Lvl L, int post) {
   }
 }
 
+// ---- the residual of a level in one kernel --------------------------------
+// k_residual_tile does the work of k_prim, k_flux_i, k_flux_j and k_res for a
+// 2-D tile of RTX x RTY cells: the primitives (and Sutherland mu) of the tile
+// and its two-cell halo go into shared memory, every i- and j-face of the
+// tile's cells is reconstructed and fluxed from there (the faces on the
+// tile's edges are evaluated by both tiles that share them), and each thread
+// forms its cell's residual, spectral radii, time step and norm partials.
+// Nothing but U, the geometry and the outputs touches HBM, and one launch
+// replaces four.  It serves levels without a turbulence model or a
+// finite-difference patch, in FP64; the face, reconstruction and viscous
+// arithmetic is the same code as the chain's.
+constexpr int RTX = RES_TILE_X, RTY = RES_TILE_Y;  // cells per tile (RTX * RTY = TILE threads)
+constexpr int RGX = RTX + 4, RGY = RTY + 4;        // tile + two halo cells on each side
+constexpr int RGN = RGX * RGY;
+static_assert(RTX * RTY == TILE, "one thread per cell of the tile");
+
+template <bool NORM, bool FINAL>
+__global__ void __launch_bounds__(TILE) k_residual_tile(Lvl L, const int4 *rt, int post) {
+  __shared__ double sd[RGN], su[RGN], sv[RGN], sp[RGN], sT[RGN], sc[RGN], smu[RGN];
+  __shared__ double sU[4][RGN];
+  __shared__ double fi[4][RTY][RTX + 1], fj[4][RTY + 1][RTX];
+  const int4 t4 = rt[blockIdx.x];
+  const int bk = t4.x, i0 = t4.y, j0 = t4.z;
+  const BlkDev &b = L.blk[bk];
+  const CaseDev &c = L.cs[b.cas];
+  const long long F = L.F, P = b.P;
+  const int nx = b.nx, ny = b.ny;
+  const int i1 = min(i0 + RTX - 1, nx - 1), j1 = min(j0 + RTY - 1, ny - 1);  // last cells of the tile
+  auto R = [&](int i, int j) { return (j - j0 + 2) * RGX + (i - i0 + 2); };
+  // (1) primitives over the tile and its halo (comput_duvtpckw + get_viscous,
+  // as k_prim), within the block's extended range -1..nx+1 x -1..ny+1
+  for (int t = threadIdx.x; t < RGN; t += TILE) {
+    const int i = i0 - 2 + t % RGX, j = j0 - 2 + t / RGX;
+    if (i < -1 || i > nx + 1 || j < -1 || j > ny + 1) continue;
+    const long long id = fidx(b, i, j);
+    const double d = L.U[id], ru = L.U[F + id], rv = L.U[2 * F + id], E = L.U[3 * F + id];
+    const double rd = rcp(d);
+    const double uu = ru * rd, v = rv * rd;
+    const double T = (E - 0.5 * d * (uu * uu + v * v)) * (rd * c.rCv);
+    const double pp = c.p00 * d * T;
+    const double st = T > 0.0 ? sqrt_p(T) : sqrt(T);
+    sd[t] = d; su[t] = uu; sv[t] = v; sT[t] = T; sp[t] = pp;
+    sc[t] = st * c.rMa;
+    sU[0][t] = d; sU[1][t] = ru; sU[2][t] = rv; sU[3][t] = E;
+    const bool own = i >= i0 && i <= i1 && j >= j0 && j <= j1;
+    if (own && !(T >= 1.0e-5)) set_status(L.status + 4 * b.cas, 3, bk, i, j);
+    if (L.visc) {
+      const double mu = c.rRe * (1.0 + c.Tsb) * (T * st) * rcp(c.Tsb + T);
+      smu[t] = mu;
+      // Amu over 0..nx x 0..ny as k_prim leaves it: the tile's cells, and the
+      // block's ghost lines next to them when the tile is on the block's edge
+      const bool wi = (i >= i0 && i <= i1) || (i == 0 && i0 == 1) || (i == nx && i1 == nx - 1);
+      const bool wj = (j >= j0 && j <= j1) || (j == 0 && j0 == 1) || (j == ny && j1 == ny - 1);
+      if (wi && wj) { L.amu[id] = mu; L.amut[id] = 0.0; }
+    }
+  }
+  __syncthreads();
+  // (2) faces: i-faces i0..i1+1 of rows j0..j1, j-faces j0..j1+1 of columns i0..i1
+  const int nfi = (i1 - i0 + 2) * (j1 - j0 + 1), nfj = (i1 - i0 + 1) * (j1 - j0 + 2);
+  for (int t = threadIdx.x; t < nfi + nfj; t += TILE) {
+    const bool ifc = t < nfi;
+    int i, j;
+    if (ifc) { i = i0 + t % (i1 - i0 + 2); j = j0 + t / (i1 - i0 + 2); }
+    else { const int u = t - nfi; i = i0 + u % (i1 - i0 + 1); j = j0 + u / (i1 - i0 + 1); }
+    const long long id = fidx(b, i, j);
+    const int r = R(i, j), st = ifc ? 1 : RGX;  // stencil stride in the tile's shared arrays
+    const double s = L.geo[(ifc ? G_SI : G_SJ) * F + id];
+    const double n1 = L.geo[(ifc ? G_NI1 : G_NJ1) * F + id], n2 = L.geo[(ifc ? G_NI2 : G_NJ2) * F + id];
+    double S0[4][4], UL[4], UR[4];
+    int scheme = L.scheme;
+    if (L.recon == Recon_Original) {
+      if (!ifc) scheme = L.gscheme;  // the global Iflag_Scheme in the j direction (sub_Residual.f90:367)
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const int q = r + (k - 2) * st;
+        S0[k][0] = sd[q]; S0[k][1] = su[q]; S0[k][2] = sv[q]; S0[k][3] = sp[q];
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+#pragma unroll
+        for (int m = 0; m < 4; m++) S0[k][m] = sU[m][r + (k - 2) * st];
+    }
+    reconstruct(L.recon, scheme, S0, c.gamma, UL, UR);
+    double QL[4] = {UL[0], UL[1] * n1 + UL[2] * n2, -UL[1] * n2 + UL[2] * n1, UL[3]};
+    double QR[4] = {UR[0], UR[1] * n1 + UR[2] * n2, -UR[1] * n2 + UR[2] * n1, UR[3]};
+    double Fl[4];
+    face_flux(L.flux, QL, QR, Fl, c.gamma, c.ggm1);
+    double F0 = -Fl[0] * s, F1 = -(Fl[1] * n1 - Fl[2] * n2) * s, F2 = -(Fl[1] * n2 + Fl[2] * n1) * s, F3 = -Fl[3] * s;
+    if (L.visc) {
+      const double *g = L.geo + id;
+      double Amu1, Amk1;
+      const int up = r - st;  // the upstream cell of the face
+      const bool lo = ifc ? i == 1 : j == 1, hi = ifc ? i == nx : j == ny;
+      if (lo) {
+        Amu1 = smu[r] + 0.0;
+        Amk1 = c.Cp * (smu[r] * c.rPr + 0.0 * (1.0 / PrT));
+      } else if (hi) {
+        Amu1 = smu[up] + 0.0;
+        Amk1 = c.Cp * (smu[up] * c.rPr + 0.0 * (1.0 / PrT));
+      } else if (ifc) {
+        Amu1 = (smu[up] + smu[r] + 0.0 + 0.0) * 0.5;
+        Amk1 = c.Cp * ((smu[up] + smu[r]) * c.rPr + (0.0 + 0.0) * (1.0 / PrT)) * 0.5;
+      } else {
+        Amu1 = (smu[r] + smu[up] + 0.0 + 0.0) * 0.5;
+        Amk1 = c.Cp * ((smu[up] + smu[r]) * c.rPr + (0.0 + 0.0) * (1.0 / PrT)) * 0.5;
+      }
+      double Diu, Div, DiT, Dju, Djv, DjT, u1, v1;
+      if (ifc) {
+        const int w = r - 1, nN = r + RGX, nS = r - RGX;
+        Diu = su[r] - su[w]; Div = sv[r] - sv[w]; DiT = sT[r] - sT[w];
+        Dju = (su[nN - 1] + su[nN] - su[nS - 1] - su[nS]) * 0.25;
+        Djv = (sv[nN - 1] + sv[nN] - sv[nS - 1] - sv[nS]) * 0.25;
+        DjT = (sT[nN - 1] + sT[nN] - sT[nS - 1] - sT[nS]) * 0.25;
+        u1 = (su[r] + su[w]) * 0.5; v1 = (sv[r] + sv[w]) * 0.5;
+        viscous_face_m(g[G_VIA * F], g[G_VIB * F], g[G_VIC * F], g[G_VID * F], Diu, Div, DiT, Dju, Djv, DjT, Amu1,
+                       Amk1, u1, v1, n1, n2, s, F1, F2, F3);
+      } else {
+        const int sN = r - RGX;
+        Diu = (su[sN + 1] + su[r + 1] - su[sN - 1] - su[r - 1]) * 0.25;
+        Div = (sv[sN + 1] + sv[r + 1] - sv[sN - 1] - sv[r - 1]) * 0.25;
+        DiT = (sT[sN + 1] + sT[r + 1] - sT[sN - 1] - sT[r - 1]) * 0.25;
+        Dju = su[r] - su[sN]; Djv = sv[r] - sv[sN]; DjT = sT[r] - sT[sN];
+        u1 = (su[r] + su[sN]) * 0.5; v1 = (sv[r] + sv[sN]) * 0.5;
+        viscous_face_m(g[G_VJA * F], g[G_VJB * F], g[G_VJC * F], g[G_VJD * F], Diu, Div, DiT, Dju, Djv, DjT, Amu1,
+                       Amk1, u1, v1, n1, n2, s, F1, F2, F3);
+      }
+    }
+    if (ifc) { fi[0][j - j0][i - i0] = F0; fi[1][j - j0][i - i0] = F1; fi[2][j - j0][i - i0] = F2; fi[3][j - j0][i - i0] = F3; }
+    else { fj[0][j - j0][i - i0] = F0; fj[1][j - j0][i - i0] = F1; fj[2][j - j0][i - i0] = F2; fj[3][j - j0][i - i0] = F3; }
+  }
+  __syncthreads();
+  // (3) the cell of this thread: flux differences, radii, time step (k_res)
+  const int tx = threadIdx.x % RTX, ty = threadIdx.x / RTX;
+  const int i = i0 + tx, j = j0 + ty;
+  const bool act = i <= i1 && j <= j1;
+  if (post & RES_SET_UN) {
+    // Un = U over 0..nx x 0..ny: the tile's cells and the ghost lines at
+    // the block's edges next to them
+    for (int t = threadIdx.x; t < RGN; t += TILE) {
+      const int ii = i0 - 2 + t % RGX, jj = j0 - 2 + t / RGX;
+      const bool wi = (ii >= i0 && ii <= i1) || (ii == 0 && i0 == 1) || (ii == nx && i1 == nx - 1);
+      const bool wj = (jj >= j0 && jj <= j1) || (jj == 0 && j0 == 1) || (jj == ny && j1 == ny - 1);
+      if (wi && wj) {
+        const long long id = fidx(b, ii, jj);
+#pragma unroll
+        for (int m = 0; m < 4; m++) L.un[m * F + id] = sU[m][t];
+      }
+    }
+  }
+  double vres[6] = {0, 0, 0, 0, 0, 0};
+  if (act) {
+    const long long id = fidx(b, i, j);
+    const int r = R(i, j);
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      double rr = fi[m][ty][tx + 1] - fi[m][ty][tx] + fj[m][ty + 1][tx] - fj[m][ty][tx];
+      vres[m] = rr;
+      if (post & (RES_ADD_FORCE | RES_FORCE_FN)) {
+        const double qf = L.qf[m * F + id];
+        if (post & RES_FORCE_FN) L.qf[m * F + id] = qf - rr;
+        if (post & RES_ADD_FORCE) rr = rr + qf;
+      }
+      L.res[m * F + id] = rr;
+    }
+    const double *g = L.geo + id;
+    const double s0 = g[G_VOL * F];
+    const double si = g[G_SIA * F], ni1 = g[G_NI1A * F], ni2 = g[G_NI2A * F];
+    const double sj = g[G_SJA * F], nj1 = g[G_NJ1A * F], nj2 = g[G_NJ2A * F];
+    const double uu = su[r], vv = sv[r], cc = sc[r], d = sd[r];
+    const double uni = uu * ni1 + vv * ni2, unj = uu * nj1 + vv * nj2;
+    const double Lci = (fabs(uni) + cc) * si, Lcj = (fabs(unj) + cc) * sj;
+    const double amu = L.visc ? smu[r] : 0.0, amut = 0.0;
+    const double tmp1 = c.gamma * rcp(d) * (amu * c.rPr + amut * (1.0 / PrT));
+    const double Lvi = tmp1 * g[G_VI2 * F], Lvj = tmp1 * g[G_VJ2 * F];
+    L.lc[L_CI * F + id] = Lci;
+    L.lc[L_CJ * F + id] = Lcj;
+    L.lc[L_VI * F + id] = Lvi;
+    L.lc[L_VJ * F + id] = Lvj;
+    double dt;
+    if (c.local_dt == 0) dt = c.dt_global;
+    else {
+      dt = c.CFL * s0 * rcp(Lci + Lcj + 1.0 * (Lvi + Lvj));
+      if (dt > c.dtmax) dt = c.dtmax;
+      if (dt < c.dtmin) dt = c.dtmin;
+    }
+    L.lc[L_DT * F + id] = dt;
+  }
+  if (NORM) {
+    tile_partials(L, act, vres);
+    if (FINAL) {
+      __shared__ int last;
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) last = atomicAdd(L.nctr, 1u) == gridDim.x - 1;
+      __syncthreads();
+      if (last) {
+        __threadfence();
+        const int w = threadIdx.x >> 5;
+        for (int k = w; k < L.ncase * 12; k += TILE / 32) final_norm(L, k / 12, k % 12);
+        if (threadIdx.x == 0) *L.nctr = 0u;
+      }
+    }
+  }
+}
+
 // per-tile partial norms of Res (max |Res| and sum Res^2 per variable)
 __global__ void __launch_bounds__(TILE) k_norm_partial(Lvl L) {
   int bk, i, j;
@@ -414,6 +620,12 @@ void launch_res(const Lvl &L, bool with_norms, int post, cudaStream_t s) {
   if (!with_norms) k_res<false, false><<<L.ntiles, TILE, 0, s>>>(L, post);
   else if (norms_fused_final(L)) k_res<true, true><<<L.ntiles, TILE, 0, s>>>(L, post);
   else k_res<true, false><<<L.ntiles, TILE, 0, s>>>(L, post);
+}
+// Lr: the level with npart, case_tile0, case_ntile and nctr of the 2-D tile list
+void launch_residual_tile(const Lvl &Lr, const int4 *rt, int ntiles, bool with_norms, int post, cudaStream_t s) {
+  if (!with_norms) k_residual_tile<false, false><<<ntiles, TILE, 0, s>>>(Lr, rt, post);
+  else if (norms_fused_final(Lr)) k_residual_tile<true, true><<<ntiles, TILE, 0, s>>>(Lr, rt, post);
+  else k_residual_tile<true, false><<<ntiles, TILE, 0, s>>>(Lr, rt, post);
 }
 void launch_norms(const Lvl &L, bool partials, cudaStream_t s) {
   if (partials) k_norm_partial<<<L.ntiles, TILE, 0, s>>>(L);

@@ -139,6 +139,8 @@ def lib():
         "ec2d_mlp_set_gemm": ([vp, ctypes.c_int], ctypes.c_int),
         "ec2d_measure_fp64_peak": ([dp], ctypes.c_int),
         "ec2d_snapshot": ([vp, ctypes.c_int], ctypes.c_int),
+        "ec2d_tile_residual": ([vp, ctypes.c_int, ip], ctypes.c_int),
+        "ec2d_clear_status": ([vp, ctypes.c_int], ctypes.c_int),
         "ec2d_snapshot_wait": ([vp, ip, ip, dp], ctypes.c_int),
         "ec2d_snapshot_U": ([vp, ctypes.c_int, dp], ctypes.c_int),
         "ec2d_snapshot_amut": ([vp, ctypes.c_int, dp], ctypes.c_int),
@@ -370,6 +372,16 @@ class Solver:
     def set_case_shape(self, case, shape):
         """Per-case shape feature of the warm-start network (the airfoil t/c)."""
         _ck(self.L.ec2d_set_case_shape(self.h, case, float(shape)), "ec2d_set_case_shape")
+
+    def clear_status(self, case=0):
+        """Clear a case's status word (0: every case)."""
+        _ck(self.L.ec2d_clear_status(self.h, case), "ec2d_clear_status")
+
+    def tile_residual(self, enable=-1):
+        """The one-kernel residual on (1) / off (0); -1 reads; returns the setting."""
+        c = ctypes.c_int()
+        _ck(self.L.ec2d_tile_residual(self.h, int(enable), ctypes.byref(c)), "ec2d_tile_residual")
+        return c.value
 
     def set_coarse_precision(self, bits):
         """64 (default) or 32: arithmetic of the coarse multigrid levels' face fluxes."""

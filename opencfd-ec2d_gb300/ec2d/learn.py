@@ -118,13 +118,41 @@ def _rms(s, c):
         return float("nan")
 
 
+def _move(gpu, s, cases, idx, keep_mask, bits):
+    """The cases of context `s` at positions keep_mask (original indices
+    idx[keep_mask]) into a new context: their U, ghosts included, copied
+    exactly, so their iteration continues bit for bit."""
+    keep = idx[keep_mask]
+    Us = [[s.download_U(k + 1, 1, b) for b in range(1, len(cases[c][1]) + 1)]
+          for k, c in enumerate(idx) if keep_mask[k]]
+    s.close()
+    s2 = _solver(gpu, [cases[c] for c in keep], bits)
+    s2.init_flow()
+    for k, c in enumerate(keep):
+        for b, U in enumerate(Us[k], start=1):
+            s2.upload_U(k + 1, 1, b, U)
+    return s2, keep
+
+
 def converge(gpu, cases, start: str, bits: int, r0=None, net=None, targets=(1e-4, 1e-6, 1e-8),
-             max_steps: int = 30000, check: int = 50, max_seconds: float = None) -> Dict:
+             max_steps: int = 30000, check: int = 50, max_seconds: float = None, retire: float = None,
+             compact: float = 0.25, fallback_steps: int = 200, fallback_ratio: float = 100.0) -> Dict:
     """Run all cases of `cases` in one context until every case's
     Res_rms(1) <= min(targets) x r0 or max_steps (r0: each case's
     freestream-start first residual, measured here when not given).
     start: 'freestream' or 'warm' (the network's prediction).  Records per
-    case and target the first step and wall time at which it was reached."""
+    case and target the first step and wall time at which it was reached.
+
+    retire: a drop at which a case is done.  A done case (or one whose
+    residual is no longer finite) has its field read back and its forces
+    taken; once at least `compact` of the context's cases are done, the rest
+    move into a new, smaller context (their state copied exactly), so the
+    time per step follows the cases still iterating.
+
+    A warm start keeps the freestream as the fallback: a case whose residual
+    stops being finite, or exceeds fallback_ratio x its freestream-start
+    residual, within the first fallback_steps steps restarts from the
+    freestream (its state replaced, its status cleared)."""
     ts = time.perf_counter()
     s = _solver(gpu, cases, bits)
     setup_s = time.perf_counter() - ts  # context set-up: grids to the device, geometry
@@ -133,38 +161,74 @@ def converge(gpu, cases, start: str, bits: int, r0=None, net=None, targets=(1e-4
         s.init_flow()
         s.step(1)
         r0 = np.array([_rms(s, c) for c in range(1, n + 1)])
+    r0 = np.asarray(r0)
     s.sync()
     t0 = time.perf_counter()
     fallback = 0
+    free_U = None
     if start == "warm":
+        s.init_flow()
+        free_U = [[s.download_U(c, 1, b) for b in range(1, len(cases[c - 1][1]) + 1)] for c in range(1, n + 1)]
         fallback = net.warm_start(s)
     else:
         s.init_flow()
+    restarted = 0
     t_start = time.perf_counter() - t0
     first = {t: np.full(n, -1) for t in targets}
     when = {t: np.full(n, np.nan) for t in targets}
-    steps = 0
+    forces = np.full((n, 3), np.nan)
+    idx = np.arange(n)  # original index of each case of the current context
+    steps, moves, d2h_s = 0, 0, 0.0
     ratio = np.ones(n)
+    done = np.zeros(n, bool)
+
+    def finish(k_mask):
+        # read the fields of the finishing cases back and take their forces
+        nonlocal d2h_s
+        tdl = time.perf_counter()
+        for k, c in enumerate(idx):
+            if k_mask[k]:
+                for b in range(1, len(cases[c][1]) + 1):
+                    s.download_U(k + 1, 1, b)
+                try:
+                    forces[c] = s.forces(k + 1)
+                except Exception:
+                    pass
+                done[c] = True
+        d2h_s += time.perf_counter() - tdl
+
     while steps < max_steps:
         s.step(check)
         steps += check
-        ratio = np.array([_rms(s, c) for c in range(1, n + 1)]) / r0
+        r = np.array([_rms(s, k) for k in range(1, len(idx) + 1)]) / r0[idx]
+        if free_U is not None and steps <= fallback_steps:
+            bad = ~np.isfinite(r) | (r > fallback_ratio)
+            for k in np.nonzero(bad)[0]:
+                for b, U in enumerate(free_U[idx[k]], start=1):
+                    s.upload_U(int(k) + 1, 1, b, U)
+                s.clear_status(int(k) + 1)
+                r[k] = 1.0
+                restarted += 1
+        ratio[idx] = r
         el = time.perf_counter() - t0
         for t in targets:
-            new = (ratio <= t) & (first[t] < 0)
-            first[t][new] = steps
-            when[t][new] = el
-        if np.all(first[min(targets)] >= 0):
+            new = (r <= t) & (first[t][idx] < 0)
+            first[t][idx[new]] = steps
+            when[t][idx[new]] = el
+        if np.all((first[min(targets)] >= 0) | ~np.isfinite(ratio)):
             break
+        if retire is not None:
+            leave = (r <= retire) | ~np.isfinite(r)
+            if leave.any() and (leave.all() or leave.sum() >= max(1, compact * len(idx))):
+                finish(leave)
+                if leave.all():
+                    break
+                s, idx = _move(gpu, s, cases, idx, ~leave, bits)
+                moves += 1
         if max_seconds is not None and el > max_seconds:
             break
     wall = time.perf_counter() - t0
-    td = time.perf_counter()
-    for c in range(1, n + 1):  # the converged fields back to the host
-        for b in range(1, len(cases[c - 1][1]) + 1):
-            s.download_U(c, 1, b)
-    d2h_s = time.perf_counter() - td
-    forces = np.array([s.forces(c) for c in range(1, n + 1)])
+    finish(~done[idx])  # the cases still in the context
     s.close()
     per = {}
     for t in targets:
@@ -176,7 +240,8 @@ def converge(gpu, cases, start: str, bits: int, r0=None, net=None, targets=(1e-4
                            and int(0.9 * n) >= 1 else None,
                            "steps_per_case": first[t].tolist()}
     return {"start": start, "bits": bits, "cases": n, "steps": steps, "seconds": wall, "start_seconds": t_start,
-            "setup_seconds": setup_s, "download_seconds": d2h_s,
+            "setup_seconds": setup_s, "download_seconds": d2h_s, "context_moves": moves,
+            "restarted_from_freestream": restarted,
             "fallback": fallback, "final_drop_max": float(np.nanmax(ratio)), "targets": per,
             "diverged": int(np.sum(~np.isfinite(ratio))),
             "forces": forces, "r0": r0, "first": first, "when": when}

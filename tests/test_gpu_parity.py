@@ -61,6 +61,65 @@ def test_device_setup_geometry_bit_identical(gpu_lib, case):
     g.close()
 
 
+@pytest.mark.parametrize("kind", ["euler_roe_char", "viscous_ausm_cons", "mg3_flat_plate", "sa_coarse_levels"])
+def test_tile_residual_equals_chain(gpu_lib, monkeypatch, kind):
+    """The one-kernel residual over shared-memory tiles (the default where no
+    turbulence model or FDM patch is on the level) against the four-kernel
+    chain (EC2D_TILE_RESIDUAL=0) on the same state: Res, spectral radii, dt,
+    mu and the norms of one evaluation, then U after a few steps.  Both run
+    the same face arithmetic; measured agreement is to the last bit or
+    within a few ulps of the face-flux scale."""
+    from ec2d import cases
+    if kind == "euler_roe_char":
+        p, bl = small_case(nx=97, ny=33, Ma=0.7, AoA=2.0, Iflag_flux=4, Iflag_Scheme=5, IFlag_Reconstruction=2,
+                           nblocks=2)
+    elif kind == "viscous_ausm_cons":
+        p, bl = small_case(nx=97, ny=33, Ma=0.5, AoA=3.0, Re=5e3, If_viscous=1, Iflag_flux=6, Iflag_Scheme=4,
+                           IFlag_Reconstruction=1, nblocks=2)
+    elif kind == "mg3_flat_plate":
+        p, bl = cases.laminar_flat_plate(97, 97, num_mesh=3)
+    else:  # SA: the fine level keeps the chain, the coarse levels take the tile kernel
+        p, bl = small_case(nx=65, ny=17, Ma=0.6, AoA=2.0, Re=1e6, If_viscous=1, Iflag_turbulence_model=2,
+                           Iflag_flux=4, Iflag_Scheme=5, first=2e-4, Num_Mesh=3, mg_lusgs=1, nblocks=2)
+    orc = make_oracle(p, bl)
+    orc.init_flow()
+    orc.step(3)
+    perturb_state(orc, seed=4)
+    runs = []
+    for tile in ("1", "0"):
+        monkeypatch.setenv("EC2D_TILE_RESIDUAL", tile)
+        g = make_gpu(p, bl)
+        g.init_flow()
+        copy_state(orc, g)
+        g.residual()
+        f = {fid: [g.field(1, 1, b, fid) for b in range(1, len(bl) + 1)] for fid in (0, 1, 2, 3, 4, 5, 7)}
+        nrm = g.norms()[:2]
+        g.step(4)
+        U = [g.download_U(1, 1, b) for b in range(1, len(bl) + 1)]
+        runs.append((f, nrm, U))
+        g.close()
+    (fa, na, Ua), (fb, nb, Ub) = runs
+    for fid in fa:
+        for a, b in zip(fa[fid], fb[fid]):
+            sc = np.abs(b).max()
+            assert np.max(np.abs(a - b)) <= 1e-13 * (sc if sc > 0 else 1.0), (kind, fid)
+    np.testing.assert_allclose(na[1], nb[1], rtol=1e-13)
+    np.testing.assert_allclose(na[0], nb[0], rtol=1e-12)
+    for a, b in zip(Ua, Ub):
+        for m in range(a.shape[0]):
+            assert np.max(np.abs(a[m] - b[m])) <= 1e-12 * np.abs(b[m]).max(), (kind, m)
+    # and the tile path against the oracle, one evaluation at 1e-12 per cell
+    monkeypatch.setenv("EC2D_TILE_RESIDUAL", "1")
+    g = make_gpu(p, bl)
+    g.init_flow()
+    copy_state(orc, g)
+    orc.residual()
+    g.residual()
+    compare_residual(orc, g)
+    compare_fields(orc, g, [1, 2, 3, 4, 5] + ([7] if p.If_viscous else []))
+    g.close()
+
+
 @pytest.mark.parametrize("flux", [1, 2, 3, 4, 5, 6])
 @pytest.mark.parametrize("recon", [0, 1, 2])
 def test_residual_inviscid(gpu_lib, flux, recon):
