@@ -444,17 +444,25 @@ def polar_metric(args, torch, gpu):
       from the freestream (the fallback).
 
     Every run is capped at args.polar_cap seconds; residuals are checked
-    every 25 V-cycles.  For each drop D the comparison uses the cases that
-    reached D in both arms: plain time = the sum of their plain times (one
-    context after the other), batched time = the wall time until the last of
-    them reached D."""
+    every 25 V-cycles.  The batched arms retire a case when it reaches the
+    comparison drop (args.polar_drop) or diverges, and move the others into
+    a smaller context once a quarter of the batch has left.  For each drop D
+    the comparison uses the cases that reached D in both arms: plain time =
+    the sum of their plain times (one context after the other), batched time
+    = the wall time until the last of them reached D."""
     import numpy as np
     from ec2d import cases, learn
     pc = cases.polar_cases(64, with_tc=True)
     cells = sum(fine_cells(bl) for _, bl, _ in pc)
-    targets = (1e-3, 1e-4, 1e-6, 1e-8)
+    # the FP64 batch gives the plain per-case V-cycle counts and runs every
+    # case to the cap (its reached counts show how deep the family gets); the
+    # batched arms retire a case at the comparison drop and move the rest
+    # into a smaller context as cases finish (or diverge)
+    targets = (1e-2, 1e-3, 1e-4, 1e-6, 1e-8)
+    drop = args.polar_drop
+    arm_targets = tuple(t for t in targets if t >= drop)
     out = {"cases": len(pc), "cells": cells, "cap_s": args.polar_cap, "check_every": 25,
-           "targets": [f"{t:.0e}" for t in targets]}
+           "targets": [f"{t:.0e}" for t in targets], "comparison_drop": f"{drop:.0e}"}
     net, learned = None, None
     if args.polar_learned:
         net, learned = learned_leg(args, gpu)
@@ -464,11 +472,12 @@ def polar_metric(args, torch, gpu):
                           max_seconds=args.polar_cap)
     r0 = fp64["r0"]
     arms = {"batched_fp64": fp64,
-            "batched_mixed": learn.converge(gpu, pc, "freestream", 32, r0=r0, targets=targets, max_steps=10 ** 6,
-                                            check=25, max_seconds=args.polar_cap)}
+            "batched_mixed": learn.converge(gpu, pc, "freestream", 32, r0=r0, targets=arm_targets,
+                                            max_steps=10 ** 6, check=25, max_seconds=args.polar_cap, retire=drop)}
     if net is not None:
-        arms["learned_batched_mixed"] = learn.converge(gpu, pc, "warm", 32, r0=r0, net=net, targets=targets,
-                                                       max_steps=10 ** 6, check=25, max_seconds=args.polar_cap)
+        arms["learned_batched_mixed"] = learn.converge(gpu, pc, "warm", 32, r0=r0, net=net, targets=arm_targets,
+                                                       max_steps=10 ** 6, check=25, max_seconds=args.polar_cap,
+                                                       retire=drop)
         net.close()
     plain_ms = plain_step_ms(torch, gpu, pc)
     out["plain_ms_per_vcycle"] = {"median": float(np.median(plain_ms)), "min": float(np.min(plain_ms)),
@@ -479,10 +488,11 @@ def polar_metric(args, torch, gpu):
                      "diverged": r["diverged"], "start_seconds": r["start_seconds"],
                      "setup_seconds": r["setup_seconds"], "download_seconds": r["download_seconds"],
                      "warm_start_fallback_cases": r["fallback"],
-                     "restarted_from_freestream": r["restarted_from_freestream"]}
+                     "restarted_from_freestream": r["restarted_from_freestream"],
+                     "context_moves": r["context_moves"]}
     plain_first = fp64["first"]
     comp = {}
-    for t in targets:
+    for t in arm_targets:
         key = f"{t:.0e}"
         ok_plain = plain_first[t] >= 0
         row = {"plain_reached": int(ok_plain.sum())}
@@ -506,7 +516,7 @@ def polar_metric(args, torch, gpu):
     out["headline"] = None
     for head in ("learned_batched_mixed", "batched_mixed"):
         best = None
-        for t in targets:
+        for t in arm_targets:
             row = comp[f"{t:.0e}"].get(head, {})
             if row.get("common_cases", 0) >= len(pc) // 4:
                 best = {"drop": f"{t:.0e}", "arm": head, **row}
@@ -861,6 +871,8 @@ def main():
     ap.add_argument("--no-polar", dest="polar", action="store_false",
                     help="skip the 64-case polar comparison (learned+batched+mixed vs plain)")
     ap.add_argument("--polar-cap", type=float, default=20.0, help="seconds per polar run")
+    ap.add_argument("--polar-drop", type=float, default=1e-3,
+                    help="the drop the polar comparison is made at (batched cases retire there)")
     ap.add_argument("--no-polar-learned", dest="polar_learned", action="store_false",
                     help="polar comparison without the warm-start network")
     ap.add_argument("--ws-gen-target", type=float, default=1e-6)

@@ -201,9 +201,11 @@ __device__ __forceinline__ double warp_sum(double q) {
 }
 
 // one CTA's partials: per variable the max |Res| and sum Res^2 of its cells
+// (NT threads in the CTA)
+template <int NT = TILE>
 __device__ __forceinline__ void tile_partials(const Lvl &L, bool act, const double *vres) {
-  __shared__ long long smax[6][TILE / 32];
-  __shared__ double ssum[6][TILE / 32];
+  __shared__ long long smax[6][NT / 32];
+  __shared__ double ssum[6][NT / 32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nv = L.nvar;
 #pragma unroll
   for (int m = 0; m < 6; m++) {
@@ -218,7 +220,7 @@ __device__ __forceinline__ void tile_partials(const Lvl &L, bool act, const doub
     long long a = 0;
     double q = 0.0;
     if (m < nv)
-      for (int k = 0; k < TILE / 32; k++) { a = max(a, smax[m][k]); q += ssum[m][k]; }
+      for (int k = 0; k < NT / 32; k++) { a = max(a, smax[m][k]); q += ssum[m][k]; }
     L.npart[(size_t)blockIdx.x * 12 + m] = __longlong_as_double(a);
     L.npart[(size_t)blockIdx.x * 12 + 6 + m] = q;
   }
@@ -341,13 +343,17 @@ __global__ void __launch_bounds__(TILE) k_res(Lvl L, int post) {
 // replaces four.  It serves levels without a turbulence model or a
 // finite-difference patch, in FP64; the face, reconstruction and viscous
 // arithmetic is the same code as the chain's.
-constexpr int RTX = RES_TILE_X, RTY = RES_TILE_Y;  // cells per tile (RTX * RTY = TILE threads)
+constexpr int RTX = RES_TILE_X, RTY = RES_TILE_Y;  // cells per tile
 constexpr int RGX = RTX + 4, RGY = RTY + 4;        // tile + two halo cells on each side
 constexpr int RGN = RGX * RGY;
-static_assert(RTX * RTY == TILE, "one thread per cell of the tile");
+constexpr int RNT = RES_TILE_THREADS;
+// one thread per face of the tile, per halo cell and per cell: every FP64
+// chain of a phase runs side by side (on the small multigrid levels the
+// kernel is as long as one thread's chain)
+static_assert((RTX + 1) * RTY + RTX * (RTY + 1) <= RNT && RGN <= RNT && RTX * RTY <= RNT, "a thread per item");
 
 template <bool NORM, bool FINAL>
-__global__ void __launch_bounds__(TILE) k_residual_tile(Lvl L, const int4 *rt, int post) {
+__global__ void __launch_bounds__(RNT) k_residual_tile(Lvl L, const int4 *rt, int post) {
   __shared__ double sd[RGN], su[RGN], sv[RGN], sp[RGN], sT[RGN], sc[RGN], smu[RGN];
   __shared__ double sU[4][RGN];
   __shared__ double fi[4][RTY][RTX + 1], fj[4][RTY + 1][RTX];
@@ -361,7 +367,7 @@ __global__ void __launch_bounds__(TILE) k_residual_tile(Lvl L, const int4 *rt, i
   auto R = [&](int i, int j) { return (j - j0 + 2) * RGX + (i - i0 + 2); };
   // (1) primitives over the tile and its halo (comput_duvtpckw + get_viscous,
   // as k_prim), within the block's extended range -1..nx+1 x -1..ny+1
-  for (int t = threadIdx.x; t < RGN; t += TILE) {
+  for (int t = threadIdx.x; t < RGN; t += RNT) {
     const int i = i0 - 2 + t % RGX, j = j0 - 2 + t / RGX;
     if (i < -1 || i > nx + 1 || j < -1 || j > ny + 1) continue;
     const long long id = fidx(b, i, j);
@@ -389,7 +395,7 @@ __global__ void __launch_bounds__(TILE) k_residual_tile(Lvl L, const int4 *rt, i
   __syncthreads();
   // (2) faces: i-faces i0..i1+1 of rows j0..j1, j-faces j0..j1+1 of columns i0..i1
   const int nfi = (i1 - i0 + 2) * (j1 - j0 + 1), nfj = (i1 - i0 + 1) * (j1 - j0 + 2);
-  for (int t = threadIdx.x; t < nfi + nfj; t += TILE) {
+  for (int t = threadIdx.x; t < nfi + nfj; t += RNT) {
     const bool ifc = t < nfi;
     int i, j;
     if (ifc) { i = i0 + t % (i1 - i0 + 2); j = j0 + t / (i1 - i0 + 2); }
@@ -465,11 +471,11 @@ __global__ void __launch_bounds__(TILE) k_residual_tile(Lvl L, const int4 *rt, i
   // (3) the cell of this thread: flux differences, radii, time step (k_res)
   const int tx = threadIdx.x % RTX, ty = threadIdx.x / RTX;
   const int i = i0 + tx, j = j0 + ty;
-  const bool act = i <= i1 && j <= j1;
+  const bool act = threadIdx.x < RTX * RTY && i <= i1 && j <= j1;
   if (post & RES_SET_UN) {
     // Un = U over 0..nx x 0..ny: the tile's cells and the ghost lines at
     // the block's edges next to them
-    for (int t = threadIdx.x; t < RGN; t += TILE) {
+    for (int t = threadIdx.x; t < RGN; t += RNT) {
       const int ii = i0 - 2 + t % RGX, jj = j0 - 2 + t / RGX;
       const bool wi = (ii >= i0 && ii <= i1) || (ii == 0 && i0 == 1) || (ii == nx && i1 == nx - 1);
       const bool wj = (jj >= j0 && jj <= j1) || (jj == 0 && j0 == 1) || (jj == ny && j1 == ny - 1);
@@ -519,7 +525,7 @@ __global__ void __launch_bounds__(TILE) k_residual_tile(Lvl L, const int4 *rt, i
     L.lc[L_DT * F + id] = dt;
   }
   if (NORM) {
-    tile_partials(L, act, vres);
+    tile_partials<RNT>(L, act, vres);
     if (FINAL) {
       __shared__ int last;
       __threadfence();
@@ -529,7 +535,7 @@ __global__ void __launch_bounds__(TILE) k_residual_tile(Lvl L, const int4 *rt, i
       if (last) {
         __threadfence();
         const int w = threadIdx.x >> 5;
-        for (int k = w; k < L.ncase * 12; k += TILE / 32) final_norm(L, k / 12, k % 12);
+        for (int k = w; k < L.ncase * 12; k += RNT / 32) final_norm(L, k / 12, k % 12);
         if (threadIdx.x == 0) *L.nctr = 0u;
       }
     }
@@ -623,9 +629,9 @@ void launch_res(const Lvl &L, bool with_norms, int post, cudaStream_t s) {
 }
 // Lr: the level with npart, case_tile0, case_ntile and nctr of the 2-D tile list
 void launch_residual_tile(const Lvl &Lr, const int4 *rt, int ntiles, bool with_norms, int post, cudaStream_t s) {
-  if (!with_norms) k_residual_tile<false, false><<<ntiles, TILE, 0, s>>>(Lr, rt, post);
-  else if (norms_fused_final(Lr)) k_residual_tile<true, true><<<ntiles, TILE, 0, s>>>(Lr, rt, post);
-  else k_residual_tile<true, false><<<ntiles, TILE, 0, s>>>(Lr, rt, post);
+  if (!with_norms) k_residual_tile<false, false><<<ntiles, RNT, 0, s>>>(Lr, rt, post);
+  else if (norms_fused_final(Lr)) k_residual_tile<true, true><<<ntiles, RNT, 0, s>>>(Lr, rt, post);
+  else k_residual_tile<true, false><<<ntiles, RNT, 0, s>>>(Lr, rt, post);
 }
 void launch_norms(const Lvl &L, bool partials, cudaStream_t s) {
   if (partials) k_norm_partial<<<L.ntiles, TILE, 0, s>>>(L);
