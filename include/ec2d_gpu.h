@@ -95,8 +95,8 @@ const char *ec2d_error_string(int code);
  *   EC2D_LUSGS_ROWS     rows per band, or rows per warp of the one-CTA shape
  *   EC2D_CONCURRENT     0: every kernel on one stream (no concurrent graph
  *                       branches; results are bit-identical either way)
- *   EC2D_TILE_RESIDUAL  0: the residual as the four-kernel chain (see
- *                       ec2d_tile_residual)
+ *   EC2D_TILE_RESIDUAL  1: the residual as one kernel over shared-memory
+ *                       tiles (see ec2d_tile_residual)
  *   EC2D_TEST_SILENT_BAND_EDGE  test hook: band edges of the banded wavefront
  *                       send nothing, so the downstream waits run out and the
  *                       next status read returns EC2D_ERR_TIMEOUT */
@@ -340,14 +340,14 @@ int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *rows_per_w
                   double *ms_per_step);
 
 /* The residual of a level as one kernel over 2-D tiles of cells whose
- * primitives and halo sit in shared memory (enable = 1, the default where a
- * level has no turbulence model and no finite-difference patch and computes
- * in FP64), or as the chain of four kernels through HBM planes (0); -1 only
- * reads the setting into *current (may be NULL).  No counterpart in the
+ * primitives and halo sit in shared memory (enable = 1; used on levels with
+ * no turbulence model and no finite-difference patch that compute in FP64),
+ * or as the chain of four kernels through HBM planes (0, the default); -1
+ * only reads the setting into *current (may be NULL).  No counterpart in the
  * reference; both forms evaluate Residual_FVM (sub_Residual.f90:200-472),
  * comput_Lvc and comput_dt with the same face arithmetic.  ec2d_autotune
- * picks the faster; EC2D_TILE_RESIDUAL=0 read by ec2d_create starts with the
- * chain. */
+ * picks the faster; EC2D_TILE_RESIDUAL=1 read by ec2d_create starts with the
+ * one-kernel form. */
 int ec2d_tile_residual(ec2d_ctx *ctx, int enable, int *current);
 
 /* Precision of the face fluxes (reconstruction, Riemann solver, viscous

@@ -134,7 +134,7 @@ struct ec2d_ctx {
   bool silent_band_edge = false;
   int lusgs_rpw = 12;       // most rows per CTA of the banded kernel (<= 16: eight lanes per row), or rows per warp of the one-lane one
   bool coarse_fp32 = false; // face fluxes of multigrid levels >= 2 in FP32
-  bool tile_residual = true; // the one-kernel residual where it applies (no turbulence model, no FDM patch, FP64)
+  bool tile_residual = false; // the one-kernel residual where it applies (no turbulence model, no FDM patch, FP64)
   bool timing = false;
   // one pseudo-time step (single grid or V-cycle) captured as a CUDA graph:
   // the replay stands for graph_launches kernel launches and advances the

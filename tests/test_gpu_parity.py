@@ -63,12 +63,12 @@ def test_device_setup_geometry_bit_identical(gpu_lib, case):
 
 @pytest.mark.parametrize("kind", ["euler_roe_char", "viscous_ausm_cons", "mg3_flat_plate", "sa_coarse_levels"])
 def test_tile_residual_equals_chain(gpu_lib, monkeypatch, kind):
-    """The one-kernel residual over shared-memory tiles (the default where no
-    turbulence model or FDM patch is on the level) against the four-kernel
-    chain (EC2D_TILE_RESIDUAL=0) on the same state: Res, spectral radii, dt,
-    mu and the norms of one evaluation, then U after a few steps.  Both run
-    the same face arithmetic; measured agreement is to the last bit or
-    within a few ulps of the face-flux scale."""
+    """The one-kernel residual over shared-memory tiles (EC2D_TILE_RESIDUAL=1,
+    used where no turbulence model or FDM patch is on the level) against the
+    four-kernel chain (0, the default) on the same state: Res, spectral radii,
+    dt, mu and the norms of one evaluation, then U after a few steps.  Both
+    run the same face arithmetic; the agreement asked is 1e-13 of each
+    field's scale."""
     from ec2d import cases
     if kind == "euler_roe_char":
         p, bl = small_case(nx=97, ny=33, Ma=0.7, AoA=2.0, Iflag_flux=4, Iflag_Scheme=5, IFlag_Reconstruction=2,
