@@ -656,8 +656,10 @@ def run_gb300(args, rank, world):
         # per row up to 16 rows, four above; 1: one CTA per block, `rows` rows
         # per warp; >1: a cluster of that many CTAs with a barrier per plane
         cs, rpw, cc, ms = t
-        kind = "one-lane" if cs != 0 else ("eight-lane bands" if rpw <= 16 else "four-lane bands")
-        return {"lusgs_kernel": kind, "lusgs_ctas": cs, "rows": rpw, "concurrent_faces": cc, "ms": ms,
+        lanes = g.lusgs_shape()[2]
+        kind = "one-lane" if cs != 0 else ("eight-lane bands" if lanes == 8 else "four-lane bands")
+        return {"lusgs_kernel": kind, "lusgs_ctas": cs, "rows": rpw, "lanes": lanes if cs == 0 else 1,
+                "concurrent_faces": cc, "ms": ms,
                 "residual": "one kernel over shared-memory tiles" if g.tile_residual() else "four-kernel chain"}
 
     tuned = {"fp64": shape(tune())}

@@ -93,6 +93,7 @@ const char *ec2d_error_string(int code);
  * otherwise make (none changes the arithmetic of a kernel):
  *   EC2D_LUSGS_CLUSTER  FP64 wavefront shape (see ec2d_autotune's lusgs_cs)
  *   EC2D_LUSGS_ROWS     rows per band, or rows per warp of the one-CTA shape
+ *   EC2D_LUSGS_LANES    lanes per row of the banded shape (4 or 8)
  *   EC2D_CONCURRENT     0: every kernel on one stream (no concurrent graph
  *                       branches; results are bit-identical either way)
  *   EC2D_TILE_RESIDUAL  1: the residual as one kernel over shared-memory
@@ -338,6 +339,12 @@ int ec2d_mlp_predict(ec2d_mlp *m, const float *feat, long long n, float *pred);
  * ec2d_create override it. */
 int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *rows_per_warp, int *concurrent,
                   double *ms_per_step);
+/* The FP64 wavefront's shape in use: lusgs_cs and rows as above, and the
+ * lanes per row of the banded kernel (8 or 4; the autotuner also tries bands
+ * of 6 and 8 rows with either, on clusters of up to 16 CTAs, and
+ * EC2D_LUSGS_LANES read by ec2d_create fixes the lanes).  No counterpart in
+ * the reference. */
+int ec2d_lusgs_shape(ec2d_ctx *ctx, int *lusgs_cs, int *rows, int *lanes);
 
 /* The residual of a level as one kernel over 2-D tiles of cells whose
  * primitives and halo sit in shared memory (enable = 1; used on levels with

@@ -133,6 +133,7 @@ struct ec2d_ctx {
   // EC2D_ERR_TIMEOUT; failure detection is tested without a GPU fault
   bool silent_band_edge = false;
   int lusgs_rpw = 12;       // most rows per CTA of the banded kernel (<= 16: eight lanes per row), or rows per warp of the one-lane one
+  int lusgs_lanes = 0;      // lanes per row of the banded kernel: 4 or 8, 0 by the rows (eight up to 16)
   bool coarse_fp32 = false; // face fluxes of multigrid levels >= 2 in FP32
   bool tile_residual = false; // the one-kernel residual where it applies (no turbulence model, no FDM patch, FP64)
   bool timing = false;
@@ -696,7 +697,8 @@ void lusgs_update(ec2d_ctx *ctx, int l, double alfa1, bool force = false) {
     K(ctx, "k_lusgs32", l, 3, [&] { launch_lusgs_fast32(L, alfa1, mode, lv.max_rows, ctx->stream); });
   } else if (lv.fast64) {
     auto go = [&](int part) {
-      launch_lusgs_fast(L, alfa1, mode | part, lv.max_rows, lv.max_cols, ctx->lusgs_cs, ctx->lusgs_rpw, ctx->stream);
+      launch_lusgs_fast(L, alfa1, mode | part, lv.max_rows, lv.max_cols, ctx->lusgs_cs, ctx->lusgs_rpw,
+                        ctx->lusgs_lanes, ctx->stream);
     };
     if (ctx->timing) {  // the record builder and the sweep timed apart (together: the k_lusgs stage)
       K(ctx, "k_lusgs_prep", l, 1, [&] { go(LUSGS_PREP_ONLY); });
@@ -970,7 +972,11 @@ int ec2d_create(int device, ec2d_ctx **out) {
   ec2d_ctx *c = new ec2d_ctx();
   c->device = device;
   if (const char *e = getenv("EC2D_LUSGS_CLUSTER")) c->lusgs_cs = std::max(0, std::min(8, atoi(e)));
-  if (const char *e = getenv("EC2D_LUSGS_ROWS")) c->lusgs_rpw = std::max(8, std::min(32, atoi(e)));
+  if (const char *e = getenv("EC2D_LUSGS_ROWS")) c->lusgs_rpw = std::max(4, std::min(32, atoi(e)));
+  if (const char *e = getenv("EC2D_LUSGS_LANES")) {
+    const int v = atoi(e);
+    c->lusgs_lanes = (v == 4 || v == 8) ? v : 0;
+  }
   if (const char *e = getenv("EC2D_TEST_SILENT_BAND_EDGE")) c->silent_band_edge = atoi(e) != 0;
   if (const char *e = getenv("EC2D_CONCURRENT")) c->concurrent = atoi(e) != 0;
   if (const char *e = getenv("EC2D_TILE_RESIDUAL")) c->tile_residual = atoi(e) != 0;
@@ -1348,20 +1354,23 @@ int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *rows_per_w
   // eight lanes per row or of 24 or 32 rows with four (where they fit), one
   // CTA per block with 32, 24 or 16 rows per warp, or a cluster of 2, 4, 8
   // CTAs (the FP32 sweep has one shape) -- x concurrent face kernels
-  std::vector<std::pair<int, int>> shapes = {{0, 12}};
+  // (cs, rows, lanes); bands of 6 or 8 rows need 12-16 CTAs per cluster
+  // (non-portable sizes, used where the device places them)
+  std::vector<std::array<int, 3>> shapes = {{0, 12, 0}};
   if (!ctx->lusgs_fp32 && ctx->P.Time_Method == Time_LU_SGS)
-    for (auto sh : {std::make_pair(0, 16), std::make_pair(0, 24), std::make_pair(0, 32), std::make_pair(1, 32),
-                    std::make_pair(1, 24),
-                    std::make_pair(1, 16), std::make_pair(2, 32), std::make_pair(4, 32), std::make_pair(8, 32)})
+    for (auto sh : std::vector<std::array<int, 3>>{{0, 16, 0}, {0, 24, 0}, {0, 32, 0}, {0, 8, 8}, {0, 8, 4},
+                                                   {0, 6, 8}, {0, 6, 4}, {1, 32, 0}, {1, 24, 0}, {1, 16, 0},
+                                                   {2, 32, 0}, {4, 32, 0}, {8, 32, 0}})
       shapes.push_back(sh);
-  const int old_cs = ctx->lusgs_cs, old_rpw = ctx->lusgs_rpw;
+  const int old_cs = ctx->lusgs_cs, old_rpw = ctx->lusgs_rpw, old_lanes = ctx->lusgs_lanes;
   const bool old_cc = ctx->concurrent;
   double best = 1e30;
-  int best_cs = old_cs, best_rpw = old_rpw, best_cc = old_cc ? 1 : 0, r = EC2D_OK;
+  int best_cs = old_cs, best_rpw = old_rpw, best_lanes = old_lanes, best_cc = old_cc ? 1 : 0, r = EC2D_OK;
   for (auto sh : shapes) {
     for (int cc = 0; cc < 2 && r == EC2D_OK; cc++) {
-      ctx->lusgs_cs = sh.first;
-      ctx->lusgs_rpw = sh.second;
+      ctx->lusgs_cs = sh[0];
+      ctx->lusgs_rpw = sh[1];
+      ctx->lusgs_lanes = sh[2];
       ctx->concurrent = cc != 0;
       drop_graph(ctx);
       if ((r = ec2d_step(ctx, 1)) != EC2D_OK) break;
@@ -1373,14 +1382,16 @@ int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *rows_per_w
       cudaEventElapsedTime(&ms, a, b);
       if (ms / trial_steps < best) {
         best = ms / trial_steps;
-        best_cs = sh.first;
-        best_rpw = sh.second;
+        best_cs = sh[0];
+        best_rpw = sh[1];
+        best_lanes = sh[2];
         best_cc = cc;
       }
     }
   }
   ctx->lusgs_cs = r == EC2D_OK ? best_cs : old_cs;
   ctx->lusgs_rpw = r == EC2D_OK ? best_rpw : old_rpw;
+  ctx->lusgs_lanes = r == EC2D_OK ? best_lanes : old_lanes;
   ctx->concurrent = r == EC2D_OK ? best_cc != 0 : old_cc;
   // then, with that shape, the one-kernel residual against the four-kernel
   // chain (where some level can take it)
@@ -1420,6 +1431,14 @@ int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *rows_per_w
   if (concurrent) *concurrent = ctx->concurrent ? 1 : 0;
   if (ms_per_step) *ms_per_step = best;
   return check_launch(ctx);
+}
+
+int ec2d_lusgs_shape(ec2d_ctx *ctx, int *cs, int *rows, int *lanes) {
+  if (!ctx) return EC2D_ERR_ARG;
+  if (cs) *cs = ctx->lusgs_cs;
+  if (rows) *rows = ctx->lusgs_rpw;
+  if (lanes) *lanes = ctx->lusgs_lanes ? ctx->lusgs_lanes : (ctx->lusgs_rpw <= 16 ? 8 : 4);
+  return EC2D_OK;
 }
 
 int ec2d_tile_residual(ec2d_ctx *ctx, int enable, int *current) {
@@ -1662,7 +1681,9 @@ int ec2d_du_lusgs(ec2d_ctx *ctx, int mesh, double alfa1) {
   const Level &lv = ctx->lv[mesh];
   const Lvl &L = lv.L;
   if (ctx->lusgs_fp32 && lv.fast32) launch_lusgs_fast32(L, alfa1, 0, lv.max_rows, ctx->stream);
-  else if (lv.fast64) launch_lusgs_fast(L, alfa1, 0, lv.max_rows, lv.max_cols, ctx->lusgs_cs, ctx->lusgs_rpw, ctx->stream);
+  else if (lv.fast64)
+    launch_lusgs_fast(L, alfa1, 0, lv.max_rows, lv.max_cols, ctx->lusgs_cs, ctx->lusgs_rpw, ctx->lusgs_lanes,
+                      ctx->stream);
   else launch_lusgs(L, alfa1, ctx->stream);
   return check_launch(ctx);
 }

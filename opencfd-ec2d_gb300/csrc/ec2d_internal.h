@@ -42,14 +42,15 @@ int lusgs_planes(int nv);
 // PREP_ONLY / SWEEP_ONLY launch one of the two kernels of the FP64 wavefront
 // (record builder, sweep), so that per-kernel timing can bracket each
 enum { LUSGS_UPDATE = 1, LUSGS_FORCE = 2, LUSGS_PREP_ONLY = 4, LUSGS_SWEEP_ONLY = 8 };
-// cs: 0 the four-lanes-per-row kernel where it fits, with at most rpw rows
-// per CTA (else one CTA per block), 1 one CTA per block with rpw rows per
-// warp, 2..8 a cluster of cs CTAs with a barrier per plane
 // mesh set-up (k_setup.cu): with finer != nullptr the level's nodes by node
 // skipping first, then areas, faces, ghost nodes, cell centres and (fdm) the
 // finite-difference metrics
 void launch_setup_geometry(const Lvl &L, const Lvl *finer, bool fdm, cudaStream_t s);
-void launch_lusgs_fast(const Lvl &L, double alfa1, int mode, int max_rows, int max_cols, int cs, int rpw,
+// cs: 0 the banded multi-lane kernel where it fits, with at most rpw rows per
+// CTA and `lanes` lanes per row (4 or 8; 0: eight up to 16 rows, four above),
+// else one CTA per block; 1 one CTA per block with rpw rows per warp; 2..8 a
+// cluster of cs CTAs with a barrier per plane
+void launch_lusgs_fast(const Lvl &L, double alfa1, int mode, int max_rows, int max_cols, int cs, int rpw, int lanes,
                        cudaStream_t s);
 size_t lusgs_smem(int nv, int rows);  // dynamic shared memory of the one-CTA FP64 sweep
 void launch_lusgs_fast32(const Lvl &L, double alfa1, int mode, int max_rows, cudaStream_t s);

@@ -841,50 +841,91 @@ __global__ void __launch_bounds__(4 * QROWS, 1) k_lusgs_sweep_quad(Lvl L, int R,
 }
 
 // the four- and eight-lane kernel serves NV = 4 levels whose blocks have at
-// most 8 bands of rows and QCOLS cells per row, when every CTA of the launch
+// most 16 bands of rows and QCOLS cells per row, when every CTA of the launch
 // gets an SM of its own (with fewer SMs, one lane per row needs fewer FP64
-// instructions)
-// rmax: most rows per CTA (16, 24 or 32: four, three or two warps share an
-// SM's FP64 unit)
+// instructions) and the device can hold one of its clusters
+// rmax: most rows per CTA (4..32); lanes: lanes per row (4 or 8; 0: eight up
+// to 16 rows, four above).  Clusters of more than 8 CTAs are non-portable
+// sizes, asked for explicitly.
 int quad_ctas(int max_rows, int rmax) {
-  rmax = std::max(8, std::min(rmax, QROWS));
+  rmax = std::max(4, std::min(rmax, QROWS));
   return (max_rows + rmax - 1) / rmax;
 }
-bool quad_fits(const Lvl &L, int max_rows, int max_cols, int rmax) {
+static int quad_lanes(int rmax, int lanes) { return lanes == 4 || lanes == 8 ? lanes : (rmax <= 16 ? 8 : 4); }
+static void (*quad_kernel(int lpr, int update))(Lvl, int, int) {
+  return lpr == 8 ? (update ? k_lusgs_sweep_quad<true, 8> : k_lusgs_sweep_quad<false, 8>)
+                  : (update ? k_lusgs_sweep_quad<true, 4> : k_lusgs_sweep_quad<false, 4>);
+}
+struct QuadShape {
+  int CS, R, lpr, th;
+  size_t smem;
+};
+static QuadShape quad_shape(int max_rows, int max_cols, int rmax, int lanes) {
+  QuadShape q;
+  q.CS = quad_ctas(max_rows, rmax);
+  q.R = (max_rows + q.CS - 1) / q.CS;
+  q.lpr = quad_lanes(rmax, lanes);
+  q.th = (q.lpr * q.R + 31) / 32 * 32;
+  q.smem = (size_t)2 * q.R * 8 * sizeof(double) + (q.CS > 1 ? (size_t)max_cols * 2 * (8 * sizeof(double) + 8) : 0);
+  return q;
+}
+// the kernel's attributes for a launch of this shape (dynamic shared memory
+// beyond 48 KiB, cluster sizes beyond 8)
+static void quad_attributes(const QuadShape &q) {
+  for (int update = 0; update < 2; update++) {
+    auto kern = quad_kernel(q.lpr, update);
+    if (q.smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)q.smem);
+    if (q.CS > 8) cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  }
+}
+bool quad_fits(const Lvl &L, int max_rows, int max_cols, int rmax, int lanes) {
   static int nsm = 0;
   if (!nsm) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   }
-  const int CS = quad_ctas(max_rows, rmax);
-  return L.nvar == 4 && max_rows >= 1 && CS <= 8 && max_cols <= QCOLS && L.nblk * CS <= nsm;
-}
-
-// at most 16 rows per CTA: eight lanes per row (15 FP64 operations per cell
-// and lane instead of 18, in up to four warps); more: four lanes per row
-void launch_quad(const Lvl &L, int update, int max_rows, int max_cols, int rmax, cudaStream_t s) {
-  const int CS = quad_ctas(max_rows, rmax);
-  const int R = (max_rows + CS - 1) / CS;
-  const int lpr = rmax <= 16 ? 8 : 4;
-  const int th = (lpr * R + 31) / 32 * 32;
-  const size_t smem = (size_t)2 * R * 8 * sizeof(double) + (CS > 1 ? (size_t)max_cols * 2 * (8 * sizeof(double) + 8) : 0);
-  auto kern = lpr == 8 ? (update ? k_lusgs_sweep_quad<true, 8> : k_lusgs_sweep_quad<false, 8>)
-                       : (update ? k_lusgs_sweep_quad<true, 4> : k_lusgs_sweep_quad<false, 4>);
-  if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const QuadShape q = quad_shape(max_rows, max_cols, rmax, lanes);
+  if (!(L.nvar == 4 && max_rows >= 1 && q.CS <= 16 && max_cols <= QCOLS && L.nblk * q.CS <= nsm)) return false;
+  if (q.CS <= 8) return true;
+  // a non-portable cluster size: launchable only if the device can place one
+  quad_attributes(q);
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(L.nblk * CS);
-  cfg.blockDim = dim3(th);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
+  cfg.gridDim = dim3(L.nblk * q.CS);
+  cfg.blockDim = dim3(q.th);
+  cfg.dynamicSmemBytes = q.smem;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = CS;
+  attr[0].val.clusterDim.x = q.CS;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, kern, L, R, CS);
+  int nclusters = 0;
+  const bool ok = cudaOccupancyMaxActiveClusters(&nclusters, quad_kernel(q.lpr, 1), &cfg) == cudaSuccess &&
+                  nclusters >= 1;
+  cudaGetLastError();  // a refused query leaves no error behind
+  return ok;
+}
+
+// eight lanes per row: 15 FP64 operations per cell and lane; four: 18
+void launch_quad(const Lvl &L, int update, int max_rows, int max_cols, int rmax, int lanes, cudaStream_t s) {
+  const QuadShape q = quad_shape(max_rows, max_cols, rmax, lanes);
+  quad_attributes(q);
+  auto kern = quad_kernel(q.lpr, update);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(L.nblk * q.CS);
+  cfg.blockDim = dim3(q.th);
+  cfg.dynamicSmemBytes = q.smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = q.CS;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, L, q.R, q.CS);
 }
 
 // CS == 1: one CTA per block, planes separated by __syncthreads.
@@ -924,17 +965,20 @@ size_t smem_bytes(int R, int th) {
 }
 
 template <int NV>
-void sweep_nv(const Lvl &L, double alfa1, int mode, int max_rows, int max_cols, int cs, int rpw, cudaStream_t s) {
+void sweep_nv(const Lvl &L, double alfa1, int mode, int max_rows, int max_cols, int cs, int rpw, int lanes,
+              cudaStream_t s) {
   if (!(mode & LUSGS_SWEEP_ONLY)) k_lusgs_prep<NV><<<L.ntiles, TILE, 0, s>>>(L, alfa1, mode & LUSGS_FORCE);
   if (mode & LUSGS_PREP_ONLY) return;
   const int update = mode & LUSGS_UPDATE;
   if (cs == 0) {
-    // the requested band height, else four-lane bands of 24 or 32 rows
-    for (int r : {rpw, 24, 32})
-      if (quad_fits(L, max_rows, max_cols, r)) {
-        launch_quad(L, update, max_rows, max_cols, r, s);
+    // the requested band height and lanes, else four-lane bands of 24 or 32 rows
+    for (int r : {rpw, 24, 32}) {
+      const int ln = r == rpw ? lanes : 0;
+      if (quad_fits(L, max_rows, max_cols, r, ln)) {
+        launch_quad(L, update, max_rows, max_cols, r, ln, s);
         return;
       }
+    }
     cs = 1;  // one CTA per block, full warps
     rpw = 32;
   }
@@ -977,11 +1021,11 @@ size_t smem_nv(int rows) {
 }
 size_t lusgs_smem(int nv, int rows) { return nv == 4 ? smem_nv<4>(rows) : nv == 5 ? smem_nv<5>(rows) : smem_nv<6>(rows); }
 
-void launch_lusgs_fast(const Lvl &L, double alfa1, int mode, int max_rows, int max_cols, int cs, int rpw,
+void launch_lusgs_fast(const Lvl &L, double alfa1, int mode, int max_rows, int max_cols, int cs, int rpw, int lanes,
                        cudaStream_t s) {
-  if (L.nvar == 4) sweep_nv<4>(L, alfa1, mode, max_rows, max_cols, cs, rpw, s);
-  else if (L.nvar == 5) sweep_nv<5>(L, alfa1, mode, max_rows, max_cols, cs, rpw, s);
-  else sweep_nv<6>(L, alfa1, mode, max_rows, max_cols, cs, rpw, s);
+  if (L.nvar == 4) sweep_nv<4>(L, alfa1, mode, max_rows, max_cols, cs, rpw, lanes, s);
+  else if (L.nvar == 5) sweep_nv<5>(L, alfa1, mode, max_rows, max_cols, cs, rpw, lanes, s);
+  else sweep_nv<6>(L, alfa1, mode, max_rows, max_cols, cs, rpw, lanes, s);
 }
 
 }  // namespace ec2d

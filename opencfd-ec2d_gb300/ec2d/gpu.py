@@ -141,6 +141,7 @@ def lib():
         "ec2d_snapshot": ([vp, ctypes.c_int], ctypes.c_int),
         "ec2d_tile_residual": ([vp, ctypes.c_int, ip], ctypes.c_int),
         "ec2d_clear_status": ([vp, ctypes.c_int], ctypes.c_int),
+        "ec2d_lusgs_shape": ([vp, ip, ip, ip], ctypes.c_int),
         "ec2d_snapshot_wait": ([vp, ip, ip, dp], ctypes.c_int),
         "ec2d_snapshot_U": ([vp, ctypes.c_int, dp], ctypes.c_int),
         "ec2d_snapshot_amut": ([vp, ctypes.c_int, dp], ctypes.c_int),
@@ -372,6 +373,12 @@ class Solver:
     def set_case_shape(self, case, shape):
         """Per-case shape feature of the warm-start network (the airfoil t/c)."""
         _ck(self.L.ec2d_set_case_shape(self.h, case, float(shape)), "ec2d_set_case_shape")
+
+    def lusgs_shape(self):
+        """(lusgs_cs, rows, lanes) of the FP64 wavefront in use."""
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _ck(self.L.ec2d_lusgs_shape(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)), "ec2d_lusgs_shape")
+        return a.value, b.value, c.value
 
     def clear_status(self, case=0):
         """Clear a case's status word (0: every case)."""

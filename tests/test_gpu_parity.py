@@ -256,16 +256,21 @@ def test_lusgs_sweep(gpu_lib, ny, turb):
 
 
 @pytest.mark.parametrize("turb,ny,shape", [(0, 41, "auto"), (0, 71, "auto"), (0, 41, "four"), (0, 71, "four"),
-                                           (0, 41, "one"), (0, 41, "barrier"), (2, 41, "auto")])
+                                           (0, 41, "one"), (0, 41, "barrier"), (2, 41, "auto"),
+                                           (0, 97, "warp4"), (0, 97, "eight8"), (0, 97, "six8"), (0, 97, "six4")])
 def test_lusgs_steps_wide_blocks(gpu_lib, monkeypatch, turb, ny, shape):
-    """LU-SGS time steps on 40- and 70-row blocks (U updated inside the
+    """LU-SGS time steps on 40- to 96-row blocks (U updated inside the
     sweep) against the oracle, with each wavefront shape: auto (eight lanes
     per row in bands of at most 12 rows on a cluster for NV = 4, one lane per
     row otherwise), four lanes per row in bands of at most 24 rows, one CTA
-    per block with one lane per row, and a two-CTA cluster with a barrier per
-    plane."""
-    monkeypatch.setenv("EC2D_LUSGS_CLUSTER", {"auto": "0", "four": "0", "one": "1", "barrier": "2"}[shape])
-    monkeypatch.setenv("EC2D_LUSGS_ROWS", {"four": "24", "one": "32", "barrier": "32"}.get(shape, "12"))
+    per block with one lane per row, a two-CTA cluster with a barrier per
+    plane, and the narrow bands on clusters of 12 and 16 CTAs (8 rows with
+    four lanes: one warp per CTA; 8 rows with eight lanes; 6 rows with eight
+    or four lanes), where the device places such clusters."""
+    monkeypatch.setenv("EC2D_LUSGS_CLUSTER", {"auto": "0", "four": "0", "one": "1", "barrier": "2"}.get(shape, "0"))
+    monkeypatch.setenv("EC2D_LUSGS_ROWS", {"four": "24", "one": "32", "barrier": "32", "warp4": "8", "eight8": "8",
+                                           "six8": "6", "six4": "6"}.get(shape, "12"))
+    monkeypatch.setenv("EC2D_LUSGS_LANES", {"warp4": "4", "six4": "4", "eight8": "8", "six8": "8"}.get(shape, "0"))
     kw = dict(ny=ny, Ma=0.6, AoA=2.0, Iflag_flux=4, Iflag_Scheme=5, Time_Method=0, CFL=5.0)
     if turb == 2:
         kw.update(If_viscous=1, Iflag_turbulence_model=2, Re=1e6, first=2e-4)
