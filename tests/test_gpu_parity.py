@@ -352,3 +352,17 @@ def test_batch_equals_single(gpu_lib):
         for b in range(1, len(bl) + 1):
             np.testing.assert_array_equal(batch.download_U(ci, 1, b), one.download_U(1, 1, b))
         np.testing.assert_array_equal(batch.norms(ci)[1], one.norms(1)[1])
+
+
+def test_symmetric_airfoil_zero_lift(gpu_lib):
+    """NACA 0012 at AoA 0 with the pointwise RK3 update (an i+j LU-SGS sweep
+    is not mirror-symmetric): the mirror symmetry of grid, scheme and force
+    integration keeps CL and CM zero to round-off on the GPU, as on the
+    oracle (test_oracle_kat)."""
+    p, bl = small_case(nx=65, ny=17, Ma=0.5, AoA=0.0, Iflag_flux=4, Iflag_Scheme=5, Time_Method=3, CFL=1.0)
+    g = make_gpu(p, bl)
+    g.init_flow()
+    g.step(120)
+    cl, cd, cm = g.forces(1)
+    assert abs(cl) < 1e-11 and abs(cm) < 1e-11
+    g.close()

@@ -172,3 +172,20 @@ def test_reference_rae2822_case_runs(oracle_lib):
     r0 = orc.norms()[1][0]
     orc.step(100)
     assert orc.norms()[1][0] < r0
+
+
+def test_flat_plate_converged_cf_is_blasius():
+    """The oracle's converged laminar flat plate (the committed fixture:
+    2 x 97x97, Re 1e4 per unit length, M 0.3, 1e-8 drop) against the Blasius
+    solution: wall skin friction within 3 % of 0.664 / sqrt(Re_x) over
+    x = 0.2..0.9 (measured 0.6-2.1 %), drag within 5 % of 1.328 / sqrt(Re)
+    (measured 3.3 %, the leading edge included)."""
+    import json
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "converged.json")) as fh:
+        fx = json.load(fh)["flat_plate"]
+    cf, xc = np.array(fx["wall"]["cf"]), np.array(fx["wall"]["xc"])
+    m = (xc > 0.2) & (xc < 0.9)
+    blasius = 0.664 / np.sqrt(1.0e4 * xc[m])
+    assert np.max(np.abs(cf[m] / blasius - 1.0)) <= 0.03
+    assert abs(fx["forces"]["cd"] / (1.328 / np.sqrt(1.0e4)) - 1.0) <= 0.05
+    assert fx["reached"] and fx["iterations"] == 6751
