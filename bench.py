@@ -392,6 +392,7 @@ def residual_hbm(torch, gpu, dev, reps=10, forms=("chain", "tile")):
                       "fp64_issue_frac": inst_pc * cells / (total_ms / 1e3) / 1e12 / (fp64_peak / 2.0)})
         out[form] = r
     g.close()
+    out["transfers"] = transfer_hbm(torch, gpu, dev, p, blocks, hbm)
     # the headline fields: the faster form
     best = min(forms, key=lambda f: out[f]["ms"])
     out["form"] = best
@@ -401,6 +402,42 @@ def residual_hbm(torch, gpu, dev, reps=10, forms=("chain", "tile")):
     out["note"] = ("FP64 instruction issue bounds this stage: fp64_issue_frac = FP64 instructions per second / the "
                    "FP64 pipe's instruction rate (measured FMA FLOP/s / 2); fp64_frac counts FLOPs, where a dadd or "
                    "dmul is one FLOP in one issue slot")
+    return out
+
+
+def transfer_hbm(torch, gpu, dev, p, blocks, hbm, reps=10):
+    """The multigrid transfers on the same 4.19 M-cell grid with a second
+    level, each launched through its C-ABI hook (interpolation2h, prolong_U)
+    and timed with CUDA events on the library's stream: the volume-weighted
+    restriction of U (flag 1; algorithmic bytes per coarse cell: read 4 fine
+    cells' U and volumes and the coarse volume, write U: 200), the
+    restriction of the residual (flag 2; read 4 fine Res, write QF: 160) and
+    the prolongation of U (flag 1; per fine cell: write U, read a quarter of
+    a coarse cell's U: 40)."""
+    g = gpu.Solver([(p.replace(Num_Mesh=2), blocks)], device=dev)
+    g.init_flow()
+    g.residual(1)
+    g.sync()
+    st = torch.cuda.ExternalStream(g.stream_handle())
+    fine = fine_cells(blocks)
+    coarse = sum(((b.nx - 1) // 2) * ((b.ny - 1) // 2) for b in blocks)
+    out = {}
+    for name, call, nbytes in (("k_restrict U", lambda: g.interpolation2h(1, 2, 1), 200.0 * coarse),
+                               ("k_restrict Res", lambda: g.interpolation2h(1, 2, 2), 160.0 * coarse),
+                               ("k_prolong U", lambda: g.prolong(2, 1, 1), 40.0 * fine)):
+        call()
+        g.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            call()
+        e1.record(st)
+        e1.synchronize()
+        us = e0.elapsed_time(e1) / reps * 1e3
+        gbs = nbytes / (us * 1e-6) / 1e9
+        out[name] = {"us": round(us, 1), "algorithmic_bytes": nbytes, "gbs": round(gbs, 1), "hbm_frac": gbs / hbm}
+    g.close()
+    out["note"] = "back-to-back launches on a working set far larger than L2 (the fine level alone is 4.19 M cells)"
     return out
 
 
