@@ -14,13 +14,13 @@ void launch_flux_j(const Lvl &L, bool fp32, cudaStream_t s);
 // post-residual steps k_res can do in the same pass (bits of `post`)
 enum { RES_ADD_FORCE = 1, RES_FORCE_FN = 2, RES_SET_UN = 4 };
 // cells per 2-D tile of the one-kernel residual (k_residual_tile) and its
-// threads: (16 + 1) x 7 i-faces + 16 x 8 j-faces = 247 faces, 20 x 11 halo
-// cells, 112 cells, each a thread of 256
-constexpr int RES_TILE_X = 16, RES_TILE_Y = 7, RES_TILE_THREADS = 256;
+// threads: (16 + 1) x 8 i-faces + 16 x 9 j-faces = 280 faces, 20 x 12 halo
+// cells, 128 cells, each a thread of 288 (the 2 x 96 x 96 flat-plate level is
+// 144 tiles, one per SM)
+constexpr int RES_TILE_X = 16, RES_TILE_Y = 8, RES_TILE_THREADS = 288;
 void launch_res(const Lvl &L, bool with_norms, int post, cudaStream_t s);
 void launch_face_metrics(const Lvl &L, cudaStream_t s);
 void launch_norms(const Lvl &L, bool partials, cudaStream_t s);
-void launch_residual_tile(const Lvl &Lr, const int4 *rt, int ntiles, bool with_norms, int post, cudaStream_t s);
 void launch_residual_tile(const Lvl &Lr, const int4 *rt, int ntiles, bool with_norms, int post, cudaStream_t s);
 bool norms_fused_final(const Lvl &L);
 // k_turb.cu
