@@ -333,9 +333,10 @@ def merge_lusgs(kt):
     return sweep
 
 
-def residual_hbm(torch, gpu, dev, reps=10, forms=("chain", "tile")):
+def residual_hbm(torch, gpu, dev, reps=10, forms=("chain", "tile"), grid=(2049, 1025)):
     """Residual evaluation (Comput_Residual_one_mesh) on a grid far larger
-    than L2: 2 blocks of 2049x1025 nodes (4.19 M cells), laminar flat-plate
+    than L2: 2 blocks of 2049x1025 nodes (4.19 M cells; `grid` sets another
+    size, e.g. a small one for instruction counts), laminar flat-plate
     physics, a perturbed state, in both forms: the four-kernel chain through
     HBM planes and the one kernel over shared-memory tiles.  Achieved =
     algorithmic bytes of the residual (176 B per cell: read U, 7 metrics, x1,
@@ -345,7 +346,7 @@ def residual_hbm(torch, gpu, dev, reps=10, forms=("chain", "tile")):
     import numpy as np
     from ec2d import cases, grids
     p, _ = cases.laminar_flat_plate(33, 33, num_mesh=1)
-    blocks = grids.flat_plate(2049, 1025, first=1.0e-4, ratio=1.0065)
+    blocks = grids.flat_plate(grid[0], grid[1], first=1.0e-4, ratio=1.0065)
     cells = fine_cells(blocks)
     g = gpu.Solver([(p, blocks)], device=dev)
     g.init_flow()
@@ -360,7 +361,8 @@ def residual_hbm(torch, gpu, dev, reps=10, forms=("chain", "tile")):
         fp64_peak = gpu.measure_fp64_peak()
     except Exception:
         fp64_peak = None
-    out = {"cells": cells, "grid": "2 x 2049x1025 (flat plate, 4.19 M cells)", "algorithmic_bytes_per_cell": 176,
+    out = {"cells": cells, "grid": f"2 x {grid[0]}x{grid[1]} (flat plate, {cells / 1e6:.2f} M cells)",
+           "algorithmic_bytes_per_cell": 176,
            "peak_gbs": hbm, "peak_source": f"{kind} hbm_gbs", "fp64_peak_tflops": fp64_peak,
            "fp64_peak_source": "measured in this run (ec2d_measure_fp64_peak: FMA chains on every SM)"}
     for form in forms:
@@ -408,12 +410,15 @@ def residual_hbm(torch, gpu, dev, reps=10, forms=("chain", "tile")):
 def transfer_hbm(torch, gpu, dev, p, blocks, hbm, reps=10):
     """The multigrid transfers on the same 4.19 M-cell grid with a second
     level, each launched through its C-ABI hook (interpolation2h, prolong_U)
-    and timed with CUDA events on the library's stream: the volume-weighted
-    restriction of U (flag 1; algorithmic bytes per coarse cell: read 4 fine
-    cells' U and volumes and the coarse volume, write U: 200), the
-    restriction of the residual (flag 2; read 4 fine Res, write QF: 160) and
-    the prolongation of U (flag 1; per fine cell: write U, read a quarter of
-    a coarse cell's U: 40)."""
+    and timed with CUDA events on the library's stream.  Algorithmic bytes:
+    the volume-weighted restriction of U (flag 1; per coarse cell read 4 fine
+    cells' U and volumes and the coarse volume, write U: 200); the
+    restriction of the residual (flag 2; read 4 fine Res, write QF: 160); the
+    cycle's forcing (flag 6; also read the coarse Res: 192); the
+    prolongation of U (flag 1; per fine cell write U, read a quarter of a
+    coarse cell's U: 40); the cycle's correction (flag 3; per fine cell read
+    and write U, write deltU, read a quarter of a coarse cell's U and Un:
+    112)."""
     g = gpu.Solver([(p.replace(Num_Mesh=2), blocks)], device=dev)
     g.init_flow()
     g.residual(1)
@@ -424,7 +429,9 @@ def transfer_hbm(torch, gpu, dev, p, blocks, hbm, reps=10):
     out = {}
     for name, call, nbytes in (("k_restrict U", lambda: g.interpolation2h(1, 2, 1), 200.0 * coarse),
                                ("k_restrict Res", lambda: g.interpolation2h(1, 2, 2), 160.0 * coarse),
-                               ("k_prolong U", lambda: g.prolong(2, 1, 1), 40.0 * fine)):
+                               ("k_restrict QF (cycle)", lambda: g.interpolation2h(1, 2, 6), 192.0 * coarse),
+                               ("k_prolong U", lambda: g.prolong(2, 1, 1), 40.0 * fine),
+                               ("k_prolong U-Un (cycle)", lambda: g.prolong(2, 1, 3), 112.0 * fine)):
         call()
         g.sync()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -437,17 +444,19 @@ def transfer_hbm(torch, gpu, dev, p, blocks, hbm, reps=10):
         gbs = nbytes / (us * 1e-6) / 1e9
         out[name] = {"us": round(us, 1), "algorithmic_bytes": nbytes, "gbs": round(gbs, 1), "hbm_frac": gbs / hbm}
     g.close()
-    out["note"] = "back-to-back launches on a working set far larger than L2 (the fine level alone is 4.19 M cells)"
+    out["note"] = f"back-to-back launches; the fine level is {fine / 1e6:.2f} M cells"
     return out
 
 
-def plain_step_ms(torch, gpu, pc, steps=10):
+def plain_step_ms(torch, gpu, pc, steps=10, mg_amut=False):
     """Milliseconds per V-cycle of every case as the plain drop-in: one
     context per case, FP64 LU-SGS, the step graph replayed, CUDA events on
     the context's stream after three warm-up V-cycles."""
     out = []
     for case in pc:
         g = gpu.Solver([case[:2]])
+        if mg_amut:
+            g.mg_eddy_viscosity(1)
         st = torch.cuda.ExternalStream(g.stream_handle())
         g.init_flow()
         g.step(3)
@@ -480,6 +489,13 @@ def polar_metric(args, torch, gpu):
       case whose residual blows up within its first 200 V-cycles restarts
       from the freestream (the fallback).
 
+    Every context of the comparison (the plain per-case timings included)
+    keeps the restricted eddy viscosity on its coarse levels
+    (ec2d_mg_eddy_viscosity; off with --no-polar-mg-eddy-viscosity): with the
+    reference's laminar coarse levels the LU-SGS V-cycle diverges on some
+    turbulent cases (7 of 64 within the cap from the freestream) and on most
+    warm starts, on the oracle as on the GPU.
+
     Every run is capped at args.polar_cap seconds; residuals are checked
     every 25 V-cycles.  The batched arms retire a case when it reaches the
     comparison drop (args.polar_drop) or diverges, and move the others into
@@ -505,18 +521,21 @@ def polar_metric(args, torch, gpu):
         net, learned = learned_leg(args, gpu)
         out["learned_training"] = learned
     t0 = time.perf_counter()
+    mg = args.polar_mg_amut
+    out["mg_eddy_viscosity"] = bool(mg)
     fp64 = learn.converge(gpu, pc, "freestream", 64, targets=targets, max_steps=10 ** 6, check=25,
-                          max_seconds=args.polar_cap)
+                          max_seconds=args.polar_cap, mg_amut=mg)
     r0 = fp64["r0"]
     arms = {"batched_fp64": fp64,
             "batched_mixed": learn.converge(gpu, pc, "freestream", 32, r0=r0, targets=arm_targets,
-                                            max_steps=10 ** 6, check=25, max_seconds=args.polar_cap, retire=drop)}
+                                            max_steps=10 ** 6, check=25, max_seconds=args.polar_cap, retire=drop,
+                                            mg_amut=mg)}
     if net is not None:
         arms["learned_batched_mixed"] = learn.converge(gpu, pc, "warm", 32, r0=r0, net=net, targets=arm_targets,
                                                        max_steps=10 ** 6, check=25, max_seconds=args.polar_cap,
-                                                       retire=drop)
+                                                       retire=drop, mg_amut=mg)
         net.close()
-    plain_ms = plain_step_ms(torch, gpu, pc)
+    plain_ms = plain_step_ms(torch, gpu, pc, mg_amut=mg)
     out["plain_ms_per_vcycle"] = {"median": float(np.median(plain_ms)), "min": float(np.min(plain_ms)),
                                   "max": float(np.max(plain_ms)), "sum": float(np.sum(plain_ms))}
     for name, r in arms.items():
@@ -904,6 +923,11 @@ def main():
                     help="keep the default launch configuration (e.g. under a profiler, whose timing misleads it)")
     ap.add_argument("--no-residual-hbm", dest="residual_hbm", action="store_false",
                     help="skip the residual bandwidth measurement on the 4.19 M-cell grid")
+    ap.add_argument("--no-polar-mg-eddy-viscosity", dest="polar_mg_amut", action="store_false",
+                    help="polar runs with laminar coarse levels, as the reference (default: the coarse levels keep "
+                         "the restricted eddy viscosity, which keeps the turbulent V-cycle from diverging)")
+    ap.add_argument("--residual-grid", default="2049x1025",
+                    help="nodes per block of the residual_hbm leg's 2-block flat plate (NXxNY)")
     ap.add_argument("--leg", default="all", choices=["all", "residual_hbm", "polar", "learned", "mlp"],
                     help="residual_hbm: the 4.19 M-cell residual alone (for profiling); polar: the 64-case "
                          "batched polar; learned: the learned warm start end to end")
@@ -930,7 +954,7 @@ def main():
         import torch
         from ec2d import gpu
         if args.leg == "residual_hbm":
-            out = residual_hbm(torch, gpu, 0)
+            out = residual_hbm(torch, gpu, 0, grid=tuple(int(v) for v in args.residual_grid.split("x")))
         elif args.leg == "polar":
             out = leg_polar(args)
         elif args.leg == "mlp":

@@ -98,6 +98,9 @@ const char *ec2d_error_string(int code);
  *                       branches; results are bit-identical either way)
  *   EC2D_TILE_RESIDUAL  1: the residual as one kernel over shared-memory
  *                       tiles (see ec2d_tile_residual)
+ *   EC2D_MG_EDDY_VISCOSITY  1: coarse multigrid levels keep the restricted
+ *                       eddy viscosity (see ec2d_mg_eddy_viscosity; this one
+ *                       changes the iteration, not the converged answer)
  *   EC2D_TEST_SILENT_BAND_EDGE  test hook: band edges of the banded wavefront
  *                       send nothing, so the downstream waits run out and the
  *                       next status read returns EC2D_ERR_TIMEOUT */
@@ -216,7 +219,13 @@ int ec2d_boundary_condition(ec2d_ctx *ctx, int mesh);     /* Boundary_condition_
 int ec2d_update_buffer(ec2d_ctx *ctx, int mesh);          /* update_buffer_onemesh, sub_boundary.f90:45 */
 int ec2d_du_lusgs(ec2d_ctx *ctx, int mesh, double alfa1); /* du_LU_SGS_2D, sub_LU_SGS.f90:4 */
 int ec2d_time_advance(ec2d_ctx *ctx, int mesh);           /* NS_Time_advance, sub_NS_singlegrid.f90:8 */
+/* interpolation2h flags 1 (U) and 2 (residual sum into QF) as in the
+ * reference; 6 is the multigrid cycle's form, QF = sum of the four fine Res
+ * - the coarse Res (comput_force_function folded in). */
 int ec2d_interpolation2h(ec2d_ctx *ctx, int m1, int m2, int flag); /* sub_NS_multigrid.f90:349 */
+/* prolong_U flags 1 (U) and 2 (deltU) as in the reference; 3 is the cycle's
+ * form: deltU = U - Un of the coarse level (comput_delt_U) prolonged into
+ * the fine DELTU and added to the fine interior U (comput_new_U). */
 int ec2d_prolong(ec2d_ctx *ctx, int m1, int m2, int flag);         /* prolong_U, sub_NS_multigrid.f90:271 */
 int ec2d_force_function(ec2d_ctx *ctx, int mesh);         /* comput_force_function, sub_NS_multigrid.f90:156 */
 
@@ -356,6 +365,20 @@ int ec2d_lusgs_shape(ec2d_ctx *ctx, int *lusgs_cs, int *rows, int *lanes);
  * picks the faster; EC2D_TILE_RESIDUAL=1 read by ec2d_create starts with the
  * one-kernel form. */
 int ec2d_tile_residual(ec2d_ctx *ctx, int enable, int *current);
+
+/* Multigrid with a turbulence model: the coarse levels keep an eddy
+ * viscosity restricted from the next finer level (enable = 1; the mean of a
+ * coarse cell's children over 0..nx, 0..ny, taken after the finer level's
+ * residual, frozen on the coarse level), or are laminar as in the reference
+ * (0, the default: Comput_Residual_one_mesh zeroes Amu_t and the coarse
+ * levels run no turbulence model, sub_Residual.f90:158-191,
+ * opencfd_ec2d_v1.5.4.f90:252-259).  -1 only reads the setting into *current
+ * (may be NULL).  The coarse problem changes, its fixed point (the fine
+ * discretisation) does not: the option is for stability.  With laminar
+ * coarse levels the LU-SGS-smoothed cycle diverges from developed turbulent
+ * fields (the oracle likewise), where the frozen eddy viscosity keeps the
+ * coarse corrections damped. */
+int ec2d_mg_eddy_viscosity(ec2d_ctx *ctx, int enable, int *current);
 
 /* Precision of the face fluxes (reconstruction, Riemann solver, viscous
  * stress) on the coarse multigrid levels: 64 (the default) or 32.  No

@@ -136,6 +136,9 @@ struct ec2d_ctx {
   int lusgs_lanes = 0;      // lanes per row of the banded kernel: 4 or 8, 0 by the rows (eight up to 16)
   bool coarse_fp32 = false; // face fluxes of multigrid levels >= 2 in FP32
   bool tile_residual = false; // the one-kernel residual where it applies (no turbulence model, no FDM patch, FP64)
+  // extension for turbulent multigrid runs: the coarse levels keep the eddy
+  // viscosity restricted from the finer level (the reference's are laminar)
+  bool mg_amut = false;
   bool timing = false;
   // one pseudo-time step (single grid or V-cycle) captured as a CUDA graph:
   // the replay stands for graph_launches kernel launches and advances the
@@ -590,13 +593,19 @@ void K(ec2d_ctx *ctx, const char *name, int level, int nk, Fn fn) {
 // post: RES_ADD_FORCE / RES_FORCE_FN / RES_SET_UN steps that follow the
 // residual in the caller's sequence, done inside k_res when the norms are
 // final there, as separate kernels otherwise
+// the coarse levels of a turbulent multigrid run keep the eddy viscosity
+// restricted from the finer level instead of zero
+static void apply_mg_amut(ec2d_ctx *ctx) {
+  const bool on = ctx->mg_amut && ctx->P.If_viscous == 1 && ctx->P.Iflag_turbulence_model != Turb_NONE;
+  for (int l = 2; l <= ctx->num_mesh; l++) ctx->lv[l].L.keep_amut = on ? 1 : 0;
+}
 void residual(ec2d_ctx *ctx, int l, int post = 0) {
   Level &lv = ctx->lv[l];
   const Lvl &L = lv.L;
   cudaStream_t s = ctx->stream;
   const bool dual = ctx->P.Time_Method == Time_Dual && l == 1;
   const bool f32 = ctx->coarse_fp32 && l >= 2;
-  if (ctx->tile_residual && lv.n_rtiles > 0 && L.turb == Turb_NONE && !L.fdm && !dual && !f32) {
+  if (ctx->tile_residual && lv.n_rtiles > 0 && L.turb == Turb_NONE && !L.fdm && !L.keep_amut && !dual && !f32) {
     // the whole residual in one kernel over 2-D tiles (norm partials inside;
     // with few cases the per-case norms and the multigrid post-steps too)
     Lvl Lr = L;
@@ -801,6 +810,17 @@ void transfer_down(ec2d_ctx *ctx, int f, int fine_post) {
   const int tm = ctx->P.Time_Method;
   const int cpost = (tm == Time_Euler1 || tm == Time_LU_SGS) ? RES_SET_UN : 0;
   const Lvl &Lf = ctx->lv[f].L, &Lc = ctx->lv[f + 1].L;
+  if (Lc.keep_amut) {
+    // the coarse eddy viscosity comes from the finer level's after its
+    // residual (the oracle's order: residual, then interpolation2h), so
+    // this transfer runs in sequence
+    residual(ctx, f, fine_post);
+    K(ctx, "k_restrict", f + 1, 1, [&] { launch_restrict(Lf, Lc, 1 | 8, ctx->stream); });
+    bc_all(ctx, f + 1);
+    residual(ctx, f + 1, cpost);
+    K(ctx, "k_restrict", f + 1, 1, [&] { launch_restrict(Lf, Lc, 2 | 4, ctx->stream); });
+    return;
+  }
   const bool par = !ctx->timing && ctx->concurrent;
   if (par) {
     cudaEventRecord(ctx->ev_b0, ctx->stream);
@@ -980,6 +1000,7 @@ int ec2d_create(int device, ec2d_ctx **out) {
   if (const char *e = getenv("EC2D_TEST_SILENT_BAND_EDGE")) c->silent_band_edge = atoi(e) != 0;
   if (const char *e = getenv("EC2D_CONCURRENT")) c->concurrent = atoi(e) != 0;
   if (const char *e = getenv("EC2D_TILE_RESIDUAL")) c->tile_residual = atoi(e) != 0;
+  if (const char *e = getenv("EC2D_MG_EDDY_VISCOSITY")) c->mg_amut = atoi(e) != 0;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
@@ -1118,6 +1139,7 @@ int ec2d_setup(ec2d_ctx *ctx) {
   ctx->stage_n = mx;
   CK(cudaDeviceSynchronize());
   ctx->setup_done = true;
+  apply_mg_amut(ctx);
   return EC2D_OK;
 }
 
@@ -1153,6 +1175,10 @@ int ec2d_init_flow(ec2d_ctx *ctx) {
   int rc = ec2d_clear_status(ctx, 0);  // a fresh start: no case carries a stop
   if (rc) return rc;
   int nm = ctx->num_mesh;
+  // coarse eddy viscosity (kept between residuals only with the multigrid
+  // eddy-viscosity extension): zero until the first restriction
+  for (int l = 2; l <= nm; l++)
+    CK(cudaMemsetAsync(ctx->lv[l].L.amut, 0, (size_t)ctx->lv[l].F * sizeof(double), ctx->stream));
   if (ctx->nvar >= 5) launch_freestream(ctx->lv[1].L, 0, 1, ctx->stream);
   launch_freestream(ctx->lv[nm].L, 1, 0, ctx->stream);
   bc_all(ctx, nm);
@@ -1397,7 +1423,7 @@ int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *rows_per_w
   // chain (where some level can take it)
   bool tile_applies = false;
   for (int l = 1; l <= ctx->num_mesh; l++)
-    tile_applies |= ctx->lv[l].L.turb == Turb_NONE && !ctx->lv[l].L.fdm;
+    tile_applies |= ctx->lv[l].L.turb == Turb_NONE && !ctx->lv[l].L.fdm && !ctx->lv[l].L.keep_amut;
   if (r == EC2D_OK && tile_applies) {
     const bool old_tile = ctx->tile_residual;
     double tbest = 1e30;
@@ -1448,6 +1474,17 @@ int ec2d_tile_residual(ec2d_ctx *ctx, int enable, int *current) {
     drop_graph(ctx);
   }
   if (current) *current = ctx->tile_residual ? 1 : 0;
+  return EC2D_OK;
+}
+
+int ec2d_mg_eddy_viscosity(ec2d_ctx *ctx, int enable, int *current) {
+  if (!ctx || enable < -1 || enable > 1) return EC2D_ERR_ARG;
+  if (enable >= 0 && (enable != 0) != ctx->mg_amut) {
+    ctx->mg_amut = enable != 0;
+    if (ctx->setup_done) apply_mg_amut(ctx);
+    drop_graph(ctx);
+  }
+  if (current) *current = ctx->mg_amut ? 1 : 0;
   return EC2D_OK;
 }
 
@@ -1695,14 +1732,14 @@ int ec2d_time_advance(ec2d_ctx *ctx, int mesh) {
   return check_launch(ctx);
 }
 int ec2d_interpolation2h(ec2d_ctx *ctx, int m1, int m2, int flag) {
-  if (!ctx || !ctx->setup_done || m2 != m1 + 1 || m1 < 1 || m2 > ctx->num_mesh || (flag != 1 && flag != 2))
+  if (!ctx || !ctx->setup_done || m2 != m1 + 1 || m1 < 1 || m2 > ctx->num_mesh || (flag != 1 && flag != 2 && flag != 6))
     return EC2D_ERR_ARG;
   cudaSetDevice(ctx->device);
   launch_restrict(ctx->lv[m1].L, ctx->lv[m2].L, flag, ctx->stream);
   return check_launch(ctx);
 }
 int ec2d_prolong(ec2d_ctx *ctx, int m1, int m2, int flag) {
-  if (!ctx || !ctx->setup_done || m2 != m1 - 1 || m2 < 1 || m1 > ctx->num_mesh || (flag != 1 && flag != 2))
+  if (!ctx || !ctx->setup_done || m2 != m1 - 1 || m2 < 1 || m1 > ctx->num_mesh || (flag < 1 || flag > 3))
     return EC2D_ERR_ARG;
   cudaSetDevice(ctx->device);
   launch_prolong(ctx->lv[m1].L, ctx->lv[m2].L, flag, ctx->stream);

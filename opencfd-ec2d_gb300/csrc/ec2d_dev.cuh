@@ -97,6 +97,7 @@ struct Lvl {
   unsigned *nctr;           // tiles of k_res done (the last one reduces the partials)
   int *status;              // per case: code, block, i, j
   int silent_band_edge;     // test hook: band edges of the four-lane wavefront send nothing
+  int keep_amut;            // coarse level: amut is restricted from the finer level, not zeroed
 };
 
 // Items (cells, faces or nodes of a block's padded index range) per tile of

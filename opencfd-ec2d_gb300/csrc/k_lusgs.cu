@@ -172,62 +172,134 @@ __global__ void k_set_un(Lvl L, int nv) {
 // flag 1 volume-weighted U, flag 2 residual sum into QF, 3 both; with 4 the
 // coarse residual already evaluated on the restricted U is subtracted from
 // the sum (QF = sum Res_h - Res_2h, comput_force_function,
-// sub_NS_multigrid.f90:156-173: the sum is rounded first, as there).  Runs
-// over the coarse level's tiles.
+// sub_NS_multigrid.f90:156-173: the sum is rounded first, as there).  With
+// 8 (an extension for turbulent cases) the coarse eddy viscosity over
+// 0..nx, 0..ny is the mean of its children's within the finer level's
+// 0..nx, 0..ny, summed j-major as the oracle does.  Runs over the coarse
+// level's tiles.  Every operand is loaded before the first store: the
+// stores may alias the loads as far as the compiler knows, so loads
+// interleaved with stores would be issued one variable at a time.
 __global__ void k_restrict(Lvl Lf, Lvl Lc, int flag) {
   int bk, i, j;
-  if (!tile_cell(Lc, bk, i, j, 1, 1)) return;
+  if (!tile_cell(Lc, bk, i, j, 0, 0)) return;
   const BlkDev &bc = Lc.blk[bk], &bf = Lf.blk[bk];
-  long long ic = fidx(bc, i, j);
-  long long f11 = fidx(bf, 2 * i - 1, 2 * j - 1), f12 = fidx(bf, 2 * i - 1, 2 * j);
-  long long f21 = fidx(bf, 2 * i, 2 * j - 1), f22 = fidx(bf, 2 * i, 2 * j);
+  const long long ic = fidx(bc, i, j);
+  if (flag & 8) {
+    double sum = 0.0;
+    int n = 0;
+    for (int jj = 2 * j - 1; jj <= 2 * j; jj++)
+      for (int ii = 2 * i - 1; ii <= 2 * i; ii++)
+        if (ii >= 0 && ii <= bf.nx && jj >= 0 && jj <= bf.ny) {
+          sum += Lf.amut[fidx(bf, ii, jj)];
+          n++;
+        }
+    Lc.amut[ic] = sum / (double)n;
+  }
+  if (i < 1 || i > bc.nx - 1 || j < 1 || j > bc.ny - 1) return;
+  const long long f11 = fidx(bf, 2 * i - 1, 2 * j - 1), f12 = fidx(bf, 2 * i - 1, 2 * j);
+  const long long f21 = fidx(bf, 2 * i, 2 * j - 1), f22 = fidx(bf, 2 * i, 2 * j);
   const long long FF = Lf.F, FC = Lc.F;
   if (flag & 1) {
     const double *vf = Lf.geo + G_VOL * FF;
-    double vc = Lc.geo[G_VOL * FC + ic];
+    const double w11 = vf[f11], w12 = vf[f12], w21 = vf[f21], w22 = vf[f22];
+    // one reciprocal of the coarse volume for the four variables (the
+    // reference divides each sum; an IEEE divide costs about a dozen FP64
+    // instructions, which bound this kernel on this part)
+    const double rvc = 1.0 / Lc.geo[G_VOL * FC + ic];
+    double u[4][4];
+#pragma unroll
     for (int m = 0; m < 4; m++) {
-      const double *u = Lf.U + m * FF;
-      Lc.U[m * FC + ic] = (u[f11] * vf[f11] + u[f12] * vf[f12] + u[f21] * vf[f21] + u[f22] * vf[f22]) / vc;
+      const double *q = Lf.U + m * FF;
+      u[m][0] = q[f11]; u[m][1] = q[f12]; u[m][2] = q[f21]; u[m][3] = q[f22];
     }
+#pragma unroll
+    for (int m = 0; m < 4; m++)
+      Lc.U[m * FC + ic] = (u[m][0] * w11 + u[m][1] * w12 + u[m][2] * w21 + u[m][3] * w22) * rvc;
   }
   if (flag & 2) {
+    double r[4][4], rc[4];
+#pragma unroll
     for (int m = 0; m < 4; m++) {
-      const double *r = Lf.res + m * FF;
-      const double sum = r[f11] + r[f12] + r[f21] + r[f22];
-      Lc.qf[m * FC + ic] = (flag & 4) ? sum - Lc.res[m * FC + ic] : sum;
+      const double *q = Lf.res + m * FF;
+      r[m][0] = q[f11]; r[m][1] = q[f12]; r[m][2] = q[f21]; r[m][3] = q[f22];
+      rc[m] = (flag & 4) ? Lc.res[m * FC + ic] : 0.0;
+    }
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      const double sum = r[m][0] + r[m][1] + r[m][2] + r[m][3];
+      Lc.qf[m * FC + ic] = (flag & 4) ? sum - rc[m] : sum;
     }
   }
 }
 
-// prolongation coarse -> fine (prolong_U, sub_NS_multigrid.f90:271-343), over
-// fine cells 0..nx2, 0..ny2; flag 1 interpolates U, flag 2 deltU, flag 3
-// deltU formed on the fly from the coarse U - Un (comput_delt_U,
+// prolongation coarse -> fine (prolong_U, sub_NS_multigrid.f90:271-343) over
+// fine cells 0..nx2, 0..ny2, weights 9/16, 3/16, 3/16, 1/16 on the nearest,
+// the two side and the diagonal coarse cells.  flag 1 interpolates U, flag 2
+// deltU, flag 3 deltU formed on the fly from the coarse U - Un (comput_delt_U,
 // sub_NS_multigrid.f90:199-216, the same subtraction) and then U += deltU on
 // the fine interior (comput_new_U, sub_NS_multigrid.f90:240-260), one pass.
+// One thread per 2 x 2 fine cells (2k, 2k+1) x (2l, 2l+1), which all take
+// their values from the coarse cells k, k+1 x l, l+1: the coarse values (and
+// their U - Un) are loaded and formed once for the four.  Runs over the
+// coarse level's tiles, k = 0..nxc-1, l = 0..nyc-1 (the fine range 0..nx2 is
+// 2 nxc cells wide).
 __global__ void k_prolong(Lvl Lc, Lvl Lf, int flag) {
-  int bk, i, j;
-  if (!tile_cell(Lf, bk, i, j, 0, 0)) return;
+  int bk, k, l;
+  if (!tile_cell(Lc, bk, k, l, 0, 1)) return;
   const BlkDev &bc = Lc.blk[bk], &bf = Lf.blk[bk];
   const double a1 = 9.0 / 16.0, a2 = 3.0 / 16.0, a3 = 1.0 / 16.0;
-  int ia1 = (i % 2 == 0) ? i / 2 : i / 2 + 1, ia2 = (i % 2 == 0) ? i / 2 + 1 : i / 2;
-  int ja1 = (j % 2 == 0) ? j / 2 : j / 2 + 1, ja2 = (j % 2 == 0) ? j / 2 + 1 : j / 2;
-  long long c11 = fidx(bc, ia1, ja1), c21 = fidx(bc, ia2, ja1), c12 = fidx(bc, ia1, ja2), c22 = fidx(bc, ia2, ja2);
-  long long id = fidx(bf, i, j);
-  const double *src = (flag == 1) ? Lc.U : Lc.deltu;
-  double *dst = (flag == 1) ? Lf.U : Lf.deltu;
-  const bool add = flag == 3 && i >= 1 && i <= bf.nx - 1 && j >= 1 && j <= bf.ny - 1;
+  const long long c00 = fidx(bc, k, l), c10 = fidx(bc, k + 1, l);
+  const long long c01 = fidx(bc, k, l + 1), c11 = fidx(bc, k + 1, l + 1);
+  const int i0 = 2 * k, j0 = 2 * l;
+  const bool has_i1 = i0 + 1 <= bf.nx, has_j1 = j0 + 1 <= bf.ny;
+  const long long f00 = fidx(bf, i0, j0), f10 = fidx(bf, i0 + 1, j0);
+  const long long f01 = fidx(bf, i0, j0 + 1), f11 = fidx(bf, i0 + 1, j0 + 1);
+  // fine interior rows and columns, where flag 3 adds the increment to U
+  const bool ai0 = flag == 3 && i0 >= 1 && i0 <= bf.nx - 1, ai1 = flag == 3 && has_i1 && i0 + 1 <= bf.nx - 1;
+  const bool aj0 = j0 >= 1 && j0 <= bf.ny - 1, aj1 = has_j1 && j0 + 1 <= bf.ny - 1;
+  double s[4][4];
+#pragma unroll
   for (int m = 0; m < 4; m++) {
-    double s11, s21, s12, s22;
     if (flag == 3) {
       const double *u = Lc.U + m * Lc.F, *un = Lc.un + m * Lc.F;
-      s11 = u[c11] - un[c11]; s21 = u[c21] - un[c21]; s12 = u[c12] - un[c12]; s22 = u[c22] - un[c22];
+      s[m][0] = u[c00] - un[c00]; s[m][1] = u[c10] - un[c10];
+      s[m][2] = u[c01] - un[c01]; s[m][3] = u[c11] - un[c11];
     } else {
-      const double *s = src + m * Lc.F;
-      s11 = s[c11]; s21 = s[c21]; s12 = s[c12]; s22 = s[c22];
+      const double *q = ((flag == 1) ? Lc.U : Lc.deltu) + m * Lc.F;
+      s[m][0] = q[c00]; s[m][1] = q[c10]; s[m][2] = q[c01]; s[m][3] = q[c11];
     }
-    const double v = a1 * s11 + a2 * (s21 + s12) + a3 * s22;
-    dst[m * Lf.F + id] = v;
-    if (add) Lf.U[m * Lf.F + id] = Lf.U[m * Lf.F + id] + v;
+  }
+  double uf[4][4];
+  if (flag == 3) {
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      const double *u = Lf.U + m * Lf.F;
+      uf[m][0] = (ai0 && aj0) ? u[f00] : 0.0; uf[m][1] = (ai1 && aj0) ? u[f10] : 0.0;
+      uf[m][2] = (ai0 && aj1) ? u[f01] : 0.0; uf[m][3] = (ai1 && aj1) ? u[f11] : 0.0;
+    }
+  }
+  double *dst = (flag == 1) ? Lf.U : Lf.deltu;
+#pragma unroll
+  for (int m = 0; m < 4; m++) {
+    const double s00 = s[m][0], s10 = s[m][1], s01 = s[m][2], s11 = s[m][3];
+    // the side pairs of the diagonal cells and of the anti-diagonal ones are
+    // the same sums (an IEEE sum does not depend on the operand order)
+    const double side_d = s10 + s01, side_a = s00 + s11;
+    const double v00 = a1 * s00 + a2 * side_d + a3 * s11;  // fine (2k, 2l)
+    const double v10 = a1 * s10 + a2 * side_a + a3 * s01;  // fine (2k+1, 2l)
+    const double v01 = a1 * s01 + a2 * side_a + a3 * s10;  // fine (2k, 2l+1)
+    const double v11 = a1 * s11 + a2 * side_d + a3 * s00;  // fine (2k+1, 2l+1)
+    double *d = dst + m * Lf.F, *u = Lf.U + m * Lf.F;
+    d[f00] = v00;
+    if (has_i1) d[f10] = v10;
+    if (has_j1) d[f01] = v01;
+    if (has_i1 && has_j1) d[f11] = v11;
+    if (flag == 3) {
+      if (ai0 && aj0) u[f00] = uf[m][0] + v00;
+      if (ai1 && aj0) u[f10] = uf[m][1] + v10;
+      if (ai0 && aj1) u[f01] = uf[m][2] + v01;
+      if (ai1 && aj1) u[f11] = uf[m][3] + v11;
+    }
   }
 }
 
@@ -263,7 +335,7 @@ void launch_restrict(const Lvl &Lf, const Lvl &Lc, int flag, cudaStream_t s) {
   k_restrict<<<Lc.ntiles, TILE, 0, s>>>(Lf, Lc, flag);
 }
 void launch_prolong(const Lvl &Lc, const Lvl &Lf, int flag, cudaStream_t s) {
-  k_prolong<<<Lf.ntiles, TILE, 0, s>>>(Lc, Lf, flag);
+  k_prolong<<<Lc.ntiles, TILE, 0, s>>>(Lc, Lf, flag);
 }
 void launch_freestream(const Lvl &L, int flow, int turb, cudaStream_t s) {
   k_freestream<<<L.ntiles, TILE, 0, s>>>(L, flow, turb);

@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(TILE) k_prim(Lvl L) {
   if (L.visc) {
     if (i >= 0 && i <= b.nx && j >= 0 && j <= b.ny)
       L.amu[id] = c.rRe * (1.0 + c.Tsb) * (T * sT) * rcp(c.Tsb + T);  // T^1.5 = T sqrt(T)
-    L.amut[id] = 0.0;
+    if (!L.keep_amut) L.amut[id] = 0.0;
   }
 }
 

@@ -140,6 +140,7 @@ def lib():
         "ec2d_measure_fp64_peak": ([dp], ctypes.c_int),
         "ec2d_snapshot": ([vp, ctypes.c_int], ctypes.c_int),
         "ec2d_tile_residual": ([vp, ctypes.c_int, ip], ctypes.c_int),
+        "ec2d_mg_eddy_viscosity": ([vp, ctypes.c_int, ip], ctypes.c_int),
         "ec2d_clear_status": ([vp, ctypes.c_int], ctypes.c_int),
         "ec2d_lusgs_shape": ([vp, ip, ip, ip], ctypes.c_int),
         "ec2d_snapshot_wait": ([vp, ip, ip, dp], ctypes.c_int),
@@ -388,6 +389,13 @@ class Solver:
         """The one-kernel residual on (1) / off (0); -1 reads; returns the setting."""
         c = ctypes.c_int()
         _ck(self.L.ec2d_tile_residual(self.h, int(enable), ctypes.byref(c)), "ec2d_tile_residual")
+        return c.value
+
+    def mg_eddy_viscosity(self, enable=-1):
+        """Coarse multigrid levels keep the restricted eddy viscosity (1) or
+        are laminar as in the reference (0); -1 reads; returns the setting."""
+        c = ctypes.c_int()
+        _ck(self.L.ec2d_mg_eddy_viscosity(self.h, int(enable), ctypes.byref(c)), "ec2d_mg_eddy_viscosity")
         return c.value
 
     def set_coarse_precision(self, bits):

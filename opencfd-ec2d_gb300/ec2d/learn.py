@@ -25,8 +25,9 @@ from . import grids
 from .inputs import FLUX, SCHEME, TIME_LUSGS, TURB_SA, Params
 
 
-def warmstart_cases(n: int, seed: int, nx: int = 257, ny: int = 65) -> List[Tuple[Params, list, float]]:
-    """n cases drawn from the polar box: (params, blocks, t/c)."""
+def warmstart_cases(n: int, seed: int, nx: int = 257, ny: int = 65, num_mesh: int = 1) -> List[Tuple[Params, list, float]]:
+    """n cases drawn from the polar box: (params, blocks, t/c); num_mesh 3
+    runs them on the 3-level V-cycle."""
     rng = np.random.default_rng(seed)
     out = []
     for _ in range(n):
@@ -37,7 +38,7 @@ def warmstart_cases(n: int, seed: int, nx: int = 257, ny: int = 65) -> List[Tupl
         p = Params(Ma=M, AoA=aoa, Re=re, Pr=0.72, If_viscous=1, Iflag_turbulence_model=TURB_SA,
                    Iflag_local_dt=1, CFL=5.0, dtmax=1.0e3, dtmin=1.0e-12, Time_Method=TIME_LUSGS,
                    Iflag_Scheme=SCHEME["MUSCL3"], Iflag_flux=FLUX["ROE"], IFlag_Reconstruction=0,
-                   Num_Mesh=1, Twall=-1.0, vt_inf=3.0, mg_lusgs=1, xaxis=0.25)
+                   Num_Mesh=num_mesh, Twall=-1.0, vt_inf=3.0, mg_lusgs=1, xaxis=0.25)
         first = 1.0e-6 * 6.5e6 / re * 4.0
         blocks = grids.naca_cgrid(nx, ny, m=0.0, p=0.0, t=tc, radius=20.0, n_wake=(nx - 1) // 8 + 1,
                                   first=first, nblocks=1)
@@ -45,28 +46,31 @@ def warmstart_cases(n: int, seed: int, nx: int = 257, ny: int = 65) -> List[Tupl
     return out
 
 
-def _solver(gpu, chunk, bits):
+def _solver(gpu, chunk, bits, mg_amut=False):
     s = gpu.Solver([(p, b) for p, b, _ in chunk])
     s.set_lusgs_precision(bits)
+    if mg_amut:
+        s.mg_eddy_viscosity(1)
     for c, (_, _, tc) in enumerate(chunk, start=1):
         s.set_case_shape(c, tc)
     return s
 
 
 def generate(gpu, net, cases, steps: int, batch: int = 64, bits: int = 32, target: float = None,
-             check: int = 500, plateau: float = 0.8, max_seconds: float = None) -> Dict:
+             check: int = 500, plateau: float = 0.8, max_seconds: float = None, mg_amut: bool = False) -> Dict:
     """Solve the cases in batches from the freestream and add every fine-mesh
     cell of the result to the network's samples.  A batch runs until every
     case's Res_rms(1) dropped below `target` x its first-iteration value, or
     until no case improved its drop by more than the factor `plateau` over
     the last four checks (`check` steps apart), or `steps` steps, or
     `max_seconds` per batch.  Records each field's drop and where it
-    stopped."""
+    stopped.  mg_amut: coarse multigrid levels keep the restricted eddy
+    viscosity (ec2d_mg_eddy_viscosity)."""
     t0 = time.perf_counter()
     drops, stopped = [], []
     for k in range(0, len(cases), batch):
         chunk = cases[k:k + batch]
-        s = _solver(gpu, chunk, bits)
+        s = _solver(gpu, chunk, bits, mg_amut)
         s.init_flow()
         s.step(1)
         r0 = np.array([_rms(s, c) for c in range(1, len(chunk) + 1)])
@@ -118,7 +122,7 @@ def _rms(s, c):
         return float("nan")
 
 
-def _move(gpu, s, cases, idx, keep_mask, bits):
+def _move(gpu, s, cases, idx, keep_mask, bits, mg_amut=False):
     """The cases of context `s` at positions keep_mask (original indices
     idx[keep_mask]) into a new context: their U, ghosts included, copied
     exactly, so their iteration continues bit for bit."""
@@ -126,7 +130,7 @@ def _move(gpu, s, cases, idx, keep_mask, bits):
     Us = [[s.download_U(k + 1, 1, b) for b in range(1, len(cases[c][1]) + 1)]
           for k, c in enumerate(idx) if keep_mask[k]]
     s.close()
-    s2 = _solver(gpu, [cases[c] for c in keep], bits)
+    s2 = _solver(gpu, [cases[c] for c in keep], bits, mg_amut)
     s2.init_flow()
     for k, c in enumerate(keep):
         for b, U in enumerate(Us[k], start=1):
@@ -136,7 +140,8 @@ def _move(gpu, s, cases, idx, keep_mask, bits):
 
 def converge(gpu, cases, start: str, bits: int, r0=None, net=None, targets=(1e-4, 1e-6, 1e-8),
              max_steps: int = 30000, check: int = 50, max_seconds: float = None, retire: float = None,
-             compact: float = 0.25, fallback_steps: int = 200, fallback_ratio: float = 100.0) -> Dict:
+             compact: float = 0.25, fallback_steps: int = 200, fallback_ratio: float = 100.0,
+             mg_amut: bool = False) -> Dict:
     """Run all cases of `cases` in one context until every case's
     Res_rms(1) <= min(targets) x r0 or max_steps (r0: each case's
     freestream-start first residual, measured here when not given).
@@ -152,9 +157,12 @@ def converge(gpu, cases, start: str, bits: int, r0=None, net=None, targets=(1e-4
     A warm start keeps the freestream as the fallback: a case whose residual
     stops being finite, or exceeds fallback_ratio x its freestream-start
     residual, within the first fallback_steps steps restarts from the
-    freestream (its state replaced, its status cleared)."""
+    freestream (its state replaced, its status cleared).
+
+    mg_amut: coarse multigrid levels keep the restricted eddy viscosity
+    (ec2d_mg_eddy_viscosity) in every context of the run."""
     ts = time.perf_counter()
-    s = _solver(gpu, cases, bits)
+    s = _solver(gpu, cases, bits, mg_amut)
     setup_s = time.perf_counter() - ts  # context set-up: grids to the device, geometry
     n = len(cases)
     if r0 is None:
@@ -223,7 +231,7 @@ def converge(gpu, cases, start: str, bits: int, r0=None, net=None, targets=(1e-4
                 finish(leave)
                 if leave.all():
                     break
-                s, idx = _move(gpu, s, cases, idx, ~leave, bits)
+                s, idx = _move(gpu, s, cases, idx, ~leave, bits, mg_amut)
                 moves += 1
         if max_seconds is not None and el > max_seconds:
             break

@@ -101,6 +101,9 @@ struct Solver {
   bool setup_done = false;
   int err = 0, err_b = 0, err_i = 0, err_j = 0;
   int dual_iflag1 = 0, dual_iflag = 0;
+  // extension, off by default: coarse levels keep an eddy viscosity
+  // restricted from the next finer level instead of the reference's zero
+  int mg_amut = 0;
 };
 
 // ----------------------------------------------------------------------------
@@ -1583,7 +1586,7 @@ int comput_residual_one_mesh(Solver &S, int nMesh) {
     // Residual, sub_Residual.f90:158-191
     if (S.If_viscous == 1) {
       get_viscous(S, B, F);
-      std::fill(B.Amu_t.v.begin(), B.Amu_t.v.end(), 0.0);
+      if (nMesh == 1 || !S.mg_amut) std::fill(B.Amu_t.v.begin(), B.Amu_t.v.end(), 0.0);
       if (MP.turb == Turb_BL) turbulence_bl(S, B, F);
       else if (MP.turb == Turb_SA) turbulence_sa(S, B, F);
       else if (MP.turb == Turb_SST) turbulence_sst(S, B, F);
@@ -1879,6 +1882,19 @@ void interpolation2h(Solver &S, int m1, int m2, int flag) {
             B2.QF(m, i, j) = B1.Res(m, i1, j1) + B1.Res(m, i1, j2) + B1.Res(m, i2, j1) + B1.Res(m, i2, j2);
         }
       }
+    // extension (mg_amut): the coarse eddy viscosity over 0..nx2, 0..ny2 is
+    // the mean of the children's within the finer level's 0..nx, 0..ny
+    // (a ghost cell's children are the finer level's ghost cells there)
+    if (flag == 1 && S.mg_amut && S.If_viscous == 1 && S.Iflag_turbulence_model != Turb_NONE)
+      for (int j = 0; j <= B2.ny; j++)
+        for (int i = 0; i <= B2.nx; i++) {
+          double sum = 0.0;
+          int n = 0;
+          for (int jj = 2 * j - 1; jj <= 2 * j; jj++)
+            for (int ii = 2 * i - 1; ii <= 2 * i; ii++)
+              if (ii >= 0 && ii <= B1.nx && jj >= 0 && jj <= B1.ny) { sum += B1.Amu_t(ii, jj); n++; }
+          B2.Amu_t(i, j) = sum / n;
+        }
   }
 }
 // fine/coarse smoother used inside the multigrid cycles (sub_NS_multigrid.f90:23-27,79-83)
@@ -1955,6 +1971,10 @@ int main_loop_step(Solver &S) {
 // init_flow_zero, sub_init.f90:423-495
 int init_flow_zero(Solver &S) {
   double d0 = 1.0, u0 = 1.0 * std::cos(S.AoA), v0 = 1.0 * std::sin(S.AoA), p0 = 1.0 / (S.gamma * S.Ma * S.Ma);
+  // coarse eddy viscosity (kept between residuals only with mg_amut): zero
+  // until the first restriction
+  for (int m = 2; m <= S.Num_Mesh; m++)
+    for (auto &B : S.mesh[m].B) std::fill(B.Amu_t.v.begin(), B.Amu_t.v.end(), 0.0);
   if (S.Nvar == 5)
     for (auto &B : S.mesh[1].B)
       for (int j = 1; j <= B.ny - 1; j++)
@@ -2067,6 +2087,10 @@ void *orc_new(const orc_params *p) {
   return S;
 }
 void orc_free(void *h) { delete (Solver *)h; }
+int orc_set_mg_amut(void *h, int enable) {
+  ((Solver *)h)->mg_amut = enable ? 1 : 0;
+  return 0;
+}
 void orc_set_threads(int n) {
 #ifdef _OPENMP
   omp_set_num_threads(n);

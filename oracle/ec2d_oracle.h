@@ -70,6 +70,9 @@ int orc_new_u(void *h, int mesh);
 int orc_forces(void *h, double *cl, double *cd, double *cm);
 int orc_wall_cf(void *h, int block, int sub, double *cf, double *xc, int maxn);
 int orc_last_error(void *h, int *blk, int *i, int *j);
+/* extension: coarse levels take the eddy viscosity restricted from the
+ * next finer level (the reference's coarse levels are laminar) */
+int orc_set_mg_amut(void *h, int enable);
 void orc_set_threads(int n);
 /* known-answer hooks: one face flux (sub_flux_split.f90) and one limiter
  * evaluation (scheme_fP side=0 / scheme_fm side=1, sub_Residual.f90:591-659) */

@@ -97,6 +97,7 @@ def lib(fast=False):
         L.orc_wall_cf.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp, dp, ctypes.c_int]
         L.orc_last_error.argtypes = [vp, ip, ip, ip]
         L.orc_set_threads.argtypes = [ctypes.c_int]
+        L.orc_set_mg_amut.argtypes = [vp, ctypes.c_int]
         L.orc_flux.argtypes = [ctypes.c_int, dp, dp, dp, ctypes.c_double]
         L.orc_scheme.argtypes = [ctypes.c_int] + [ctypes.c_double] * 4 + [ctypes.c_int]
         L.orc_scheme.restype = ctypes.c_double
@@ -231,6 +232,27 @@ class Oracle:
 
     def prolong(self, m1, m2, flag):
         self.L.orc_prolong(self.h, m1, m2, flag)
+
+    def set_mg_amut(self, enable=True):
+        """Extension: coarse levels keep the eddy viscosity restricted from
+        the next finer level (the reference zeroes it there)."""
+        self.L.orc_set_mg_amut(self.h, int(enable))
+
+    def force_function(self, mesh):
+        """QF -= Res (comput_force_function, sub_NS_multigrid.f90:156-173)."""
+        self.L.orc_force_function(self.h, mesh)
+
+    def set_un(self, mesh):
+        """Un = U (Set_Un, sub_NS_multigrid.f90:219-237)."""
+        self.L.orc_set_un(self.h, mesh)
+
+    def delt_u(self, mesh):
+        """deltU = U - Un (comput_delt_U, sub_NS_multigrid.f90:199-216)."""
+        self.L.orc_delt_u(self.h, mesh)
+
+    def new_u(self, mesh):
+        """U += deltU on the interior (comput_new_U, sub_NS_multigrid.f90:240-260)."""
+        self.L.orc_new_u(self.h, mesh)
 
     def forces(self):
         cl, cd, cm = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()

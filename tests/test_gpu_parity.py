@@ -313,6 +313,97 @@ def test_multigrid_cycles(gpu_lib, tm):
     compare_U(orc, g, tol=1e-9)
 
 
+def test_multigrid_eddy_viscosity_extension(gpu_lib):
+    """The coarse-level eddy viscosity extension (ec2d_mg_eddy_viscosity; the
+    oracle's set_mg_amut) on an SA case under the 3-level LU-SGS V-cycle:
+    the fine U after 4 V-cycles within the multigrid bound, the coarse
+    levels' eddy viscosity (restricted after the finer residual, then frozen)
+    within 1e-9 of its scale and not zero, and the default still laminar."""
+    p, bl = small_case(nx=65, ny=17, Ma=0.6, AoA=2.0, Re=1e6, If_viscous=1, Iflag_turbulence_model=2,
+                       Iflag_flux=4, Iflag_Scheme=5, first=2e-4, Num_Mesh=3, mg_lusgs=1, nblocks=2,
+                       Time_Method=0, CFL=2.0)
+    orc = make_oracle(p, bl)
+    orc.set_mg_amut(True)
+    orc.init_flow()
+    g = make_gpu(p, bl)
+    assert g.mg_eddy_viscosity() == 0
+    assert g.mg_eddy_viscosity(1) == 1
+    g.init_flow()
+    orc.step(4); g.step(4)
+    compare_U(orc, g, tol=1e-9)
+    for mesh in (2, 3):
+        compare_fields(orc, g, [8], mesh=mesh, tol=1e-9)
+        assert max(np.abs(g.field(1, mesh, b, 8)).max() for b in (1, 2)) > 0.0
+    g.close()
+    g = make_gpu(p, bl)
+    g.init_flow()
+    g.step(2)
+    assert max(np.abs(g.field(1, 2, b, 8)).max() for b in (1, 2)) == 0.0
+    g.close()
+
+
+@pytest.mark.parametrize("nblocks", [1, 2])
+def test_transfer_operators(gpu_lib, nblocks):
+    """Each multigrid transfer against the oracle's reference routines on
+    seeded random states (the operators are linear, so any state exercises
+    every weight), levels 1 <-> 2 and 2 <-> 3: interpolation2h flags 1 and 2;
+    the cycle's QF = sum Res_h - Res_2h (flag 6) against flag 2 then
+    comput_force_function; prolong_U flags 1 and 2 over fine cells 0..nx,
+    0..ny (the ghost ring included); the cycle's fused prolongation (flag 3)
+    against comput_delt_U, prolong_U flag 2 and comput_new_U.  Within 1e-14
+    of the field's largest value (FMA contraction on the GPU only)."""
+    p, bl = small_case(nx=65, ny=17, Ma=0.6, AoA=2.0, Num_Mesh=3, Time_Method=1, nblocks=nblocks)
+    orc = make_oracle(p, bl)
+    orc.init_flow()
+    g = make_gpu(p, bl)
+    g.init_flow()
+    rng = np.random.default_rng(11 + nblocks)
+    nb = len(bl)
+    F_RES, F_QF, F_DELTU, F_UN = 0, 19, 20, 21
+
+    def seed_U(mesh):
+        for b in range(1, nb + 1):
+            U = orc.get_U(mesh, b) * rng.uniform(0.8, 1.2, (orc.nvar(mesh), 1, 1)) + \
+                rng.uniform(-0.05, 0.05, orc.get_U(mesh, b).shape)
+            orc.set_U(mesh, b, U)
+            g.upload_U(1, mesh, b, U)
+
+    def seed_field(mesh, fid):
+        for b in range(1, nb + 1):
+            r = rng.standard_normal(orc.field(mesh, b, fid).size)
+            assert g.field(1, mesh, b, fid).size == r.size
+            orc.set_field(mesh, b, fid, r)
+            g.set_field(1, mesh, b, fid, r)
+
+    def same_field(mesh, fid):
+        for b in range(1, nb + 1):
+            a, c = orc.field(mesh, b, fid), g.field(1, mesh, b, fid)
+            assert a.shape == c.shape
+            np.testing.assert_allclose(c, a, rtol=0, atol=1e-14 * np.abs(a).max())
+
+    for f, c in ((1, 2), (2, 3)):
+        seed_U(f); seed_U(c)
+        orc.interpolation2h(f, c, 1); g.interpolation2h(f, c, 1)
+        compare_U(orc, g, mesh=c, tol=1e-14)
+        seed_field(f, F_RES); seed_field(c, F_RES); seed_field(c, F_QF)
+        orc.interpolation2h(f, c, 2); g.interpolation2h(f, c, 2)
+        same_field(c, F_QF)
+        orc.interpolation2h(f, c, 2); orc.force_function(c)
+        g.interpolation2h(f, c, 6)
+        same_field(c, F_QF)
+        seed_U(f); seed_U(c)
+        orc.prolong(c, f, 1); g.prolong(c, f, 1)
+        compare_U(orc, g, mesh=f, tol=1e-14)
+        seed_field(c, F_DELTU); seed_field(f, F_DELTU)
+        orc.prolong(c, f, 2); g.prolong(c, f, 2)
+        same_field(f, F_DELTU)
+        seed_U(f); seed_U(c); seed_field(c, F_UN); seed_field(f, F_DELTU)
+        orc.delt_u(c); orc.prolong(c, f, 2); orc.new_u(f)
+        g.prolong(c, f, 3)
+        same_field(f, F_DELTU)
+        compare_U(orc, g, mesh=f, tol=1e-14)
+
+
 def test_multigrid_viscous_lusgs_flat_plate(gpu_lib):
     from ec2d import cases
     p, bl = cases.laminar_flat_plate(33, 33, num_mesh=3)
@@ -352,6 +443,29 @@ def test_batch_equals_single(gpu_lib):
         for b in range(1, len(bl) + 1):
             np.testing.assert_array_equal(batch.download_U(ci, 1, b), one.download_U(1, 1, b))
         np.testing.assert_array_equal(batch.norms(ci)[1], one.norms(1)[1])
+
+
+def test_batch_equals_single_turbulent_multigrid(gpu_lib):
+    """Two SA cases under the 3-level LU-SGS V-cycle with the coarse eddy
+    viscosity kept (the polar's configuration), batched in one context and
+    each alone: U and norms bit-identical, so the batch's V-cycle counts are
+    the single runs'."""
+    from ec2d import gpu
+    kw = dict(Re=1e6, If_viscous=1, Iflag_turbulence_model=2, Iflag_flux=4, Iflag_Scheme=5, first=2e-4,
+              Num_Mesh=3, mg_lusgs=1, Time_Method=0, CFL=2.0)
+    cs = [small_case(Ma=0.6, AoA=1.0, **kw), small_case(nx=97, ny=17, Ma=0.7, AoA=3.0, nblocks=2, **kw)]
+    batch = gpu.Solver(cs)
+    batch.mg_eddy_viscosity(1)
+    batch.init_flow(); batch.step(6)
+    for ci, (p, bl) in enumerate(cs, start=1):
+        one = gpu.Solver([(p, bl)])
+        one.mg_eddy_viscosity(1)
+        one.init_flow(); one.step(6)
+        for b in range(1, len(bl) + 1):
+            np.testing.assert_array_equal(batch.download_U(ci, 1, b), one.download_U(1, 1, b))
+        np.testing.assert_array_equal(batch.norms(ci)[1], one.norms(1)[1])
+        one.close()
+    batch.close()
 
 
 def test_symmetric_airfoil_zero_lift(gpu_lib):

@@ -189,3 +189,27 @@ def test_flat_plate_converged_cf_is_blasius():
     assert np.max(np.abs(cf[m] / blasius - 1.0)) <= 0.03
     assert abs(fx["forces"]["cd"] / (1.328 / np.sqrt(1.0e4)) - 1.0) <= 0.05
     assert fx["reached"] and fx["iterations"] == 6751
+
+
+def test_mg_eddy_viscosity_keeps_turbulent_cycle_stable():
+    """A transonic SA case of the polar family (case 62: 257x65 C-grid,
+    M 0.716, AoA 6.35, Re 4.2e6) under the 3-level LU-SGS V-cycle from the
+    freestream: with laminar coarse levels (the reference's
+    Comput_Residual_one_mesh zeroes Amu_t, sub_Residual.f90:158-191) the
+    cycle stops on T < 1e-5 in the wake next to the cut after about 750
+    V-cycles (measured: 751); with the coarse levels keeping the eddy
+    viscosity restricted from the finer level it runs on."""
+    import oracle
+    from ec2d import cases
+    p, bl, _ = cases.polar_cases(64, with_tc=True)[62]
+    orc = oracle.Oracle(p, bl, threads=8, fast=True)
+    orc.init_flow()
+    with pytest.raises(RuntimeError, match="code 2"):
+        orc.step(1000)
+    orc = oracle.Oracle(p, bl, threads=8, fast=True)
+    orc.set_mg_amut(True)
+    orc.init_flow()
+    orc.step(1)
+    r0 = orc.norms()[1][0]
+    orc.step(999)
+    assert np.isfinite(orc.norms()[1][0]) and orc.norms()[1][0] < r0
