@@ -333,7 +333,7 @@ def merge_lusgs(kt):
     return sweep
 
 
-def residual_hbm(torch, gpu, dev, reps=10, forms=("chain", "tile"), grid=(2049, 1025)):
+def residual_hbm(torch, gpu, dev, reps=10, forms=("chain", "tile"), grid=(2049, 1025), transfer_reps=10):
     """Residual evaluation (Comput_Residual_one_mesh) on a grid far larger
     than L2: 2 blocks of 2049x1025 nodes (4.19 M cells; `grid` sets another
     size, e.g. a small one for instruction counts), laminar flat-plate
@@ -394,7 +394,7 @@ def residual_hbm(torch, gpu, dev, reps=10, forms=("chain", "tile"), grid=(2049, 
                       "fp64_issue_frac": inst_pc * cells / (total_ms / 1e3) / 1e12 / (fp64_peak / 2.0)})
         out[form] = r
     g.close()
-    out["transfers"] = transfer_hbm(torch, gpu, dev, p, blocks, hbm)
+    out["transfers"] = transfer_hbm(torch, gpu, dev, p, blocks, hbm, reps=transfer_reps)
     # the headline fields: the faster form
     best = min(forms, key=lambda f: out[f]["ms"])
     out["form"] = best
@@ -926,6 +926,7 @@ def main():
     ap.add_argument("--no-polar-mg-eddy-viscosity", dest="polar_mg_amut", action="store_false",
                     help="polar runs with laminar coarse levels, as the reference (default: the coarse levels keep "
                          "the restricted eddy viscosity, which keeps the turbulent V-cycle from diverging)")
+    ap.add_argument("--transfer-reps", type=int, default=10, help="timed launches per transfer form")
     ap.add_argument("--residual-grid", default="2049x1025",
                     help="nodes per block of the residual_hbm leg's 2-block flat plate (NXxNY)")
     ap.add_argument("--leg", default="all", choices=["all", "residual_hbm", "polar", "learned", "mlp"],
@@ -954,7 +955,8 @@ def main():
         import torch
         from ec2d import gpu
         if args.leg == "residual_hbm":
-            out = residual_hbm(torch, gpu, 0, grid=tuple(int(v) for v in args.residual_grid.split("x")))
+            out = residual_hbm(torch, gpu, 0, grid=tuple(int(v) for v in args.residual_grid.split("x")),
+                               transfer_reps=args.transfer_reps)
         elif args.leg == "polar":
             out = leg_polar(args)
         elif args.leg == "mlp":
