@@ -46,11 +46,13 @@ def warmstart_cases(n: int, seed: int, nx: int = 257, ny: int = 65, num_mesh: in
     return out
 
 
-def _solver(gpu, chunk, bits, mg_amut=False):
+def _solver(gpu, chunk, bits, mg_amut=False, configure=None):
     s = gpu.Solver([(p, b) for p, b, _ in chunk])
     s.set_lusgs_precision(bits)
     if mg_amut:
         s.mg_eddy_viscosity(1)
+    if configure is not None:
+        configure(s)
     for c, (_, _, tc) in enumerate(chunk, start=1):
         s.set_case_shape(c, tc)
     return s
@@ -122,7 +124,7 @@ def _rms(s, c):
         return float("nan")
 
 
-def _move(gpu, s, cases, idx, keep_mask, bits, mg_amut=False):
+def _move(gpu, s, cases, idx, keep_mask, bits, mg_amut=False, configure=None):
     """The cases of context `s` at positions keep_mask (original indices
     idx[keep_mask]) into a new context: their U, ghosts included, copied
     exactly, so their iteration continues bit for bit."""
@@ -130,7 +132,7 @@ def _move(gpu, s, cases, idx, keep_mask, bits, mg_amut=False):
     Us = [[s.download_U(k + 1, 1, b) for b in range(1, len(cases[c][1]) + 1)]
           for k, c in enumerate(idx) if keep_mask[k]]
     s.close()
-    s2 = _solver(gpu, [cases[c] for c in keep], bits, mg_amut)
+    s2 = _solver(gpu, [cases[c] for c in keep], bits, mg_amut, configure)
     s2.init_flow()
     for k, c in enumerate(keep):
         for b, U in enumerate(Us[k], start=1):
@@ -141,7 +143,7 @@ def _move(gpu, s, cases, idx, keep_mask, bits, mg_amut=False):
 def converge(gpu, cases, start: str, bits: int, r0=None, net=None, targets=(1e-4, 1e-6, 1e-8),
              max_steps: int = 30000, check: int = 50, max_seconds: float = None, retire: float = None,
              compact: float = 0.25, fallback_steps: int = 200, fallback_ratio: float = 100.0,
-             mg_amut: bool = False) -> Dict:
+             mg_amut: bool = False, configure=None) -> Dict:
     """Run all cases of `cases` in one context until every case's
     Res_rms(1) <= min(targets) x r0 or max_steps (r0: each case's
     freestream-start first residual, measured here when not given).
@@ -160,9 +162,11 @@ def converge(gpu, cases, start: str, bits: int, r0=None, net=None, targets=(1e-4
     freestream (its state replaced, its status cleared).
 
     mg_amut: coarse multigrid levels keep the restricted eddy viscosity
-    (ec2d_mg_eddy_viscosity) in every context of the run."""
+    (ec2d_mg_eddy_viscosity) in every context of the run; configure: a
+    callable applied to every context the run creates (e.g. the coarse
+    levels' flux precision)."""
     ts = time.perf_counter()
-    s = _solver(gpu, cases, bits, mg_amut)
+    s = _solver(gpu, cases, bits, mg_amut, configure)
     setup_s = time.perf_counter() - ts  # context set-up: grids to the device, geometry
     n = len(cases)
     if r0 is None:
@@ -231,7 +235,7 @@ def converge(gpu, cases, start: str, bits: int, r0=None, net=None, targets=(1e-4
                 finish(leave)
                 if leave.all():
                     break
-                s, idx = _move(gpu, s, cases, idx, ~leave, bits, mg_amut)
+                s, idx = _move(gpu, s, cases, idx, ~leave, bits, mg_amut, configure)
                 moves += 1
         if max_seconds is not None and el > max_seconds:
             break
