@@ -326,7 +326,8 @@ __device__ __forceinline__ void split_sw(double d, double u, double v, double cc
                                          double gamma, double *fp, double *fm) {
   double tmp1 = 2.0 * (gamma - 1.0), tmp3 = (3.0 - gamma) / (2.0 * (gamma - 1.0));
   double vs = A1 * u + A2 * v, ss = sqrt(A1 * A1 + A2 * A2);
-  double ak1 = A1 / ss, ak2 = A2 / ss;
+  const double rss = 1.0 / ss;
+  double ak1 = A1 * rss, ak2 = A2 * rss;
   double E1 = vs, E2 = vs - cc * ss, E3 = vs + cc * ss;
   double E1P = (E1 + fabs(E1)) * 0.5, E2P = (E2 + fabs(E2)) * 0.5, E3P = (E3 + fabs(E3)) * 0.5;
   double E1M = E1 - E1P, E2M = E2 - E2P, E3M = E3 - E3P;
@@ -354,46 +355,52 @@ __global__ void k_fdm_split(Lvl L) {
   const long long F = L.F;
   long long id = fidx(b, i, j);
   double d = L.q[Q_D * F + id], u = L.q[Q_U * F + id], v = L.q[Q_V * F + id], cc = L.q[Q_C * F + id];
-  double J = L.met[M_JAC * F + id];
+  const double rJ = 1.0 / L.met[M_JAC * F + id];  // one divide for the four metric quotients
   double fp[4], fm[4];
-  split_sw(d, u, v, cc, L.met[M_KX * F + id] / J, L.met[M_KY * F + id] / J, c.gamma, fp, fm);
+  split_sw(d, u, v, cc, L.met[M_KX * F + id] * rJ, L.met[M_KY * F + id] * rJ, c.gamma, fp, fm);
   for (int m = 0; m < 4; m++) { L.fdm[(D_SPI + m) * F + id] = fp[m]; L.fdm[(D_SPI + 4 + m) * F + id] = fm[m]; }
-  split_sw(d, u, v, cc, L.met[M_IX * F + id] / J, L.met[M_IY * F + id] / J, c.gamma, fp, fm);
+  split_sw(d, u, v, cc, L.met[M_IX * F + id] * rJ, L.met[M_IY * F + id] * rJ, c.gamma, fp, fm);
   for (int m = 0; m < 4; m++) { L.fdm[(D_SPJ + m) * F + id] = fp[m]; L.fdm[(D_SPJ + 4 + m) * F + id] = fm[m]; }
 }
 
 // fp_weno5 at point k (v[k-2..k+2]) and fm_weno5 producing hj(k-1) from v[k-2..k+2]
-__device__ __forceinline__ double weno5_p(double vm2, double vm1, double v0, double vp1, double vp2) {
+// (sub_Finite_Difference.f90:207-275).  The reference forms the weights as
+// a_k = C_k / (ep + S_k)^2 and W_k = a_k / sum(a), six divides per
+// evaluation; over the common denominator D_0 D_1 D_2 (D_k = (ep + S_k)^2)
+// the same weights are W_k = C_k prod_{l != k} D_l / sum_m C_m prod_{l != m} D_l,
+// one divide.  The results agree to a few ulps; an IEEE divide costs about a
+// dozen FP64 instructions, and the sixteen evaluations per cell made the
+// divides most of the kernel's FP64 work.  D_k lies in [1e-12, ~1e10], so the
+// products stay far inside the FP64 range.
+__device__ __forceinline__ double weno5_mix(double S0, double S1, double S2, double q03, double q13, double q23) {
   const double ep = 1.0e-6, C03 = 3.0 / 10.0, C13 = 3.0 / 5.0, C23 = 1.0 / 10.0;
+  const double D0 = (ep + S0) * (ep + S0), D1 = (ep + S1) * (ep + S1), D2 = (ep + S2) * (ep + S2);
+  const double n0 = C03 * (D1 * D2), n1 = C13 * (D0 * D2), n2 = C23 * (D0 * D1);
+  return (n0 * q03 + n1 * q13 + n2 * q23) / (n0 + n1 + n2);
+}
+__device__ __forceinline__ double weno5_p(double vm2, double vm1, double v0, double vp1, double vp2) {
   double t0 = v0 - 2.0 * vp1 + vp2, t1 = 3.0 * v0 - 4.0 * vp1 + vp2;
-  double S0 = 13.0 / 12.0 * (t0 * t0) + 1.0 / 4.0 * (t1 * t1);
+  const double S0 = 13.0 / 12.0 * (t0 * t0) + 1.0 / 4.0 * (t1 * t1);
   t0 = vm1 - 2.0 * v0 + vp1; t1 = vm1 - vp1;
-  double S1 = 13.0 / 12.0 * (t0 * t0) + 1.0 / 4.0 * (t1 * t1);
+  const double S1 = 13.0 / 12.0 * (t0 * t0) + 1.0 / 4.0 * (t1 * t1);
   t0 = vm2 - 2.0 * vm1 + v0; t1 = vm2 - 4.0 * vm1 + 3.0 * v0;
-  double S2 = 13.0 / 12.0 * (t0 * t0) + 1.0 / 4.0 * (t1 * t1);
-  double a0 = C03 / ((ep + S0) * (ep + S0)), a1 = C13 / ((ep + S1) * (ep + S1)), a2 = C23 / ((ep + S2) * (ep + S2));
-  double sum = a0 + a1 + a2;
-  double W0 = a0 / sum, W1 = a1 / sum, W2 = a2 / sum;
-  double q03 = 1.0 / 3.0 * v0 + 5.0 / 6.0 * vp1 - 1.0 / 6.0 * vp2;
-  double q13 = -1.0 / 6.0 * vm1 + 5.0 / 6.0 * v0 + 1.0 / 3.0 * vp1;
-  double q23 = 1.0 / 3.0 * vm2 - 7.0 / 6.0 * vm1 + 11.0 / 6.0 * v0;
-  return W0 * q03 + W1 * q13 + W2 * q23;
+  const double S2 = 13.0 / 12.0 * (t0 * t0) + 1.0 / 4.0 * (t1 * t1);
+  const double q03 = 1.0 / 3.0 * v0 + 5.0 / 6.0 * vp1 - 1.0 / 6.0 * vp2;
+  const double q13 = -1.0 / 6.0 * vm1 + 5.0 / 6.0 * v0 + 1.0 / 3.0 * vp1;
+  const double q23 = 1.0 / 3.0 * vm2 - 7.0 / 6.0 * vm1 + 11.0 / 6.0 * v0;
+  return weno5_mix(S0, S1, S2, q03, q13, q23);
 }
 __device__ __forceinline__ double weno5_m(double vm2, double vm1, double v0, double vp1, double vp2) {
-  const double ep = 1.0e-6, C03 = 3.0 / 10.0, C13 = 3.0 / 5.0, C23 = 1.0 / 10.0;
   double t0 = v0 - 2.0 * vm1 + vm2, t1 = 3.0 * v0 - 4.0 * vm1 + vm2;
-  double S0 = 13.0 / 12.0 * (t0 * t0) + 1.0 / 4.0 * (t1 * t1);
+  const double S0 = 13.0 / 12.0 * (t0 * t0) + 1.0 / 4.0 * (t1 * t1);
   t0 = vp1 - 2.0 * v0 + vm1; t1 = vp1 - vm1;
-  double S1 = 13.0 / 12.0 * (t0 * t0) + 1.0 / 4.0 * (t1 * t1);
+  const double S1 = 13.0 / 12.0 * (t0 * t0) + 1.0 / 4.0 * (t1 * t1);
   t0 = vp2 - 2.0 * vp1 + v0; t1 = vp2 - 4.0 * vp1 + 3.0 * v0;
-  double S2 = 13.0 / 12.0 * (t0 * t0) + 1.0 / 4.0 * (t1 * t1);
-  double a0 = C03 / ((ep + S0) * (ep + S0)), a1 = C13 / ((ep + S1) * (ep + S1)), a2 = C23 / ((ep + S2) * (ep + S2));
-  double sum = a0 + a1 + a2;
-  double W0 = a0 / sum, W1 = a1 / sum, W2 = a2 / sum;
-  double q03 = 1.0 / 3.0 * v0 + 5.0 / 6.0 * vm1 - 1.0 / 6.0 * vm2;
-  double q13 = -1.0 / 6.0 * vp1 + 5.0 / 6.0 * v0 + 1.0 / 3.0 * vm1;
-  double q23 = 1.0 / 3.0 * vp2 - 7.0 / 6.0 * vp1 + 11.0 / 6.0 * v0;
-  return W0 * q03 + W1 * q13 + W2 * q23;
+  const double S2 = 13.0 / 12.0 * (t0 * t0) + 1.0 / 4.0 * (t1 * t1);
+  const double q03 = 1.0 / 3.0 * v0 + 5.0 / 6.0 * vm1 - 1.0 / 6.0 * vm2;
+  const double q13 = -1.0 / 6.0 * vp1 + 5.0 / 6.0 * v0 + 1.0 / 3.0 * vm1;
+  const double q23 = 1.0 / 3.0 * vp2 - 7.0 / 6.0 * vp1 + 11.0 / 6.0 * v0;
+  return weno5_mix(S0, S1, S2, q03, q13, q23);
 }
 
 // WENO5 half-point fluxes (sub_Finite_Difference.f90:37-77) and the central
@@ -430,18 +437,18 @@ __global__ void k_fdm_flux(Lvl L) {
     double ui = 0.5 * (uu[id + 1] - uu[id - 1]), vi = 0.5 * (vv[id + 1] - vv[id - 1]), Ti = 0.5 * (TT[id + 1] - TT[id - 1]);
     double uj = 0.5 * (uu[id + P] - uu[id - P]), vj = 0.5 * (vv[id + P] - vv[id - P]), Tj = 0.5 * (TT[id + P] - TT[id - P]);
     double Akx = L.met[M_KX * F + id], Aky = L.met[M_KY * F + id], Aix = L.met[M_IX * F + id], Aiy = L.met[M_IY * F + id];
-    double J = L.met[M_JAC * F + id];
+    const double rJ = 1.0 / L.met[M_JAC * F + id];
     double ux = ui * Akx + uj * Aix, vx = vi * Akx + vj * Aix, Tx = Ti * Akx + Tj * Aix;
     double uy = ui * Aky + uj * Aiy, vy = vi * Aky + vj * Aiy, Ty = Ti * Aky + Tj * Aiy;
     double t11 = (4.0 / 3.0 * ux - 2.0 / 3.0 * vy) * mu0, t22 = (4.0 / 3.0 * vy - 2.0 / 3.0 * ux) * mu0;
     double t12 = (uy + vx) * mu0;
     double E1 = uu[id] * t11 + vv[id] * t12 + Ak0 * Tx, E2 = uu[id] * t12 + vv[id] * t22 + Ak0 * Ty;
-    L.fdm[(D_EV1 + 0) * F + id] = (Akx * t11 + Aky * t12) / J;
-    L.fdm[(D_EV1 + 1) * F + id] = (Akx * t12 + Aky * t22) / J;
-    L.fdm[(D_EV1 + 2) * F + id] = (Akx * E1 + Aky * E2) / J;
-    L.fdm[(D_EV2 + 0) * F + id] = (Aix * t11 + Aiy * t12) / J;
-    L.fdm[(D_EV2 + 1) * F + id] = (Aix * t12 + Aiy * t22) / J;
-    L.fdm[(D_EV2 + 2) * F + id] = (Aix * E1 + Aiy * E2) / J;
+    L.fdm[(D_EV1 + 0) * F + id] = (Akx * t11 + Aky * t12) * rJ;
+    L.fdm[(D_EV1 + 1) * F + id] = (Akx * t12 + Aky * t22) * rJ;
+    L.fdm[(D_EV1 + 2) * F + id] = (Akx * E1 + Aky * E2) * rJ;
+    L.fdm[(D_EV2 + 0) * F + id] = (Aix * t11 + Aiy * t12) * rJ;
+    L.fdm[(D_EV2 + 1) * F + id] = (Aix * t12 + Aiy * t22) * rJ;
+    L.fdm[(D_EV2 + 2) * F + id] = (Aix * E1 + Aiy * E2) * rJ;
   }
 }
 
