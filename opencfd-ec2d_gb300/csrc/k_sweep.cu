@@ -53,15 +53,15 @@ constexpr int TILE = EC2D_TILE;
 //       the reference multiplies the flux difference by +-0.5 s, and the
 //       normal flux is linear in n, so F_n(W, s) = 0.5 s F_n(W, n) and the
 //       constant half F_n(U_nb) of the difference moves into the record
-//  G1I..GCJ  NV = 4 only: (gamma - 1) times n1, n2 and cc of face i and j,
-//       the pressure coefficients of the four-lane sweep, which ships
+//  G1I..GCJ  NV = 4 and 5: (gamma - 1) times n1, n2 and cc of face i and j,
+//       the pressure coefficients of the multi-lane sweep, which ships
 //       p / (gamma - 1)
 template <int NV>
 struct Rec {
   static constexpr int A = 0, U = NV, C0 = 2 * NV, CI = 3 * NV, CJ = CI + 1, IA = CI + 2, IA5 = CI + 3,
                        N1I = CI + 4, N2I = CI + 5, N1J = CI + 6, N2J = CI + 7, G1I = CI + 8, G2I = CI + 9,
                        GCI = CI + 10, G1J = CI + 11, G2J = CI + 12, GCJ = CI + 13,
-                       N = (CI + 8 + (NV == 4 ? 6 : 0) + 1) / 2 * 2;
+                       N = (CI + 8 + (NV <= 5 ? 6 : 0) + 1) / 2 * 2;
   static_assert(N % 2 == 0, "records are whole 16-byte units");
 };
 
@@ -75,7 +75,8 @@ struct Slot {
   static_assert(S % 2 == 0, "slots are whole 16-byte units");
 };
 
-int lusgs_planes(int nv) { return 3 * nv + 10 + (nv == 4 ? 4 : 0); }  // at least Rec<NV>::N and the FP32 record
+// at least Rec<NV>::N (26, 30, 26 for NV = 4, 5, 6) and the FP32 record
+int lusgs_planes(int nv) { return 3 * nv + 10 + (nv == 4 ? 4 : nv == 5 ? 6 : 0); }
 
 // normal flux of the Euler part (+ convected turbulence variables), the F(U)
 // half of comput_DFn (sub_LU_SGS.f90:122-137)
@@ -177,7 +178,7 @@ __global__ void __launch_bounds__(TILE) k_lusgs_prep(Lvl L, double alfa1, int fo
       r[dir == 0 ? RC::CI : RC::CJ] = cc;
       r[dir == 0 ? RC::N1I : RC::N1J] = s1;
       r[dir == 0 ? RC::N2I : RC::N2J] = s2;
-      if (NV == 4) {
+      if (NV <= 5) {
         r[dir == 0 ? RC::G1I : RC::G1J] = gm1 * s1;
         r[dir == 0 ? RC::G2I : RC::G2J] = gm1 * s2;
         r[dir == 0 ? RC::GCI : RC::GCJ] = gm1 * cc;
@@ -192,7 +193,7 @@ __global__ void __launch_bounds__(TILE) k_lusgs_prep(Lvl L, double alfa1, int fo
     rb[RC::C0 + m] = K[1][m];
   }
 #pragma unroll
-  for (int k = RC::CI + 8 + (NV == 4 ? 6 : 0); k < RC::N; k++) rf[k] = rb[k] = 0.0;
+  for (int k = RC::CI + 8 + (NV <= 5 ? 6 : 0); k < RC::N; k++) rf[k] = rb[k] = 0.0;
   double2 *wf = reinterpret_cast<double2 *>(L.rec + cell * RC::N);
   double2 *wb = reinterpret_cast<double2 *>(L.rec + ((size_t)L.ncell + cell) * RC::N);
 #pragma unroll
@@ -563,7 +564,12 @@ constexpr int QWAIT = 1 << 20;   // polls of an inbox mbarrier before the wait g
 struct QRec {
   double a, u, c0, ki, kj;  // ki, kj: the lane's raw coefficient field of face i and j
   double2 c, ia, ni, nj;    // (0.5 Lc + Lv) i / j, 1/alfa, scaled normals of face i and j
+  double a4, u4, c04, ia5;  // NV = 5: the SA row's A, U, C0 and 1/(alfa + Lv)
 };
+// doubles per row of a slot and per inbox entry: rho, rho u, rho v, H (or E),
+// u, v, p / (gamma - 1), one spare; NV = 5 adds U + dU and dU of nu~
+template <int NV>
+constexpr int qslot() { return NV == 5 ? 10 : 8; }
 // per-lane record offsets of the pressure coefficient g_q: (gamma - 1) n1
 // (q = 1), n2 (q = 2), cc (q = 3, sign flipped below), any field for q = 0
 // (zeroed)
@@ -574,8 +580,9 @@ struct QLane {
   int offk, offn, offc;
   bool own;
 };
+template <int NV = 4>
 __device__ __forceinline__ QLane qlane(int q, bool own = true) {
-  using RC = Rec<4>;
+  using RC = Rec<NV>;
   QLane l;
   l.offi = q == 1 ? RC::G1I : q == 2 ? RC::G2I : RC::GCI;
   l.offj = q == 1 ? RC::G1J : q == 2 ? RC::G2J : RC::GCJ;
@@ -593,15 +600,25 @@ __device__ __forceinline__ double qcoef(double x, const QLane &l) {
 }
 // four lanes per row load both faces' fields; eight load their half's face
 // only (into ki, ni, c.x) and the fields their half uses
-template <bool FWD, bool update, int LPR = 4>
+template <bool FWD, bool update, int LPR = 4, int NV = 4>
 __device__ __forceinline__ void qload(QRec &r, const double *rec, int q, const QLane &l) {
-  using RC = Rec<4>;
+  using RC = Rec<NV>;
   if (LPR == 8) {
     if (!FWD || l.own) r.a = __ldcg(rec + RC::A + q);
     if (FWD || !update) r.u = __ldcg(rec + RC::U + q);
     if (!FWD && l.own) r.c0 = __ldcg(rec + RC::C0 + q);
     r.ki = __ldcg(rec + l.offk);
-    r.ni = __ldcg(reinterpret_cast<const double2 *>(rec + l.offn));
+    if (NV == 5) {
+      // the normals sit at odd offsets of a 5-variable record: two 8-byte loads
+      r.ni.x = __ldcg(rec + l.offn);
+      r.ni.y = __ldcg(rec + l.offn + 1);
+      r.a4 = __ldcg(rec + RC::A + 4);
+      r.u4 = __ldcg(rec + RC::U + 4);
+      if (!FWD) r.c04 = __ldcg(rec + RC::C0 + 4);
+      r.ia5 = __ldcg(rec + RC::IA5);
+    } else {
+      r.ni = __ldcg(reinterpret_cast<const double2 *>(rec + l.offn));
+    }
     r.c.x = __ldcg(rec + l.offc);
     r.ia.x = __ldcg(rec + RC::IA);
     return;
@@ -621,10 +638,10 @@ __device__ __forceinline__ void qload(QRec &r, const double *rec, int q, const Q
 // the entry's mbarrier in the receiving CTA: no fence on the sending side.
 // The receiver arms every entry's mbarrier at start-up (one arrival expecting
 // 64 bytes), so phase 0 completes when the entry has landed.
-__device__ __forceinline__ void qarm(unsigned long long *mb) {
+__device__ __forceinline__ void qarm(unsigned long long *mb, unsigned bytes) {
   const unsigned a = (unsigned)__cvta_generic_to_shared(mb);
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(1) : "memory");
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(64) : "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
 }
 // bounded wait for an inbox entry (phase 0 of its mbarrier); false: gave up
 __device__ __forceinline__ bool qwait(const unsigned long long *mb) {
@@ -660,14 +677,19 @@ struct QBand {
 // has three planes to arrive, enough for a read that crosses to the other
 // die's L2.  The band-edge state goes to the next band by st.async, its
 // bytes counted on the receiving entry's mbarrier (no fence on this side).
-template <bool update, bool FWD, int LPR>
+// NV = 5 (eight lanes only): every lane also carries the SA row, the
+// upstream neighbour of its half adding F_n(nu~_2) + (0.5 Lc + Lv) dnu~ as
+// the one-lane sweep does; lane q = 0 of the leading half stores it.
+template <bool update, bool FWD, int LPR, int NV = 4>
 __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBand &B, double *slot, double *inbox,
                                       unsigned long long *mbar, unsigned rbox, unsigned rmbar, const double *rsrc,
                                       double *recBw, double gm1) {
-  using RC = Rec<4>;
+  using RC = Rec<NV>;
+  constexpr int QS = qslot<NV>();
+  static_assert(NV == 4 || LPR == 8, "the SA row rides on the eight-lane form only");
   const int R = B.R, rl = B.rl, q = B.q, j = B.j, rows = B.rows, ni = B.ni;
   const long long F = L.F;
-  const QLane ln = qlane(q, LPR == 4 || !((threadIdx.x >> 2) & 1));
+  const QLane ln = qlane<NV>(q, LPR == 4 || !((threadIdx.x >> 2) & 1));
   // this row's neighbour across the band edge comes through the inbox; the
   // band's edge row feeds the next band's inbox
   const bool from_box = B.row_ok && (FWD ? (rl == 0 && B.rank > 0) : (rl == R - 1 && (int)B.rank + 1 < B.CS && j < rows));
@@ -686,13 +708,14 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
     for (int c = 0; c < 3; c++) {
       if (c >= ni) break;
       const int m = (m0 + c) & 3;
-      if (m == 0) qload<FWD, update, LPR>(r0, src(c), q, ln);
-      else if (m == 1) qload<FWD, update, LPR>(r1, src(c), q, ln);
-      else if (m == 2) qload<FWD, update, LPR>(r2, src(c), q, ln);
-      else qload<FWD, update, LPR>(r3, src(c), q, ln);
+      if (m == 0) qload<FWD, update, LPR, NV>(r0, src(c), q, ln);
+      else if (m == 1) qload<FWD, update, LPR, NV>(r1, src(c), q, ln);
+      else if (m == 2) qload<FWD, update, LPR, NV>(r2, src(c), q, ln);
+      else qload<FWD, update, LPR, NV>(r3, src(c), q, ln);
     }
   }
   double wx = 0.0, wu = 0.0, wv = 0.0, wp = 0.0;  // the row's previous cell
+  double wt = 0.0, wd = 0.0;                        // and its nu~ + dnu~, dnu~ (NV = 5)
   int gave_up = 0;                                 // first column whose inbox wait gave up
   const int gl = (threadIdx.x & 31) & ~(LPR - 1);  // the row's first lane
   // eight lanes per row: lanes 0-3 take the row's own previous cell, lanes
@@ -704,8 +727,8 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
     const int i = p - j, buf = p & 1;
     const bool act = B.row_ok && i >= 1 && i <= ni;
     const int k = FWD ? i - 1 : ni - i;
-    if (act && k + 3 < ni) qload<FWD, update, LPR>(ahead, src(k + 3), q, ln);
-    double acc = 0.0;
+    if (act && k + 3 < ni) qload<FWD, update, LPR, NV>(ahead, src(k + 3), q, ln);
+    double acc = 0.0, acc4 = 0.0;
     if (act) {
       if (LPR == 4) {
         acc = FWD ? cur.a : cur.c0;
@@ -719,9 +742,9 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
             // after one wait has given up the row no longer waits (its results
             // are void; the step reports EC2D_ERR_TIMEOUT)
             if (!gave_up && !qwait(mbar + i - 1)) gave_up = i;
-            s = inbox + (size_t)(i - 1) * 8;
+            s = inbox + (size_t)(i - 1) * QS;
           } else {
-            s = slot + ((size_t)(buf ^ 1) * R + (FWD ? rl - 1 : rl + 1)) * 8;
+            s = slot + ((size_t)(buf ^ 1) * R + (FWD ? rl - 1 : rl + 1)) * QS;
           }
           const double2 uv = *reinterpret_cast<const double2 *>(s + 4);
           const double sp = s[6], sx = s[q];
@@ -730,10 +753,10 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
         }
       } else {
         // both halves run the same FP64 instructions on their own operands
-        const double *s = slot + ((size_t)(buf ^ 1) * R + min(max(FWD ? rl - 1 : rl + 1, 0), R - 1)) * 8;
+        const double *s = slot + ((size_t)(buf ^ 1) * R + min(max(FWD ? rl - 1 : rl + 1, 0), R - 1)) * QS;
         if (row_nb && from_box) {
           if (!gave_up && !qwait(mbar + i - 1)) gave_up = i;
-          s = inbox + (size_t)(i - 1) * 8;
+          s = inbox + (size_t)(i - 1) * QS;
         }
         const double2 uv = *reinterpret_cast<const double2 *>(s + 4);
         const double sp = s[6], sx = s[q];
@@ -741,17 +764,33 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
         const double X = own_nb ? wx : sx, Uu = own_nb ? wu : uv.x, Vv = own_nb ? wv : uv.y, P = own_nb ? wp : sp;
         // the record fields of this half's face (loaded per half)
         acc = own_nb ? (FWD ? cur.a : cur.c0) : 0.0;
+        if (NV == 5) acc4 = own_nb ? (FWD ? cur.a4 : cur.c04) : 0.0;
         if (has) {
           const double w = fma(Uu, cur.ni.x, fma(Vv, cur.ni.y, cur.c.x));
           acc = fma(X, w, fma(P, qcoef(cur.ki, ln), acc));
+          if (NV == 5) {
+            // F_n(nu~_2) + (0.5 Lc + Lv) dnu~: the dissipation on the
+            // increment, as the one-lane sweep (add_shipped) forms it
+            const double T2 = own_nb ? wt : s[7], D2 = own_nb ? wd : s[8];
+            const double un = fma(Uu, cur.ni.x, Vv * cur.ni.y);
+            acc4 = fma(cur.c.x, D2, fma(T2, un, acc4));
+          }
         }
       }
     }
     // eight lanes: the two halves of the row add their neighbours' terms
     const double other = LPR == 8 ? __shfl_xor_sync(0xffffffffu, acc, 4) : 0.0;
-    double st = 0.0, dn = 0.0;
+    const double other4 = NV == 5 ? __shfl_xor_sync(0xffffffffu, acc4, 4) : 0.0;
+    double st = 0.0, dn = 0.0, st4 = 0.0, dn4 = 0.0;
     if (act) {
       if (LPR == 8) acc = acc + other;
+      if (NV == 5) {
+        // the SA row never takes the fused U update (the reference adds dU
+        // after the sweep; only the mean flow is carried as U + dU)
+        acc4 = acc4 + other4;
+        dn4 = FWD ? acc4 * cur.ia5 : fma(acc4, cur.ia5, cur.a4);
+        st4 = cur.u4 + dn4;
+      }
       if (update) {
         // U + dU* going forward (carried in the backward record), U + dU* + dU** going backward
         st = fma(acc, cur.ia.x, FWD ? cur.u : cur.a);
@@ -769,26 +808,39 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
       const double H = fma(gm1, pr, s3);
       const double x = q == 3 ? H : st;
       if (to_box && lead && q == 0) {
-        const unsigned a = rbox + 64u * (unsigned)(i - 1), m = rmbar + 8u * (unsigned)(i - 1);
+        const unsigned a = rbox + 8u * QS * (unsigned)(i - 1), m = rmbar + 8u * (unsigned)(i - 1);
         qsend2(a, s0, s1, m);
         qsend2(a + 16u, s2, H, m);
         qsend2(a + 32u, u, v, m);
-        qsend2(a + 48u, pr, 0.0, m);
+        if (NV == 5) {
+          qsend2(a + 48u, pr, st4, m);
+          qsend2(a + 64u, dn4, 0.0, m);
+        } else {
+          qsend2(a + 48u, pr, 0.0, m);
+        }
       }
-      double *o = slot + ((size_t)buf * R + rl) * 8;
+      double *o = slot + ((size_t)buf * R + rl) * QS;
       if (lead) o[q] = x;
       if (lead && q == 0) *reinterpret_cast<double2 *>(o + 4) = make_double2(u, v);
       if (lead && q == 1) o[6] = pr;
+      if (NV == 5 && lead && q == 2) *reinterpret_cast<double2 *>(o + 8) = make_double2(dn4, 0.0);
+      if (NV == 5 && lead && q == 3) o[7] = st4;
       wx = x; wu = u; wv = v; wp = pr;
+      wt = st4; wd = dn4;
       if (lead) {
         if (FWD) {
           recBw[(size_t)(i - 1) * RC::N + RC::A + q] = update ? st : dn;
+          if (NV == 5 && q == 0) recBw[(size_t)(i - 1) * RC::N + RC::A + 4] = dn4;
         } else {
           // an updating sweep writes U only (DU is read nowhere but inside
           // du_LU_SGS_2D and the update that follows it)
           const long long id = bd.off + (long long)(j + 2) * bd.P + (i + 2);
           if (update) L.U[q * F + id] = st;
           else L.du[q * F + id] = dn;
+          if (NV == 5 && q == 0) {
+            if (update) L.U[4 * F + id] = st4;
+            else L.du[4 * F + id] = dn4;
+          }
         }
       }
     }
@@ -804,9 +856,11 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
   if (gave_up) set_status(L.status + 4 * bd.cas, 4, B.bk, gave_up, j);
 }
 
-template <bool update, int LPR>
+template <bool update, int LPR, int NV = 4>
 __global__ void __launch_bounds__(4 * QROWS, 1) k_lusgs_sweep_quad(Lvl L, int R, int CS) {
-  extern __shared__ __align__(16) double sh[];  // [2][R][8] slots | inbox F [ni][8] | inbox B | mbarriers F [ni] | B
+  // [2][R][QS] slots | inbox F [ni][QS] | inbox B | mbarriers F [ni] | B
+  extern __shared__ __align__(16) double sh[];
+  constexpr int QS = qslot<NV>();
   QBand B;
   B.rank = CS > 1 ? cluster_rank() : 0u;
   B.bk = blockIdx.x / CS;
@@ -821,27 +875,27 @@ __global__ void __launch_bounds__(4 * QROWS, 1) k_lusgs_sweep_quad(Lvl L, int R,
   const int ni = B.ni;
   const double gm1 = L.cs[bd.cas].gamma - 1.0;
   double *slot = sh;
-  double *inF = sh + (size_t)2 * R * 8, *inB = inF + (size_t)ni * 8;
-  unsigned long long *mbF = reinterpret_cast<unsigned long long *>(inB + (size_t)ni * 8), *mbB = mbF + ni;
+  double *inF = sh + (size_t)2 * R * QS, *inB = inF + (size_t)ni * QS;
+  unsigned long long *mbF = reinterpret_cast<unsigned long long *>(inB + (size_t)ni * QS), *mbB = mbF + ni;
   unsigned rboxF = 0, rmbF = 0, rboxB = 0, rmbB = 0;
   if (CS > 1) {
-    for (int t = threadIdx.x; t < 2 * ni; t += blockDim.x) qarm(mbF + t);
+    for (int t = threadIdx.x; t < 2 * ni; t += blockDim.x) qarm(mbF + t, 8u * QS);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     if ((int)B.rank + 1 < CS) { rboxF = remote_smem(inF, B.rank + 1); rmbF = remote_smem(mbF, B.rank + 1); }
     if (B.rank > 0) { rboxB = remote_smem(inB, B.rank - 1); rmbB = remote_smem(mbB, B.rank - 1); }
     cluster_barrier();  // every inbox armed before any CTA writes into one
   }
   const int jr = B.row_ok ? B.j : 1;  // record pointers of idle rows stay in the array
-  const double *recF = L.rec + ((size_t)bd.cell0 + (size_t)(jr - 1) * ni) * Rec<4>::N;
-  const double *recB = recF + (size_t)L.ncell * Rec<4>::N;
-  double *recBw = L.rec + ((size_t)L.ncell + bd.cell0 + (size_t)(jr - 1) * ni) * Rec<4>::N;
-  qpass<update, true, LPR>(L, bd, B, slot, inF, mbF, rboxF, rmbF, recF, recBw, gm1);
-  qpass<update, false, LPR>(L, bd, B, slot, inB, mbB, rboxB, rmbB, recB, recBw, gm1);
+  const double *recF = L.rec + ((size_t)bd.cell0 + (size_t)(jr - 1) * ni) * Rec<NV>::N;
+  const double *recB = recF + (size_t)L.ncell * Rec<NV>::N;
+  double *recBw = L.rec + ((size_t)L.ncell + bd.cell0 + (size_t)(jr - 1) * ni) * Rec<NV>::N;
+  qpass<update, true, LPR, NV>(L, bd, B, slot, inF, mbF, rboxF, rmbF, recF, recBw, gm1);
+  qpass<update, false, LPR, NV>(L, bd, B, slot, inB, mbB, rboxB, rmbB, recB, recBw, gm1);
   if (CS > 1) cluster_barrier();  // no CTA leaves while a neighbour may still write into it
 }
 
-// the four- and eight-lane kernel serves NV = 4 levels whose blocks have at
-// most 16 bands of rows and QCOLS cells per row, when every CTA of the launch
+// the four- and eight-lane kernel serves NV = 4 levels (and NV = 5 with eight
+// lanes) whose blocks have at most 16 bands of rows and QCOLS cells per row, when every CTA of the launch
 // gets an SM of its own (with fewer SMs, one lane per row needs fewer FP64
 // instructions) and the device can hold one of its clusters
 // rmax: most rows per CTA (4..32); lanes: lanes per row (4 or 8; 0: eight up
@@ -852,28 +906,31 @@ int quad_ctas(int max_rows, int rmax) {
   return (max_rows + rmax - 1) / rmax;
 }
 static int quad_lanes(int rmax, int lanes) { return lanes == 4 || lanes == 8 ? lanes : (rmax <= 16 ? 8 : 4); }
-static void (*quad_kernel(int lpr, int update))(Lvl, int, int) {
+static void (*quad_kernel(int lpr, int update, int nv))(Lvl, int, int) {
+  if (nv == 5) return update ? k_lusgs_sweep_quad<true, 8, 5> : k_lusgs_sweep_quad<false, 8, 5>;
   return lpr == 8 ? (update ? k_lusgs_sweep_quad<true, 8> : k_lusgs_sweep_quad<false, 8>)
                   : (update ? k_lusgs_sweep_quad<true, 4> : k_lusgs_sweep_quad<false, 4>);
 }
 struct QuadShape {
-  int CS, R, lpr, th;
+  int CS, R, lpr, th, nv;
   size_t smem;
 };
-static QuadShape quad_shape(int max_rows, int max_cols, int rmax, int lanes) {
+static QuadShape quad_shape(int max_rows, int max_cols, int rmax, int lanes, int nv) {
   QuadShape q;
   q.CS = quad_ctas(max_rows, rmax);
   q.R = (max_rows + q.CS - 1) / q.CS;
-  q.lpr = quad_lanes(rmax, lanes);
+  q.lpr = nv == 5 ? 8 : quad_lanes(rmax, lanes);
+  q.nv = nv;
   q.th = (q.lpr * q.R + 31) / 32 * 32;
-  q.smem = (size_t)2 * q.R * 8 * sizeof(double) + (q.CS > 1 ? (size_t)max_cols * 2 * (8 * sizeof(double) + 8) : 0);
+  const size_t qs = nv == 5 ? 10 : 8;  // qslot<NV>()
+  q.smem = (size_t)2 * q.R * qs * sizeof(double) + (q.CS > 1 ? (size_t)max_cols * 2 * (qs * sizeof(double) + 8) : 0);
   return q;
 }
 // the kernel's attributes for a launch of this shape (dynamic shared memory
 // beyond 48 KiB, cluster sizes beyond 8)
 static void quad_attributes(const QuadShape &q) {
   for (int update = 0; update < 2; update++) {
-    auto kern = quad_kernel(q.lpr, update);
+    auto kern = quad_kernel(q.lpr, update, q.nv);
     if (q.smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)q.smem);
     if (q.CS > 8) cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   }
@@ -885,8 +942,10 @@ bool quad_fits(const Lvl &L, int max_rows, int max_cols, int rmax, int lanes) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   }
-  const QuadShape q = quad_shape(max_rows, max_cols, rmax, lanes);
-  if (!(L.nvar == 4 && max_rows >= 1 && q.CS <= 16 && max_cols <= QCOLS && L.nblk * q.CS <= nsm)) return false;
+  const QuadShape q = quad_shape(max_rows, max_cols, rmax, lanes, L.nvar);
+  // NV = 5 rides on eight lanes per row, so at most 16 rows per band
+  const bool nv_ok = L.nvar == 4 || (L.nvar == 5 && std::max(4, std::min(rmax, QROWS)) <= 16 && lanes != 4);
+  if (!(nv_ok && max_rows >= 1 && q.CS <= 16 && max_cols <= QCOLS && L.nblk * q.CS <= nsm)) return false;
   if (q.CS <= 8) return true;
   // a non-portable cluster size: launchable only if the device can place one
   quad_attributes(q);
@@ -902,7 +961,7 @@ bool quad_fits(const Lvl &L, int max_rows, int max_cols, int rmax, int lanes) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   int nclusters = 0;
-  const bool ok = cudaOccupancyMaxActiveClusters(&nclusters, quad_kernel(q.lpr, 1), &cfg) == cudaSuccess &&
+  const bool ok = cudaOccupancyMaxActiveClusters(&nclusters, quad_kernel(q.lpr, 1, q.nv), &cfg) == cudaSuccess &&
                   nclusters >= 1;
   cudaGetLastError();  // a refused query leaves no error behind
   return ok;
@@ -910,9 +969,9 @@ bool quad_fits(const Lvl &L, int max_rows, int max_cols, int rmax, int lanes) {
 
 // eight lanes per row: 15 FP64 operations per cell and lane; four: 18
 void launch_quad(const Lvl &L, int update, int max_rows, int max_cols, int rmax, int lanes, cudaStream_t s) {
-  const QuadShape q = quad_shape(max_rows, max_cols, rmax, lanes);
+  const QuadShape q = quad_shape(max_rows, max_cols, rmax, lanes, L.nvar);
   quad_attributes(q);
-  auto kern = quad_kernel(q.lpr, update);
+  auto kern = quad_kernel(q.lpr, update, q.nv);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(L.nblk * q.CS);
   cfg.blockDim = dim3(q.th);
