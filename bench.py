@@ -650,6 +650,43 @@ def leg_mlp(args):
     return out
 
 
+def leg_rans(args):
+    """The RANS workload (4-block 513x129 NACA 2412, M 0.73, AoA 2.8,
+    Re 6.5e6, Roe, MUSCL3, WENO5 patch on every block, 3-level V-cycle,
+    LU-SGS, FP64) with SA and with SST, each with the reference's laminar
+    coarse levels and with the coarse eddy viscosity kept: ms per V-cycle
+    (20 V-cycles after 20, CUDA graphs, CUDA events on the context's
+    stream) and per kernel (10 V-cycles with per-kernel event timing)."""
+    import torch
+    from ec2d import cases, gpu
+    out = {}
+    for turb, name in ((2, "sa"), (3, "sst")):
+        p, bl, fdm = cases.rans_naca2412(turb=turb)
+        for amut in (0, 1):
+            g = gpu.Solver([(p, bl)], fdm_blocks=[fdm])
+            g.mg_eddy_viscosity(amut)
+            g.init_flow()
+            g.step(20)
+            g.sync()
+            st = torch.cuda.ExternalStream(g.stream_handle())
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            g.step(20)
+            e1.record(st)
+            e1.synchronize()
+            g.kernel_timing(True)
+            g.step(10)
+            kt = g.kernel_times()
+            g.kernel_timing(False)
+            out[f"{name}{'_mg_eddy_viscosity' if amut else ''}"] = {
+                "ms_per_vcycle": e0.elapsed_time(e1) / 20,
+                "kernels_ms_per_vcycle": {f"{n}@{l}": round(v[2] / 10, 4)
+                                          for (n, l), v in sorted(kt.items(), key=lambda kv: -kv[1][2])[:12]},
+                "cells": fine_cells(bl), "lusgs_shape": g.lusgs_shape()}
+            g.close()
+    return out
+
+
 def leg_learned(args):
     """Learned warm start (512 training + 64 held-out SA cases on a 257x65
     C-grid): data generation, training, and the held-out polar to a 1e-8 drop
@@ -929,7 +966,7 @@ def main():
     ap.add_argument("--transfer-reps", type=int, default=10, help="timed launches per transfer form")
     ap.add_argument("--residual-grid", default="2049x1025",
                     help="nodes per block of the residual_hbm leg's 2-block flat plate (NXxNY)")
-    ap.add_argument("--leg", default="all", choices=["all", "residual_hbm", "polar", "learned", "mlp"],
+    ap.add_argument("--leg", default="all", choices=["all", "residual_hbm", "polar", "learned", "mlp", "rans"],
                     help="residual_hbm: the 4.19 M-cell residual alone (for profiling); polar: the 64-case "
                          "batched polar; learned: the learned warm start end to end")
     ap.add_argument("--no-polar", dest="polar", action="store_false",
@@ -961,6 +998,8 @@ def main():
             out = leg_polar(args)
         elif args.leg == "mlp":
             out = leg_mlp(args)
+        elif args.leg == "rans":
+            out = leg_rans(args)
         else:
             out = leg_learned(args)
         print(json.dumps({args.leg: out}, default=float), flush=True)
