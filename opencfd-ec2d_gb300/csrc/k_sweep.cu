@@ -53,7 +53,7 @@ constexpr int TILE = EC2D_TILE;
 //       the reference multiplies the flux difference by +-0.5 s, and the
 //       normal flux is linear in n, so F_n(W, s) = 0.5 s F_n(W, n) and the
 //       constant half F_n(U_nb) of the difference moves into the record
-//  G1I..GCJ  NV = 4 and 5: (gamma - 1) times n1, n2 and cc of face i and j,
+//  G1I..GCJ  (gamma - 1) times n1, n2 and cc of face i and j,
 //       the pressure coefficients of the multi-lane sweep, which ships
 //       p / (gamma - 1)
 template <int NV>
@@ -61,7 +61,7 @@ struct Rec {
   static constexpr int A = 0, U = NV, C0 = 2 * NV, CI = 3 * NV, CJ = CI + 1, IA = CI + 2, IA5 = CI + 3,
                        N1I = CI + 4, N2I = CI + 5, N1J = CI + 6, N2J = CI + 7, G1I = CI + 8, G2I = CI + 9,
                        GCI = CI + 10, G1J = CI + 11, G2J = CI + 12, GCJ = CI + 13,
-                       N = (CI + 8 + (NV <= 5 ? 6 : 0) + 1) / 2 * 2;
+                       N = (CI + 8 + 6 + 1) / 2 * 2;
   static_assert(N % 2 == 0, "records are whole 16-byte units");
 };
 
@@ -75,8 +75,9 @@ struct Slot {
   static_assert(S % 2 == 0, "slots are whole 16-byte units");
 };
 
-// at least Rec<NV>::N (26, 30, 26 for NV = 4, 5, 6) and the FP32 record
-int lusgs_planes(int nv) { return 3 * nv + 10 + (nv == 4 ? 4 : nv == 5 ? 6 : 0); }
+// at least Rec<NV>::N (26, 30, 32 for NV = 4, 5, 6) and the FP32 record
+int lusgs_planes(int nv) { return 3 * nv + 15; }
+static_assert(Rec<4>::N <= 3 * 4 + 15 && Rec<5>::N <= 3 * 5 + 15 && Rec<6>::N <= 3 * 6 + 15, "record planes");
 
 // normal flux of the Euler part (+ convected turbulence variables), the F(U)
 // half of comput_DFn (sub_LU_SGS.f90:122-137)
@@ -178,7 +179,7 @@ __global__ void __launch_bounds__(TILE) k_lusgs_prep(Lvl L, double alfa1, int fo
       r[dir == 0 ? RC::CI : RC::CJ] = cc;
       r[dir == 0 ? RC::N1I : RC::N1J] = s1;
       r[dir == 0 ? RC::N2I : RC::N2J] = s2;
-      if (NV <= 5) {
+      {
         r[dir == 0 ? RC::G1I : RC::G1J] = gm1 * s1;
         r[dir == 0 ? RC::G2I : RC::G2J] = gm1 * s2;
         r[dir == 0 ? RC::GCI : RC::GCJ] = gm1 * cc;
@@ -193,7 +194,7 @@ __global__ void __launch_bounds__(TILE) k_lusgs_prep(Lvl L, double alfa1, int fo
     rb[RC::C0 + m] = K[1][m];
   }
 #pragma unroll
-  for (int k = RC::CI + 8 + (NV <= 5 ? 6 : 0); k < RC::N; k++) rf[k] = rb[k] = 0.0;
+  for (int k = RC::CI + 8 + 6; k < RC::N; k++) rf[k] = rb[k] = 0.0;
   double2 *wf = reinterpret_cast<double2 *>(L.rec + cell * RC::N);
   double2 *wb = reinterpret_cast<double2 *>(L.rec + ((size_t)L.ncell + cell) * RC::N);
 #pragma unroll
@@ -564,12 +565,14 @@ constexpr int QWAIT = 1 << 20;   // polls of an inbox mbarrier before the wait g
 struct QRec {
   double a, u, c0, ki, kj;  // ki, kj: the lane's raw coefficient field of face i and j
   double2 c, ia, ni, nj;    // (0.5 Lc + Lv) i / j, 1/alfa, scaled normals of face i and j
-  double a4, u4, c04, ia5;  // NV = 5: the SA row's A, U, C0 and 1/(alfa + Lv)
+  double at[2], ut[2], c0t[2];  // NV = 5, 6: the turbulence rows' A, U and C0
+  double ia5;                   // NV = 5: 1/(alfa + Lv) of the SA row
 };
 // doubles per row of a slot and per inbox entry: rho, rho u, rho v, H (or E),
-// u, v, p / (gamma - 1), one spare; NV = 5 adds U + dU and dU of nu~
+// u, v, p / (gamma - 1), one spare; then U + dU and dU of each turbulence
+// variable (NV = 5: nu~; 6: k, omega)
 template <int NV>
-constexpr int qslot() { return NV == 5 ? 10 : 8; }
+constexpr int qslot() { return 8 + 2 * (NV - 4); }
 // per-lane record offsets of the pressure coefficient g_q: (gamma - 1) n1
 // (q = 1), n2 (q = 2), cc (q = 3, sign flipped below), any field for q = 0
 // (zeroed)
@@ -612,12 +615,15 @@ __device__ __forceinline__ void qload(QRec &r, const double *rec, int q, const Q
       // the normals sit at odd offsets of a 5-variable record: two 8-byte loads
       r.ni.x = __ldcg(rec + l.offn);
       r.ni.y = __ldcg(rec + l.offn + 1);
-      r.a4 = __ldcg(rec + RC::A + 4);
-      r.u4 = __ldcg(rec + RC::U + 4);
-      if (!FWD) r.c04 = __ldcg(rec + RC::C0 + 4);
       r.ia5 = __ldcg(rec + RC::IA5);
     } else {
       r.ni = __ldcg(reinterpret_cast<const double2 *>(rec + l.offn));
+    }
+#pragma unroll
+    for (int t = 0; t < NV - 4; t++) {
+      r.at[t] = __ldcg(rec + RC::A + 4 + t);
+      r.ut[t] = __ldcg(rec + RC::U + 4 + t);
+      if (!FWD) r.c0t[t] = __ldcg(rec + RC::C0 + 4 + t);
     }
     r.c.x = __ldcg(rec + l.offc);
     r.ia.x = __ldcg(rec + RC::IA);
@@ -677,16 +683,17 @@ struct QBand {
 // has three planes to arrive, enough for a read that crosses to the other
 // die's L2.  The band-edge state goes to the next band by st.async, its
 // bytes counted on the receiving entry's mbarrier (no fence on this side).
-// NV = 5 (eight lanes only): every lane also carries the SA row, the
-// upstream neighbour of its half adding F_n(nu~_2) + (0.5 Lc + Lv) dnu~ as
-// the one-lane sweep does; lane q = 0 of the leading half stores it.
+// NV = 5, 6 (eight lanes only): every lane also carries the turbulence
+// rows, the upstream neighbour of its half adding F_n(X_2) + (0.5 Lc + Lv) dX
+// as the one-lane sweep does; lane q = 0 of the leading half stores them.
 template <bool update, bool FWD, int LPR, int NV = 4>
 __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBand &B, double *slot, double *inbox,
                                       unsigned long long *mbar, unsigned rbox, unsigned rmbar, const double *rsrc,
                                       double *recBw, double gm1) {
   using RC = Rec<NV>;
   constexpr int QS = qslot<NV>();
-  static_assert(NV == 4 || LPR == 8, "the SA row rides on the eight-lane form only");
+  static_assert(NV == 4 || LPR == 8, "the turbulence rows ride on the eight-lane form only");
+  constexpr int NT = NV - 4;  // turbulence rows
   const int R = B.R, rl = B.rl, q = B.q, j = B.j, rows = B.rows, ni = B.ni;
   const long long F = L.F;
   const QLane ln = qlane<NV>(q, LPR == 4 || !((threadIdx.x >> 2) & 1));
@@ -715,7 +722,7 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
     }
   }
   double wx = 0.0, wu = 0.0, wv = 0.0, wp = 0.0;  // the row's previous cell
-  double wt = 0.0, wd = 0.0;                        // and its nu~ + dnu~, dnu~ (NV = 5)
+  double wt[2] = {0.0, 0.0}, wd[2] = {0.0, 0.0};   // and its turbulence X + dX, dX
   int gave_up = 0;                                 // first column whose inbox wait gave up
   const int gl = (threadIdx.x & 31) & ~(LPR - 1);  // the row's first lane
   // eight lanes per row: lanes 0-3 take the row's own previous cell, lanes
@@ -728,7 +735,7 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
     const bool act = B.row_ok && i >= 1 && i <= ni;
     const int k = FWD ? i - 1 : ni - i;
     if (act && k + 3 < ni) qload<FWD, update, LPR, NV>(ahead, src(k + 3), q, ln);
-    double acc = 0.0, acc4 = 0.0;
+    double acc = 0.0, acct[2] = {0.0, 0.0};
     if (act) {
       if (LPR == 4) {
         acc = FWD ? cur.a : cur.c0;
@@ -764,32 +771,40 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
         const double X = own_nb ? wx : sx, Uu = own_nb ? wu : uv.x, Vv = own_nb ? wv : uv.y, P = own_nb ? wp : sp;
         // the record fields of this half's face (loaded per half)
         acc = own_nb ? (FWD ? cur.a : cur.c0) : 0.0;
-        if (NV == 5) acc4 = own_nb ? (FWD ? cur.a4 : cur.c04) : 0.0;
+#pragma unroll
+        for (int t = 0; t < NT; t++) acct[t] = own_nb ? (FWD ? cur.at[t] : cur.c0t[t]) : 0.0;
         if (has) {
           const double w = fma(Uu, cur.ni.x, fma(Vv, cur.ni.y, cur.c.x));
           acc = fma(X, w, fma(P, qcoef(cur.ki, ln), acc));
-          if (NV == 5) {
-            // F_n(nu~_2) + (0.5 Lc + Lv) dnu~: the dissipation on the
-            // increment, as the one-lane sweep (add_shipped) forms it
-            const double T2 = own_nb ? wt : s[7], D2 = own_nb ? wd : s[8];
+          if (NT > 0) {
+            // F_n(X_2) + (0.5 Lc + Lv) dX: the dissipation on the increment,
+            // as the one-lane sweep (add_shipped) forms it
             const double un = fma(Uu, cur.ni.x, Vv * cur.ni.y);
-            acc4 = fma(cur.c.x, D2, fma(T2, un, acc4));
+#pragma unroll
+            for (int t = 0; t < NT; t++) {
+              const double T2 = own_nb ? wt[t] : s[8 + 2 * t], D2 = own_nb ? wd[t] : s[9 + 2 * t];
+              acct[t] = fma(cur.c.x, D2, fma(T2, un, acct[t]));
+            }
           }
         }
       }
     }
     // eight lanes: the two halves of the row add their neighbours' terms
     const double other = LPR == 8 ? __shfl_xor_sync(0xffffffffu, acc, 4) : 0.0;
-    const double other4 = NV == 5 ? __shfl_xor_sync(0xffffffffu, acc4, 4) : 0.0;
-    double st = 0.0, dn = 0.0, st4 = 0.0, dn4 = 0.0;
+    double othert[2] = {0.0, 0.0};
+#pragma unroll
+    for (int t = 0; t < NT; t++) othert[t] = __shfl_xor_sync(0xffffffffu, acct[t], 4);
+    double st = 0.0, dn = 0.0, stt[2] = {0.0, 0.0}, dnt[2] = {0.0, 0.0};
     if (act) {
       if (LPR == 8) acc = acc + other;
-      if (NV == 5) {
-        // the SA row never takes the fused U update (the reference adds dU
-        // after the sweep; only the mean flow is carried as U + dU)
-        acc4 = acc4 + other4;
-        dn4 = FWD ? acc4 * cur.ia5 : fma(acc4, cur.ia5, cur.a4);
-        st4 = cur.u4 + dn4;
+#pragma unroll
+      for (int t = 0; t < NT; t++) {
+        // the turbulence rows never take the fused U update (only the mean
+        // flow is carried as U + dU); the SA row has its own 1/alfa
+        const double inv = NV == 5 ? cur.ia5 : cur.ia.x;
+        const double a = acct[t] + othert[t];
+        dnt[t] = FWD ? a * inv : fma(a, inv, cur.at[t]);
+        stt[t] = cur.ut[t] + dnt[t];
       }
       if (update) {
         // U + dU* going forward (carried in the backward record), U + dU* + dU** going backward
@@ -812,35 +827,39 @@ __device__ __forceinline__ void qpass(const Lvl &L, const BlkDev &bd, const QBan
         qsend2(a, s0, s1, m);
         qsend2(a + 16u, s2, H, m);
         qsend2(a + 32u, u, v, m);
-        if (NV == 5) {
-          qsend2(a + 48u, pr, st4, m);
-          qsend2(a + 64u, dn4, 0.0, m);
-        } else {
-          qsend2(a + 48u, pr, 0.0, m);
-        }
+        qsend2(a + 48u, pr, 0.0, m);
+#pragma unroll
+        for (int t = 0; t < NT; t++) qsend2(a + 64u + 16u * t, stt[t], dnt[t], m);
       }
       double *o = slot + ((size_t)buf * R + rl) * QS;
       if (lead) o[q] = x;
       if (lead && q == 0) *reinterpret_cast<double2 *>(o + 4) = make_double2(u, v);
       if (lead && q == 1) o[6] = pr;
-      if (NV == 5 && lead && q == 2) *reinterpret_cast<double2 *>(o + 8) = make_double2(dn4, 0.0);
-      if (NV == 5 && lead && q == 3) o[7] = st4;
+#pragma unroll
+      for (int t = 0; t < NT; t++) {
+        if (lead && q == 2 + t) *reinterpret_cast<double2 *>(o + 8 + 2 * t) = make_double2(stt[t], dnt[t]);
+        wt[t] = stt[t];
+        wd[t] = dnt[t];
+      }
       wx = x; wu = u; wv = v; wp = pr;
-      wt = st4; wd = dn4;
       if (lead) {
         if (FWD) {
           recBw[(size_t)(i - 1) * RC::N + RC::A + q] = update ? st : dn;
-          if (NV == 5 && q == 0) recBw[(size_t)(i - 1) * RC::N + RC::A + 4] = dn4;
+#pragma unroll
+          for (int t = 0; t < NT; t++)
+            if (q == 0) recBw[(size_t)(i - 1) * RC::N + RC::A + 4 + t] = dnt[t];
         } else {
           // an updating sweep writes U only (DU is read nowhere but inside
           // du_LU_SGS_2D and the update that follows it)
           const long long id = bd.off + (long long)(j + 2) * bd.P + (i + 2);
           if (update) L.U[q * F + id] = st;
           else L.du[q * F + id] = dn;
-          if (NV == 5 && q == 0) {
-            if (update) L.U[4 * F + id] = st4;
-            else L.du[4 * F + id] = dn4;
-          }
+#pragma unroll
+          for (int t = 0; t < NT; t++)
+            if (q == 0) {
+              if (update) L.U[(4 + t) * F + id] = stt[t];
+              else L.du[(4 + t) * F + id] = dnt[t];
+            }
         }
       }
     }
@@ -908,6 +927,7 @@ int quad_ctas(int max_rows, int rmax) {
 static int quad_lanes(int rmax, int lanes) { return lanes == 4 || lanes == 8 ? lanes : (rmax <= 16 ? 8 : 4); }
 static void (*quad_kernel(int lpr, int update, int nv))(Lvl, int, int) {
   if (nv == 5) return update ? k_lusgs_sweep_quad<true, 8, 5> : k_lusgs_sweep_quad<false, 8, 5>;
+  if (nv == 6) return update ? k_lusgs_sweep_quad<true, 8, 6> : k_lusgs_sweep_quad<false, 8, 6>;
   return lpr == 8 ? (update ? k_lusgs_sweep_quad<true, 8> : k_lusgs_sweep_quad<false, 8>)
                   : (update ? k_lusgs_sweep_quad<true, 4> : k_lusgs_sweep_quad<false, 4>);
 }
@@ -919,10 +939,10 @@ static QuadShape quad_shape(int max_rows, int max_cols, int rmax, int lanes, int
   QuadShape q;
   q.CS = quad_ctas(max_rows, rmax);
   q.R = (max_rows + q.CS - 1) / q.CS;
-  q.lpr = nv == 5 ? 8 : quad_lanes(rmax, lanes);
+  q.lpr = nv > 4 ? 8 : quad_lanes(rmax, lanes);
   q.nv = nv;
   q.th = (q.lpr * q.R + 31) / 32 * 32;
-  const size_t qs = nv == 5 ? 10 : 8;  // qslot<NV>()
+  const size_t qs = 8 + 2 * (nv - 4);  // qslot<NV>()
   q.smem = (size_t)2 * q.R * qs * sizeof(double) + (q.CS > 1 ? (size_t)max_cols * 2 * (qs * sizeof(double) + 8) : 0);
   return q;
 }
@@ -943,8 +963,8 @@ bool quad_fits(const Lvl &L, int max_rows, int max_cols, int rmax, int lanes) {
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   }
   const QuadShape q = quad_shape(max_rows, max_cols, rmax, lanes, L.nvar);
-  // NV = 5 rides on eight lanes per row, so at most 16 rows per band
-  const bool nv_ok = L.nvar == 4 || (L.nvar == 5 && std::max(4, std::min(rmax, QROWS)) <= 16 && lanes != 4);
+  // NV = 5, 6 ride on eight lanes per row, so at most 16 rows per band
+  const bool nv_ok = L.nvar == 4 || (L.nvar <= 6 && std::max(4, std::min(rmax, QROWS)) <= 16 && lanes != 4);
   if (!(nv_ok && max_rows >= 1 && q.CS <= 16 && max_cols <= QCOLS && L.nblk * q.CS <= nsm)) return false;
   if (q.CS <= 8) return true;
   // a non-portable cluster size: launchable only if the device can place one
