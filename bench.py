@@ -855,13 +855,19 @@ def run_gb300(args, rank, world):
     d2h = 12 * 8 + 4 * 4
     torch.cuda.synchronize()
     barrier()
-    t0 = time.perf_counter()
+    # each step from the host's U to the host's norms (wall clock), after the
+    # same 512 MiB L2 flush as the device-timed steps, which stays outside
+    t_e2e = 0.0
     for k in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
         for b in range(1, nbl + 1):
             g.upload_U(1, 1, b, host[b - 1][1])
         g.step(1)
         g.norms(1, 1)
-    t_e2e = max_over_ranks(time.perf_counter() - t0)
+        t_e2e += time.perf_counter() - t0
+    t_e2e = max_over_ranks(t_e2e)
     e2e = {"value": cells * args.steps * world / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h}
 

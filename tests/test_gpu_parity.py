@@ -201,9 +201,8 @@ def test_boundary_wall_isothermal_symmetry_sa(gpu_lib):
 
 # NV = 4 (default shape): 16, 40 and 70 rows per block run eight lanes per
 # row in bands of 8, 10 and 12 rows on clusters of 2, 4 and 6 CTAs (the last
-# band short).  NV = 5 (SA) takes the same eight-lane bands, the SA row
-# carried by every lane; NV = 6 (SST): 16 rows run four lanes per row in one
-# CTA, 40 and 70 rows one lane per row.
+# band short).  NV = 5 (SA) and 6 (SST) take the same eight-lane bands, the
+# turbulence rows carried by every lane.
 @pytest.mark.parametrize("ny", [17, 41, 71])
 @pytest.mark.parametrize("turb", [0, 2, 3])
 def test_lusgs_sweep(gpu_lib, ny, turb):
