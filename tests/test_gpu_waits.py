@@ -1,4 +1,4 @@
-"""Failure detection of the four-lane LU-SGS wavefront without a GPU fault.
+"""Failure detection of the banded LU-SGS wavefront without a GPU fault.
 
 The bands of a tall block hand their edge rows to the next band through
 bounded waits.  With the band edges silenced (the EC2D_TEST_SILENT_BAND_EDGE
@@ -15,11 +15,19 @@ pytestmark = pytest.mark.gpu
 EC2D_ERR_TIMEOUT = 4
 
 
-def test_band_edge_wait_runs_out(gpu_lib, monkeypatch):
+# Euler (4 variables) and SA (5: the SA row rides on the same bands and its
+# inbox entries are 80 bytes)
+CASES = {"euler": dict(), "sa": dict(If_viscous=1, Iflag_turbulence_model=2, Re=1e6, first=2e-4)}
+
+
+@pytest.mark.parametrize("kind", ["euler", "sa"])
+def test_band_edge_wait_runs_out(gpu_lib, monkeypatch, kind):
     from ec2d import gpu
     monkeypatch.setenv("EC2D_TEST_SILENT_BAND_EDGE", "1")
     monkeypatch.setenv("EC2D_LUSGS_CLUSTER", "0")  # banded wavefront, 40 rows: four bands of 10
-    p, bl = small_case(ny=41, Ma=0.6, AoA=2.0, Iflag_flux=4, Iflag_Scheme=5, Time_Method=0, CFL=5.0)
+    p, bl = small_case(ny=41, Ma=0.6, AoA=2.0, Iflag_flux=4, Iflag_Scheme=5, Time_Method=0, CFL=5.0,
+                       **CASES[kind])
+    nv = 4 if kind == "euler" else 5
     g = make_gpu(p, bl)
     g.init_flow()
     g.step(1)
@@ -30,7 +38,7 @@ def test_band_edge_wait_runs_out(gpu_lib, monkeypatch):
     assert code == EC2D_ERR_TIMEOUT and blk >= 1 and i >= 1 and j >= 1
     # the context still answers: the state can be read back
     g.sync()
-    assert g.download_U(1, 1, 1).shape[0] == 4
+    assert g.download_U(1, 1, 1).shape[0] == nv
     g.close()
     # and the process's GPU context stays usable: with the hook cleared, a new
     # context in the same process steps with a clean status and finite U, and
