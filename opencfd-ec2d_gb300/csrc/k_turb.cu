@@ -355,12 +355,13 @@ __global__ void k_fdm_split(Lvl L) {
   const long long F = L.F;
   long long id = fidx(b, i, j);
   double d = L.q[Q_D * F + id], u = L.q[Q_U * F + id], v = L.q[Q_V * F + id], cc = L.q[Q_C * F + id];
-  const double rJ = 1.0 / L.met[M_JAC * F + id];  // one divide for the four metric quotients
+  const double rJ = 1.0 / L.met[M_JAC * F + id];  // one divide for the metric quotients
   double fp[4], fm[4];
-  split_sw(d, u, v, cc, L.met[M_KX * F + id] * rJ, L.met[M_KY * F + id] * rJ, c.gamma, fp, fm);
-  for (int m = 0; m < 4; m++) { L.fdm[(D_SPI + m) * F + id] = fp[m]; L.fdm[(D_SPI + 4 + m) * F + id] = fm[m]; }
-  split_sw(d, u, v, cc, L.met[M_IX * F + id] * rJ, L.met[M_IY * F + id] * rJ, c.gamma, fp, fm);
-  for (int m = 0; m < 4; m++) { L.fdm[(D_SPJ + m) * F + id] = fp[m]; L.fdm[(D_SPJ + 4 + m) * F + id] = fm[m]; }
+  // blockIdx.y: 0 the i-direction split, 1 the j-direction split (two threads per cell)
+  const int dir = blockIdx.y;
+  const int mx = dir == 0 ? M_KX : M_IX, my = dir == 0 ? M_KY : M_IY, out = dir == 0 ? D_SPI : D_SPJ;
+  split_sw(d, u, v, cc, L.met[mx * F + id] * rJ, L.met[my * F + id] * rJ, c.gamma, fp, fm);
+  for (int m = 0; m < 4; m++) { L.fdm[(out + m) * F + id] = fp[m]; L.fdm[(out + 4 + m) * F + id] = fm[m]; }
 }
 
 // fp_weno5 at point k (v[k-2..k+2]) and fm_weno5 producing hj(k-1) from v[k-2..k+2]
@@ -404,8 +405,12 @@ __device__ __forceinline__ double weno5_m(double vm2, double vm1, double v0, dou
 }
 
 // WENO5 half-point fluxes (sub_Finite_Difference.f90:37-77) and the central
-// viscous tensors Ev1/Ev2 (:87-117); indices are FDM cells = FVM cells
+// viscous tensors Ev1/Ev2 (:87-117); indices are FDM cells = FVM cells.
+// blockIdx.y picks the part: 0 the i-direction fluxes, 1 the j-direction
+// fluxes, 2 the viscous tensors, so a cell's three independent chains run
+// on three threads.
 __global__ void k_fdm_flux(Lvl L) {
+  const int part = blockIdx.y;
   int bk, i, j;
   if (!tile_xy(L, bk, i, j)) return;
   const BlkDev &b = L.blk[bk];
@@ -414,7 +419,7 @@ __global__ void k_fdm_flux(Lvl L) {
   const CaseDev &c = L.cs[b.cas];
   const long long F = L.F, P = b.P;
   long long id = fidx(b, i, j);
-  if (j >= LFDM && j <= nyF - LFDM && i >= LFDM && i <= nxF - LFDM) {
+  if (part == 0 && j >= LFDM && j <= nyF - LFDM && i >= LFDM && i <= nxF - LFDM) {
     for (int m = 0; m < 4; m++) {
       const double *fp = L.fdm + (D_SPI + m) * F, *fm = L.fdm + (D_SPI + 4 + m) * F;
       double h1 = weno5_p(fp[id - 2], fp[id - 1], fp[id], fp[id + 1], fp[id + 2]);
@@ -422,7 +427,7 @@ __global__ void k_fdm_flux(Lvl L) {
       L.fdm[(D_FI + m) * F + id] = -(h1 + h2);
     }
   }
-  if (i >= LFDM && i <= nxF - LFDM && j >= LFDM && j <= nyF - LFDM) {
+  if (part == 1 && i >= LFDM && i <= nxF - LFDM && j >= LFDM && j <= nyF - LFDM) {
     for (int m = 0; m < 4; m++) {
       const double *fp = L.fdm + (D_SPJ + m) * F, *fm = L.fdm + (D_SPJ + 4 + m) * F;
       double h1 = weno5_p(fp[id - 2 * P], fp[id - P], fp[id], fp[id + P], fp[id + 2 * P]);
@@ -430,7 +435,7 @@ __global__ void k_fdm_flux(Lvl L) {
       L.fdm[(D_FJ + m) * F + id] = -(h1 + h2);
     }
   }
-  if (L.visc && i >= 2 && i <= nxF - 1 && j >= 2 && j <= nyF - 1) {
+  if (part == 2 && L.visc && i >= 2 && i <= nxF - 1 && j >= 2 && j <= nyF - 1) {
     const double *uu = L.q + Q_U * F, *vv = L.q + Q_V * F, *TT = L.q + Q_T * F;
     double mu0 = L.amu[id] + L.amut[id];
     double Ak0 = c.Cp * (L.amu[id] / c.Pr + L.amut[id] / PrT);
@@ -477,8 +482,8 @@ __global__ void k_fdm_res(Lvl L) {
 }
 
 void launch_fdm(const Lvl &L, cudaStream_t s) {
-  k_fdm_split<<<L.ntiles, TILE, 0, s>>>(L);
-  k_fdm_flux<<<L.ntiles, TILE, 0, s>>>(L);
+  k_fdm_split<<<dim3(L.ntiles, 2), TILE, 0, s>>>(L);
+  k_fdm_flux<<<dim3(L.ntiles, L.visc ? 3 : 2), TILE, 0, s>>>(L);
   k_fdm_res<<<L.ntiles, TILE, 0, s>>>(L);
 }
 
