@@ -478,9 +478,11 @@ def polar_metric(args, torch, gpu):
 
     * plain: the GPU drop-in, one case per context, FP64.  Its time to a
       drop D for case c is that case's V-cycles to D times its own ms per
-      V-cycle (plain_step_ms).  The V-cycle counts come from the FP64 batch,
-      whose per-case arithmetic is the plain drop-in's bit for bit (one launch
-      per stage covers every case; cases never read each other's data).
+      V-cycle (plain_step_ms).  The V-cycle counts come from the FP64 batch
+      (one launch per stage covers every case; cases never read each
+      other's data); a lone case runs the eight-lane wavefront, the batch's
+      150 blocks the one-lane one, so the two differ in the wavefront's
+      summation order only.
     * batched_mixed: all 64 cases in one context, FP32 LU-SGS (FP64
       residual, boundary conditions, transfers, norms), freestream start.
     * learned_batched_mixed: the same from the warm-start network's
@@ -684,6 +686,22 @@ def leg_rans(args):
                                           for (n, l), v in sorted(kt.items(), key=lambda kv: -kv[1][2])[:12]},
                 "cells": fine_cells(bl), "lusgs_shape": g.lusgs_shape()}
             g.close()
+    return out
+
+
+def leg_fp64(args):
+    """The FP64 cost model of the latency-bound kernels: clock64 cycles per
+    dependent operation per warp (ec2d_measure_op_cycles) for FP64 fma, the
+    FP64 divide, the refined FP64 reciprocal of the face and wavefront paths
+    and FP32 fma, with 1-8 warps in one CTA and 1-8 independent chains per
+    thread; and the FP64 FMA throughput of the whole GPU."""
+    from ec2d import gpu
+    ops = {0: "fp64_fma", 1: "fp64_divide", 2: "fp64_refined_reciprocal", 3: "fp32_fma"}
+    shapes = [(1, 1), (1, 2), (1, 4), (1, 8), (2, 1), (4, 1), (4, 4), (8, 1)]
+    out = {"unit": "clock64 cycles per operation and warp", "shapes": "warps x independent chains per thread"}
+    for op, name in ops.items():
+        out[name] = {f"{w}x{c}": round(gpu.measure_op_cycles(op, w, c), 2) for w, c in shapes}
+    out["fp64_peak_tflops"] = gpu.measure_fp64_peak()
     return out
 
 
@@ -972,7 +990,7 @@ def main():
     ap.add_argument("--transfer-reps", type=int, default=10, help="timed launches per transfer form")
     ap.add_argument("--residual-grid", default="2049x1025",
                     help="nodes per block of the residual_hbm leg's 2-block flat plate (NXxNY)")
-    ap.add_argument("--leg", default="all", choices=["all", "residual_hbm", "polar", "learned", "mlp", "rans"],
+    ap.add_argument("--leg", default="all", choices=["all", "residual_hbm", "polar", "learned", "mlp", "rans", "fp64"],
                     help="residual_hbm: the 4.19 M-cell residual alone (for profiling); polar: the 64-case "
                          "batched polar; learned: the learned warm start end to end")
     ap.add_argument("--no-polar", dest="polar", action="store_false",
@@ -1006,6 +1024,8 @@ def main():
             out = leg_mlp(args)
         elif args.leg == "rans":
             out = leg_rans(args)
+        elif args.leg == "fp64":
+            out = leg_fp64(args)
         else:
             out = leg_learned(args)
         print(json.dumps({args.leg: out}, default=float), flush=True)

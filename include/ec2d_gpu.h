@@ -245,6 +245,14 @@ int ec2d_kernel_times(ec2d_ctx *ctx, char *buf, int buflen);
  * that bounds the residual and LU-SGS kernels on this part. */
 int ec2d_measure_fp64_peak(double *tflops);
 
+/* The cost model behind the latency-bound kernels: clock64 cycles per
+ * operation of a chain of dependent operations, per warp, in one CTA of
+ * `warps` warps (1..32) whose threads run `chains` (1, 2, 4, 8) independent
+ * chains each.  op 0: FP64 fma; 1: FP64 divide; 2: the refined FP64
+ * reciprocal of the face and wavefront paths; 3: FP32 fma.  No counterpart in
+ * the reference. */
+int ec2d_measure_op_cycles(int op, int warps, int chains, double *cycles);
+
 /* Residual norms without any device allocation.  No counterpart in the
  * reference: it serves hosts that cannot call cudaMalloc (a Fortran/OpenACC
  * host whose device memory belongs to another allocator or memory pool, or a

@@ -31,7 +31,81 @@ __global__ void __launch_bounds__(256) k_fp64_fma(double *sink, int iters, doubl
   if (s == -1.0) sink[blockIdx.x] = s;  // never true; keeps the chains live
 }
 
+// The cost model of the latency-bound kernels: one CTA of `warps` warps,
+// every thread runs C independent chains of `iters` dependent operations;
+// lane 0 of each warp records clock64 cycles per operation and chain.
+// OP 0: FP64 fma; 1: FP64 divide; 2: the refined FP64 reciprocal of the face
+// and wavefront paths (rcp.approx + one third-order step); 3: FP32 fma.
+template <int C, int OP>
+__global__ void __launch_bounds__(1024) k_op_cycles(int iters, double *cyc) {
+  double a[C];
+  float f[C];
+#pragma unroll
+  for (int k = 0; k < C; k++) {
+    a[k] = 1.0 + 1e-3 * (threadIdx.x + k);
+    f[k] = 1.0f + 1e-3f * (threadIdx.x + k);
+  }
+  __syncthreads();
+  const long long t0 = clock64();
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int k = 0; k < C; k++) {
+      if (OP == 0) a[k] = fma(a[k], 0.999, 0.001);
+      if (OP == 1) a[k] = 1.5 / a[k];  // stays between a and 1.5 / a
+      if (OP == 2) {
+        double r;
+        asm volatile("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(a[k]));
+        const double e = fma(-a[k], r, 1.0);
+        a[k] = 1.5 * fma(r, fma(e, e, e), r);
+      }
+      if (OP == 3) f[k] = fmaf(f[k], 0.999f, 0.001f);
+    }
+  }
+  const long long t1 = clock64();
+  double sum = 0.0;
+#pragma unroll
+  for (int k = 0; k < C; k++) sum += a[k] + (double)f[k];
+  if ((threadIdx.x & 31) == 0) cyc[threadIdx.x >> 5] = (double)(t1 - t0) / ((double)iters * C) + (sum == -1.0);
+}
+
+template <int OP>
+void launch_op(int chains, int warps, int iters, double *d) {
+  switch (chains) {
+    case 1: k_op_cycles<1, OP><<<1, warps * 32>>>(iters, d); break;
+    case 2: k_op_cycles<2, OP><<<1, warps * 32>>>(iters, d); break;
+    case 4: k_op_cycles<4, OP><<<1, warps * 32>>>(iters, d); break;
+    default: k_op_cycles<8, OP><<<1, warps * 32>>>(iters, d); break;
+  }
+}
+
 }  // namespace
+
+extern "C" int ec2d_measure_op_cycles(int op, int warps, int chains, double *cycles) {
+  if (!cycles || op < 0 || op > 3 || warps < 1 || warps > 32 || (chains != 1 && chains != 2 && chains != 4 && chains != 8))
+    return EC2D_ERR_ARG;
+  double *d = nullptr;
+  if (cudaMalloc(&d, 32 * sizeof(double)) != cudaSuccess) return EC2D_ERR_NOMEM;
+  const int iters = op == 1 ? 512 : 4096;
+  double best = 0.0;
+  for (int rep = 0; rep < 3; rep++) {  // the first launch warms up
+    if (op == 0) launch_op<0>(chains, warps, iters, d);
+    else if (op == 1) launch_op<1>(chains, warps, iters, d);
+    else if (op == 2) launch_op<2>(chains, warps, iters, d);
+    else launch_op<3>(chains, warps, iters, d);
+    double h[32];
+    if (cudaMemcpy(h, d, warps * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
+      cudaFree(d);
+      return EC2D_ERR_CUDA;
+    }
+    double mean = 0.0;
+    for (int w = 0; w < warps; w++) mean += h[w] / warps;
+    if (rep > 0 && (best == 0.0 || mean < best)) best = mean;
+  }
+  cudaFree(d);
+  if (cudaGetLastError() != cudaSuccess) return EC2D_ERR_CUDA;
+  *cycles = best;
+  return EC2D_OK;
+}
 
 extern "C" int ec2d_measure_fp64_peak(double *tflops) {
   if (!tflops) return EC2D_ERR_ARG;

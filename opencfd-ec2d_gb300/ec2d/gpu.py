@@ -138,6 +138,7 @@ def lib():
         "ec2d_mlp_predict": ([vp, fp, ctypes.c_longlong, fp], ctypes.c_int),
         "ec2d_mlp_set_gemm": ([vp, ctypes.c_int], ctypes.c_int),
         "ec2d_measure_fp64_peak": ([dp], ctypes.c_int),
+        "ec2d_measure_op_cycles": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, dp], ctypes.c_int),
         "ec2d_snapshot": ([vp, ctypes.c_int], ctypes.c_int),
         "ec2d_tile_residual": ([vp, ctypes.c_int, ip], ctypes.c_int),
         "ec2d_mg_eddy_viscosity": ([vp, ctypes.c_int, ip], ctypes.c_int),
@@ -164,6 +165,14 @@ def measure_fp64_peak():
     t = ctypes.c_double()
     _ck(lib().ec2d_measure_fp64_peak(ctypes.byref(t)), "ec2d_measure_fp64_peak")
     return t.value
+
+
+def measure_op_cycles(op, warps=1, chains=1):
+    """clock64 cycles per dependent operation per warp (op 0 FP64 fma, 1 FP64
+    divide, 2 refined FP64 reciprocal, 3 FP32 fma)."""
+    c = ctypes.c_double()
+    _ck(lib().ec2d_measure_op_cycles(int(op), int(warps), int(chains), ctypes.byref(c)), "ec2d_measure_op_cycles")
+    return c.value
 
 
 def _fp(a):
