@@ -701,6 +701,11 @@ def leg_fp64(args):
     out = {"unit": "clock64 cycles per operation and warp", "shapes": "warps x independent chains per thread"}
     for op, name in ops.items():
         out[name] = {f"{w}x{c}": round(gpu.measure_op_cycles(op, w, c), 2) for w, c in shapes}
+    out["cta_barrier_cycles"] = {f"{w} warps": round(gpu.measure_op_cycles(4, w, 1), 1) for w in (1, 3, 8)}
+    out["cluster_barrier_cycles"] = {f"{c} CTAs": round(gpu.measure_op_cycles(5, 1, c), 1) for c in (2, 4, 8)}
+    rel, ulps = gpu.check_reciprocal(40_000_000)
+    out["reciprocal"] = {"inputs": 40_000_000, "range": "[2^-8, 2^9)", "approx_max_rel_err": rel,
+                         "refined_max_ulps_from_ieee_quotient": ulps}
     out["fp64_peak_tflops"] = gpu.measure_fp64_peak()
     return out
 

@@ -249,9 +249,16 @@ int ec2d_measure_fp64_peak(double *tflops);
  * operation of a chain of dependent operations, per warp, in one CTA of
  * `warps` warps (1..32) whose threads run `chains` (1, 2, 4, 8) independent
  * chains each.  op 0: FP64 fma; 1: FP64 divide; 2: the refined FP64
- * reciprocal of the face and wavefront paths; 3: FP32 fma.  No counterpart in
- * the reference. */
+ * reciprocal of the face and wavefront paths; 3: FP32 fma; 4: a CTA barrier
+ * (cycles per barrier); 5: a cluster barrier among `chains` CTAs.  No
+ * counterpart in the reference. */
 int ec2d_measure_op_cycles(int op, int warps, int chains, double *cycles);
+
+/* The refined reciprocal of the face and wavefront paths checked on the
+ * device on n inputs spread over [2^-8, 2^9): the largest relative error of
+ * the hardware approximation and the largest distance of the refined value
+ * from the IEEE quotient, in ulps.  No counterpart in the reference. */
+int ec2d_check_reciprocal(long long n, double *approx_rel, double *refined_ulps);
 
 /* Residual norms without any device allocation.  No counterpart in the
  * reference: it serves hosts that cannot call cudaMalloc (a Fortran/OpenACC

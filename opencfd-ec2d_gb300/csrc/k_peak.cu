@@ -9,6 +9,7 @@
 // the grid is 8 CTAs of 256 threads per SM.  FLOPs = 2 per FMA.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 
 #include "../../include/ec2d_gpu.h"
@@ -68,6 +69,55 @@ __global__ void __launch_bounds__(1024) k_op_cycles(int iters, double *cyc) {
   if ((threadIdx.x & 31) == 0) cyc[threadIdx.x >> 5] = (double)(t1 - t0) / ((double)iters * C) + (sum == -1.0);
 }
 
+// barriers: OP 4 a CTA barrier per iteration; OP 5 a cluster barrier
+// (arrive.release + wait.acquire) per iteration, launched as one cluster
+template <int OP>
+__global__ void __launch_bounds__(1024) k_barrier_cycles(int iters, double *cyc) {
+  __syncthreads();
+  const long long t0 = clock64();
+  for (int it = 0; it < iters; it++) {
+    if (OP == 4) __syncthreads();
+    else asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+  }
+  const long long t1 = clock64();
+  if (threadIdx.x == 0 && blockIdx.x == 0) cyc[0] = (double)(t1 - t0) / iters;
+}
+
+// The refined reciprocal against the IEEE quotient on n inputs spread over
+// [2^-8, 2^9) by a hash of the index: per block the largest relative error
+// of rcp.approx and the largest distance of the refined value in ulps.
+__global__ void k_rcp_check(long long n, double *out) {
+  __shared__ double s_rel[256], s_ulp[256];
+  double rel = 0.0, ulp = 0.0;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    unsigned long long h = (unsigned long long)k * 0x9E3779B97F4A7C15ull;
+    h ^= h >> 29;
+    h *= 0xBF58476D1CE4E5B9ull;
+    h ^= h >> 32;
+    const double m = 1.0 + (double)(h >> 12) * 0x1.0p-52;       // [1, 2)
+    const double x = ldexp(m, (int)((h >> 4) % 17) - 8);         // [2^-8, 2^9)
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    const double q = 1.0 / x;  // IEEE quotient
+    rel = fmax(rel, fabs(r - q) / q);
+    const double e = fma(-x, r, 1.0);
+    const double rr = fma(r, fma(e, e, e), r);
+    const double u = fabs(rr - q) / (nextafter(q, 2.0 * q) - q);
+    ulp = fmax(ulp, u);
+  }
+  s_rel[threadIdx.x] = rel;
+  s_ulp[threadIdx.x] = ulp;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      s_rel[threadIdx.x] = fmax(s_rel[threadIdx.x], s_rel[threadIdx.x + w]);
+      s_ulp[threadIdx.x] = fmax(s_ulp[threadIdx.x], s_ulp[threadIdx.x + w]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { out[2 * blockIdx.x] = s_rel[0]; out[2 * blockIdx.x + 1] = s_ulp[0]; }
+}
+
 template <int OP>
 void launch_op(int chains, int warps, int iters, double *d) {
   switch (chains) {
@@ -81,7 +131,7 @@ void launch_op(int chains, int warps, int iters, double *d) {
 }  // namespace
 
 extern "C" int ec2d_measure_op_cycles(int op, int warps, int chains, double *cycles) {
-  if (!cycles || op < 0 || op > 3 || warps < 1 || warps > 32 || (chains != 1 && chains != 2 && chains != 4 && chains != 8))
+  if (!cycles || op < 0 || op > 5 || warps < 1 || warps > 32 || (chains != 1 && chains != 2 && chains != 4 && chains != 8))
     return EC2D_ERR_ARG;
   double *d = nullptr;
   if (cudaMalloc(&d, 32 * sizeof(double)) != cudaSuccess) return EC2D_ERR_NOMEM;
@@ -91,19 +141,52 @@ extern "C" int ec2d_measure_op_cycles(int op, int warps, int chains, double *cyc
     if (op == 0) launch_op<0>(chains, warps, iters, d);
     else if (op == 1) launch_op<1>(chains, warps, iters, d);
     else if (op == 2) launch_op<2>(chains, warps, iters, d);
-    else launch_op<3>(chains, warps, iters, d);
+    else if (op == 3) launch_op<3>(chains, warps, iters, d);
+    else if (op == 4) k_barrier_cycles<4><<<1, warps * 32>>>(iters, d);
+    else {
+      // a cluster of `chains` CTAs of `warps` warps each
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(chains);
+      cfg.blockDim = dim3(warps * 32);
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = chains;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      cudaLaunchKernelEx(&cfg, k_barrier_cycles<5>, iters, d);
+    }
+    const int nw = op >= 4 ? 1 : warps;
     double h[32];
-    if (cudaMemcpy(h, d, warps * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
+    if (cudaMemcpy(h, d, nw * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
       cudaFree(d);
       return EC2D_ERR_CUDA;
     }
     double mean = 0.0;
-    for (int w = 0; w < warps; w++) mean += h[w] / warps;
+    for (int w = 0; w < nw; w++) mean += h[w] / nw;
     if (rep > 0 && (best == 0.0 || mean < best)) best = mean;
   }
   cudaFree(d);
   if (cudaGetLastError() != cudaSuccess) return EC2D_ERR_CUDA;
   *cycles = best;
+  return EC2D_OK;
+}
+
+extern "C" int ec2d_check_reciprocal(long long n, double *approx_rel, double *refined_ulps) {
+  if (n < 1 || !approx_rel || !refined_ulps) return EC2D_ERR_ARG;
+  const int blocks = 304, threads = 256;
+  double *d = nullptr;
+  if (cudaMalloc(&d, 2 * blocks * sizeof(double)) != cudaSuccess) return EC2D_ERR_NOMEM;
+  k_rcp_check<<<blocks, threads>>>(n, d);
+  double h[2 * 304];
+  const cudaError_t err = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (err != cudaSuccess || cudaGetLastError() != cudaSuccess) return EC2D_ERR_CUDA;
+  double rel = 0.0, ulp = 0.0;
+  for (int b = 0; b < blocks; b++) { rel = std::max(rel, h[2 * b]); ulp = std::max(ulp, h[2 * b + 1]); }
+  *approx_rel = rel;
+  *refined_ulps = ulp;
   return EC2D_OK;
 }
 

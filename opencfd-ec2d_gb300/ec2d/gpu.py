@@ -139,6 +139,7 @@ def lib():
         "ec2d_mlp_set_gemm": ([vp, ctypes.c_int], ctypes.c_int),
         "ec2d_measure_fp64_peak": ([dp], ctypes.c_int),
         "ec2d_measure_op_cycles": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, dp], ctypes.c_int),
+        "ec2d_check_reciprocal": ([ctypes.c_longlong, dp, dp], ctypes.c_int),
         "ec2d_snapshot": ([vp, ctypes.c_int], ctypes.c_int),
         "ec2d_tile_residual": ([vp, ctypes.c_int, ip], ctypes.c_int),
         "ec2d_mg_eddy_viscosity": ([vp, ctypes.c_int, ip], ctypes.c_int),
@@ -167,9 +168,19 @@ def measure_fp64_peak():
     return t.value
 
 
+def check_reciprocal(n=40_000_000):
+    """(largest relative error of the hardware reciprocal approximation,
+    largest distance of the refined reciprocal from the IEEE quotient in
+    ulps) over n inputs in [2^-8, 2^9)."""
+    a, u = ctypes.c_double(), ctypes.c_double()
+    _ck(lib().ec2d_check_reciprocal(int(n), ctypes.byref(a), ctypes.byref(u)), "ec2d_check_reciprocal")
+    return a.value, u.value
+
+
 def measure_op_cycles(op, warps=1, chains=1):
     """clock64 cycles per dependent operation per warp (op 0 FP64 fma, 1 FP64
-    divide, 2 refined FP64 reciprocal, 3 FP32 fma)."""
+    divide, 2 refined FP64 reciprocal, 3 FP32 fma), or per barrier (4 CTA
+    barrier with `warps` warps, 5 cluster barrier among `chains` CTAs)."""
     c = ctypes.c_double()
     _ck(lib().ec2d_measure_op_cycles(int(op), int(warps), int(chains), ctypes.byref(c)), "ec2d_measure_op_cycles")
     return c.value

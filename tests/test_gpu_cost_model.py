@@ -22,3 +22,16 @@ def test_fp64_cost_model(gpu_lib):
     with pytest.raises(gpu.EC2DError):
         gpu.measure_op_cycles(0, 33, 1)
     assert gpu.measure_fp64_peak() > 0.1
+    # a cluster barrier costs more than a CTA barrier
+    assert gpu.measure_op_cycles(5, 1, 4) > gpu.measure_op_cycles(4, 4, 1)
+
+
+def test_refined_reciprocal_within_an_ulp(gpu_lib):
+    """rcp<double> of the face and wavefront paths (the hardware
+    approximation refined by one third-order step) against the IEEE quotient
+    on 4 M inputs: the approximation within 2^-19 relative, the refined
+    value within one ulp."""
+    from ec2d import gpu
+    rel, ulps = gpu.check_reciprocal(4_000_000)
+    assert 0.0 < rel < 2.0 ** -19
+    assert ulps <= 1.0
