@@ -240,6 +240,14 @@ module ec2d_gpu_mod
       type(c_ptr), value :: ctx
       integer(c_int), value :: bits
     end function
+
+    ! turbulent multigrid: coarse levels keep the restricted eddy viscosity
+    integer(c_int) function ec2d_mg_eddy_viscosity(ctx, enable, current) bind(C)
+      import
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: enable
+      integer(c_int) :: current
+    end function
     integer(c_int) function ec2d_set_coarse_precision(ctx, bits) bind(C)
       import
       type(c_ptr), value :: ctx
