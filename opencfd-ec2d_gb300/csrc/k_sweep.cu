@@ -643,7 +643,8 @@ __device__ __forceinline__ void qload(QRec &r, const double *rec, int q, const Q
 // Inbox entries arrive by st.async, each 16-byte store counting its bytes on
 // the entry's mbarrier in the receiving CTA: no fence on the sending side.
 // The receiver arms every entry's mbarrier at start-up (one arrival expecting
-// 64 bytes), so phase 0 completes when the entry has landed.
+// the entry's bytes: 64, or 80 / 96 with the SA / SST rows), so phase 0
+// completes when the entry has landed.
 __device__ __forceinline__ void qarm(unsigned long long *mb, unsigned bytes) {
   const unsigned a = (unsigned)__cvta_generic_to_shared(mb);
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(1) : "memory");
