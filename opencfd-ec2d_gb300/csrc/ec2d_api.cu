@@ -723,10 +723,12 @@ void lusgs_update(ec2d_ctx *ctx, int l, double alfa1, bool force = false) {
 }
 // NS_Time_advance_LU_SGS (sub_NS_singlegrid.f90:185-224); on a coarse level of
 // an LU-SGS-smoothed multigrid cycle the forcing is added after the residual
-void step_lusgs(ec2d_ctx *ctx, int l, double alfa1 = 0.0, bool fresh = false) {
+// bc: false leaves the boundary conditions after the update to the caller
+// (a multigrid transfer issues them after its fork, see transfer_down)
+void step_lusgs(ec2d_ctx *ctx, int l, double alfa1 = 0.0, bool fresh = false, bool bc = true) {
   if (!fresh) residual(ctx, l, l != 1 ? RES_ADD_FORCE : 0);
   lusgs_update(ctx, l, alfa1, fresh && l != 1);
-  bc_all(ctx, l);
+  if (bc) bc_all(ctx, l);
   advance_counters(ctx, l);
 }
 void clip(ec2d_ctx *ctx, int l) {
@@ -772,23 +774,34 @@ int time_advance(ec2d_ctx *ctx, int l) {
   clip(ctx, l);
   return EC2D_OK;
 }
-void mg_smooth_fine(ec2d_ctx *ctx) {
+// Returns the work it left to the transfer that follows: SMOOTH_BC, the
+// level's boundary conditions after the LU-SGS update, and SMOOTH_CLIP, the
+// turbulence clip after them (force_vt_kw)
+enum { SMOOTH_BC = 1, SMOOTH_CLIP = 2 };
+int mg_smooth_fine(ec2d_ctx *ctx) {
   int tm = ctx->P.Time_Method;
   if (tm == Time_Euler1) step_euler(ctx, 1);
-  else if (tm == Time_LU_SGS) { step_lusgs(ctx, 1); clip(ctx, 1); }
-  else step_rk3(ctx, 1);
+  else if (tm == Time_LU_SGS) {
+    step_lusgs(ctx, 1, 0.0, false, false);
+    return SMOOTH_BC | SMOOTH_CLIP;
+  } else step_rk3(ctx, 1);
+  return 0;
 }
 // Un = U of the coarse level (Euler and LU-SGS smoothing) is taken by the
 // residual evaluation just before (RES_SET_UN, see transfer_down), and the
 // first smoothing step reuses that evaluation (U is unchanged since)
-void mg_smooth_coarse(ec2d_ctx *ctx, int l) {
+// defer_bc: a transfer follows and issues the boundary conditions (the
+// return value as for mg_smooth_fine)
+int mg_smooth_coarse(ec2d_ctx *ctx, int l, bool defer_bc = false) {
   const int Time_step_coarse_mesh = 3;
   int tm = ctx->P.Time_Method;
   if (tm == Time_Euler1) {
     for (int m = 0; m < Time_step_coarse_mesh; m++) step_euler(ctx, l, m == 0);
   } else if (tm == Time_LU_SGS) {
-    step_lusgs(ctx, l, 0.0, true);
+    step_lusgs(ctx, l, 0.0, true, !defer_bc);
+    return defer_bc ? SMOOTH_BC : 0;
   } else step_rk3(ctx, l);
+  return 0;
 }
 // the work issued while it is in effect goes to the second stream pair
 void swap_branch(ec2d_ctx *ctx) {
@@ -806,14 +819,22 @@ void swap_branch(ec2d_ctx *ctx) {
 // kernels it runs on the second stream pair beside the first (graph
 // branches); the forcing QF = sum Res_h - R_2h(U_2h) is formed where the two
 // join, with the same two roundings as the reference's sum then subtract.
-void transfer_down(ec2d_ctx *ctx, int f, int fine_post) {
+// pending: the smoother's boundary conditions (and clip) of level f, issued
+// here on the first chain, after the fork: the restriction of U reads the
+// interior mean-flow variables only, which neither of them writes.
+void transfer_down(ec2d_ctx *ctx, int f, int fine_post, int pending = 0) {
   const int tm = ctx->P.Time_Method;
   const int cpost = (tm == Time_Euler1 || tm == Time_LU_SGS) ? RES_SET_UN : 0;
   const Lvl &Lf = ctx->lv[f].L, &Lc = ctx->lv[f + 1].L;
+  auto finish_smoothing = [&] {
+    if (pending & SMOOTH_BC) bc_all(ctx, f);
+    if (pending & SMOOTH_CLIP) clip(ctx, f);
+  };
   if (Lc.keep_amut) {
     // the coarse eddy viscosity comes from the finer level's after its
     // residual (the oracle's order: residual, then interpolation2h), so
     // this transfer runs in sequence
+    finish_smoothing();
     residual(ctx, f, fine_post);
     K(ctx, "k_restrict", f + 1, 1, [&] { launch_restrict(Lf, Lc, 1 | 8, ctx->stream); });
     bc_all(ctx, f + 1);
@@ -826,6 +847,8 @@ void transfer_down(ec2d_ctx *ctx, int f, int fine_post) {
     cudaEventRecord(ctx->ev_b0, ctx->stream);
     cudaStreamWaitEvent(ctx->stream2, ctx->ev_b0, 0);
     swap_branch(ctx);
+  } else {
+    finish_smoothing();
   }
   K(ctx, "k_restrict", f + 1, 1, [&] { launch_restrict(Lf, Lc, 1, ctx->stream); });
   bc_all(ctx, f + 1);
@@ -833,6 +856,7 @@ void transfer_down(ec2d_ctx *ctx, int f, int fine_post) {
   if (par) {
     swap_branch(ctx);
     cudaEventRecord(ctx->ev_b1, ctx->stream2);
+    finish_smoothing();
   }
   residual(ctx, f, fine_post);
   if (par) cudaStreamWaitEvent(ctx->stream, ctx->ev_b1, 0);
@@ -846,18 +870,18 @@ void correct_from(ec2d_ctx *ctx, int c) {
 }
 // NS_2stge_multigrid (sub_NS_multigrid.f90:14-58)
 void mg2(ec2d_ctx *ctx) {
-  mg_smooth_fine(ctx);
-  transfer_down(ctx, 1, 0);
+  const int pend = mg_smooth_fine(ctx);
+  transfer_down(ctx, 1, 0, pend);
   mg_smooth_coarse(ctx, 2);
   correct_from(ctx, 2);
   bc_all(ctx, 1);
 }
 // NS_3stge_multigrid (sub_NS_multigrid.f90:66-142)
 void mg3(ec2d_ctx *ctx) {
-  mg_smooth_fine(ctx);
-  transfer_down(ctx, 1, 0);
-  mg_smooth_coarse(ctx, 2);
-  transfer_down(ctx, 2, RES_ADD_FORCE);
+  const int pend1 = mg_smooth_fine(ctx);
+  transfer_down(ctx, 1, 0, pend1);
+  const int pend2 = mg_smooth_coarse(ctx, 2, true);
+  transfer_down(ctx, 2, RES_ADD_FORCE, pend2);
   mg_smooth_coarse(ctx, 3);
   correct_from(ctx, 3);
   correct_from(ctx, 2);
