@@ -371,8 +371,9 @@ __global__ void k_fdm_split(Lvl L) {
 // the same weights are W_k = C_k prod_{l != k} D_l / sum_m C_m prod_{l != m} D_l,
 // one divide.  The results agree to a few ulps; an IEEE divide costs about a
 // dozen FP64 instructions, and the sixteen evaluations per cell made the
-// divides most of the kernel's FP64 work.  D_k lies in [1e-12, ~1e10], so the
-// products stay far inside the FP64 range.
+// divides most of the kernel's FP64 work.  D_k >= 1e-12, so the numerators
+// and the denominator stay above 1e-36, and they overflow only for smoothness
+// indicators S_k beyond about 1e50, far from any split flux of this solver.
 __device__ __forceinline__ double weno5_mix(double S0, double S1, double S2, double q03, double q13, double q23) {
   const double ep = 1.0e-6, C03 = 3.0 / 10.0, C13 = 3.0 / 5.0, C23 = 1.0 / 10.0;
   const double D0 = (ep + S0) * (ep + S0), D1 = (ep + S1) * (ep + S1), D2 = (ep + S2) * (ep + S2);
