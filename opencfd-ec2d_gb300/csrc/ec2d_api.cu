@@ -76,8 +76,8 @@ struct Level {
   std::vector<HLevelBlock> hb;
   std::vector<BlkDev> blk;
   std::vector<SubDev> sub;
-  std::vector<int2> tiles;
-  std::vector<int> case_tile0, case_ntile, case_ncell;
+  std::vector<int2> tiles, ctiles;  // extended and core windows (core_ij)
+  std::vector<int> case_tile0, case_ntile, case_ncell;  // case ranges of ctiles
   std::vector<int4> wall_faces;          // (block, face, k, 0) for forces
   std::vector<int> case_face0, case_nface;
   long long F = 0;
@@ -271,11 +271,11 @@ int build_level(ec2d_ctx *ctx, int l) {
   // device layout
   std::vector<int> case_first_block(ncase, -1);
   long long off = 0;
-  int tile = 0, sub0 = 0;
+  int tile = 0, ctile = 0, sub0 = 0;
   lv.case_tile0.assign(ncase, 0); lv.case_ntile.assign(ncase, 0); lv.case_ncell.assign(ncase, 0);
   for (int k = 0; k < (int)lv.hb.size(); k++) {
     auto &B = lv.hb[k];
-    if (case_first_block[B.cas] < 0) { case_first_block[B.cas] = k; lv.case_tile0[B.cas] = tile; }
+    if (case_first_block[B.cas] < 0) { case_first_block[B.cas] = k; lv.case_tile0[B.cas] = ctile; }
     BlkDev d{};
     d.nx = B.nx; d.ny = B.ny; d.P = B.nx + 5; d.cas = B.cas; d.off = off; d.fdm = B.fdm ? 1 : 0;
     d.nsub = B.nsub; d.sub0 = sub0; d.tile0 = tile;
@@ -286,7 +286,10 @@ int build_level(ec2d_ctx *ctx, int l) {
     int nt = (items + TILE - 1) / TILE;
     for (int t = 0; t < nt; t++) lv.tiles.push_back(make_int2(k, t * TILE));
     tile += nt;
-    lv.case_ntile[B.cas] += nt;
+    const int nct = ((B.nx + 1) * (B.ny + 1) + TILE - 1) / TILE;
+    for (int t = 0; t < nct; t++) lv.ctiles.push_back(make_int2(k, t * TILE));
+    ctile += nct;
+    lv.case_ntile[B.cas] += nct;
     lv.case_ncell[B.cas] += (B.nx - 1) * (B.ny - 1);
     for (int s = 0; s < B.nsub; s++) {
       const int *c = &B.bc[9 * s];
@@ -395,6 +398,7 @@ int build_level(ec2d_ctx *ctx, int l) {
   L.nblk = (int)lv.blk.size();
   L.ncase = ncase;
   L.ntiles = (int)lv.tiles.size();
+  L.nctiles = (int)lv.ctiles.size();
   L.F = F;
   L.level = l;
   L.nvar = (l == 1) ? ctx->nvar : 4;
@@ -409,11 +413,13 @@ int build_level(ec2d_ctx *ctx, int l) {
   BlkDev *dblk = dalloc<BlkDev>(lv, lv.blk.size());
   SubDev *dsub = dalloc<SubDev>(lv, lv.sub.size());
   int2 *dtiles = dalloc<int2>(lv, lv.tiles.size());
-  if (!dblk || !dsub || !dtiles) return EC2D_ERR_NOMEM;
+  int2 *dctiles = dalloc<int2>(lv, lv.ctiles.size());
+  if (!dblk || !dsub || !dtiles || !dctiles) return EC2D_ERR_NOMEM;
   CK(cudaMemcpy(dblk, lv.blk.data(), lv.blk.size() * sizeof(BlkDev), cudaMemcpyHostToDevice));
   if (!lv.sub.empty()) CK(cudaMemcpy(dsub, lv.sub.data(), lv.sub.size() * sizeof(SubDev), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(dtiles, lv.tiles.data(), lv.tiles.size() * sizeof(int2), cudaMemcpyHostToDevice));
-  L.blk = dblk; L.sub = dsub; L.tiles = dtiles; L.cs = ctx->d_cases;
+  CK(cudaMemcpy(dctiles, lv.ctiles.data(), lv.ctiles.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  L.blk = dblk; L.sub = dsub; L.tiles = dtiles; L.ctiles = dctiles; L.cs = ctx->d_cases;
   L.U = dalloc<double>(lv, nv * F);
   L.q = dalloc<double>(lv, NQ * F);
   L.amu = dalloc<double>(lv, F);
@@ -447,7 +453,7 @@ int build_level(ec2d_ctx *ctx, int l) {
     L.bcn = nbcn ? dalloc<double2>(lv, nbcn) : nullptr;
     if (nbcn && !L.bcn) return EC2D_ERR_NOMEM;
   }
-  L.npart = dalloc<double>(lv, lv.tiles.size() * 12);
+  L.npart = dalloc<double>(lv, lv.ctiles.size() * 12);
   L.norms = dalloc<double>(lv, ncase * 12);
   L.status = dalloc<int>(lv, ncase * 4);
   L.silent_band_edge = ctx->silent_band_edge ? 1 : 0;

@@ -81,7 +81,9 @@ struct Lvl {
   const BlkDev *blk;
   const SubDev *sub;
   const CaseDev *cs;
-  const int2 *tiles;        // (block, first linear index) of 256-item tiles
+  const int2 *tiles;        // (block, first linear index) of the extended window's tiles
+  const int2 *ctiles;       // the same over the core window (core_ij)
+  int nctiles;
   double *U, *q, *amu, *amut, *res, *lc, *du, *geo, *un, *deltu, *qf, *un1;
   double *fi, *fj;          // face-flux scratch, 6 planes each
   double *tb;               // turbulence scratch planes
@@ -110,6 +112,25 @@ constexpr int EC2D_TILE = 128;
 
 __host__ __device__ __forceinline__ long long fidx(const BlkDev &b, int i, int j) {
   return b.off + (long long)(j + 2) * b.P + (i + 2);
+}
+
+// Tiles of a level come in two windows per block.  The extended window
+// (Lvl::tiles, i = -1..nx+1, j = -1..ny+1) reaches the second ghost layer,
+// where the primitives and the explicit updates are formed.  The core window
+// (Lvl::ctiles, i = 0..nx, j = 0..ny) holds every face, every interior cell
+// and the range of Set_Un: the face, residual, norm and record kernels walk
+// it.  On two blocks of 97 x 97 nodes the extended window takes 158 tiles and
+// the core window 152, so those kernels give no SM of the 152 a second CTA
+// (whose warps would share sub-partitions and double the FP64 chain time).
+__device__ __forceinline__ bool core_ij(const Lvl &L, int &bk, int &i, int &j) {
+  const int2 t = L.ctiles[blockIdx.x];
+  bk = t.x;
+  const BlkDev &b = L.blk[bk];
+  const int W = b.nx + 1, lin = t.y + (int)threadIdx.x;
+  if (lin >= W * (b.ny + 1)) return false;
+  i = lin % W;
+  j = lin / W;
+  return true;
 }
 
 // Reciprocal on the face and wavefront paths.  FP64: the hardware's

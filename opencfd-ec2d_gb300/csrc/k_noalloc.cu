@@ -4,10 +4,11 @@
 // memory is owned by another allocator or framework memory pool, or a host
 // that must not allocate once its run has started (fixed memory budget).
 // ec2d_residual_norms_noalloc gives them the max / sum-of-squares residual
-// norms of a residual array they already hold on the device.  It is the
-// two-pass tile reduction of the context path (tile_partials/final_norm in
-// k_residual.cu), but its tile partials live in a file-scope __device__ array
-// instead of context scratch.  As there, the max is taken on the bit patterns
+// norms of a residual array they already hold on the device.  It has the
+// two-pass structure of the context path's reduction (tile partials, then a
+// per-quantity pass over them; k_residual.cu), with plain warp trees, and its
+// tile partials live in a file-scope __device__ array instead of context
+// scratch.  As there, the max is taken on the bit patterns
 // of |Res| (non-negative doubles order like their bits as integers), so a NaN
 // residual gives a NaN max instead of being dropped as fmax would drop it.
 //

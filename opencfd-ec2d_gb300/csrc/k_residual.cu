@@ -6,9 +6,11 @@
 //   k_flux_i/j  reconstruction + Riemann flux + viscous stress  Residual_FVM face loops
 //   k_res       flux differences, spectral radii, time step    Residual_FVM:460-468, comput_Lvc, comput_dt
 //   k_norm_*    max / RMS residual norms, deterministic order  sub_Residual.f90:72-106
-// Work is distributed by 256-item tiles of each block's extended index range
-// [-1,nx+1] x [-1,ny+1]; a kernel maps the tile item to (i,j) and keeps the
-// items that lie in its own index range.
+// Work is distributed by EC2D_TILE-item tiles of each block's extended index
+// range [-1,nx+1] x [-1,ny+1] (k_prim: the primitives of both ghost layers)
+// or of its core range [0,nx] x [0,ny] (the face, residual and norm kernels,
+// core_ij); a kernel maps the tile item to (i,j) and keeps the items that lie
+// in its own index range.
 #include "ec2d_dev.cuh"
 #include "ec2d_internal.h"
 
@@ -68,7 +70,7 @@ __device__ __forceinline__ bool in_fdm_core(const BlkDev &b, int i, int j) {
 template <typename T>
 __global__ void __launch_bounds__(TILE) k_flux_i(Lvl L) {
   int bk, i, j;
-  if (!tile_ij(L, bk, i, j)) return;
+  if (!core_ij(L, bk, i, j)) return;
   const BlkDev &b = L.blk[bk];
   if (i < 1 || i > b.nx || j < 1 || j > b.ny - 1) return;
   if (in_fdm_core(b, i, j)) return;
@@ -127,7 +129,7 @@ __global__ void __launch_bounds__(TILE) k_flux_i(Lvl L) {
 template <typename T>
 __global__ void __launch_bounds__(TILE) k_flux_j(Lvl L) {
   int bk, i, j;
-  if (!tile_ij(L, bk, i, j)) return;
+  if (!core_ij(L, bk, i, j)) return;
   const BlkDev &b = L.blk[bk];
   if (i < 1 || i > b.nx - 1 || j < 1 || j > b.ny) return;
   if (in_fdm_core(b, i, j)) return;
@@ -200,20 +202,73 @@ __device__ __forceinline__ double warp_sum(double q) {
   return q;
 }
 
+// NV variables (4 or 8) reduced over a warp at once by a transposed
+// butterfly: at each of the first log2(NV) exchanges a lane keeps half of the
+// variables it carries and combines them with its partner's copies, so one
+// instruction serves several variables (four sums take 2 + 1 + 3 FP64 adds per
+// lane instead of 4 x 5, eight take 4 + 2 + 1 + 2 instead of 8 x 5).  Lane l
+// ends with the warp's value of variable l / (32 / NV); every lane of that
+// group holds the same bits (each exchange adds the same two operands on both
+// sides), and the order of the operations is fixed.
+struct OpMax { __device__ long long operator()(long long a, long long b) const { return max(a, b); } };
+struct OpAdd { __device__ double operator()(double a, double b) const { return a + b; } };
+template <int NV, typename T, typename Op>
+__device__ __forceinline__ T warp_reduce_vars(const T (&v)[NV], Op op) {
+  static_assert(NV == 4 || NV == 8, "four or eight variables");
+  constexpr int R = NV == 4 ? 2 : 3;  // exchanges that halve the variables
+  const int lane = threadIdx.x & 31;
+  T c[NV];
+#pragma unroll
+  for (int k = 0; k < NV; k++) c[k] = v[k];
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const int o = 16 >> r, n = NV >> (r + 1);  // lanes o apart; variables kept
+    const bool hi = lane & o;
+#pragma unroll
+    for (int k = 0; k < NV / 2; k++) {
+      if (k < n) {
+        const T keep = hi ? c[n + k] : c[k], send = hi ? c[k] : c[n + k];
+        c[k] = op(keep, __shfl_xor_sync(0xffffffffu, send, o));
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 32 / NV / 2; o > 0; o >>= 1) c[0] = op(c[0], __shfl_xor_sync(0xffffffffu, c[0], o));
+  return c[0];
+}
+
+// one warp's max |Res| bits and sum Res^2 of NV variables into the CTA's
+// shared arrays (column w)
+template <int NV, int NW>
+__device__ __forceinline__ void warp_partials(bool act, const double *vres, int nv, long long (*smax)[NW],
+                                              double (*ssum)[NW]) {
+  long long a[NV];
+  double q[NV];
+#pragma unroll
+  for (int m = 0; m < NV; m++) {
+    // variables past the sixth are zero at compile time (no FP64 work)
+    const double r = (m < 6 && act && m < nv) ? vres[m < 6 ? m : 0] : 0.0;
+    a[m] = __double_as_longlong(fabs(r));
+    q[m] = m < 6 ? r * r : 0.0;
+  }
+  const long long am = warp_reduce_vars<NV>(a, OpMax());
+  const double qs = warp_reduce_vars<NV>(q, OpAdd());
+  const int lane = threadIdx.x & 31, g = lane / (32 / NV);
+  if (lane % (32 / NV) == 0 && g < nv) {
+    smax[g][threadIdx.x >> 5] = am;
+    ssum[g][threadIdx.x >> 5] = qs;
+  }
+}
+
 // one CTA's partials: per variable the max |Res| and sum Res^2 of its cells
 // (NT threads in the CTA)
 template <int NT = TILE>
 __device__ __forceinline__ void tile_partials(const Lvl &L, bool act, const double *vres) {
   __shared__ long long smax[6][NT / 32];
   __shared__ double ssum[6][NT / 32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nv = L.nvar;
-#pragma unroll
-  for (int m = 0; m < 6; m++) {
-    if (m >= nv) break;
-    const long long a = warp_max_bits(act ? __double_as_longlong(fabs(vres[m])) : 0ll);
-    const double q = warp_sum(act ? vres[m] * vres[m] : 0.0);
-    if (lane == 0) { smax[m][w] = a; ssum[m][w] = q; }
-  }
+  const int nv = L.nvar;
+  if (nv <= 4) warp_partials<4, NT / 32>(act, vres, nv, smax, ssum);
+  else warp_partials<8, NT / 32>(act, vres, nv, smax, ssum);
   __syncthreads();
   if (threadIdx.x < 6) {
     const int m = threadIdx.x;
@@ -227,20 +282,30 @@ __device__ __forceinline__ void tile_partials(const Lvl &L, bool act, const doub
 }
 
 // per case and quantity (max[6], rms[6]) from the tile partials: one warp per
-// (case, quantity), lanes over tiles, then the warp tree
+// (case, quantity), lanes over tiles with four loads in flight per lane (four
+// accumulators in a fixed order), then the warp tree
 __device__ __forceinline__ void final_norm(const Lvl &L, int cs, int m) {
   const int lane = threadIdx.x & 31;
-  const int t0 = L.case_tile0[cs], nt = L.case_ntile[cs];
+  const int nt = L.case_ntile[cs];
+  const double *p = L.npart + (size_t)L.case_tile0[cs] * 12 + m;
   double out = 0.0;
   if (m < 6) {
-    long long a = 0;
-    for (int t = lane; t < nt; t += 32) a = max(a, __double_as_longlong(L.npart[(size_t)(t0 + t) * 12 + m]));
-    out = __longlong_as_double(warp_max_bits(a));
+    long long a[4] = {0, 0, 0, 0};
+    for (int t = lane; t < nt; t += 128) {
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+        if (t + 32 * k < nt) a[k] = max(a[k], __double_as_longlong(p[(size_t)(t + 32 * k) * 12]));
+    }
+    out = __longlong_as_double(warp_max_bits(max(max(a[0], a[1]), max(a[2], a[3]))));
   } else {
-    double q = 0.0;
-    for (int t = lane; t < nt; t += 32) q += L.npart[(size_t)(t0 + t) * 12 + m];
-    q = warp_sum(q);
-    out = (m - 6 < L.nvar) ? sqrt(q / (1.0 * L.case_ncell[cs])) : 0.0;
+    double q[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int t = lane; t < nt; t += 128) {
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+        if (t + 32 * k < nt) q[k] += p[(size_t)(t + 32 * k) * 12];
+    }
+    const double s = warp_sum((q[0] + q[1]) + (q[2] + q[3]));
+    out = (m - 6 < L.nvar) ? sqrt(s / (1.0 * L.case_ncell[cs])) : 0.0;
   }
   if (lane == 0) L.norms[cs * 12 + m] = out;
 }
@@ -257,7 +322,7 @@ __device__ __forceinline__ void final_norm(const Lvl &L, int cs, int m) {
 template <bool NORM, bool FINAL>
 __global__ void __launch_bounds__(TILE) k_res(Lvl L, int post) {
   int bk, i, j;
-  bool act = tile_ij(L, bk, i, j);
+  bool act = core_ij(L, bk, i, j);
   if (act) {
     const BlkDev &b0 = L.blk[bk];
     if ((post & RES_SET_UN) && i >= 0 && i <= b0.nx && j >= 0 && j <= b0.ny) {
@@ -289,7 +354,9 @@ __global__ void __launch_bounds__(TILE) k_res(Lvl L, int post) {
       }
     }
     if (NORM)
-      for (int m = 4; m < L.nvar; m++) vres[m] = L.res[m * F + id];
+#pragma unroll
+      for (int m = 4; m < 6; m++)
+        if (m < L.nvar) vres[m] = L.res[m * F + id];  // constant indices: vres stays in registers
     const double *g = L.geo + id;
     const double s0 = g[G_VOL * F];
     const double si = g[G_SIA * F], ni1 = g[G_NI1A * F], ni2 = g[G_NI2A * F];
@@ -547,12 +614,14 @@ __global__ void __launch_bounds__(TILE) k_norm_partial(Lvl L) {
   int bk, i, j;
   double vres[6] = {0, 0, 0, 0, 0, 0};
   bool act = false;
-  if (tile_ij(L, bk, i, j)) {
+  if (core_ij(L, bk, i, j)) {
     const BlkDev &b = L.blk[bk];
     if (i >= 1 && i <= b.nx - 1 && j >= 1 && j <= b.ny - 1) {
       act = true;
       long long id = fidx(b, i, j);
-      for (int m = 0; m < L.nvar; m++) vres[m] = L.res[m * L.F + id];
+#pragma unroll
+      for (int m = 0; m < 6; m++)
+        if (m < L.nvar) vres[m] = L.res[m * L.F + id];
     }
   }
   tile_partials(L, act, vres);
@@ -612,20 +681,20 @@ void launch_face_metrics(const Lvl &L, cudaStream_t s) { k_face_metrics<<<L.ntil
 
 void launch_prim(const Lvl &L, cudaStream_t s) { k_prim<<<L.ntiles, TILE, 0, s>>>(L); }
 void launch_flux_i(const Lvl &L, bool fp32, cudaStream_t s) {
-  if (fp32) k_flux_i<float><<<L.ntiles, TILE, 0, s>>>(L);
-  else k_flux_i<double><<<L.ntiles, TILE, 0, s>>>(L);
+  if (fp32) k_flux_i<float><<<L.nctiles, TILE, 0, s>>>(L);
+  else k_flux_i<double><<<L.nctiles, TILE, 0, s>>>(L);
 }
 void launch_flux_j(const Lvl &L, bool fp32, cudaStream_t s) {
-  if (fp32) k_flux_j<float><<<L.ntiles, TILE, 0, s>>>(L);
-  else k_flux_j<double><<<L.ntiles, TILE, 0, s>>>(L);
+  if (fp32) k_flux_j<float><<<L.nctiles, TILE, 0, s>>>(L);
+  else k_flux_j<double><<<L.nctiles, TILE, 0, s>>>(L);
 }
 // with_norms: the tile partials inside k_res; with few cases the last CTA of
 // k_res also forms the per-case norms (norms_fused_final() tells the caller)
 bool norms_fused_final(const Lvl &L) { return L.ncase <= 8; }
 void launch_res(const Lvl &L, bool with_norms, int post, cudaStream_t s) {
-  if (!with_norms) k_res<false, false><<<L.ntiles, TILE, 0, s>>>(L, post);
-  else if (norms_fused_final(L)) k_res<true, true><<<L.ntiles, TILE, 0, s>>>(L, post);
-  else k_res<true, false><<<L.ntiles, TILE, 0, s>>>(L, post);
+  if (!with_norms) k_res<false, false><<<L.nctiles, TILE, 0, s>>>(L, post);
+  else if (norms_fused_final(L)) k_res<true, true><<<L.nctiles, TILE, 0, s>>>(L, post);
+  else k_res<true, false><<<L.nctiles, TILE, 0, s>>>(L, post);
 }
 // Lr: the level with npart, case_tile0, case_ntile and nctr of the 2-D tile list
 void launch_residual_tile(const Lvl &Lr, const int4 *rt, int ntiles, bool with_norms, int post, cudaStream_t s) {
@@ -634,7 +703,7 @@ void launch_residual_tile(const Lvl &Lr, const int4 *rt, int ntiles, bool with_n
   else k_residual_tile<true, false><<<ntiles, RNT, 0, s>>>(Lr, rt, post);
 }
 void launch_norms(const Lvl &L, bool partials, cudaStream_t s) {
-  if (partials) k_norm_partial<<<L.ntiles, TILE, 0, s>>>(L);
+  if (partials) k_norm_partial<<<L.nctiles, TILE, 0, s>>>(L);
   k_norm_final<<<L.ncase, 384, 0, s>>>(L);
 }
 

@@ -115,11 +115,9 @@ template <int NV>
 // whose residual was evaluated on entry, Add_force_function)
 __global__ void __launch_bounds__(TILE) k_lusgs_prep(Lvl L, double alfa1, int force) {
   using RC = Rec<NV>;
-  int2 t = L.tiles[blockIdx.x];
-  const BlkDev &b = L.blk[t.x];
-  int W = b.nx + 3, lin = t.y + threadIdx.x;
-  if (lin >= W * (b.ny + 3)) return;
-  int i = lin % W - 1, j = lin / W - 1;
+  int bk, i, j;
+  if (!core_ij(L, bk, i, j)) return;
+  const BlkDev &b = L.blk[bk];
   if (i < 1 || i > b.nx - 1 || j < 1 || j > b.ny - 1) return;
   const CaseDev &c = L.cs[b.cas];
   const long long F = L.F, P = b.P;
@@ -1047,7 +1045,7 @@ size_t smem_bytes(int R, int th) {
 template <int NV>
 void sweep_nv(const Lvl &L, double alfa1, int mode, int max_rows, int max_cols, int cs, int rpw, int lanes,
               cudaStream_t s) {
-  if (!(mode & LUSGS_SWEEP_ONLY)) k_lusgs_prep<NV><<<L.ntiles, TILE, 0, s>>>(L, alfa1, mode & LUSGS_FORCE);
+  if (!(mode & LUSGS_SWEEP_ONLY)) k_lusgs_prep<NV><<<L.nctiles, TILE, 0, s>>>(L, alfa1, mode & LUSGS_FORCE);
   if (mode & LUSGS_PREP_ONLY) return;
   const int update = mode & LUSGS_UPDATE;
   if (cs == 0) {

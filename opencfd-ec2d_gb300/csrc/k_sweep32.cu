@@ -60,11 +60,9 @@ struct S32 {
 template <int NV>
 __global__ void __launch_bounds__(TILE) k_lusgs_prep32(Lvl L, double alfa1, int force) {
   using RC = R32<NV>;
-  int2 t = L.tiles[blockIdx.x];
-  const BlkDev &b = L.blk[t.x];
-  int W = b.nx + 3, lin = t.y + threadIdx.x;
-  if (lin >= W * (b.ny + 3)) return;
-  int i = lin % W - 1, j = lin / W - 1;
+  int bk, i, j;
+  if (!core_ij(L, bk, i, j)) return;
+  const BlkDev &b = L.blk[bk];
   if (i < 1 || i > b.nx - 1 || j < 1 || j > b.ny - 1) return;
   const CaseDev &c = L.cs[b.cas];
   const long long F = L.F, P = b.P;
@@ -318,7 +316,7 @@ size_t smem32(int rows) {
 
 template <int NV>
 void sweep32_nv(const Lvl &L, double alfa1, int mode, int max_rows, cudaStream_t s) {
-  k_lusgs_prep32<NV><<<L.ntiles, TILE, 0, s>>>(L, alfa1, mode & LUSGS_FORCE);
+  k_lusgs_prep32<NV><<<L.nctiles, TILE, 0, s>>>(L, alfa1, mode & LUSGS_FORCE);
   const int update = mode & LUSGS_UPDATE;
   int th = ((max_rows + 31) / 32) * 32;
   size_t smem = smem32<NV>(max_rows);
