@@ -670,7 +670,7 @@ void residual(ec2d_ctx *ctx, int l, int post = 0) {
   const bool fused = !L.fdm && !dual;  // Res final after k_res: norm partials fused into it
   // Within a step the norms of an evaluation whose Res stays as k_res
   // leaves it (no forcing added) go to the norms branch: the kernels that
-  // follow read Res, and the norms are read after the step.  k_res without
+  // follow only read Res, and the norms are read after the step.  k_res without
   // them is about half as long (7 against 14 us per launch on the flat
   // plate's levels); the partials and the reduction are the same kernels
   // as for the FDM patch, so the norms are bit-identical either way.
@@ -928,7 +928,14 @@ void mg3(ec2d_ctx *ctx) {
 }
 
 int one_step(ec2d_ctx *ctx) {
-  if (ctx->num_mesh == 1) return time_advance(ctx, 1);
+  if (ctx->num_mesh == 1) {
+    // dual time stepping reads the norms on the host inside the step
+    ctx->norm_branch = ctx->P.Time_Method != Time_Dual;
+    const int r = time_advance(ctx, 1);
+    ctx->norm_branch = false;
+    join_norms(ctx, 1);
+    return r;
+  }
   ctx->norm_branch = true;
   if (ctx->num_mesh == 2) mg2(ctx);
   else mg3(ctx);
