@@ -323,6 +323,7 @@ int build_level(ec2d_ctx *ctx, int l) {
       // the copied strip must have the same cell count on both sides
       if ((sd.iend - sd.ist + sd.jend - sd.jst) != (c1[3] - c1[2] + c1[5] - c1[4])) return EC2D_ERR_ARG;
       sd.nbk = nb; sd.nface = c1[1]; sd.nist = c1[2]; sd.niend = c1[3]; sd.njst = c1[4]; sd.njend = c1[5];
+      sd.nP = lv.blk[nb].P; sd.noff = lv.blk[nb].off;
     }
   }
   // physical boundary conditions: a subface joins the earliest barrier phase

@@ -60,6 +60,8 @@ struct SubDev {
   int phase, nitem;         // physical BC: barrier phase within the block, work items
   int nbk;                  // level-global index of the neighbour block (-1: physical)
   int nface, nist, niend, njst, njend;  // the neighbour subface it reads
+  int nP;                   // the neighbour block's frame pitch and offset (halo copy)
+  long long noff;
   int nrm0;                 // far-field / symmetry: first node's entry in Lvl::bcn (-1: none)
 };
 

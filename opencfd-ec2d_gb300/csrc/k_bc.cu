@@ -212,19 +212,28 @@ __device__ void corner(const Lvl &L, const CaseDev &c, long long i1, long long i
 
 // phases: 1 physical BCs, 2 halo copy, 4 corners, 8 nu~/k/omega clip
 constexpr int BC_SMEM_SUBS = 32;  // subfaces of a block staged in shared memory
+// Threads per block's CTA.  A phase costs the longest chain of its threads
+// (a far-field item is some 45 dependent FP64 operations), so a thread that
+// takes a second item doubles the phase: 512 threads give one item per
+// thread to the phases of blocks up to 2 x 256 boundary items (the flat
+// plate's 96-cell blocks have 384 in their single physical phase).
+constexpr int BC_THREADS = 512;
 
-__global__ void __launch_bounds__(256) k_bc(Lvl L, int phases) {
+__global__ void __launch_bounds__(BC_THREADS, 1) k_bc(Lvl L, int phases) {
   const int bk = blockIdx.x;
   const BlkDev &b = L.blk[bk];
   const CaseDev &c = L.cs[b.cas];
   const long long F = L.F;
-  if (phases & 1) {
-    // the block's subface table in shared memory (global beyond 32)
-    __shared__ SubDev ssub[BC_SMEM_SUBS];
-    const int nsub = b.nsub;
+  // the block's subface table in shared memory (global beyond 32), read by
+  // the physical and the halo phases
+  __shared__ SubDev ssub[BC_SMEM_SUBS];
+  const int nsub = b.nsub;
+  if (phases & 3) {
     for (int ks = threadIdx.x; ks < min(nsub, BC_SMEM_SUBS); ks += blockDim.x) ssub[ks] = L.sub[b.sub0 + ks];
     __syncthreads();
-    auto sub = [&](int ks) -> const SubDev & { return ks < BC_SMEM_SUBS ? ssub[ks] : L.sub[b.sub0 + ks]; };
+  }
+  auto sub = [&](int ks) -> const SubDev & { return ks < BC_SMEM_SUBS ? ssub[ks] : L.sub[b.sub0 + ks]; };
+  if (phases & 1) {
     // subfaces of one phase touch disjoint cells (grouped at set-up in
     // subface order): their items are spread over the CTA together
     for (int ph = 0; ph < b.nphase; ph++) {
@@ -256,10 +265,9 @@ __global__ void __launch_bounds__(256) k_bc(Lvl L, int phases) {
     }
   }
   if (phases & 2) {
-    for (int ks = 0; ks < b.nsub; ks++) {
-      const SubDev s = L.sub[b.sub0 + ks];
+    for (int ks = 0; ks < nsub; ks++) {
+      const SubDev &s = sub(ks);
       if (s.neighb < 0) continue;
-      const BlkDev &nb = L.blk[s.nbk];
       int n1 = s.iend - s.ist + s.jend - s.jst;
       for (int t = threadIdx.x; t < n1 * LAP; t += blockDim.x) {
         int l = t % LAP + 1, k = t / LAP + 1;
@@ -274,7 +282,7 @@ __global__ void __launch_bounds__(256) k_bc(Lvl L, int phases) {
         else if (s.face == 2) { di = s.ist + k - 1; dj = s.jst - LAP - 1 + l; }
         else if (s.face == 3) { di = s.iend + l - 1; dj = s.jst + k - 1; }
         else { di = s.ist + k - 1; dj = s.jend + l - 1; }
-        long long src = fidx(nb, si, sj), dst = fidx(b, di, dj);
+        long long src = s.noff + (long long)(sj + 2) * s.nP + (si + 2), dst = fidx(b, di, dj);
         for (int m = 0; m < L.nvar; m++) L.U[m * F + dst] = L.U[m * F + src];
       }
     }
@@ -300,7 +308,7 @@ __global__ void __launch_bounds__(256) k_bc(Lvl L, int phases) {
   }
 }
 
-void launch_bc(const Lvl &L, int phases, cudaStream_t s) { k_bc<<<L.nblk, 256, 0, s>>>(L, phases); }
+void launch_bc(const Lvl &L, int phases, cudaStream_t s) { k_bc<<<L.nblk, BC_THREADS, 0, s>>>(L, phases); }
 
 // set-up: the edge normals of every far-field and symmetry node (grid y: block)
 __global__ void __launch_bounds__(256) k_bc_normals(Lvl L) {
