@@ -139,7 +139,10 @@ int ec2d_block_dims(ec2d_ctx *ctx, int case_id, int mesh, int block, int *nx, in
 
 /* Freestream start including the coarse-to-fine pre-iterations
  * (init_flow_zero, sub_init.f90:423-495) for every case; clears every
- * case's status word. */
+ * case's status word.  Like the reference's start, which follows the mesh
+ * set-up, it runs with the coarse forcing QF zero, the dual-time first-step
+ * flags unset and the step counters and times at zero, so a context that has
+ * stepped before (or been autotuned) starts exactly as a new one. */
 int ec2d_init_flow(ec2d_ctx *ctx);
 
 /* Copy the conservative field of one block in or out, Fortran layout
@@ -356,7 +359,11 @@ int ec2d_mlp_predict(ec2d_mlp *m, const float *feat, long long n, float *pred);
  * whether independent kernels run concurrently on two stream pairs (the i-
  * and j-face flux kernels; at a multigrid transfer the fine residual and the
  * restriction + coarse boundary conditions + coarse entry residual).
- * The fine-mesh U and the step counters are restored afterwards.  Outputs
+ * The fine-mesh U and the step counters (with dual time stepping also the
+ * two physical time levels and the first-step flags) are restored
+ * afterwards; other scratch of the steps (residuals, coarse levels, the
+ * coarse forcing) is formed anew before the next step or ec2d_init_flow
+ * reads it.  Outputs
  * (may be NULL): the choices and the winner's milliseconds per step.  The
  * default shape, before any autotune, is 0 with 12-row bands; the
  * environment variables EC2D_LUSGS_CLUSTER and EC2D_LUSGS_ROWS read by
@@ -380,6 +387,33 @@ int ec2d_lusgs_shape(ec2d_ctx *ctx, int *lusgs_cs, int *rows, int *lanes);
  * picks the faster; EC2D_TILE_RESIDUAL=1 read by ec2d_create starts with the
  * one-kernel form. */
 int ec2d_tile_residual(ec2d_ctx *ctx, int enable, int *current);
+
+/* The launch choices ec2d_autotune makes, read and set directly, so that a
+ * host can keep the winners of one autotune and reuse them in later runs of
+ * the same cases without timing the candidates again.  No counterpart in the
+ * reference.  lusgs_cs and rows as in ec2d_autotune, lanes 4 or 8 (0: by the
+ * band height, eight up to 16 rows), concurrent and tile_residual 0 or 1
+ * (see ec2d_autotune and ec2d_tile_residual).  ec2d_set_launch_config takes
+ * the ranges the EC2D_LUSGS_* variables take (lusgs_cs 0..8, rows 4..32);
+ * where a level cannot take a wavefront shape the launcher falls back to one
+ * it can, as it does for any shape.  None of the choices changes the
+ * discretisation: the wavefront shape changes only the summation order of
+ * the sweep's records, the other two nothing.  Setting drops the captured
+ * step graph; the next ec2d_step captures the new launches.  Outputs of
+ * ec2d_launch_config may be NULL. */
+int ec2d_launch_config(ec2d_ctx *ctx, int *lusgs_cs, int *rows, int *lanes, int *concurrent, int *tile_residual);
+int ec2d_set_launch_config(ec2d_ctx *ctx, int lusgs_cs, int rows, int lanes, int concurrent, int tile_residual);
+/* A one-line description of everything the launch choices depend on, after
+ * ec2d_setup: the library version and a digest of its sources, the device
+ * (name, compute capability, SM count), the method flags, the LU-SGS and
+ * coarse precisions, the coarse eddy-viscosity option, the number of cases,
+ * and per multigrid level the variables and every block shape in cells with
+ * its count.  Contexts with equal signatures time their candidates alike, so
+ * a host keys its cache of ec2d_autotune results by it (ec2d/tuning.py keeps
+ * one as a JSON file).  No counterpart in the reference.  *needed (may be
+ * NULL) receives the length including the terminating NUL; buf = NULL only
+ * queries it; a buf shorter than that returns EC2D_ERR_ARG. */
+int ec2d_launch_signature(ec2d_ctx *ctx, char *buf, int len, int *needed);
 
 /* Multigrid with a turbulence model: the coarse levels keep an eddy
  * viscosity restricted from the next finer level (enable = 1; the mean of a

@@ -261,6 +261,25 @@ module ec2d_gpu_mod
       integer(c_int) :: lusgs_cs, rows_per_warp, concurrent
       real(c_double) :: ms_per_step
     end function
+    ! the autotuner's choices, read and applied without timing (a host keeps
+    ! them per launch signature: buf receives a NUL-terminated line)
+    integer(c_int) function ec2d_launch_config(ctx, lusgs_cs, rows, lanes, concurrent, tile_residual) bind(C)
+      import
+      type(c_ptr), value :: ctx
+      integer(c_int) :: lusgs_cs, rows, lanes, concurrent, tile_residual
+    end function
+    integer(c_int) function ec2d_set_launch_config(ctx, lusgs_cs, rows, lanes, concurrent, tile_residual) bind(C)
+      import
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lusgs_cs, rows, lanes, concurrent, tile_residual
+    end function
+    integer(c_int) function ec2d_launch_signature(ctx, buf, len, needed) bind(C)
+      import
+      type(c_ptr), value :: ctx
+      character(kind=c_char) :: buf(*)
+      integer(c_int), value :: len
+      integer(c_int) :: needed
+    end function
     integer(c_int) function ec2d_set_case_shape(ctx, case_id, shape) bind(C)
       import
       type(c_ptr), value :: ctx

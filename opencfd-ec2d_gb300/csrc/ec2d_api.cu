@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <set>
 #include <string>
@@ -1259,6 +1260,16 @@ int ec2d_init_flow(ec2d_ctx *ctx) {
   int rc = ec2d_clear_status(ctx, 0);  // a fresh start: no case carries a stop
   if (rc) return rc;
   int nm = ctx->num_mesh;
+  // the reference starts (init_flow_zero) right after the meshes are made,
+  // with the coarse forcing QF zero (sub_init.f90:315), which the coarse
+  // pre-steps below add (sub_NS_singlegrid.f90:77,146), and with the dual-time
+  // first-step flags unset and the step counters at zero: a context that has
+  // stepped, or been autotuned, starts here exactly as a new one does
+  for (int l = 2; l <= nm; l++)
+    CK(cudaMemsetAsync(ctx->lv[l].L.qf, 0, (size_t)4 * ctx->lv[l].F * sizeof(double), ctx->stream));
+  ctx->dual_iflag = ctx->dual_iflag1 = 0;
+  for (auto &c : ctx->cases)
+    for (int l = 0; l < 4; l++) { c.kstep[l] = 0; c.tt[l] = 0.0; }
   // coarse eddy viscosity (kept between residuals only with the multigrid
   // eddy-viscosity extension): zero until the first restriction
   for (int l = 2; l <= nm; l++)
@@ -1447,12 +1458,20 @@ int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *rows_per_w
   if (!ctx || !ctx->setup_done || trial_steps < 1) return EC2D_ERR_ARG;
   cudaSetDevice(ctx->device);
   // snapshot of the state a trial changes: fine-mesh U and the step counters
-  // (coarse levels are rebuilt from the fine mesh by every V-cycle)
+  // (coarse levels are rebuilt from the fine mesh by every V-cycle), and with
+  // dual time stepping the two physical time levels and the first-step flags
   const Level &lv = ctx->lv[1];
   const size_t bytes = (size_t)lv.L.nvar * lv.F * sizeof(double);
+  const bool dual = ctx->P.Time_Method == Time_Dual;
+  const size_t nelem = bytes / sizeof(double);
   double *snap = nullptr;
-  CK(cudaMalloc(&snap, bytes));
+  CK(cudaMalloc(&snap, (dual ? 3 : 1) * bytes));
   CK(cudaMemcpyAsync(snap, lv.L.U, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+  if (dual) {
+    CK(cudaMemcpyAsync(snap + nelem, lv.L.un, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(snap + 2 * nelem, lv.L.un1, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  const int dflag = ctx->dual_iflag, dflag1 = ctx->dual_iflag1;
   std::vector<std::array<int, 4>> ks(ctx->cases.size());
   std::vector<std::array<double, 4>> ts(ctx->cases.size());
   for (size_t c = 0; c < ctx->cases.size(); c++)
@@ -1529,6 +1548,12 @@ int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *rows_per_w
   }
   drop_graph(ctx);
   cudaMemcpyAsync(lv.L.U, snap, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
+  if (dual) {
+    cudaMemcpyAsync(lv.L.un, snap + nelem, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaMemcpyAsync(lv.L.un1, snap + 2 * nelem, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
+  }
+  ctx->dual_iflag = dflag;
+  ctx->dual_iflag1 = dflag1;
   cudaStreamSynchronize(ctx->stream);
   cudaFree(snap);
   cudaEventDestroy(a);
@@ -1558,6 +1583,73 @@ int ec2d_tile_residual(ec2d_ctx *ctx, int enable, int *current) {
     drop_graph(ctx);
   }
   if (current) *current = ctx->tile_residual ? 1 : 0;
+  return EC2D_OK;
+}
+
+int ec2d_launch_config(ec2d_ctx *ctx, int *lusgs_cs, int *rows, int *lanes, int *concurrent, int *tile_residual) {
+  if (!ctx) return EC2D_ERR_ARG;
+  if (lusgs_cs) *lusgs_cs = ctx->lusgs_cs;
+  if (rows) *rows = ctx->lusgs_rpw;
+  if (lanes) *lanes = ctx->lusgs_lanes;
+  if (concurrent) *concurrent = ctx->concurrent ? 1 : 0;
+  if (tile_residual) *tile_residual = ctx->tile_residual ? 1 : 0;
+  return EC2D_OK;
+}
+
+// the ranges ec2d_create accepts from EC2D_LUSGS_* (the sweep launcher
+// clamps the cluster size and falls back from shapes a level cannot take)
+int ec2d_set_launch_config(ec2d_ctx *ctx, int lusgs_cs, int rows, int lanes, int concurrent, int tile_residual) {
+  if (!ctx || lusgs_cs < 0 || lusgs_cs > 8 || rows < 4 || rows > 32 || (lanes != 0 && lanes != 4 && lanes != 8) ||
+      concurrent < 0 || concurrent > 1 || tile_residual < 0 || tile_residual > 1)
+    return EC2D_ERR_ARG;
+  if (lusgs_cs != ctx->lusgs_cs || rows != ctx->lusgs_rpw || lanes != ctx->lusgs_lanes ||
+      (concurrent != 0) != ctx->concurrent || (tile_residual != 0) != ctx->tile_residual) {
+    ctx->lusgs_cs = lusgs_cs;
+    ctx->lusgs_rpw = rows;
+    ctx->lusgs_lanes = lanes;
+    ctx->concurrent = concurrent != 0;
+    ctx->tile_residual = tile_residual != 0;
+    drop_graph(ctx);
+  }
+  return EC2D_OK;
+}
+
+// digest of the library's sources, written by the build (ec2d_build.py)
+extern "C" const char ec2d_internal_build_id[];
+
+int ec2d_launch_signature(ec2d_ctx *ctx, char *buf, int len, int *needed) {
+  if (!ctx || !ctx->setup_done || len < 0) return EC2D_ERR_ARG;
+  cudaDeviceProp pr;
+  CK(cudaGetDeviceProperties(&pr, ctx->device));
+  const ec2d_params &P = ctx->P;
+  char t[512];
+  snprintf(t, sizeof t, "ec2d-launch-1 lib=%d build=%s dev=%s sm=%d%d sms=%d", ec2d_version(),
+           ec2d_internal_build_id, pr.name, pr.major, pr.minor, pr.multiProcessorCount);
+  std::string s = t;
+  snprintf(t, sizeof t,
+           " visc=%d turb=%d time=%d local_dt=%d scheme=%d flux=%d recon=%d mesh=%d mg_lusgs=%d lusgs=%d"
+           " coarse=%d mg_amut=%d cases=%d",
+           P.If_viscous, P.Iflag_turbulence_model, P.Time_Method, P.Iflag_local_dt, P.Iflag_Scheme, P.Iflag_flux,
+           P.IFlag_Reconstruction, ctx->num_mesh, P.mg_lusgs, ctx->lusgs_fp32 ? 32 : 64, ctx->coarse_fp32 ? 32 : 64,
+           ctx->mg_amut ? 1 : 0, (int)ctx->cases.size());
+  s += t;
+  // per level: variables, then each block shape (cells, 'f' on finite-
+  // difference blocks) with its count, in sorted order
+  for (int l = 1; l <= ctx->num_mesh; l++) {
+    std::map<std::array<int, 3>, int> shapes;
+    for (const HLevelBlock &hb : ctx->lv[l].hb) shapes[{hb.nx - 1, hb.ny - 1, hb.fdm ? 1 : 0}]++;
+    snprintf(t, sizeof t, " L%d:nv%d", l, ctx->lv[l].L.nvar);
+    s += t;
+    for (const auto &kv : shapes) {
+      snprintf(t, sizeof t, ",%dx%d%s*%d", kv.first[0], kv.first[1], kv.first[2] ? "f" : "", kv.second);
+      s += t;
+    }
+  }
+  const int n = (int)s.size() + 1;
+  if (needed) *needed = n;
+  if (!buf) return EC2D_OK;
+  if (len < n) return EC2D_ERR_ARG;
+  memcpy(buf, s.c_str(), (size_t)n);
   return EC2D_OK;
 }
 

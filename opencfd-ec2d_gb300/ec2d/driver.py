@@ -10,7 +10,13 @@ its own while the steps go on, and the files of a snapshot are written once
 the next snapshot is taken or the run ends, so the marching does not wait for
 the device-to-host copy.
 
-  python -m ec2d.driver <case_dir> [--steps N] [--fix-nvar-restart]
+With a tuning cache (--tuning-cache FILE, or the EC2D_TUNING_CACHE
+environment variable) the launch choices of the autotuner are taken from the
+file when this case's launch signature is stored there, and otherwise timed
+once and added to it (ec2d/tuning.py); without one the library's default
+choices are used.
+
+  python -m ec2d.driver <case_dir> [--steps N] [--fix-nvar-restart] [--tuning-cache FILE]
 """
 from __future__ import annotations
 
@@ -18,7 +24,7 @@ import argparse
 import os
 import time
 
-from . import gpu, inputs, outputs
+from . import gpu, inputs, outputs, tuning
 
 
 def read_fdm(directory: str):
@@ -32,7 +38,8 @@ def read_fdm(directory: str):
     return [int(lines[6 + k].split()[0]) for k in range(n)]
 
 
-def run(directory: str, steps: int = None, device: int = 0, fix_nvar: bool = False, quiet: bool = False) -> dict:
+def run(directory: str, steps: int = None, device: int = 0, fix_nvar: bool = False, quiet: bool = False,
+        tuning_cache: str = None) -> dict:
     p, blocks = inputs.read_case(directory)
     fdm = read_fdm(directory)
     s = gpu.Solver([(p, blocks)], device=device, fdm_blocks=[fdm])
@@ -40,6 +47,10 @@ def run(directory: str, steps: int = None, device: int = 0, fix_nvar: bool = Fal
         s.init_flow()
     else:
         outputs.restart(s, directory, fix_nvar=fix_nvar)
+    tuned = None
+    if tuning_cache or os.environ.get(tuning.ENV):
+        # the autotuner restores U and the step counters it advances
+        tuned = tuning.autotune_cached(s, tuning_cache)
     geometry = outputs.read_blocks(s)  # x1, y1 (constant) for the snapshot files
     res_path = os.path.join(directory, "Residual.dat")
     pending, written, done, tt, kstep = None, [], 0, 0.0, 0
@@ -65,7 +76,7 @@ def run(directory: str, steps: int = None, device: int = 0, fix_nvar: bool = Fal
     forces = s.forces(1)
     s.close()
     return {"steps": done, "kstep": kstep, "tt": tt, "seconds": time.perf_counter() - t0, "files": written,
-            "forces": forces}
+            "forces": forces, "tuning": tuned}
 
 
 def main():
@@ -75,8 +86,10 @@ def main():
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--fix-nvar-restart", action="store_true",
                     help="read SST2d.dat for 6-variable states on restart (the reference tests NVAR == 5)")
+    ap.add_argument("--tuning-cache", default=None,
+                    help="JSON file of autotuner results keyed by launch signature (read, and extended on a miss)")
     a = ap.parse_args()
-    r = run(a.case_dir, a.steps, a.device, a.fix_nvar_restart)
+    r = run(a.case_dir, a.steps, a.device, a.fix_nvar_restart, tuning_cache=a.tuning_cache)
     print(f"steps {r['steps']} Kstep {r['kstep']} tt {r['tt']} ({r['seconds']:.2f} s); CL CD CM {r['forces']}")
 
 

@@ -142,6 +142,10 @@ def lib():
         "ec2d_check_reciprocal": ([ctypes.c_longlong, dp, dp], ctypes.c_int),
         "ec2d_snapshot": ([vp, ctypes.c_int], ctypes.c_int),
         "ec2d_tile_residual": ([vp, ctypes.c_int, ip], ctypes.c_int),
+        "ec2d_launch_config": ([vp, ip, ip, ip, ip, ip], ctypes.c_int),
+        "ec2d_set_launch_config": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int],
+                                   ctypes.c_int),
+        "ec2d_launch_signature": ([vp, ctypes.c_char_p, ctypes.c_int, ip], ctypes.c_int),
         "ec2d_mg_eddy_viscosity": ([vp, ctypes.c_int, ip], ctypes.c_int),
         "ec2d_clear_status": ([vp, ctypes.c_int], ctypes.c_int),
         "ec2d_lusgs_shape": ([vp, ip, ip, ip], ctypes.c_int),
@@ -410,6 +414,28 @@ class Solver:
         c = ctypes.c_int()
         _ck(self.L.ec2d_tile_residual(self.h, int(enable), ctypes.byref(c)), "ec2d_tile_residual")
         return c.value
+
+    LAUNCH_KEYS = ("lusgs_cs", "rows", "lanes", "concurrent", "tile_residual")
+
+    def launch_config(self):
+        """The launch choices in use (what ec2d_autotune picks), as a dict."""
+        v = [ctypes.c_int() for _ in self.LAUNCH_KEYS]
+        _ck(self.L.ec2d_launch_config(self.h, *[ctypes.byref(x) for x in v]), "ec2d_launch_config")
+        return {k: x.value for k, x in zip(self.LAUNCH_KEYS, v)}
+
+    def set_launch_config(self, cfg):
+        """Apply launch choices (a dict as launch_config returns) without timing them."""
+        _ck(self.L.ec2d_set_launch_config(self.h, *[int(cfg[k]) for k in self.LAUNCH_KEYS]),
+            "ec2d_set_launch_config")
+
+    def launch_signature(self):
+        """What the launch choices depend on (device, library build, method
+        flags, block shapes per level), one line; the autotuner cache's key."""
+        n = ctypes.c_int()
+        _ck(self.L.ec2d_launch_signature(self.h, None, 0, ctypes.byref(n)), "ec2d_launch_signature")
+        buf = ctypes.create_string_buffer(n.value)
+        _ck(self.L.ec2d_launch_signature(self.h, buf, n.value, ctypes.byref(n)), "ec2d_launch_signature")
+        return buf.value.decode()
 
     def mg_eddy_viscosity(self, enable=-1):
         """Coarse multigrid levels keep the restricted eddy viscosity (1) or

@@ -3,6 +3,7 @@ unit, in parallel, then a shared-library link.  Usage: python ec2d_build.py [-v]
 from __future__ import annotations
 
 import concurrent.futures as cf
+import hashlib
 import os
 import shutil
 import subprocess
@@ -37,6 +38,26 @@ def _stale(obj: str, deps) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def _write_build_id(paths, extra) -> str:
+    """A translation unit holding a digest of the library's sources, headers
+    and flags (ec2d_launch_signature reports it, so launch choices cached by
+    a host are not reused after the kernels change); rewritten only when the
+    digest changes, so an unchanged tree rebuilds nothing."""
+    h = hashlib.sha256()
+    for p in sorted(paths, key=os.path.basename):
+        h.update(os.path.basename(p).encode() + b"\0")
+        with open(p, "rb") as fh:
+            h.update(fh.read())
+    h.update(repr((ARCH, FLAGS, sorted(FILE_FLAGS.items()), list(extra))).encode())
+    src = os.path.join(OUT, "build_id.cpp")
+    text = f'extern "C" const char ec2d_internal_build_id[] = "{h.hexdigest()[:16]}";\n'
+    old = open(src).read() if os.path.exists(src) else None
+    if old != text:
+        with open(src, "w") as fh:
+            fh.write(text)
+    return src
+
+
 def build(verbose: bool = False, extra=()) -> str:
     os.makedirs(OUT, exist_ok=True)
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
@@ -44,6 +65,11 @@ def build(verbose: bool = False, extra=()) -> str:
     headers.append(os.path.join(HERE, "..", "include", "ec2d_gpu.h"))
     srcs = [s for s in SOURCES if os.path.exists(os.path.join(SRC, s))]
     objs, jobs = [], []
+    bid = _write_build_id([os.path.join(SRC, s) for s in srcs] + headers, extra)
+    bid_obj = os.path.join(OUT, "build_id.o")
+    objs.append(bid_obj)
+    if _stale(bid_obj, [bid]):
+        jobs.append([nvcc(), "-Xcompiler", "-fPIC", "-c", bid, "-o", bid_obj])
     for s in srcs:
         src = os.path.join(SRC, s)
         obj = os.path.join(OUT, s.replace(".cu", ".o"))

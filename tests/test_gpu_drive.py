@@ -53,3 +53,34 @@ def test_output_files_from_the_device(gpu_lib, tmp_path):
     U = g.download_U(1, 1, 2)
     nx, ny, _ = g.dims(1, 1, 2)
     np.testing.assert_allclose(zones[1][:, 2].reshape(ny + 1, nx + 1), U[0, 1:nx + 2, 1:ny + 2].T, atol=1e-10)
+
+
+@pytest.mark.parametrize("method", ["lusgs_mg3", "dual"])
+def test_init_flow_restarts_a_used_context(gpu_lib, method):
+    """ec2d_init_flow on a context that has stepped starts as a new context
+    does (the reference starts right after the mesh set-up): the coarse
+    pre-steps, which add the coarse forcing, run with it zero; the dual-time
+    first-step flags are unset; the counters are back at zero.  The steps
+    after it are bit-identical to a new context's."""
+    if method == "lusgs_mg3":
+        p, bl = small_case(nx=65, ny=17, Ma=0.6, AoA=2.0, Iflag_flux=4, Iflag_Scheme=5, Time_Method=0, Num_Mesh=3,
+                           CFL=4.0, Pre_Step_Mesh=(0, 5, 5), mg_lusgs=1, nblocks=2)
+    else:
+        p, bl = small_case(Ma=0.5, AoA=3.0, Re=5e3, If_viscous=1, Iflag_flux=4, Iflag_Scheme=5, Time_Method=-1,
+                           CFL=5.0, dt_global=0.05, Nstep_Inner_Limit=6, Res_Inner_Limit=1e-12)
+    a = make_gpu(p, bl)
+    a.init_flow()
+    a.step(7)
+    a.init_flow()
+    a.step(4)
+    b = make_gpu(p, bl)
+    b.init_flow()
+    b.step(4)
+    for blk in range(1, len(bl) + 1):
+        np.testing.assert_array_equal(a.download_U(1, 1, blk), b.download_U(1, 1, blk))
+    na, nb = a.norms(), b.norms()
+    np.testing.assert_array_equal(na[0], nb[0])
+    np.testing.assert_array_equal(na[1], nb[1])
+    assert na[2] == nb[2] == 4 and na[3] == nb[3]
+    a.close()
+    b.close()
