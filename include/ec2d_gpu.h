@@ -144,6 +144,16 @@ int ec2d_block_dims(ec2d_ctx *ctx, int case_id, int mesh, int block, int *nx, in
  * flags unset and the step counters and times at zero, so a context that has
  * stepped before (or been autotuned) starts exactly as a new one. */
 int ec2d_init_flow(ec2d_ctx *ctx);
+/* Dual time stepping (Time_Method -1): start the physical-time history
+ * from the current U of every case, U(n) = U(n-1) = U, with the first-step
+ * flags unset, so that the next physical step takes the one-step form
+ * (Dual_time_LU_SGS, sub_NS_singlegrid.f90:239-245, and the time term of
+ * Comput_Residual_one_mesh, sub_Residual.f90:27-34, whose comment assumes
+ * U(n-1) = U(n) on the first step).  ec2d_init_flow ends with it; a host
+ * calls it after uploading a restart state (init_flow_read), which the
+ * reference leaves with U(n) at its allocation fill (sub_init.f90:162) and
+ * U(n-1) unset.  Does nothing for the other time methods. */
+int ec2d_dual_time_start(ec2d_ctx *ctx);
 
 /* Copy the conservative field of one block in or out, Fortran layout
  * U(NVAR,-1:nx+1,-1:ny+1) (the reference's B%U).  Host pointers may be

@@ -115,6 +115,12 @@ module ec2d_gpu_mod
       import
       type(c_ptr), value :: ctx
     end function
+    ! dual time stepping after a restart (init_flow_read + ec2d_upload_U):
+    ! U(n) = U(n-1) = the restart state, first physical step one-step form
+    integer(c_int) function ec2d_dual_time_start(ctx) bind(C)
+      import
+      type(c_ptr), value :: ctx
+    end function
     integer(c_int) function ec2d_upload_U(ctx, case_id, mesh, block, U) bind(C)
       import
       type(c_ptr), value :: ctx

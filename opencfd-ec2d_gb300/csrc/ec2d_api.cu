@@ -1254,6 +1254,23 @@ int ec2d_clear_status(ec2d_ctx *ctx, int case_id) {
   return EC2D_OK;
 }
 
+// U(n) = U(n-1) = U on the fine mesh and the first-step flags unset: the
+// first physical step after it is the one-step form (alfa1 = 1/dt, Sfac =
+// 1/(3 dt), sub_NS_singlegrid.f90:239-245, sub_Residual.f90:27-34), whose
+// comment assumes U(n-1) = U(n); the reference's code leaves Un at its
+// allocation fill (sub_init.f90:162) and Un1 unset
+int ec2d_dual_time_start(ec2d_ctx *ctx) {
+  if (!ctx || !ctx->setup_done) return EC2D_ERR_ARG;
+  if (ctx->P.Time_Method != Time_Dual) return EC2D_OK;
+  cudaSetDevice(ctx->device);
+  const Lvl &L = ctx->lv[1].L;
+  const size_t bytes = (size_t)L.nvar * ctx->lv[1].F * sizeof(double);
+  CK(cudaMemcpyAsync(L.un, L.U, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(L.un1, L.U, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+  ctx->dual_iflag = ctx->dual_iflag1 = 0;
+  return EC2D_OK;
+}
+
 int ec2d_init_flow(ec2d_ctx *ctx) {
   if (!ctx || !ctx->setup_done) return EC2D_ERR_ARG;
   cudaSetDevice(ctx->device);
@@ -1288,12 +1305,8 @@ int ec2d_init_flow(ec2d_ctx *ctx) {
       bc_all(ctx, l - 1);
     }
   }
-  if (ctx->P.Time_Method == Time_Dual) {
-    const Lvl &L = ctx->lv[1].L;
-    size_t bytes = (size_t)L.nvar * ctx->lv[1].F * sizeof(double);
-    CK(cudaMemcpyAsync(L.un, L.U, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(L.un1, L.U, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
-  }
+  rc = ec2d_dual_time_start(ctx);
+  if (rc) return rc;
   return check_launch(ctx);
 }
 

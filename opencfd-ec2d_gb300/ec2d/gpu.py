@@ -89,6 +89,7 @@ def lib():
         "ec2d_num_mesh": ([vp, ip], ctypes.c_int),
         "ec2d_block_dims": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ip, ip, ip], ctypes.c_int),
         "ec2d_init_flow": ([vp], ctypes.c_int),
+        "ec2d_dual_time_start": ([vp], ctypes.c_int),
         "ec2d_upload_U": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp], ctypes.c_int),
         "ec2d_download_U": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp], ctypes.c_int),
         "ec2d_step": ([vp, ctypes.c_int], ctypes.c_int),
@@ -256,6 +257,10 @@ class Solver:
 
     def init_flow(self):
         _ck(self.L.ec2d_init_flow(self.h), "ec2d_init_flow")
+
+    def dual_time_start(self):
+        """Dual time stepping: U(n) = U(n-1) = the current U, first step one-step form."""
+        _ck(self.L.ec2d_dual_time_start(self.h), "ec2d_dual_time_start")
 
     def upload_U(self, case, mesh, block, U):
         U = np.asfortranarray(U, dtype=np.float64)

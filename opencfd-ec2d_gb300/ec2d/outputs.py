@@ -207,7 +207,9 @@ def restart(solver, directory: str, case: int = 1, fix_nvar: bool = False) -> No
     `directory` (read_flow), then the boundary conditions and the block halo
     on the fine mesh (init_flow_read ends with Boundary_condition_onemesh(1)
     and update_buffer_onemesh(1)).  The step counter and time restart at
-    zero, as in the reference."""
+    zero, as in the reference; with dual time stepping U(n) and U(n-1) are
+    the restart state (ec2d_dual_time_start), for every case of the
+    context."""
     params = solver.params[case - 1]
     dims = [solver.dims(case, 1, b) for b in range(1, solver.nblocks[case - 1] + 1)]
     Us = read_flow(directory, params, dims, fix_nvar=fix_nvar)
@@ -220,3 +222,6 @@ def restart(solver, directory: str, case: int = 1, fix_nvar: bool = False) -> No
         solver.upload_U(case, 1, b, cur)
     solver.bc(1)
     solver.halo(1)
+    # dual time stepping: the physical-time history starts from the restart
+    # state (ec2d_dual_time_start; a no-op for the other time methods)
+    solver.dual_time_start()

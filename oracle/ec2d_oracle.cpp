@@ -2175,14 +2175,27 @@ int orc_block_dims(void *h, int mesh, int block, int *nx, int *ny) {
   *nx = B.nx; *ny = B.ny;
   return 0;
 }
+// The start of dual time stepping from the current U: U(n) = U(n-1) = U and
+// the first-step flags unset, so the first physical step is the one-step
+// form (alfa1 = 1/dt, Sfac = 1/(3 dt), sub_NS_singlegrid.f90:239-245,
+// sub_Residual.f90:27-34).  The reference's comment there assumes
+// U(n-1) = U(n) on the first step, but its code leaves Un at the allocation
+// fill (1,0,0,0) (sub_init.f90:162) and Un1 unset (:155); this sets them as
+// the comment says, after a freestream start and after a restart alike.
+int orc_dual_time_start(void *h) {
+  Solver &S = *(Solver *)h;
+  if (S.Time_Method != Time_dual_LU_SGS) return 0;
+  for (auto &B : S.mesh[1].B)
+    for (int j = 1; j <= B.ny - 1; j++)
+      for (int i = 1; i <= B.nx - 1; i++)
+        for (int m = 1; m <= S.Nvar; m++) { B.Un(m, i, j) = B.U(m, i, j); B.Un1(m, i, j) = B.U(m, i, j); }
+  S.dual_iflag = S.dual_iflag1 = 0;
+  return 0;
+}
 int orc_init_flow(void *h) {
   Solver &S = *(Solver *)h;
   int r = init_flow_zero(S);
-  if (!r && S.Time_Method == Time_dual_LU_SGS)
-    for (auto &B : S.mesh[1].B)
-      for (int j = 1; j <= B.ny - 1; j++)
-        for (int i = 1; i <= B.nx - 1; i++)
-          for (int m = 1; m <= S.Nvar; m++) { B.Un(m, i, j) = B.U(m, i, j); B.Un1(m, i, j) = B.U(m, i, j); }
+  if (!r) orc_dual_time_start(h);
   return r;
 }
 int orc_get_U(void *h, int mesh, int block, double *U) {

@@ -50,6 +50,7 @@ int orc_num_mesh(void *h);
 int orc_nvar(void *h, int mesh);
 int orc_block_dims(void *h, int mesh, int block, int *nx, int *ny);
 int orc_init_flow(void *h);
+int orc_dual_time_start(void *h); /* Un = Un1 = U on mesh 1, first-step flags unset */
 int orc_get_U(void *h, int mesh, int block, double *U);
 int orc_set_U(void *h, int mesh, int block, const double *U);
 int orc_get_field(void *h, int mesh, int block, int field, double *out);

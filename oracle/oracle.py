@@ -75,7 +75,7 @@ def lib(fast=False):
         L.orc_new.argtypes = [ctypes.POINTER(OrcParams)]
         L.orc_free.argtypes = [vp]
         L.orc_add_block.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp, dp, ctypes.c_int, ip]
-        for name in ("orc_setup", "orc_init_flow", "orc_num_mesh"):
+        for name in ("orc_setup", "orc_init_flow", "orc_dual_time_start", "orc_num_mesh"):
             getattr(L, name).argtypes = [vp]
         L.orc_set_fdm_block.argtypes = [vp, ctypes.c_int]
         L.orc_set_dw.argtypes = [vp, ctypes.c_int, dp]
@@ -177,6 +177,10 @@ class Oracle:
 
     def init_flow(self):
         self._check(self.L.orc_init_flow(self.h), "init_flow")
+
+    def dual_time_start(self):
+        """Dual time stepping restarts its physical-time history from the current U."""
+        self._check(self.L.orc_dual_time_start(self.h), "dual_time_start")
 
     def get_U(self, mesh, block):
         nx, ny = self.dims(mesh, block)

@@ -140,3 +140,34 @@ def test_driver_writes_kstep_save_files_from_snapshots(gpu_lib, tmp_path):
     g.close()
     for name in ("flow2d-0000010.dat", "flow2d-0000020.dat"):
         assert open(d1 / name).read() == open(d2 / name).read()
+
+
+def test_dual_time_restart_starts_the_history_from_the_files(gpu_lib, tmp_path):
+    """A dual-time restart: U(n) after outputs.restart is the restart state
+    (ec2d_dual_time_start), not the freestream that init_flow set, and the
+    next physical step starts from it in the one-step form, as the stepping
+    of a context handed the same state does."""
+    from ec2d import gpu, outputs
+    p, bl = small_case(Ma=0.5, AoA=3.0, Re=5e3, If_viscous=1, Iflag_flux=4, Iflag_Scheme=5, Time_Method=-1,
+                       CFL=5.0, dt_global=0.05, Nstep_Inner_Limit=6, Res_Inner_Limit=1e-12)
+    a = make_gpu(p, bl)
+    a.init_flow()
+    a.step(3)
+    outputs.write_output(str(tmp_path), a, p, kstep=3)
+    b_ = make_gpu(p, bl)
+    outputs.restart(b_, str(tmp_path))
+    c = make_gpu(p, bl)
+    c.init_flow()
+    for k in range(1, len(bl) + 1):
+        nx, ny, nv = b_.dims(1, 1, k)
+        U = b_.download_U(1, 1, k)
+        un = b_.field(1, 1, k, gpu.F_UN, shape=(nv, nx + 1, ny + 1))
+        np.testing.assert_array_equal(un[:, 1:nx, 1:ny], U[:, 2:nx + 1, 2:ny + 1])
+        c.upload_U(1, 1, k, U)
+    c.dual_time_start()
+    b_.step(2)
+    c.step(2)
+    for k in range(1, len(bl) + 1):
+        np.testing.assert_array_equal(b_.download_U(1, 1, k), c.download_U(1, 1, k))
+    for g in (a, b_, c):
+        g.close()

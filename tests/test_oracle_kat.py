@@ -213,3 +213,26 @@ def test_mg_eddy_viscosity_keeps_turbulent_cycle_stable():
     r0 = orc.norms()[1][0]
     orc.step(999)
     assert np.isfinite(orc.norms()[1][0]) and orc.norms()[1][0] < r0
+
+
+def test_dual_time_start_is_the_whole_history(oracle_lib):
+    """orc_dual_time_start makes U(n) = U(n-1) = U and the next physical step
+    the one-step form: an oracle handed a developed state and started there
+    steps exactly as the oracle that developed it and was started there; one
+    left with the freestream history of its own start steps differently."""
+    p, bl = small_case(Ma=0.5, AoA=3.0, Re=5e3, If_viscous=1, Iflag_flux=4, Iflag_Scheme=5, Time_Method=-1,
+                       CFL=5.0, dt_global=0.05, Nstep_Inner_Limit=4, Res_Inner_Limit=1e-12)
+    a = make_oracle(p, bl)
+    a.init_flow()
+    a.step(2)
+    state = a.get_U(1, 1)
+    b, c = make_oracle(p, bl), make_oracle(p, bl)
+    for o in (b, c):
+        o.init_flow()
+        o.set_U(1, 1, state)
+    a.dual_time_start()
+    b.dual_time_start()
+    for o in (a, b, c):
+        o.step(1)
+    np.testing.assert_array_equal(a.get_U(1, 1), b.get_U(1, 1))
+    assert not np.array_equal(a.get_U(1, 1), c.get_U(1, 1))
