@@ -369,9 +369,9 @@ int ec2d_mlp_predict(ec2d_mlp *m, const float *feat, long long n, float *pred);
  * whether independent kernels run concurrently on two stream pairs (the i-
  * and j-face flux kernels; at a multigrid transfer the fine residual and the
  * restriction + coarse boundary conditions + coarse entry residual).
- * The fine-mesh U and the step counters (with dual time stepping also the
- * two physical time levels and the first-step flags) are restored
- * afterwards; other scratch of the steps (residuals, coarse levels, the
+ * The fine-mesh U, the step counters and every case's status word (with
+ * dual time stepping also the two physical time levels and the first-step
+ * flags) are restored afterwards; other scratch of the steps (residuals, coarse levels, the
  * coarse forcing) is formed anew before the next step or ec2d_init_flow
  * reads it.  Outputs
  * (may be NULL): the choices and the winner's milliseconds per step.  The

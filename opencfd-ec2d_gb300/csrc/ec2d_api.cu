@@ -1485,6 +1485,12 @@ int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *rows_per_w
     CK(cudaMemcpyAsync(snap + 2 * nelem, lv.L.un1, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
   }
   const int dflag = ctx->dual_iflag, dflag1 = ctx->dual_iflag1;
+  // the status words of every level (a trial step on a state that trips the
+  // T < 1e-5 test must not leave its stop on the restored state)
+  const size_t nst = 4 * ctx->cases.size();
+  std::vector<std::vector<int>> st(ctx->num_mesh + 1, std::vector<int>(nst));
+  for (int l = 1; l <= ctx->num_mesh; l++)
+    CK(cudaMemcpyAsync(st[l].data(), ctx->lv[l].L.status, nst * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   std::vector<std::array<int, 4>> ks(ctx->cases.size());
   std::vector<std::array<double, 4>> ts(ctx->cases.size());
   for (size_t c = 0; c < ctx->cases.size(); c++)
@@ -1567,6 +1573,8 @@ int ec2d_autotune(ec2d_ctx *ctx, int trial_steps, int *lusgs_cs, int *rows_per_w
   }
   ctx->dual_iflag = dflag;
   ctx->dual_iflag1 = dflag1;
+  for (int l = 1; l <= ctx->num_mesh; l++)
+    cudaMemcpyAsync(ctx->lv[l].L.status, st[l].data(), nst * sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
   cudaStreamSynchronize(ctx->stream);
   cudaFree(snap);
   cudaEventDestroy(a);

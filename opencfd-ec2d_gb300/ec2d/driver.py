@@ -2,7 +2,8 @@
 host over the C-ABI: read the case directory, hand it to the library, march
 until t_end (or a step count), print and record the residuals every
 Kstep_show steps and write the flow files every Kstep_save steps and at the
-end.
+end.  SA and SST runs take the wall distance from the case's dist_wall.dat,
+or write it there (and dw.dat) from the distances formed on the device.
 
 The flow files at Kstep_save come from asynchronous snapshots
 (ec2d_snapshot): the library copies U to pinned host memory on a stream of
@@ -38,11 +39,35 @@ def read_fdm(directory: str):
     return [int(lines[6 + k].split()[0]) for k in range(n)]
 
 
+def write_wall_distance(solver, directory: str, dims) -> None:
+    """dist_wall.dat and dw.dat from the distances the library formed on the
+    device (comput_dw writes both when it had to compute them,
+    sub_turbulence_SST.f90:342-362)."""
+    dws, cells = [], []
+    for k, (nx, ny) in enumerate(dims, start=1):
+        dw = solver.field(1, 1, k, gpu.F_DW, shape=(nx + 1, ny + 1))[1:nx, 1:ny]
+        x1 = solver.field(1, 1, k, gpu.F_X1, shape=(nx + 3, ny + 3))[2:nx + 1, 2:ny + 1]
+        y1 = solver.field(1, 1, k, gpu.F_Y1, shape=(nx + 3, ny + 3))[2:nx + 1, 2:ny + 1]
+        dws.append(dw)
+        cells.append((x1, y1, dw))
+    inputs.write_dist_wall(os.path.join(directory, "dist_wall.dat"), dws, dims)
+    inputs.write_dw_tecplot(os.path.join(directory, "dw.dat"), cells)
+
+
 def run(directory: str, steps: int = None, device: int = 0, fix_nvar: bool = False, quiet: bool = False,
         tuning_cache: str = None) -> dict:
     p, blocks = inputs.read_case(directory)
     fdm = read_fdm(directory)
-    s = gpu.Solver([(p, blocks)], device=device, fdm_blocks=[fdm])
+    # the wall distance of SA and SST runs (comput_dw,
+    # opencfd_ec2d_v1.5.4.f90:164): read from dist_wall.dat where the case
+    # directory has one, else formed on the device and written there
+    dims = [(b.nx, b.ny) for b in blocks]
+    turbulent = p.Iflag_turbulence_model in (inputs.TURB_SA, inputs.TURB_SST)
+    dw_path = os.path.join(directory, "dist_wall.dat")
+    dw = inputs.read_dist_wall(dw_path, dims) if turbulent and os.path.exists(dw_path) else None
+    s = gpu.Solver([(p, blocks)], device=device, fdm_blocks=[fdm], dw=None if dw is None else [dw])
+    if turbulent and dw is None:
+        write_wall_distance(s, directory, dims)
     if p.Iflag_init == 0:
         s.init_flow()
     else:

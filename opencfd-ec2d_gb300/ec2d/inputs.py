@@ -11,6 +11,9 @@ the Fortran code runs here and vice versa:
 * ``Mesh2d.dat``  -- node coordinates, read at sub_init.f90:121-127,176.
 * ``Residual.dat`` records, written at opencfd_ec2d_v1.5.4.f90:275-277.
 * ``flow2d.dat`` Tecplot snapshot, written at opencfd_ec2d_v1.5.4.f90:323-339.
+* ``dist_wall.dat`` cell wall distances, read or written by comput_dw
+  (sub_turbulence_SST.f90:295-348), and its Tecplot view ``dw.dat``
+  (:350-362).
 """
 from __future__ import annotations
 
@@ -237,6 +240,72 @@ def write_case(directory: str, p: Params, blocks: Sequence[Block], title: str = 
     write_control(os.path.join(directory, "control.in"), p)
     write_bc(os.path.join(directory, "bc2d_1.in"), blocks, title)
     write_mesh(os.path.join(directory, "Mesh2d.dat"), blocks)
+
+
+def _list_directed(text: str) -> List[str]:
+    """The values of Fortran list-directed records: separated by blanks,
+    commas or line ends, ``r*c`` standing for r copies of c."""
+    out: List[str] = []
+    for tok in re.split(r"[\s,]+", text.strip()):
+        if not tok:
+            continue
+        if "*" in tok:
+            r, c = tok.split("*", 1)
+            out.extend([c] * int(r))
+        else:
+            out.append(tok)
+    return out
+
+
+def read_dist_wall(path: str, dims: Sequence) -> List[np.ndarray]:
+    """dist_wall.dat as comput_dw reads it (sub_turbulence_SST.f90:295-306):
+    the block count, the (nx, ny) node counts of every block, then each
+    block's cell distances dw(1:nx-1,1:ny-1), i fastest.  `dims` holds the
+    (nx, ny) of the mesh's blocks; one Fortran-ordered (nx-1, ny-1) array per
+    block is returned.  A file written for another mesh (other block count
+    or sizes) raises ValueError; the reference would read its numbers into
+    the mesh's blocks all the same."""
+    v = _list_directed(open(path).read())
+    nb = int(v[0])
+    sizes = [(int(v[1 + 2 * k]), int(v[2 + 2 * k])) for k in range(nb)]
+    want = [(int(nx), int(ny)) for nx, ny in dims]
+    if sizes != want:
+        raise ValueError(f"{path} was written for blocks {sizes}, the mesh has {want}")
+    pos, out = 1 + 2 * nb, []
+    for nx, ny in sizes:
+        n = (nx - 1) * (ny - 1)
+        vals = [float(t.replace("D", "E").replace("d", "e")) for t in v[pos:pos + n]]
+        if len(vals) != n:
+            raise ValueError(f"{path} ends inside a block")
+        out.append(np.array(vals).reshape((nx - 1, ny - 1), order="F"))
+        pos += n
+    return out
+
+
+def write_dist_wall(path: str, dws: Sequence, dims: Sequence) -> None:
+    """dist_wall.dat as comput_dw writes it (sub_turbulence_SST.f90:342-348),
+    every value with the digits that read back to the same double."""
+    with open(path, "w") as fh:
+        fh.write(f" {len(dws)}\n")
+        fh.write(" " + " ".join(f"{int(nx)} {int(ny)}" for nx, ny in dims) + "\n")
+        for d in dws:
+            flat = np.asarray(d, dtype=np.float64).reshape(-1, order="F")
+            for k in range(0, flat.size, 4):
+                fh.write(" " + " ".join(repr(float(x)) for x in flat[k:k + 4]) + "\n")
+
+
+def write_dw_tecplot(path: str, cells: Sequence) -> None:
+    """dw.dat (sub_turbulence_SST.f90:350-362): per block a zone of its cell
+    centres and wall distances, i fastest; `cells` holds one (x1, y1, dw)
+    triple of (nx-1, ny-1) arrays per block."""
+    with open(path, "w") as fh:
+        fh.write(" variables=x,y,dw\n")
+        for x1, y1, dw in cells:
+            ni, nj = np.shape(dw)
+            fh.write(f" zone i= {ni} j= {nj}\n")
+            for j in range(nj):
+                for i in range(ni):
+                    fh.write(f" {float(x1[i, j])!r} {float(y1[i, j])!r} {float(dw[i, j])!r}\n")
 
 
 def residual_record(kstep: int, res_max6, res_rms, nvar: int) -> str:

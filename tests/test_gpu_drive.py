@@ -84,3 +84,34 @@ def test_init_flow_restarts_a_used_context(gpu_lib, method):
     assert na[2] == nb[2] == 4 and na[3] == nb[3]
     a.close()
     b.close()
+
+
+def test_driver_wall_distance_file(gpu_lib, tmp_path):
+    """An SA run of the main-loop driver without dist_wall.dat writes it (and
+    dw.dat) from the distances formed on the device, bit for bit; a run whose
+    case directory holds that file reads it and marches exactly as the first
+    run did; a file with other distances changes the run (it is read)."""
+    import shutil
+
+    from ec2d import driver, gpu, inputs
+    p, bl = small_case(Ma=0.5, AoA=2.0, Re=1e6, If_viscous=1, Iflag_turbulence_model=2, Iflag_flux=4,
+                       Iflag_Scheme=5, CFL=5.0, first=2e-4, nblocks=2, Kstep_show=5, Kstep_save=1000, t_end=1.0e9)
+    dims = [(b.nx, b.ny) for b in bl]
+    dirs = [tmp_path / n for n in ("computed", "read", "scaled")]
+    inputs.write_case(str(dirs[0]), p, bl)
+    r0 = driver.run(str(dirs[0]), steps=10, quiet=True)
+    assert os.path.exists(dirs[0] / "dist_wall.dat") and os.path.exists(dirs[0] / "dw.dat")
+    dws = inputs.read_dist_wall(str(dirs[0] / "dist_wall.dat"), dims)
+    g = make_gpu(p, bl)
+    for k, (nx, ny) in enumerate(dims, start=1):
+        np.testing.assert_array_equal(dws[k - 1], g.field(1, 1, k, gpu.F_DW, shape=(nx + 1, ny + 1))[1:nx, 1:ny])
+    g.close()
+    inputs.write_case(str(dirs[1]), p, bl)
+    shutil.copy(dirs[0] / "dist_wall.dat", dirs[1] / "dist_wall.dat")
+    r1 = driver.run(str(dirs[1]), steps=10, quiet=True)
+    assert open(dirs[1] / "Residual.dat").read() == open(dirs[0] / "Residual.dat").read()
+    assert r1["forces"] == r0["forces"] and not os.path.exists(dirs[1] / "dw.dat")
+    inputs.write_case(str(dirs[2]), p, bl)
+    inputs.write_dist_wall(str(dirs[2] / "dist_wall.dat"), [2.0 * d for d in dws], dims)
+    driver.run(str(dirs[2]), steps=10, quiet=True)
+    assert open(dirs[2] / "Residual.dat").read() != open(dirs[0] / "Residual.dat").read()

@@ -152,3 +152,18 @@ def test_autotune_restores_dual_time_levels(gpu_lib):
     assert na[2] == nb[2] == 5 and na[3] == nb[3]
     a.close()
     b.close()
+
+
+def test_autotune_restores_status_words(gpu_lib):
+    """Trial steps on a state that trips the T < 1e-5 test (a context not yet
+    started: U is zero) set the case's status word; the autotuner restores
+    it with U, so the stop is not reported for the restored state."""
+    p, bl = _case()
+    g = make_gpu(p, bl)
+    assert g.status(1)[0] == 0
+    g.autotune(trial_steps=1)
+    assert g.status(1)[0] == 0
+    g.init_flow()
+    g.step(2)
+    assert g.status(1)[0] == 0
+    g.close()

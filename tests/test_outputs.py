@@ -46,3 +46,39 @@ def test_turbulence_files():
     b6, _ = _block(4, 3, 6, 3)
     names, zones = outputs.parse_tecplot(outputs.format_turbulence([b6]))
     assert names == ["x", "y", "Kt", "Wt"] and zones[0].shape == (20, 4)
+
+
+def test_dist_wall_round_trip_and_fortran_records(tmp_path):
+    """dist_wall.dat (comput_dw, sub_turbulence_SST.f90:295-348): what is
+    written reads back to the same doubles, a file in the Fortran compiler's
+    list-directed style (repeat counts, D exponents, records wrapped across
+    lines) reads as the numbers it holds, and a file for another mesh is
+    refused."""
+    import numpy as np
+
+    from ec2d import inputs
+    rng = np.random.default_rng(5)
+    dims = [(5, 4), (3, 3)]
+    dws = [rng.random((nx - 1, ny - 1)) * 10.0 ** rng.integers(-6, 2, (nx - 1, ny - 1)) for nx, ny in dims]
+    path = str(tmp_path / "dist_wall.dat")
+    inputs.write_dist_wall(path, dws, dims)
+    back = inputs.read_dist_wall(path, dims)
+    for a, b in zip(dws, back):
+        assert b.shape == a.shape and np.array_equal(a, b)
+    text = ("           2\n           5           4           3\n           3\n"
+            "   1.0000000000000000       0.50000000000000000     3*0.25000000000000000\n"
+            "   1.5D-002   2.5E-003  6*7.0000000000000000    \n"
+            "   0.125000000000000000       4.0000000000000000E-004   1.0 2.0\n")
+    with open(path, "w") as fh:
+        fh.write(text)
+    got = inputs.read_dist_wall(path, dims)
+    assert got[0].reshape(-1, order="F").tolist() == [1.0, 0.5, 0.25, 0.25, 0.25, 1.5e-2, 2.5e-3] + [7.0] * 5
+    assert got[1].reshape(-1, order="F").tolist() == [7.0, 0.125, 4.0e-4, 1.0]
+    import pytest
+    with pytest.raises(ValueError):
+        inputs.read_dist_wall(path, [(5, 4), (3, 4)])
+    x1 = [np.arange(12.0).reshape(4, 3), np.zeros((2, 2))]
+    inputs.write_dw_tecplot(str(tmp_path / "dw.dat"), [(x, x, d) for x, d in zip(x1, got)])
+    lines = open(tmp_path / "dw.dat").read().splitlines()
+    assert lines[0].split() == ["variables=x,y,dw"] and lines[1].split() == ["zone", "i=", "4", "j=", "3"]
+    assert len(lines) == 2 + 12 + 1 + 4
