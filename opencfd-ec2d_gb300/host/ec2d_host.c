@@ -17,9 +17,18 @@
  * Residual.dat record, format (I8,13E24.10) (opencfd_ec2d_v1.5.4.f90:266-279).
  * The input files are read in the reference's formats, unchanged.
  *
- *   ec2d_host [case_dir] [--steps N] [--device D]
+ *   ec2d_host [case_dir] [--steps N] [--device D] [--fix-nvar-restart]
  *
  * --steps N stops after N steps (the reference stops only on tt >= t_end).
+ * SA and SST runs take the wall distance from dist_wall.dat when the case
+ * has one, else write it (and dw.dat) from the distances formed on the
+ * device, as comput_dw does (sub_turbulence_SST.f90:274-365).
+ * Iflag_init = 1 in control.in restarts from flow2d.dat (and SA2d.dat /
+ * SST2d.dat) as init_flow_read does (sub_init.f90:499-560); the reference
+ * reads the turbulence files under NVAR == 5 for both models (:523, :541),
+ * which --fix-nvar-restart corrects (SST2d.dat for NVAR == 6), and without
+ * which an SA restart stops with a message where the reference would read
+ * SST2d.dat into a 5-variable state.
  * At the end it prints the last step's residual norms and CL, CD, CM.
  * Exit status: 0, or the EC2D_ERR_* code of the failing call (a T < 1e-5
  * state prints the reference's message and stops, as sub_Residual.f90:143-146
@@ -208,6 +217,175 @@ static void e24(FILE *f, double v) {
   fprintf(f, "%24s", out);
 }
 
+static int fail(const char *what, int r);
+
+/* dist_wall.dat as comput_dw reads it (sub_turbulence_SST.f90:295-306): the
+ * block count, the (nx, ny) of every block, then each block's cell distances
+ * dw(1:nx-1,1:ny-1), i fastest, as list-directed values (r*c repeats
+ * included).  dw[m] receives (nx-1)(ny-1) values (malloc'ed).  0: read;
+ * 1: absent; -1: unreadable or written for another mesh. */
+static int read_dist_wall(const char *path, const host_block *B, int nb, double **dw) {
+  FILE *f = fopen(path, "r");
+  if (!f) return 1;
+  char tok[128];
+  double rep_val = 0.0;
+  long rep = 0;
+  int bad = 0;
+  /* the next value of the stream, with r*c repeats expanded */
+#define NEXT(out)                                                     \
+  do {                                                                \
+    if (rep > 0) { rep--; (out) = rep_val; break; }                   \
+    if (fscanf(f, " %127[^ \t\r\n,]%*[ \t\r\n,]", tok) < 1) { bad = 1; (out) = 0; break; } \
+    char *star = strchr(tok, '*');                                    \
+    if (star) { *star = 0; rep = atol(tok) - 1; rep_val = fnum(star + 1); (out) = rep_val; } \
+    else (out) = fnum(tok);                                           \
+  } while (0)
+  double v;
+  NEXT(v);
+  if (bad || (int)v != nb) bad = 1;
+  for (int m = 0; m < nb && !bad; m++) {
+    double a, b;
+    NEXT(a);
+    NEXT(b);
+    if ((int)a != B[m].nx || (int)b != B[m].ny) bad = 1;
+  }
+  for (int m = 0; m < nb && !bad; m++) {
+    size_t n = (size_t)(B[m].nx - 1) * (B[m].ny - 1);
+    dw[m] = (double *)malloc(n * sizeof(double));
+    if (!dw[m]) { bad = 1; break; }
+    for (size_t k = 0; k < n && !bad; k++) NEXT(dw[m][k]);
+  }
+#undef NEXT
+  fclose(f);
+  return bad ? -1 : 0;
+}
+
+/* dist_wall.dat and dw.dat (sub_turbulence_SST.f90:342-362) from the
+ * distances formed on the device, every value with 17 significant digits
+ * (it reads back to the same double). */
+static int write_dist_wall(const char *dir, ec2d_ctx *ctx, int cs, const host_block *B, int nb) {
+  char path[4096], path2[4096];
+  snprintf(path, sizeof(path), "%s/dist_wall.dat", dir);
+  snprintf(path2, sizeof(path2), "%s/dw.dat", dir);
+  FILE *f = fopen(path, "w"), *g = fopen(path2, "w");
+  int r = 0;
+  if (!f || !g) { if (f) fclose(f); if (g) fclose(g); return 1; }
+  fprintf(f, " %d\n", nb);
+  for (int m = 0; m < nb; m++) fprintf(f, " %d %d", B[m].nx, B[m].ny);
+  fprintf(f, "\n");
+  fprintf(g, " variables=x,y,dw\n");
+  for (int m = 0; m < nb && !r; m++) {
+    const int nx = B[m].nx, ny = B[m].ny;
+    /* DW (0:nx,0:ny); X1, Y1 (-1:nx+1,-1:ny+1) */
+    double *dw = (double *)malloc((size_t)(nx + 1) * (ny + 1) * sizeof(double));
+    double *x1 = (double *)malloc((size_t)(nx + 3) * (ny + 3) * sizeof(double));
+    double *y1 = (double *)malloc((size_t)(nx + 3) * (ny + 3) * sizeof(double));
+    if (!dw || !x1 || !y1) r = EC2D_ERR_NOMEM;
+    if (!r) r = ec2d_get_field(ctx, cs, 1, m + 1, EC2D_F_DW, dw);
+    if (!r) r = ec2d_get_field(ctx, cs, 1, m + 1, EC2D_F_X1, x1);
+    if (!r) r = ec2d_get_field(ctx, cs, 1, m + 1, EC2D_F_Y1, y1);
+    if (!r) {
+      int col = 0;
+      fprintf(g, " zone i= %d j= %d\n", nx - 1, ny - 1);
+      for (int j = 1; j <= ny - 1; j++)
+        for (int i = 1; i <= nx - 1; i++) {
+          const double d = dw[(size_t)j * (nx + 1) + i];
+          const size_t c = (size_t)(j + 1) * (nx + 3) + (i + 1);
+          fprintf(f, " %.17g", d);
+          if (++col % 4 == 0) fprintf(f, "\n");
+          fprintf(g, " %.17g %.17g %.17g\n", x1[c], y1[c], d);
+        }
+      if (col % 4) fprintf(f, "\n");
+    }
+    free(dw); free(x1); free(y1);
+  }
+  fclose(f);
+  fclose(g);
+  return r;
+}
+
+/* One Tecplot file of `output` (flow2d.dat: x, y, d, u, v, T; SA2d.dat: x, y,
+ * nu~; SST2d.dat: x, y, k, omega): a title line, then per block a zone line
+ * and (nx+1)(ny+1) records over i = 0..nx fastest, j = 0..ny, as
+ * init_flow_read reads them with list-directed reads.  Returns per block the
+ * `ncol` columns of every record in `cols[m]` (malloc'ed), or -1. */
+static int read_zones(const char *path, const host_block *B, int nb, int ncol, double **cols) {
+  FILE *f = fopen(path, "r");
+  if (!f) return -1;
+  static char line[MAXLINE];
+  int ok = fgets(line, sizeof(line), f) != NULL;
+  for (int m = 0; m < nb && ok; m++) {
+    size_t n = (size_t)(B[m].nx + 1) * (B[m].ny + 1);
+    cols[m] = (double *)malloc(n * ncol * sizeof(double));
+    if (!cols[m] || !fgets(line, sizeof(line), f)) { ok = 0; break; }
+    for (size_t k = 0; k < n && ok; k++) {
+      if (!fgets(line, sizeof(line), f)) { ok = 0; break; }
+      char *t[8];
+      if (split(line, t, 8) < ncol) { ok = 0; break; }
+      for (int c = 0; c < ncol; c++) cols[m][k * ncol + c] = fnum(t[c]);
+    }
+  }
+  fclose(f);
+  return ok ? 0 : -1;
+}
+
+/* init_flow_read (sub_init.f90:499-560) over the library: the freestream start
+ * (which leaves the ghost ring and the variables the files do not hold at the
+ * freestream), each block's 0..nx x 0..ny from the files, then the boundary
+ * conditions and the halo on the fine mesh, and with dual time stepping the
+ * physical-time history started from the restart state. */
+static int restart(const char *dir, ec2d_ctx *ctx, int cs, const ec2d_params *P, const host_block *B, int nb,
+                   int nvar, int fix_nvar) {
+  double *flow[MAXB] = {0}, *turb[MAXB] = {0};
+  const char *tname = NULL;
+  int tcol = 0, r = 1;
+  if (nvar == 5) { tname = "SA2d.dat"; tcol = 3; }
+  if (nvar == 6 && fix_nvar) { tname = "SST2d.dat"; tcol = 4; }
+  if (nvar == 5 && !fix_nvar) {
+    fprintf(stderr, "restart: sub_init.f90:541 reads SST2d.dat into U(5:6) of a 5-variable (SA) state as well; "
+                    "run with --fix-nvar-restart\n");
+    return 1;
+  }
+  if (read_zones(path_in(dir, "flow2d.dat"), B, nb, 6, flow)) {
+    fprintf(stderr, "cannot read %s\n", path_in(dir, "flow2d.dat"));
+    goto done;
+  }
+  if (tname && read_zones(path_in(dir, tname), B, nb, tcol, turb)) {
+    fprintf(stderr, "cannot read %s\n", path_in(dir, tname));
+    goto done;
+  }
+  if ((r = ec2d_init_flow(ctx))) { fail("ec2d_init_flow", r); goto done; }
+  const double Cv = 1.0 / (P->gamma * (P->gamma - 1.0) * P->Ma * P->Ma);
+  for (int m = 0; m < nb; m++) {
+    const int nx = B[m].nx, ny = B[m].ny, W = nx + 3;
+    double *U = (double *)malloc((size_t)nvar * W * (ny + 3) * sizeof(double));
+    if (!U) { r = EC2D_ERR_NOMEM; goto done; }
+    if ((r = ec2d_download_U(ctx, cs, 1, m + 1, U))) { free(U); fail("ec2d_download_U", r); goto done; }
+    for (int j = 0; j <= ny; j++)
+      for (int i = 0; i <= nx; i++) {
+        const double *q = flow[m] + ((size_t)j * (nx + 1) + i) * 6;
+        const double d0 = q[2], u0 = q[3], v0 = q[4], T0 = q[5];
+        double *u = U + (size_t)nvar * ((size_t)(j + 1) * W + (i + 1)); /* U(NVAR,-1:nx+1,-1:ny+1) */
+        u[0] = d0;
+        u[1] = d0 * u0;
+        u[2] = d0 * v0;
+        u[3] = d0 * Cv * T0 + 0.5 * d0 * (u0 * u0 + v0 * v0);
+        if (turb[m]) {
+          const double *w = turb[m] + ((size_t)j * (nx + 1) + i) * tcol;
+          for (int c = 2; c < tcol; c++) u[4 + c - 2] = w[c];
+        }
+      }
+    r = ec2d_upload_U(ctx, cs, 1, m + 1, U);
+    free(U);
+    if (r) { fail("ec2d_upload_U", r); goto done; }
+  }
+  if ((r = ec2d_boundary_condition(ctx, 1)) || (r = ec2d_update_buffer(ctx, 1)) || (r = ec2d_dual_time_start(ctx)))
+    fail("restart", r);
+done:
+  for (int m = 0; m < nb; m++) { free(flow[m]); free(turb[m]); }
+  return r;
+}
+
 static int fail(const char *what, int r) {
   fprintf(stderr, "%s: %s (%d)\n", what, ec2d_error_string(r), r);
   return r;
@@ -216,10 +394,11 @@ static int fail(const char *what, int r) {
 int main(int argc, char **argv) {
   const char *dir = ".";
   long max_steps = -1;
-  int device = 0;
+  int device = 0, fix_nvar = 0;
   for (int a = 1; a < argc; a++) {
     if (!strcmp(argv[a], "--steps") && a + 1 < argc) max_steps = atol(argv[++a]);
     else if (!strcmp(argv[a], "--device") && a + 1 < argc) device = atoi(argv[++a]);
+    else if (!strcmp(argv[a], "--fix-nvar-restart")) fix_nvar = 1;
     else dir = argv[a];
   }
   ec2d_params P;
@@ -240,8 +419,28 @@ int main(int argc, char **argv) {
       return fail("ec2d_add_block", r);
   for (int k = 0; k < nfdm; k++)
     if ((r = ec2d_set_fdm_block(ctx, cs, fdm[k]))) return fail("ec2d_set_fdm_block", r);
+  /* comput_dw for SA and SST (opencfd_ec2d_v1.5.4.f90:164): dist_wall.dat
+   * when the case has one, else the distances formed on the device, written
+   * to dist_wall.dat and dw.dat after the set-up */
+  const int turbulent = P.Iflag_turbulence_model == 2 || P.Iflag_turbulence_model == 3;
+  int have_dw = 0;
+  if (turbulent) {
+    double *dw[MAXB] = {0};
+    int rd = read_dist_wall(path_in(dir, "dist_wall.dat"), B, nb, dw);
+    if (rd < 0) fprintf(stderr, "dist_wall.dat unreadable or for another mesh: distances formed anew\n");
+    for (int m = 0; m < nb && rd == 0; m++)
+      if ((r = ec2d_set_wall_distance(ctx, cs, m + 1, dw[m]))) return fail("ec2d_set_wall_distance", r);
+    have_dw = rd == 0;
+    for (int m = 0; m < nb; m++) free(dw[m]);
+  }
   if ((r = ec2d_setup(ctx))) return fail("ec2d_setup", r);
-  if ((r = ec2d_init_flow(ctx))) return fail("ec2d_init_flow", r);
+  if (turbulent && !have_dw && (r = write_dist_wall(dir, ctx, cs, B, nb))) return fail("dist_wall.dat", r);
+  if (P.Iflag_init == 0) {
+    if ((r = ec2d_init_flow(ctx))) return fail("ec2d_init_flow", r);
+  } else if ((r = restart(dir, ctx, cs, &P, B, nb, nvar, fix_nvar))) {
+    ec2d_destroy(ctx);
+    return r;
+  }
   printf(" Start ......\n");
 
   double rmax[6] = {0}, rrms[6] = {0}, tt = 0.0;

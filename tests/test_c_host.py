@@ -98,3 +98,75 @@ def test_c_host_main_loop_equals_ctypes(gpu_lib, tmp_path, kind):
     np.testing.assert_array_equal(np.array(out["forces"].split(), dtype=float), np.array(g.forces(1)))
     np.testing.assert_array_equal(np.array(out["res_rms"].split(), dtype=float), g.norms()[1][:p.nvar()])
     g.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["euler", "sa"])
+def test_c_host_restart_equals_python_restart(gpu_lib, tmp_path, kind):
+    """Iflag_init = 1: the C host's init_flow_read (flow2d.dat, and SA2d.dat
+    with --fix-nvar-restart) leaves the state outputs.restart leaves, so both
+    hosts write the same Residual.dat records after the restart; an SA
+    restart without the flag stops with the reference's NVAR problem named."""
+    from ec2d import cases, gpu, inputs, outputs
+    if kind == "euler":
+        p, bl = cases.small_cgrid_case(65, 17, Ma=0.7, AoA=2.0, Iflag_flux=4, Iflag_Scheme=5, Time_Method=0,
+                                       CFL=5.0, Kstep_show=5, nblocks=2)
+    else:
+        p, bl = cases.small_cgrid_case(65, 17, Ma=0.6, AoA=2.0, Re=1e6, If_viscous=1, Iflag_turbulence_model=2,
+                                       Iflag_flux=4, Iflag_Scheme=5, CFL=5.0, first=2e-4, nblocks=2, Kstep_show=5)
+    g = gpu.Solver([(p, bl)])
+    g.init_flow()
+    g.step(10)
+    inputs.write_case(str(tmp_path), p.replace(Iflag_init=1), bl)
+    outputs.write_output(str(tmp_path), g, p, kstep=10)
+    g.close()
+    fix = kind == "sa"
+    if fix:
+        r = subprocess.run([_host(), str(tmp_path), "--steps", "10"], capture_output=True, text=True, timeout=120)
+        assert r.returncode == 1 and "sub_init.f90:541" in r.stderr
+    args = [_host(), str(tmp_path), "--steps", "10"] + (["--fix-nvar-restart"] if fix else [])
+    r = subprocess.run(args, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    recs = open(tmp_path / "Residual.dat").read().splitlines()
+    h = gpu.Solver([(p, bl)])
+    outputs.restart(h, str(tmp_path), fix_nvar=fix)
+    expect = []
+    for _ in range(2):
+        h.step(5)
+        rmax, rrms, kstep, _ = h.norms()
+        expect.append(inputs.residual_record(kstep, rmax, rrms, p.nvar()).rstrip("\n"))
+    assert recs == expect
+    h.close()
+
+
+@pytest.mark.gpu
+def test_c_host_wall_distance_file(gpu_lib, tmp_path):
+    """SA: without dist_wall.dat the C host writes it from the device's
+    distances (bit for bit); given one (here with doubled distances) it reads
+    it, and marches as the Python driver does with the same file."""
+    import shutil
+
+    from ec2d import cases, driver, gpu, inputs
+    p, bl = cases.small_cgrid_case(65, 17, Ma=0.6, AoA=2.0, Re=1e6, If_viscous=1, Iflag_turbulence_model=2,
+                                   Iflag_flux=4, Iflag_Scheme=5, CFL=5.0, first=2e-4, nblocks=2, Kstep_show=5,
+                                   t_end=1.0e9)
+    dims = [(b.nx, b.ny) for b in bl]
+    a, b_, c = tmp_path / "a", tmp_path / "b", tmp_path / "c"
+    inputs.write_case(str(a), p, bl)
+    r = subprocess.run([_host(), str(a), "--steps", "2"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    dws = inputs.read_dist_wall(str(a / "dist_wall.dat"), dims)
+    g = gpu.Solver([(p, bl)])
+    for k, (nx, ny) in enumerate(dims, start=1):
+        np.testing.assert_array_equal(dws[k - 1], g.field(1, 1, k, gpu.F_DW, shape=(nx + 1, ny + 1))[1:nx, 1:ny])
+    g.close()
+    assert open(a / "dw.dat").readline().split() == ["variables=x,y,dw"]
+    for d in (b_, c):
+        inputs.write_case(str(d), p, bl)
+        inputs.write_dist_wall(str(d / "dist_wall.dat"), [2.0 * x for x in dws], dims)
+    r = subprocess.run([_host(), str(b_), "--steps", "10"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    driver.run(str(c), steps=10, quiet=True)
+    assert open(b_ / "Residual.dat").read() == open(c / "Residual.dat").read()
+    assert not os.path.exists(b_ / "dw.dat")
+    shutil.rmtree(a)
