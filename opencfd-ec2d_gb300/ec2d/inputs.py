@@ -284,14 +284,15 @@ def read_dist_wall(path: str, dims: Sequence) -> List[np.ndarray]:
 
 def write_dist_wall(path: str, dws: Sequence, dims: Sequence) -> None:
     """dist_wall.dat as comput_dw writes it (sub_turbulence_SST.f90:342-348),
-    every value with the digits that read back to the same double."""
+    every value with 17 significant digits, as list-directed output writes a
+    double: it reads back to the same double."""
     with open(path, "w") as fh:
         fh.write(f" {len(dws)}\n")
         fh.write(" " + " ".join(f"{int(nx)} {int(ny)}" for nx, ny in dims) + "\n")
         for d in dws:
             flat = np.asarray(d, dtype=np.float64).reshape(-1, order="F")
             for k in range(0, flat.size, 4):
-                fh.write(" " + " ".join(repr(float(x)) for x in flat[k:k + 4]) + "\n")
+                fh.write(" " + " ".join(f"{float(x):.17g}" for x in flat[k:k + 4]) + "\n")
 
 
 def write_dw_tecplot(path: str, cells: Sequence) -> None:
@@ -305,7 +306,7 @@ def write_dw_tecplot(path: str, cells: Sequence) -> None:
             fh.write(f" zone i= {ni} j= {nj}\n")
             for j in range(nj):
                 for i in range(ni):
-                    fh.write(f" {float(x1[i, j])!r} {float(y1[i, j])!r} {float(dw[i, j])!r}\n")
+                    fh.write(f" {float(x1[i, j]):.17g} {float(y1[i, j]):.17g} {float(dw[i, j]):.17g}\n")
 
 
 def residual_record(kstep: int, res_max6, res_rms, nvar: int) -> str:

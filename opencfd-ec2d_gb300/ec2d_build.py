@@ -104,7 +104,9 @@ def build_host(verbose: bool = False) -> str:
     inc = os.path.join(HERE, "..", "include")
     if os.path.exists(HOST) and not _stale(HOST, [HOST_SRC, LIB, os.path.join(inc, "ec2d_gpu.h")]):
         return HOST
-    cmd = [os.environ.get("CC", "gcc"), "-O2", "-std=c11", "-Wall", "-I", inc, HOST_SRC, "-o", HOST,
+    # no contraction of products into FMAs (aarch64 has them in its base
+    # ISA): the host's output arithmetic rounds like the Python host's
+    cmd = [os.environ.get("CC", "gcc"), "-O2", "-std=c11", "-ffp-contract=off", "-Wall", "-I", inc, HOST_SRC, "-o", HOST,
            "-L", os.path.dirname(LIB), "-lec2d_gpu", "-Wl,-rpath,$ORIGIN"]
     if verbose:
         print(" ".join(cmd), flush=True)

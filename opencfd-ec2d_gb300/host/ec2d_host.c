@@ -13,8 +13,10 @@
  *       NS_Time_advance(1) / NS_2stge_multigrid / NS_3stge_multigrid
  *       if (mod(Kstep, Kstep_show) == 0) call output_Res(1)
  *
- * with the step body replaced by ec2d_step and output_Res writing the same
- * Residual.dat record, format (I8,13E24.10) (opencfd_ec2d_v1.5.4.f90:266-279).
+ * with the step body replaced by ec2d_step, output_Res writing the same
+ * Residual.dat record, format (I8,13E24.10) (opencfd_ec2d_v1.5.4.f90:266-279),
+ * and output(1) the same flow2d*.dat / SA2d.dat / SST2d.dat files every
+ * Kstep_save steps and at the end (:182-186, :284-371).
  * The input files are read in the reference's formats, unchanged.
  *
  *   ec2d_host [case_dir] [--steps N] [--device D] [--fix-nvar-restart]
@@ -262,7 +264,7 @@ static int read_dist_wall(const char *path, const host_block *B, int nb, double 
 
 /* dist_wall.dat and dw.dat (sub_turbulence_SST.f90:342-362) from the
  * distances formed on the device, every value with 17 significant digits
- * (it reads back to the same double). */
+ * as list-directed output writes a double (it reads back to the same one). */
 static int write_dist_wall(const char *dir, ec2d_ctx *ctx, int cs, const host_block *B, int nb) {
   char path[4096], path2[4096];
   snprintf(path, sizeof(path), "%s/dist_wall.dat", dir);
@@ -386,6 +388,79 @@ done:
   return r;
 }
 
+/* One zone of an `output` file: the header line, then per cell of
+ * i = 0..nx (fastest), j = 0..ny the columns in F20.10 */
+static void zone(FILE *f, int nx, int ny, const double *const *cols, int ncol) {
+  fprintf(f, "  zone i= %11d j= %11d\n", nx + 1, ny + 1);
+  for (int j = 0; j <= ny; j++)
+    for (int i = 0; i <= nx; i++) {
+      const size_t c = (size_t)(j + 1) * (nx + 3) + (i + 1); /* (-1:nx+1,-1:ny+1) */
+      for (int k = 0; k < ncol; k++) fprintf(f, "%20.10f", cols[k][c]);
+      fprintf(f, "\n");
+    }
+}
+
+/* output(1) (opencfd_ec2d_v1.5.4.f90:284-371): flow2d-<Kstep>.dat (x, y, d,
+ * u, v, T, p), flow2d.dat (the same and Amut Re) and SA2d.dat (x, y, nu~) or
+ * SST2d.dat (x, y, k, omega), every block over 0..nx x 0..ny, read from the
+ * device with ec2d_download_U and ec2d_get_field */
+static int output(const char *dir, ec2d_ctx *ctx, int cs, const ec2d_params *P, const host_block *B, int nb,
+                  int nvar, int kstep) {
+  char p1[4096], p2[4096], p3[4096];
+  snprintf(p1, sizeof(p1), "%s/flow2d-%07d.dat", dir, kstep);
+  snprintf(p2, sizeof(p2), "%s/flow2d.dat", dir);
+  snprintf(p3, sizeof(p3), "%s/%s", dir, nvar == 5 ? "SA2d.dat" : "SST2d.dat");
+  FILE *f1 = fopen(p1, "w"), *f2 = fopen(p2, "w"), *f3 = nvar >= 5 ? fopen(p3, "w") : NULL;
+  int r = (!f1 || !f2 || (nvar >= 5 && !f3)) ? 1 : 0;
+  if (!r) {
+    fprintf(f1, " variables=x,y,d,u,v,T,p\n");
+    fprintf(f2, " variables=x,y,d,u,v,T,p,Amut\n");
+    if (f3) fprintf(f3, nvar == 5 ? " variables=x,y,vt\n" : " variables=x,y,Kt,Wt\n");
+  }
+  const double gamma = P->gamma, Ma = P->Ma, Cv = 1.0 / (gamma * (gamma - 1.0) * Ma * Ma);
+  for (int m = 0; m < nb && !r; m++) {
+    const int nx = B[m].nx, ny = B[m].ny;
+    const size_t n = (size_t)(nx + 3) * (ny + 3);
+    double *U = (double *)malloc(nvar * n * sizeof(double)), *w = (double *)malloc(8 * n * sizeof(double));
+    if (!U || !w) r = EC2D_ERR_NOMEM;
+    double *x1 = w, *y1 = w + n, *d = w + 2 * n, *u = w + 3 * n, *v = w + 4 * n, *T = w + 5 * n, *pp = w + 6 * n,
+           *amut = w + 7 * n;
+    if (!r) r = ec2d_download_U(ctx, cs, 1, m + 1, U);
+    if (!r) r = ec2d_get_field(ctx, cs, 1, m + 1, EC2D_F_X1, x1);
+    if (!r) r = ec2d_get_field(ctx, cs, 1, m + 1, EC2D_F_Y1, y1);
+    if (!r) r = ec2d_get_field(ctx, cs, 1, m + 1, EC2D_F_AMUT, amut);
+    if (!r) {
+      for (size_t k = 0; k < n; k++) {
+        const double *q = U + (size_t)nvar * k; /* U(NVAR,-1:nx+1,-1:ny+1) */
+        d[k] = q[0];
+        u[k] = q[1] / d[k];
+        v[k] = q[2] / d[k];
+        T[k] = (q[3] - 0.5 * d[k] * (u[k] * u[k] + v[k] * v[k])) / (Cv * d[k]);
+        pp[k] = d[k] * T[k] / (gamma * Ma * Ma);
+        amut[k] = amut[k] * P->Re;
+      }
+      const double *c7[8] = {x1, y1, d, u, v, T, pp, amut};
+      zone(f1, nx, ny, c7, 7);
+      zone(f2, nx, ny, c7, 8);
+      if (f3) {
+        /* the turbulence variables, gathered into the free columns */
+        for (size_t k = 0; k < n; k++) {
+          d[k] = U[(size_t)nvar * k + 4];
+          if (nvar == 6) u[k] = U[(size_t)nvar * k + 5];
+        }
+        const double *ct[4] = {x1, y1, d, u};
+        zone(f3, nx, ny, ct, nvar == 5 ? 3 : 4);
+      }
+    }
+    free(U);
+    free(w);
+  }
+  if (f1) fclose(f1);
+  if (f2) fclose(f2);
+  if (f3) fclose(f3);
+  return r;
+}
+
 static int fail(const char *what, int r) {
   fprintf(stderr, "%s: %s (%d)\n", what, ec2d_error_string(r), r);
   return r;
@@ -460,7 +535,11 @@ int main(int argc, char **argv) {
       return r;
     }
     if (r) return fail("ec2d_residual", r);
-    if (kstep % P.Kstep_show == 0) { /* output_Res(1) */
+    /* (a zero Kstep_save or Kstep_show, for which the reference's mod is
+     * undefined, writes every step, as the Python driver does) */
+    if (kstep % (P.Kstep_save > 0 ? P.Kstep_save : 1) == 0 && (r = output(dir, ctx, cs, &P, B, nb, nvar, kstep)))
+      return fail("output", r); /* output(1) */
+    if (kstep % (P.Kstep_show > 0 ? P.Kstep_show : 1) == 0) { /* output_Res(1) */
       FILE *f = fopen(rpath, "a");
       if (f) {
         fprintf(f, "%8d", kstep);
@@ -471,6 +550,7 @@ int main(int argc, char **argv) {
       }
     }
   }
+  if ((r = output(dir, ctx, cs, &P, B, nb, nvar, kstep))) return fail("output", r); /* the final output(1) */
   double cl = 0, cd = 0, cm = 0;
   if ((r = ec2d_forces(ctx, cs, &cl, &cd, &cm))) return fail("ec2d_forces", r);
   printf("steps %ld kstep %d tt %.17g\n", done, kstep, tt);

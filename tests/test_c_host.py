@@ -120,6 +120,11 @@ def test_c_host_restart_equals_python_restart(gpu_lib, tmp_path, kind):
     inputs.write_case(str(tmp_path), p.replace(Iflag_init=1), bl)
     outputs.write_output(str(tmp_path), g, p, kstep=10)
     g.close()
+    # the Python host restarts from its own copy: the C host's final output(1)
+    # replaces flow2d.dat in the case directory
+    import shutil
+    py_dir = tmp_path.parent / (tmp_path.name + "_py")
+    shutil.copytree(tmp_path, py_dir)
     fix = kind == "sa"
     if fix:
         r = subprocess.run([_host(), str(tmp_path), "--steps", "10"], capture_output=True, text=True, timeout=120)
@@ -129,7 +134,7 @@ def test_c_host_restart_equals_python_restart(gpu_lib, tmp_path, kind):
     assert r.returncode == 0, r.stdout + r.stderr
     recs = open(tmp_path / "Residual.dat").read().splitlines()
     h = gpu.Solver([(p, bl)])
-    outputs.restart(h, str(tmp_path), fix_nvar=fix)
+    outputs.restart(h, str(py_dir), fix_nvar=fix)
     expect = []
     for _ in range(2):
         h.step(5)
@@ -170,3 +175,23 @@ def test_c_host_wall_distance_file(gpu_lib, tmp_path):
     assert open(b_ / "Residual.dat").read() == open(c / "Residual.dat").read()
     assert not os.path.exists(b_ / "dw.dat")
     shutil.rmtree(a)
+
+
+@pytest.mark.gpu
+def test_c_host_flow_files_equal_the_python_driver(gpu_lib, tmp_path):
+    """output(1) of the C host every Kstep_save steps and at the end
+    (flow2d-<Kstep>.dat, flow2d.dat, SA2d.dat) is the Python driver's text,
+    byte for byte, for the same SA run."""
+    from ec2d import cases, driver, inputs
+    p, bl = cases.small_cgrid_case(65, 17, Ma=0.6, AoA=2.0, Re=1e6, If_viscous=1, Iflag_turbulence_model=2,
+                                   Iflag_flux=4, Iflag_Scheme=5, CFL=5.0, first=2e-4, nblocks=2, Kstep_show=5,
+                                   Kstep_save=10, t_end=1.0e9)
+    a, b_ = tmp_path / "c", tmp_path / "py"
+    for d in (a, b_):
+        inputs.write_case(str(d), p, bl)
+    r = subprocess.run([_host(), str(a), "--steps", "20"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    driver.run(str(b_), steps=20, quiet=True)
+    for name in ("flow2d-0000010.dat", "flow2d-0000020.dat", "flow2d.dat", "SA2d.dat", "Residual.dat",
+                 "dist_wall.dat", "dw.dat"):
+        assert open(a / name).read() == open(b_ / name).read(), name
