@@ -82,3 +82,43 @@ def test_dist_wall_round_trip_and_fortran_records(tmp_path):
     lines = open(tmp_path / "dw.dat").read().splitlines()
     assert lines[0].split() == ["variables=x,y,dw"] and lines[1].split() == ["zone", "i=", "4", "j=", "3"]
     assert len(lines) == 2 + 12 + 1 + 4
+
+
+def test_read_flow_cp_file(tmp_path):
+    """read_flow-1.2.f90 as ec2d.read_flow: Cp.dat holds one zone per wall
+    subface (neighb = -10) over its node index range, Cp = -2 (p - p_inf)
+    with p the p column of flow2d.dat and p_inf = 1/(1.4 Ma^2) -- the
+    program's own gamma, not the case's."""
+    import numpy as np
+
+    from ec2d import cases, inputs, outputs, read_flow
+    p, bl = cases.small_cgrid_case(33, 9, Ma=0.5, gamma=1.3, nblocks=2)
+    inputs.write_case(str(tmp_path), p, bl)
+    rng = np.random.default_rng(11)
+    blocks = []
+    for b in bl:
+        shape = (b.nx + 3, b.ny + 3)
+        d = 1.0 + 0.1 * rng.random(shape)
+        U = np.stack([d, 0.2 * d, 0.05 * d, 2.0 + rng.random(shape)])
+        blocks.append({"nx": b.nx, "ny": b.ny, "U": U, "x1": rng.random(shape), "y1": rng.random(shape),
+                       "amut": np.zeros(shape)})
+    with open(tmp_path / "flow2d.dat", "w") as fh:
+        fh.write(outputs.format_blocks(blocks, p.gamma, p.Ma, p.Re, with_amut=True))
+    read_flow.write_cp(str(tmp_path))
+    lines = open(tmp_path / "Cp.dat").read().splitlines()
+    assert lines[0].split() == ["variable=x,Cp"]
+    walls = [(k, s) for k, b in enumerate(bl) for s in b.bc if s[6] == -10]
+    assert walls
+    flow = outputs._zones(str(tmp_path / "flow2d.dat"), 7)
+    p00 = 1.0 / (1.4 * p.Ma * p.Ma)
+    pos = 1
+    for k, s in walls:
+        ni, _, rows = flow[k]
+        n = (s[5] - s[4] + 1) * (s[3] - s[2] + 1)
+        assert lines[pos].split() == ["zone", "i=", str(n)]
+        got = np.array([[float(t) for t in ln.split()] for ln in lines[pos + 1:pos + 1 + n]])
+        want = np.array([(rows[j * ni + i][0], -(rows[j * ni + i][6] - p00) * 2.0)
+                         for j in range(s[4], s[5] + 1) for i in range(s[2], s[3] + 1)])
+        np.testing.assert_array_equal(got, want)
+        pos += 1 + n
+    assert pos == len(lines)
