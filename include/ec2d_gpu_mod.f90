@@ -162,6 +162,39 @@ module ec2d_gpu_mod
       integer(c_int), value :: case_id
       integer(c_int) :: code, block, i, j
     end function
+    integer(c_int) function ec2d_clear_status(ctx, case_id) bind(C)
+      import
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: case_id
+    end function
+    ! output(1) at Kstep_save without stalling the loop: ec2d_snapshot queues
+    ! a copy of a case's U and Amu_t to pinned host memory behind the steps;
+    ! after later steps, ec2d_snapshot_wait gives its Kstep and tt and
+    ! ec2d_snapshot_U / ec2d_snapshot_amut fill the reference's arrays
+    ! U(NVAR,-1:nx+1,-1:ny+1) and Amu_t(-1:nx+1,-1:ny+1) of each block
+    integer(c_int) function ec2d_snapshot(ctx, case_id) bind(C)
+      import
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: case_id
+    end function
+    integer(c_int) function ec2d_snapshot_wait(ctx, case_id, kstep, tt) bind(C)
+      import
+      type(c_ptr), value :: ctx
+      integer(c_int) :: case_id, kstep
+      real(c_double) :: tt
+    end function
+    integer(c_int) function ec2d_snapshot_U(ctx, block, U) bind(C)
+      import
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: block
+      real(c_double) :: U(*)
+    end function
+    integer(c_int) function ec2d_snapshot_amut(ctx, block, amut) bind(C)
+      import
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: block
+      real(c_double) :: amut(*)
+    end function
     integer(c_int) function ec2d_forces(ctx, case_id, cl, cd, cm) bind(C)
       import
       type(c_ptr), value :: ctx
