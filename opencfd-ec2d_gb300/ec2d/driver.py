@@ -24,6 +24,7 @@ from __future__ import annotations
 import argparse
 import os
 import time
+import warnings
 
 from . import gpu, inputs, outputs, tuning
 
@@ -37,6 +38,24 @@ def read_fdm(directory: str):
     lines = open(path).read().splitlines()
     n = int(lines[4].split()[0])
     return [int(lines[6 + k].split()[0]) for k in range(n)]
+
+
+def read_wall_distance(directory: str, p, dims):
+    """The distances of the case's dist_wall.dat for an SA or SST run, or
+    None: for the other models, without the file, or (with a warning) for a
+    file written for another mesh or cut short, whose distances are then
+    formed anew and the file rewritten.  The reference would read such a
+    file into the mesh's blocks as it stands."""
+    if p.Iflag_turbulence_model not in (inputs.TURB_SA, inputs.TURB_SST):
+        return None
+    path = os.path.join(directory, "dist_wall.dat")
+    if not os.path.exists(path):
+        return None
+    try:
+        return inputs.read_dist_wall(path, dims)
+    except ValueError as e:
+        warnings.warn(f"{e}; the wall distances are formed anew")
+        return None
 
 
 def write_wall_distance(solver, directory: str, dims) -> None:
@@ -63,8 +82,7 @@ def run(directory: str, steps: int = None, device: int = 0, fix_nvar: bool = Fal
     # directory has one, else formed on the device and written there
     dims = [(b.nx, b.ny) for b in blocks]
     turbulent = p.Iflag_turbulence_model in (inputs.TURB_SA, inputs.TURB_SST)
-    dw_path = os.path.join(directory, "dist_wall.dat")
-    dw = inputs.read_dist_wall(dw_path, dims) if turbulent and os.path.exists(dw_path) else None
+    dw = read_wall_distance(directory, p, dims)
     s = gpu.Solver([(p, blocks)], device=device, fdm_blocks=[fdm], dw=None if dw is None else [dw])
     if turbulent and dw is None:
         write_wall_distance(s, directory, dims)

@@ -122,3 +122,23 @@ def test_read_flow_cp_file(tmp_path):
         np.testing.assert_array_equal(got, want)
         pos += 1 + n
     assert pos == len(lines)
+
+
+def test_driver_wall_distance_choice(tmp_path):
+    """Which distances the main-loop driver hands to the library: the file's
+    for SA and SST runs, none (formed on the device) for the other models,
+    without the file, or -- with a warning -- for a file of another mesh."""
+    import numpy as np
+    import pytest
+
+    from ec2d import driver, inputs
+    dims = [(5, 4), (3, 3)]
+    dws = [np.full((nx - 1, ny - 1), 0.5) for nx, ny in dims]
+    sa, lam = inputs.Params(Iflag_turbulence_model=2), inputs.Params(Iflag_turbulence_model=0)
+    assert driver.read_wall_distance(str(tmp_path), sa, dims) is None
+    inputs.write_dist_wall(str(tmp_path / "dist_wall.dat"), dws, dims)
+    got = driver.read_wall_distance(str(tmp_path), sa, dims)
+    assert all(np.array_equal(a, b) for a, b in zip(got, dws))
+    assert driver.read_wall_distance(str(tmp_path), lam, dims) is None
+    with pytest.warns(UserWarning):
+        assert driver.read_wall_distance(str(tmp_path), sa, [(5, 4), (3, 5)]) is None
